@@ -1,0 +1,227 @@
+/*
+ * vkhr_cuda.h -- C ABI of the GB300 (sm_103a) backend for vkhr's volumetric
+ * level-of-detail path: the strand-density voxelizer and the volume raymarcher.
+ *
+ * Every entry point takes plain device pointers and sizes and returns a
+ * vkhr_status; nothing throws across this boundary.  All work is ordered on
+ * the caller's CUDA stream (passed as `void*`, i.e. a cudaStream_t; NULL is
+ * the legacy default stream).  The library owns only its scratch memory
+ * (held by the context); inputs and outputs are always caller-owned.
+ *
+ * Reference interfaces replaced (paths inside the vkhr project):
+ *   vkhr::HairStyle::generate_bounding_box / get_bounding_box
+ *                                        src/vkhr/scene_graph/hair_style.cc:215-255
+ *   vkhr::HairStyle::generate_tangents   src/vkhr/scene_graph/hair_style.cc:171-194
+ *   vkhr::HairStyle::generate_indices    src/vkhr/scene_graph/hair_style.cc:196-213
+ *   vkhr::HairStyle::voxelize_vertices   src/vkhr/scene_graph/hair_style.cc:257-294
+ *   vkhr::HairStyle::voxelize_segments   src/vkhr/scene_graph/hair_style.cc:296-342
+ *   vkhr::HairStyle::Volume::normalize   src/vkhr/scene_graph/hair_style.cc:344-357
+ *   vulkan::Volume::draw + volume.frag   src/vkhr/rasterizer/volume.cc:104-112,
+ *                                        share/shaders/volumes/volume.frag:31-103
+ */
+#ifndef VKHR_CUDA_H
+#define VKHR_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VKHR_CUDA_ABI_VERSION 1
+
+typedef enum vkhr_status {
+    VKHR_OK = 0,
+    VKHR_ERR_INVALID_ARG = 1,      /* null pointer, bad size, bad enum value      */
+    VKHR_ERR_DEGENERATE_AABB = 2,  /* a zero (or NaN) extent: voxel size would be 0 */
+    VKHR_ERR_OOM = 3,              /* scratch allocation failed                   */
+    VKHR_ERR_CUDA = 4,             /* a CUDA runtime call failed (see last error) */
+    VKHR_ERR_TIMEOUT = 5,          /* a bounded device wait ran out               */
+    VKHR_ERR_NAN_INPUT = 6,        /* non-finite vertex coordinates               */
+    VKHR_ERR_CAPACITY = 7,         /* fixed-capacity scratch was too small        */
+    VKHR_ERR_NOT_SUPPORTED = 8     /* valid request this build does not implement */
+} vkhr_status;
+
+/* vkhr::AABB (include/vkhr/scene_graph/hair_style.hh:16-21), same layout:
+ * origin = min corner, size = max - min, radius = |size|, volume = x*y*z.   */
+typedef struct vkhr_aabb {
+    float origin[3];
+    float radius;
+    float size[3];
+    float volume;
+} vkhr_aabb;
+
+/* How the linear voxel index is formed.  The reference evaluates
+ * `voxel.x + voxel.y*width + voxel.z*width*height` in FP32
+ * (hair_style.cc:276, :321), which is exact only below 2^24 voxels.
+ *  REF_FP32 reproduces that expression bit for bit (identical to EXACT at
+ *           <= 2^24 voxels, i.e. up to 256^3); visits whose FP32 index falls
+ *           outside [0, w*h*d) are dropped (the reference writes out of bounds).
+ *  EXACT    integer indexing; visits with a negative coordinate are dropped. */
+typedef enum vkhr_index_mode {
+    VKHR_INDEX_REF_FP32 = 0,
+    VKHR_INDEX_EXACT = 1
+} vkhr_index_mode;
+
+/* Density texel formats the raymarcher samples. */
+typedef enum vkhr_density_format {
+    VKHR_DENSITY_U8_UNORM = 0,  /* reference: R8_UNORM of normalize()d densities */
+    VKHR_DENSITY_U32_COUNT = 1, /* raw uint32 strand counts, sampled as floats   */
+    VKHR_DENSITY_F32 = 2        /* FP32 density                                  */
+} vkhr_density_format;
+
+/* Tangent texel formats. */
+typedef enum vkhr_tangent_format {
+    VKHR_TANGENT_I8_SNORM = 0,  /* reference: R8G8B8A8_SNORM, 4 bytes per voxel */
+    VKHR_TANGENT_F32X4 = 1      /* FP32 x4, 16 bytes per voxel                   */
+} vkhr_tangent_format;
+
+/* Shading models of the Params UBO (kajiya-kay.glsl:4, approximate_deep_shadows.glsl:4,
+ * local_ambient_occlusion.glsl:4). */
+enum {
+    VKHR_SHADING_KAJIYA_KAY = 0,
+    VKHR_SHADING_ADSM = 2,
+    VKHR_SHADING_LAO = 3
+};
+
+/* Renderer::Type (include/vkhr/renderer.hh:14): 0 rasterizer, 1 hybrid, 2 raymarcher. */
+enum {
+    VKHR_RENDERER_RASTERIZER = 0,
+    VKHR_RENDERER_HYBRID = 1,
+    VKHR_RENDERER_RAYMARCHER = 2
+};
+
+/* Every scalar the raymarch reads.  Field groups mirror the reference UBOs:
+ *   camera  -- Camera UBO (share/shaders/scene_graph/camera.glsl:4-11),
+ *              matrices column-major exactly as glm::mat4 stores them;
+ *   light   -- Lights UBO entry 0 (share/shaders/scene_graph/lights.glsl:4-13);
+ *   strand  -- Strand UBO (share/shaders/strands/strand.glsl:8-16);
+ *   params  -- Params UBO (share/shaders/scene_graph/params.glsl:7-33);
+ *   fixed   -- literals of volume.frag (:78 thickness 11.0, :86 AO kernel 2);
+ *   ext     -- knobs beyond the reference; their defaults reduce to it. */
+typedef struct vkhr_raymarch_params {
+    int32_t width, height;              /* framebuffer size in pixels                */
+
+    float view[16];                     /* camera.view                               */
+    float projection[16];               /* camera.projection (Vulkan y-flip applied) */
+    float camera_position[3];           /* camera.position                           */
+    float look_at_distance;             /* camera.look_at_distance                   */
+
+    float light_origin[3];              /* lights[0].origin                          */
+    float light_intensity[3];           /* lights[0].intensity                       */
+
+    vkhr_aabb volume_bounds;            /* volume_bounds                             */
+    int32_t volume_resolution[3];       /* volume_resolution                         */
+    float hair_color[3];                /* hair_color                                */
+    float hair_alpha;                   /* hair_alpha                                */
+    float hair_exponent;                /* hair_exponent                             */
+
+    int32_t shading_model;              /* shading_model                             */
+    int32_t deep_shadows_on;            /* deep_shadows_on (YES = 1)                 */
+    float isosurface;                   /* isosurface                                */
+    float raycast_steps;                /* raycast_steps                             */
+    float occlusion_radius;             /* occlusion_radius                          */
+    float ao_exponent;                  /* ao_exponent                               */
+    float ao_max;                       /* ao_max                                    */
+    float magnified_distance;           /* magnified_distance                        */
+    int32_t renderer;                   /* renderer                                  */
+    float minified_distance;            /* minified_distance                         */
+
+    float shadow_thickness;             /* 11.0 in volume.frag:78                    */
+    float ao_kernel_size;               /* 2 in volume.frag:86                       */
+
+    float shadow_steps;                 /* ext: <= 0 means raycast_steps (reference) */
+    float kd;                           /* ext: diffuse scale, 1 = reference         */
+    int32_t density_format;             /* vkhr_density_format                       */
+    int32_t tangent_format;             /* vkhr_tangent_format                       */
+} vkhr_raymarch_params;
+
+/* Opaque library context: one per host thread (or externally synchronised).
+ * It pins a device and owns grow-only scratch buffers. */
+typedef struct vkhr_ctx vkhr_ctx;
+
+/* ---- context ------------------------------------------------------------- */
+vkhr_status vkhr_create(int device, vkhr_ctx** out_ctx);
+vkhr_status vkhr_destroy(vkhr_ctx* ctx);
+const char* vkhr_status_string(vkhr_status status);
+/* Text of the last failure seen by this context (never NULL). */
+const char* vkhr_last_error(const vkhr_ctx* ctx);
+int vkhr_abi_version(void);
+
+/* ---- strand data preparation ----------------------------------------------
+ * Replaces HairStyle::generate_bounding_box + get_bounding_box
+ * (hair_style.cc:215-255): min/max start at (0,0,0), so the box always holds
+ * the world origin.  Writes the AABB to *out_bounds (host memory) and
+ * synchronises the stream.  NaN/Inf vertices give VKHR_ERR_NAN_INPUT. */
+vkhr_status vkhr_bounding_box(vkhr_ctx* ctx, const float* d_vertices, uint32_t vertex_count,
+                              vkhr_aabb* out_bounds, void* stream);
+
+/* Replaces HairStyle::generate_tangents (hair_style.cc:171-194).  Strand s has
+ * h_segments[s] segments (the HAIR `segments` array; strand_count entries,
+ * host memory) and segments+1 vertices; the last vertex repeats the previous
+ * tangent.  d_tangents receives vertex_count float3 (12 bytes each). */
+vkhr_status vkhr_generate_tangents(vkhr_ctx* ctx, const float* d_vertices, const uint16_t* h_segments,
+                                   uint32_t strand_count, float* d_tangents, void* stream);
+
+/* Replaces HairStyle::generate_indices (hair_style.cc:196-213): two uint32 per
+ * segment, skipping the last vertex of every strand.  d_indices receives
+ * 2 * sum(segments) entries. */
+vkhr_status vkhr_generate_indices(vkhr_ctx* ctx, const uint16_t* h_segments, uint32_t strand_count,
+                                  uint32_t* d_indices, void* stream);
+
+/* ---- voxelization ----------------------------------------------------------
+ * Outputs (all device memory, x fastest, then y, then z):
+ *   d_counts     uint32 per voxel: the exact number of visits (never saturates);
+ *   d_densities  uint8 per voxel: HairStyle::Volume::densities, i.e.
+ *                min(count, 255) (optional, may be NULL);
+ *   d_tangents   int8 x4 per voxel: HairStyle::Volume::tangents, bit-exact
+ *                including the reference's serial summation order and its
+ *                stop-at-255 rule (optional, may be NULL; needs d_tangent_in).
+ * d_vertices / d_tangent_in are float3 arrays (12-byte stride, glm::vec3).
+ * bounds is host memory.  Scratch comes from the context; the first call at
+ * a new size may allocate and reads one 8-byte count back to the host. */
+
+/* Replaces HairStyle::voxelize_vertices (hair_style.cc:257-294). */
+vkhr_status vkhr_voxelize_vertices(vkhr_ctx* ctx, const float* d_vertices, const float* d_tangent_in,
+                                   uint32_t vertex_count, const vkhr_aabb* bounds,
+                                   int32_t width, int32_t height, int32_t depth, int32_t index_mode,
+                                   uint32_t* d_counts, uint8_t* d_densities, int8_t* d_tangents,
+                                   void* stream);
+
+/* Replaces HairStyle::voxelize_segments (hair_style.cc:296-342).  d_indices
+ * holds index_count uint32 (pairs; an odd trailing index is ignored, as the
+ * reference's `i < indices.size() - 1` loop does). */
+vkhr_status vkhr_voxelize_segments(vkhr_ctx* ctx, const float* d_vertices, const float* d_tangent_in,
+                                   const uint32_t* d_indices, uint64_t index_count, const vkhr_aabb* bounds,
+                                   int32_t width, int32_t height, int32_t depth, int32_t index_mode,
+                                   uint32_t* d_counts, uint8_t* d_densities, int8_t* d_tangents,
+                                   void* stream);
+
+/* Replaces HairStyle::Volume::normalize (hair_style.cc:344-357): u8 min-max
+ * rescale in place.  A constant volume (max == min) maps to 0, where the
+ * reference divides by zero. */
+vkhr_status vkhr_normalize_densities(vkhr_ctx* ctx, uint8_t* d_densities, uint64_t voxel_count, void* stream);
+
+/* ---- raymarch ---------------------------------------------------------------
+ * Replaces the Vulkan draw of the volume proxy cube (volume.cc:104-112) and
+ * the fragment shader volume.frag:31-103 with its includes.  One ray per
+ * pixel centre whose ray enters the AABB from outside (the front faces the
+ * reference rasterizes with back-face culling); a camera inside the box
+ * covers no pixel, as in the reference.
+ *   d_density   density texels in params->density_format;
+ *   d_tangent   tangent texels in params->tangent_format;
+ *   d_depth_in  optional depth buffer (width*height floats, NULL = cleared 1.0);
+ *   d_rgba      width*height float4: (shading*occlusion, coverage) clamped
+ *               to [0,1] as packUnorm4x8 does (ppll.glsl:32); 0 where no
+ *               fragment survives (discarded or not covered);
+ *   d_depth_out optional width*height floats: fragment depth, 1.0 elsewhere. */
+vkhr_status vkhr_raymarch(vkhr_ctx* ctx, const vkhr_raymarch_params* params,
+                          const void* d_density, const void* d_tangent, const float* d_depth_in,
+                          float* d_rgba, float* d_depth_out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VKHR_CUDA_H */

@@ -1,0 +1,214 @@
+"""Python bindings of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Loads oracle/liboracle.so (the C restatement) and, when it was built here,
+oracle/_ref/libvkhr_ref.so (the reference's own voxelizer and raymarch shader
+compiled from its sources).  Only tests/, __graft_entry__.smoke() and the CPU
+baseline legs of bench.py import this module.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from vkhr_gb300 import _abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libvkhr_ref.so")
+REFERENCE_ROOT = "/root/reference"
+
+_lib = None
+_ref = None
+
+
+def build(with_reference=None):
+    """Compile liboracle.so (always) and _ref (when the reference sources exist)."""
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+    if with_reference is None:
+        with_reference = os.path.isfile(os.path.join(REFERENCE_ROOT, "src/vkhr/scene_graph/hair_style.cc"))
+    if with_reference:
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+
+
+class PixelDiag(C.Structure):
+    _fields_ = [("iso_margin", C.c_double), ("tangent_len", C.c_double), ("steps_taken", C.c_int32),
+                ("covered", C.c_int32)]
+
+
+DIAG_DTYPE = np.dtype([("iso_margin", np.float64), ("tangent_len", np.float64), ("steps_taken", np.int32),
+                       ("covered", np.int32)])
+
+P = C.c_void_p
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build(with_reference=False)
+        _lib = C.CDLL(LIB)
+        _lib.oracle_bounding_box.argtypes = [P, C.c_uint32, C.POINTER(_abi.AABB)]
+        _lib.oracle_generate_tangents.argtypes = [P, P, C.c_uint32, P]
+        _lib.oracle_generate_indices.argtypes = [P, C.c_uint32, P]
+        _lib.oracle_voxelize_vertices.argtypes = [P, P, C.c_uint32, C.POINTER(_abi.AABB), C.c_int, C.c_int, C.c_int,
+                                                  C.c_int, P, P, P]
+        _lib.oracle_voxelize_vertices.restype = C.c_uint64
+        _lib.oracle_voxelize_segments.argtypes = [P, P, P, C.c_uint64, C.POINTER(_abi.AABB), C.c_int, C.c_int,
+                                                  C.c_int, C.c_int, P, P, P]
+        _lib.oracle_voxelize_segments.restype = C.c_uint64
+        _lib.oracle_segment_visits.argtypes = [P, P, C.c_uint64, C.POINTER(_abi.AABB), C.c_int, C.c_int, C.c_int]
+        _lib.oracle_segment_visits.restype = C.c_uint32
+        _lib.oracle_normalize.argtypes = [P, C.c_uint64]
+        _lib.oracle_pixel_entry.argtypes = [C.POINTER(_abi.RaymarchParams), C.c_int, C.c_int, P]
+        _lib.oracle_raymarch_f64.argtypes = [C.POINTER(_abi.RaymarchParams), P, P, P, P, P, P, C.c_int, C.c_int,
+                                             C.c_int]
+        _lib.oracle_raymarch_f32.argtypes = [C.POINTER(_abi.RaymarchParams), P, P, P, P, P, C.c_int, C.c_int,
+                                             C.c_int]
+        _lib.oracle_max_threads.restype = C.c_int
+    return _lib
+
+
+def has_reference():
+    return os.path.exists(REF_LIB)
+
+
+def ref():
+    global _ref
+    if _ref is None:
+        lib()
+        _ref = C.CDLL(REF_LIB)
+        _ref.ref_prepare.argtypes = [P, C.c_uint32, P, C.c_uint32, P, P, C.POINTER(_abi.AABB)]
+        _ref.ref_voxelize.argtypes = [C.c_int, P, C.c_uint32, P, P, C.c_uint64, C.c_int, C.c_int, C.c_int, C.c_int,
+                                      P, P]
+        _ref.ref_raymarch.argtypes = [C.POINTER(_abi.RaymarchParams), P, P, P, P, P, C.c_int, C.c_int, C.c_int]
+        _ref.ref_raymarch.restype = C.c_int
+    return _ref
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+# ---- voxelizer ---------------------------------------------------------------
+
+def bounding_box(vertices):
+    v = _f32(vertices)
+    b = _abi.AABB()
+    lib().oracle_bounding_box(_p(v), v.shape[0], C.byref(b))
+    return b
+
+
+def generate_tangents(vertices, segments):
+    v = _f32(vertices)
+    s = np.ascontiguousarray(segments, dtype=np.uint16)
+    t = np.zeros_like(v)
+    lib().oracle_generate_tangents(_p(v), _p(s), s.shape[0], _p(t))
+    return t
+
+
+def generate_indices(segments):
+    s = np.ascontiguousarray(segments, dtype=np.uint16)
+    out = np.zeros(2 * int(s.astype(np.int64).sum()), dtype=np.uint32)
+    lib().oracle_generate_indices(_p(s), s.shape[0], _p(out))
+    return out
+
+
+def voxelize(mode, vertices, tangents, indices, bounds, res, index_mode=_abi.INDEX_REF_FP32):
+    """mode 'vertices' or 'segments'; returns (counts u32, densities u8, tangents i8x4, dropped)."""
+    w, h, d = (int(x) for x in res)
+    n = w * h * d
+    v = _f32(vertices)
+    t = None if tangents is None else _f32(tangents)
+    counts = np.zeros(n, dtype=np.uint32)
+    dens = np.zeros(n, dtype=np.uint8)
+    tq = np.zeros((n, 4), dtype=np.int8)
+    if mode == "vertices":
+        dropped = lib().oracle_voxelize_vertices(_p(v), _p(t), v.shape[0], C.byref(bounds), w, h, d, index_mode,
+                                                 _p(counts), _p(dens), _p(tq))
+    else:
+        idx = np.ascontiguousarray(indices, dtype=np.uint32)
+        dropped = lib().oracle_voxelize_segments(_p(v), _p(t), _p(idx), idx.shape[0], C.byref(bounds), w, h, d,
+                                                 index_mode, _p(counts), _p(dens), _p(tq))
+    return counts, dens, tq, int(dropped)
+
+
+def segment_visits(vertices, indices, bounds, res):
+    v = _f32(vertices)
+    idx = np.ascontiguousarray(indices, dtype=np.uint32)
+    w, h, d = (int(x) for x in res)
+    return np.array([lib().oracle_segment_visits(_p(v), _p(idx), p, C.byref(bounds), w, h, d)
+                     for p in range(idx.shape[0] // 2)], dtype=np.int64)
+
+
+def normalize(densities):
+    d = np.ascontiguousarray(densities, dtype=np.uint8).copy()
+    lib().oracle_normalize(_p(d), d.size)
+    return d
+
+
+# ---- raymarch ----------------------------------------------------------------
+
+def raymarch(params, density, tangent, depth_in=None, precision="f64", rows=None, threads=0, diag=False):
+    """Returns (rgba (H, W, 4) f32, depth (H, W) f32[, diag]) for rows [r0, r1)."""
+    W, H = params.width, params.height
+    r0, r1 = (0, H) if rows is None else rows
+    rgba = np.zeros((H, W, 4), dtype=np.float32)
+    depth = np.ones((H, W), dtype=np.float32)
+    dens = np.ascontiguousarray(density)
+    tan = np.ascontiguousarray(tangent)
+    din = None if depth_in is None else _f32(depth_in)
+    if precision == "f64":
+        dg = np.zeros((H, W), dtype=DIAG_DTYPE) if diag else None
+        lib().oracle_raymarch_f64(C.byref(params), _p(dens), _p(tan), _p(din), _p(rgba), _p(depth), _p(dg), r0, r1,
+                                  threads)
+        return (rgba, depth, dg) if diag else (rgba, depth)
+    lib().oracle_raymarch_f32(C.byref(params), _p(dens), _p(tan), _p(din), _p(rgba), _p(depth), r0, r1, threads)
+    return rgba, depth
+
+
+def max_threads():
+    return int(lib().oracle_max_threads())
+
+
+# ---- the reference's own code (built here only) -----------------------------
+
+def ref_prepare(vertices, segments):
+    v = _f32(vertices)
+    s = np.ascontiguousarray(segments, dtype=np.uint16)
+    t = np.zeros_like(v)
+    idx = np.zeros(2 * int(s.astype(np.int64).sum()), dtype=np.uint32)
+    b = _abi.AABB()
+    ref().ref_prepare(_p(v), v.shape[0], _p(s), s.shape[0], _p(t), _p(idx), C.byref(b))
+    return t, idx, b
+
+
+def ref_voxelize(mode, vertices, tangents, indices, res, normalize=False):
+    w, h, d = (int(x) for x in res)
+    n = w * h * d
+    v = _f32(vertices)
+    t = _f32(tangents)
+    idx = np.ascontiguousarray(indices if indices is not None else np.zeros(0), dtype=np.uint32)
+    dens = np.zeros(n, dtype=np.uint8)
+    tq = np.zeros((n, 4), dtype=np.int8)
+    ref().ref_voxelize(1 if mode == "segments" else 0, _p(v), v.shape[0], _p(t), _p(idx), idx.shape[0], w, h, d,
+                       1 if normalize else 0, _p(dens), _p(tq))
+    return dens, tq
+
+
+def ref_raymarch(params, density, tangent, depth_in=None, rows=None, threads=0):
+    W, H = params.width, params.height
+    r0, r1 = (0, H) if rows is None else rows
+    rgba = np.zeros((H, W, 4), dtype=np.float32)
+    depth = np.ones((H, W), dtype=np.float32)
+    dens = np.ascontiguousarray(density)
+    tan = np.ascontiguousarray(tangent)
+    din = None if depth_in is None else _f32(depth_in)
+    rc = ref().ref_raymarch(C.byref(params), _p(dens), _p(tan), _p(din), _p(rgba), _p(depth), r0, r1, threads)
+    if rc != 0:
+        raise ValueError("the reference shader supports reference semantics only (shadow_steps <= 0, kd == 1)")
+    return rgba, depth

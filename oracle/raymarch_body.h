@@ -1,0 +1,315 @@
+/*
+ * raymarch_body.h -- CPU oracle (test infrastructure only): the raymarch of
+ * share/shaders/volumes/volume.frag:31-103 and its includes, written once and
+ * instantiated by raymarch.c for REAL = double (parity oracle) and
+ * REAL = float (CPU baseline).  The loop variables `t` are FP32 in both, as
+ * in the GLSL, so both instantiations run the same iteration counts.
+ *
+ * Expects: REAL, SFX(name) (suffixing macro), SQRT_FN, POW_FN, FLOOR_FN.
+ */
+
+typedef struct SFX(vec3) { REAL x, y, z; } SFX(vec3);
+
+static inline SFX(vec3) SFX(v3)(REAL x, REAL y, REAL z) { SFX(vec3) r = {x, y, z}; return r; }
+static inline SFX(vec3) SFX(add)(SFX(vec3) a, SFX(vec3) b) { return SFX(v3)(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline SFX(vec3) SFX(sub)(SFX(vec3) a, SFX(vec3) b) { return SFX(v3)(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline SFX(vec3) SFX(scale)(SFX(vec3) a, REAL s) { return SFX(v3)(a.x * s, a.y * s, a.z * s); }
+static inline SFX(vec3) SFX(mul)(SFX(vec3) a, SFX(vec3) b) { return SFX(v3)(a.x * b.x, a.y * b.y, a.z * b.z); }
+static inline REAL SFX(dot)(SFX(vec3) a, SFX(vec3) b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline SFX(vec3) SFX(from)(const float* f) { return SFX(v3)((REAL)f[0], (REAL)f[1], (REAL)f[2]); }
+
+/* GLSL normalize(v) = v / length(v); a zero vector gives NaN components, as
+ * 0/0 does on the GPU, and the output clamp below turns them into 0. */
+static inline SFX(vec3) SFX(normalize)(SFX(vec3) a, REAL* len_out)
+{
+    REAL l = SQRT_FN(SFX(dot)(a, a));
+    if (len_out) *len_out = l;
+    return SFX(v3)(a.x / l, a.y / l, a.z / l);
+}
+
+/* GLSL mix(x, y, a) = x * (1 - a) + y * a. */
+static inline SFX(vec3) SFX(mix)(SFX(vec3) a, SFX(vec3) b, REAL t)
+{
+    return SFX(add)(SFX(scale)(a, (REAL)1 - t), SFX(scale)(b, t));
+}
+
+typedef struct SFX(vol) {
+    const void* data;
+    int fmt;       /* vkhr_density_format or vkhr_tangent_format */
+    int n[3];
+    SFX(vec3) origin, size;
+} SFX(vol);
+
+static inline REAL SFX(texel_density)(const SFX(vol)* v, long i, long j, long k)
+{
+    if (i < 0 || j < 0 || k < 0 || i >= v->n[0] || j >= v->n[1] || k >= v->n[2]) return 0; /* border */
+    size_t at = (size_t)i + (size_t)v->n[0] * ((size_t)j + (size_t)v->n[1] * (size_t)k);
+    switch (v->fmt) {
+    case VKHR_DENSITY_U8_UNORM: return (REAL)((const uint8_t*)v->data)[at] / (REAL)255; /* UNORM: c/255 */
+    case VKHR_DENSITY_U32_COUNT: return (REAL)((const uint32_t*)v->data)[at];
+    default: return (REAL)((const float*)v->data)[at];
+    }
+}
+
+static inline SFX(vec3) SFX(texel_tangent)(const SFX(vol)* v, long i, long j, long k)
+{
+    if (i < 0 || j < 0 || k < 0 || i >= v->n[0] || j >= v->n[1] || k >= v->n[2]) return SFX(v3)(0, 0, 0);
+    size_t at = (size_t)i + (size_t)v->n[0] * ((size_t)j + (size_t)v->n[1] * (size_t)k);
+    if (v->fmt == VKHR_TANGENT_I8_SNORM) {
+        const int8_t* q = (const int8_t*)v->data + 4 * at;
+        REAL c[3];
+        for (int a = 0; a < 3; ++a) { /* SNORM: max(c/127, -1) */
+            c[a] = (REAL)q[a] / (REAL)127;
+            if (c[a] < (REAL)-1) c[a] = (REAL)-1;
+        }
+        return SFX(v3)(c[0], c[1], c[2]);
+    }
+    const float* f = (const float*)v->data + 4 * at;
+    return SFX(v3)((REAL)f[0], (REAL)f[1], (REAL)f[2]);
+}
+
+/* Texel-space coordinate set-up of a LINEAR, CLAMP_TO_BORDER lookup (Vulkan
+ * spec "Texel Coordinate Systems": u = s*size - 0.5, i0 = floor(u), alpha =
+ * frac(u)).  Returns 0 when all eight taps are border texels. */
+static inline int SFX(tex_setup)(const SFX(vol)* v, SFX(vec3) P, long i0[3], REAL a[3])
+{
+    /* sample_volume.glsl:8 -- (fragment_position - volume_origin) / volume_size */
+    SFX(vec3) uvw = SFX(v3)((P.x - v->origin.x) / v->size.x, (P.y - v->origin.y) / v->size.y,
+                            (P.z - v->origin.z) / v->size.z);
+    REAL s[3] = {uvw.x, uvw.y, uvw.z};
+    for (int c = 0; c < 3; ++c) {
+        REAL u = s[c] * (REAL)v->n[c] - (REAL)0.5;
+        if (!(u > (REAL)-2 && u < (REAL)(v->n[c] + 1))) return 0;
+        REAL f = FLOOR_FN(u);
+        i0[c] = (long)f;
+        a[c] = u - f;
+    }
+    return 1;
+}
+
+static REAL SFX(sample_density)(const SFX(vol)* v, SFX(vec3) P)
+{
+    long i0[3];
+    REAL a[3];
+    if (!SFX(tex_setup)(v, P, i0, a)) return 0;
+    REAL acc = 0;
+    for (int dz = 0; dz < 2; ++dz)
+        for (int dy = 0; dy < 2; ++dy)
+            for (int dx = 0; dx < 2; ++dx) {
+                REAL w = (dx ? a[0] : (REAL)1 - a[0]) * (dy ? a[1] : (REAL)1 - a[1]) * (dz ? a[2] : (REAL)1 - a[2]);
+                acc += w * SFX(texel_density)(v, i0[0] + dx, i0[1] + dy, i0[2] + dz);
+            }
+    return acc;
+}
+
+static SFX(vec3) SFX(sample_tangent)(const SFX(vol)* v, SFX(vec3) P)
+{
+    long i0[3];
+    REAL a[3];
+    SFX(vec3) acc = SFX(v3)(0, 0, 0);
+    if (!SFX(tex_setup)(v, P, i0, a)) return acc;
+    for (int dz = 0; dz < 2; ++dz)
+        for (int dy = 0; dy < 2; ++dy)
+            for (int dx = 0; dx < 2; ++dx) {
+                REAL w = (dx ? a[0] : (REAL)1 - a[0]) * (dy ? a[1] : (REAL)1 - a[1]) * (dz ? a[2] : (REAL)1 - a[2]);
+                acc = SFX(add)(acc, SFX(scale)(SFX(texel_tangent)(v, i0[0] + dx, i0[1] + dy, i0[2] + dz), w));
+            }
+    return acc;
+}
+
+/* (projection * view * vec4(P, 1)).z / .w with pv = projection * view. */
+static inline REAL SFX(clip_depth)(const REAL pv[16], SFX(vec3) P)
+{
+    REAL z = pv[2] * P.x + pv[6] * P.y + pv[10] * P.z + pv[14];
+    REAL w = pv[3] * P.x + pv[7] * P.y + pv[11] * P.z + pv[15];
+    return z / w;
+}
+
+/* volume_rendering.glsl:19-52 (volume_surface). */
+static void SFX(volume_surface)(const SFX(vol)* dv, const REAL pv[16], SFX(vec3) start, SFX(vec3) end,
+                                float steps, REAL iso, float depth_buffer, SFX(vec3)* surf_out,
+                                REAL* a_out, double* margin, int* taken)
+{
+    REAL acc = 0;
+    float step_size = 1.0f / steps;
+    SFX(vec3) surface_point = SFX(v3)(0, 0, 0);
+    int surface_point_found = 0, entry_point_found = 0;
+    SFX(vec3) entry_point = SFX(v3)(0, 0, 0);
+    double m = 1.0 / 0.0;
+    int k = 0;
+    for (float t = 0.0f; t < 1.0f; t += step_size) {
+        SFX(vec3) P = SFX(mix)(start, end, (REAL)t);
+        REAL depth = SFX(clip_depth)(pv, P);
+        if ((REAL)depth_buffer < depth) break;
+        ++k;
+        REAL density = SFX(sample_density)(dv, P);
+        acc += density;
+        if (density != (REAL)0) {
+            double dm = fabs((double)acc - (double)iso) / (double)iso;
+            if (dm < m) m = dm;
+            if (acc <= iso) surface_point = P;
+            if (acc >= iso) surface_point_found = 1;
+            if (!entry_point_found) {
+                entry_point = P;
+                entry_point_found = 1;
+            }
+        }
+    }
+    if (!surface_point_found && entry_point_found) surface_point = entry_point;
+    *surf_out = surface_point;
+    *a_out = acc / iso;
+    if (margin) *margin = m;
+    if (taken) *taken = k;
+}
+
+/* kajiya-kay.glsl:7-24; `kd` scales the diffuse term (1 = reference). */
+static SFX(vec3) SFX(kajiya_kay)(SFX(vec3) diffuse, SFX(vec3) specular, REAL p, SFX(vec3) tangent,
+                                  SFX(vec3) light, SFX(vec3) eye, REAL kd)
+{
+    REAL cosTL = SFX(dot)(tangent, light);
+    REAL cosTE = SFX(dot)(tangent, eye);
+    REAL a = (REAL)1 - cosTL * cosTL, b = (REAL)1 - cosTE * cosTE;
+    REAL sinTL = SQRT_FN(a > 0 ? a : 0); /* sqrt of a negative rounding residue: 0 */
+    REAL sinTE = SQRT_FN(b > 0 ? b : 0);
+    REAL c = cosTL * cosTE + sinTL * sinTE;
+    REAL spec = POW_FN(c > 0 ? c : 0, p);
+    return SFX(add)(SFX(scale)(diffuse, kd * sinTL), SFX(scale)(specular, spec));
+}
+
+/* approximate_deep_shadows.glsl:24-36. */
+static REAL SFX(deep_shadows)(const SFX(vol)* dv, SFX(vec3) s, SFX(vec3) light, float steps, REAL alpha,
+                               REAL thickness)
+{
+    REAL strands = 0;
+    float step_size = 1.0f / steps;
+    for (float t = 0.0f; t < 1.0f; t += step_size) {
+        SFX(vec3) point = SFX(mix)(s, light, (REAL)t);
+        strands += SFX(sample_density)(dv, point) * thickness;
+    }
+    return POW_FN((REAL)1 - alpha, strands);
+}
+
+/* local_ambient_occlusion.glsl:9-30. */
+static REAL SFX(lao)(const SFX(vol)* dv, SFX(vec3) s, float kernel_size, REAL radius, REAL intensity,
+                     REAL min_intensity)
+{
+    REAL density = 0;
+    float kernel_radius = (kernel_size - 1.0f) / 2.0f;
+    SFX(vec3) voxel_space = SFX(v3)(dv->size.x / (REAL)dv->n[0], dv->size.y / (REAL)dv->n[1],
+                                    dv->size.z / (REAL)dv->n[2]);
+    REAL voxel_scaling = radius / (REAL)kernel_radius;
+    SFX(vec3) sc = SFX(scale)(voxel_space, voxel_scaling);
+    for (float z = -kernel_radius; z <= +kernel_radius; z += 1.0f)
+        for (float y = -kernel_radius; y <= +kernel_radius; y += 1.0f)
+            for (float x = -kernel_radius; x <= +kernel_radius; x += 1.0f) {
+                SFX(vec3) q = SFX(add)(s, SFX(mul)(SFX(v3)((REAL)x, (REAL)y, (REAL)z), sc));
+                REAL r = SFX(sample_density)(dv, q);
+                density += r < min_intensity ? r : min_intensity;
+            }
+    REAL k3 = (REAL)kernel_size * (REAL)kernel_size * (REAL)kernel_size;
+    return POW_FN((REAL)1 - density / k3, intensity);
+}
+
+/* scheme.glsl:7-11 */
+static REAL SFX(lod)(int renderer, REAL mag, REAL min_d, REAL cur)
+{
+    if (renderer == 0) return 0;
+    if (renderer == 2) return 1;
+    REAL t = (cur - mag) / (min_d - mag);
+    t = t < 0 ? 0 : (t > 1 ? 1 : t);
+    return t * t * ((REAL)3 - (REAL)2 * t);
+}
+
+/* packUnorm4x8's clamp(c, 0, 1) (ppll.glsl:32) with IEEE 754-2008 min/max,
+ * which return the non-NaN operand: NaN maps to 0. */
+static inline float SFX(clamp01)(REAL x) { return (float)(x > 0 ? (x < 1 ? x : 1) : 0); }
+
+/* volume.frag:31-103 for one pixel whose entry point is `start`. */
+static void SFX(shade_pixel)(const vkhr_raymarch_params* p, const SFX(vol)* dv, const SFX(vol)* tv,
+                             const REAL pv[16], SFX(vec3) start, float depth_buffer, float* rgba,
+                             float* depth_out, oracle_pixel_diag* diag)
+{
+    SFX(vec3) cam = SFX(from)(p->camera_position);
+    REAL radius = (REAL)p->volume_bounds.radius;
+    SFX(vec3) dir = SFX(normalize)(SFX(sub)(start, cam), NULL);
+    SFX(vec3) end = SFX(add)(start, SFX(scale)(dir, radius));
+
+    SFX(vec3) surf;
+    REAL a;
+    double margin;
+    int taken;
+    SFX(volume_surface)(dv, pv, start, end, p->raycast_steps, (REAL)p->isosurface, depth_buffer, &surf, &a,
+                        &margin, &taken);
+    if (diag) { diag->iso_margin = margin; diag->steps_taken = taken; diag->tangent_len = 0; }
+    rgba[0] = rgba[1] = rgba[2] = rgba[3] = 0.0f;
+    if (depth_out) *depth_out = 1.0f;
+    if (a == (REAL)0) return; /* discard */
+
+    REAL coverage = SFX(lod)(p->renderer, (REAL)p->magnified_distance, (REAL)p->minified_distance,
+                             (REAL)p->look_at_distance) * a * (REAL)p->hair_alpha;
+    SFX(vec3) shading = SFX(v3)(1, 1, 1);
+    SFX(vec3) lo = SFX(from)(p->light_origin);
+    SFX(vec3) L = SFX(normalize)(SFX(sub)(lo, surf), NULL);
+    SFX(vec3) E = SFX(normalize)(SFX(sub)(surf, cam), NULL);
+    REAL tlen;
+    SFX(vec3) T = SFX(normalize)(SFX(sample_tangent)(tv, surf), &tlen);
+    if (diag) diag->tangent_len = (double)tlen;
+    if (p->shading_model == VKHR_SHADING_KAJIYA_KAY)
+        shading = SFX(kajiya_kay)(SFX(from)(p->hair_color), SFX(from)(p->light_intensity), (REAL)p->hair_exponent,
+                                  T, L, E, (REAL)p->kd);
+    REAL occlusion = 1;
+    if (p->deep_shadows_on == 1 && p->shading_model != VKHR_SHADING_LAO) {
+        float ss = p->shadow_steps > 0.0f ? p->shadow_steps : p->raycast_steps;
+        occlusion *= SFX(deep_shadows)(dv, surf, lo, ss, (REAL)p->hair_alpha, (REAL)p->shadow_thickness);
+    }
+    if (p->shading_model != VKHR_SHADING_ADSM)
+        occlusion *= SFX(lao)(dv, surf, p->ao_kernel_size, (REAL)p->occlusion_radius, (REAL)p->ao_exponent,
+                              (REAL)p->ao_max);
+    rgba[0] = SFX(clamp01)(shading.x * occlusion);
+    rgba[1] = SFX(clamp01)(shading.y * occlusion);
+    rgba[2] = SFX(clamp01)(shading.z * occlusion);
+    rgba[3] = SFX(clamp01)(coverage);
+    if (depth_out) *depth_out = (float)SFX(clip_depth)(pv, surf);
+}
+
+static void SFX(raymarch_rows)(const vkhr_raymarch_params* p, const void* density, const void* tangent,
+                               const float* depth_in, float* rgba, float* depth_out, oracle_pixel_diag* diag,
+                               int row_begin, int row_end, int threads)
+{
+    SFX(vol) dv, tv;
+    dv.data = density; dv.fmt = p->density_format;
+    tv.data = tangent; tv.fmt = p->tangent_format;
+    for (int c = 0; c < 3; ++c) { dv.n[c] = tv.n[c] = p->volume_resolution[c]; }
+    dv.origin = tv.origin = SFX(from)(p->volume_bounds.origin);
+    dv.size = tv.size = SFX(from)(p->volume_bounds.size);
+    REAL pv[16];
+    for (int c = 0; c < 4; ++c)       /* column c of projection * view */
+        for (int r = 0; r < 4; ++r) {
+            REAL s = 0;
+            for (int k = 0; k < 4; ++k) s += (REAL)p->projection[k * 4 + r] * (REAL)p->view[c * 4 + k];
+            pv[c * 4 + r] = s;
+        }
+    const int W = p->width;
+    double inv[16];
+    int invertible = oracle_vp_inverse(p, inv);
+    if (threads <= 0) threads = oracle_max_threads();
+#pragma omp parallel for schedule(dynamic) num_threads(threads)
+    for (int y = row_begin; y < row_end; ++y) {
+        for (int x = 0; x < W; ++x) {
+            size_t at = (size_t)y * (size_t)W + (size_t)x;
+            double st[3];
+            oracle_pixel_diag* dg = diag ? diag + at : NULL;
+            if (dg) { dg->iso_margin = 1.0 / 0.0; dg->tangent_len = 0; dg->steps_taken = 0; dg->covered = 0; }
+            if (!invertible || !oracle_pixel_entry_inv(p, inv, x, y, st)) {
+                rgba[4 * at + 0] = rgba[4 * at + 1] = rgba[4 * at + 2] = rgba[4 * at + 3] = 0.0f;
+                if (depth_out) depth_out[at] = 1.0f;
+                continue;
+            }
+            if (dg) dg->covered = 1;
+            float db = depth_in ? depth_in[at] : 1.0f;
+            SFX(shade_pixel)(p, &dv, &tv, pv, SFX(v3)((REAL)st[0], (REAL)st[1], (REAL)st[2]), db, rgba + 4 * at,
+                             depth_out ? depth_out + at : NULL, dg);
+            if (dg) dg->covered = 1;
+        }
+    }
+}

@@ -1,0 +1,88 @@
+/*
+ * vkhr_oracle.h -- CPU oracle for vkhr's volumetric level-of-detail path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
+ * algorithms, used as the checker in tests/, in __graft_entry__.smoke() and as
+ * the timed CPU baseline in bench.py.  No product code path links or calls it.
+ *
+ * Voxelizer: strict IEEE FP32 in the reference's operation order (build with
+ * -O2 -fno-fast-math -ffp-contract=off); bit-exact with the reference's own
+ * hair_style.cc compiled from its sources (oracle/_ref, see oracle/Makefile).
+ * Raymarcher: a transcription of share/shaders/volumes/volume.frag and its
+ * includes, instantiated in FP64 (the parity oracle; loop variables `t` stay
+ * FP32 as in GLSL so iteration counts match) and in FP32 (CPU baseline).
+ */
+#ifndef VKHR_ORACLE_H
+#define VKHR_ORACLE_H
+
+#include <stdint.h>
+#include <stddef.h>
+#include "../include/vkhr_cuda.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* hair_style.cc:215-255 (generate_bounding_box + get_bounding_box). */
+void oracle_bounding_box(const float* vertices, uint32_t vertex_count, vkhr_aabb* out);
+
+/* hair_style.cc:171-194. tangents: vertex_count float3. */
+void oracle_generate_tangents(const float* vertices, const uint16_t* segments, uint32_t strand_count,
+                              float* tangents);
+
+/* hair_style.cc:196-213. indices: 2*sum(segments) uint32. */
+void oracle_generate_indices(const uint16_t* segments, uint32_t strand_count, uint32_t* indices);
+
+/* hair_style.cc:257-294.  counts: uint32 (never saturating), densities: u8
+ * (reference, saturating at 255), tangents_q: int8 x4 per voxel (w = 0).
+ * Any output may be NULL.  Returns the number of dropped visits (coordinates
+ * whose index falls outside the grid; undefined behaviour in the reference). */
+uint64_t oracle_voxelize_vertices(const float* vertices, const float* tangents, uint32_t vertex_count,
+                                  const vkhr_aabb* bounds, int w, int h, int d, int index_mode,
+                                  uint32_t* counts, uint8_t* densities, int8_t* tangents_q);
+
+/* hair_style.cc:296-342. */
+uint64_t oracle_voxelize_segments(const float* vertices, const float* tangents, const uint32_t* indices,
+                                  uint64_t index_count, const vkhr_aabb* bounds, int w, int h, int d,
+                                  int index_mode, uint32_t* counts, uint8_t* densities, int8_t* tangents_q);
+
+/* Number of voxels one segment visits (the reference's `while (steps-- > 0.0f)`). */
+uint32_t oracle_segment_visits(const float* vertices, const uint32_t* indices, uint64_t pair,
+                               const vkhr_aabb* bounds, int w, int h, int d);
+
+/* hair_style.cc:344-357 (constant volume -> 0, the reference divides by 0). */
+void oracle_normalize(uint8_t* densities, uint64_t n);
+
+/* Rasterizer stand-in for the proxy cube (volume.vert:17-25, volume.cc:60-102,
+ * back-face culling): world-space entry point of the ray through the centre
+ * of pixel (px, py) into the AABB.  Returns 0 when no front face covers it. */
+int oracle_pixel_entry(const vkhr_raymarch_params* p, int px, int py, double start[3]);
+/* The same with inverse(projection * view) precomputed by oracle_vp_inverse. */
+int oracle_vp_inverse(const vkhr_raymarch_params* p, double inv[16]);
+int oracle_pixel_entry_inv(const vkhr_raymarch_params* p, const double inv[16], int px, int py, double start[3]);
+
+/* Per-pixel diagnostics of the FP64 raymarch. */
+typedef struct oracle_pixel_diag {
+    double iso_margin;   /* min over nonzero samples of |acc - iso| / iso (inf if none) */
+    double tangent_len;  /* length of the sampled tangent before normalisation         */
+    int32_t steps_taken; /* primary-loop iterations executed                          */
+    int32_t covered;     /* 1 if the pixel spawned a ray                              */
+} oracle_pixel_diag;
+
+/* volume.frag:31-103 over rows [row_begin, row_end) with `threads` OpenMP
+ * threads (<= 0: all).  rgba: width*height*4, depth_out: width*height (may be
+ * NULL), diag: width*height (may be NULL, FP64 only).  depth_in may be NULL. */
+void oracle_raymarch_f64(const vkhr_raymarch_params* p, const void* density, const void* tangent,
+                         const float* depth_in, float* rgba, float* depth_out, oracle_pixel_diag* diag,
+                         int row_begin, int row_end, int threads);
+void oracle_raymarch_f32(const vkhr_raymarch_params* p, const void* density, const void* tangent,
+                         const float* depth_in, float* rgba, float* depth_out,
+                         int row_begin, int row_end, int threads);
+
+int oracle_max_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

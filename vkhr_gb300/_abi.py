@@ -1,0 +1,117 @@
+"""ctypes mirror of the C ABI declared in include/vkhr_cuda.h.
+
+The structures here must stay layout-identical to the header; the native
+library exports ``vkhr_sizeof_*`` helpers and the tests compare them.
+"""
+import ctypes as C
+
+VKHR_OK = 0
+VKHR_ERR_INVALID_ARG = 1
+VKHR_ERR_DEGENERATE_AABB = 2
+VKHR_ERR_OOM = 3
+VKHR_ERR_CUDA = 4
+VKHR_ERR_TIMEOUT = 5
+VKHR_ERR_NAN_INPUT = 6
+VKHR_ERR_CAPACITY = 7
+VKHR_ERR_NOT_SUPPORTED = 8
+
+STATUS_NAMES = {
+    0: "VKHR_OK",
+    1: "VKHR_ERR_INVALID_ARG",
+    2: "VKHR_ERR_DEGENERATE_AABB",
+    3: "VKHR_ERR_OOM",
+    4: "VKHR_ERR_CUDA",
+    5: "VKHR_ERR_TIMEOUT",
+    6: "VKHR_ERR_NAN_INPUT",
+    7: "VKHR_ERR_CAPACITY",
+    8: "VKHR_ERR_NOT_SUPPORTED",
+}
+
+INDEX_REF_FP32 = 0
+INDEX_EXACT = 1
+
+DENSITY_U8_UNORM = 0
+DENSITY_U32_COUNT = 1
+DENSITY_F32 = 2
+
+TANGENT_I8_SNORM = 0
+TANGENT_F32X4 = 1
+
+SHADING_KAJIYA_KAY = 0
+SHADING_ADSM = 2
+SHADING_LAO = 3
+
+RENDERER_RASTERIZER = 0
+RENDERER_HYBRID = 1
+RENDERER_RAYMARCHER = 2
+
+
+class AABB(C.Structure):
+    """vkhr::AABB (include/vkhr/scene_graph/hair_style.hh:16-21)."""
+
+    _fields_ = [
+        ("origin", C.c_float * 3),
+        ("radius", C.c_float),
+        ("size", C.c_float * 3),
+        ("volume", C.c_float),
+    ]
+
+    def as_dict(self):
+        return {
+            "origin": tuple(self.origin),
+            "radius": self.radius,
+            "size": tuple(self.size),
+            "volume": self.volume,
+        }
+
+
+class RaymarchParams(C.Structure):
+    """vkhr_raymarch_params: the camera, light, strand and params UBOs."""
+
+    _fields_ = [
+        ("width", C.c_int32),
+        ("height", C.c_int32),
+        ("view", C.c_float * 16),
+        ("projection", C.c_float * 16),
+        ("camera_position", C.c_float * 3),
+        ("look_at_distance", C.c_float),
+        ("light_origin", C.c_float * 3),
+        ("light_intensity", C.c_float * 3),
+        ("volume_bounds", AABB),
+        ("volume_resolution", C.c_int32 * 3),
+        ("hair_color", C.c_float * 3),
+        ("hair_alpha", C.c_float),
+        ("hair_exponent", C.c_float),
+        ("shading_model", C.c_int32),
+        ("deep_shadows_on", C.c_int32),
+        ("isosurface", C.c_float),
+        ("raycast_steps", C.c_float),
+        ("occlusion_radius", C.c_float),
+        ("ao_exponent", C.c_float),
+        ("ao_max", C.c_float),
+        ("magnified_distance", C.c_float),
+        ("renderer", C.c_int32),
+        ("minified_distance", C.c_float),
+        ("shadow_thickness", C.c_float),
+        ("ao_kernel_size", C.c_float),
+        ("shadow_steps", C.c_float),
+        ("kd", C.c_float),
+        ("density_format", C.c_int32),
+        ("tangent_format", C.c_int32),
+    ]
+
+
+def aabb_from(origin, size):
+    """AABB with radius/volume derived exactly as get_bounding_box does (FP32)."""
+    import numpy as np
+
+    o = np.asarray(origin, dtype=np.float32)
+    s = np.asarray(size, dtype=np.float32)
+    b = AABB()
+    for c in range(3):
+        b.origin[c] = float(o[c])
+        b.size[c] = float(s[c])
+    dot = np.float32(np.float32(s[0] * s[0]) + np.float32(s[1] * s[1])) + np.float32(s[2] * s[2])
+    b.radius = float(np.sqrt(np.float32(dot)))
+    b.volume = float(np.float32(np.float32(s[0] * s[1]) * s[2]))
+    return b
