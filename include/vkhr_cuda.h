@@ -148,6 +148,19 @@ const char* vkhr_status_string(vkhr_status status);
 /* Text of the last failure seen by this context (never NULL). */
 const char* vkhr_last_error(const vkhr_ctx* ctx);
 int vkhr_abi_version(void);
+/* Kernel tracer: with profiling on, every kernel launch is bracketed by a
+ * CUDA event pair on its own stream (the reference brackets each pass with
+ * Vulkan timestamp queries, src/vkpp/query.cc:124-137).  Enabling clears the
+ * record; vkhr_profile_read waits for record `index` and returns its kernel
+ * name and duration in milliseconds.  At most 4096 launches are recorded. */
+vkhr_status vkhr_set_profiling(vkhr_ctx* ctx, int enable);
+int vkhr_profile_count(const vkhr_ctx* ctx);
+vkhr_status vkhr_profile_read(vkhr_ctx* ctx, int index, const char** name, float* ms);
+/* Number of kernels this context has launched so far (instrumentation). */
+uint64_t vkhr_launch_count(const vkhr_ctx* ctx);
+/* sizeof of the ABI structures as this library was compiled (layout checks). */
+size_t vkhr_sizeof_aabb(void);
+size_t vkhr_sizeof_raymarch_params(void);
 
 /* ---- strand data preparation ----------------------------------------------
  * Replaces HairStyle::generate_bounding_box + get_bounding_box

@@ -1,0 +1,68 @@
+"""Generates the golden fixtures of tests/golden from the reference's own code.
+
+Runs the reference's voxelizer (src/vkhr/scene_graph/hair_style.cc, compiled
+unmodified into oracle/_ref by `make -C oracle ref`) and its raymarch shader
+(share/shaders/volumes/volume.frag and includes, compiled as C++) on small
+seeded synthetic styles, and stores inputs and outputs as .npz files.
+Needs the reference sources; run from the repository root:
+
+    make -C oracle ref && python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle as O  # noqa: E402
+from vkhr_gb300 import scene, strands  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def aabb_arr(b):
+    return np.array(list(b.origin) + [b.radius] + list(b.size) + [b.volume], dtype=np.float32)
+
+
+def voxel_case(name, st, resolutions):
+    t, idx, b = O.ref_prepare(st.vertices, st.segments)
+    out = {"vertices": st.vertices, "segments": st.segments, "tangents": t, "indices": idx, "aabb": aabb_arr(b)}
+    for k, res in enumerate(resolutions):
+        out["res%d" % k] = np.array(res, dtype=np.int32)
+        for mode in ("vertices", "segments"):
+            d, tq = O.ref_voxelize(mode, st.vertices, t, idx, res)
+            dn, _ = O.ref_voxelize(mode, st.vertices, t, idx, res, normalize=True)
+            out["%s%d_densities" % (mode, k)] = d
+            out["%s%d_tangents" % (mode, k)] = tq
+            out["%s%d_normalized" % (mode, k)] = dn
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), **out)
+
+
+def raymarch_case(name, st, res, W, H, **kw):
+    t, idx, b = O.ref_prepare(st.vertices, st.segments)
+    dn, tq = O.ref_voxelize("segments", st.vertices, t, idx, res, normalize=True)
+    p = scene.make_params(b, res, W, H, **kw)
+    rgba, depth = O.ref_raymarch(p, dn, tq)
+    params = np.frombuffer(bytes(p), dtype=np.uint8)
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), params=params, densities=dn, tangents=tq, rgba=rgba,
+                        depth=depth)
+
+
+def main():
+    voxel_case("voxel_hemisphere", strands.hemisphere_style(256, 8, seed=11), [(16, 16, 16), (13, 9, 21)])
+    voxel_case("voxel_ragged", strands.ragged_style([2, 0, 3, 9, 1, 17, 0, 5, 30, 2], seed=12), [(8, 8, 8), (20, 7, 11)])
+    crowded = strands.disk_style(1500, 6, disk_radius=0.02, step_length=0.01, seed=13)
+    voxel_case("voxel_crowded", crowded, [(4, 4, 4)])
+    raymarch_case("raymarch_hemisphere", strands.hemisphere_style(512, 12, seed=14), (24, 24, 24), 64, 48,
+                  raycast_steps=96.0)
+    raymarch_case("raymarch_disk", strands.disk_style(2000, 9, seed=15), (32, 28, 20), 80, 60, raycast_steps=128.0,
+                  view_direction=(0.3, 0.4, 1.0))
+    for f in sorted(os.listdir(OUT)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(OUT, f)))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,147 @@
+"""GPU raymarch parity: vkhr_raymarch (C ABI) against the FP64 oracle
+transcription of volume.frag.
+
+Tolerance (per channel, over well-conditioned pixels): RMS <= 1e-3 and
+max |diff| <= 2e-2.  A pixel is excluded only when its isosurface decision
+lies within 1e-4 (relative) of the threshold or its surface tangent sample
+is shorter than 1e-4; excluded pixels are counted and must stay below 0.5%
+of the emitted fragments.
+"""
+import numpy as np
+import pytest
+
+from vkhr_gb300 import _abi, scene
+from tests._helpers import image_errors, style, to_dev
+
+pytestmark = pytest.mark.gpu
+
+RMS_TOL = 1e-3
+MAX_TOL = 2e-2
+
+
+def _volume(O, kind, n, verts, res, mode="segments", **kw):
+    st, t, idx = style(kind, n, verts, **kw)
+    b = O.bounding_box(st.vertices)
+    c, d, tq, _ = O.voxelize(mode, st.vertices, t, idx, b, res)
+    return b, c, O.normalize(d), tq
+
+
+def _gpu_raymarch(ctx, p, dens, tan, depth_in=None):
+    import torch
+
+    dd = to_dev(dens, torch)
+    dt = to_dev(tan, torch)
+    di = None if depth_in is None else to_dev(depth_in.astype(np.float32), torch)
+    rgba = torch.full((p.height, p.width, 4), -7.0, dtype=torch.float32, device="cuda")
+    depth = torch.full((p.height, p.width), -7.0, dtype=torch.float32, device="cuda")
+    ctx.raymarch(p, dd.data_ptr(), dt.data_ptr(), None if di is None else di.data_ptr(), rgba.data_ptr(),
+                 depth.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    return rgba.cpu().numpy(), depth.cpu().numpy()
+
+
+def _compare(gpu, gdepth, ref, rdepth, diag, rows=None):
+    if rows is not None:
+        gpu, gdepth = gpu[rows[0]:rows[1]], gdepth[rows[0]:rows[1]]
+        ref, rdepth, diag = ref[rows[0]:rows[1]], rdepth[rows[0]:rows[1]], diag[rows[0]:rows[1]]
+    rms, mx, excluded, emitted = image_errors(gpu, ref, diag)
+    assert emitted > 0
+    assert excluded <= max(2, 0.005 * emitted), (excluded, emitted)
+    assert np.all(rms <= RMS_TOL), rms
+    assert np.all(mx <= MAX_TOL), mx
+    ok = (diag["iso_margin"] >= 1e-4)
+    assert np.abs(gdepth - rdepth)[ok].max() <= 1e-4
+    return rms, mx
+
+
+def test_small_reference_semantics(ctx, oracle_lib):
+    """4,096 x 16 hemisphere style, 64^3, 640x480, 256 steps (shadows reuse them)."""
+    b, c, dn, tq = _volume(oracle_lib, "hemi", 4096, 16, (64, 64, 64))
+    p = scene.make_params(b, (64, 64, 64), 640, 480, raycast_steps=256.0)
+    ref, rdepth, diag = oracle_lib.raymarch(p, dn, tq, diag=True)
+    gpu, gdepth = _gpu_raymarch(ctx, p, dn, tq)
+    _compare(gpu, gdepth, ref, rdepth, diag)
+
+
+def test_extension_knobs(ctx, oracle_lib):
+    """kd 0.4, 32-step shadows, a hybrid-renderer LoD blend and non-power-of-two steps."""
+    b, c, dn, tq = _volume(oracle_lib, "hemi", 4096, 16, (64, 64, 64))
+    p = scene.make_params(b, (64, 64, 64), 320, 240, raycast_steps=201.0, shadow_steps=32.0, kd=0.4,
+                          renderer=_abi.RENDERER_HYBRID, hair_alpha=0.8)
+    p.magnified_distance, p.minified_distance = 2.0, 6.0
+    ref, rdepth, diag = oracle_lib.raymarch(p, dn, tq, diag=True)
+    gpu, gdepth = _gpu_raymarch(ctx, p, dn, tq)
+    _compare(gpu, gdepth, ref, rdepth, diag)
+
+
+@pytest.mark.parametrize("model", [_abi.SHADING_ADSM, _abi.SHADING_LAO, 1])
+def test_shading_models(ctx, oracle_lib, model):
+    b, c, dn, tq = _volume(oracle_lib, "hemi", 2048, 16, (48, 48, 48))
+    p = scene.make_params(b, (48, 48, 48), 200, 150, raycast_steps=128.0, shading_model=model)
+    ref, rdepth, diag = oracle_lib.raymarch(p, dn, tq, diag=True)
+    gpu, gdepth = _gpu_raymarch(ctx, p, dn, tq)
+    _compare(gpu, gdepth, ref, rdepth, diag)
+
+
+def test_raw_counts_iso_one(ctx, oracle_lib):
+    """uint32 count texels with an isosurface of 1 count/voxel."""
+    b, c, dn, tq = _volume(oracle_lib, "hemi", 4096, 16, (64, 64, 64))
+    p = scene.make_params(b, (64, 64, 64), 320, 240, raycast_steps=256.0, isosurface=1.0, shadow_steps=32.0,
+                          density_format=_abi.DENSITY_U32_COUNT)
+    ref, rdepth, diag = oracle_lib.raymarch(p, c, tq, diag=True)
+    gpu, gdepth = _gpu_raymarch(ctx, p, c, tq)
+    _compare(gpu, gdepth, ref, rdepth, diag)
+
+
+def test_float_texels(ctx, oracle_lib):
+    rng = np.random.default_rng(4)
+    b, c, dn, tq = _volume(oracle_lib, "hemi", 2048, 16, (40, 40, 40))
+    dens = (dn.astype(np.float32) / 255.0) * rng.lognormal(0.0, 0.2, dn.shape).astype(np.float32)
+    tan = np.concatenate([tq[:, :3].astype(np.float32) / 127.0, np.zeros((tq.shape[0], 1), np.float32)], axis=1)
+    p = scene.make_params(b, (40, 40, 40), 160, 120, raycast_steps=128.0, density_format=_abi.DENSITY_F32,
+                          tangent_format=_abi.TANGENT_F32X4)
+    ref, rdepth, diag = oracle_lib.raymarch(p, dens, tan, diag=True)
+    gpu, gdepth = _gpu_raymarch(ctx, p, dens, tan)
+    _compare(gpu, gdepth, ref, rdepth, diag)
+
+
+def test_depth_buffer_breaks_rays(ctx, oracle_lib):
+    b, c, dn, tq = _volume(oracle_lib, "hemi", 2048, 16, (48, 48, 48))
+    p = scene.make_params(b, (48, 48, 48), 160, 120, raycast_steps=128.0)
+    _, rdepth0 = oracle_lib.raymarch(p, dn, tq)
+    depth_in = np.ones((120, 160), np.float32)
+    depth_in[:, :80] = np.where(rdepth0[:, :80] < 1.0, rdepth0[:, :80] + 2e-3, 0.5)  # occluder mid-volume
+    ref, rdepth, diag = oracle_lib.raymarch(p, dn, tq, depth_in=depth_in, diag=True)
+    gpu, gdepth = _gpu_raymarch(ctx, p, dn, tq, depth_in)
+    _compare(gpu, gdepth, ref, rdepth, diag)
+
+
+def test_camera_inside_volume_covers_nothing(ctx, oracle_lib):
+    b, c, dn, tq = _volume(oracle_lib, "hemi", 1024, 8, (32, 32, 32))
+    p = scene.make_params(b, (32, 32, 32), 64, 48, camera_distance=0.1, raycast_steps=64.0)
+    gpu, gdepth = _gpu_raymarch(ctx, p, dn, tq)
+    assert not gpu.any() and np.all(gdepth == 1.0)
+
+
+def test_production_view_rows(ctx, oracle_lib):
+    """136,320 x 13 style, 256^3, 1920x1080, 512 steps, 64-step shadows:
+    the full frame on the GPU, three row bands against the FP64 oracle."""
+    b, c, dn, tq = _volume(oracle_lib, "disk", 136_320, 13, (256, 256, 256))
+    p = scene.make_params(b, (256, 256, 256), 1920, 1080, raycast_steps=512.0, shadow_steps=64.0)
+    gpu, gdepth = _gpu_raymarch(ctx, p, dn, tq)
+    for rows in ((300, 340), (520, 560), (760, 800)):
+        ref, rdepth, diag = oracle_lib.raymarch(p, dn, tq, diag=True, rows=rows)
+        _compare(gpu, gdepth, ref, rdepth, diag, rows=rows)
+
+
+def test_errors(ctx, oracle_lib):
+    from vkhr_gb300._native import VkhrError
+
+    b, c, dn, tq = _volume(oracle_lib, "hemi", 256, 8, (16, 16, 16))
+    for field, value in (("raycast_steps", 0.0), ("raycast_steps", -3.0), ("raycast_steps", 1e9),
+                         ("width", 0), ("isosurface", 0.0)):
+        p = scene.make_params(b, (16, 16, 16), 32, 24, raycast_steps=64.0)
+        setattr(p, field, value)
+        with pytest.raises(VkhrError) as e:
+            _gpu_raymarch(ctx, p, dn, tq)
+        assert e.value.status == _abi.VKHR_ERR_INVALID_ARG

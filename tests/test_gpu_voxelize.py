@@ -1,0 +1,158 @@
+"""GPU voxelizer parity: libvkhr_cuda.so (through the C ABI) against the oracle,
+bit-exact on counts, u8 densities and int8 tangents
+(hair_style.cc:257-342 semantics)."""
+import numpy as np
+import pytest
+
+from vkhr_gb300 import _abi, strands
+from tests._helpers import gpu_voxelize, style
+
+pytestmark = pytest.mark.gpu
+
+
+def _check(ctx, O, mode, v, t, idx, b, res, index_mode=_abi.INDEX_REF_FP32):
+    c_ref, d_ref, t_ref, dropped = O.voxelize(mode, v, t, idx, b, res, index_mode)
+    c, d, tq = gpu_voxelize(ctx, mode, v, t, idx, b, res, index_mode)
+    assert np.array_equal(c, c_ref), "counts differ in %d voxels" % int((c != c_ref).sum())
+    assert np.array_equal(d, d_ref), "u8 densities differ in %d voxels" % int((d != d_ref).sum())
+    bad = np.any(tq != t_ref, axis=1)
+    assert not bad.any(), "tangents differ in %d voxels" % int(bad.sum())
+    return c_ref
+
+
+@pytest.mark.parametrize("mode", ["vertices", "segments"])
+@pytest.mark.parametrize("res", [(64, 64, 64), (37, 50, 29)])
+def test_small_style(ctx, oracle_lib, mode, res):
+    st, t, idx = style("hemi", 4096, 16)
+    b = oracle_lib.bounding_box(st.vertices)
+    c = _check(ctx, oracle_lib, mode, st.vertices, t, idx, b, res)
+    assert c.sum() > 0
+
+
+@pytest.mark.parametrize("mode", ["vertices", "segments"])
+def test_production_style_256(ctx, oracle_lib, mode):
+    """136,320 strands x 13 vertices (1,635,840 segments) into 256^3, full size."""
+    st, t, idx = style("disk", 136_320, 13)
+    b = oracle_lib.bounding_box(st.vertices)
+    c = _check(ctx, oracle_lib, mode, st.vertices, t, idx, b, (256, 256, 256))
+    if mode == "vertices":
+        assert int(c.sum(dtype=np.uint64)) == st.vertex_count
+
+
+def test_saturation_and_crowded_voxels(ctx, oracle_lib):
+    """Thousands of visits per voxel: the stop-at-255 rule and the shared-memory
+    sort path (counts > 16 and > 2048) must still match bit for bit."""
+    st, t, idx = style("disk", 20_000, 8, disk_radius=0.02, step_length=0.01)
+    b = oracle_lib.bounding_box(st.vertices)
+    for mode in ("vertices", "segments"):
+        c = _check(ctx, oracle_lib, mode, st.vertices, t, idx, b, (8, 8, 8))
+        assert c.max() > 2048
+
+
+def test_exact_index_mode(ctx, oracle_lib):
+    st, t, idx = style("hemi", 2048, 12)
+    b = oracle_lib.bounding_box(st.vertices)
+    for mode in ("vertices", "segments"):
+        _check(ctx, oracle_lib, mode, st.vertices, t, idx, b, (48, 40, 56), _abi.INDEX_EXACT)
+
+
+def test_ref_fp32_index_rounding_large_grid(ctx, oracle_lib):
+    """Above 2^24 voxels the reference's FP32 index rounds; REF_FP32 mode
+    reproduces the rounding, EXACT does not."""
+    st, t, idx = style("hemi", 256, 8)
+    b = oracle_lib.bounding_box(st.vertices)
+    res = (512, 512, 80)  # 20.9M voxels > 2^24
+    c_ref = _check(ctx, oracle_lib, "vertices", st.vertices, t, idx, b, res, _abi.INDEX_REF_FP32)
+    c_ex = _check(ctx, oracle_lib, "vertices", st.vertices, t, idx, b, res, _abi.INDEX_EXACT)
+    assert not np.array_equal(c_ref, c_ex)
+
+
+def test_ragged_and_degenerate_strands(ctx, oracle_lib):
+    """Uneven strand lengths, zero-segment strands and zero-length segments."""
+    segs = [4, 0, 1, 5, 31, 2, 0, 17, 3]  # a first strand without segments is undefined in the reference
+    st = strands.ragged_style(segs, seed=3)
+    v = st.vertices.copy()
+    v[3] = v[2]  # a zero-length segment (NaN tangent, no visit)
+    t = strands.generate_tangents(v, st.segments)
+    idx = strands.generate_indices(st.segments)
+    b = oracle_lib.bounding_box(v)
+    for mode in ("vertices", "segments"):
+        _check(ctx, oracle_lib, mode, v, t, idx, b, (16, 16, 16))
+
+
+def test_custom_bounds_drop_outside(ctx, oracle_lib):
+    """Vertices outside caller-supplied bounds: below the box they are dropped
+    (undefined behaviour in the reference), above it they clamp to res-1."""
+    st, t, idx = style("hemi", 1024, 10)
+    b = _abi.aabb_from((-0.5, 0.0, -0.5), (1.0, 0.8, 1.0))
+    for mode in ("vertices", "segments"):
+        for im in (_abi.INDEX_REF_FP32, _abi.INDEX_EXACT):
+            _check(ctx, oracle_lib, mode, st.vertices, t, idx, b, (32, 32, 32), im)
+
+
+def test_empty_input(ctx, oracle_lib):
+    b = _abi.aabb_from((0, 0, 0), (1, 1, 1))
+    v = np.zeros((0, 3), np.float32)
+    c, d, tq = gpu_voxelize(ctx, "vertices", v, v, [], b, (8, 8, 8))
+    assert c.sum() == 0 and d.sum() == 0 and not tq.any()
+    c, d, tq = gpu_voxelize(ctx, "segments", v, v, [], b, (8, 8, 8))
+    assert c.sum() == 0 and d.sum() == 0 and not tq.any()
+
+
+def test_counts_only(ctx, oracle_lib):
+    st, t, idx = style("hemi", 4096, 16)
+    b = oracle_lib.bounding_box(st.vertices)
+    c_ref, d_ref, _, _ = oracle_lib.voxelize("segments", st.vertices, t, idx, b, (64, 64, 64))
+    c, d, tq = gpu_voxelize(ctx, "segments", st.vertices, None, idx, b, (64, 64, 64), want_tangents=False)
+    assert np.array_equal(c, c_ref) and np.array_equal(d, d_ref)
+
+
+def test_errors(ctx, oracle_lib):
+    from vkhr_gb300._native import VkhrError
+
+    st, t, idx = style("hemi", 64, 4)
+    flat = _abi.aabb_from((0, 0, 0), (1, 0, 1))
+    with pytest.raises(VkhrError) as e:
+        gpu_voxelize(ctx, "vertices", st.vertices, t, idx, flat, (8, 8, 8))
+    assert e.value.status == _abi.VKHR_ERR_DEGENERATE_AABB
+    b = oracle_lib.bounding_box(st.vertices)
+    with pytest.raises(VkhrError) as e:
+        gpu_voxelize(ctx, "vertices", st.vertices, t, idx, b, (0, 8, 8))
+    assert e.value.status == _abi.VKHR_ERR_INVALID_ARG
+    far = st.vertices.copy()
+    far[1] = (1e9, 0.0, 0.0)  # a segment spanning > 2^24 voxels: the reference never terminates
+    with pytest.raises(VkhrError) as e:
+        gpu_voxelize(ctx, "segments", far, t, idx, b, (8, 8, 8))
+    assert e.value.status == _abi.VKHR_ERR_INVALID_ARG
+
+
+def test_normalize(ctx, oracle_lib):
+    import torch
+
+    st, t, idx = style("hemi", 4096, 16)
+    b = oracle_lib.bounding_box(st.vertices)
+    _, d_ref, _, _ = oracle_lib.voxelize("segments", st.vertices, t, idx, b, (64, 64, 64))
+    dd = torch.from_numpy(d_ref.copy()).cuda()
+    ctx.normalize_densities(dd.data_ptr(), dd.numel(), torch.cuda.current_stream().cuda_stream)
+    assert np.array_equal(dd.cpu().numpy(), oracle_lib.normalize(d_ref))
+    const = torch.full((1000,), 9, dtype=torch.uint8, device="cuda")
+    ctx.normalize_densities(const.data_ptr(), const.numel(), torch.cuda.current_stream().cuda_stream)
+    assert int(const.sum()) == 0
+
+
+def test_prepare_kernels(ctx, oracle_lib):
+    import torch
+
+    st = strands.ragged_style([3, 0, 7, 12, 1], seed=5)
+    dv = torch.from_numpy(st.vertices).cuda()
+    b = ctx.bounding_box(dv.data_ptr(), st.vertex_count, torch.cuda.current_stream().cuda_stream)
+    bo = oracle_lib.bounding_box(st.vertices)
+    assert b.as_dict() == bo.as_dict()
+    dt = torch.empty_like(dv)
+    ctx.generate_tangents(dv.data_ptr(), st.segments, dt.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    t_ref = oracle_lib.generate_tangents(st.vertices, st.segments)
+    assert np.array_equal(dt.cpu().numpy().view(np.uint32), t_ref.view(np.uint32))
+    di = torch.empty(2 * st.segment_count, dtype=torch.int32, device="cuda")
+    ctx.generate_indices(st.segments, di.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(di.cpu().numpy().view(np.uint32), oracle_lib.generate_indices(st.segments))

@@ -1,0 +1,145 @@
+"""ctypes binding of libvkhr_cuda.so (the C ABI in include/vkhr_cuda.h).
+
+There is no fallback: importing this module without the built library, or
+using it without a CUDA device, raises.
+"""
+import ctypes as C
+import os
+
+from . import _abi
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libvkhr_cuda.so")
+
+EXPORTS = [
+    "vkhr_abi_version", "vkhr_create", "vkhr_destroy", "vkhr_status_string", "vkhr_last_error",
+    "vkhr_bounding_box", "vkhr_generate_tangents", "vkhr_generate_indices",
+    "vkhr_voxelize_vertices", "vkhr_voxelize_segments", "vkhr_normalize_densities", "vkhr_raymarch",
+    "vkhr_launch_count", "vkhr_sizeof_aabb", "vkhr_sizeof_raymarch_params",
+    "vkhr_set_profiling", "vkhr_profile_count", "vkhr_profile_read",
+]
+
+_lib = None
+
+
+class VkhrError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("%s: %s" % (_abi.STATUS_NAMES.get(status, status), message))
+        self.status = status
+
+
+def load():
+    """Load the library (no CUDA call is made)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libvkhr_cuda.so is not built (run __graft_entry__.build() or "
+                          "python vkhr_gb300/build.py): the GB300 path has no CPU fallback")
+    lib = C.CDLL(LIB_PATH)
+    P = C.c_void_p
+    lib.vkhr_abi_version.restype = C.c_int
+    lib.vkhr_create.argtypes = [C.c_int, C.POINTER(C.c_void_p)]
+    lib.vkhr_destroy.argtypes = [P]
+    lib.vkhr_status_string.argtypes = [C.c_int]
+    lib.vkhr_status_string.restype = C.c_char_p
+    lib.vkhr_last_error.argtypes = [P]
+    lib.vkhr_last_error.restype = C.c_char_p
+    lib.vkhr_bounding_box.argtypes = [P, P, C.c_uint32, C.POINTER(_abi.AABB), P]
+    lib.vkhr_generate_tangents.argtypes = [P, P, P, C.c_uint32, P, P]
+    lib.vkhr_generate_indices.argtypes = [P, P, C.c_uint32, P, P]
+    lib.vkhr_voxelize_vertices.argtypes = [P, P, P, C.c_uint32, C.POINTER(_abi.AABB), C.c_int32, C.c_int32,
+                                           C.c_int32, C.c_int32, P, P, P, P]
+    lib.vkhr_voxelize_segments.argtypes = [P, P, P, P, C.c_uint64, C.POINTER(_abi.AABB), C.c_int32, C.c_int32,
+                                           C.c_int32, C.c_int32, P, P, P, P]
+    lib.vkhr_normalize_densities.argtypes = [P, P, C.c_uint64, P]
+    lib.vkhr_raymarch.argtypes = [P, C.POINTER(_abi.RaymarchParams), P, P, P, P, P, P]
+    lib.vkhr_set_profiling.argtypes = [P, C.c_int]
+    lib.vkhr_profile_count.argtypes = [P]
+    lib.vkhr_profile_read.argtypes = [P, C.c_int, C.POINTER(C.c_char_p), C.POINTER(C.c_float)]
+    lib.vkhr_launch_count.argtypes = [P]
+    lib.vkhr_launch_count.restype = C.c_uint64
+    lib.vkhr_sizeof_aabb.restype = C.c_size_t
+    lib.vkhr_sizeof_raymarch_params.restype = C.c_size_t
+    for name in EXPORTS:
+        getattr(lib, name).restype = getattr(lib, name).restype or C.c_int
+    _lib = lib
+    return lib
+
+
+class Context:
+    """Owns one vkhr_ctx (device pinned at creation, scratch grows on demand)."""
+
+    def __init__(self, device=0):
+        self.lib = load()
+        h = C.c_void_p()
+        s = self.lib.vkhr_create(int(device), C.byref(h))
+        if s != _abi.VKHR_OK:
+            raise VkhrError(s, "vkhr_create(%d) failed" % device)
+        self.handle = h
+        self.device = device
+
+    def check(self, status):
+        if status != _abi.VKHR_OK:
+            raise VkhrError(status, self.lib.vkhr_last_error(self.handle).decode())
+
+    def set_profiling(self, enable):
+        self.check(self.lib.vkhr_set_profiling(self.handle, 1 if enable else 0))
+
+    def profile(self):
+        """[(kernel name, ms)] for every launch since profiling was enabled."""
+        out = []
+        for i in range(self.lib.vkhr_profile_count(self.handle)):
+            name = C.c_char_p()
+            ms = C.c_float()
+            self.check(self.lib.vkhr_profile_read(self.handle, i, C.byref(name), C.byref(ms)))
+            out.append((name.value.decode(), float(ms.value)))
+        return out
+
+    def launch_count(self):
+        return int(self.lib.vkhr_launch_count(self.handle))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.vkhr_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # thin wrappers: every pointer argument is a raw device address (int) or None
+    def bounding_box(self, d_vertices, vertex_count, stream=None):
+        b = _abi.AABB()
+        self.check(self.lib.vkhr_bounding_box(self.handle, d_vertices, vertex_count, C.byref(b), stream))
+        return b
+
+    def generate_tangents(self, d_vertices, segments_u16, d_tangents, stream=None):
+        self.check(self.lib.vkhr_generate_tangents(self.handle, d_vertices, segments_u16.ctypes.data,
+                                                   segments_u16.shape[0], d_tangents, stream))
+
+    def generate_indices(self, segments_u16, d_indices, stream=None):
+        self.check(self.lib.vkhr_generate_indices(self.handle, segments_u16.ctypes.data, segments_u16.shape[0],
+                                                  d_indices, stream))
+
+    def voxelize_vertices(self, d_vertices, d_tangent_in, vertex_count, bounds, res, index_mode, d_counts,
+                          d_densities, d_tangents, stream=None):
+        w, h, d = res
+        self.check(self.lib.vkhr_voxelize_vertices(self.handle, d_vertices, d_tangent_in, vertex_count,
+                                                   C.byref(bounds), w, h, d, index_mode, d_counts, d_densities,
+                                                   d_tangents, stream))
+
+    def voxelize_segments(self, d_vertices, d_tangent_in, d_indices, index_count, bounds, res, index_mode, d_counts,
+                          d_densities, d_tangents, stream=None):
+        w, h, d = res
+        self.check(self.lib.vkhr_voxelize_segments(self.handle, d_vertices, d_tangent_in, d_indices, index_count,
+                                                   C.byref(bounds), w, h, d, index_mode, d_counts, d_densities,
+                                                   d_tangents, stream))
+
+    def normalize_densities(self, d_densities, n, stream=None):
+        self.check(self.lib.vkhr_normalize_densities(self.handle, d_densities, n, stream))
+
+    def raymarch(self, params, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, stream=None):
+        self.check(self.lib.vkhr_raymarch(self.handle, C.byref(params), d_density, d_tangent, d_depth_in, d_rgba,
+                                          d_depth_out, stream))

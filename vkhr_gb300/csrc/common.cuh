@@ -1,0 +1,88 @@
+// common.cuh -- shared definitions of the GB300 backend (context, scratch,
+// error plumbing, exact FP32 helpers).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <cstdio>
+
+#include "../../include/vkhr_cuda.h"
+
+// Device status bits (ctx->d_words[WORD_STATUS]).
+enum : unsigned {
+    VKHR_DEV_STEPS_OVERFLOW = 1u,   // a segment spans >= 2^24 voxels (the reference never terminates)
+    VKHR_DEV_LIST_OVERFLOW = 2u,    // fixed-capacity visit list too small
+    VKHR_DEV_TIMEOUT = 4u,          // a bounded device wait gave up
+};
+
+// Slots of the small device word array every context owns.
+enum {
+    WORD_TOTAL_VISITS = 0,   // visits counted by the count pass
+    WORD_LIST_CURSOR = 1,    // allocation cursor of the visit list
+    WORD_HEAVY_COUNT = 2,    // voxels routed to the heavy resolve
+    WORD_STATUS = 3,         // VKHR_DEV_* bits
+    WORD_MEDIUM_COUNT = 4,   // voxels routed to the medium resolve
+    WORD_AABB = 5,           // bounding-box / normalize scratch (8 slots)
+    WORD_COUNT = 16
+};
+
+struct vkhr_ctx {
+    int device;
+    int sm_count;
+    // grow-only scratch
+    uint32_t* cursor;          // per-voxel list cursor (u32 x voxels)
+    size_t cursor_cap;         // in elements
+    uint32_t* list;            // visit keys
+    size_t list_cap;           // in elements
+    uint32_t* heavy;           // voxel ids routed to the heavy resolve
+    size_t heavy_cap;          // in elements
+    unsigned long long* d_words;
+    unsigned long long* h_words; // pinned mirror
+    cudaEvent_t ev;
+    unsigned long long launches; // kernels this context has launched
+    // kernel tracer (vkhr_set_profiling): an event pair around every launch
+    int profiling;
+    int prof_n;
+    cudaEvent_t* prof_ev;        // 2 * kProfileMax events
+    const char** prof_name;      // kProfileMax kernel names
+    char last_error[512];
+};
+
+constexpr int kProfileMax = 4096;
+
+void vkhr_prof_begin(vkhr_ctx* ctx, const char* name, cudaStream_t st);
+void vkhr_prof_end(vkhr_ctx* ctx, cudaStream_t st);
+
+// Launch bookkeeping: every kernel launch of the library goes through this.
+#define VKHR_LAUNCH(ctx, kernel, grid, block, smem, stream, ...)                                  \
+    do {                                                                                           \
+        if ((ctx)->profiling) vkhr_prof_begin((ctx), #kernel, (stream));                           \
+        kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);                                \
+        if ((ctx)->profiling) vkhr_prof_end((ctx), (stream));                                      \
+        ++(ctx)->launches;                                                                         \
+    } while (0)
+
+#define VKHR_CUDA_TRY(ctx, call)                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) return vkhr_fail_cuda((ctx), e_, #call, __FILE__, __LINE__);       \
+    } while (0)
+
+vkhr_status vkhr_fail(vkhr_ctx* ctx, vkhr_status s, const char* msg);
+vkhr_status vkhr_fail_cuda(vkhr_ctx* ctx, cudaError_t e, const char* what, const char* file, int line);
+
+// Grow-only device buffer; contents are not preserved on growth.
+vkhr_status vkhr_reserve(vkhr_ctx* ctx, void** ptr, size_t* cap_elems, size_t need_elems, size_t elem_bytes);
+
+static inline unsigned vkhr_blocks(size_t n, unsigned threads)
+{
+    size_t b = (n + threads - 1) / threads;
+    return (unsigned)(b == 0 ? 1 : b);
+}
+
+// ---- exact FP32 helpers (no contraction, round-to-nearest) ---------------------
+// glm::min(x, y) = y < x ? y : x and glm::max(x, y) = x < y ? y : x.
+__device__ __forceinline__ float glm_min(float x, float y) { return (y < x) ? y : x; }
+__device__ __forceinline__ float glm_max(float x, float y) { return (x < y) ? y : x; }

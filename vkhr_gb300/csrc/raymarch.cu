@@ -1,0 +1,426 @@
+// raymarch.cu -- volume raymarcher: the proxy-cube entry, isosurface march,
+// Kajiya-Kay shading, density self-shadowing and local ambient occlusion of
+// share/shaders/volumes/volume.frag:31-103 and its includes, in FP32 on GB300.
+//
+// One thread per pixel; a warp covers an 8x4 pixel tile so that neighbouring
+// rays walk neighbouring voxels.  Differences from a literal translation, all
+// exact with respect to the shader's outputs:
+//   * the proxy cube's rasterization becomes a slab test of the pixel-centre
+//     ray against the AABB (front faces only: a camera inside covers nothing);
+//   * the per-step depth test (volume_rendering.glsl:30-34) is skipped when
+//     the ray's far end already passes it (depth grows monotonically along a
+//     ray that moves away from the camera);
+//   * the primary march stops once the isosurface point is frozen
+//     (acc > iso), found, and coverage lod*(acc/iso)*alpha >= 1, after which
+//     no later sample can change any output (coverage is clamped to 1);
+//   * texture filtering is a software trilinear with FP32 weights at Vulkan's
+//     texel centres, CLAMP_TO_BORDER reading 0.
+#include "common.cuh"
+
+#include <algorithm>
+#include <cmath>
+
+namespace {
+
+constexpr int kTileW = 8, kTileH = 4;         // pixels per warp
+constexpr int kWarpsX = 2, kWarpsY = 2;       // warps per block
+constexpr float kMaxSteps = 1048576.0f;       // 2^20: t += 1/steps still advances below 1
+
+struct RayConsts {
+    int W, H;
+    float inv_vp[16];
+    float pv[16];
+    float cam[3];
+    float radius;
+    float lo[3], hi[3];
+    int res[3];
+    float tsc[3], tbias[3];   // texel coordinate u = P * tsc + tbias = (P - origin) / size * N - 0.5
+    float voxel_space[3];
+    float light[3], intensity[3], color[3];
+    float alpha, exponent, iso, kd;
+    float steps, shadow_steps, thickness, ao_kernel, ao_radius, ao_exp, ao_max;
+    float lod;
+    int shading_model, deep_shadows_on;
+};
+
+template <int DF>
+struct DensityTexel;
+template <>
+struct DensityTexel<VKHR_DENSITY_U8_UNORM> {
+    typedef uint8_t T;
+    static __device__ __forceinline__ float load(const T* p, size_t i) { return (float)__ldg(p + i); }
+    static constexpr float scale = 1.0f / 255.0f; // UNORM c / 255
+};
+template <>
+struct DensityTexel<VKHR_DENSITY_U32_COUNT> {
+    typedef uint32_t T;
+    static __device__ __forceinline__ float load(const T* p, size_t i) { return (float)__ldg(p + i); }
+    static constexpr float scale = 1.0f;
+};
+template <>
+struct DensityTexel<VKHR_DENSITY_F32> {
+    typedef float T;
+    static __device__ __forceinline__ float load(const T* p, size_t i) { return __ldg(p + i); }
+    static constexpr float scale = 1.0f;
+};
+
+struct Vec3 {
+    float x, y, z;
+};
+__device__ __forceinline__ Vec3 v3(float x, float y, float z) { return Vec3{x, y, z}; }
+__device__ __forceinline__ Vec3 operator+(Vec3 a, Vec3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ Vec3 operator-(Vec3 a, Vec3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ Vec3 operator*(Vec3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float dot(Vec3 a, Vec3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ Vec3 normalize(Vec3 a)
+{
+    float l = sqrtf(dot(a, a));
+    return v3(a.x / l, a.y / l, a.z / l); // 0/0 -> NaN for a zero vector, as on the GPU
+}
+// GLSL mix(x, y, a) = x * (1 - a) + y * a
+__device__ __forceinline__ Vec3 mix(Vec3 a, Vec3 b, float t)
+{
+    const float u = 1.0f - t;
+    return v3(fmaf(b.x, t, a.x * u), fmaf(b.y, t, a.y * u), fmaf(b.z, t, a.z * u));
+}
+__device__ __forceinline__ float clip_depth(const RayConsts& c, Vec3 p)
+{
+    float z = fmaf(c.pv[2], p.x, fmaf(c.pv[6], p.y, fmaf(c.pv[10], p.z, c.pv[14])));
+    float w = fmaf(c.pv[3], p.x, fmaf(c.pv[7], p.y, fmaf(c.pv[11], p.z, c.pv[15])));
+    return z / w;
+}
+
+// Texel-space set-up; false when all eight taps read the border.
+__device__ __forceinline__ bool tex_setup(const RayConsts& c, Vec3 p, int i0[3], float a[3])
+{
+    const float pp[3] = {p.x, p.y, p.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        float u = fmaf(pp[k], c.tsc[k], c.tbias[k]);
+        if (!(u > -2.0f && u < (float)(c.res[k] + 1))) return false;
+        float f = floorf(u);
+        i0[k] = (int)f;
+        a[k] = u - f;
+    }
+    return true;
+}
+
+template <int DF>
+__device__ __forceinline__ float sample_density(const RayConsts& c, const typename DensityTexel<DF>::T* __restrict__ d,
+                                                Vec3 p)
+{
+    typedef DensityTexel<DF> TX;
+    int i0[3];
+    float a[3];
+    if (!tex_setup(c, p, i0, a)) return 0.0f;
+    const int nx = c.res[0], ny = c.res[1], nz = c.res[2];
+    float v[8];
+    if (i0[0] >= 0 && i0[0] + 1 < nx && i0[1] >= 0 && i0[1] + 1 < ny && i0[2] >= 0 && i0[2] + 1 < nz) {
+        const size_t sy = (size_t)nx, sz = (size_t)nx * ny;
+        const size_t b = (size_t)i0[0] + sy * i0[1] + sz * i0[2];
+        v[0] = TX::load(d, b);
+        v[1] = TX::load(d, b + 1);
+        v[2] = TX::load(d, b + sy);
+        v[3] = TX::load(d, b + sy + 1);
+        v[4] = TX::load(d, b + sz);
+        v[5] = TX::load(d, b + sz + 1);
+        v[6] = TX::load(d, b + sz + sy);
+        v[7] = TX::load(d, b + sz + sy + 1);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int x = i0[0] + (k & 1), y = i0[1] + ((k >> 1) & 1), z = i0[2] + (k >> 2);
+            v[k] = (x >= 0 && y >= 0 && z >= 0 && x < nx && y < ny && z < nz)
+                       ? TX::load(d, (size_t)x + (size_t)nx * ((size_t)y + (size_t)ny * z))
+                       : 0.0f;
+        }
+    }
+    const float x00 = fmaf(a[0], v[1] - v[0], v[0]);
+    const float x10 = fmaf(a[0], v[3] - v[2], v[2]);
+    const float x01 = fmaf(a[0], v[5] - v[4], v[4]);
+    const float x11 = fmaf(a[0], v[7] - v[6], v[6]);
+    const float y0 = fmaf(a[1], x10 - x00, x00);
+    const float y1 = fmaf(a[1], x11 - x01, x01);
+    return fmaf(a[2], y1 - y0, y0) * TX::scale;
+}
+
+template <int TF>
+__device__ __forceinline__ Vec3 tangent_texel(const void* t, int x, int y, int z, const int* n)
+{
+    if (x < 0 || y < 0 || z < 0 || x >= n[0] || y >= n[1] || z >= n[2]) return v3(0.0f, 0.0f, 0.0f);
+    const size_t i = (size_t)x + (size_t)n[0] * ((size_t)y + (size_t)n[1] * z);
+    if (TF == VKHR_TANGENT_I8_SNORM) {
+        const char4 q = __ldg(reinterpret_cast<const char4*>(t) + i);
+        return v3(fmaxf((float)q.x / 127.0f, -1.0f), fmaxf((float)q.y / 127.0f, -1.0f),
+                  fmaxf((float)q.z / 127.0f, -1.0f));
+    }
+    const float4 f = __ldg(reinterpret_cast<const float4*>(t) + i);
+    return v3(f.x, f.y, f.z);
+}
+
+template <int TF>
+__device__ Vec3 sample_tangent(const RayConsts& c, const void* t, Vec3 p)
+{
+    int i0[3];
+    float a[3];
+    Vec3 acc = v3(0.0f, 0.0f, 0.0f);
+    if (!tex_setup(c, p, i0, a)) return acc;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int dx = k & 1, dy = (k >> 1) & 1, dz = k >> 2;
+        const float w = (dx ? a[0] : 1.0f - a[0]) * (dy ? a[1] : 1.0f - a[1]) * (dz ? a[2] : 1.0f - a[2]);
+        acc = acc + tangent_texel<TF>(t, i0[0] + dx, i0[1] + dy, i0[2] + dz, c.res) * w;
+    }
+    return acc;
+}
+
+template <int DF, int TF>
+__global__ void __launch_bounds__(32 * kWarpsX * kWarpsY)
+raymarch_kernel(const __grid_constant__ RayConsts c, const typename DensityTexel<DF>::T* __restrict__ dens,
+                const void* __restrict__ tang, const float* __restrict__ depth_in, float4* __restrict__ rgba,
+                float* __restrict__ depth_out)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int px = (blockIdx.x * kWarpsX + (warp % kWarpsX)) * kTileW + (lane % kTileW);
+    const int py = (blockIdx.y * kWarpsY + (warp / kWarpsX)) * kTileH + (lane / kTileW);
+    if (px >= c.W || py >= c.H) return;
+    const size_t at = (size_t)py * c.W + px;
+
+    // ---- proxy cube: entry point of the pixel-centre ray ---------------------
+    const float nx = 2.0f * ((float)px + 0.5f) / (float)c.W - 1.0f;
+    const float ny = 2.0f * ((float)py + 0.5f) / (float)c.H - 1.0f;
+    float f[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) f[r] = c.inv_vp[r] * nx + c.inv_vp[4 + r] * ny + c.inv_vp[8 + r] + c.inv_vp[12 + r];
+    const float dir[3] = {f[0] / f[3] - c.cam[0], f[1] / f[3] - c.cam[1], f[2] / f[3] - c.cam[2]};
+    float tmin = -INFINITY, tmax = INFINITY;
+    bool hit = true;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        if (dir[k] == 0.0f) {
+            if (c.cam[k] < c.lo[k] || c.cam[k] > c.hi[k]) hit = false;
+            continue;
+        }
+        float t0 = (c.lo[k] - c.cam[k]) / dir[k], t1 = (c.hi[k] - c.cam[k]) / dir[k];
+        tmin = fmaxf(tmin, fminf(t0, t1));
+        tmax = fminf(tmax, fmaxf(t0, t1));
+    }
+    float4 out = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float out_depth = 1.0f;
+    if (hit && tmin > 0.0f && tmin <= tmax) {
+        const Vec3 cam = v3(c.cam[0], c.cam[1], c.cam[2]);
+        const Vec3 start = v3(fmaf(tmin, dir[0], c.cam[0]), fmaf(tmin, dir[1], c.cam[1]), fmaf(tmin, dir[2], c.cam[2]));
+        const Vec3 end = start + normalize(start - cam) * c.radius;
+        const float db = depth_in ? depth_in[at] : 1.0f;
+        const bool depth_test = !(clip_depth(c, end) < db);
+
+        // ---- volume_surface (volume_rendering.glsl:19-52) --------------------
+        const float step = 1.0f / c.steps;
+        float acc = 0.0f;
+        Vec3 surf = v3(0.0f, 0.0f, 0.0f), entry = v3(0.0f, 0.0f, 0.0f);
+        bool found = false, entered = false;
+        for (float t = 0.0f; t < 1.0f; t += step) {
+            const Vec3 P = mix(start, end, t);
+            if (depth_test && db < clip_depth(c, P)) break;
+            const float rho = sample_density<DF>(c, dens, P);
+            acc += rho;
+            if (rho != 0.0f) {
+                if (acc <= c.iso) surf = P;
+                if (acc >= c.iso) found = true;
+                if (!entered) { entry = P; entered = true; }
+                if (acc > c.iso && c.lod * (acc / c.iso) * c.alpha >= 1.0f) break; // outputs final
+            }
+        }
+        if (!found && entered) surf = entry;
+        const float a = acc / c.iso;
+        if (a != 0.0f) {
+            const float coverage = c.lod * a * c.alpha;
+            // ---- shading (volume.frag:50-67, kajiya-kay.glsl:7-24) ------------
+            Vec3 shading = v3(1.0f, 1.0f, 1.0f);
+            const Vec3 light = v3(c.light[0], c.light[1], c.light[2]);
+            if (c.shading_model == VKHR_SHADING_KAJIYA_KAY) {
+                const Vec3 L = normalize(light - surf);
+                const Vec3 E = normalize(surf - cam);
+                const Vec3 T = normalize(sample_tangent<TF>(c, tang, surf));
+                const float cosTL = dot(T, L), cosTE = dot(T, E);
+                const float sinTL = sqrtf(fmaxf(1.0f - cosTL * cosTL, 0.0f));
+                const float sinTE = sqrtf(fmaxf(1.0f - cosTE * cosTE, 0.0f));
+                const float spec = powf(fmaxf(cosTL * cosTE + sinTL * sinTE, 0.0f), c.exponent);
+                const float dk = c.kd * sinTL;
+                shading = v3(c.color[0] * dk + c.intensity[0] * spec, c.color[1] * dk + c.intensity[1] * spec,
+                             c.color[2] * dk + c.intensity[2] * spec);
+            }
+            float occlusion = 1.0f;
+            // ---- volume_approximated_deep_shadows (approximate_deep_shadows.glsl:24-36)
+            if (c.deep_shadows_on == 1 && c.shading_model != VKHR_SHADING_LAO) {
+                const float sstep = 1.0f / c.shadow_steps;
+                float strands = 0.0f;
+                for (float t = 0.0f; t < 1.0f; t += sstep)
+                    strands += sample_density<DF>(c, dens, mix(surf, light, t)) * c.thickness;
+                occlusion *= powf(1.0f - c.alpha, strands);
+            }
+            // ---- local_ambient_occlusion (local_ambient_occlusion.glsl:9-30)
+            if (c.shading_model != VKHR_SHADING_ADSM) {
+                const float kr = (c.ao_kernel - 1.0f) / 2.0f;
+                const float scale = c.ao_radius / kr;
+                const Vec3 sc = v3(c.voxel_space[0] * scale, c.voxel_space[1] * scale, c.voxel_space[2] * scale);
+                float dsum = 0.0f;
+                for (float z = -kr; z <= kr; z += 1.0f)
+                    for (float y = -kr; y <= kr; y += 1.0f)
+                        for (float x = -kr; x <= kr; x += 1.0f) {
+                            const Vec3 q = v3(surf.x + x * sc.x, surf.y + y * sc.y, surf.z + z * sc.z);
+                            dsum += fminf(sample_density<DF>(c, dens, q), c.ao_max);
+                        }
+                occlusion *= powf(1.0f - dsum / (c.ao_kernel * c.ao_kernel * c.ao_kernel), c.ao_exp);
+            }
+            // packUnorm4x8 clamp (ppll.glsl:32); NaN -> 0
+            out = make_float4(__saturatef(shading.x * occlusion), __saturatef(shading.y * occlusion),
+                              __saturatef(shading.z * occlusion), __saturatef(coverage));
+            out_depth = clip_depth(c, surf);
+        }
+    }
+    rgba[at] = out;
+    if (depth_out) depth_out[at] = out_depth;
+}
+
+bool invert4(const double m[16], double inv[16])
+{
+    double a[4][8];
+    for (int r = 0; r < 4; ++r)
+        for (int k = 0; k < 4; ++k) {
+            a[r][k] = m[k * 4 + r];
+            a[r][k + 4] = r == k ? 1.0 : 0.0;
+        }
+    for (int k = 0; k < 4; ++k) {
+        int piv = k;
+        for (int r = k + 1; r < 4; ++r)
+            if (std::fabs(a[r][k]) > std::fabs(a[piv][k])) piv = r;
+        if (a[piv][k] == 0.0) return false;
+        if (piv != k)
+            for (int j = 0; j < 8; ++j) std::swap(a[k][j], a[piv][j]);
+        const double d = a[k][k];
+        for (int j = 0; j < 8; ++j) a[k][j] /= d;
+        for (int r = 0; r < 4; ++r)
+            if (r != k) {
+                const double f = a[r][k];
+                for (int j = 0; j < 8; ++j) a[r][j] -= f * a[k][j];
+            }
+    }
+    for (int r = 0; r < 4; ++r)
+        for (int k = 0; k < 4; ++k) inv[k * 4 + r] = a[r][k + 4];
+    return true;
+}
+
+vkhr_status make_consts(vkhr_ctx* ctx, const vkhr_raymarch_params* p, RayConsts& c)
+{
+    if (p->width <= 0 || p->height <= 0) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "width/height must be > 0");
+    if (!(p->raycast_steps > 0.0f) || !(p->raycast_steps <= kMaxSteps))
+        return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "raycast_steps must be in (0, 2^20]");
+    const float sst = p->shadow_steps > 0.0f ? p->shadow_steps : p->raycast_steps;
+    if (!(sst <= kMaxSteps)) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "shadow_steps must be <= 2^20");
+    if (!(p->ao_kernel_size >= 2.0f && p->ao_kernel_size <= 16.0f))
+        return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "ao_kernel_size must be in [2, 16]");
+    if (!(p->isosurface > 0.0f)) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "isosurface must be > 0");
+    if (p->density_format < 0 || p->density_format > 2 || p->tangent_format < 0 || p->tangent_format > 1)
+        return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "unknown texel format");
+    for (int k = 0; k < 3; ++k) {
+        if (p->volume_resolution[k] <= 0) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "volume_resolution must be > 0");
+        if (!(p->volume_bounds.size[k] > 0.0f) || !std::isfinite(p->volume_bounds.size[k]))
+            return vkhr_fail(ctx, VKHR_ERR_DEGENERATE_AABB, "every AABB extent must be finite and > 0");
+    }
+    c.W = p->width;
+    c.H = p->height;
+    double pv[16], inv[16];
+    for (int col = 0; col < 4; ++col)
+        for (int r = 0; r < 4; ++r) {
+            double s = 0.0;
+            for (int k = 0; k < 4; ++k) s += (double)p->projection[k * 4 + r] * (double)p->view[col * 4 + k];
+            pv[col * 4 + r] = s;
+        }
+    if (!invert4(pv, inv)) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "projection * view is singular");
+    for (int i = 0; i < 16; ++i) {
+        c.pv[i] = (float)pv[i];
+        c.inv_vp[i] = (float)inv[i];
+    }
+    for (int k = 0; k < 3; ++k) {
+        c.cam[k] = p->camera_position[k];
+        c.lo[k] = p->volume_bounds.origin[k];
+        c.hi[k] = p->volume_bounds.origin[k] + p->volume_bounds.size[k];
+        c.res[k] = p->volume_resolution[k];
+        const double s = (double)p->volume_resolution[k] / (double)p->volume_bounds.size[k];
+        c.tsc[k] = (float)s;
+        c.tbias[k] = (float)(-(double)p->volume_bounds.origin[k] * s - 0.5);
+        c.voxel_space[k] = p->volume_bounds.size[k] / (float)p->volume_resolution[k];
+        c.light[k] = p->light_origin[k];
+        c.intensity[k] = p->light_intensity[k];
+        c.color[k] = p->hair_color[k];
+    }
+    c.radius = p->volume_bounds.radius;
+    c.alpha = p->hair_alpha;
+    c.exponent = p->hair_exponent;
+    c.iso = p->isosurface;
+    c.kd = p->kd;
+    c.steps = p->raycast_steps;
+    c.shadow_steps = sst;
+    c.thickness = p->shadow_thickness;
+    c.ao_kernel = p->ao_kernel_size;
+    c.ao_radius = p->occlusion_radius;
+    c.ao_exp = p->ao_exponent;
+    c.ao_max = p->ao_max;
+    // lod() of scheme.glsl:7-11 for the camera's look-at distance
+    if (p->renderer == VKHR_RENDERER_RASTERIZER) c.lod = 0.0f;
+    else if (p->renderer == VKHR_RENDERER_RAYMARCHER) c.lod = 1.0f;
+    else {
+        float t = (p->look_at_distance - p->magnified_distance) / (p->minified_distance - p->magnified_distance);
+        t = std::min(std::max(t, 0.0f), 1.0f);
+        c.lod = t * t * (3.0f - 2.0f * t);
+    }
+    c.shading_model = p->shading_model;
+    c.deep_shadows_on = p->deep_shadows_on;
+    return VKHR_OK;
+}
+
+template <int DF, int TF>
+void launch(vkhr_ctx* ctx, const RayConsts& c, const void* dens, const void* tang, const float* din, float* rgba,
+            float* dout, cudaStream_t st)
+{
+    const dim3 block(32 * kWarpsX * kWarpsY);
+    const dim3 grid((c.W + kTileW * kWarpsX - 1) / (kTileW * kWarpsX), (c.H + kTileH * kWarpsY - 1) / (kTileH * kWarpsY));
+    VKHR_LAUNCH(ctx, (raymarch_kernel<DF, TF>), grid, block, 0, st, c, (const typename DensityTexel<DF>::T*)dens, tang,
+                din, reinterpret_cast<float4*>(rgba), dout);
+}
+
+} // namespace
+
+extern "C" vkhr_status vkhr_raymarch(vkhr_ctx* ctx, const vkhr_raymarch_params* params, const void* d_density,
+                                     const void* d_tangent, const float* d_depth_in, float* d_rgba, float* d_depth_out,
+                                     void* stream)
+{
+    if (!ctx) return VKHR_ERR_INVALID_ARG;
+    if (!params || !d_density || !d_tangent || !d_rgba)
+        return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "params, d_density, d_tangent and d_rgba are required");
+    if (reinterpret_cast<uintptr_t>(d_rgba) & 15u) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_rgba must be 16-byte aligned");
+    RayConsts c;
+    vkhr_status s = make_consts(ctx, params, c);
+    if (s != VKHR_OK) return s;
+    const size_t tan_align = params->tangent_format == VKHR_TANGENT_I8_SNORM ? 4 : 16;
+    if (reinterpret_cast<uintptr_t>(d_tangent) & (tan_align - 1))
+        return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_tangent is misaligned for its format");
+    VKHR_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    const int df = params->density_format, tf = params->tangent_format;
+    if (df == VKHR_DENSITY_U8_UNORM && tf == VKHR_TANGENT_I8_SNORM)
+        launch<VKHR_DENSITY_U8_UNORM, VKHR_TANGENT_I8_SNORM>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
+    else if (df == VKHR_DENSITY_U8_UNORM)
+        launch<VKHR_DENSITY_U8_UNORM, VKHR_TANGENT_F32X4>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
+    else if (df == VKHR_DENSITY_U32_COUNT && tf == VKHR_TANGENT_I8_SNORM)
+        launch<VKHR_DENSITY_U32_COUNT, VKHR_TANGENT_I8_SNORM>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
+    else if (df == VKHR_DENSITY_U32_COUNT)
+        launch<VKHR_DENSITY_U32_COUNT, VKHR_TANGENT_F32X4>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
+    else if (tf == VKHR_TANGENT_I8_SNORM)
+        launch<VKHR_DENSITY_F32, VKHR_TANGENT_I8_SNORM>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
+    else
+        launch<VKHR_DENSITY_F32, VKHR_TANGENT_F32X4>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
+    VKHR_CUDA_TRY(ctx, cudaGetLastError());
+    return VKHR_OK;
+}
