@@ -1,0 +1,247 @@
+// vkhr/cuda.hh -- C++17 facade over the C ABI (vkhr_cuda.h) for the vkhr host.
+//
+// Header-only; needs no CUDA headers: device memory goes through the ABI's
+// vkhr_malloc / vkhr_upload / vkhr_download.  Errors from the ABI become
+// vkhr::cuda::Error exceptions (the reference's Vulkan layer throws
+// vkpp::Exception the same way, include/vkpp/exception.hh).
+//
+// Drop-in points in the reference:
+//   * vkhr::cuda::voxelize_segments(style, 256, 256, 256) replaces
+//     style.voxelize_segments(256, 256, 256) at src/vkhr/rasterizer/hair_style.cc:75
+//     and returns the same HairStyle::Volume-shaped result (u8 densities,
+//     i8vec4 tangents, resolution, bounds), bit-identical to it;
+//   * vkhr::cuda::voxelize_vertices likewise for HairStyle::voxelize_vertices
+//     (src/vkhr/scene_graph/hair_style.cc:257-294);
+//   * vkhr::Raymarcher::draw renders the volume.frag raymarch
+//     (share/shaders/volumes/volume.frag:31-103) headlessly into RGBA + depth.
+// The templates accept the reference's own vkhr::HairStyle (any type with
+// `vertices`, `tangents`, `indices` vectors of 12-byte vec3 / uint32 and a
+// get_bounding_box() returning an AABB-shaped struct).
+#ifndef VKHR_CUDA_HH
+#define VKHR_CUDA_HH
+
+#include "../vkhr_cuda.h"
+
+#include <cstdint>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+namespace vkhr {
+namespace cuda {
+
+class Error : public std::runtime_error {
+public:
+    Error(vkhr_status s, const std::string& what) : std::runtime_error(what), status(s) {}
+    vkhr_status status;
+};
+
+class Context {
+public:
+    explicit Context(int device = 0)
+    {
+        vkhr_status s = vkhr_create(device, &ctx_);
+        if (s != VKHR_OK) throw Error(s, std::string("vkhr_create: ") + vkhr_status_string(s));
+    }
+    ~Context() { vkhr_destroy(ctx_); }
+    Context(const Context&) = delete;
+    Context& operator=(const Context&) = delete;
+
+    vkhr_ctx* get() const { return ctx_; }
+
+    void check(vkhr_status s) const
+    {
+        if (s != VKHR_OK) throw Error(s, vkhr_last_error(ctx_));
+    }
+
+    // ---- device buffers -----------------------------------------------------
+    class Buffer {
+    public:
+        Buffer() = default;
+        Buffer(const Context& c, size_t bytes) : ctx_(&c), bytes_(bytes) { c.check(vkhr_malloc(c.get(), bytes, &ptr_)); }
+        ~Buffer() { release(); }
+        Buffer(Buffer&& o) noexcept { *this = std::move(o); }
+        Buffer& operator=(Buffer&& o) noexcept
+        {
+            if (this != &o) {
+                release();
+                ctx_ = o.ctx_;
+                ptr_ = o.ptr_;
+                bytes_ = o.bytes_;
+                o.ptr_ = nullptr;
+            }
+            return *this;
+        }
+        void* data() const { return ptr_; }
+        size_t size() const { return bytes_; }
+        void upload(const void* src, size_t bytes, void* stream = nullptr) const
+        {
+            ctx_->check(vkhr_upload(ctx_->get(), ptr_, src, bytes, stream));
+        }
+        void download(void* dst, size_t bytes, void* stream = nullptr) const
+        {
+            ctx_->check(vkhr_download(ctx_->get(), dst, ptr_, bytes, stream));
+        }
+
+    private:
+        void release()
+        {
+            if (ptr_ && ctx_) vkhr_free(ctx_->get(), ptr_);
+            ptr_ = nullptr;
+        }
+        const Context* ctx_ = nullptr;
+        void* ptr_ = nullptr;
+        size_t bytes_ = 0;
+    };
+
+    template <class T>
+    Buffer upload(const std::vector<T>& v, void* stream = nullptr) const
+    {
+        Buffer b(*this, v.size() * sizeof(T));
+        b.upload(v.data(), v.size() * sizeof(T), stream);
+        return b;
+    }
+
+    void sync(void* stream = nullptr) const { check(vkhr_sync(ctx_, stream)); }
+
+private:
+    vkhr_ctx* ctx_ = nullptr;
+};
+
+// HairStyle::Volume with the same fields as the reference (hair_style.hh:89-101)
+// plus the exact uint32 counts.  `tangents` holds 4 int8 per voxel (i8vec4).
+struct Volume {
+    int resolution[3];
+    vkhr_aabb bounds;
+    std::vector<unsigned char> densities;
+    std::vector<int8_t> tangents;  // x, y, z, w per voxel
+    std::vector<uint32_t> counts;
+
+    // Volume::normalize (hair_style.cc:344-357), on the host data.
+    void normalize(Context& ctx)
+    {
+        Context::Buffer d(ctx, densities.size());
+        d.upload(densities.data(), densities.size());
+        ctx.check(vkhr_normalize_densities(ctx.get(), static_cast<uint8_t*>(d.data()), densities.size(), nullptr));
+        d.download(densities.data(), densities.size());
+        ctx.sync();
+    }
+};
+
+template <class AABBLike>
+vkhr_aabb to_aabb(const AABBLike& a)
+{
+    vkhr_aabb b;
+    for (int c = 0; c < 3; ++c) {
+        b.origin[c] = a.origin[c];
+        b.size[c] = a.size[c];
+    }
+    b.radius = a.radius;
+    b.volume = a.volume;
+    return b;
+}
+
+namespace detail {
+template <class Style>
+Volume voxelize(Context& ctx, const Style& style, bool segments, int w, int h, int d, int index_mode)
+{
+    static_assert(sizeof(style.vertices[0]) == 12, "vertices must be 12-byte vec3");
+    static_assert(sizeof(style.tangents[0]) == 12, "tangents must be 12-byte vec3");
+    const size_t n = (size_t)w * (size_t)h * (size_t)d;
+    Volume vol;
+    vol.resolution[0] = w;
+    vol.resolution[1] = h;
+    vol.resolution[2] = d;
+    vol.bounds = to_aabb(style.get_bounding_box());
+    Context::Buffer v = ctx.upload(style.vertices);
+    Context::Buffer t = ctx.upload(style.tangents);
+    Context::Buffer counts(ctx, n * 4), dens(ctx, n), tq(ctx, n * 4);
+    if (segments) {
+        Context::Buffer idx = ctx.upload(style.indices);
+        ctx.check(vkhr_voxelize_segments(ctx.get(), static_cast<const float*>(v.data()),
+                                         static_cast<const float*>(t.data()), static_cast<const uint32_t*>(idx.data()),
+                                         style.indices.size(), &vol.bounds, w, h, d, index_mode,
+                                         static_cast<uint32_t*>(counts.data()), static_cast<uint8_t*>(dens.data()),
+                                         static_cast<int8_t*>(tq.data()), nullptr));
+        ctx.sync();
+    } else {
+        ctx.check(vkhr_voxelize_vertices(ctx.get(), static_cast<const float*>(v.data()),
+                                         static_cast<const float*>(t.data()), (uint32_t)style.vertices.size(),
+                                         &vol.bounds, w, h, d, index_mode, static_cast<uint32_t*>(counts.data()),
+                                         static_cast<uint8_t*>(dens.data()), static_cast<int8_t*>(tq.data()), nullptr));
+    }
+    vol.densities.resize(n);
+    vol.tangents.resize(4 * n);
+    vol.counts.resize(n);
+    dens.download(vol.densities.data(), n);
+    tq.download(vol.tangents.data(), 4 * n);
+    counts.download(vol.counts.data(), 4 * n);
+    ctx.sync();
+    return vol;
+}
+} // namespace detail
+
+// HairStyle::voxelize_vertices (hair_style.cc:257-294) on the GPU.
+template <class Style>
+Volume voxelize_vertices(Context& ctx, const Style& style, int w, int h, int d,
+                         int index_mode = VKHR_INDEX_REF_FP32)
+{
+    return detail::voxelize(ctx, style, false, w, h, d, index_mode);
+}
+
+// HairStyle::voxelize_segments (hair_style.cc:296-342) on the GPU.
+template <class Style>
+Volume voxelize_segments(Context& ctx, const Style& style, int w, int h, int d,
+                         int index_mode = VKHR_INDEX_REF_FP32)
+{
+    return detail::voxelize(ctx, style, true, w, h, d, index_mode);
+}
+
+} // namespace cuda
+
+// Headless raymarcher: the draw of vulkan::Volume (src/vkhr/rasterizer/volume.cc:104-112)
+// with volume.frag, into device buffers; `Image` holds the host copy.
+class Raymarcher {
+public:
+    struct Image {
+        int width = 0, height = 0;
+        std::vector<float> rgba;   // width*height*4, packUnorm4x8-clamped colour + coverage
+        std::vector<float> depth;  // width*height, 1.0 where no fragment
+    };
+
+    explicit Raymarcher(cuda::Context& ctx) : ctx_(ctx) {}
+
+    // Raymarch a normalized Volume (u8 densities, i8vec4 tangents) with the
+    // UBO contents in `params` (density/tangent formats are set here).
+    Image draw(const cuda::Volume& vol, vkhr_raymarch_params params)
+    {
+        params.density_format = VKHR_DENSITY_U8_UNORM;
+        params.tangent_format = VKHR_TANGENT_I8_SNORM;
+        for (int c = 0; c < 3; ++c) params.volume_resolution[c] = vol.resolution[c];
+        params.volume_bounds = vol.bounds;
+        cuda::Context::Buffer d = ctx_.upload(vol.densities);
+        cuda::Context::Buffer t = ctx_.upload(vol.tangents);
+        const size_t px = (size_t)params.width * (size_t)params.height;
+        cuda::Context::Buffer rgba(ctx_, px * 16), depth(ctx_, px * 4);
+        ctx_.check(vkhr_raymarch(ctx_.get(), &params, d.data(), t.data(), nullptr, static_cast<float*>(rgba.data()),
+                                 static_cast<float*>(depth.data()), nullptr));
+        Image img;
+        img.width = params.width;
+        img.height = params.height;
+        img.rgba.resize(px * 4);
+        img.depth.resize(px);
+        rgba.download(img.rgba.data(), px * 16);
+        depth.download(img.depth.data(), px * 4);
+        ctx_.sync();
+        return img;
+    }
+
+private:
+    cuda::Context& ctx_;
+};
+
+} // namespace vkhr
+
+#endif

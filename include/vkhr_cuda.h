@@ -162,6 +162,16 @@ uint64_t vkhr_launch_count(const vkhr_ctx* ctx);
 size_t vkhr_sizeof_aabb(void);
 size_t vkhr_sizeof_raymarch_params(void);
 
+/* ---- device memory helpers ---------------------------------------------------
+ * So that a host without the CUDA toolkit (the reference's C++17 code) can
+ * stage its std::vector data: plain cudaMalloc / cudaFree / cudaMemcpyAsync
+ * on the context's device.  Copies are stream-ordered; vkhr_sync waits. */
+vkhr_status vkhr_malloc(vkhr_ctx* ctx, size_t bytes, void** d_out);
+vkhr_status vkhr_free(vkhr_ctx* ctx, void* d_ptr);
+vkhr_status vkhr_upload(vkhr_ctx* ctx, void* d_dst, const void* h_src, size_t bytes, void* stream);
+vkhr_status vkhr_download(vkhr_ctx* ctx, void* h_dst, const void* d_src, size_t bytes, void* stream);
+vkhr_status vkhr_sync(vkhr_ctx* ctx, void* stream);
+
 /* ---- strand data preparation ----------------------------------------------
  * Replaces HairStyle::generate_bounding_box + get_bounding_box
  * (hair_style.cc:215-255): min/max start at (0,0,0), so the box always holds

@@ -16,6 +16,7 @@ EXPORTS = [
     "vkhr_voxelize_vertices", "vkhr_voxelize_segments", "vkhr_normalize_densities", "vkhr_raymarch",
     "vkhr_launch_count", "vkhr_sizeof_aabb", "vkhr_sizeof_raymarch_params",
     "vkhr_set_profiling", "vkhr_profile_count", "vkhr_profile_read",
+    "vkhr_malloc", "vkhr_free", "vkhr_upload", "vkhr_download", "vkhr_sync",
 ]
 
 _lib = None
@@ -53,6 +54,11 @@ def load():
                                            C.c_int32, C.c_int32, P, P, P, P]
     lib.vkhr_normalize_densities.argtypes = [P, P, C.c_uint64, P]
     lib.vkhr_raymarch.argtypes = [P, C.POINTER(_abi.RaymarchParams), P, P, P, P, P, P]
+    lib.vkhr_malloc.argtypes = [P, C.c_size_t, C.POINTER(C.c_void_p)]
+    lib.vkhr_free.argtypes = [P, P]
+    lib.vkhr_upload.argtypes = [P, P, P, C.c_size_t, P]
+    lib.vkhr_download.argtypes = [P, P, P, C.c_size_t, P]
+    lib.vkhr_sync.argtypes = [P, P]
     lib.vkhr_set_profiling.argtypes = [P, C.c_int]
     lib.vkhr_profile_count.argtypes = [P]
     lib.vkhr_profile_read.argtypes = [P, C.c_int, C.POINTER(C.c_char_p), C.POINTER(C.c_float)]

@@ -148,6 +148,50 @@ vkhr_status vkhr_destroy(vkhr_ctx* ctx)
     return VKHR_OK;
 }
 
+vkhr_status vkhr_malloc(vkhr_ctx* ctx, size_t bytes, void** out)
+{
+    if (!ctx || !out) return VKHR_ERR_INVALID_ARG;
+    *out = nullptr;
+    VKHR_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    VKHR_CUDA_TRY(ctx, cudaMalloc(out, bytes ? bytes : 1));
+    return VKHR_OK;
+}
+
+vkhr_status vkhr_free(vkhr_ctx* ctx, void* p)
+{
+    if (!ctx) return VKHR_ERR_INVALID_ARG;
+    if (!p) return VKHR_OK;
+    VKHR_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    VKHR_CUDA_TRY(ctx, cudaFree(p));
+    return VKHR_OK;
+}
+
+vkhr_status vkhr_upload(vkhr_ctx* ctx, void* dst, const void* src, size_t bytes, void* stream)
+{
+    if (!ctx || (bytes && (!dst || !src))) return VKHR_ERR_INVALID_ARG;
+    if (!bytes) return VKHR_OK;
+    VKHR_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    VKHR_CUDA_TRY(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, (cudaStream_t)stream));
+    return VKHR_OK;
+}
+
+vkhr_status vkhr_download(vkhr_ctx* ctx, void* dst, const void* src, size_t bytes, void* stream)
+{
+    if (!ctx || (bytes && (!dst || !src))) return VKHR_ERR_INVALID_ARG;
+    if (!bytes) return VKHR_OK;
+    VKHR_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    VKHR_CUDA_TRY(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    return VKHR_OK;
+}
+
+vkhr_status vkhr_sync(vkhr_ctx* ctx, void* stream)
+{
+    if (!ctx) return VKHR_ERR_INVALID_ARG;
+    VKHR_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    VKHR_CUDA_TRY(ctx, cudaStreamSynchronize((cudaStream_t)stream));
+    return VKHR_OK;
+}
+
 uint64_t vkhr_launch_count(const vkhr_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
 size_t vkhr_sizeof_aabb(void) { return sizeof(vkhr_aabb); }
