@@ -31,13 +31,8 @@ def build(with_reference=None):
         subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
 
 
-class PixelDiag(C.Structure):
-    _fields_ = [("iso_margin", C.c_double), ("tangent_len", C.c_double), ("steps_taken", C.c_int32),
-                ("covered", C.c_int32)]
-
-
-DIAG_DTYPE = np.dtype([("iso_margin", np.float64), ("tangent_len", np.float64), ("steps_taken", np.int32),
-                       ("covered", np.int32)])
+DIAG_DTYPE = np.dtype([("iso_margin", np.float64), ("support_margin", np.float64), ("tangent_len", np.float64),
+                       ("steps_taken", np.int32), ("covered", np.int32)])
 
 P = C.c_void_p
 

@@ -87,6 +87,48 @@ static inline int SFX(tex_setup)(const SFX(vol)* v, SFX(vec3) P, long i0[3], REA
     return 1;
 }
 
+/* Distance, in texels, from sample P to the boundary where the shader's
+ * `density != 0.0` test flips.  A texel j carries nonzero trilinear weight
+ * iff max_k |j_k - u_k| < 1 (u = texel-space position).  For a nonzero
+ * sample the margin is the largest, over its nonzero taps, of min_k(1 - |j_k - u_k|);
+ * for a zero sample it is the smallest, over nonzero texels of the 4^3
+ * neighbourhood, of max_k |j_k - u_k| - 1 (capped at 1).  Test-side only. */
+static double SFX(support_margin)(const SFX(vol)* v, SFX(vec3) P)
+{
+    long i0[3];
+    REAL a[3];
+    if (!SFX(tex_setup)(v, P, i0, a)) return 1.0;
+    double best_nz = -1.0;
+    for (int dz = 0; dz < 2; ++dz)
+        for (int dy = 0; dy < 2; ++dy)
+            for (int dx = 0; dx < 2; ++dx) {
+                if (SFX(texel_density)(v, i0[0] + dx, i0[1] + dy, i0[2] + dz) == (REAL)0) continue;
+                double wx = dx ? (double)a[0] : 1.0 - (double)a[0];
+                double wy = dy ? (double)a[1] : 1.0 - (double)a[1];
+                double wz = dz ? (double)a[2] : 1.0 - (double)a[2];
+                double m = wx < wy ? wx : wy;
+                m = m < wz ? m : wz;
+                if (m > best_nz) best_nz = m;
+            }
+    if (best_nz >= 0.0) return best_nz; /* weight 0 on every nonzero tap still counts as zero */
+    double best = 1.0;
+    for (int ez = -1; ez <= 2; ++ez)
+        for (int ey = -1; ey <= 2; ++ey)
+            for (int ex = -1; ex <= 2; ++ex) {
+                const int e[3] = {ex, ey, ez};
+                double dmax = 0.0;
+                for (int k = 0; k < 3; ++k) {
+                    double d = e[k] == -1 ? 1.0 + (double)a[k]
+                             : e[k] == 0 ? (double)a[k]
+                             : e[k] == 1 ? 1.0 - (double)a[k] : 2.0 - (double)a[k];
+                    if (d > dmax) dmax = d;
+                }
+                if (dmax - 1.0 >= best) continue;
+                if (SFX(texel_density)(v, i0[0] + ex, i0[1] + ey, i0[2] + ez) != (REAL)0) best = dmax - 1.0;
+            }
+    return best;
+}
+
 static REAL SFX(sample_density)(const SFX(vol)* v, SFX(vec3) P)
 {
     long i0[3];
@@ -128,8 +170,9 @@ static inline REAL SFX(clip_depth)(const REAL pv[16], SFX(vec3) P)
 /* volume_rendering.glsl:19-52 (volume_surface). */
 static void SFX(volume_surface)(const SFX(vol)* dv, const REAL pv[16], SFX(vec3) start, SFX(vec3) end,
                                 float steps, REAL iso, float depth_buffer, SFX(vec3)* surf_out,
-                                REAL* a_out, double* margin, int* taken)
+                                REAL* a_out, double* margin, int* taken, double* support_margin)
 {
+    double sm = 1.0 / 0.0;
     REAL acc = 0;
     float step_size = 1.0f / steps;
     SFX(vec3) surface_point = SFX(v3)(0, 0, 0);
@@ -143,6 +186,12 @@ static void SFX(volume_surface)(const SFX(vol)* dv, const REAL pv[16], SFX(vec3)
         if ((REAL)depth_buffer < depth) break;
         ++k;
         REAL density = SFX(sample_density)(dv, P);
+        /* before the surface point freezes, a sample's zero/nonzero status
+         * decides the entry and surface points */
+        if (support_margin && !(acc > iso)) {
+            double sup = SFX(support_margin)(dv, P);
+            if (sup < sm) sm = sup;
+        }
         acc += density;
         if (density != (REAL)0) {
             double dm = fabs((double)acc - (double)iso) / (double)iso;
@@ -160,6 +209,7 @@ static void SFX(volume_surface)(const SFX(vol)* dv, const REAL pv[16], SFX(vec3)
     *a_out = acc / iso;
     if (margin) *margin = m;
     if (taken) *taken = k;
+    if (support_margin) *support_margin = sm;
 }
 
 /* kajiya-kay.glsl:7-24; `kd` scales the diffuse term (1 = reference). */
@@ -236,11 +286,16 @@ static void SFX(shade_pixel)(const vkhr_raymarch_params* p, const SFX(vol)* dv, 
 
     SFX(vec3) surf;
     REAL a;
-    double margin;
+    double margin, support;
     int taken;
     SFX(volume_surface)(dv, pv, start, end, p->raycast_steps, (REAL)p->isosurface, depth_buffer, &surf, &a,
-                        &margin, &taken);
-    if (diag) { diag->iso_margin = margin; diag->steps_taken = taken; diag->tangent_len = 0; }
+                        &margin, &taken, diag ? &support : NULL);
+    if (diag) {
+        diag->iso_margin = margin;
+        diag->steps_taken = taken;
+        diag->tangent_len = 0;
+        diag->support_margin = support;
+    }
     rgba[0] = rgba[1] = rgba[2] = rgba[3] = 0.0f;
     if (depth_out) *depth_out = 1.0f;
     if (a == (REAL)0) return; /* discard */
@@ -299,7 +354,13 @@ static void SFX(raymarch_rows)(const vkhr_raymarch_params* p, const void* densit
             size_t at = (size_t)y * (size_t)W + (size_t)x;
             double st[3];
             oracle_pixel_diag* dg = diag ? diag + at : NULL;
-            if (dg) { dg->iso_margin = 1.0 / 0.0; dg->tangent_len = 0; dg->steps_taken = 0; dg->covered = 0; }
+            if (dg) {
+                dg->iso_margin = 1.0 / 0.0;
+                dg->support_margin = 1.0 / 0.0;
+                dg->tangent_len = 0;
+                dg->steps_taken = 0;
+                dg->covered = 0;
+            }
             if (!invertible || !oracle_pixel_entry_inv(p, inv, x, y, st)) {
                 rgba[4 * at + 0] = rgba[4 * at + 1] = rgba[4 * at + 2] = rgba[4 * at + 3] = 0.0f;
                 if (depth_out) depth_out[at] = 1.0f;

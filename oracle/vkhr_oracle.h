@@ -64,6 +64,9 @@ int oracle_pixel_entry_inv(const vkhr_raymarch_params* p, const double inv[16], 
 /* Per-pixel diagnostics of the FP64 raymarch. */
 typedef struct oracle_pixel_diag {
     double iso_margin;   /* min over nonzero samples of |acc - iso| / iso (inf if none) */
+    double support_margin; /* min over samples taken before the surface froze of their
+                              distance in texels to flipping `density != 0` (see
+                              support_margin in raymarch_body.h; inf if none)          */
     double tangent_len;  /* length of the sampled tangent before normalisation         */
     int32_t steps_taken; /* primary-loop iterations executed                          */
     int32_t covered;     /* 1 if the pixel spawned a ray                              */

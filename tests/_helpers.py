@@ -45,14 +45,23 @@ def gpu_voxelize(ctx, mode, vertices, tangents, indices, bounds, res, index_mode
             None if tq is None else tq.cpu().numpy())
 
 
-def image_errors(gpu, ref, diag, margin=1e-4, tangent_floor=1e-4):
-    """Per-channel RMS and max over well-conditioned pixels + the excluded count.
-
-    A pixel is ill-conditioned when its isosurface decision is within
-    `margin` (relative) of the threshold, or its surface tangent sample is
-    shorter than `tangent_floor` (normalisation amplifies rounding)."""
+def ill_conditioned(ref, diag, margin=1e-4, support=2e-4, tangent_floor=1e-4):
+    """Pixels whose shader result hinges on a decision FP32 cannot resolve:
+    the isosurface test within `margin` (relative) of the threshold, a
+    `density != 0` test on a sample whose nonzero taps carry less than
+    `support` trilinear weight (about FP32's position resolution in texels),
+    or a surface tangent shorter than `tangent_floor` (normalisation
+    amplifies rounding)."""
     emitted = ref[..., 3] > 0
-    ill = (diag["iso_margin"] < margin) | (emitted & (diag["tangent_len"] < tangent_floor) & (diag["tangent_len"] > 0))
+    return ((diag["iso_margin"] < margin) | (diag["support_margin"] < support)
+            | (emitted & (diag["tangent_len"] < tangent_floor) & (diag["tangent_len"] > 0)))
+
+
+def image_errors(gpu, ref, diag, **kw):
+    """Per-channel RMS and max over well-conditioned pixels, the excluded
+    count and the emitted-fragment count."""
+    emitted = ref[..., 3] > 0
+    ill = ill_conditioned(ref, diag, **kw)
     ok = ~ill
     d = np.abs(gpu.astype(np.float64) - ref.astype(np.float64))
     rms = np.sqrt((d[ok] ** 2).mean(axis=0)) if ok.any() else np.zeros(4)

@@ -2,10 +2,11 @@
 transcription of volume.frag.
 
 Tolerance (per channel, over well-conditioned pixels): RMS <= 1e-3 and
-max |diff| <= 2e-2.  A pixel is excluded only when its isosurface decision
-lies within 1e-4 (relative) of the threshold or its surface tangent sample
-is shorter than 1e-4; excluded pixels are counted and must stay below 0.5%
-of the emitted fragments.
+max |diff| <= 2e-2.  A pixel is excluded only when its result hinges on a
+decision FP32 cannot resolve (tests/_helpers.py ill_conditioned): the
+isosurface test within 1e-4 (relative) of the threshold, a `density != 0`
+test within 2e-4 texel of flipping, or a surface tangent shorter than 1e-4.
+Excluded pixels are counted and must stay below 1% of the emitted fragments.
 """
 import numpy as np
 import pytest
@@ -46,7 +47,7 @@ def _compare(gpu, gdepth, ref, rdepth, diag, rows=None):
         ref, rdepth, diag = ref[rows[0]:rows[1]], rdepth[rows[0]:rows[1]], diag[rows[0]:rows[1]]
     rms, mx, excluded, emitted = image_errors(gpu, ref, diag)
     assert emitted > 0
-    assert excluded <= max(2, 0.005 * emitted), (excluded, emitted)
+    assert excluded <= max(2, 0.01 * emitted), (excluded, emitted)
     assert np.all(rms <= RMS_TOL), rms
     assert np.all(mx <= MAX_TOL), mx
     ok = (diag["iso_margin"] >= 1e-4)

@@ -38,6 +38,8 @@ struct vkhr_ctx {
     size_t list_cap;           // in elements
     uint32_t* heavy;           // voxel ids routed to the heavy resolve
     size_t heavy_cap;          // in elements
+    uint32_t* occ;             // raymarch brick-occupancy bitmap
+    size_t occ_cap;            // in 32-bit words
     unsigned long long* d_words;
     unsigned long long* h_words; // pinned mirror
     cudaEvent_t ev;

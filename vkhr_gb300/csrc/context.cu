@@ -136,6 +136,7 @@ vkhr_status vkhr_destroy(vkhr_ctx* ctx)
     if (ctx->cursor) cudaFree(ctx->cursor);
     if (ctx->list) cudaFree(ctx->list);
     if (ctx->heavy) cudaFree(ctx->heavy);
+    if (ctx->occ) cudaFree(ctx->occ);
     if (ctx->d_words) cudaFree(ctx->d_words);
     if (ctx->h_words) cudaFreeHost(ctx->h_words);
     if (ctx->ev) cudaEventDestroy(ctx->ev);

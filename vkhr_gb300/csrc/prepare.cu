@@ -75,28 +75,40 @@ __global__ void aabb_finish_kernel(const int* mm, vkhr_aabb* out)
     out->volume = __fmul_rn(__fmul_rn(s[0], s[1]), s[2]);
 }
 
-// generate_tangents (hair_style.cc:171-194): one thread per strand; tangent =
-// d * (1 / sqrt(dot(d, d))) (glm::normalize), last vertex repeats the previous.
+// generate_tangents (hair_style.cc:171-194), pass 1: one thread per strand
+// writes its segment tangents d * (1 / sqrt(dot(d, d))) (glm::normalize).
 __global__ void tangents_kernel(const float* __restrict__ v, const uint32_t* __restrict__ first_vertex,
                                 const uint16_t* __restrict__ segs, uint32_t strands, float* t)
 {
     for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < strands; s += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t v0 = first_vertex[s];
         const uint32_t n = segs[s];
-        float last[3] = {0.0f, 0.0f, 0.0f};
         for (uint32_t k = 0; k < n; ++k) {
             float d[3];
             for (int a = 0; a < 3; ++a) d[a] = __fsub_rn(v[3 * (v0 + k + 1) + a], v[3 * (v0 + k) + a]);
             float dot = __fadd_rn(__fadd_rn(__fmul_rn(d[0], d[0]), __fmul_rn(d[1], d[1])), __fmul_rn(d[2], d[2]));
             float inv = __fdiv_rn(1.0f, __fsqrt_rn(dot));
-            for (int a = 0; a < 3; ++a) {
-                last[a] = __fmul_rn(d[a], inv);
-                t[3 * (v0 + k) + a] = last[a];
-            }
+            for (int a = 0; a < 3; ++a) t[3 * (v0 + k) + a] = __fmul_rn(d[a], inv);
         }
-        if (n == 0 && v0 > 0) // tangents.back() is the previous strand's last tangent
-            for (int a = 0; a < 3; ++a) last[a] = t[3 * (v0 - 1) + a];
-        for (int a = 0; a < 3; ++a) t[3 * (v0 + n) + a] = last[a];
+    }
+}
+
+// Pass 2: a strand's last vertex repeats tangents.back(), the tangent of the
+// vertex before it: its own last segment's, or, for a strand without
+// segments, the previous strand's last vertex (followed back across
+// consecutive segment-less strands; 0 before the first segment).
+__global__ void tangents_last_kernel(const uint32_t* __restrict__ first_vertex, const uint16_t* __restrict__ segs,
+                                     uint32_t strands, float* t)
+{
+    for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < strands; s += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t last = (uint64_t)first_vertex[s] + segs[s];
+        int64_t src = -1;
+        for (int64_t q = (int64_t)s; q >= 0; --q)
+            if (segs[q] > 0) {
+                src = (int64_t)first_vertex[q] + segs[q] - 1;
+                break;
+            }
+        for (int a = 0; a < 3; ++a) t[3 * last + a] = src >= 0 ? t[3 * src + a] : 0.0f;
     }
 }
 
@@ -180,8 +192,9 @@ vkhr_status vkhr_generate_tangents(vkhr_ctx* ctx, const float* d_vertices, const
     uint64_t verts = 0;
     vkhr_status s = upload_strands(ctx, h_segments, strand_count, st, &segs, &first, &verts);
     if (s == VKHR_OK) {
-        VKHR_LAUNCH(ctx, tangents_kernel, std::min(vkhr_blocks(strand_count, 128), (unsigned)ctx->sm_count * 16),
-                    128, 0, st, d_vertices, first, segs, strand_count, d_tangents);
+        const unsigned blocks = std::min(vkhr_blocks(strand_count, 128), (unsigned)ctx->sm_count * 16);
+        VKHR_LAUNCH(ctx, tangents_kernel, blocks, 128, 0, st, d_vertices, first, segs, strand_count, d_tangents);
+        VKHR_LAUNCH(ctx, tangents_last_kernel, blocks, 128, 0, st, first, segs, strand_count, d_tangents);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) s = vkhr_fail_cuda(ctx, e, "tangents_kernel", __FILE__, __LINE__);
     }

@@ -41,7 +41,12 @@ struct RayConsts {
     float steps, shadow_steps, thickness, ao_kernel, ao_radius, ao_exp, ao_max;
     float lod;
     int shading_model, deep_shadows_on;
+    int steps_pow2, shadow_pow2;  // 1/steps is exact and t = i * step: empty space may be jumped
+    int nb[3];                    // occupancy bricks per axis, (res + 8) / 8
 };
+
+constexpr int kBrick = 8;          // occupancy brick edge in texel cells
+constexpr float kSkipMargin = 0.01f; // texels kept between a predicted sample and a brick face
 
 template <int DF>
 struct DensityTexel;
@@ -174,11 +179,99 @@ __device__ Vec3 sample_tangent(const RayConsts& c, const void* t, Vec3 p)
     return acc;
 }
 
+// Occupancy of the texel-cell grid.  A sample with lower tap i0 = floor(u)
+// (u = s * N - 0.5 per axis) reads texels i0 and i0 + 1; shifting to
+// cell = i0 + 1 in [0, N], brick k covers cells [8k, 8k + 8), i.e. texels
+// [8k - 1, 8k + 7].  A brick is occupied when any of those texels is nonzero;
+// every sample whose cell lies in an empty brick is exactly 0.  One warp per brick.
+template <int DF>
+__global__ void occupancy_kernel(const typename DensityTexel<DF>::T* __restrict__ d, int nx, int ny, int nz, int bx,
+                                 int by, int bz, uint32_t* __restrict__ bits)
+{
+    typedef DensityTexel<DF> TX;
+    const int lane = threadIdx.x & 31;
+    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    const uint64_t total = (uint64_t)bx * by * bz;
+    for (uint64_t b = blockIdx.x * (uint64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); b < total; b += warps) {
+        const int kx = (int)(b % bx), ky = (int)((b / bx) % by), kz = (int)(b / ((uint64_t)bx * by));
+        bool nz_found = false;
+        for (int i = lane; i < (kBrick + 1) * (kBrick + 1) * (kBrick + 1) && !nz_found; i += 32) {
+            const int x = kBrick * kx - 1 + i % (kBrick + 1);
+            const int y = kBrick * ky - 1 + (i / (kBrick + 1)) % (kBrick + 1);
+            const int z = kBrick * kz - 1 + i / ((kBrick + 1) * (kBrick + 1));
+            if (x >= 0 && y >= 0 && z >= 0 && x < nx && y < ny && z < nz)
+                nz_found = TX::load(d, (size_t)x + (size_t)nx * ((size_t)y + (size_t)ny * z)) != 0.0f;
+        }
+        if (__any_sync(0xffffffffu, nz_found) && lane == 0) atomicOr(bits + (b >> 5), 1u << (b & 31));
+    }
+}
+
+// Classifies one sample position (texel coordinates u).  Returns 1 when the
+// sample is exactly zero (border, or an empty brick), 2 when it is zero and
+// the ray has left the grid for good (moving away along every such axis),
+// 0 when it must be sampled.  box_lo/box_hi receive the current brick's
+// texel-coordinate extent for the empty-space jump.
+__device__ __forceinline__ int classify(const RayConsts& c, const uint32_t* __restrict__ occ, const float u[3],
+                                        const float du[3], float box_lo[3], float box_hi[3])
+{
+    int cell[3];
+    bool outside = false, leaving = false;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float f = floorf(u[k]);
+        if (!(f >= -1.0f && f <= (float)(c.res[k] - 1))) {
+            outside = true;
+            if ((u[k] < -1.0f - kSkipMargin && du[k] <= 0.0f) || (u[k] > (float)c.res[k] + kSkipMargin && du[k] >= 0.0f) ||
+                !(u[k] == u[k]))
+                leaving = true;
+            cell[k] = 0;
+        } else {
+            cell[k] = (int)f + 1;
+        }
+    }
+    if (outside) { // zero, but no brick to jump across: step singly
+#pragma unroll
+        for (int k = 0; k < 3; ++k) box_lo[k] = box_hi[k] = u[k];
+        return leaving ? 2 : 1;
+    }
+    const int bxk = cell[0] / kBrick, byk = cell[1] / kBrick, bzk = cell[2] / kBrick;
+    const uint32_t b = (uint32_t)bxk + (uint32_t)c.nb[0] * ((uint32_t)byk + (uint32_t)c.nb[1] * (uint32_t)bzk);
+    if (__ldg(occ + (b >> 5)) & (1u << (b & 31))) return 0;
+    box_lo[0] = (float)(kBrick * bxk - 1);
+    box_lo[1] = (float)(kBrick * byk - 1);
+    box_lo[2] = (float)(kBrick * bzk - 1);
+    box_hi[0] = box_lo[0] + (float)kBrick;
+    box_hi[1] = box_lo[1] + (float)kBrick;
+    box_hi[2] = box_lo[2] + (float)kBrick;
+    return 1;
+}
+
+// Whole steps that stay inside the empty brick [lo, hi) from u along du
+// (per unit t), keeping kSkipMargin texels from its faces.
+__device__ __forceinline__ float steps_inside(const float u[3], const float du[3], const float lo[3], const float hi[3],
+                                              float step)
+{
+    float te = INFINITY;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        if (du[k] > 0.0f) te = fminf(te, (hi[k] - kSkipMargin - u[k]) / du[k]);
+        else if (du[k] < 0.0f) te = fminf(te, (lo[k] + kSkipMargin - u[k]) / du[k]);
+    }
+    return floorf(te / step);
+}
+
+__device__ __forceinline__ void texel_coords(const RayConsts& c, Vec3 p, float u[3])
+{
+    u[0] = fmaf(p.x, c.tsc[0], c.tbias[0]);
+    u[1] = fmaf(p.y, c.tsc[1], c.tbias[1]);
+    u[2] = fmaf(p.z, c.tsc[2], c.tbias[2]);
+}
+
 template <int DF, int TF>
 __global__ void __launch_bounds__(32 * kWarpsX * kWarpsY)
 raymarch_kernel(const __grid_constant__ RayConsts c, const typename DensityTexel<DF>::T* __restrict__ dens,
-                const void* __restrict__ tang, const float* __restrict__ depth_in, float4* __restrict__ rgba,
-                float* __restrict__ depth_out)
+                const void* __restrict__ tang, const uint32_t* __restrict__ occ, const float* __restrict__ depth_in,
+                float4* __restrict__ rgba, float* __restrict__ depth_out)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int px = (blockIdx.x * kWarpsX + (warp % kWarpsX)) * kTileW + (lane % kTileW);
@@ -216,12 +309,28 @@ raymarch_kernel(const __grid_constant__ RayConsts c, const typename DensityTexel
 
         // ---- volume_surface (volume_rendering.glsl:19-52) --------------------
         const float step = 1.0f / c.steps;
+        const bool jump = c.steps_pow2 && !depth_test;
+        float us[3], ue[3], du[3];
+        texel_coords(c, start, us);
+        texel_coords(c, end, ue);
+        du[0] = ue[0] - us[0];
+        du[1] = ue[1] - us[1];
+        du[2] = ue[2] - us[2];
         float acc = 0.0f;
         Vec3 surf = v3(0.0f, 0.0f, 0.0f), entry = v3(0.0f, 0.0f, 0.0f);
         bool found = false, entered = false;
-        for (float t = 0.0f; t < 1.0f; t += step) {
+        for (float t = 0.0f; t < 1.0f;) {
             const Vec3 P = mix(start, end, t);
             if (depth_test && db < clip_depth(c, P)) break;
+            float u[3], lo[3], hi[3];
+            texel_coords(c, P, u);
+            const int z = classify(c, occ, u, du, lo, hi);
+            if (z == 2) break; // left the grid: every later sample adds exactly 0
+            if (z == 1) {      // exactly 0: acc and the decisions are unchanged
+                const float n = jump ? steps_inside(u, du, lo, hi, step) : 0.0f;
+                t = n >= 1.0f ? fmaf(n, step, t) : t + step;
+                continue;
+            }
             const float rho = sample_density<DF>(c, dens, P);
             acc += rho;
             if (rho != 0.0f) {
@@ -230,6 +339,7 @@ raymarch_kernel(const __grid_constant__ RayConsts c, const typename DensityTexel
                 if (!entered) { entry = P; entered = true; }
                 if (acc > c.iso && c.lod * (acc / c.iso) * c.alpha >= 1.0f) break; // outputs final
             }
+            t += step;
         }
         if (!found && entered) surf = entry;
         const float a = acc / c.iso;
@@ -254,9 +364,27 @@ raymarch_kernel(const __grid_constant__ RayConsts c, const typename DensityTexel
             // ---- volume_approximated_deep_shadows (approximate_deep_shadows.glsl:24-36)
             if (c.deep_shadows_on == 1 && c.shading_model != VKHR_SHADING_LAO) {
                 const float sstep = 1.0f / c.shadow_steps;
+                float ls[3], le[3], dl[3];
+                texel_coords(c, surf, ls);
+                texel_coords(c, light, le);
+                dl[0] = le[0] - ls[0];
+                dl[1] = le[1] - ls[1];
+                dl[2] = le[2] - ls[2];
                 float strands = 0.0f;
-                for (float t = 0.0f; t < 1.0f; t += sstep)
-                    strands += sample_density<DF>(c, dens, mix(surf, light, t)) * c.thickness;
+                for (float t = 0.0f; t < 1.0f;) {
+                    const Vec3 Q = mix(surf, light, t);
+                    float u[3], lo[3], hi[3];
+                    texel_coords(c, Q, u);
+                    const int z = classify(c, occ, u, dl, lo, hi);
+                    if (z == 2) break;
+                    if (z == 1) {
+                        const float n = c.shadow_pow2 ? steps_inside(u, dl, lo, hi, sstep) : 0.0f;
+                        t = n >= 1.0f ? fmaf(n, sstep, t) : t + sstep;
+                        continue;
+                    }
+                    strands += sample_density<DF>(c, dens, Q) * c.thickness;
+                    t += sstep;
+                }
                 occlusion *= powf(1.0f - c.alpha, strands);
             }
             // ---- local_ambient_occlusion (local_ambient_occlusion.glsl:9-30)
@@ -377,17 +505,33 @@ vkhr_status make_consts(vkhr_ctx* ctx, const vkhr_raymarch_params* p, RayConsts&
     }
     c.shading_model = p->shading_model;
     c.deep_shadows_on = p->deep_shadows_on;
+    auto pow2 = [](float x) {
+        int e;
+        return std::frexp(x, &e) == 0.5f;
+    };
+    c.steps_pow2 = pow2(c.steps) ? 1 : 0;
+    c.shadow_pow2 = pow2(c.shadow_steps) ? 1 : 0;
+    for (int k = 0; k < 3; ++k) c.nb[k] = (c.res[k] + kBrick) / kBrick;
     return VKHR_OK;
 }
 
 template <int DF, int TF>
-void launch(vkhr_ctx* ctx, const RayConsts& c, const void* dens, const void* tang, const float* din, float* rgba,
-            float* dout, cudaStream_t st)
+vkhr_status launch(vkhr_ctx* ctx, const RayConsts& c, const void* dens, const void* tang, const float* din, float* rgba,
+                   float* dout, cudaStream_t st)
 {
+    const size_t bricks = (size_t)c.nb[0] * c.nb[1] * c.nb[2];
+    const size_t words = (bricks + 31) / 32;
+    vkhr_status s = vkhr_reserve(ctx, (void**)&ctx->occ, &ctx->occ_cap, words, sizeof(uint32_t));
+    if (s != VKHR_OK) return s;
+    VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->occ, 0, words * sizeof(uint32_t), st));
+    const unsigned oblocks = (unsigned)std::min<size_t>((bricks + 7) / 8, (size_t)ctx->sm_count * 32);
+    VKHR_LAUNCH(ctx, occupancy_kernel<DF>, oblocks, 256, 0, st, (const typename DensityTexel<DF>::T*)dens, c.res[0],
+                c.res[1], c.res[2], c.nb[0], c.nb[1], c.nb[2], ctx->occ);
     const dim3 block(32 * kWarpsX * kWarpsY);
     const dim3 grid((c.W + kTileW * kWarpsX - 1) / (kTileW * kWarpsX), (c.H + kTileH * kWarpsY - 1) / (kTileH * kWarpsY));
     VKHR_LAUNCH(ctx, (raymarch_kernel<DF, TF>), grid, block, 0, st, c, (const typename DensityTexel<DF>::T*)dens, tang,
-                din, reinterpret_cast<float4*>(rgba), dout);
+                ctx->occ, din, reinterpret_cast<float4*>(rgba), dout);
+    return VKHR_OK;
 }
 
 } // namespace
@@ -410,17 +554,17 @@ extern "C" vkhr_status vkhr_raymarch(vkhr_ctx* ctx, const vkhr_raymarch_params* 
     cudaStream_t st = (cudaStream_t)stream;
     const int df = params->density_format, tf = params->tangent_format;
     if (df == VKHR_DENSITY_U8_UNORM && tf == VKHR_TANGENT_I8_SNORM)
-        launch<VKHR_DENSITY_U8_UNORM, VKHR_TANGENT_I8_SNORM>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
+        s = launch<VKHR_DENSITY_U8_UNORM, VKHR_TANGENT_I8_SNORM>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
     else if (df == VKHR_DENSITY_U8_UNORM)
-        launch<VKHR_DENSITY_U8_UNORM, VKHR_TANGENT_F32X4>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
+        s = launch<VKHR_DENSITY_U8_UNORM, VKHR_TANGENT_F32X4>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
     else if (df == VKHR_DENSITY_U32_COUNT && tf == VKHR_TANGENT_I8_SNORM)
-        launch<VKHR_DENSITY_U32_COUNT, VKHR_TANGENT_I8_SNORM>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
+        s = launch<VKHR_DENSITY_U32_COUNT, VKHR_TANGENT_I8_SNORM>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
     else if (df == VKHR_DENSITY_U32_COUNT)
-        launch<VKHR_DENSITY_U32_COUNT, VKHR_TANGENT_F32X4>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
+        s = launch<VKHR_DENSITY_U32_COUNT, VKHR_TANGENT_F32X4>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
     else if (tf == VKHR_TANGENT_I8_SNORM)
-        launch<VKHR_DENSITY_F32, VKHR_TANGENT_I8_SNORM>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
+        s = launch<VKHR_DENSITY_F32, VKHR_TANGENT_I8_SNORM>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
     else
-        launch<VKHR_DENSITY_F32, VKHR_TANGENT_F32X4>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
+        s = launch<VKHR_DENSITY_F32, VKHR_TANGENT_F32X4>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
     VKHR_CUDA_TRY(ctx, cudaGetLastError());
     return VKHR_OK;
 }

@@ -490,9 +490,9 @@ vkhr_status voxelize_impl(vkhr_ctx* ctx, bool segments, const float* v, const fl
     vkhr_status s = make_grid(ctx, bounds, w, h, d, mode, g);
     if (s != VKHR_OK) return s;
     if (!counts) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_counts is NULL");
-    if (tq && !tan_in) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_tangents requested without d_tangent_in");
     if (n_items >= (1ull << 32)) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "more than 2^32 - 1 vertices or pairs");
     const uint32_t n_in = (uint32_t)n_items; // vertices, or index pairs
+    if (tq && !tan_in && n_in) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_tangents requested without d_tangent_in");
     if (n_in && !v) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_vertices is NULL");
     if (segments && n_in && !idx) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_indices is NULL");
     if (segments && idx && (reinterpret_cast<uintptr_t>(idx) & 7u))
