@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from vkhr_gb300 import _abi, scene
-from tests._helpers import image_errors, style, to_dev
+from tests._helpers import ill_conditioned, image_errors, style, to_dev
 
 pytestmark = pytest.mark.gpu
 
@@ -50,11 +50,12 @@ def _compare(gpu, gdepth, ref, rdepth, diag, rows=None):
     assert excluded <= max(2, 0.01 * emitted), (excluded, emitted)
     assert np.all(rms <= RMS_TOL), rms
     assert np.all(mx <= MAX_TOL), mx
-    ok = (diag["iso_margin"] >= 1e-4)
+    ok = ~ill_conditioned(ref, diag)
     dd = np.abs(gdepth - rdepth)
     bad = np.argwhere(ok & (dd > 1e-4))
-    info = [(int(y), int(x), float(diag["iso_margin"][y, x]), float(diag["tangent_len"][y, x]), float(rdepth[y, x]),
-             float(gdepth[y, x]), ref[y, x].tolist(), gpu[y, x].tolist()) for y, x in bad[:8]]
+    info = [(int(y), int(x), float(diag["iso_margin"][y, x]), float(diag["support_margin"][y, x]),
+             float(diag["tangent_len"][y, x]), float(rdepth[y, x]), float(gdepth[y, x]), ref[y, x].tolist(),
+             gpu[y, x].tolist()) for y, x in bad[:8]]
     assert len(bad) == 0, info
     return rms, mx
 
