@@ -221,10 +221,15 @@ vkhr_status vkhr_voxelize_segments(vkhr_ctx* ctx, const float* d_vertices, const
                                    uint32_t* d_counts, uint8_t* d_densities, int8_t* d_tangents,
                                    void* stream);
 
+/* Waits for the stream and reports errors that kernels recorded on the device
+ * since the last voxelization started (e.g. a capacity overflow). */
+vkhr_status vkhr_check_status(vkhr_ctx* ctx, void* stream);
+
 /* Replaces HairStyle::Volume::normalize (hair_style.cc:344-357): u8 min-max
  * rescale in place.  A constant volume (max == min) maps to 0, where the
  * reference divides by zero. */
 vkhr_status vkhr_normalize_densities(vkhr_ctx* ctx, uint8_t* d_densities, uint64_t voxel_count, void* stream);
+/* (d_densities must be 16-byte aligned, as cudaMalloc returns.) */
 
 /* ---- raymarch ---------------------------------------------------------------
  * Replaces the Vulkan draw of the volume proxy cube (volume.cc:104-112) and

@@ -40,6 +40,7 @@ def gpu_voxelize(ctx, mode, vertices, tangents, indices, bounds, res, index_mode
                                                                                                    device="cuda")
         ctx.voxelize_segments(p(dv), p(dt), p(di), int(len(indices)), bounds, res, index_mode, p(counts), p(dens),
                               p(tq), s)
+    ctx.check_status(s)  # errors the kernels recorded on the device
     torch.cuda.synchronize()
     return (counts.cpu().numpy().view(np.uint32), None if dens is None else dens.cpu().numpy(),
             None if tq is None else tq.cpu().numpy())

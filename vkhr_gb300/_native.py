@@ -16,7 +16,7 @@ EXPORTS = [
     "vkhr_voxelize_vertices", "vkhr_voxelize_segments", "vkhr_normalize_densities", "vkhr_raymarch",
     "vkhr_launch_count", "vkhr_sizeof_aabb", "vkhr_sizeof_raymarch_params",
     "vkhr_set_profiling", "vkhr_profile_count", "vkhr_profile_read",
-    "vkhr_malloc", "vkhr_free", "vkhr_upload", "vkhr_download", "vkhr_sync",
+    "vkhr_malloc", "vkhr_free", "vkhr_upload", "vkhr_download", "vkhr_sync", "vkhr_check_status",
 ]
 
 _lib = None
@@ -53,6 +53,7 @@ def load():
     lib.vkhr_voxelize_segments.argtypes = [P, P, P, P, C.c_uint64, C.POINTER(_abi.AABB), C.c_int32, C.c_int32,
                                            C.c_int32, C.c_int32, P, P, P, P]
     lib.vkhr_normalize_densities.argtypes = [P, P, C.c_uint64, P]
+    lib.vkhr_check_status.argtypes = [P, P]
     lib.vkhr_raymarch.argtypes = [P, C.POINTER(_abi.RaymarchParams), P, P, P, P, P, P]
     lib.vkhr_malloc.argtypes = [P, C.c_size_t, C.POINTER(C.c_void_p)]
     lib.vkhr_free.argtypes = [P, P]
@@ -142,6 +143,9 @@ class Context:
         self.check(self.lib.vkhr_voxelize_segments(self.handle, d_vertices, d_tangent_in, d_indices, index_count,
                                                    C.byref(bounds), w, h, d, index_mode, d_counts, d_densities,
                                                    d_tangents, stream))
+
+    def check_status(self, stream=None):
+        self.check(self.lib.vkhr_check_status(self.handle, stream))
 
     def normalize_densities(self, d_densities, n, stream=None):
         self.check(self.lib.vkhr_normalize_densities(self.handle, d_densities, n, stream))

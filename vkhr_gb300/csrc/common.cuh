@@ -15,29 +15,45 @@ enum : unsigned {
     VKHR_DEV_STEPS_OVERFLOW = 1u,   // a segment spans >= 2^24 voxels (the reference never terminates)
     VKHR_DEV_LIST_OVERFLOW = 2u,    // fixed-capacity visit list too small
     VKHR_DEV_TIMEOUT = 4u,          // a bounded device wait gave up
+    VKHR_DEV_REPLAY_MISMATCH = 8u,  // a brick replay disagreed with its binning (internal error)
 };
 
 // Slots of the small device word array every context owns.
 enum {
-    WORD_TOTAL_VISITS = 0,   // visits counted by the count pass
-    WORD_LIST_CURSOR = 1,    // allocation cursor of the visit list
-    WORD_HEAVY_COUNT = 2,    // voxels routed to the heavy resolve
-    WORD_STATUS = 3,         // VKHR_DEV_* bits
-    WORD_MEDIUM_COUNT = 4,   // voxels routed to the medium resolve
-    WORD_AABB = 5,           // bounding-box / normalize scratch (8 slots)
-    WORD_COUNT = 16
+    WORD_TOTAL_VISITS = 0,      // voxel visits of the current voxelization
+    WORD_LIST_CURSOR = 1,       // global path: allocation cursor of the visit list
+    WORD_HEAVY_COUNT = 2,       // global path: crowded-voxel descriptors
+    WORD_STATUS = 3,            // VKHR_DEV_* bits
+    WORD_RUNS_TOTAL = 4,        // brick path: run items
+    WORD_MAX_BRICK_VISITS = 5,  // brick path: largest brick
+    WORD_BHEAVY_COUNT = 6,      // brick path: crowded-voxel descriptors
+    WORD_HKEYS_CURSOR = 7,      // brick path: crowded-voxel key buffer cursor
+    WORD_BRICK_QUEUE = 8,       // brick path: next brick to resolve
+    WORD_NORM = 9,              // normalize: min, max (2 slots); words below are cleared per voxelization
+    WORD_AABB = 11,             // bounding-box scratch (8 slots)
+    WORD_COUNT = 24
 };
 
 struct vkhr_ctx {
     int device;
     int sm_count;
-    // grow-only scratch
-    uint32_t* cursor;          // per-voxel list cursor (u32 x voxels)
-    size_t cursor_cap;         // in elements
-    uint32_t* list;            // visit keys
-    size_t list_cap;           // in elements
-    uint32_t* heavy;           // voxel ids routed to the heavy resolve
-    size_t heavy_cap;          // in elements
+    // grow-only scratch (capacities in elements)
+    uint32_t* brick_runs;      // voxelizer: runs, visits and run-list cursor per brick (3 x bricks)
+    uint32_t* brick_visits;
+    uint32_t* brick_cursor;
+    size_t brick_cap;
+    uint2* items;              // voxelizer: run items (pair or vertex, first step << 8 | length)
+    size_t items_cap;
+    uint32_t* hkeys;           // voxelizer: keys of crowded voxels
+    size_t hkeys_cap;
+    uint4* hdesc;              // voxelizer: crowded voxels (voxel, key offset, count)
+    size_t hdesc_cap;
+    uint32_t* cursor;          // global path: per-voxel list cursor
+    size_t cursor_cap;
+    uint32_t* list;            // global path: visit keys
+    size_t list_cap;
+    uint4* gdesc;              // global path: crowded voxels
+    size_t gdesc_cap;
     uint32_t* occ;             // raymarch brick-occupancy bitmap
     size_t occ_cap;            // in 32-bit words
     unsigned long long* d_words;

@@ -133,9 +133,9 @@ vkhr_status vkhr_destroy(vkhr_ctx* ctx)
     if (!ctx) return VKHR_OK;
     cudaSetDevice(ctx->device);
     cudaDeviceSynchronize();
-    if (ctx->cursor) cudaFree(ctx->cursor);
-    if (ctx->list) cudaFree(ctx->list);
-    if (ctx->heavy) cudaFree(ctx->heavy);
+    void* bufs[] = {ctx->brick_runs, ctx->items, ctx->hkeys, ctx->hdesc, ctx->cursor, ctx->list, ctx->gdesc};
+    for (void* b : bufs)
+        if (b) cudaFree(b);
     if (ctx->occ) cudaFree(ctx->occ);
     if (ctx->d_words) cudaFree(ctx->d_words);
     if (ctx->h_words) cudaFreeHost(ctx->h_words);

@@ -1,22 +1,32 @@
 // voxelize.cu -- strand-density voxelizer (vertex-count and segment modes).
 //
 // Bit-exact restatement of vkhr::HairStyle::voxelize_vertices / _segments
-// (src/vkhr/scene_graph/hair_style.cc:257-342) for GB300:
+// (src/vkhr/scene_graph/hair_style.cc:257-342) for GB300.  Every visit is
+// computed with the reference's FP32 operation sequence (IEEE division, no
+// FMA contraction, glm's min/max), so counts are exact; the int8 tangents
+// are bit-identical too because each voxel's tangents are summed in the
+// reference's serial order (ascending vertex index / index-pair number) and
+// only the first 255 visits count, as `if (densities[pos] != 255)` does.
 //
-//   1. count    one thread per vertex / index pair: the reference's FP32
-//               coordinate and stepping arithmetic (no contraction, IEEE
-//               division), red.global.add into uint32 counts;
-//   2. ranges   each voxel with visits gets a contiguous slice of a visit
-//               list (block-wide scan, one atomic per 4096 voxels);
-//   3. fill     the same visits again, each appends its serial key (vertex
-//               index, or index-pair number) to its voxel's slice;
-//   4. resolve  per voxel: u8 density = min(count, 255); the keys are sorted
-//               (register sorting network, or a shared-memory bitonic sort
-//               for crowded voxels), the first min(count, 255) tangents are
-//               summed in that order in FP32 and quantised.  This reproduces
-//               the reference's serial loop, its stop-at-255 rule and its
-//               float summation order exactly, so the int8 tangents are
-//               bit-identical too, independent of atomic ordering.
+// Brick path (every voxel whose 8^3 brick receives <= kBrickCap visits):
+//   1. bin (count)  one thread per vertex / index pair walks its visits and
+//                   splits them into runs of consecutive visits inside one
+//                   brick; warp-aggregated atomics count runs and visits per
+//                   brick (32K bricks at 256^3, hot in L2);
+//   2. bin ranges   each brick gets a slice of the run list;
+//   3. bin (fill)   the same walk again writes (pair, first step, length)
+//                   run items into the bricks' slices;
+//   4. brick        one CTA per brick replays its runs twice with the exact
+//                   stepping: counts per voxel in shared memory, then the
+//                   serial keys bucketed per voxel; each voxel's keys are
+//                   sorted in shared memory and its tangents summed in that
+//                   order; the brick's 512 counts, u8 densities and int8x4
+//                   tangents are written once;
+//   5. crowded      voxels with > 64 visits: one CTA each sorts its keys in
+//                   shared-memory tiles (carrying the 256 smallest forward).
+// Global path (only bricks above kBrickCap): per-voxel global atomics, a
+// visit list and the same ordered resolve; it runs before step 4 and only
+// when such a brick exists.
 #include "common.cuh"
 
 #include <algorithm>
@@ -24,12 +34,16 @@
 
 namespace {
 
-constexpr int kSmallSort = 16;     // voxels with <= this many visits resolve in the main pass
-constexpr int kMediumSort = 64;    // <= this many: one thread per voxel, 64-key register network
-constexpr int kHeavyTile = 2048;   // shared-memory sort tile of the heavy resolve
-constexpr int kKeep = 256;         // smallest keys carried between heavy tiles (>= 255)
+constexpr int kBrickThreads = 512;     // one thread per voxel of an 8^3 brick
+constexpr int kBrickCap = 24576;       // visits a brick resolves in shared memory
+constexpr int kBrickSmall = 64;        // <= this many visits: sorted by the voxel's thread
+constexpr int kSmallSort = 16;         // global path: register-network resolve
+constexpr int kMediumSort = 64;        // global path: 64-key register network
+constexpr int kHeavyTile = 2048;       // crowded voxels: shared-memory sort tile
+constexpr int kKeep = 256;             // smallest keys carried between tiles (>= 255)
 constexpr int kRangeThreads = 256;
 constexpr int kRangeItems = 16;
+constexpr uint32_t kNoBrick = 0xffffffffu;
 
 struct Grid {
     float org[3];
@@ -37,8 +51,16 @@ struct Grid {
     float rm1[3];  // resolution - 1.0f
     float fw, fh;  // (float)width, (float)height
     float fn;      // (float)(width * height * depth)
-    uint32_t w, h, n;
+    uint32_t w, h, d, n, wh;
+    uint32_t nbx, nby, nbz, nb; // bricks
     int mode;
+    int exact_coords; // the linear index always equals the clamped coordinates' exact index
+};
+
+struct Visit {
+    uint32_t lin;   // linear voxel index
+    uint32_t brick;
+    uint32_t local; // (x & 7) | (y & 7) << 3 | (z & 7) << 6
 };
 
 __device__ __forceinline__ bool linear_index(const Grid& g, float vx, float vy, float vz, uint32_t& out)
@@ -57,163 +79,200 @@ __device__ __forceinline__ bool linear_index(const Grid& g, float vx, float vy, 
     return true;
 }
 
+// Visit of the clamped voxel coordinate (vx, vy, vz): its linear index as the
+// reference forms it, and the brick/local position of that index.
+__device__ __forceinline__ bool locate(const Grid& g, float vx, float vy, float vz, Visit& o)
+{
+    if (!linear_index(g, vx, vy, vz, o.lin)) return false;
+    uint32_t x, y, z;
+    if (g.exact_coords && vx >= 0.0f && vy >= 0.0f && vz >= 0.0f) {
+        x = (uint32_t)vx;
+        y = (uint32_t)vy;
+        z = (uint32_t)vz;
+    } else { // the FP32 index may have wrapped or rounded: decompose it
+        z = o.lin / g.wh;
+        const uint32_t r = o.lin - z * g.wh;
+        y = r / g.w;
+        x = r - y * g.w;
+    }
+    o.brick = (x >> 3) + g.nbx * ((y >> 3) + g.nby * (z >> 3));
+    o.local = (x & 7u) | ((y & 7u) << 3) | ((z & 7u) << 6);
+    return true;
+}
+
 // hair_style.cc:274-276: voxel = min(floor((vertex - origin) / voxel_size), resolution - 1)
-__device__ __forceinline__ bool vertex_voxel(const Grid& g, const float* __restrict__ v, uint32_t i, uint32_t& out)
+__device__ __forceinline__ bool vertex_visit(const Grid& g, const float* __restrict__ v, uint32_t i, Visit& o)
 {
     float c[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a)
         c[a] = glm_min(floorf(__fdiv_rn(__fsub_rn(__ldg(v + 3 * (size_t)i + a), g.org[a]), g.vs[a])), g.rm1[a]);
-    return linear_index(g, c[0], c[1], c[2], out);
+    return locate(g, c[0], c[1], c[2], o);
 }
 
-// hair_style.cc:311-329 for one index pair; calls f(voxel) per visit in serial order.
-template <class F>
-__device__ __forceinline__ void segment_visits(const Grid& g, const float* __restrict__ v, uint32_t i0, uint32_t i1,
-                                               unsigned& status, F&& f)
-{
+// One index pair of voxelize_segments (hair_style.cc:311-329).
+struct Seg {
     float root[3], dir[3];
+    uint32_t n; // iterations of `while (steps-- > 0.0f)`
+};
+
+__device__ __forceinline__ bool seg_setup(const Grid& g, const float* __restrict__ v, uint2 ij, Seg& s,
+                                          unsigned& status)
+{
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        root[a] = __fdiv_rn(__fsub_rn(__ldg(v + 3 * (size_t)i0 + a), g.org[a]), g.vs[a]);
-        float tip = __fdiv_rn(__fsub_rn(__ldg(v + 3 * (size_t)i1 + a), g.org[a]), g.vs[a]);
-        dir[a] = __fsub_rn(tip, root[a]);
+        s.root[a] = __fdiv_rn(__fsub_rn(__ldg(v + 3 * (size_t)ij.x + a), g.org[a]), g.vs[a]);
+        const float tip = __fdiv_rn(__fsub_rn(__ldg(v + 3 * (size_t)ij.y + a), g.org[a]), g.vs[a]);
+        s.dir[a] = __fsub_rn(tip, s.root[a]);
     }
-    float steps = glm_max(glm_max(fabsf(dir[0]), fabsf(dir[1])), fabsf(dir[2])); // compMax(abs(direction))
+    const float steps = glm_max(glm_max(fabsf(s.dir[0]), fabsf(s.dir[1])), fabsf(s.dir[2])); // compMax(abs(dir))
 #pragma unroll
-    for (int a = 0; a < 3; ++a) dir[a] = __fdiv_rn(dir[a], steps);
-    if (!(steps > 0.0f)) return;  // `while (steps-- > 0.0f)` never runs (0 or NaN)
-    if (steps > 16777216.0f) {    // the FP32 decrement no longer terminates reliably
+    for (int a = 0; a < 3; ++a) s.dir[a] = __fdiv_rn(s.dir[a], steps);
+    s.n = 0;
+    if (!(steps > 0.0f)) return false;  // 0 or NaN: the loop never runs
+    if (steps > 16777216.0f) {          // the FP32 decrement no longer terminates reliably
         status |= VKHR_DEV_STEPS_OVERFLOW;
-        return;
+        return false;
     }
     // Below 2^24 every `steps - 1.0f` is exact, so the loop runs ceil(steps) times.
-    const uint32_t n = (uint32_t)ceilf(steps);
-    for (uint32_t k = 0; k < n; ++k) {
-        uint32_t vox;
-        if (linear_index(g, glm_min(floorf(root[0]), g.rm1[0]), glm_min(floorf(root[1]), g.rm1[1]),
-                         glm_min(floorf(root[2]), g.rm1[2]), vox))
-            f(vox);
+    s.n = (uint32_t)ceilf(steps);
+    return true;
+}
+
+__device__ __forceinline__ bool seg_visit(const Grid& g, const Seg& s, Visit& o)
+{
+    return locate(g, glm_min(floorf(s.root[0]), g.rm1[0]), glm_min(floorf(s.root[1]), g.rm1[1]),
+                  glm_min(floorf(s.root[2]), g.rm1[2]), o);
+}
+
+__device__ __forceinline__ void seg_advance(Seg& s)
+{
 #pragma unroll
-        for (int a = 0; a < 3; ++a) root[a] = __fadd_rn(root[a], dir[a]);
+    for (int a = 0; a < 3; ++a) s.root[a] = __fadd_rn(s.root[a], s.dir[a]); // root += direction
+}
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+// ---- brick path -----------------------------------------------------------------
+
+// A run of `len` consecutive visits (steps k0 .. k0+len-1 of pair / vertex p)
+// inside brick b: counted (FILL = false) or written to the brick's slice.
+template <bool FILL>
+__device__ __forceinline__ void emit_run(uint32_t b, uint32_t p, uint32_t k0, uint32_t len, uint32_t* runs,
+                                         uint32_t* visits, uint32_t* cursor, uint2* items, size_t items_cap,
+                                         unsigned& status)
+{
+    const unsigned peers = __match_any_sync(__activemask(), b);
+    const int leader = __ffs(peers) - 1;
+    if (!FILL) {
+        const unsigned tot = __reduce_add_sync(peers, len);
+        if ((int)lane_id() == leader) {
+            atomicAdd(runs + b, (uint32_t)__popc(peers));
+            atomicAdd(visits + b, tot);
+        }
+    } else {
+        uint32_t base = 0;
+        if ((int)lane_id() == leader) base = atomicAdd(cursor + b, (uint32_t)__popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        const uint32_t slot = base + __popc(peers & ((1u << lane_id()) - 1u));
+        if (slot < items_cap) items[slot] = make_uint2(p, (k0 << 8) | len);
+        else status |= VKHR_DEV_LIST_OVERFLOW;
     }
 }
 
-__device__ __forceinline__ void warp_add_total(unsigned long long local, unsigned long long* total)
+template <bool FILL, bool SEG>
+__global__ void bin_kernel(Grid g, const float* __restrict__ v, const uint2* __restrict__ pairs, uint32_t n_in,
+                           uint32_t* runs, uint32_t* visits, uint32_t* cursor, uint2* items, size_t items_cap,
+                           unsigned long long* words)
 {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
-    if ((threadIdx.x & 31) == 0 && local) atomicAdd(total, local);
-}
-
-__global__ void count_vertices_kernel(Grid g, const float* __restrict__ v, uint32_t n_vertices, uint32_t* counts,
-                                      unsigned long long* words)
-{
-    unsigned long long local = 0;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n_vertices; i += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t vox;
-        if (vertex_voxel(g, v, i, vox)) {
-            atomicAdd(counts + vox, 1u);
-            ++local;
+    unsigned status = 0;
+    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n_in; p += (uint64_t)gridDim.x * blockDim.x) {
+        if (SEG) {
+            Seg s;
+            if (!seg_setup(g, v, __ldg(pairs + p), s, status)) continue;
+            uint32_t cur = kNoBrick, k0 = 0, len = 0;
+            for (uint32_t k = 0; k < s.n; ++k) {
+                Visit o;
+                const bool ok = seg_visit(g, s, o);
+                if (ok && o.brick == cur && len < 255u) {
+                    ++len;
+                } else {
+                    if (len) emit_run<FILL>(cur, (uint32_t)p, k0, len, runs, visits, cursor, items, items_cap, status);
+                    cur = ok ? o.brick : kNoBrick;
+                    k0 = k;
+                    len = ok ? 1u : 0u;
+                }
+                seg_advance(s);
+            }
+            if (len) emit_run<FILL>(cur, (uint32_t)p, k0, len, runs, visits, cursor, items, items_cap, status);
+        } else {
+            Visit o;
+            if (vertex_visit(g, v, (uint32_t)p, o))
+                emit_run<FILL>(o.brick, (uint32_t)p, 0u, 1u, runs, visits, cursor, items, items_cap, status);
         }
     }
-    warp_add_total(local, words + WORD_TOTAL_VISITS);
-}
-
-__global__ void count_segments_kernel(Grid g, const float* __restrict__ v, const uint2* __restrict__ pairs_idx,
-                                      uint32_t n_pairs, uint32_t* counts, unsigned long long* words)
-{
-    unsigned long long local = 0;
-    unsigned status = 0;
-    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n_pairs; p += (uint64_t)gridDim.x * blockDim.x) {
-        uint2 ij = __ldg(pairs_idx + p);
-        segment_visits(g, v, ij.x, ij.y, status, [&](uint32_t vox) {
-            atomicAdd(counts + vox, 1u);
-            ++local;
-        });
-    }
-    warp_add_total(local, words + WORD_TOTAL_VISITS);
     if (status) atomicOr(words + WORD_STATUS, (unsigned long long)status);
 }
 
-// Gives each voxel with visits a contiguous slice [cursor, cursor + count) of
-// the visit list.  Voxels are read warp-striped (coalesced); slices are
-// handed out per thread in the same order; one atomic per block.
-__global__ void __launch_bounds__(kRangeThreads) alloc_ranges_kernel(const uint32_t* __restrict__ counts, uint32_t n,
-                                                                   uint32_t* cursor, unsigned long long* words)
+// Slices of the run list per brick (one atomic per 4096 bricks), plus the
+// totals: runs, visits and the largest brick.
+__global__ void __launch_bounds__(kRangeThreads) bin_ranges_kernel(const uint32_t* __restrict__ runs,
+                                                                 const uint32_t* __restrict__ visits, uint32_t nb,
+                                                                 uint32_t* cursor, unsigned long long* words)
 {
     __shared__ uint32_t warp_sums[kRangeThreads / 32];
     __shared__ uint32_t block_base;
     const uint32_t tile = kRangeThreads * kRangeItems;
-    for (uint64_t base = (uint64_t)blockIdx.x * tile; base < n; base += (uint64_t)gridDim.x * tile) {
+    for (uint64_t base = (uint64_t)blockIdx.x * tile; base < nb; base += (uint64_t)gridDim.x * tile) {
         uint32_t c[kRangeItems];
-        uint32_t sum = 0;
+        uint32_t sum = 0, vmax = 0;
+        unsigned long long vsum = 0;
 #pragma unroll
         for (int j = 0; j < kRangeItems; ++j) {
-            uint64_t i = base + (uint64_t)j * kRangeThreads + threadIdx.x;
-            c[j] = i < n ? __ldg(counts + i) : 0u;
+            const uint64_t i = base + (uint64_t)j * kRangeThreads + threadIdx.x;
+            c[j] = i < nb ? __ldg(runs + i) : 0u;
+            const uint32_t vv = i < nb ? __ldg(visits + i) : 0u;
             sum += c[j];
+            vsum += vv;
+            vmax = max(vmax, vv);
         }
-        // block-wide exclusive scan of the per-thread sums
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         uint32_t incl = sum;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
             if (lane >= o) incl += y;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            vsum += __shfl_down_sync(0xffffffffu, vsum, o);
+            vmax = max(vmax, __shfl_down_sync(0xffffffffu, vmax, o));
+        }
+        if (lane == 0) {
+            if (vsum) atomicAdd(words + WORD_TOTAL_VISITS, vsum);
+            atomicMax(words + WORD_MAX_BRICK_VISITS, (unsigned long long)vmax);
         }
         if (lane == 31) warp_sums[warp] = incl;
         __syncthreads();
         if (threadIdx.x == 0) {
             uint32_t run = 0;
             for (int w = 0; w < kRangeThreads / 32; ++w) {
-                uint32_t t = warp_sums[w];
+                const uint32_t t = warp_sums[w];
                 warp_sums[w] = run;
                 run += t;
             }
-            block_base = run ? (uint32_t)atomicAdd(words + WORD_LIST_CURSOR, (unsigned long long)run) : 0u;
+            block_base = run ? (uint32_t)atomicAdd(words + WORD_RUNS_TOTAL, (unsigned long long)run) : 0u;
         }
         __syncthreads();
         uint32_t start = block_base + warp_sums[warp] + (incl - sum);
 #pragma unroll
         for (int j = 0; j < kRangeItems; ++j) {
-            uint64_t i = base + (uint64_t)j * kRangeThreads + threadIdx.x;
-            if (i < n) cursor[i] = start;
+            const uint64_t i = base + (uint64_t)j * kRangeThreads + threadIdx.x;
+            if (i < nb) cursor[i] = start;
             start += c[j];
         }
         __syncthreads();
     }
-}
-
-__global__ void fill_vertices_kernel(Grid g, const float* __restrict__ v, uint32_t n_vertices, uint32_t* cursor,
-                                     uint32_t* list, size_t list_cap, unsigned long long* words)
-{
-    unsigned status = 0;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n_vertices; i += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t vox;
-        if (vertex_voxel(g, v, i, vox)) {
-            uint32_t slot = atomicAdd(cursor + vox, 1u);
-            if (slot < list_cap) list[slot] = (uint32_t)i;
-            else status |= VKHR_DEV_LIST_OVERFLOW;
-        }
-    }
-    if (status) atomicOr(words + WORD_STATUS, (unsigned long long)status);
-}
-
-__global__ void fill_segments_kernel(Grid g, const float* __restrict__ v, const uint2* __restrict__ pairs_idx,
-                                     uint32_t n_pairs, uint32_t* cursor, uint32_t* list, size_t list_cap,
-                                     unsigned long long* words)
-{
-    unsigned status = 0;
-    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n_pairs; p += (uint64_t)gridDim.x * blockDim.x) {
-        uint2 ij = __ldg(pairs_idx + p);
-        segment_visits(g, v, ij.x, ij.y, status, [&](uint32_t vox) {
-            uint32_t slot = atomicAdd(cursor + vox, 1u);
-            if (slot < list_cap) list[slot] = (uint32_t)p;
-            else status |= VKHR_DEV_LIST_OVERFLOW;
-        });
-    }
-    if (status) atomicOr(words + WORD_STATUS, (unsigned long long)status);
 }
 
 // Tangent of a visit key: the vertex's own (voxelize_vertices) or the pair's
@@ -226,15 +285,326 @@ __device__ __forceinline__ uint32_t key_vertex(uint32_t key, const uint2* __rest
 // i8vec3(sum / float(density) * 127.0f), truncating; NaN gives 0.
 __device__ __forceinline__ int quantize1(float s, float m)
 {
-    float q = __fmul_rn(__fdiv_rn(s, m), 127.0f);
+    const float q = __fmul_rn(__fdiv_rn(s, m), 127.0f);
     return (q == q) ? __float2int_rz(q) : 0;
 }
 
 __device__ __forceinline__ uint32_t pack_tangent(float sx, float sy, float sz, uint32_t m)
 {
     const float fm = (float)m;
-    int x = quantize1(sx, fm), y = quantize1(sy, fm), z = quantize1(sz, fm);
+    const int x = quantize1(sx, fm), y = quantize1(sy, fm), z = quantize1(sz, fm);
     return ((uint32_t)(x & 0xff)) | ((uint32_t)(y & 0xff) << 8) | ((uint32_t)(z & 0xff) << 16);
+}
+
+// Replays run item `it` of brick b and calls f(local, key) per visit.
+template <bool SEG, class F>
+__device__ __forceinline__ void replay(const Grid& g, const float* __restrict__ v, const uint2* __restrict__ pairs,
+                                       uint2 it, uint32_t b, unsigned& status, F&& f)
+{
+    if (SEG) {
+        Seg s;
+        unsigned ignore = 0;
+        if (!seg_setup(g, v, __ldg(pairs + it.x), s, ignore)) return;
+        const uint32_t k0 = it.y >> 8, len = it.y & 255u;
+        for (uint32_t k = 0; k < k0; ++k) seg_advance(s);
+        for (uint32_t k = 0; k < len; ++k) {
+            Visit o;
+            if (seg_visit(g, s, o) && o.brick == b) f(o.local, it.x);
+            else status |= VKHR_DEV_REPLAY_MISMATCH;
+            seg_advance(s);
+        }
+    } else {
+        Visit o;
+        if (vertex_visit(g, v, it.x, o) && o.brick == b) f(o.local, it.x);
+        else status |= VKHR_DEV_REPLAY_MISMATCH;
+    }
+}
+
+// Exclusive scan of 512 values, one per thread; `warp_sums` holds 16 words.
+__device__ __forceinline__ uint32_t block_exclusive_scan_512(uint32_t x, uint32_t* warp_sums)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t s = lane < kBrickThreads / 32 ? warp_sums[lane] : 0u;
+        uint32_t si = s;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, si, o);
+            if (lane >= o) si += y;
+        }
+        if (lane < kBrickThreads / 32) warp_sums[lane] = si - s;
+    }
+    __syncthreads();
+    return warp_sums[warp] + incl - x;
+}
+
+template <bool SEG, bool TANG>
+__global__ void __launch_bounds__(kBrickThreads, 2)
+brick_kernel(Grid g, const float* __restrict__ v, const float* __restrict__ tan, const uint2* __restrict__ pairs,
+             const uint32_t* __restrict__ runs, const uint32_t* __restrict__ cursor, const uint32_t* __restrict__ visits,
+             const uint2* __restrict__ items, uint32_t* counts, uint8_t* dens, uint32_t* tq, uint4* hdesc,
+             size_t hdesc_cap, uint32_t* hkeys, size_t hkeys_cap, unsigned long long* words)
+{
+    extern __shared__ uint32_t sm[];
+    uint32_t* cnt = sm;                       // visits per local voxel
+    uint32_t* off = sm + kBrickThreads;       // slice cursor per local voxel
+    uint32_t* warp_sums = sm + 2 * kBrickThreads;
+    uint32_t* keys = sm + 2 * kBrickThreads + 32;
+    __shared__ uint32_t next;
+    const int tid = threadIdx.x;
+    unsigned status = 0;
+    for (;;) {
+        if (tid == 0) next = (uint32_t)atomicAdd(words + WORD_BRICK_QUEUE, 1ull);
+        __syncthreads();
+        const uint32_t b = next;
+        __syncthreads();
+        if (b >= g.nb) break;
+        const uint32_t V = visits[b];
+        if (V > (uint32_t)kBrickCap) continue; // resolved by the global path
+        const uint32_t nit = runs[b], start = cursor[b] - nit;
+        cnt[tid] = 0;
+        __syncthreads();
+        if (V) {
+            for (uint32_t i = tid; i < nit; i += kBrickThreads)
+                replay<SEG>(g, v, pairs, items[start + i], b, status,
+                            [&](uint32_t l, uint32_t) { atomicAdd(cnt + l, 1u); });
+            __syncthreads();
+            if (TANG) {
+                off[tid] = block_exclusive_scan_512(cnt[tid], warp_sums);
+                __syncthreads();
+                for (uint32_t i = tid; i < nit; i += kBrickThreads)
+                    replay<SEG>(g, v, pairs, items[start + i], b, status, [&](uint32_t l, uint32_t key) {
+                        const uint32_t slot = atomicAdd(off + l, 1u);
+                        if (slot < (uint32_t)kBrickCap) keys[slot] = key;
+                    });
+                __syncthreads();
+            }
+        }
+        const uint32_t bx = b % g.nbx, by = (b / g.nbx) % g.nby, bz = b / (g.nbx * g.nby);
+        const uint32_t x = bx * 8 + (tid & 7), y = by * 8 + ((tid >> 3) & 7), z = bz * 8 + (tid >> 6);
+        if (x < g.w && y < g.h && z < g.d) {
+            const uint32_t c = cnt[tid];
+            const uint32_t vi = x + g.w * (y + g.h * z);
+            counts[vi] = c;
+            if (dens) dens[vi] = (uint8_t)(c < 255u ? c : 255u);
+            if (TANG) {
+                if (c == 0) {
+                    tq[vi] = 0u;
+                } else if (c <= (uint32_t)kBrickSmall) {
+                    uint32_t* k = keys + (off[tid] - c);
+                    for (uint32_t i = 1; i < c; ++i) { // insertion sort: serial order
+                        const uint32_t key = k[i];
+                        uint32_t j = i;
+                        while (j > 0 && k[j - 1] > key) {
+                            k[j] = k[j - 1];
+                            --j;
+                        }
+                        k[j] = key;
+                    }
+                    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+                    for (uint32_t i = 0; i < c; ++i) {
+                        const float* t = tan + 3 * (size_t)key_vertex(k[i], SEG ? pairs : nullptr);
+                        sx = __fadd_rn(sx, __ldg(t + 0));
+                        sy = __fadd_rn(sy, __ldg(t + 1));
+                        sz = __fadd_rn(sz, __ldg(t + 2));
+                    }
+                    tq[vi] = pack_tangent(sx, sy, sz, c);
+                } else { // crowded: hand the keys to a CTA of its own
+                    const unsigned long long hb = atomicAdd(words + WORD_HKEYS_CURSOR, (unsigned long long)c);
+                    const unsigned long long hd = atomicAdd(words + WORD_BHEAVY_COUNT, 1ull);
+                    if (hb + c <= hkeys_cap && hd < hdesc_cap) {
+                        const uint32_t* k = keys + (off[tid] - c);
+                        for (uint32_t i = 0; i < c; ++i) hkeys[hb + i] = k[i];
+                        hdesc[hd] = make_uint4(vi, (uint32_t)hb, c, 0u);
+                    } else {
+                        status |= VKHR_DEV_LIST_OVERFLOW;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (status) atomicOr(words + WORD_STATUS, (unsigned long long)status);
+}
+
+__device__ void block_bitonic_sort(uint32_t* s, int n)
+{
+    for (int k = 2; k <= n; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const bool up = (i & k) == 0;
+                    const uint32_t a = s[i], bb = s[l];
+                    if ((a > bb) == up) { s[i] = bb; s[l] = a; }
+                }
+            }
+            __syncthreads();
+        }
+}
+
+// Tangent of a crowded voxel from its c keys at src: the smallest min(c, 255)
+// keys in ascending (serial) order by repeated tile sorts that carry the
+// kKeep smallest forward, then a sequential FP32 sum.  Block-wide.
+__device__ void resolve_crowded(const uint32_t* src, uint32_t c, const float* __restrict__ tan,
+                                const uint2* __restrict__ pairs, uint32_t* keys, float (*tv)[kKeep], uint32_t* out)
+{
+    const uint32_t m = c < 255u ? c : 255u;
+    uint32_t done = 0;
+    int first = 0;
+    while (done < c) {
+        const uint32_t take = min((uint32_t)(kHeavyTile - first), c - done);
+        for (int i = threadIdx.x; i < kHeavyTile - first; i += blockDim.x)
+            keys[first + i] = (uint32_t)i < take ? src[done + i] : 0xffffffffu;
+        __syncthreads();
+        block_bitonic_sort(keys, kHeavyTile);
+        done += take;
+        first = kKeep;
+    }
+    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+        const float* t = tan + 3 * (size_t)key_vertex(keys[i], pairs);
+        tv[0][i] = t[0];
+        tv[1][i] = t[1];
+        tv[2][i] = t[2];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+        for (uint32_t i = 0; i < m; ++i) {
+            sx = __fadd_rn(sx, tv[0][i]);
+            sy = __fadd_rn(sy, tv[1][i]);
+            sz = __fadd_rn(sz, tv[2][i]);
+        }
+        *out = pack_tangent(sx, sy, sz, m);
+    }
+    __syncthreads();
+}
+
+// One CTA per crowded voxel of the brick path (descriptors: voxel, key offset, count).
+__global__ void __launch_bounds__(256) crowded_kernel(const uint4* __restrict__ hdesc, size_t hdesc_cap,
+                                                      const uint32_t* __restrict__ hkeys, const float* __restrict__ tan,
+                                                      const uint2* __restrict__ pairs, uint32_t* tq,
+                                                      const unsigned long long* words)
+{
+    __shared__ uint32_t keys[kHeavyTile];
+    __shared__ float tv[3][kKeep];
+    unsigned long long nh = words[WORD_BHEAVY_COUNT];
+    if (nh > hdesc_cap) nh = hdesc_cap;
+    for (unsigned long long h = blockIdx.x; h < nh; h += gridDim.x) {
+        const uint4 d = hdesc[h];
+        resolve_crowded(hkeys + d.y, d.z, tan, pairs, keys, tv, tq + d.x);
+    }
+}
+
+// ---- global path (bricks with more than kBrickCap visits) ---------------------------
+// Runs only when words[WORD_MAX_BRICK_VISITS] > kBrickCap; visits of other
+// bricks are ignored.
+
+__device__ __forceinline__ bool crowded_brick(const uint32_t* __restrict__ visits, uint32_t b)
+{
+    return __ldg(visits + b) > (uint32_t)kBrickCap;
+}
+
+__device__ __forceinline__ bool global_path_needed(const unsigned long long* words)
+{
+    return words[WORD_MAX_BRICK_VISITS] > (unsigned long long)kBrickCap;
+}
+
+__global__ void global_clear_kernel(uint32_t* counts, uint32_t n, const unsigned long long* words)
+{
+    if (!global_path_needed(words)) return;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        counts[i] = 0u;
+}
+
+template <bool FILL, bool SEG>
+__global__ void global_visit_kernel(Grid g, const float* __restrict__ v, const uint2* __restrict__ pairs,
+                                    uint32_t n_in, const uint32_t* __restrict__ visits, uint32_t* counts,
+                                    uint32_t* gcursor, uint32_t* list, size_t list_cap, unsigned long long* words)
+{
+    if (!global_path_needed(words)) return;
+    unsigned status = 0;
+    auto visit = [&](const Visit& o, uint32_t key) {
+        if (!crowded_brick(visits, o.brick)) return;
+        if (!FILL) {
+            atomicAdd(counts + o.lin, 1u);
+        } else {
+            const uint32_t slot = atomicAdd(gcursor + o.lin, 1u);
+            if (slot < list_cap) list[slot] = key;
+            else status |= VKHR_DEV_LIST_OVERFLOW;
+        }
+    };
+    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n_in; p += (uint64_t)gridDim.x * blockDim.x) {
+        if (SEG) {
+            Seg s;
+            unsigned ignore = 0;
+            if (!seg_setup(g, v, __ldg(pairs + p), s, ignore)) continue;
+            for (uint32_t k = 0; k < s.n; ++k) {
+                Visit o;
+                if (seg_visit(g, s, o)) visit(o, (uint32_t)p);
+                seg_advance(s);
+            }
+        } else {
+            Visit o;
+            if (vertex_visit(g, v, (uint32_t)p, o)) visit(o, (uint32_t)p);
+        }
+    }
+    if (status) atomicOr(words + WORD_STATUS, (unsigned long long)status);
+}
+
+// Slices [gcursor, gcursor + count) of the global visit list per voxel.
+__global__ void __launch_bounds__(kRangeThreads) global_ranges_kernel(const uint32_t* __restrict__ counts, uint32_t n,
+                                                                    uint32_t* gcursor, unsigned long long* words)
+{
+    if (!global_path_needed(words)) return;
+    __shared__ uint32_t warp_sums[kRangeThreads / 32];
+    __shared__ uint32_t block_base;
+    const uint32_t tile = kRangeThreads * kRangeItems;
+    for (uint64_t base = (uint64_t)blockIdx.x * tile; base < n; base += (uint64_t)gridDim.x * tile) {
+        uint32_t c[kRangeItems];
+        uint32_t sum = 0;
+#pragma unroll
+        for (int j = 0; j < kRangeItems; ++j) {
+            const uint64_t i = base + (uint64_t)j * kRangeThreads + threadIdx.x;
+            c[j] = i < n ? __ldg(counts + i) : 0u;
+            sum += c[j];
+        }
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        uint32_t incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) warp_sums[warp] = incl;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t run = 0;
+            for (int w = 0; w < kRangeThreads / 32; ++w) {
+                const uint32_t t = warp_sums[w];
+                warp_sums[w] = run;
+                run += t;
+            }
+            block_base = run ? (uint32_t)atomicAdd(words + WORD_LIST_CURSOR, (unsigned long long)run) : 0u;
+        }
+        __syncthreads();
+        uint32_t start = block_base + warp_sums[warp] + (incl - sum);
+#pragma unroll
+        for (int j = 0; j < kRangeItems; ++j) {
+            const uint64_t i = base + (uint64_t)j * kRangeThreads + threadIdx.x;
+            if (i < n) gcursor[i] = start;
+            start += c[j];
+        }
+        __syncthreads();
+    }
 }
 
 template <int N, int CAP>
@@ -249,25 +619,25 @@ __device__ __forceinline__ void sort_network(uint32_t (&x)[CAP])
                 const int l = i ^ j;
                 if (l > i) {
                     const bool up = (i & k) == 0;
-                    uint32_t a = x[i], b = x[l];
+                    const uint32_t a = x[i], b = x[l];
                     if ((a > b) == up) { x[i] = b; x[l] = a; }
                 }
             }
 }
 
 template <int N>
-__device__ __forceinline__ uint32_t resolve_small(uint32_t c, const uint32_t* __restrict__ list, uint32_t start,
-                                                  const float* __restrict__ tan, const uint2* __restrict__ pairs_idx)
+__device__ __forceinline__ uint32_t resolve_registers(uint32_t c, const uint32_t* __restrict__ list, uint32_t start,
+                                                      const float* __restrict__ tan, const uint2* __restrict__ pairs)
 {
-    uint32_t k[kSmallSort];
+    uint32_t k[N];
 #pragma unroll
-    for (int i = 0; i < kSmallSort; ++i) k[i] = (i < N && (uint32_t)i < c) ? __ldg(list + start + i) : 0xffffffffu;
-    if (N > 2) sort_network<N, kSmallSort>(k);
+    for (int i = 0; i < N; ++i) k[i] = (uint32_t)i < c ? __ldg(list + start + i) : 0xffffffffu;
+    sort_network<N, N>(k);
     float sx = 0.0f, sy = 0.0f, sz = 0.0f;
 #pragma unroll
     for (int i = 0; i < N; ++i)
         if ((uint32_t)i < c) {
-            const float* t = tan + 3 * (size_t)key_vertex(k[i], pairs_idx);
+            const float* t = tan + 3 * (size_t)key_vertex(k[i], pairs);
             sx = __fadd_rn(sx, __ldg(t + 0));
             sy = __fadd_rn(sy, __ldg(t + 1));
             sz = __fadd_rn(sz, __ldg(t + 2));
@@ -275,152 +645,86 @@ __device__ __forceinline__ uint32_t resolve_small(uint32_t c, const uint32_t* __
     return pack_tangent(sx, sy, sz, c);
 }
 
-__global__ void resolve_kernel(uint32_t n, const uint32_t* __restrict__ counts, const uint32_t* __restrict__ cursor,
-                               const uint32_t* __restrict__ list, const float* __restrict__ tan,
-                               const uint2* __restrict__ pairs_idx, uint8_t* dens, uint32_t* tq, uint32_t* heavy,
-                               size_t heavy_cap, unsigned long long* words)
+// Resolves the global path's voxels (crowded bricks only; other voxels are
+// written by the brick kernel afterwards).  Voxels with more than
+// kMediumSort visits go to crowded descriptors over the global list.
+__global__ void global_resolve_kernel(Grid g, const uint32_t* __restrict__ visits, const uint32_t* __restrict__ counts,
+                                      const uint32_t* __restrict__ gcursor, const uint32_t* __restrict__ list,
+                                      const float* __restrict__ tan, const uint2* __restrict__ pairs, uint8_t* dens,
+                                      uint32_t* tq, uint4* gdesc, size_t gdesc_cap, unsigned long long* words)
 {
-    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t c = __ldg(counts + v);
-        if (dens) dens[v] = (uint8_t)(c < 255u ? c : 255u);
+    if (!global_path_needed(words)) return;
+    for (uint64_t vi = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; vi < g.n; vi += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t z = (uint32_t)(vi / g.wh), r = (uint32_t)(vi - (uint64_t)z * g.wh), y = r / g.w, x = r - y * g.w;
+        if (!crowded_brick(visits, (x >> 3) + g.nbx * ((y >> 3) + g.nby * (z >> 3)))) continue;
+        const uint32_t c = counts[vi];
+        if (dens) dens[vi] = (uint8_t)(c < 255u ? c : 255u);
         if (!tq) continue;
-        if (c == 0) { tq[v] = 0u; continue; }
-        const uint32_t start = __ldg(cursor + v) - c;
-        uint32_t packed;
-        if (c <= 2) packed = resolve_small<2>(c, list, start, tan, pairs_idx);      // order-free
-        else if (c <= 4) packed = resolve_small<4>(c, list, start, tan, pairs_idx);
-        else if (c <= 8) packed = resolve_small<8>(c, list, start, tan, pairs_idx);
-        else if (c <= kSmallSort) packed = resolve_small<kSmallSort>(c, list, start, tan, pairs_idx);
+        if (c == 0) { tq[vi] = 0u; continue; }
+        const uint32_t start = gcursor[vi] - c;
+        if (c <= kSmallSort) tq[vi] = resolve_registers<kSmallSort>(c, list, start, tan, pairs);
+        else if (c <= kMediumSort) tq[vi] = resolve_registers<kMediumSort>(c, list, start, tan, pairs);
         else {
-            // crowded voxels: medium ones to a register-network pass, the
-            // rest to one block each; both lists share the heavy buffer
-            // (medium from the front, crowded from the back)
-            const bool medium = c <= kMediumSort;
-            unsigned long long slot = atomicAdd(words + (medium ? WORD_MEDIUM_COUNT : WORD_HEAVY_COUNT), 1ull);
-            const unsigned long long at = medium ? slot : heavy_cap - 1 - slot;
-            if (slot < heavy_cap / 2) heavy[at] = (uint32_t)v;
+            const unsigned long long hd = atomicAdd(words + WORD_HEAVY_COUNT, 1ull);
+            if (hd < gdesc_cap) gdesc[hd] = make_uint4((uint32_t)vi, start, c, 0u);
             else atomicOr(words + WORD_STATUS, (unsigned long long)VKHR_DEV_LIST_OVERFLOW);
-            continue;
         }
-        tq[v] = packed;
     }
 }
 
-// Voxels with kSmallSort < count <= kMediumSort: one thread each, keys sorted
-// by a 64-wide register network (SIMT across voxels beats cooperation within one).
-__global__ void __launch_bounds__(128) resolve_medium_kernel(const uint32_t* __restrict__ counts,
-                                                             const uint32_t* __restrict__ cursor,
+__global__ void __launch_bounds__(256) global_crowded_kernel(const uint4* __restrict__ gdesc, size_t gdesc_cap,
                                                              const uint32_t* __restrict__ list,
                                                              const float* __restrict__ tan,
-                                                             const uint2* __restrict__ pairs_idx,
-                                                             const uint32_t* __restrict__ medium, size_t heavy_cap,
-                                                             uint32_t* tq, const unsigned long long* words)
+                                                             const uint2* __restrict__ pairs, uint32_t* tq,
+                                                             const unsigned long long* words)
 {
-    unsigned long long nm = words[WORD_MEDIUM_COUNT];
-    if (nm > heavy_cap / 2) nm = heavy_cap / 2;
-    for (unsigned long long h = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; h < nm;
-         h += (unsigned long long)gridDim.x * blockDim.x) {
-        const uint32_t v = medium[h];
-        const uint32_t c = counts[v];
-        const uint32_t start = cursor[v] - c;
-        uint32_t k[kMediumSort];
-#pragma unroll
-        for (int i = 0; i < kMediumSort; ++i) k[i] = (uint32_t)i < c ? __ldg(list + start + i) : 0xffffffffu;
-        sort_network<kMediumSort, kMediumSort>(k);
-        float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-#pragma unroll
-        for (int i = 0; i < kMediumSort; ++i)
-            if ((uint32_t)i < c) {
-                const float* t = tan + 3 * (size_t)key_vertex(k[i], pairs_idx);
-                sx = __fadd_rn(sx, __ldg(t + 0));
-                sy = __fadd_rn(sy, __ldg(t + 1));
-                sz = __fadd_rn(sz, __ldg(t + 2));
-            }
-        tq[v] = pack_tangent(sx, sy, sz, c);
-    }
-}
-
-__device__ void block_bitonic_sort(uint32_t* s, int n)
-{
-    for (int k = 2; k <= n; k <<= 1)
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = threadIdx.x; i < n; i += blockDim.x) {
-                const int l = i ^ j;
-                if (l > i) {
-                    const bool up = (i & k) == 0;
-                    uint32_t a = s[i], b = s[l];
-                    if ((a > b) == up) { s[i] = b; s[l] = a; }
-                }
-            }
-            __syncthreads();
-        }
-}
-
-// One block per crowded voxel: the first min(count, 255) keys in serial order
-// by repeated tile sorts that carry the smallest kKeep keys forward.
-__global__ void __launch_bounds__(256) resolve_heavy_kernel(const uint32_t* __restrict__ counts,
-                                                            const uint32_t* __restrict__ cursor,
-                                                            const uint32_t* __restrict__ list,
-                                                            const float* __restrict__ tan,
-                                                            const uint2* __restrict__ pairs_idx,
-                                                            const uint32_t* __restrict__ heavy, size_t heavy_cap,
-                                                            uint32_t* tq, const unsigned long long* words)
-{
+    if (!global_path_needed(words)) return;
     __shared__ uint32_t keys[kHeavyTile];
     __shared__ float tv[3][kKeep];
     unsigned long long nh = words[WORD_HEAVY_COUNT];
-    if (nh > heavy_cap / 2) nh = heavy_cap / 2;
+    if (nh > gdesc_cap) nh = gdesc_cap;
     for (unsigned long long h = blockIdx.x; h < nh; h += gridDim.x) {
-        const uint32_t v = heavy[heavy_cap - 1 - h];
-        const uint32_t c = counts[v];
-        const uint32_t start = cursor[v] - c;
-        const uint32_t m = c < 255u ? c : 255u;
-        uint32_t done = 0;
-        int first = 0; // slots already holding carried keys
-        while (done < c) {
-            const uint32_t take = min((uint32_t)(kHeavyTile - first), c - done);
-            for (int i = threadIdx.x; i < kHeavyTile - first; i += blockDim.x)
-                keys[first + i] = (uint32_t)i < take ? list[start + done + i] : 0xffffffffu;
-            __syncthreads();
-            block_bitonic_sort(keys, kHeavyTile);
-            done += take;
-            first = kKeep;
-        }
-        for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
-            const float* t = tan + 3 * (size_t)key_vertex(keys[i], pairs_idx);
-            tv[0][i] = t[0];
-            tv[1][i] = t[1];
-            tv[2][i] = t[2];
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-            for (uint32_t i = 0; i < m; ++i) {
-                sx = __fadd_rn(sx, tv[0][i]);
-                sy = __fadd_rn(sy, tv[1][i]);
-                sz = __fadd_rn(sz, tv[2][i]);
-            }
-            tq[v] = pack_tangent(sx, sy, sz, m);
-        }
-        __syncthreads();
+        const uint4 d = gdesc[h];
+        resolve_crowded(list + d.y, d.z, tan, pairs, keys, tv, tq + d.x);
     }
 }
+
+// ---- Volume::normalize ------------------------------------------------------------------
 
 __global__ void init_minmax_kernel(unsigned long long* words)
 {
     if (threadIdx.x == 0) {
-        words[WORD_AABB + 0] = 255ull;
-        words[WORD_AABB + 1] = 0ull;
+        words[WORD_NORM + 0] = 255ull;
+        words[WORD_NORM + 1] = 0ull;
     }
 }
 
 __global__ void minmax_u8_kernel(const uint8_t* __restrict__ d, uint64_t n, unsigned long long* words)
 {
+    __shared__ uint32_t s_lo, s_hi;
+    if (threadIdx.x == 0) {
+        s_lo = 255u;
+        s_hi = 0u;
+    }
+    __syncthreads();
     uint32_t lo = 255, hi = 0;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t x = d[i];
-        lo = min(lo, x);
-        hi = max(hi, x);
+    const uint64_t n16 = n / 16;
+    const uint4* d16 = reinterpret_cast<const uint4*>(d);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n16; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint4 q = __ldg(d16 + i);
+        const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+#pragma unroll
+            for (int s = 0; s < 32; s += 8) {
+                const uint32_t x = (w[k] >> s) & 0xffu;
+                lo = min(lo, x);
+                hi = max(hi, x);
+            }
+    }
+    for (uint64_t i = n16 * 16 + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        lo = min(lo, (uint32_t)d[i]);
+        hi = max(hi, (uint32_t)d[i]);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -428,21 +732,38 @@ __global__ void minmax_u8_kernel(const uint8_t* __restrict__ d, uint64_t n, unsi
         hi = max(hi, __shfl_down_sync(0xffffffffu, hi, o));
     }
     if ((threadIdx.x & 31) == 0) {
-        atomicMin(words + WORD_AABB + 0, (unsigned long long)lo);
-        atomicMax(words + WORD_AABB + 1, (unsigned long long)hi);
+        atomicMin(&s_lo, lo);
+        atomicMax(&s_hi, hi);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        atomicMin(words + WORD_NORM + 0, (unsigned long long)s_lo);
+        atomicMax(words + WORD_NORM + 1, (unsigned long long)s_hi);
     }
 }
 
 // hair_style.cc:344-357: d = u8((d - min) * (255.0f / (max - min))), truncating.
+__device__ __forceinline__ uint32_t rescale1(uint32_t x, uint32_t lo, uint32_t hi, float scaling)
+{
+    return hi > lo ? (__float2uint_rz(__fmul_rn((float)(x - lo), scaling)) & 0xffu) : 0u;
+}
+
 __global__ void rescale_u8_kernel(uint8_t* d, uint64_t n, const unsigned long long* words)
 {
-    const uint32_t lo = (uint32_t)words[WORD_AABB + 0], hi = (uint32_t)words[WORD_AABB + 1];
+    const uint32_t lo = (uint32_t)words[WORD_NORM + 0], hi = (uint32_t)words[WORD_NORM + 1];
     const float scaling = hi > lo ? __fdiv_rn(255.0f, (float)(int)(hi - lo)) : 0.0f;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t x = (uint32_t)d[i] - lo;
-        d[i] = hi > lo ? (uint8_t)__float2uint_rz(__fmul_rn((float)x, scaling)) : (uint8_t)0;
+    const uint64_t n4 = n / 4;
+    uint32_t* d4 = reinterpret_cast<uint32_t*>(d);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n4; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t q = d4[i];
+        d4[i] = rescale1(q & 0xffu, lo, hi, scaling) | (rescale1((q >> 8) & 0xffu, lo, hi, scaling) << 8) |
+                (rescale1((q >> 16) & 0xffu, lo, hi, scaling) << 16) | (rescale1(q >> 24, lo, hi, scaling) << 24);
     }
+    for (uint64_t i = n4 * 4 + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        d[i] = (uint8_t)rescale1(d[i], lo, hi, scaling);
 }
+
+// ---- host ----------------------------------------------------------------------------------
 
 vkhr_status make_grid(vkhr_ctx* ctx, const vkhr_aabb* b, int32_t w, int32_t h, int32_t d, int32_t mode, Grid& g)
 {
@@ -466,18 +787,37 @@ vkhr_status make_grid(vkhr_ctx* ctx, const vkhr_aabb* b, int32_t w, int32_t h, i
     g.fn = (float)n;
     g.w = (uint32_t)w;
     g.h = (uint32_t)h;
+    g.d = (uint32_t)d;
     g.n = (uint32_t)n;
+    g.wh = (uint32_t)w * (uint32_t)h;
+    g.nbx = (g.w + 7) / 8;
+    g.nby = (g.h + 7) / 8;
+    g.nbz = (g.d + 7) / 8;
+    g.nb = g.nbx * g.nby * g.nbz;
     g.mode = mode;
+    g.exact_coords = (mode == VKHR_INDEX_EXACT || n <= (1ull << 24)) ? 1 : 0;
     return VKHR_OK;
 }
 
-vkhr_status check_device_status(vkhr_ctx* ctx)
+vkhr_status check_device_status(vkhr_ctx* ctx, unsigned long long s)
 {
-    const unsigned long long s = ctx->h_words[WORD_STATUS];
     if (s & VKHR_DEV_STEPS_OVERFLOW)
         return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG,
                          "a segment spans more than 2^24 voxels (vertices far outside the bounds)");
     if (s & VKHR_DEV_LIST_OVERFLOW) return vkhr_fail(ctx, VKHR_ERR_CAPACITY, "visit list overflow");
+    if (s & VKHR_DEV_REPLAY_MISMATCH) return vkhr_fail(ctx, VKHR_ERR_CUDA, "brick replay disagreed with binning");
+    return VKHR_OK;
+}
+
+template <bool SEG, bool TANG>
+vkhr_status launch_brick(vkhr_ctx* ctx, const Grid& g, const float* v, const float* tan_in, const uint2* pairs,
+                         uint32_t* counts, uint8_t* dens, uint32_t* tq, cudaStream_t st, unsigned blocks, size_t smem)
+{
+    VKHR_CUDA_TRY(ctx, cudaFuncSetAttribute(brick_kernel<SEG, TANG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)smem));
+    VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG>), blocks, kBrickThreads, smem, st, g, v, tan_in, pairs, ctx->brick_runs,
+                ctx->brick_cursor, ctx->brick_visits, ctx->items, counts, dens, tq, ctx->hdesc, ctx->hdesc_cap,
+                ctx->hkeys, ctx->hkeys_cap, ctx->d_words);
     return VKHR_OK;
 }
 
@@ -497,82 +837,114 @@ vkhr_status voxelize_impl(vkhr_ctx* ctx, bool segments, const float* v, const fl
     if (segments && n_in && !idx) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_indices is NULL");
     if (segments && idx && (reinterpret_cast<uintptr_t>(idx) & 7u))
         return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_indices must be 8-byte aligned");
+    if (tq && (reinterpret_cast<uintptr_t>(tq) & 3u))
+        return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_tangents must be 4-byte aligned");
     VKHR_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     const uint2* pairs = reinterpret_cast<const uint2*>(idx);
+    const bool tang = tq != nullptr;
+    uint32_t* tq32 = reinterpret_cast<uint32_t*>(tq);
 
-    if (tq) {
-        s = vkhr_reserve(ctx, (void**)&ctx->cursor, &ctx->cursor_cap, g.n, sizeof(uint32_t));
-        if (s != VKHR_OK) return s;
-    }
-    VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_words, 0, 5 * sizeof(unsigned long long), st));
-    VKHR_CUDA_TRY(ctx, cudaMemsetAsync(counts, 0, (size_t)g.n * sizeof(uint32_t), st));
+    // per-brick bookkeeping: runs, visits, cursor
+    s = vkhr_reserve(ctx, (void**)&ctx->brick_runs, &ctx->brick_cap, 3ull * g.nb, sizeof(uint32_t));
+    if (s != VKHR_OK) return s;
+    ctx->brick_visits = ctx->brick_runs + g.nb;
+    ctx->brick_cursor = ctx->brick_runs + 2ull * g.nb;
+    VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_words, 0, WORD_NORM * sizeof(unsigned long long), st));
+    VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->brick_runs, 0, 2ull * g.nb * sizeof(uint32_t), st));
     const unsigned threads = 256;
-    const unsigned max_blocks = (unsigned)ctx->sm_count * 16;
-    const unsigned blocks = std::min(vkhr_blocks(n_in, threads), max_blocks);
-    if (n_in) {
-        if (segments) VKHR_LAUNCH(ctx, count_segments_kernel, blocks, threads, 0, st, g, v, pairs, n_in, counts, ctx->d_words);
-        else VKHR_LAUNCH(ctx, count_vertices_kernel, blocks, threads, 0, st, g, v, n_in, counts, ctx->d_words);
-        VKHR_CUDA_TRY(ctx, cudaGetLastError());
-    }
-    const unsigned vblocks = std::min(vkhr_blocks(g.n, threads), (unsigned)ctx->sm_count * 32);
-    if (!tq) {
-        if (dens) {
-            VKHR_LAUNCH(ctx, resolve_kernel, vblocks, threads, 0, st, g.n, counts, nullptr, nullptr, nullptr, nullptr, dens, nullptr,
-                                                        nullptr, 0, ctx->d_words);
-            VKHR_CUDA_TRY(ctx, cudaGetLastError());
-        }
-        if (segments) {
-            VKHR_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->h_words, ctx->d_words, 4 * sizeof(unsigned long long),
-                                               cudaMemcpyDeviceToHost, st));
-            VKHR_CUDA_TRY(ctx, cudaStreamSynchronize(st));
-            return check_device_status(ctx);
-        }
-        return VKHR_OK;
-    }
-
-    // The visit total sizes the list.  Vertex mode: bounded by the vertex
-    // count, no round trip.  Segment mode: read it back while the GPU
-    // allocates ranges.
-    VKHR_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->h_words, ctx->d_words, 4 * sizeof(unsigned long long),
-                                       cudaMemcpyDeviceToHost, st));
-    VKHR_CUDA_TRY(ctx, cudaEventRecord(ctx->ev, st));
-    const unsigned rblocks = std::min(vkhr_blocks(g.n, kRangeThreads * kRangeItems), (unsigned)ctx->sm_count * 8);
-    VKHR_LAUNCH(ctx, alloc_ranges_kernel, rblocks, kRangeThreads, 0, st, counts, g.n, ctx->cursor, ctx->d_words);
-    VKHR_CUDA_TRY(ctx, cudaGetLastError());
-    uint64_t total = n_in;
-    if (segments) {
-        VKHR_CUDA_TRY(ctx, cudaEventSynchronize(ctx->ev));
-        s = check_device_status(ctx);
-        if (s != VKHR_OK) return s;
-        total = ctx->h_words[WORD_TOTAL_VISITS];
-        if (total >= (1ull << 32))
-            return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "more than 2^32 - 1 voxel visits in one call");
-    }
-    s = vkhr_reserve(ctx, (void**)&ctx->list, &ctx->list_cap, total ? total : 1, sizeof(uint32_t));
-    if (s != VKHR_OK) return s;
-    // medium voxels (> kSmallSort visits each) fill the buffer from the front,
-    // crowded ones (> kMediumSort) from the back: each list fits its half.
-    s = vkhr_reserve(ctx, (void**)&ctx->heavy, &ctx->heavy_cap, 2 * (total / (kSmallSort + 1) + 1),
-                     sizeof(uint32_t));
-    if (s != VKHR_OK) return s;
+    const unsigned in_blocks = std::min(vkhr_blocks(n_in, threads), (unsigned)ctx->sm_count * 16);
     if (n_in) {
         if (segments)
-            VKHR_LAUNCH(ctx, fill_segments_kernel, blocks, threads, 0, st, g, v, pairs, n_in, ctx->cursor, ctx->list, ctx->list_cap,
-                                                             ctx->d_words);
+            VKHR_LAUNCH(ctx, (bin_kernel<false, true>), in_blocks, threads, 0, st, g, v, pairs, n_in, ctx->brick_runs,
+                        ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap, ctx->d_words);
         else
-            VKHR_LAUNCH(ctx, fill_vertices_kernel, blocks, threads, 0, st, g, v, n_in, ctx->cursor, ctx->list, ctx->list_cap,
-                                                             ctx->d_words);
+            VKHR_LAUNCH(ctx, (bin_kernel<false, false>), in_blocks, threads, 0, st, g, v, pairs, n_in, ctx->brick_runs,
+                        ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap, ctx->d_words);
+    }
+    const unsigned rblocks = std::min(vkhr_blocks(g.nb, kRangeThreads * kRangeItems), (unsigned)ctx->sm_count * 8);
+    VKHR_LAUNCH(ctx, bin_ranges_kernel, rblocks, kRangeThreads, 0, st, ctx->brick_runs, ctx->brick_visits, g.nb,
+                ctx->brick_cursor, ctx->d_words);
+    VKHR_CUDA_TRY(ctx, cudaGetLastError());
+
+    // Sizes of the run list and the crowded-voxel buffers.  Vertex mode is
+    // bounded by the vertex count; segment mode reads the totals back.
+    uint64_t runs_total = n_in, visits_total = n_in;
+    bool global_path = true; // vertex mode: launched, exits on the device when unneeded
+    if (segments) {
+        VKHR_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->h_words, ctx->d_words, WORD_NORM * sizeof(unsigned long long),
+                                           cudaMemcpyDeviceToHost, st));
+        VKHR_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+        s = check_device_status(ctx, ctx->h_words[WORD_STATUS]);
+        if (s != VKHR_OK) return s;
+        runs_total = ctx->h_words[WORD_RUNS_TOTAL];
+        visits_total = ctx->h_words[WORD_TOTAL_VISITS];
+        global_path = ctx->h_words[WORD_MAX_BRICK_VISITS] > (unsigned long long)kBrickCap;
+        if (visits_total >= (1ull << 32))
+            return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "more than 2^32 - 1 voxel visits in one call");
+    }
+    s = vkhr_reserve(ctx, (void**)&ctx->items, &ctx->items_cap, runs_total ? runs_total : 1, sizeof(uint2));
+    if (s != VKHR_OK) return s;
+    if (tang) {
+        s = vkhr_reserve(ctx, (void**)&ctx->hkeys, &ctx->hkeys_cap, visits_total ? visits_total : 1, sizeof(uint32_t));
+        if (s != VKHR_OK) return s;
+        s = vkhr_reserve(ctx, (void**)&ctx->hdesc, &ctx->hdesc_cap, visits_total / (kBrickSmall + 1) + 1,
+                         sizeof(uint4));
+        if (s != VKHR_OK) return s;
+    }
+    if (global_path && n_in) {
+        s = vkhr_reserve(ctx, (void**)&ctx->cursor, &ctx->cursor_cap, g.n, sizeof(uint32_t));
+        if (s != VKHR_OK) return s;
+        s = vkhr_reserve(ctx, (void**)&ctx->list, &ctx->list_cap, visits_total ? visits_total : 1, sizeof(uint32_t));
+        if (s != VKHR_OK) return s;
+        s = vkhr_reserve(ctx, (void**)&ctx->gdesc, &ctx->gdesc_cap, visits_total / (kMediumSort + 1) + 1,
+                         sizeof(uint4));
+        if (s != VKHR_OK) return s;
+        const unsigned vblocks = std::min(vkhr_blocks(g.n, threads), (unsigned)ctx->sm_count * 32);
+        VKHR_LAUNCH(ctx, global_clear_kernel, vblocks, threads, 0, st, counts, g.n, ctx->d_words);
+        if (segments)
+            VKHR_LAUNCH(ctx, (global_visit_kernel<false, true>), in_blocks, threads, 0, st, g, v, pairs, n_in,
+                        ctx->brick_visits, counts, ctx->cursor, ctx->list, ctx->list_cap, ctx->d_words);
+        else
+            VKHR_LAUNCH(ctx, (global_visit_kernel<false, false>), in_blocks, threads, 0, st, g, v, pairs, n_in,
+                        ctx->brick_visits, counts, ctx->cursor, ctx->list, ctx->list_cap, ctx->d_words);
+        const unsigned gr = std::min(vkhr_blocks(g.n, kRangeThreads * kRangeItems), (unsigned)ctx->sm_count * 8);
+        VKHR_LAUNCH(ctx, global_ranges_kernel, gr, kRangeThreads, 0, st, counts, g.n, ctx->cursor, ctx->d_words);
+        if (tang) {
+            if (segments)
+                VKHR_LAUNCH(ctx, (global_visit_kernel<true, true>), in_blocks, threads, 0, st, g, v, pairs, n_in,
+                            ctx->brick_visits, counts, ctx->cursor, ctx->list, ctx->list_cap, ctx->d_words);
+            else
+                VKHR_LAUNCH(ctx, (global_visit_kernel<true, false>), in_blocks, threads, 0, st, g, v, pairs, n_in,
+                            ctx->brick_visits, counts, ctx->cursor, ctx->list, ctx->list_cap, ctx->d_words);
+        }
+        VKHR_LAUNCH(ctx, global_resolve_kernel, vblocks, threads, 0, st, g, ctx->brick_visits, counts, ctx->cursor,
+                    ctx->list, tan_in, segments ? pairs : nullptr, dens, tang ? tq32 : nullptr, ctx->gdesc,
+                    ctx->gdesc_cap, ctx->d_words);
+        if (tang)
+            VKHR_LAUNCH(ctx, global_crowded_kernel, (unsigned)ctx->sm_count * 2, 256, 0, st, ctx->gdesc, ctx->gdesc_cap,
+                        ctx->list, tan_in, segments ? pairs : nullptr, tq32, ctx->d_words);
         VKHR_CUDA_TRY(ctx, cudaGetLastError());
     }
-    uint32_t* tq32 = reinterpret_cast<uint32_t*>(tq);
-    VKHR_LAUNCH(ctx, resolve_kernel, vblocks, threads, 0, st, g.n, counts, ctx->cursor, ctx->list, tan_in,
-                                                segments ? pairs : nullptr, dens, tq32, ctx->heavy, ctx->heavy_cap,
-                                                ctx->d_words);
-    VKHR_CUDA_TRY(ctx, cudaGetLastError());
-    VKHR_LAUNCH(ctx, resolve_medium_kernel, (unsigned)ctx->sm_count * 8, 128, 0, st, counts, ctx->cursor, ctx->list,
-                tan_in, segments ? pairs : nullptr, ctx->heavy, ctx->heavy_cap, tq32, ctx->d_words);
-    VKHR_LAUNCH(ctx, resolve_heavy_kernel, (unsigned)ctx->sm_count * 2, 256, 0, st, counts, ctx->cursor, ctx->list,
-                tan_in, segments ? pairs : nullptr, ctx->heavy, ctx->heavy_cap, tq32, ctx->d_words);
+    if (n_in) {
+        if (segments)
+            VKHR_LAUNCH(ctx, (bin_kernel<true, true>), in_blocks, threads, 0, st, g, v, pairs, n_in, ctx->brick_runs,
+                        ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap, ctx->d_words);
+        else
+            VKHR_LAUNCH(ctx, (bin_kernel<true, false>), in_blocks, threads, 0, st, g, v, pairs, n_in, ctx->brick_runs,
+                        ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap, ctx->d_words);
+    }
+    const size_t smem = (size_t)(2 * kBrickThreads + 32 + (tang ? kBrickCap : 0)) * sizeof(uint32_t);
+    const unsigned bblocks = std::min(g.nb, (unsigned)ctx->sm_count * 2);
+    if (segments)
+        s = tang ? launch_brick<true, true>(ctx, g, v, tan_in, pairs, counts, dens, tq32, st, bblocks, smem)
+                 : launch_brick<true, false>(ctx, g, v, tan_in, pairs, counts, dens, tq32, st, bblocks, smem);
+    else
+        s = tang ? launch_brick<false, true>(ctx, g, v, tan_in, pairs, counts, dens, tq32, st, bblocks, smem)
+                 : launch_brick<false, false>(ctx, g, v, tan_in, pairs, counts, dens, tq32, st, bblocks, smem);
+    if (s != VKHR_OK) return s;
+    if (tang)
+        VKHR_LAUNCH(ctx, crowded_kernel, (unsigned)ctx->sm_count * 2, 256, 0, st, ctx->hdesc, ctx->hdesc_cap, ctx->hkeys,
+                    tan_in, segments ? pairs : nullptr, tq32, ctx->d_words);
     VKHR_CUDA_TRY(ctx, cudaGetLastError());
     return VKHR_OK;
 }
@@ -600,18 +972,31 @@ vkhr_status vkhr_voxelize_segments(vkhr_ctx* ctx, const float* d_vertices, const
                          depth, index_mode, d_counts, d_densities, d_tangents, (cudaStream_t)stream);
 }
 
+vkhr_status vkhr_check_status(vkhr_ctx* ctx, void* stream)
+{
+    if (!ctx) return VKHR_ERR_INVALID_ARG;
+    VKHR_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    VKHR_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->h_words, ctx->d_words, WORD_NORM * sizeof(unsigned long long),
+                                       cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    VKHR_CUDA_TRY(ctx, cudaStreamSynchronize((cudaStream_t)stream));
+    return check_device_status(ctx, ctx->h_words[WORD_STATUS]);
+}
+
 vkhr_status vkhr_normalize_densities(vkhr_ctx* ctx, uint8_t* d, uint64_t n, void* stream)
 {
     if (!ctx) return VKHR_ERR_INVALID_ARG;
     if (n == 0) return VKHR_OK;
     if (!d) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_densities is NULL");
+    if (reinterpret_cast<uintptr_t>(d) & 15u)
+        return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_densities must be 16-byte aligned");
     cudaStream_t st = (cudaStream_t)stream;
     VKHR_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     VKHR_LAUNCH(ctx, init_minmax_kernel, 1, 32, 0, st, ctx->d_words);
-    const unsigned blocks = std::min(vkhr_blocks(n, 256), (unsigned)ctx->sm_count * 8);
+    const unsigned blocks = std::min(vkhr_blocks(n / 16 + 1, 256), (unsigned)ctx->sm_count * 4);
     VKHR_LAUNCH(ctx, minmax_u8_kernel, blocks, 256, 0, st, d, n, ctx->d_words);
     VKHR_CUDA_TRY(ctx, cudaGetLastError());
-    VKHR_LAUNCH(ctx, rescale_u8_kernel, blocks, 256, 0, st, d, n, ctx->d_words);
+    const unsigned rb = std::min(vkhr_blocks(n / 4 + 1, 256), (unsigned)ctx->sm_count * 8);
+    VKHR_LAUNCH(ctx, rescale_u8_kernel, rb, 256, 0, st, d, n, ctx->d_words);
     VKHR_CUDA_TRY(ctx, cudaGetLastError());
     return VKHR_OK;
 }
