@@ -28,9 +28,10 @@ enum {
     WORD_MAX_BRICK_VISITS = 5,  // brick path: largest brick
     WORD_BHEAVY_COUNT = 6,      // brick path: crowded-voxel descriptors
     WORD_HKEYS_CURSOR = 7,      // brick path: crowded-voxel key buffer cursor
-    WORD_BRICK_QUEUE = 8,       // brick path: next brick to resolve
-    WORD_NORM = 9,              // normalize: min, max (2 slots); words below are cleared per voxelization
-    WORD_AABB = 11,             // bounding-box scratch (8 slots)
+    WORD_BRICK_QUEUE = 8,       // brick path: next entry of the occupied-brick list
+    WORD_BRICK_LIST = 9,        // brick path: occupied bricks resolved in shared memory
+    WORD_NORM = 10,             // normalize: min, max (2 slots); words below are cleared per voxelization
+    WORD_AABB = 12,             // bounding-box scratch (8 slots)
     WORD_COUNT = 24
 };
 
@@ -42,8 +43,12 @@ struct vkhr_ctx {
     uint32_t* brick_visits;
     uint32_t* brick_cursor;
     size_t brick_cap;
-    uint2* items;              // voxelizer: run items (pair or vertex, first step << 8 | length)
+    uint2* items;              // voxelizer: run items (pair, first step << 8 | length) or (vertex, voxel)
     size_t items_cap;
+    uint32_t* brick_list;      // voxelizer: occupied bricks of the shared-memory path
+    size_t brick_list_cap;
+    float4* pair_rec;          // voxelizer: per index pair {root.xyz, steps}, {direction.xyz, 0}
+    size_t pair_rec_cap;
     uint32_t* hkeys;           // voxelizer: keys of crowded voxels
     size_t hkeys_cap;
     uint4* hdesc;              // voxelizer: crowded voxels (voxel, key offset, count)

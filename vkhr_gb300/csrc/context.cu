@@ -133,7 +133,8 @@ vkhr_status vkhr_destroy(vkhr_ctx* ctx)
     if (!ctx) return VKHR_OK;
     cudaSetDevice(ctx->device);
     cudaDeviceSynchronize();
-    void* bufs[] = {ctx->brick_runs, ctx->items, ctx->hkeys, ctx->hdesc, ctx->cursor, ctx->list, ctx->gdesc};
+    void* bufs[] = {ctx->brick_runs, ctx->items, ctx->brick_list, ctx->pair_rec, ctx->hkeys, ctx->hdesc,
+                    ctx->cursor, ctx->list, ctx->gdesc};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (ctx->occ) cudaFree(ctx->occ);

@@ -12,11 +12,15 @@
 //   1. bin (count)  one thread per vertex / index pair walks its visits and
 //                   splits them into runs of consecutive visits inside one
 //                   brick; warp-aggregated atomics count runs and visits per
-//                   brick (32K bricks at 256^3, hot in L2);
-//   2. bin ranges   each brick gets a slice of the run list;
+//                   brick (32K bricks at 256^3, hot in L2).  A pair's set-up
+//                   (its root, direction and step count: nine IEEE divisions)
+//                   is stored once as a 32-byte record;
+//   2. bin ranges   each brick gets a slice of the run list; occupied bricks
+//                   are listed; empty bricks are zeroed by a streaming kernel;
 //   3. bin (fill)   the same walk again writes (pair, first step, length)
-//                   run items into the bricks' slices;
-//   4. brick        one CTA per brick replays its runs twice with the exact
+//                   run items -- (vertex, voxel) items in vertex mode -- into
+//                   the bricks' slices;
+//   4. brick        one CTA per occupied brick replays its runs twice with the exact
 //                   stepping: counts per voxel in shared memory, then the
 //                   serial keys bucketed per voxel; each voxel's keys are
 //                   sorted in shared memory and its tangents summed in that
@@ -151,14 +155,34 @@ __device__ __forceinline__ void seg_advance(Seg& s)
     for (int a = 0; a < 3; ++a) s.root[a] = __fadd_rn(s.root[a], s.dir[a]); // root += direction
 }
 
+// The set-up of a pair, stored once by the counting bin pass.
+__device__ __forceinline__ void seg_store(const Seg& s, float4* rec)
+{
+    rec[0] = make_float4(s.root[0], s.root[1], s.root[2], __uint_as_float(s.n));
+    rec[1] = make_float4(s.dir[0], s.dir[1], s.dir[2], 0.0f);
+}
+
+__device__ __forceinline__ void seg_load(const float4* __restrict__ rec, Seg& s)
+{
+    const float4 a = __ldg(rec), b = __ldg(rec + 1);
+    s.root[0] = a.x;
+    s.root[1] = a.y;
+    s.root[2] = a.z;
+    s.n = __float_as_uint(a.w);
+    s.dir[0] = b.x;
+    s.dir[1] = b.y;
+    s.dir[2] = b.z;
+}
+
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
 // ---- brick path -----------------------------------------------------------------
 
-// A run of `len` consecutive visits (steps k0 .. k0+len-1 of pair / vertex p)
-// inside brick b: counted (FILL = false) or written to the brick's slice.
+// A run of `len` consecutive visits inside brick b -- steps k0 .. k0+len-1 of
+// pair p (payload k0 << 8 | len), or vertex p alone (payload = its local
+// voxel) -- counted (FILL = false) or written to the brick's slice.
 template <bool FILL>
-__device__ __forceinline__ void emit_run(uint32_t b, uint32_t p, uint32_t k0, uint32_t len, uint32_t* runs,
+__device__ __forceinline__ void emit_run(uint32_t b, uint32_t p, uint32_t payload, uint32_t len, uint32_t* runs,
                                          uint32_t* visits, uint32_t* cursor, uint2* items, size_t items_cap,
                                          unsigned& status)
 {
@@ -175,21 +199,26 @@ __device__ __forceinline__ void emit_run(uint32_t b, uint32_t p, uint32_t k0, ui
         if ((int)lane_id() == leader) base = atomicAdd(cursor + b, (uint32_t)__popc(peers));
         base = __shfl_sync(peers, base, leader);
         const uint32_t slot = base + __popc(peers & ((1u << lane_id()) - 1u));
-        if (slot < items_cap) items[slot] = make_uint2(p, (k0 << 8) | len);
+        if (slot < items_cap) items[slot] = make_uint2(p, payload);
         else status |= VKHR_DEV_LIST_OVERFLOW;
     }
 }
 
 template <bool FILL, bool SEG>
 __global__ void bin_kernel(Grid g, const float* __restrict__ v, const uint2* __restrict__ pairs, uint32_t n_in,
-                           uint32_t* runs, uint32_t* visits, uint32_t* cursor, uint2* items, size_t items_cap,
-                           unsigned long long* words)
+                           float4* pair_rec, uint32_t* runs, uint32_t* visits, uint32_t* cursor, uint2* items,
+                           size_t items_cap, unsigned long long* words)
 {
     unsigned status = 0;
     for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n_in; p += (uint64_t)gridDim.x * blockDim.x) {
         if (SEG) {
             Seg s;
-            if (!seg_setup(g, v, __ldg(pairs + p), s, status)) continue;
+            if (FILL) {
+                seg_load(pair_rec + 2 * p, s);
+            } else {
+                seg_setup(g, v, __ldg(pairs + p), s, status);
+                seg_store(s, pair_rec + 2 * p);
+            }
             uint32_t cur = kNoBrick, k0 = 0, len = 0;
             for (uint32_t k = 0; k < s.n; ++k) {
                 Visit o;
@@ -197,18 +226,21 @@ __global__ void bin_kernel(Grid g, const float* __restrict__ v, const uint2* __r
                 if (ok && o.brick == cur && len < 255u) {
                     ++len;
                 } else {
-                    if (len) emit_run<FILL>(cur, (uint32_t)p, k0, len, runs, visits, cursor, items, items_cap, status);
+                    if (len)
+                        emit_run<FILL>(cur, (uint32_t)p, (k0 << 8) | len, len, runs, visits, cursor, items, items_cap,
+                                       status);
                     cur = ok ? o.brick : kNoBrick;
                     k0 = k;
                     len = ok ? 1u : 0u;
                 }
                 seg_advance(s);
             }
-            if (len) emit_run<FILL>(cur, (uint32_t)p, k0, len, runs, visits, cursor, items, items_cap, status);
+            if (len)
+                emit_run<FILL>(cur, (uint32_t)p, (k0 << 8) | len, len, runs, visits, cursor, items, items_cap, status);
         } else {
             Visit o;
             if (vertex_visit(g, v, (uint32_t)p, o))
-                emit_run<FILL>(o.brick, (uint32_t)p, 0u, 1u, runs, visits, cursor, items, items_cap, status);
+                emit_run<FILL>(o.brick, (uint32_t)p, o.local, 1u, runs, visits, cursor, items, items_cap, status);
         }
     }
     if (status) atomicOr(words + WORD_STATUS, (unsigned long long)status);
@@ -218,7 +250,8 @@ __global__ void bin_kernel(Grid g, const float* __restrict__ v, const uint2* __r
 // totals: runs, visits and the largest brick.
 __global__ void __launch_bounds__(kRangeThreads) bin_ranges_kernel(const uint32_t* __restrict__ runs,
                                                                  const uint32_t* __restrict__ visits, uint32_t nb,
-                                                                 uint32_t* cursor, unsigned long long* words)
+                                                                 uint32_t* cursor, uint32_t* list,
+                                                                 unsigned long long* words)
 {
     __shared__ uint32_t warp_sums[kRangeThreads / 32];
     __shared__ uint32_t block_base;
@@ -270,8 +303,30 @@ __global__ void __launch_bounds__(kRangeThreads) bin_ranges_kernel(const uint32_
             const uint64_t i = base + (uint64_t)j * kRangeThreads + threadIdx.x;
             if (i < nb) cursor[i] = start;
             start += c[j];
+            // bricks for the shared-memory resolve: visited, within capacity
+            const uint32_t vv = i < nb ? __ldg(visits + i) : 0u;
+            const bool listed = vv > 0u && vv <= (uint32_t)kBrickCap;
+            const unsigned m = __ballot_sync(0xffffffffu, listed);
+            uint32_t at = 0;
+            if (lane == 0 && m) at = (uint32_t)atomicAdd(words + WORD_BRICK_LIST, (unsigned long long)__popc(m));
+            at = __shfl_sync(0xffffffffu, at, 0);
+            if (listed) list[at + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
         }
         __syncthreads();
+    }
+}
+
+// Zeroes every voxel of the bricks no visit reached (visited bricks are
+// written by the brick kernel or the global path).
+__global__ void zero_empty_kernel(Grid g, const uint32_t* __restrict__ visits, uint32_t* counts, uint8_t* dens,
+                                  uint32_t* tq)
+{
+    for (uint64_t vi = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; vi < g.n; vi += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t z = (uint32_t)(vi / g.wh), r = (uint32_t)(vi - (uint64_t)z * g.wh), y = r / g.w, x = r - y * g.w;
+        if (__ldg(visits + (x >> 3) + g.nbx * ((y >> 3) + g.nby * (z >> 3)))) continue;
+        counts[vi] = 0u;
+        if (dens) dens[vi] = 0;
+        if (tq) tq[vi] = 0u;
     }
 }
 
@@ -298,13 +353,12 @@ __device__ __forceinline__ uint32_t pack_tangent(float sx, float sy, float sz, u
 
 // Replays run item `it` of brick b and calls f(local, key) per visit.
 template <bool SEG, class F>
-__device__ __forceinline__ void replay(const Grid& g, const float* __restrict__ v, const uint2* __restrict__ pairs,
-                                       uint2 it, uint32_t b, unsigned& status, F&& f)
+__device__ __forceinline__ void replay(const Grid& g, const float4* __restrict__ pair_rec, uint2 it, uint32_t b,
+                                       unsigned& status, F&& f)
 {
     if (SEG) {
         Seg s;
-        unsigned ignore = 0;
-        if (!seg_setup(g, v, __ldg(pairs + it.x), s, ignore)) return;
+        seg_load(pair_rec + 2 * (size_t)it.x, s);
         const uint32_t k0 = it.y >> 8, len = it.y & 255u;
         for (uint32_t k = 0; k < k0; ++k) seg_advance(s);
         for (uint32_t k = 0; k < len; ++k) {
@@ -314,9 +368,7 @@ __device__ __forceinline__ void replay(const Grid& g, const float* __restrict__ 
             seg_advance(s);
         }
     } else {
-        Visit o;
-        if (vertex_visit(g, v, it.x, o) && o.brick == b) f(o.local, it.x);
-        else status |= VKHR_DEV_REPLAY_MISMATCH;
+        f(it.y & 511u, it.x); // vertex items carry their voxel
     }
 }
 
@@ -348,8 +400,8 @@ __device__ __forceinline__ uint32_t block_exclusive_scan_512(uint32_t x, uint32_
 
 template <bool SEG, bool TANG>
 __global__ void __launch_bounds__(kBrickThreads, 2)
-brick_kernel(Grid g, const float* __restrict__ v, const float* __restrict__ tan, const uint2* __restrict__ pairs,
-             const uint32_t* __restrict__ runs, const uint32_t* __restrict__ cursor, const uint32_t* __restrict__ visits,
+brick_kernel(Grid g, const float4* __restrict__ pair_rec, const float* __restrict__ tan, const uint2* __restrict__ pairs,
+             const uint32_t* __restrict__ runs, const uint32_t* __restrict__ cursor, const uint32_t* __restrict__ list,
              const uint2* __restrict__ items, uint32_t* counts, uint8_t* dens, uint32_t* tq, uint4* hdesc,
              size_t hdesc_cap, uint32_t* hkeys, size_t hkeys_cap, unsigned long long* words)
 {
@@ -361,32 +413,29 @@ brick_kernel(Grid g, const float* __restrict__ v, const float* __restrict__ tan,
     __shared__ uint32_t next;
     const int tid = threadIdx.x;
     unsigned status = 0;
+    const uint32_t listed = (uint32_t)words[WORD_BRICK_LIST];
     for (;;) {
         if (tid == 0) next = (uint32_t)atomicAdd(words + WORD_BRICK_QUEUE, 1ull);
         __syncthreads();
-        const uint32_t b = next;
+        const uint32_t q = next;
         __syncthreads();
-        if (b >= g.nb) break;
-        const uint32_t V = visits[b];
-        if (V > (uint32_t)kBrickCap) continue; // resolved by the global path
+        if (q >= listed) break;
+        const uint32_t b = list[q];              // visited, and within kBrickCap
         const uint32_t nit = runs[b], start = cursor[b] - nit;
         cnt[tid] = 0;
         __syncthreads();
-        if (V) {
-            for (uint32_t i = tid; i < nit; i += kBrickThreads)
-                replay<SEG>(g, v, pairs, items[start + i], b, status,
-                            [&](uint32_t l, uint32_t) { atomicAdd(cnt + l, 1u); });
+        for (uint32_t i = tid; i < nit; i += kBrickThreads)
+            replay<SEG>(g, pair_rec, items[start + i], b, status, [&](uint32_t l, uint32_t) { atomicAdd(cnt + l, 1u); });
+        __syncthreads();
+        if (TANG) {
+            off[tid] = block_exclusive_scan_512(cnt[tid], warp_sums);
             __syncthreads();
-            if (TANG) {
-                off[tid] = block_exclusive_scan_512(cnt[tid], warp_sums);
-                __syncthreads();
-                for (uint32_t i = tid; i < nit; i += kBrickThreads)
-                    replay<SEG>(g, v, pairs, items[start + i], b, status, [&](uint32_t l, uint32_t key) {
-                        const uint32_t slot = atomicAdd(off + l, 1u);
-                        if (slot < (uint32_t)kBrickCap) keys[slot] = key;
-                    });
-                __syncthreads();
-            }
+            for (uint32_t i = tid; i < nit; i += kBrickThreads)
+                replay<SEG>(g, pair_rec, items[start + i], b, status, [&](uint32_t l, uint32_t key) {
+                    const uint32_t slot = atomicAdd(off + l, 1u);
+                    if (slot < (uint32_t)kBrickCap) keys[slot] = key;
+                });
+            __syncthreads();
         }
         const uint32_t bx = b % g.nbx, by = (b / g.nbx) % g.nby, bz = b / (g.nbx * g.nby);
         const uint32_t x = bx * 8 + (tid & 7), y = by * 8 + ((tid >> 3) & 7), z = bz * 8 + (tid >> 6);
@@ -810,14 +859,14 @@ vkhr_status check_device_status(vkhr_ctx* ctx, unsigned long long s)
 }
 
 template <bool SEG, bool TANG>
-vkhr_status launch_brick(vkhr_ctx* ctx, const Grid& g, const float* v, const float* tan_in, const uint2* pairs,
-                         uint32_t* counts, uint8_t* dens, uint32_t* tq, cudaStream_t st, unsigned blocks, size_t smem)
+vkhr_status launch_brick(vkhr_ctx* ctx, const Grid& g, const float* tan_in, const uint2* pairs, uint32_t* counts,
+                         uint8_t* dens, uint32_t* tq, cudaStream_t st, unsigned blocks, size_t smem)
 {
     VKHR_CUDA_TRY(ctx, cudaFuncSetAttribute(brick_kernel<SEG, TANG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)smem));
-    VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG>), blocks, kBrickThreads, smem, st, g, v, tan_in, pairs, ctx->brick_runs,
-                ctx->brick_cursor, ctx->brick_visits, ctx->items, counts, dens, tq, ctx->hdesc, ctx->hdesc_cap,
-                ctx->hkeys, ctx->hkeys_cap, ctx->d_words);
+    VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG>), blocks, kBrickThreads, smem, st, g, ctx->pair_rec, tan_in, pairs,
+                ctx->brick_runs, ctx->brick_cursor, ctx->brick_list, ctx->items, counts, dens, tq, ctx->hdesc,
+                ctx->hdesc_cap, ctx->hkeys, ctx->hkeys_cap, ctx->d_words);
     return VKHR_OK;
 }
 
@@ -849,21 +898,29 @@ vkhr_status voxelize_impl(vkhr_ctx* ctx, bool segments, const float* v, const fl
     if (s != VKHR_OK) return s;
     ctx->brick_visits = ctx->brick_runs + g.nb;
     ctx->brick_cursor = ctx->brick_runs + 2ull * g.nb;
+    s = vkhr_reserve(ctx, (void**)&ctx->brick_list, &ctx->brick_list_cap, g.nb, sizeof(uint32_t));
+    if (s != VKHR_OK) return s;
+    if (segments && n_in) {
+        s = vkhr_reserve(ctx, (void**)&ctx->pair_rec, &ctx->pair_rec_cap, 2ull * n_in, sizeof(float4));
+        if (s != VKHR_OK) return s;
+    }
     VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_words, 0, WORD_NORM * sizeof(unsigned long long), st));
     VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->brick_runs, 0, 2ull * g.nb * sizeof(uint32_t), st));
     const unsigned threads = 256;
     const unsigned in_blocks = std::min(vkhr_blocks(n_in, threads), (unsigned)ctx->sm_count * 16);
     if (n_in) {
         if (segments)
-            VKHR_LAUNCH(ctx, (bin_kernel<false, true>), in_blocks, threads, 0, st, g, v, pairs, n_in, ctx->brick_runs,
+            VKHR_LAUNCH(ctx, (bin_kernel<false, true>), in_blocks, threads, 0, st, g, v, pairs, n_in, ctx->pair_rec, ctx->brick_runs,
                         ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap, ctx->d_words);
         else
-            VKHR_LAUNCH(ctx, (bin_kernel<false, false>), in_blocks, threads, 0, st, g, v, pairs, n_in, ctx->brick_runs,
+            VKHR_LAUNCH(ctx, (bin_kernel<false, false>), in_blocks, threads, 0, st, g, v, pairs, n_in, ctx->pair_rec, ctx->brick_runs,
                         ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap, ctx->d_words);
     }
     const unsigned rblocks = std::min(vkhr_blocks(g.nb, kRangeThreads * kRangeItems), (unsigned)ctx->sm_count * 8);
     VKHR_LAUNCH(ctx, bin_ranges_kernel, rblocks, kRangeThreads, 0, st, ctx->brick_runs, ctx->brick_visits, g.nb,
-                ctx->brick_cursor, ctx->d_words);
+                ctx->brick_cursor, ctx->brick_list, ctx->d_words);
+    const unsigned zblocks = std::min(vkhr_blocks(g.n, threads), (unsigned)ctx->sm_count * 32);
+    VKHR_LAUNCH(ctx, zero_empty_kernel, zblocks, threads, 0, st, g, ctx->brick_visits, counts, dens, tq32);
     VKHR_CUDA_TRY(ctx, cudaGetLastError());
 
     // Sizes of the run list and the crowded-voxel buffers.  Vertex mode is
@@ -927,20 +984,20 @@ vkhr_status voxelize_impl(vkhr_ctx* ctx, bool segments, const float* v, const fl
     }
     if (n_in) {
         if (segments)
-            VKHR_LAUNCH(ctx, (bin_kernel<true, true>), in_blocks, threads, 0, st, g, v, pairs, n_in, ctx->brick_runs,
+            VKHR_LAUNCH(ctx, (bin_kernel<true, true>), in_blocks, threads, 0, st, g, v, pairs, n_in, ctx->pair_rec, ctx->brick_runs,
                         ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap, ctx->d_words);
         else
-            VKHR_LAUNCH(ctx, (bin_kernel<true, false>), in_blocks, threads, 0, st, g, v, pairs, n_in, ctx->brick_runs,
+            VKHR_LAUNCH(ctx, (bin_kernel<true, false>), in_blocks, threads, 0, st, g, v, pairs, n_in, ctx->pair_rec, ctx->brick_runs,
                         ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap, ctx->d_words);
     }
     const size_t smem = (size_t)(2 * kBrickThreads + 32 + (tang ? kBrickCap : 0)) * sizeof(uint32_t);
     const unsigned bblocks = std::min(g.nb, (unsigned)ctx->sm_count * 2);
     if (segments)
-        s = tang ? launch_brick<true, true>(ctx, g, v, tan_in, pairs, counts, dens, tq32, st, bblocks, smem)
-                 : launch_brick<true, false>(ctx, g, v, tan_in, pairs, counts, dens, tq32, st, bblocks, smem);
+        s = tang ? launch_brick<true, true>(ctx, g, tan_in, pairs, counts, dens, tq32, st, bblocks, smem)
+                 : launch_brick<true, false>(ctx, g, tan_in, pairs, counts, dens, tq32, st, bblocks, smem);
     else
-        s = tang ? launch_brick<false, true>(ctx, g, v, tan_in, pairs, counts, dens, tq32, st, bblocks, smem)
-                 : launch_brick<false, false>(ctx, g, v, tan_in, pairs, counts, dens, tq32, st, bblocks, smem);
+        s = tang ? launch_brick<false, true>(ctx, g, tan_in, pairs, counts, dens, tq32, st, bblocks, smem)
+                 : launch_brick<false, false>(ctx, g, tan_in, pairs, counts, dens, tq32, st, bblocks, smem);
     if (s != VKHR_OK) return s;
     if (tang)
         VKHR_LAUNCH(ctx, crowded_kernel, (unsigned)ctx->sm_count * 2, 256, 0, st, ctx->hdesc, ctx->hdesc_cap, ctx->hkeys,
