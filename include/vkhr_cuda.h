@@ -248,6 +248,26 @@ vkhr_status vkhr_raymarch(vkhr_ctx* ctx, const vkhr_raymarch_params* params,
                           const void* d_density, const void* d_tangent, const float* d_depth_in,
                           float* d_rgba, float* d_depth_out, void* stream);
 
+/* Allocation-free raymarch.  No counterpart in the reference: it exists for
+ * callers that may not allocate device memory at all -- a real-time frame
+ * loop that forbids cudaMalloc (which synchronises the device and takes an
+ * unbounded time), or a host engine that owns the whole GPU memory budget and
+ * does not let plugins allocate.  Same inputs, outputs and results as
+ * vkhr_raymarch, but no context: the raymarch's only scratch (its brick
+ * occupancy bitmap) lives in a fixed 128 KiB array inside the library that
+ * every device loading the library holds until the process exits.
+ *   - Limit: ((w+8)/8) * ((h+8)/8) * ((d+8)/8) <= 1,048,576 occupancy bricks
+ *     (volumes up to about 800^3); larger grids return VKHR_ERR_CAPACITY.
+ *   - The first call on a device looks up the array's device address (and
+ *     the SM count); make that first call before any stream capture.
+ *   - All calls share the one array and it keeps the previous call's bits
+ *     (each call clears the part it uses): calls that can overlap on the GPU
+ *     (different streams, or different host threads) race; order them.
+ *   - Allocates nothing: no cudaMalloc/cudaFree, no allocating library call.
+ *   - Status only (no context, so no vkhr_last_error text). */
+vkhr_status vkhr_raymarch_static(const vkhr_raymarch_params* params, const void* d_density, const void* d_tangent,
+                                 const float* d_depth_in, float* d_rgba, float* d_depth_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

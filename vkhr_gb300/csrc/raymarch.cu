@@ -19,6 +19,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 
 namespace {
 
@@ -567,4 +568,87 @@ extern "C" vkhr_status vkhr_raymarch(vkhr_ctx* ctx, const vkhr_raymarch_params* 
         s = launch<VKHR_DENSITY_F32, VKHR_TANGENT_F32X4>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
     VKHR_CUDA_TRY(ctx, cudaGetLastError());
     return VKHR_OK;
+}
+
+// ---- raymarch without allocations ---------------------------------------------------------
+// For callers that may not allocate device memory at all: a real-time frame
+// loop that forbids cudaMalloc (it synchronises the device and its latency is
+// unbounded), or a host engine that owns the GPU memory budget and does not
+// let plugins allocate.  The only scratch the raymarch needs, the brick
+// occupancy bitmap, lives in a fixed array in the library's device image.
+namespace {
+
+constexpr size_t kStaticOccupancyWords = 32768; // 128 KiB: up to 1,048,576 occupancy bricks
+constexpr int kMaxStaticDevices = 64;
+
+__device__ __align__(256) uint32_t g_static_occupancy[kStaticOccupancyWords];
+
+std::once_flag g_static_once[kMaxStaticDevices];
+uint32_t* g_static_occupancy_ptr[kMaxStaticDevices];
+int g_static_sm_count[kMaxStaticDevices];
+cudaError_t g_static_error[kMaxStaticDevices];
+
+template <int DF, int TF>
+cudaError_t launch_static(const RayConsts& c, const void* dens, const void* tang, const float* din, float* rgba,
+                          float* dout, uint32_t* occ, size_t words, int sm_count, cudaStream_t st)
+{
+    // the array keeps the previous call's bits: clear the part this grid uses
+    cudaError_t e = cudaMemsetAsync(occ, 0, words * sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    const size_t bricks = (size_t)c.nb[0] * c.nb[1] * c.nb[2];
+    const unsigned oblocks = (unsigned)std::min<size_t>((bricks + 7) / 8, (size_t)sm_count * 32);
+    occupancy_kernel<DF><<<oblocks, 256, 0, st>>>((const typename DensityTexel<DF>::T*)dens, c.res[0], c.res[1],
+                                                   c.res[2], c.nb[0], c.nb[1], c.nb[2], occ);
+    const dim3 block(32 * kWarpsX * kWarpsY);
+    const dim3 grid((c.W + kTileW * kWarpsX - 1) / (kTileW * kWarpsX), (c.H + kTileH * kWarpsY - 1) / (kTileH * kWarpsY));
+    raymarch_kernel<DF, TF><<<grid, block, 0, st>>>(c, (const typename DensityTexel<DF>::T*)dens, tang, occ, din,
+                                                     reinterpret_cast<float4*>(rgba), dout);
+    return cudaGetLastError();
+}
+
+} // namespace
+
+extern "C" vkhr_status vkhr_raymarch_static(const vkhr_raymarch_params* params, const void* d_density,
+                                            const void* d_tangent, const float* d_depth_in, float* d_rgba,
+                                            float* d_depth_out, void* stream)
+{
+    if (!params || !d_density || !d_tangent || !d_rgba) return VKHR_ERR_INVALID_ARG;
+    if (reinterpret_cast<uintptr_t>(d_rgba) & 15u) return VKHR_ERR_INVALID_ARG;
+    const size_t tan_align = params->tangent_format == VKHR_TANGENT_I8_SNORM ? 4 : 16;
+    if (reinterpret_cast<uintptr_t>(d_tangent) & (tan_align - 1)) return VKHR_ERR_INVALID_ARG;
+    RayConsts c;
+    vkhr_status s = make_consts(nullptr, params, c);
+    if (s != VKHR_OK) return s;
+    const size_t bricks = (size_t)c.nb[0] * c.nb[1] * c.nb[2];
+    const size_t words = (bricks + 31) / 32;
+    if (words > kStaticOccupancyWords) return VKHR_ERR_CAPACITY; // grid above the fixed scratch (~800^3)
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return VKHR_ERR_CUDA;
+    if (dev < 0 || dev >= kMaxStaticDevices) return VKHR_ERR_NOT_SUPPORTED;
+    // first call on this device: resolve the array's device address (host
+    // code cannot use the symbol itself) and the SM count
+    std::call_once(g_static_once[dev], [dev]() {
+        cudaError_t e = cudaGetSymbolAddress((void**)&g_static_occupancy_ptr[dev], g_static_occupancy);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g_static_sm_count[dev], cudaDevAttrMultiProcessorCount, dev);
+        g_static_error[dev] = e;
+    });
+    if (g_static_error[dev] != cudaSuccess) return VKHR_ERR_CUDA;
+    uint32_t* occ = g_static_occupancy_ptr[dev];
+    const int sms = g_static_sm_count[dev];
+    cudaStream_t st = (cudaStream_t)stream;
+    const int df = params->density_format, tf = params->tangent_format;
+    cudaError_t e;
+    if (df == VKHR_DENSITY_U8_UNORM && tf == VKHR_TANGENT_I8_SNORM)
+        e = launch_static<VKHR_DENSITY_U8_UNORM, VKHR_TANGENT_I8_SNORM>(c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, occ, words, sms, st);
+    else if (df == VKHR_DENSITY_U8_UNORM)
+        e = launch_static<VKHR_DENSITY_U8_UNORM, VKHR_TANGENT_F32X4>(c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, occ, words, sms, st);
+    else if (df == VKHR_DENSITY_U32_COUNT && tf == VKHR_TANGENT_I8_SNORM)
+        e = launch_static<VKHR_DENSITY_U32_COUNT, VKHR_TANGENT_I8_SNORM>(c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, occ, words, sms, st);
+    else if (df == VKHR_DENSITY_U32_COUNT)
+        e = launch_static<VKHR_DENSITY_U32_COUNT, VKHR_TANGENT_F32X4>(c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, occ, words, sms, st);
+    else if (tf == VKHR_TANGENT_I8_SNORM)
+        e = launch_static<VKHR_DENSITY_F32, VKHR_TANGENT_I8_SNORM>(c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, occ, words, sms, st);
+    else
+        e = launch_static<VKHR_DENSITY_F32, VKHR_TANGENT_F32X4>(c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, occ, words, sms, st);
+    return e == cudaSuccess ? VKHR_OK : VKHR_ERR_CUDA;
 }
