@@ -49,6 +49,8 @@ struct vkhr_ctx {
     size_t brick_list_cap;
     float4* pair_rec;          // voxelizer: per index pair {root.xyz, steps}, {direction.xyz, 0}
     size_t pair_rec_cap;
+    float4* pair_tan;          // voxelizer: per index pair, the tangent of its first vertex
+    size_t pair_tan_cap;
     uint32_t* hkeys;           // voxelizer: keys of crowded voxels
     size_t hkeys_cap;
     uint4* hdesc;              // voxelizer: crowded voxels (voxel, key offset, count)

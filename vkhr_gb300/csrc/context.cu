@@ -133,7 +133,7 @@ vkhr_status vkhr_destroy(vkhr_ctx* ctx)
     if (!ctx) return VKHR_OK;
     cudaSetDevice(ctx->device);
     cudaDeviceSynchronize();
-    void* bufs[] = {ctx->brick_runs, ctx->items, ctx->brick_list, ctx->pair_rec, ctx->hkeys, ctx->hdesc,
+    void* bufs[] = {ctx->brick_runs, ctx->items, ctx->brick_list, ctx->pair_rec, ctx->pair_tan, ctx->hkeys, ctx->hdesc,
                     ctx->cursor, ctx->list, ctx->gdesc};
     for (void* b : bufs)
         if (b) cudaFree(b);

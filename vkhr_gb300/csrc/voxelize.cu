@@ -206,8 +206,9 @@ __device__ __forceinline__ void emit_run(uint32_t b, uint32_t p, uint32_t payloa
 
 template <bool FILL, bool SEG>
 __global__ void bin_kernel(Grid g, const float* __restrict__ v, const uint2* __restrict__ pairs, uint32_t n_in,
-                           float4* pair_rec, uint32_t* runs, uint32_t* visits, uint32_t* cursor, uint2* items,
-                           size_t items_cap, unsigned long long* words)
+                           const float* __restrict__ tan_in, float4* pair_rec, float4* pair_tan, uint32_t* runs,
+                           uint32_t* visits, uint32_t* cursor, uint2* items, size_t items_cap,
+                           unsigned long long* words)
 {
     unsigned status = 0;
     for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n_in; p += (uint64_t)gridDim.x * blockDim.x) {
@@ -216,8 +217,12 @@ __global__ void bin_kernel(Grid g, const float* __restrict__ v, const uint2* __r
             if (FILL) {
                 seg_load(pair_rec + 2 * p, s);
             } else {
-                seg_setup(g, v, __ldg(pairs + p), s, status);
+                const uint2 ij = __ldg(pairs + p);
+                seg_setup(g, v, ij, s, status);
                 seg_store(s, pair_rec + 2 * p);
+                if (tan_in) // tangents[indices[i]]: every visit of the pair adds this one
+                    pair_tan[p] = make_float4(__ldg(tan_in + 3 * (size_t)ij.x), __ldg(tan_in + 3 * (size_t)ij.x + 1),
+                                              __ldg(tan_in + 3 * (size_t)ij.x + 2), 0.0f);
             }
             uint32_t cur = kNoBrick, k0 = 0, len = 0;
             for (uint32_t k = 0; k < s.n; ++k) {
@@ -317,17 +322,17 @@ __global__ void __launch_bounds__(kRangeThreads) bin_ranges_kernel(const uint32_
 }
 
 // Zeroes every voxel of the bricks no visit reached (visited bricks are
-// written by the brick kernel or the global path).
+// written by the brick kernel or the global path).  Grid: (x chunks, y, z).
 __global__ void zero_empty_kernel(Grid g, const uint32_t* __restrict__ visits, uint32_t* counts, uint8_t* dens,
                                   uint32_t* tq)
 {
-    for (uint64_t vi = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; vi < g.n; vi += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t z = (uint32_t)(vi / g.wh), r = (uint32_t)(vi - (uint64_t)z * g.wh), y = r / g.w, x = r - y * g.w;
-        if (__ldg(visits + (x >> 3) + g.nbx * ((y >> 3) + g.nby * (z >> 3)))) continue;
-        counts[vi] = 0u;
-        if (dens) dens[vi] = 0;
-        if (tq) tq[vi] = 0u;
-    }
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+    if (x >= g.w) return;
+    if (__ldg(visits + (x >> 3) + g.nbx * ((y >> 3) + g.nby * (z >> 3)))) return;
+    const size_t vi = x + (size_t)g.w * (y + (size_t)g.h * z);
+    counts[vi] = 0u;
+    if (dens) dens[vi] = 0;
+    if (tq) tq[vi] = 0u;
 }
 
 // Tangent of a visit key: the vertex's own (voxelize_vertices) or the pair's
@@ -400,7 +405,8 @@ __device__ __forceinline__ uint32_t block_exclusive_scan_512(uint32_t x, uint32_
 
 template <bool SEG, bool TANG>
 __global__ void __launch_bounds__(kBrickThreads, 2)
-brick_kernel(Grid g, const float4* __restrict__ pair_rec, const float* __restrict__ tan, const uint2* __restrict__ pairs,
+brick_kernel(Grid g, const float4* __restrict__ pair_rec, const float4* __restrict__ pair_tan,
+             const float* __restrict__ tan, const uint2* __restrict__ pairs,
              const uint32_t* __restrict__ runs, const uint32_t* __restrict__ cursor, const uint32_t* __restrict__ list,
              const uint2* __restrict__ items, uint32_t* counts, uint8_t* dens, uint32_t* tq, uint4* hdesc,
              size_t hdesc_cap, uint32_t* hkeys, size_t hkeys_cap, unsigned long long* words)
@@ -458,12 +464,34 @@ brick_kernel(Grid g, const float4* __restrict__ pair_rec, const float* __restric
                         }
                         k[j] = key;
                     }
+                    // gather 8 tangents at a time (independent loads), then add them in key order
                     float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-                    for (uint32_t i = 0; i < c; ++i) {
-                        const float* t = tan + 3 * (size_t)key_vertex(k[i], SEG ? pairs : nullptr);
-                        sx = __fadd_rn(sx, __ldg(t + 0));
-                        sy = __fadd_rn(sy, __ldg(t + 1));
-                        sz = __fadd_rn(sz, __ldg(t + 2));
+                    for (uint32_t i0 = 0; i0 < c; i0 += 8) {
+                        float tx[8], ty[8], tz[8];
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) {
+                            if (i0 + j < c) {
+                                if (SEG) {
+                                    const float4 t = __ldg(pair_tan + k[i0 + j]);
+                                    tx[j] = t.x;
+                                    ty[j] = t.y;
+                                    tz[j] = t.z;
+                                } else {
+                                    const float* t = tan + 3 * (size_t)k[i0 + j];
+                                    tx[j] = __ldg(t);
+                                    ty[j] = __ldg(t + 1);
+                                    tz[j] = __ldg(t + 2);
+                                }
+                            }
+                        }
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) {
+                            if (i0 + j < c) {
+                                sx = __fadd_rn(sx, tx[j]);
+                                sy = __fadd_rn(sy, ty[j]);
+                                sz = __fadd_rn(sz, tz[j]);
+                            }
+                        }
                     }
                     tq[vi] = pack_tangent(sx, sy, sz, c);
                 } else { // crowded: hand the keys to a CTA of its own
@@ -818,6 +846,7 @@ vkhr_status make_grid(vkhr_ctx* ctx, const vkhr_aabb* b, int32_t w, int32_t h, i
 {
     if (!b) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "bounds is NULL");
     if (w <= 0 || h <= 0 || d <= 0) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "resolution must be positive");
+    if (h > 65535 || d > 65535) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "height and depth must be <= 65535");
     const uint64_t n = (uint64_t)w * (uint64_t)h * (uint64_t)d;
     if (n >= (1ull << 32)) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "more than 2^32 - 1 voxels");
     if (mode != VKHR_INDEX_REF_FP32 && mode != VKHR_INDEX_EXACT)
@@ -864,7 +893,7 @@ vkhr_status launch_brick(vkhr_ctx* ctx, const Grid& g, const float* tan_in, cons
 {
     VKHR_CUDA_TRY(ctx, cudaFuncSetAttribute(brick_kernel<SEG, TANG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)smem));
-    VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG>), blocks, kBrickThreads, smem, st, g, ctx->pair_rec, tan_in, pairs,
+    VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG>), blocks, kBrickThreads, smem, st, g, ctx->pair_rec, ctx->pair_tan, tan_in, pairs,
                 ctx->brick_runs, ctx->brick_cursor, ctx->brick_list, ctx->items, counts, dens, tq, ctx->hdesc,
                 ctx->hdesc_cap, ctx->hkeys, ctx->hkeys_cap, ctx->d_words);
     return VKHR_OK;
@@ -903,6 +932,10 @@ vkhr_status voxelize_impl(vkhr_ctx* ctx, bool segments, const float* v, const fl
     if (segments && n_in) {
         s = vkhr_reserve(ctx, (void**)&ctx->pair_rec, &ctx->pair_rec_cap, 2ull * n_in, sizeof(float4));
         if (s != VKHR_OK) return s;
+        if (tang) {
+            s = vkhr_reserve(ctx, (void**)&ctx->pair_tan, &ctx->pair_tan_cap, n_in, sizeof(float4));
+            if (s != VKHR_OK) return s;
+        }
     }
     VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_words, 0, WORD_NORM * sizeof(unsigned long long), st));
     VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->brick_runs, 0, 2ull * g.nb * sizeof(uint32_t), st));
@@ -910,17 +943,19 @@ vkhr_status voxelize_impl(vkhr_ctx* ctx, bool segments, const float* v, const fl
     const unsigned in_blocks = std::min(vkhr_blocks(n_in, threads), (unsigned)ctx->sm_count * 16);
     if (n_in) {
         if (segments)
-            VKHR_LAUNCH(ctx, (bin_kernel<false, true>), in_blocks, threads, 0, st, g, v, pairs, n_in, ctx->pair_rec, ctx->brick_runs,
+            VKHR_LAUNCH(ctx, (bin_kernel<false, true>), in_blocks, threads, 0, st, g, v, pairs, n_in, tang ? tan_in : nullptr,
+                        ctx->pair_rec, ctx->pair_tan, ctx->brick_runs,
                         ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap, ctx->d_words);
         else
-            VKHR_LAUNCH(ctx, (bin_kernel<false, false>), in_blocks, threads, 0, st, g, v, pairs, n_in, ctx->pair_rec, ctx->brick_runs,
+            VKHR_LAUNCH(ctx, (bin_kernel<false, false>), in_blocks, threads, 0, st, g, v, pairs, n_in, tang ? tan_in : nullptr,
+                        ctx->pair_rec, ctx->pair_tan, ctx->brick_runs,
                         ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap, ctx->d_words);
     }
     const unsigned rblocks = std::min(vkhr_blocks(g.nb, kRangeThreads * kRangeItems), (unsigned)ctx->sm_count * 8);
     VKHR_LAUNCH(ctx, bin_ranges_kernel, rblocks, kRangeThreads, 0, st, ctx->brick_runs, ctx->brick_visits, g.nb,
                 ctx->brick_cursor, ctx->brick_list, ctx->d_words);
-    const unsigned zblocks = std::min(vkhr_blocks(g.n, threads), (unsigned)ctx->sm_count * 32);
-    VKHR_LAUNCH(ctx, zero_empty_kernel, zblocks, threads, 0, st, g, ctx->brick_visits, counts, dens, tq32);
+    VKHR_LAUNCH(ctx, zero_empty_kernel, dim3((g.w + 255) / 256, g.h, g.d), 256, 0, st, g, ctx->brick_visits, counts,
+                dens, tq32);
     VKHR_CUDA_TRY(ctx, cudaGetLastError());
 
     // Sizes of the run list and the crowded-voxel buffers.  Vertex mode is
@@ -984,10 +1019,12 @@ vkhr_status voxelize_impl(vkhr_ctx* ctx, bool segments, const float* v, const fl
     }
     if (n_in) {
         if (segments)
-            VKHR_LAUNCH(ctx, (bin_kernel<true, true>), in_blocks, threads, 0, st, g, v, pairs, n_in, ctx->pair_rec, ctx->brick_runs,
+            VKHR_LAUNCH(ctx, (bin_kernel<true, true>), in_blocks, threads, 0, st, g, v, pairs, n_in, tang ? tan_in : nullptr,
+                        ctx->pair_rec, ctx->pair_tan, ctx->brick_runs,
                         ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap, ctx->d_words);
         else
-            VKHR_LAUNCH(ctx, (bin_kernel<true, false>), in_blocks, threads, 0, st, g, v, pairs, n_in, ctx->pair_rec, ctx->brick_runs,
+            VKHR_LAUNCH(ctx, (bin_kernel<true, false>), in_blocks, threads, 0, st, g, v, pairs, n_in, tang ? tan_in : nullptr,
+                        ctx->pair_rec, ctx->pair_tan, ctx->brick_runs,
                         ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap, ctx->d_words);
     }
     const size_t smem = (size_t)(2 * kBrickThreads + 32 + (tang ? kBrickCap : 0)) * sizeof(uint32_t);
