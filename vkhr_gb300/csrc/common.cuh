@@ -24,7 +24,7 @@ enum {
     WORD_LIST_CURSOR = 1,       // global path: allocation cursor of the visit list
     WORD_HEAVY_COUNT = 2,       // global path: crowded-voxel descriptors
     WORD_STATUS = 3,            // VKHR_DEV_* bits
-    WORD_RUNS_TOTAL = 4,        // brick path: run items
+    WORD_BRICK_CURSOR = 4,      // brick path: allocation cursor of the visit list
     WORD_MAX_BRICK_VISITS = 5,  // brick path: largest brick
     WORD_BHEAVY_COUNT = 6,      // brick path: crowded-voxel descriptors
     WORD_HKEYS_CURSOR = 7,      // brick path: crowded-voxel key buffer cursor

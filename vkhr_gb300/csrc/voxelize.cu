@@ -11,21 +11,20 @@
 // Brick path (every voxel whose 8^3 brick receives <= kBrickCap visits):
 //   1. bin (count)  one thread per vertex / index pair walks its visits and
 //                   splits them into runs of consecutive visits inside one
-//                   brick; warp-aggregated atomics count runs and visits per
-//                   brick (32K bricks at 256^3, hot in L2).  A pair's set-up
-//                   (its root, direction and step count: nine IEEE divisions)
-//                   is stored once as a 32-byte record;
-//   2. bin ranges   each brick gets a slice of the run list; occupied bricks
-//                   are listed; empty bricks are zeroed by a streaming kernel;
-//   3. bin (fill)   the same walk again writes (pair, first step, length)
-//                   run items -- (vertex, voxel) items in vertex mode -- into
-//                   the bricks' slices;
-//   4. brick        one CTA per occupied brick replays its runs twice with the exact
-//                   stepping: counts per voxel in shared memory, then the
-//                   serial keys bucketed per voxel; each voxel's keys are
-//                   sorted in shared memory and its tangents summed in that
-//                   order; the brick's 512 counts, u8 densities and int8x4
-//                   tangents are written once;
+//                   brick; warp-aggregated atomics count visits per brick
+//                   (32K bricks at 256^3, hot in L2).  A pair's set-up (its
+//                   root, direction and step count: nine IEEE divisions) and
+//                   its first vertex's tangent are stored once;
+//   2. bin ranges   each brick gets a slice of the visit list; occupied
+//                   bricks are listed; empty bricks are zeroed by a streaming
+//                   kernel;
+//   3. bin (fill)   the same walk again reserves one slice range per run and
+//                   writes (serial key, local voxel) entries into it;
+//   4. brick        one CTA per occupied brick reads its entries twice: counts
+//                   per voxel in shared memory, then the keys bucketed per
+//                   voxel; each voxel's keys are sorted in shared memory and
+//                   its tangents summed in that order; the brick's 512
+//                   counts, u8 densities and int8x4 tangents are written once;
 //   5. crowded      voxels with > 64 visits: one CTA each sorts its keys in
 //                   shared-memory tiles (carrying the 256 smallest forward).
 // Global path (only bricks above kBrickCap): per-voxel global atomics, a
@@ -87,13 +86,16 @@ __device__ __forceinline__ bool linear_index(const Grid& g, float vx, float vy, 
 // reference forms it, and the brick/local position of that index.
 __device__ __forceinline__ bool locate(const Grid& g, float vx, float vy, float vz, Visit& o)
 {
-    if (!linear_index(g, vx, vy, vz, o.lin)) return false;
     uint32_t x, y, z;
     if (g.exact_coords && vx >= 0.0f && vy >= 0.0f && vz >= 0.0f) {
+        // coordinates in [0, res-1] (clamped above): the FP32 index of the
+        // reference is exact below 2^24 voxels, so it is this voxel's index
         x = (uint32_t)vx;
         y = (uint32_t)vy;
         z = (uint32_t)vz;
+        o.lin = x + g.w * (y + g.h * z);
     } else { // the FP32 index may have wrapped or rounded: decompose it
+        if (!linear_index(g, vx, vy, vz, o.lin)) return false;
         z = o.lin / g.wh;
         const uint32_t r = o.lin - z * g.wh;
         y = r / g.w;
@@ -178,37 +180,33 @@ __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
 // ---- brick path -----------------------------------------------------------------
 
-// A run of `len` consecutive visits inside brick b -- steps k0 .. k0+len-1 of
-// pair p (payload k0 << 8 | len), or vertex p alone (payload = its local
-// voxel) -- counted (FILL = false) or written to the brick's slice.
+// A run of `len` (<= 7) consecutive visits of one pair / vertex inside brick b,
+// their local voxels packed 9 bits each: counted per brick (FILL = false;
+// warp-aggregated), or written as (key, local voxel) entries into the
+// brick's slice of the visit list.
 template <bool FILL>
-__device__ __forceinline__ void emit_run(uint32_t b, uint32_t p, uint32_t payload, uint32_t len, uint32_t* runs,
-                                         uint32_t* visits, uint32_t* cursor, uint2* items, size_t items_cap,
-                                         unsigned& status)
+__device__ __forceinline__ void emit_run(uint32_t b, uint32_t key, uint64_t locals, uint32_t len, uint32_t* visits,
+                                         uint32_t* cursor, uint2* entries, size_t entries_cap, unsigned& status)
 {
-    const unsigned peers = __match_any_sync(__activemask(), b);
-    const int leader = __ffs(peers) - 1;
     if (!FILL) {
+        const unsigned peers = __match_any_sync(__activemask(), b);
         const unsigned tot = __reduce_add_sync(peers, len);
-        if ((int)lane_id() == leader) {
-            atomicAdd(runs + b, (uint32_t)__popc(peers));
-            atomicAdd(visits + b, tot);
-        }
+        if ((int)lane_id() == __ffs(peers) - 1) atomicAdd(visits + b, tot);
     } else {
-        uint32_t base = 0;
-        if ((int)lane_id() == leader) base = atomicAdd(cursor + b, (uint32_t)__popc(peers));
-        base = __shfl_sync(peers, base, leader);
-        const uint32_t slot = base + __popc(peers & ((1u << lane_id()) - 1u));
-        if (slot < items_cap) items[slot] = make_uint2(p, payload);
-        else status |= VKHR_DEV_LIST_OVERFLOW;
+        const uint32_t base = atomicAdd(cursor + b, len);
+        if ((uint64_t)base + len <= entries_cap) {
+            for (uint32_t j = 0; j < len; ++j) entries[base + j] = make_uint2(key, (uint32_t)(locals >> (9 * j)) & 511u);
+        } else {
+            status |= VKHR_DEV_LIST_OVERFLOW;
+        }
     }
 }
 
 template <bool FILL, bool SEG>
 __global__ void bin_kernel(Grid g, const float* __restrict__ v, const uint2* __restrict__ pairs, uint32_t n_in,
-                           const float* __restrict__ tan_in, float4* pair_rec, float4* pair_tan, uint32_t* runs,
-                           uint32_t* visits, uint32_t* cursor, uint2* items, size_t items_cap,
-                           unsigned long long* words)
+                           const float* __restrict__ tan_in,
+                           float4* pair_rec, float4* pair_tan, uint32_t* visits, uint32_t* cursor, uint2* entries,
+                           size_t entries_cap, unsigned long long* words)
 {
     unsigned status = 0;
     for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n_in; p += (uint64_t)gridDim.x * blockDim.x) {
@@ -224,37 +222,37 @@ __global__ void bin_kernel(Grid g, const float* __restrict__ v, const uint2* __r
                     pair_tan[p] = make_float4(__ldg(tan_in + 3 * (size_t)ij.x), __ldg(tan_in + 3 * (size_t)ij.x + 1),
                                               __ldg(tan_in + 3 * (size_t)ij.x + 2), 0.0f);
             }
-            uint32_t cur = kNoBrick, k0 = 0, len = 0;
+            uint32_t cur = kNoBrick, len = 0;
+            uint64_t locals = 0;
             for (uint32_t k = 0; k < s.n; ++k) {
                 Visit o;
                 const bool ok = seg_visit(g, s, o);
-                if (ok && o.brick == cur && len < 255u) {
+                if (ok && o.brick == cur && len < 7u) {
+                    locals |= (uint64_t)o.local << (9 * len);
                     ++len;
                 } else {
-                    if (len)
-                        emit_run<FILL>(cur, (uint32_t)p, (k0 << 8) | len, len, runs, visits, cursor, items, items_cap,
-                                       status);
+                    if (len) emit_run<FILL>(cur, (uint32_t)p, locals, len, visits, cursor, entries, entries_cap, status);
                     cur = ok ? o.brick : kNoBrick;
-                    k0 = k;
                     len = ok ? 1u : 0u;
+                    locals = ok ? (uint64_t)o.local : 0ull;
                 }
                 seg_advance(s);
             }
-            if (len)
-                emit_run<FILL>(cur, (uint32_t)p, (k0 << 8) | len, len, runs, visits, cursor, items, items_cap, status);
+            if (len) emit_run<FILL>(cur, (uint32_t)p, locals, len, visits, cursor, entries, entries_cap, status);
         } else {
             Visit o;
             if (vertex_visit(g, v, (uint32_t)p, o))
-                emit_run<FILL>(o.brick, (uint32_t)p, o.local, 1u, runs, visits, cursor, items, items_cap, status);
+                emit_run<FILL>(o.brick, (uint32_t)p, (uint64_t)o.local, 1u, visits, cursor, entries, entries_cap,
+                               status);
         }
     }
     if (status) atomicOr(words + WORD_STATUS, (unsigned long long)status);
 }
 
-// Slices of the run list per brick (one atomic per 4096 bricks), plus the
-// totals: runs, visits and the largest brick.
-__global__ void __launch_bounds__(kRangeThreads) bin_ranges_kernel(const uint32_t* __restrict__ runs,
-                                                                 const uint32_t* __restrict__ visits, uint32_t nb,
+// Slices of the visit list per brick (one atomic per 4096 bricks), the
+// visit total, the largest brick, and the list of bricks the shared-memory
+// resolve handles.
+__global__ void __launch_bounds__(kRangeThreads) bin_ranges_kernel(const uint32_t* __restrict__ visits, uint32_t nb,
                                                                  uint32_t* cursor, uint32_t* list,
                                                                  unsigned long long* words)
 {
@@ -268,11 +266,10 @@ __global__ void __launch_bounds__(kRangeThreads) bin_ranges_kernel(const uint32_
 #pragma unroll
         for (int j = 0; j < kRangeItems; ++j) {
             const uint64_t i = base + (uint64_t)j * kRangeThreads + threadIdx.x;
-            c[j] = i < nb ? __ldg(runs + i) : 0u;
-            const uint32_t vv = i < nb ? __ldg(visits + i) : 0u;
+            c[j] = i < nb ? __ldg(visits + i) : 0u;
             sum += c[j];
-            vsum += vv;
-            vmax = max(vmax, vv);
+            vsum += c[j];
+            vmax = max(vmax, c[j]);
         }
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         uint32_t incl = sum;
@@ -299,7 +296,7 @@ __global__ void __launch_bounds__(kRangeThreads) bin_ranges_kernel(const uint32_
                 warp_sums[w] = run;
                 run += t;
             }
-            block_base = run ? (uint32_t)atomicAdd(words + WORD_RUNS_TOTAL, (unsigned long long)run) : 0u;
+            block_base = run ? (uint32_t)atomicAdd(words + WORD_BRICK_CURSOR, (unsigned long long)run) : 0u;
         }
         __syncthreads();
         uint32_t start = block_base + warp_sums[warp] + (incl - sum);
@@ -309,8 +306,7 @@ __global__ void __launch_bounds__(kRangeThreads) bin_ranges_kernel(const uint32_
             if (i < nb) cursor[i] = start;
             start += c[j];
             // bricks for the shared-memory resolve: visited, within capacity
-            const uint32_t vv = i < nb ? __ldg(visits + i) : 0u;
-            const bool listed = vv > 0u && vv <= (uint32_t)kBrickCap;
+            const bool listed = c[j] > 0u && c[j] <= (uint32_t)kBrickCap;
             const unsigned m = __ballot_sync(0xffffffffu, listed);
             uint32_t at = 0;
             if (lane == 0 && m) at = (uint32_t)atomicAdd(words + WORD_BRICK_LIST, (unsigned long long)__popc(m));
@@ -356,27 +352,6 @@ __device__ __forceinline__ uint32_t pack_tangent(float sx, float sy, float sz, u
     return ((uint32_t)(x & 0xff)) | ((uint32_t)(y & 0xff) << 8) | ((uint32_t)(z & 0xff) << 16);
 }
 
-// Replays run item `it` of brick b and calls f(local, key) per visit.
-template <bool SEG, class F>
-__device__ __forceinline__ void replay(const Grid& g, const float4* __restrict__ pair_rec, uint2 it, uint32_t b,
-                                       unsigned& status, F&& f)
-{
-    if (SEG) {
-        Seg s;
-        seg_load(pair_rec + 2 * (size_t)it.x, s);
-        const uint32_t k0 = it.y >> 8, len = it.y & 255u;
-        for (uint32_t k = 0; k < k0; ++k) seg_advance(s);
-        for (uint32_t k = 0; k < len; ++k) {
-            Visit o;
-            if (seg_visit(g, s, o) && o.brick == b) f(o.local, it.x);
-            else status |= VKHR_DEV_REPLAY_MISMATCH;
-            seg_advance(s);
-        }
-    } else {
-        f(it.y & 511u, it.x); // vertex items carry their voxel
-    }
-}
-
 // Exclusive scan of 512 values, one per thread; `warp_sums` holds 16 words.
 __device__ __forceinline__ uint32_t block_exclusive_scan_512(uint32_t x, uint32_t* warp_sums)
 {
@@ -405,10 +380,9 @@ __device__ __forceinline__ uint32_t block_exclusive_scan_512(uint32_t x, uint32_
 
 template <bool SEG, bool TANG>
 __global__ void __launch_bounds__(kBrickThreads, 2)
-brick_kernel(Grid g, const float4* __restrict__ pair_rec, const float4* __restrict__ pair_tan,
-             const float* __restrict__ tan, const uint2* __restrict__ pairs,
-             const uint32_t* __restrict__ runs, const uint32_t* __restrict__ cursor, const uint32_t* __restrict__ list,
-             const uint2* __restrict__ items, uint32_t* counts, uint8_t* dens, uint32_t* tq, uint4* hdesc,
+brick_kernel(Grid g, const float4* __restrict__ pair_tan, const float* __restrict__ tan,
+             const uint32_t* __restrict__ visits, const uint32_t* __restrict__ cursor, const uint32_t* __restrict__ list,
+             const uint2* __restrict__ entries, uint32_t* counts, uint8_t* dens, uint32_t* tq, uint4* hdesc,
              size_t hdesc_cap, uint32_t* hkeys, size_t hkeys_cap, unsigned long long* words)
 {
     extern __shared__ uint32_t sm[];
@@ -427,20 +401,19 @@ brick_kernel(Grid g, const float4* __restrict__ pair_rec, const float4* __restri
         __syncthreads();
         if (q >= listed) break;
         const uint32_t b = list[q];              // visited, and within kBrickCap
-        const uint32_t nit = runs[b], start = cursor[b] - nit;
+        const uint32_t nv = visits[b], start = cursor[b] - nv;
         cnt[tid] = 0;
         __syncthreads();
-        for (uint32_t i = tid; i < nit; i += kBrickThreads)
-            replay<SEG>(g, pair_rec, items[start + i], b, status, [&](uint32_t l, uint32_t) { atomicAdd(cnt + l, 1u); });
+        for (uint32_t i = tid; i < nv; i += kBrickThreads) atomicAdd(cnt + (__ldg(&entries[start + i].y) & 511u), 1u);
         __syncthreads();
         if (TANG) {
             off[tid] = block_exclusive_scan_512(cnt[tid], warp_sums);
             __syncthreads();
-            for (uint32_t i = tid; i < nit; i += kBrickThreads)
-                replay<SEG>(g, pair_rec, items[start + i], b, status, [&](uint32_t l, uint32_t key) {
-                    const uint32_t slot = atomicAdd(off + l, 1u);
-                    if (slot < (uint32_t)kBrickCap) keys[slot] = key;
-                });
+            for (uint32_t i = tid; i < nv; i += kBrickThreads) {
+                const uint2 e = __ldg(entries + start + i);
+                const uint32_t slot = atomicAdd(off + (e.y & 511u), 1u);
+                if (slot < (uint32_t)kBrickCap) keys[slot] = e.x;
+            }
             __syncthreads();
         }
         const uint32_t bx = b % g.nbx, by = (b / g.nbx) % g.nby, bz = b / (g.nbx * g.nby);
@@ -888,13 +861,13 @@ vkhr_status check_device_status(vkhr_ctx* ctx, unsigned long long s)
 }
 
 template <bool SEG, bool TANG>
-vkhr_status launch_brick(vkhr_ctx* ctx, const Grid& g, const float* tan_in, const uint2* pairs, uint32_t* counts,
-                         uint8_t* dens, uint32_t* tq, cudaStream_t st, unsigned blocks, size_t smem)
+vkhr_status launch_brick(vkhr_ctx* ctx, const Grid& g, const float* tan_in, uint32_t* counts, uint8_t* dens,
+                         uint32_t* tq, cudaStream_t st, unsigned blocks, size_t smem)
 {
     VKHR_CUDA_TRY(ctx, cudaFuncSetAttribute(brick_kernel<SEG, TANG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)smem));
-    VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG>), blocks, kBrickThreads, smem, st, g, ctx->pair_rec, ctx->pair_tan, tan_in, pairs,
-                ctx->brick_runs, ctx->brick_cursor, ctx->brick_list, ctx->items, counts, dens, tq, ctx->hdesc,
+    VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG>), blocks, kBrickThreads, smem, st, g, ctx->pair_tan, tan_in,
+                ctx->brick_visits, ctx->brick_cursor, ctx->brick_list, ctx->items, counts, dens, tq, ctx->hdesc,
                 ctx->hdesc_cap, ctx->hkeys, ctx->hkeys_cap, ctx->d_words);
     return VKHR_OK;
 }
@@ -922,11 +895,11 @@ vkhr_status voxelize_impl(vkhr_ctx* ctx, bool segments, const float* v, const fl
     const bool tang = tq != nullptr;
     uint32_t* tq32 = reinterpret_cast<uint32_t*>(tq);
 
-    // per-brick bookkeeping: runs, visits, cursor
+    // per-brick bookkeeping: visits and visit-list cursor
     s = vkhr_reserve(ctx, (void**)&ctx->brick_runs, &ctx->brick_cap, 3ull * g.nb, sizeof(uint32_t));
     if (s != VKHR_OK) return s;
-    ctx->brick_visits = ctx->brick_runs + g.nb;
-    ctx->brick_cursor = ctx->brick_runs + 2ull * g.nb;
+    ctx->brick_visits = ctx->brick_runs;
+    ctx->brick_cursor = ctx->brick_runs + g.nb;
     s = vkhr_reserve(ctx, (void**)&ctx->brick_list, &ctx->brick_list_cap, g.nb, sizeof(uint32_t));
     if (s != VKHR_OK) return s;
     if (segments && n_in) {
@@ -937,30 +910,35 @@ vkhr_status voxelize_impl(vkhr_ctx* ctx, bool segments, const float* v, const fl
             if (s != VKHR_OK) return s;
         }
     }
+    if (!segments) { // vertex mode: every bound is the vertex count, no read-back needed
+        s = vkhr_reserve(ctx, (void**)&ctx->items, &ctx->items_cap, n_in ? n_in : 1, sizeof(uint2));
+        if (s != VKHR_OK) return s;
+    }
     VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_words, 0, WORD_NORM * sizeof(unsigned long long), st));
-    VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->brick_runs, 0, 2ull * g.nb * sizeof(uint32_t), st));
+    VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->brick_visits, 0, (size_t)g.nb * sizeof(uint32_t), st));
     const unsigned threads = 256;
     const unsigned in_blocks = std::min(vkhr_blocks(n_in, threads), (unsigned)ctx->sm_count * 16);
+    const float* tan_rec = tang ? tan_in : nullptr;
     if (n_in) {
         if (segments)
-            VKHR_LAUNCH(ctx, (bin_kernel<false, true>), in_blocks, threads, 0, st, g, v, pairs, n_in, tang ? tan_in : nullptr,
-                        ctx->pair_rec, ctx->pair_tan, ctx->brick_runs,
-                        ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap, ctx->d_words);
+            VKHR_LAUNCH(ctx, (bin_kernel<false, true>), in_blocks, threads, 0, st, g, v, pairs, n_in, tan_rec,
+                        ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap,
+                        ctx->d_words);
         else
-            VKHR_LAUNCH(ctx, (bin_kernel<false, false>), in_blocks, threads, 0, st, g, v, pairs, n_in, tang ? tan_in : nullptr,
-                        ctx->pair_rec, ctx->pair_tan, ctx->brick_runs,
-                        ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap, ctx->d_words);
+            VKHR_LAUNCH(ctx, (bin_kernel<false, false>), in_blocks, threads, 0, st, g, v, pairs, n_in, tan_rec,
+                        ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap,
+                        ctx->d_words);
     }
     const unsigned rblocks = std::min(vkhr_blocks(g.nb, kRangeThreads * kRangeItems), (unsigned)ctx->sm_count * 8);
-    VKHR_LAUNCH(ctx, bin_ranges_kernel, rblocks, kRangeThreads, 0, st, ctx->brick_runs, ctx->brick_visits, g.nb,
-                ctx->brick_cursor, ctx->brick_list, ctx->d_words);
+    VKHR_LAUNCH(ctx, bin_ranges_kernel, rblocks, kRangeThreads, 0, st, ctx->brick_visits, g.nb, ctx->brick_cursor,
+                ctx->brick_list, ctx->d_words);
     VKHR_LAUNCH(ctx, zero_empty_kernel, dim3((g.w + 255) / 256, g.h, g.d), 256, 0, st, g, ctx->brick_visits, counts,
                 dens, tq32);
     VKHR_CUDA_TRY(ctx, cudaGetLastError());
 
-    // Sizes of the run list and the crowded-voxel buffers.  Vertex mode is
-    // bounded by the vertex count; segment mode reads the totals back.
-    uint64_t runs_total = n_in, visits_total = n_in;
+    // Sizes of the visit list and the crowded-voxel buffers.  Vertex mode is
+    // bounded by the vertex count; segment mode reads the total back.
+    uint64_t visits_total = n_in;
     bool global_path = true; // vertex mode: launched, exits on the device when unneeded
     if (segments) {
         VKHR_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->h_words, ctx->d_words, WORD_NORM * sizeof(unsigned long long),
@@ -968,14 +946,13 @@ vkhr_status voxelize_impl(vkhr_ctx* ctx, bool segments, const float* v, const fl
         VKHR_CUDA_TRY(ctx, cudaStreamSynchronize(st));
         s = check_device_status(ctx, ctx->h_words[WORD_STATUS]);
         if (s != VKHR_OK) return s;
-        runs_total = ctx->h_words[WORD_RUNS_TOTAL];
         visits_total = ctx->h_words[WORD_TOTAL_VISITS];
         global_path = ctx->h_words[WORD_MAX_BRICK_VISITS] > (unsigned long long)kBrickCap;
         if (visits_total >= (1ull << 32))
             return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "more than 2^32 - 1 voxel visits in one call");
+        s = vkhr_reserve(ctx, (void**)&ctx->items, &ctx->items_cap, visits_total ? visits_total : 1, sizeof(uint2));
+        if (s != VKHR_OK) return s;
     }
-    s = vkhr_reserve(ctx, (void**)&ctx->items, &ctx->items_cap, runs_total ? runs_total : 1, sizeof(uint2));
-    if (s != VKHR_OK) return s;
     if (tang) {
         s = vkhr_reserve(ctx, (void**)&ctx->hkeys, &ctx->hkeys_cap, visits_total ? visits_total : 1, sizeof(uint32_t));
         if (s != VKHR_OK) return s;
@@ -1019,22 +996,22 @@ vkhr_status voxelize_impl(vkhr_ctx* ctx, bool segments, const float* v, const fl
     }
     if (n_in) {
         if (segments)
-            VKHR_LAUNCH(ctx, (bin_kernel<true, true>), in_blocks, threads, 0, st, g, v, pairs, n_in, tang ? tan_in : nullptr,
-                        ctx->pair_rec, ctx->pair_tan, ctx->brick_runs,
-                        ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap, ctx->d_words);
+            VKHR_LAUNCH(ctx, (bin_kernel<true, true>), in_blocks, threads, 0, st, g, v, pairs, n_in, tan_rec,
+                        ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap,
+                        ctx->d_words);
         else
-            VKHR_LAUNCH(ctx, (bin_kernel<true, false>), in_blocks, threads, 0, st, g, v, pairs, n_in, tang ? tan_in : nullptr,
-                        ctx->pair_rec, ctx->pair_tan, ctx->brick_runs,
-                        ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap, ctx->d_words);
+            VKHR_LAUNCH(ctx, (bin_kernel<true, false>), in_blocks, threads, 0, st, g, v, pairs, n_in, tan_rec,
+                        ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap,
+                        ctx->d_words);
     }
     const size_t smem = (size_t)(2 * kBrickThreads + 32 + (tang ? kBrickCap : 0)) * sizeof(uint32_t);
     const unsigned bblocks = std::min(g.nb, (unsigned)ctx->sm_count * 2);
     if (segments)
-        s = tang ? launch_brick<true, true>(ctx, g, tan_in, pairs, counts, dens, tq32, st, bblocks, smem)
-                 : launch_brick<true, false>(ctx, g, tan_in, pairs, counts, dens, tq32, st, bblocks, smem);
+        s = tang ? launch_brick<true, true>(ctx, g, tan_in, counts, dens, tq32, st, bblocks, smem)
+                 : launch_brick<true, false>(ctx, g, tan_in, counts, dens, tq32, st, bblocks, smem);
     else
-        s = tang ? launch_brick<false, true>(ctx, g, tan_in, pairs, counts, dens, tq32, st, bblocks, smem)
-                 : launch_brick<false, false>(ctx, g, tan_in, pairs, counts, dens, tq32, st, bblocks, smem);
+        s = tang ? launch_brick<false, true>(ctx, g, tan_in, counts, dens, tq32, st, bblocks, smem)
+                 : launch_brick<false, false>(ctx, g, tan_in, counts, dens, tq32, st, bblocks, smem);
     if (s != VKHR_OK) return s;
     if (tang)
         VKHR_LAUNCH(ctx, crowded_kernel, (unsigned)ctx->sm_count * 2, 256, 0, st, ctx->hdesc, ctx->hdesc_cap, ctx->hkeys,
