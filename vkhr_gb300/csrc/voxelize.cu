@@ -38,8 +38,10 @@
 namespace {
 
 constexpr int kBrickThreads = 512;     // one thread per voxel of an 8^3 brick
-constexpr int kBrickCap = 24576;       // visits a brick resolves in shared memory
-constexpr int kBrickSmall = 64;        // <= this many visits: sorted by the voxel's thread
+constexpr int kBrickCap = 22528;       // visits a brick resolves in shared memory
+constexpr int kBrickThread = 16;       // <= this many visits: sorted and summed by the voxel's thread
+constexpr int kBrickSmall = 64;        // <= this many visits: sorted by one warp (2 keys per lane)
+constexpr int kBrickWarps = kBrickThreads / 32;
 constexpr int kSmallSort = 16;         // global path: register-network resolve
 constexpr int kMediumSort = 64;        // global path: 64-key register network
 constexpr int kHeavyTile = 2048;       // crowded voxels: shared-memory sort tile
@@ -181,17 +183,15 @@ __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 // ---- brick path -----------------------------------------------------------------
 
 // A run of `len` (<= 7) consecutive visits of one pair / vertex inside brick b,
-// their local voxels packed 9 bits each: counted per brick (FILL = false;
-// warp-aggregated), or written as (key, local voxel) entries into the
+// their local voxels packed 9 bits each: counted per brick (FILL = false),
+// or written as (key, local voxel) entries into the
 // brick's slice of the visit list.
 template <bool FILL>
 __device__ __forceinline__ void emit_run(uint32_t b, uint32_t key, uint64_t locals, uint32_t len, uint32_t* visits,
                                          uint32_t* cursor, uint2* entries, size_t entries_cap, unsigned& status)
 {
     if (!FILL) {
-        const unsigned peers = __match_any_sync(__activemask(), b);
-        const unsigned tot = __reduce_add_sync(peers, len);
-        if ((int)lane_id() == __ffs(peers) - 1) atomicAdd(visits + b, tot);
+        atomicAdd(visits + b, len); // fire-and-forget reduction
     } else {
         const uint32_t base = atomicAdd(cursor + b, len);
         if ((uint64_t)base + len <= entries_cap) {
@@ -378,6 +378,37 @@ __device__ __forceinline__ uint32_t block_exclusive_scan_512(uint32_t x, uint32_
     return warp_sums[warp] + incl - x;
 }
 
+// Ascending bitonic sort of 64 keys held two per lane (index lane and lane + 32).
+__device__ __forceinline__ void warp_sort64(uint32_t& a, uint32_t& b)
+{
+    const unsigned lane = lane_id();
+#pragma unroll
+    for (unsigned k = 2; k <= 64; k <<= 1) {
+#pragma unroll
+        for (unsigned j = k >> 1; j > 0; j >>= 1) {
+            if (j == 32) { // partner is the lane's other register
+                const bool up = (lane & k) == 0;
+                if ((a > b) == up) { const uint32_t t = a; a = b; b = t; }
+            } else {
+                const bool lower = (lane & j) == 0;
+                const uint32_t oa = __shfl_xor_sync(0xffffffffu, a, j), ob = __shfl_xor_sync(0xffffffffu, b, j);
+                const bool upa = (lane & k) == 0, upb = ((lane + 32) & k) == 0;
+                a = (lower == upa) ? min(a, oa) : max(a, oa);
+                b = (lower == upb) ? min(b, ob) : max(b, ob);
+            }
+        }
+    }
+}
+
+template <bool SEG>
+__device__ __forceinline__ float4 visit_tangent(const float4* __restrict__ pair_tan, const float* __restrict__ tan,
+                                                uint32_t key)
+{
+    if (SEG) return __ldg(pair_tan + key);
+    const float* t = tan + 3 * (size_t)key;
+    return make_float4(__ldg(t), __ldg(t + 1), __ldg(t + 2), 0.0f);
+}
+
 template <bool SEG, bool TANG>
 __global__ void __launch_bounds__(kBrickThreads, 2)
 brick_kernel(Grid g, const float4* __restrict__ pair_tan, const float* __restrict__ tan,
@@ -389,8 +420,10 @@ brick_kernel(Grid g, const float4* __restrict__ pair_tan, const float* __restric
     uint32_t* cnt = sm;                       // visits per local voxel
     uint32_t* off = sm + kBrickThreads;       // slice cursor per local voxel
     uint32_t* warp_sums = sm + 2 * kBrickThreads;
-    uint32_t* keys = sm + 2 * kBrickThreads + 32;
-    __shared__ uint32_t next;
+    uint32_t* wlist = sm + 2 * kBrickThreads + 32;             // voxels for the warp resolve
+    float* wtan = reinterpret_cast<float*>(wlist + kBrickThreads); // per warp: 64 x 3 tangents
+    uint32_t* keys = wlist + kBrickThreads + kBrickWarps * 3 * 64;
+    __shared__ uint32_t next, wcount;
     const int tid = threadIdx.x;
     unsigned status = 0;
     const uint32_t listed = (uint32_t)words[WORD_BRICK_LIST];
@@ -403,6 +436,7 @@ brick_kernel(Grid g, const float4* __restrict__ pair_tan, const float* __restric
         const uint32_t b = list[q];              // visited, and within kBrickCap
         const uint32_t nv = visits[b], start = cursor[b] - nv;
         cnt[tid] = 0;
+        if (tid == 0) wcount = 0;
         __syncthreads();
         for (uint32_t i = tid; i < nv; i += kBrickThreads) atomicAdd(cnt + (__ldg(&entries[start + i].y) & 511u), 1u);
         __syncthreads();
@@ -426,7 +460,9 @@ brick_kernel(Grid g, const float4* __restrict__ pair_tan, const float* __restric
             if (TANG) {
                 if (c == 0) {
                     tq[vi] = 0u;
-                } else if (c <= (uint32_t)kBrickSmall) {
+                } else if (c > (uint32_t)kBrickThread && c <= (uint32_t)kBrickSmall) {
+                    wlist[atomicAdd(&wcount, 1u)] = (uint32_t)tid; // resolved by a warp below
+                } else if (c <= (uint32_t)kBrickThread) {
                     uint32_t* k = keys + (off[tid] - c);
                     for (uint32_t i = 1; i < c; ++i) { // insertion sort: serial order
                         const uint32_t key = k[i];
@@ -440,31 +476,17 @@ brick_kernel(Grid g, const float4* __restrict__ pair_tan, const float* __restric
                     // gather 8 tangents at a time (independent loads), then add them in key order
                     float sx = 0.0f, sy = 0.0f, sz = 0.0f;
                     for (uint32_t i0 = 0; i0 < c; i0 += 8) {
-                        float tx[8], ty[8], tz[8];
+                        float4 tv[8];
 #pragma unroll
-                        for (int j = 0; j < 8; ++j) {
-                            if (i0 + j < c) {
-                                if (SEG) {
-                                    const float4 t = __ldg(pair_tan + k[i0 + j]);
-                                    tx[j] = t.x;
-                                    ty[j] = t.y;
-                                    tz[j] = t.z;
-                                } else {
-                                    const float* t = tan + 3 * (size_t)k[i0 + j];
-                                    tx[j] = __ldg(t);
-                                    ty[j] = __ldg(t + 1);
-                                    tz[j] = __ldg(t + 2);
-                                }
-                            }
-                        }
+                        for (int j = 0; j < 8; ++j)
+                            if (i0 + j < c) tv[j] = visit_tangent<SEG>(pair_tan, tan, k[i0 + j]);
 #pragma unroll
-                        for (int j = 0; j < 8; ++j) {
+                        for (int j = 0; j < 8; ++j)
                             if (i0 + j < c) {
-                                sx = __fadd_rn(sx, tx[j]);
-                                sy = __fadd_rn(sy, ty[j]);
-                                sz = __fadd_rn(sz, tz[j]);
+                                sx = __fadd_rn(sx, tv[j].x);
+                                sy = __fadd_rn(sy, tv[j].y);
+                                sz = __fadd_rn(sz, tv[j].z);
                             }
-                        }
                     }
                     tq[vi] = pack_tangent(sx, sy, sz, c);
                 } else { // crowded: hand the keys to a CTA of its own
@@ -478,6 +500,43 @@ brick_kernel(Grid g, const float4* __restrict__ pair_tan, const float* __restric
                         status |= VKHR_DEV_LIST_OVERFLOW;
                     }
                 }
+            }
+        }
+        if (TANG) {
+            __syncthreads();
+            // voxels with kBrickThread < count <= kBrickSmall: a warp sorts the keys
+            // (two per lane), gathers the tangents in parallel and lane 0 adds them in order
+            const unsigned lane = lane_id(), warp = (unsigned)tid >> 5;
+            float* wt = wtan + warp * 3 * 64;
+            for (uint32_t m = warp; m < wcount; m += kBrickWarps) {
+                const uint32_t l = wlist[m], c = cnt[l];
+                const uint32_t* k = keys + (off[l] - c);
+                uint32_t ka = lane < c ? k[lane] : 0xffffffffu, kb = lane + 32 < c ? k[lane + 32] : 0xffffffffu;
+                warp_sort64(ka, kb);
+                if (lane < c) {
+                    const float4 t = visit_tangent<SEG>(pair_tan, tan, ka);
+                    wt[lane] = t.x;
+                    wt[64 + lane] = t.y;
+                    wt[128 + lane] = t.z;
+                }
+                if (lane + 32 < c) {
+                    const float4 t = visit_tangent<SEG>(pair_tan, tan, kb);
+                    wt[lane + 32] = t.x;
+                    wt[64 + lane + 32] = t.y;
+                    wt[128 + lane + 32] = t.z;
+                }
+                __syncwarp();
+                if (lane == 0) {
+                    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+                    for (uint32_t i = 0; i < c; ++i) {
+                        sx = __fadd_rn(sx, wt[i]);
+                        sy = __fadd_rn(sy, wt[64 + i]);
+                        sz = __fadd_rn(sz, wt[128 + i]);
+                    }
+                    const uint32_t lx = bx * 8 + (l & 7), ly = by * 8 + ((l >> 3) & 7), lz = bz * 8 + (l >> 6);
+                    tq[lx + g.w * (ly + g.h * lz)] = pack_tangent(sx, sy, sz, c);
+                }
+                __syncwarp();
             }
         }
         __syncthreads();
@@ -1004,7 +1063,8 @@ vkhr_status voxelize_impl(vkhr_ctx* ctx, bool segments, const float* v, const fl
                         ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap,
                         ctx->d_words);
     }
-    const size_t smem = (size_t)(2 * kBrickThreads + 32 + (tang ? kBrickCap : 0)) * sizeof(uint32_t);
+    const size_t smem = (size_t)(2 * kBrickThreads + 32 + kBrickThreads + kBrickWarps * 3 * 64 + (tang ? kBrickCap : 0)) *
+                        sizeof(uint32_t);
     const unsigned bblocks = std::min(g.nb, (unsigned)ctx->sm_count * 2);
     if (segments)
         s = tang ? launch_brick<true, true>(ctx, g, tan_in, counts, dens, tq32, st, bblocks, smem)
