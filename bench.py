@@ -142,8 +142,10 @@ def cpu_frame(O, st, t, idx, b, rows_sample):
 
 
 def reference_arm(args):
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
+    from vkhr_gb300 import replicas
+
+    rank, _, _ = replicas.world()
+    if rank != 0:  # the CPU reference runs once, on rank 0
         return 0
     from oracle import oracle as O
 
@@ -180,15 +182,12 @@ def reference_arm(args):
 
 def gb300_arm(args):
     import torch
-    import torch.distributed as dist
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from vkhr_gb300 import _abi, _native, replicas, scene
+
+    rank, world, local = replicas.world()
     torch.cuda.set_device(local)
-    if world > 1:
-        dist.init_process_group("nccl")
-    from vkhr_gb300 import _abi, _native, scene
+    replicas.init("nccl")  # N replicas of the frame, one per GPU; no data-path collective
 
     ctx = _native.Context(local)
     dev = torch.device("cuda", local)
@@ -230,8 +229,7 @@ def gb300_arm(args):
            torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     clocks = ClockSampler(local)
     clocks.start()
-    if world > 1:
-        dist.barrier()
+    replicas.barrier()
     torch.cuda.synchronize()
     launches0 = ctx.launch_count()
     wall0 = time.perf_counter()
@@ -245,16 +243,11 @@ def gb300_arm(args):
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
     launches = ctx.launch_count() - launches0
-    if world > 1:
-        dist.barrier()
+    replicas.barrier()
     clocks.stop()
     vox_ms = [e[0].elapsed_time(e[1]) for e in ev]
     ray_ms = [e[1].elapsed_time(e[2]) for e in ev]
-    step_ms = sum(vox_ms + ray_ms) / args.steps
-    if world > 1:
-        tt = torch.tensor([step_ms], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        step_ms = float(tt.item())
+    step_ms = replicas.max_over_ranks(sum(vox_ms + ray_ms) / args.steps, device=dev)
     px = W * H
     value = world * px / (step_ms / 1e3) / 1e6
 
@@ -350,6 +343,8 @@ def gb300_arm(args):
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
+        import torch.distributed as dist
+
         dist.destroy_process_group()
     return 0
 

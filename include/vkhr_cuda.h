@@ -161,6 +161,8 @@ uint64_t vkhr_launch_count(const vkhr_ctx* ctx);
 /* sizeof of the ABI structures as this library was compiled (layout checks). */
 size_t vkhr_sizeof_aabb(void);
 size_t vkhr_sizeof_raymarch_params(void);
+size_t vkhr_sizeof_voxel_job(void);
+size_t vkhr_sizeof_raymarch_job(void);
 
 /* ---- device memory helpers ---------------------------------------------------
  * So that a host without the CUDA toolkit (the reference's C++17 code) can
@@ -221,6 +223,38 @@ vkhr_status vkhr_voxelize_segments(vkhr_ctx* ctx, const float* d_vertices, const
                                    uint32_t* d_counts, uint8_t* d_densities, int8_t* d_tangents,
                                    void* stream);
 
+/* One style of a batched voxelization: the arguments of vkhr_voxelize_vertices
+ * (item_count = vertex_count, d_indices unused) or vkhr_voxelize_segments
+ * (item_count = index_count). */
+typedef struct vkhr_voxel_job {
+    const float* d_vertices;
+    const float* d_tangent_in;
+    const uint32_t* d_indices;
+    uint64_t item_count;
+    vkhr_aabb bounds;
+    int32_t width, height, depth;
+    int32_t index_mode;
+    uint32_t* d_counts;
+    uint8_t* d_densities;
+    int8_t* d_tangents;
+} vkhr_voxel_job;
+
+/* Voxelizes job_count (1..256) styles with one launch per phase: the
+ * per-style loop of the reference's loader (hair_style.cc:75, once per
+ * HairStyle) fused into one call.  Results per job are those of the
+ * single-style entry point; either every job requests d_tangents or none.
+ * No reference counterpart as a single call. */
+vkhr_status vkhr_voxelize_batched(vkhr_ctx* ctx, int32_t segments, const vkhr_voxel_job* jobs, int32_t job_count,
+                                  void* stream);
+
+/* Segment voxelization normally reads its visit total back to size the visit
+ * list.  A nonzero budget fixes that capacity instead (max_visits < 2^32), so
+ * the call never waits on the host and can be captured into a CUDA graph
+ * after one uncaptured call at the same sizes; a batch that needs more visits
+ * reports VKHR_ERR_CAPACITY from vkhr_check_status.  0 restores the default.
+ * No reference counterpart. */
+vkhr_status vkhr_set_visit_budget(vkhr_ctx* ctx, uint64_t max_visits);
+
 /* Waits for the stream and reports errors that kernels recorded on the device
  * since the last voxelization started (e.g. a capacity overflow). */
 vkhr_status vkhr_check_status(vkhr_ctx* ctx, void* stream);
@@ -247,6 +281,41 @@ vkhr_status vkhr_normalize_densities(vkhr_ctx* ctx, uint8_t* d_densities, uint64
 vkhr_status vkhr_raymarch(vkhr_ctx* ctx, const vkhr_raymarch_params* params,
                           const void* d_density, const void* d_tangent, const float* d_depth_in,
                           float* d_rgba, float* d_depth_out, void* stream);
+
+/* One view of a batched raymarch: its parameters (width x height is the whole
+ * view the camera projects to), its volume, and the region [x0, x0 + w) x
+ * [y0, y0 + h) of the view to render.  Outputs use the region's layout: pixel
+ * (x0 + i, y0 + j) of the view lands at d_rgba[j * pitch + i] (float4) and
+ * d_depth_out[j * pitch + i]; d_depth_in (optional) is read the same way, so
+ * regions of several views can be packed into one atlas. */
+typedef struct vkhr_raymarch_job {
+    vkhr_raymarch_params params;
+    const void* d_density;
+    const void* d_tangent;
+    const float* d_depth_in;
+    float* d_rgba;
+    float* d_depth_out;
+    int32_t x0, y0, w, h;
+    int32_t pitch;
+    int32_t reserved;
+} vkhr_raymarch_job;
+
+/* Raymarches job_count (1..256) views in one persistent launch fed by a
+ * device tile queue (the per-style Volume::draw calls of
+ * Rasterizer::strand_dvr, rasterizer.cc, as one call).  Each pixel equals the
+ * one vkhr_raymarch computes for the same view.  All jobs share one density
+ * and one tangent format.  After one uncaptured call at the same sizes the
+ * call can be captured into a CUDA graph; the graph then re-reads the job
+ * table staged in the context, so the context makes no other batched
+ * raymarch while that graph is in use.  No reference counterpart as a single
+ * call. */
+vkhr_status vkhr_raymarch_batched(vkhr_ctx* ctx, const vkhr_raymarch_job* jobs, int32_t job_count, void* stream);
+
+/* Screen footprint of params' volume: the smallest pixel rectangle (x0, y0,
+ * w, h) outside which vkhr_raymarch writes only background (rgba 0, depth
+ * 1.0), with 2 pixels of margin; the whole view when a box corner is behind
+ * the camera; w = h = 0 when the box is off screen.  Host-only. */
+vkhr_status vkhr_raymarch_footprint(const vkhr_raymarch_params* params, int32_t rect[4]);
 
 /* Allocation-free raymarch.  No counterpart in the reference: it exists for
  * callers that may not allocate device memory at all -- a real-time frame

@@ -25,6 +25,8 @@ def test_every_declared_symbol_is_exported(native_lib):
 def test_struct_layouts(native_lib):
     assert native_lib.vkhr_sizeof_aabb() == C.sizeof(_abi.AABB) == 32
     assert native_lib.vkhr_sizeof_raymarch_params() == C.sizeof(_abi.RaymarchParams)
+    assert native_lib.vkhr_sizeof_voxel_job() == C.sizeof(_abi.VoxelJob) == 104
+    assert native_lib.vkhr_sizeof_raymarch_job() == C.sizeof(_abi.RaymarchJob)
     assert native_lib.vkhr_abi_version() == 1
 
 

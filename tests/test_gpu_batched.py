@@ -1,0 +1,183 @@
+"""Batched voxelization (vkhr_voxelize_batched): many styles of uneven size in
+one launch per phase, each bit-exact against the oracle's single-style
+HairStyle::voxelize_* (hair_style.cc:257-342); the visit budget that makes
+the call capturable, and a CUDA-graph replay over new vertex data."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from vkhr_gb300 import _abi
+from vkhr_gb300._native import VkhrError
+from tests._helpers import style, to_dev
+
+pytestmark = pytest.mark.gpu
+
+RES_CHOICES = [(16, 16, 16), (24, 24, 24), (32, 32, 32), (37, 50, 29), (48, 48, 48), (64, 64, 64)]
+
+
+def _styles(seed, n_jobs, crowded=True):
+    """Uneven styles: strand counts log-uniform in [50, 3000], 8-32 vertices
+    per strand, grids from RES_CHOICES; optionally one dense style in an 8^3
+    grid whose bricks exceed the shared-memory capacity (global path)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for j in range(n_jobs):
+        n = int(np.exp(rng.uniform(np.log(50), np.log(3000))))
+        verts = int(rng.integers(8, 33))
+        kind = "disk" if j % 2 else "hemi"
+        res = RES_CHOICES[int(rng.integers(len(RES_CHOICES)))]
+        mode = _abi.INDEX_EXACT if j % 5 == 3 else _abi.INDEX_REF_FP32
+        out.append((style(kind, n, verts, seed=seed * 100 + j), res, mode))
+    if crowded:
+        out.insert(n_jobs // 2, (style("hemi", 6000, 16, seed=seed * 100 + 99), (8, 8, 8), _abi.INDEX_REF_FP32))
+    return out
+
+
+class _Batch:
+    """Device buffers and the job table of one batch."""
+
+    def __init__(self, torch, oracle, styles, segments, tangents=True):
+        self.torch, self.styles, self.segments = torch, styles, segments
+        self.keep, self.jobs, self.outs = [], [], []
+        for (st, t, idx), res, mode in styles:
+            b = oracle.bounding_box(st.vertices)
+            n = res[0] * res[1] * res[2]
+            dv, dt = to_dev(st.vertices, torch), to_dev(t, torch)
+            di = to_dev(idx.astype(np.uint32), torch)
+            counts = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+            dens = torch.full((n,), 77, dtype=torch.uint8, device="cuda")
+            tq = torch.full((n, 4), 55, dtype=torch.int8, device="cuda") if tangents else None
+            self.keep += [dv, dt, di]
+            self.outs.append((counts, dens, tq))
+            j = _abi.VoxelJob()
+            j.d_vertices, j.d_tangent_in = dv.data_ptr(), dt.data_ptr()
+            j.d_indices = di.data_ptr() if segments else None
+            j.item_count = len(idx) if segments else st.vertex_count
+            j.bounds = b
+            j.width, j.height, j.depth = res
+            j.index_mode = mode
+            j.d_counts, j.d_densities = counts.data_ptr(), dens.data_ptr()
+            j.d_tangents = tq.data_ptr() if tq is not None else None
+            self.jobs.append(j)
+        self.bounds = [j.bounds for j in self.jobs]
+
+    def poison(self):
+        for counts, dens, tq in self.outs:
+            counts.fill_(-1)
+            dens.fill_(77)
+            if tq is not None:
+                tq.fill_(55)
+
+    def check(self, oracle, vertices=None):
+        m = "segments" if self.segments else "vertices"
+        for k, (((st, t, idx), res, mode), (counts, dens, tq)) in enumerate(zip(self.styles, self.outs)):
+            v = st.vertices if vertices is None else vertices[k]
+            c_ref, d_ref, t_ref, _ = oracle.voxelize(m, v, t, idx, self.bounds[k], res, mode)
+            c = counts.cpu().numpy().view(np.uint32)
+            assert np.array_equal(c, c_ref), "job %d: counts differ in %d voxels" % (k, int((c != c_ref).sum()))
+            d = dens.cpu().numpy()
+            assert np.array_equal(d, d_ref), "job %d: densities differ in %d voxels" % (k, int((d != d_ref).sum()))
+            if tq is not None:
+                bad = np.any(tq.cpu().numpy() != t_ref, axis=1)
+                assert not bad.any(), "job %d: tangents differ in %d voxels" % (k, int(bad.sum()))
+
+
+@pytest.mark.parametrize("segments", [True, False])
+def test_batched_matches_single_style(ctx, oracle_lib, segments):
+    import torch
+
+    batch = _Batch(torch, oracle_lib, _styles(1, 16), segments)
+    s = torch.cuda.current_stream().cuda_stream
+    ctx.voxelize_batched(segments, batch.jobs, s)
+    ctx.check_status(s)
+    batch.check(oracle_lib)
+
+
+def test_batched_counts_only(ctx, oracle_lib):
+    import torch
+
+    batch = _Batch(torch, oracle_lib, _styles(2, 6, crowded=False), True, tangents=False)
+    s = torch.cuda.current_stream().cuda_stream
+    ctx.voxelize_batched(True, batch.jobs, s)
+    ctx.check_status(s)
+    batch.check(oracle_lib)
+
+
+def test_batched_rejects_bad_tables(ctx, oracle_lib):
+    import torch
+
+    batch = _Batch(torch, oracle_lib, _styles(3, 2, crowded=False), True)
+    s = torch.cuda.current_stream().cuda_stream
+    with pytest.raises(VkhrError) as e:
+        ctx.voxelize_batched(True, [], s)
+    assert e.value.status == _abi.VKHR_ERR_INVALID_ARG
+    mixed = [batch.jobs[0], _abi.VoxelJob.from_buffer_copy(batch.jobs[1])]
+    mixed[1].d_tangents = None
+    with pytest.raises(VkhrError) as e:
+        ctx.voxelize_batched(True, mixed, s)
+    assert e.value.status == _abi.VKHR_ERR_INVALID_ARG
+    bad = _abi.VoxelJob.from_buffer_copy(batch.jobs[0])
+    bad.width = 0
+    with pytest.raises(VkhrError):
+        ctx.voxelize_batched(True, [batch.jobs[1], bad], s)
+
+
+def test_visit_budget_overflow_is_reported(ctx, oracle_lib):
+    import torch
+
+    batch = _Batch(torch, oracle_lib, _styles(4, 4), True)
+    s = torch.cuda.current_stream().cuda_stream
+    ctx.set_visit_budget(1000)
+    try:
+        ctx.voxelize_batched(True, batch.jobs, s)
+        with pytest.raises(VkhrError) as e:
+            ctx.check_status(s)
+        assert e.value.status == _abi.VKHR_ERR_CAPACITY
+    finally:
+        ctx.set_visit_budget(0)
+    batch.poison()
+    ctx.voxelize_batched(True, batch.jobs, s)  # the context stays usable
+    ctx.check_status(s)
+    batch.check(oracle_lib)
+
+
+@pytest.mark.parametrize("segments", [True, False])
+def test_batched_graph_replay(ctx, oracle_lib, segments):
+    """Capture once with a visit budget, then replay over new vertex data in
+    the same buffers: every replay equals the oracle on that data."""
+    import torch
+
+    styles = _styles(5, 16)
+    batch = _Batch(torch, oracle_lib, styles, segments)
+    s = torch.cuda.current_stream().cuda_stream
+    ctx.voxelize_batched(segments, batch.jobs, s)  # without a budget: sized from the counted visits
+    ctx.check_status(s)
+    visits = sum(int(c.cpu().numpy().view(np.uint32).sum(dtype=np.uint64)) for c, _, _ in batch.outs)
+    ctx.set_visit_budget(2 * visits + 4096 if segments else 0)
+    try:
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            ctx.voxelize_batched(segments, batch.jobs, side.cuda_stream)  # sizes the scratch for the budget
+        ctx.check_status(side.cuda_stream)
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            ctx.voxelize_batched(segments, batch.jobs, torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        rng = np.random.default_rng(7)
+        for rep in range(2):
+            moved = []
+            for k, ((st, t, idx), res, mode) in enumerate(styles):
+                v = (st.vertices + rng.normal(0, 0.01, st.vertices.shape)).astype(np.float32)
+                batch.keep[3 * k].copy_(torch.from_numpy(v))
+                moved.append(v)
+            batch.poison()
+            torch.cuda.synchronize()
+            graph.replay()
+            torch.cuda.synchronize()
+            ctx.check_status(None)
+            batch.check(oracle_lib, vertices=moved)
+    finally:
+        ctx.set_visit_budget(0)

@@ -65,6 +65,25 @@ class AABB(C.Structure):
         }
 
 
+class VoxelJob(C.Structure):
+    """vkhr_voxel_job: one style of a batched voxelization."""
+
+    _fields_ = [
+        ("d_vertices", C.c_void_p),
+        ("d_tangent_in", C.c_void_p),
+        ("d_indices", C.c_void_p),
+        ("item_count", C.c_uint64),
+        ("bounds", AABB),
+        ("width", C.c_int32),
+        ("height", C.c_int32),
+        ("depth", C.c_int32),
+        ("index_mode", C.c_int32),
+        ("d_counts", C.c_void_p),
+        ("d_densities", C.c_void_p),
+        ("d_tangents", C.c_void_p),
+    ]
+
+
 class RaymarchParams(C.Structure):
     """vkhr_raymarch_params: the camera, light, strand and params UBOs."""
 
@@ -115,3 +134,22 @@ def aabb_from(origin, size):
     b.radius = float(np.sqrt(np.float32(dot)))
     b.volume = float(np.float32(np.float32(s[0] * s[1]) * s[2]))
     return b
+
+
+class RaymarchJob(C.Structure):
+    """vkhr_raymarch_job: one view of a batched raymarch and its region."""
+
+    _fields_ = [
+        ("params", RaymarchParams),
+        ("d_density", C.c_void_p),
+        ("d_tangent", C.c_void_p),
+        ("d_depth_in", C.c_void_p),
+        ("d_rgba", C.c_void_p),
+        ("d_depth_out", C.c_void_p),
+        ("x0", C.c_int32),
+        ("y0", C.c_int32),
+        ("w", C.c_int32),
+        ("h", C.c_int32),
+        ("pitch", C.c_int32),
+        ("reserved", C.c_int32),
+    ]

@@ -17,6 +17,8 @@ EXPORTS = [
     "vkhr_launch_count", "vkhr_sizeof_aabb", "vkhr_sizeof_raymarch_params",
     "vkhr_set_profiling", "vkhr_profile_count", "vkhr_profile_read",
     "vkhr_malloc", "vkhr_free", "vkhr_upload", "vkhr_download", "vkhr_sync", "vkhr_check_status",
+    "vkhr_voxelize_batched", "vkhr_set_visit_budget", "vkhr_sizeof_voxel_job",
+    "vkhr_raymarch_batched", "vkhr_raymarch_footprint", "vkhr_sizeof_raymarch_job",
 ]
 
 _lib = None
@@ -52,6 +54,10 @@ def load():
                                            C.c_int32, C.c_int32, P, P, P, P]
     lib.vkhr_voxelize_segments.argtypes = [P, P, P, P, C.c_uint64, C.POINTER(_abi.AABB), C.c_int32, C.c_int32,
                                            C.c_int32, C.c_int32, P, P, P, P]
+    lib.vkhr_voxelize_batched.argtypes = [P, C.c_int32, C.POINTER(_abi.VoxelJob), C.c_int32, P]
+    lib.vkhr_set_visit_budget.argtypes = [P, C.c_uint64]
+    lib.vkhr_raymarch_batched.argtypes = [P, C.POINTER(_abi.RaymarchJob), C.c_int32, P]
+    lib.vkhr_raymarch_footprint.argtypes = [C.POINTER(_abi.RaymarchParams), C.POINTER(C.c_int32)]
     lib.vkhr_normalize_densities.argtypes = [P, P, C.c_uint64, P]
     lib.vkhr_check_status.argtypes = [P, P]
     lib.vkhr_raymarch.argtypes = [P, C.POINTER(_abi.RaymarchParams), P, P, P, P, P, P]
@@ -67,6 +73,8 @@ def load():
     lib.vkhr_launch_count.restype = C.c_uint64
     lib.vkhr_sizeof_aabb.restype = C.c_size_t
     lib.vkhr_sizeof_raymarch_params.restype = C.c_size_t
+    lib.vkhr_sizeof_voxel_job.restype = C.c_size_t
+    lib.vkhr_sizeof_raymarch_job.restype = C.c_size_t
     for name in EXPORTS:
         getattr(lib, name).restype = getattr(lib, name).restype or C.c_int
     _lib = lib
@@ -144,6 +152,19 @@ class Context:
                                                    C.byref(bounds), w, h, d, index_mode, d_counts, d_densities,
                                                    d_tangents, stream))
 
+    def voxelize_batched(self, segments, jobs, stream=None):
+        """jobs: a sequence of _abi.VoxelJob (item_count = vertex or index count)."""
+        arr = (_abi.VoxelJob * len(jobs))(*jobs)
+        self.check(self.lib.vkhr_voxelize_batched(self.handle, 1 if segments else 0, arr, len(jobs), stream))
+
+    def raymarch_batched(self, jobs, stream=None):
+        """jobs: a sequence of _abi.RaymarchJob."""
+        arr = (_abi.RaymarchJob * len(jobs))(*jobs)
+        self.check(self.lib.vkhr_raymarch_batched(self.handle, arr, len(jobs), stream))
+
+    def set_visit_budget(self, max_visits):
+        self.check(self.lib.vkhr_set_visit_budget(self.handle, int(max_visits)))
+
     def check_status(self, stream=None):
         self.check(self.lib.vkhr_check_status(self.handle, stream))
 
@@ -153,3 +174,13 @@ class Context:
     def raymarch(self, params, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, stream=None):
         self.check(self.lib.vkhr_raymarch(self.handle, C.byref(params), d_density, d_tangent, d_depth_in, d_rgba,
                                           d_depth_out, stream))
+
+
+def raymarch_footprint(params):
+    """(x0, y0, w, h): pixels outside it are background in vkhr_raymarch."""
+    lib = load()
+    r = (C.c_int32 * 4)()
+    st = lib.vkhr_raymarch_footprint(C.byref(params), r)
+    if st != 0:
+        raise VkhrError(st, "vkhr_raymarch_footprint")
+    return tuple(int(x) for x in r)

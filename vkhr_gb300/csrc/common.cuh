@@ -32,6 +32,7 @@ enum {
     WORD_BRICK_LIST = 9,        // brick path: occupied bricks resolved in shared memory
     WORD_NORM = 10,             // normalize: min, max (2 slots); words below are cleared per voxelization
     WORD_AABB = 12,             // bounding-box scratch (8 slots)
+    WORD_RAY_QUEUE = 20,        // batched raymarch: next tile
     WORD_COUNT = 24
 };
 
@@ -61,6 +62,15 @@ struct vkhr_ctx {
     size_t list_cap;
     uint4* gdesc;              // global path: crowded voxels
     size_t gdesc_cap;
+    void* d_jobs;              // voxelizer: device job table of the current batch
+    size_t jobs_cap;           // in bytes
+    void* h_jobs;              // pinned staging of the job table
+    cudaEvent_t jobs_ev;       // recorded after the staging was copied out
+    uint64_t visit_budget;     // segment mode: fixed visit capacity (0 = size from the counted total)
+    void* d_rjobs;             // raymarch: device job table of the current batch
+    size_t rjobs_cap;          // in bytes
+    void* h_rjobs;             // pinned staging of the raymarch job table
+    cudaEvent_t rjobs_ev;      // recorded after the staging was copied out
     uint32_t* occ;             // raymarch brick-occupancy bitmap
     size_t occ_cap;            // in 32-bit words
     unsigned long long* d_words;
@@ -76,6 +86,8 @@ struct vkhr_ctx {
 };
 
 constexpr int kProfileMax = 4096;
+constexpr size_t kJobTableBytes = 64 * 1024;  // pinned staging of a voxelizer batch's job table
+constexpr size_t kRayTableBytes = 128 * 1024; // pinned staging of a raymarch batch's job table
 
 void vkhr_prof_begin(vkhr_ctx* ctx, const char* name, cudaStream_t st);
 void vkhr_prof_end(vkhr_ctx* ctx, cudaStream_t st);

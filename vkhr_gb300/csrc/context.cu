@@ -119,6 +119,10 @@ vkhr_status vkhr_create(int device, vkhr_ctx** out)
     if (e == cudaSuccess) e = cudaMemset(ctx->d_words, 0, WORD_COUNT * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_words, WORD_COUNT * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->jobs_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_jobs, kJobTableBytes);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->rjobs_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_rjobs, kRayTableBytes);
     if (e != cudaSuccess) {
         cudaGetLastError();
         vkhr_destroy(ctx);
@@ -134,13 +138,17 @@ vkhr_status vkhr_destroy(vkhr_ctx* ctx)
     cudaSetDevice(ctx->device);
     cudaDeviceSynchronize();
     void* bufs[] = {ctx->brick_runs, ctx->items, ctx->brick_list, ctx->pair_rec, ctx->pair_tan, ctx->hkeys, ctx->hdesc,
-                    ctx->cursor, ctx->list, ctx->gdesc};
+                    ctx->cursor, ctx->list, ctx->gdesc, ctx->d_jobs, ctx->d_rjobs};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (ctx->occ) cudaFree(ctx->occ);
     if (ctx->d_words) cudaFree(ctx->d_words);
     if (ctx->h_words) cudaFreeHost(ctx->h_words);
     if (ctx->ev) cudaEventDestroy(ctx->ev);
+    if (ctx->jobs_ev) cudaEventDestroy(ctx->jobs_ev);
+    if (ctx->h_jobs) cudaFreeHost(ctx->h_jobs);
+    if (ctx->rjobs_ev) cudaEventDestroy(ctx->rjobs_ev);
+    if (ctx->h_rjobs) cudaFreeHost(ctx->h_rjobs);
     if (ctx->prof_ev) {
         for (int i = 0; i < 2 * kProfileMax; ++i) cudaEventDestroy(ctx->prof_ev[i]);
         delete[] ctx->prof_ev;
@@ -197,6 +205,8 @@ vkhr_status vkhr_sync(vkhr_ctx* ctx, void* stream)
 uint64_t vkhr_launch_count(const vkhr_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
 size_t vkhr_sizeof_aabb(void) { return sizeof(vkhr_aabb); }
+size_t vkhr_sizeof_voxel_job(void) { return sizeof(vkhr_voxel_job); }
+size_t vkhr_sizeof_raymarch_job(void) { return sizeof(vkhr_raymarch_job); }
 size_t vkhr_sizeof_raymarch_params(void) { return sizeof(vkhr_raymarch_params); }
 
 } // extern "C"

@@ -268,18 +268,13 @@ __device__ __forceinline__ void texel_coords(const RayConsts& c, Vec3 p, float u
     u[2] = fmaf(p.z, c.tsc[2], c.tbias[2]);
 }
 
+// The fragment of pixel (px, py) of the c.W x c.H view: colour + coverage
+// and depth.  depth_at points at the pixel's depth-buffer value (NULL: 1.0).
 template <int DF, int TF>
-__global__ void __launch_bounds__(32 * kWarpsX * kWarpsY)
-raymarch_kernel(const __grid_constant__ RayConsts c, const typename DensityTexel<DF>::T* __restrict__ dens,
-                const void* __restrict__ tang, const uint32_t* __restrict__ occ, const float* __restrict__ depth_in,
-                float4* __restrict__ rgba, float* __restrict__ depth_out)
+__device__ __forceinline__ void march_pixel(const RayConsts& c, const typename DensityTexel<DF>::T* __restrict__ dens,
+                                            const void* __restrict__ tang, const uint32_t* __restrict__ occ,
+                                            const float* depth_at, int px, int py, float4& out, float& out_depth)
 {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int px = (blockIdx.x * kWarpsX + (warp % kWarpsX)) * kTileW + (lane % kTileW);
-    const int py = (blockIdx.y * kWarpsY + (warp / kWarpsX)) * kTileH + (lane / kTileW);
-    if (px >= c.W || py >= c.H) return;
-    const size_t at = (size_t)py * c.W + px;
-
     // ---- proxy cube: entry point of the pixel-centre ray ---------------------
     const float nx = 2.0f * ((float)px + 0.5f) / (float)c.W - 1.0f;
     const float ny = 2.0f * ((float)py + 0.5f) / (float)c.H - 1.0f;
@@ -299,13 +294,13 @@ raymarch_kernel(const __grid_constant__ RayConsts c, const typename DensityTexel
         tmin = fmaxf(tmin, fminf(t0, t1));
         tmax = fminf(tmax, fmaxf(t0, t1));
     }
-    float4 out = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    float out_depth = 1.0f;
+    out = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    out_depth = 1.0f;
     if (hit && tmin > 0.0f && tmin <= tmax) {
         const Vec3 cam = v3(c.cam[0], c.cam[1], c.cam[2]);
         const Vec3 start = v3(fmaf(tmin, dir[0], c.cam[0]), fmaf(tmin, dir[1], c.cam[1]), fmaf(tmin, dir[2], c.cam[2]));
         const Vec3 end = start + normalize(start - cam) * c.radius;
-        const float db = depth_in ? depth_in[at] : 1.0f;
+        const float db = depth_at ? *depth_at : 1.0f;
         const bool depth_test = !(clip_depth(c, end) < db);
 
         // ---- volume_surface (volume_rendering.glsl:19-52) --------------------
@@ -408,8 +403,129 @@ raymarch_kernel(const __grid_constant__ RayConsts c, const typename DensityTexel
             out_depth = clip_depth(c, surf);
         }
     }
+}
+
+template <int DF, int TF>
+__global__ void __launch_bounds__(32 * kWarpsX * kWarpsY)
+raymarch_kernel(const __grid_constant__ RayConsts c, const typename DensityTexel<DF>::T* __restrict__ dens,
+                const void* __restrict__ tang, const uint32_t* __restrict__ occ, const float* __restrict__ depth_in,
+                float4* __restrict__ rgba, float* __restrict__ depth_out)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int px = (blockIdx.x * kWarpsX + (warp % kWarpsX)) * kTileW + (lane % kTileW);
+    const int py = (blockIdx.y * kWarpsY + (warp / kWarpsX)) * kTileH + (lane / kTileW);
+    if (px >= c.W || py >= c.H) return;
+    const size_t at = (size_t)py * c.W + px;
+    float4 out;
+    float out_depth;
+    march_pixel<DF, TF>(c, dens, tang, occ, depth_in ? depth_in + at : nullptr, px, py, out, out_depth);
     rgba[at] = out;
     if (depth_out) depth_out[at] = out_depth;
+}
+
+// ---- batched raymarch ------------------------------------------------------------
+// Many views (one style each) in one persistent launch.  Each job renders a
+// rectangular region of its own view; the regions' tiles form one index
+// space that CTAs pull from a device queue, most expensive jobs first.
+
+constexpr int kMaxRayJobs = 256;
+constexpr int kRegionTileW = kTileW * kWarpsX, kRegionTileH = kTileH * kWarpsY;
+
+struct RayJob {
+    RayConsts c;
+    const void* dens;
+    const void* tang;
+    const float* depth_in; // region layout, may be NULL
+    float4* rgba;          // region layout: pixel (x0 + i, y0 + j) at [j * pitch + i]
+    float* depth_out;      // may be NULL
+    uint32_t* occ;         // this view's occupancy bitmap
+    int x0, y0, w, h, pitch, tiles_x;
+    uint32_t tile_base;    // first tile of the job in the batch
+    uint32_t brick_base;   // first occupancy brick of the job in the batch
+};
+
+static_assert(sizeof(RayJob) % 4 == 0, "RayJob is copied as 32-bit words");
+static_assert(sizeof(RayJob) * kMaxRayJobs <= kRayTableBytes, "raymarch job table staging too small");
+
+// Largest j with base[j] <= x (base ascending, base[0] = 0).
+__device__ __forceinline__ int find_base(const uint32_t* base, int nj, uint32_t x)
+{
+    int lo = 0, hi = nj - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (base[mid] <= x) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int DF>
+__global__ void occupancy_batched_kernel(const RayJob* __restrict__ jobs, int nj, uint32_t total_bricks)
+{
+    typedef DensityTexel<DF> TX;
+    __shared__ uint32_t s_base[kMaxRayJobs];
+    for (int j = threadIdx.x; j < nj; j += blockDim.x) s_base[j] = jobs[j].brick_base;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); b < total_bricks; b += warps) {
+        const RayJob& J = jobs[find_base(s_base, nj, b)];
+        const uint32_t lb = b - J.brick_base;
+        const int bx = J.c.nb[0], by = J.c.nb[1];
+        const int nx = J.c.res[0], ny = J.c.res[1], nz = J.c.res[2];
+        const int kx = (int)(lb % (uint32_t)bx), ky = (int)((lb / (uint32_t)bx) % (uint32_t)by),
+                  kz = (int)(lb / ((uint32_t)bx * (uint32_t)by));
+        const typename TX::T* d = (const typename TX::T*)J.dens;
+        bool nz_found = false;
+        for (int i = lane; i < (kBrick + 1) * (kBrick + 1) * (kBrick + 1) && !nz_found; i += 32) {
+            const int x = kBrick * kx - 1 + i % (kBrick + 1);
+            const int y = kBrick * ky - 1 + (i / (kBrick + 1)) % (kBrick + 1);
+            const int z = kBrick * kz - 1 + i / ((kBrick + 1) * (kBrick + 1));
+            if (x >= 0 && y >= 0 && z >= 0 && x < nx && y < ny && z < nz)
+                nz_found = TX::load(d, (size_t)x + (size_t)nx * ((size_t)y + (size_t)ny * z)) != 0.0f;
+        }
+        if (__any_sync(0xffffffffu, nz_found) && lane == 0) atomicOr(J.occ + (lb >> 5), 1u << (lb & 31));
+    }
+}
+
+template <int DF, int TF>
+__global__ void __launch_bounds__(32 * kWarpsX * kWarpsY)
+raymarch_batched_kernel(const RayJob* __restrict__ jobs, int nj, uint32_t total_tiles, unsigned long long* words)
+{
+    __shared__ RayJob sj;
+    __shared__ uint32_t s_base[kMaxRayJobs];
+    __shared__ uint32_t s_next;
+    for (int j = threadIdx.x; j < nj; j += blockDim.x) s_base[j] = jobs[j].tile_base;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lx = (warp % kWarpsX) * kTileW + (lane % kTileW), ly = (warp / kWarpsX) * kTileH + (lane / kTileW);
+    int cur = -1;
+    for (;;) {
+        if (threadIdx.x == 0) s_next = (uint32_t)atomicAdd(words + WORD_RAY_QUEUE, 1ull);
+        __syncthreads();
+        const uint32_t tile = s_next;
+        __syncthreads();
+        if (tile >= total_tiles) break;
+        const int j = find_base(s_base, nj, tile);
+        if (j != cur) { // every thread finished the previous tile before the barrier above
+            const uint32_t* src = reinterpret_cast<const uint32_t*>(jobs + j);
+            uint32_t* dst = reinterpret_cast<uint32_t*>(&sj);
+            for (int i = threadIdx.x; i < (int)(sizeof(RayJob) / 4); i += blockDim.x) dst[i] = __ldg(src + i);
+            __syncthreads();
+            cur = j;
+        }
+        const uint32_t t = tile - sj.tile_base;
+        const int rx = (int)(t % (uint32_t)sj.tiles_x) * kRegionTileW + lx;
+        const int ry = (int)(t / (uint32_t)sj.tiles_x) * kRegionTileH + ly;
+        if (rx < sj.w && ry < sj.h) {
+            const size_t at = (size_t)ry * sj.pitch + rx;
+            float4 out;
+            float out_depth;
+            march_pixel<DF, TF>(sj.c, (const typename DensityTexel<DF>::T*)sj.dens, sj.tang, sj.occ,
+                                sj.depth_in ? sj.depth_in + at : nullptr, sj.x0 + rx, sj.y0 + ry, out, out_depth);
+            sj.rgba[at] = out;
+            if (sj.depth_out) sj.depth_out[at] = out_depth;
+        }
+    }
 }
 
 bool invert4(const double m[16], double inv[16])
@@ -567,6 +683,176 @@ extern "C" vkhr_status vkhr_raymarch(vkhr_ctx* ctx, const vkhr_raymarch_params* 
     else
         s = launch<VKHR_DENSITY_F32, VKHR_TANGENT_F32X4>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
     VKHR_CUDA_TRY(ctx, cudaGetLastError());
+    return VKHR_OK;
+}
+
+// ---- batched raymarch: host side ------------------------------------------------------
+namespace {
+
+template <int DF, int TF>
+vkhr_status launch_batched(vkhr_ctx* ctx, const RayJob* d_jobs, int nj, uint32_t total_bricks, uint32_t total_tiles,
+                           cudaStream_t st)
+{
+    const unsigned oblocks = (unsigned)std::min<size_t>((total_bricks + 7) / 8, (size_t)ctx->sm_count * 32);
+    if (total_bricks)
+        VKHR_LAUNCH(ctx, occupancy_batched_kernel<DF>, oblocks ? oblocks : 1, 256, 0, st, d_jobs, nj, total_bricks);
+    if (!total_tiles) return VKHR_OK;
+    static int per_sm = 0; // resident CTAs per SM of this instantiation
+    if (!per_sm) {
+        int n = 0;
+        VKHR_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, raymarch_batched_kernel<DF, TF>,
+                                                                         32 * kWarpsX * kWarpsY, 0));
+        per_sm = n > 0 ? n : 1;
+    }
+    const unsigned blocks = (unsigned)std::min<uint64_t>((uint64_t)ctx->sm_count * per_sm, total_tiles);
+    VKHR_LAUNCH(ctx, (raymarch_batched_kernel<DF, TF>), blocks, 32 * kWarpsX * kWarpsY, 0, st, d_jobs, nj,
+                total_tiles, ctx->d_words);
+    return VKHR_OK;
+}
+
+} // namespace
+
+extern "C" vkhr_status vkhr_raymarch_batched(vkhr_ctx* ctx, const vkhr_raymarch_job* jobs, int32_t job_count,
+                                             void* stream)
+{
+    if (!ctx) return VKHR_ERR_INVALID_ARG;
+    if (!jobs || job_count <= 0 || job_count > kMaxRayJobs)
+        return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "job count must be in [1, 256]");
+    const int df = jobs[0].params.density_format, tf = jobs[0].params.tangent_format;
+    // most expensive first: the queue hands out big jobs' tiles before small ones
+    int order[kMaxRayJobs];
+    double cost[kMaxRayJobs];
+    for (int j = 0; j < job_count; ++j) {
+        const vkhr_raymarch_job& in = jobs[j];
+        if (!in.d_density || !in.d_tangent || !in.d_rgba)
+            return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_density, d_tangent and d_rgba are required");
+        if (in.params.density_format != df || in.params.tangent_format != tf)
+            return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "every job of a batch uses the same texel formats");
+        if (reinterpret_cast<uintptr_t>(in.d_rgba) & 15u)
+            return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_rgba must be 16-byte aligned");
+        const size_t tan_align = tf == VKHR_TANGENT_I8_SNORM ? 4 : 16;
+        if (reinterpret_cast<uintptr_t>(in.d_tangent) & (tan_align - 1))
+            return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_tangent is misaligned for its format");
+        if (in.w < 0 || in.h < 0 || in.x0 < 0 || in.y0 < 0 || (int64_t)in.x0 + in.w > in.params.width ||
+            (int64_t)in.y0 + in.h > in.params.height || in.pitch < in.w)
+            return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "region outside the view, or pitch < region width");
+        order[j] = j;
+        cost[j] = (double)in.w * in.h * std::max(in.params.raycast_steps, 1.0f);
+    }
+    std::stable_sort(order, order + job_count, [&](int a, int b) { return cost[a] > cost[b]; });
+    RayJob* table = reinterpret_cast<RayJob*>(ctx->h_rjobs);
+    // the staging is reused once the previous batch's copy has run (not under capture: see below)
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    VKHR_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    VKHR_CUDA_TRY(ctx, cudaStreamIsCapturing(st, &cap));
+    const bool capturing = cap != cudaStreamCaptureStatusNone;
+    if (!capturing) VKHR_CUDA_TRY(ctx, cudaEventSynchronize(ctx->rjobs_ev));
+    uint64_t tiles = 0, bricks = 0, words = 0;
+    size_t occ_at[kMaxRayJobs];
+    for (int k = 0; k < job_count; ++k) {
+        const vkhr_raymarch_job& in = jobs[order[k]];
+        RayJob& J = table[k];
+        vkhr_status s = make_consts(ctx, &in.params, J.c);
+        if (s != VKHR_OK) return s;
+        J.dens = in.d_density;
+        J.tang = in.d_tangent;
+        J.depth_in = in.d_depth_in;
+        J.rgba = reinterpret_cast<float4*>(in.d_rgba);
+        J.depth_out = in.d_depth_out;
+        J.x0 = in.x0;
+        J.y0 = in.y0;
+        J.w = in.w;
+        J.h = in.h;
+        J.pitch = in.pitch;
+        J.tiles_x = (in.w + kRegionTileW - 1) / kRegionTileW;
+        J.tile_base = (uint32_t)tiles;
+        J.brick_base = (uint32_t)bricks;
+        tiles += (uint64_t)J.tiles_x * ((in.h + kRegionTileH - 1) / kRegionTileH);
+        const uint64_t nb = (uint64_t)J.c.nb[0] * J.c.nb[1] * J.c.nb[2];
+        bricks += nb;
+        occ_at[k] = (size_t)words;
+        words += (nb + 31) / 32;
+        if (tiles >= (1ull << 32) || bricks >= (1ull << 32))
+            return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "batch too large (2^32 tiles or bricks)");
+    }
+    vkhr_status s = vkhr_reserve(ctx, (void**)&ctx->occ, &ctx->occ_cap, (size_t)words, sizeof(uint32_t));
+    if (s != VKHR_OK) return s;
+    s = vkhr_reserve(ctx, &ctx->d_rjobs, &ctx->rjobs_cap, (size_t)job_count * sizeof(RayJob), 1);
+    if (s != VKHR_OK) return s;
+    for (int k = 0; k < job_count; ++k) table[k].occ = ctx->occ + occ_at[k];
+    // Under capture the graph's copy reads the staging at every replay: the
+    // staging then holds this table until the context's next raymarch batch.
+    VKHR_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_rjobs, table, (size_t)job_count * sizeof(RayJob), cudaMemcpyHostToDevice,
+                                       st));
+    if (!capturing) VKHR_CUDA_TRY(ctx, cudaEventRecord(ctx->rjobs_ev, st));
+    VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->occ, 0, (size_t)words * sizeof(uint32_t), st));
+    VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_words + WORD_RAY_QUEUE, 0, sizeof(unsigned long long), st));
+    const RayJob* d_jobs = reinterpret_cast<const RayJob*>(ctx->d_rjobs);
+    const uint32_t nbk = (uint32_t)bricks, nt = (uint32_t)tiles;
+    if (df == VKHR_DENSITY_U8_UNORM && tf == VKHR_TANGENT_I8_SNORM)
+        s = launch_batched<VKHR_DENSITY_U8_UNORM, VKHR_TANGENT_I8_SNORM>(ctx, d_jobs, job_count, nbk, nt, st);
+    else if (df == VKHR_DENSITY_U8_UNORM)
+        s = launch_batched<VKHR_DENSITY_U8_UNORM, VKHR_TANGENT_F32X4>(ctx, d_jobs, job_count, nbk, nt, st);
+    else if (df == VKHR_DENSITY_U32_COUNT && tf == VKHR_TANGENT_I8_SNORM)
+        s = launch_batched<VKHR_DENSITY_U32_COUNT, VKHR_TANGENT_I8_SNORM>(ctx, d_jobs, job_count, nbk, nt, st);
+    else if (df == VKHR_DENSITY_U32_COUNT)
+        s = launch_batched<VKHR_DENSITY_U32_COUNT, VKHR_TANGENT_F32X4>(ctx, d_jobs, job_count, nbk, nt, st);
+    else if (tf == VKHR_TANGENT_I8_SNORM)
+        s = launch_batched<VKHR_DENSITY_F32, VKHR_TANGENT_I8_SNORM>(ctx, d_jobs, job_count, nbk, nt, st);
+    else
+        s = launch_batched<VKHR_DENSITY_F32, VKHR_TANGENT_F32X4>(ctx, d_jobs, job_count, nbk, nt, st);
+    if (s != VKHR_OK) return s;
+    VKHR_CUDA_TRY(ctx, cudaGetLastError());
+    return VKHR_OK;
+}
+
+extern "C" vkhr_status vkhr_raymarch_footprint(const vkhr_raymarch_params* p, int32_t rect[4])
+{
+    if (!p || !rect || p->width <= 0 || p->height <= 0) return VKHR_ERR_INVALID_ARG;
+    double pv[16];
+    for (int col = 0; col < 4; ++col)
+        for (int r = 0; r < 4; ++r) {
+            double s = 0.0;
+            for (int k = 0; k < 4; ++k) s += (double)p->projection[k * 4 + r] * (double)p->view[col * 4 + k];
+            pv[col * 4 + r] = s;
+        }
+    const double W = p->width, H = p->height;
+    double lo[2] = {INFINITY, INFINITY}, hi[2] = {-INFINITY, -INFINITY};
+    for (int k = 0; k < 8; ++k) {
+        double x[4] = {p->volume_bounds.origin[0] + ((k & 1) ? p->volume_bounds.size[0] : 0.0f),
+                       p->volume_bounds.origin[1] + ((k & 2) ? p->volume_bounds.size[1] : 0.0f),
+                       p->volume_bounds.origin[2] + ((k & 4) ? p->volume_bounds.size[2] : 0.0f), 1.0};
+        double clip[4];
+        for (int r = 0; r < 4; ++r) clip[r] = pv[r] * x[0] + pv[4 + r] * x[1] + pv[8 + r] * x[2] + pv[12 + r] * x[3];
+        if (!(clip[3] > 1e-6) || !std::isfinite(clip[0] / clip[3]) || !std::isfinite(clip[1] / clip[3])) {
+            rect[0] = rect[1] = 0; // a corner behind the camera (or the camera inside): the whole view
+            rect[2] = p->width;
+            rect[3] = p->height;
+            return VKHR_OK;
+        }
+        for (int a = 0; a < 2; ++a) {
+            lo[a] = std::min(lo[a], clip[a] / clip[3]);
+            hi[a] = std::max(hi[a], clip[a] / clip[3]);
+        }
+    }
+    // pixel centre (i + 0.5) / n * 2 - 1 in NDC; 2 pixels of margin for the FP32 ray set-up
+    const double n[2] = {W, H};
+    int64_t a0[2], a1[2];
+    for (int a = 0; a < 2; ++a) {
+        a0[a] = (int64_t)std::floor(std::max(-1e9, (lo[a] + 1.0) * 0.5 * n[a] - 0.5)) - 2;
+        a1[a] = (int64_t)std::ceil(std::min(1e9, (hi[a] + 1.0) * 0.5 * n[a] - 0.5)) + 2;
+        a0[a] = std::max<int64_t>(a0[a], 0);
+        a1[a] = std::min<int64_t>(a1[a], (int64_t)n[a] - 1);
+    }
+    if (a0[0] > a1[0] || a0[1] > a1[1]) {
+        rect[0] = rect[1] = rect[2] = rect[3] = 0;
+        return VKHR_OK;
+    }
+    rect[0] = (int32_t)a0[0];
+    rect[1] = (int32_t)a0[1];
+    rect[2] = (int32_t)(a1[0] - a0[0] + 1);
+    rect[3] = (int32_t)(a1[1] - a0[1] + 1);
     return VKHR_OK;
 }
 

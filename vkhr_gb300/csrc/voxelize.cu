@@ -34,6 +34,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 
 namespace {
 
@@ -67,6 +68,48 @@ struct Visit {
     uint32_t brick;
     uint32_t local; // (x & 7) | (y & 7) << 3 | (z & 7) << 6
 };
+
+// One style of a batch.  Items (index pairs, or vertices) and bricks of all
+// styles share one global index space; a style owns [item_base, +n_in) and
+// [brick_base, +g.nb).  Keys stay style-local (pair / vertex numbers).
+constexpr int kMaxJobs = 256;
+
+struct VoxJob {
+    Grid g;
+    const float* v;
+    const float* tan;   // tangent input (NULL: counts only)
+    const uint2* pairs; // NULL in vertex mode
+    uint32_t* counts;
+    uint8_t* dens;
+    uint32_t* tq;
+    uint32_t item_base;
+    uint32_t n_in;
+    uint32_t brick_base;
+    uint32_t pad;
+};
+
+static_assert(sizeof(VoxJob) * kMaxJobs <= kJobTableBytes, "job table staging too small");
+
+// Largest j with base[j] <= x (base ascending, base[0] = 0).
+__device__ __forceinline__ int find_job(const uint32_t* base, int nj, uint32_t x)
+{
+    int lo = 0, hi = nj - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (base[mid] <= x) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void load_bases(const VoxJob* jobs, int nj, uint32_t* item_base, uint32_t* brick_base)
+{
+    for (int j = threadIdx.x; j < nj; j += blockDim.x) {
+        if (item_base) item_base[j] = jobs[j].item_base;
+        if (brick_base) brick_base[j] = jobs[j].brick_base;
+    }
+    __syncthreads();
+}
 
 __device__ __forceinline__ bool linear_index(const Grid& g, float vx, float vy, float vz, uint32_t& out)
 {
@@ -203,24 +246,29 @@ __device__ __forceinline__ void emit_run(uint32_t b, uint32_t key, uint64_t loca
 }
 
 template <bool FILL, bool SEG>
-__global__ void bin_kernel(Grid g, const float* __restrict__ v, const uint2* __restrict__ pairs, uint32_t n_in,
-                           const float* __restrict__ tan_in,
-                           float4* pair_rec, float4* pair_tan, uint32_t* visits, uint32_t* cursor, uint2* entries,
-                           size_t entries_cap, unsigned long long* words)
+__global__ void bin_kernel(const VoxJob* __restrict__ jobs, int nj, uint32_t total_items, float4* pair_rec,
+                           float4* pair_tan, uint32_t* visits, uint32_t* cursor, uint2* entries, size_t entries_cap,
+                           unsigned long long* words)
 {
+    __shared__ uint32_t s_item_base[kMaxJobs];
+    load_bases(jobs, nj, s_item_base, nullptr);
     unsigned status = 0;
-    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n_in; p += (uint64_t)gridDim.x * blockDim.x) {
+    for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < total_items;
+         q += (uint64_t)gridDim.x * blockDim.x) {
+        const VoxJob& J = jobs[find_job(s_item_base, nj, (uint32_t)q)];
+        const Grid& g = J.g;
+        const uint32_t p = (uint32_t)q - J.item_base;
         if (SEG) {
             Seg s;
             if (FILL) {
-                seg_load(pair_rec + 2 * p, s);
+                seg_load(pair_rec + 2 * q, s);
             } else {
-                const uint2 ij = __ldg(pairs + p);
-                seg_setup(g, v, ij, s, status);
-                seg_store(s, pair_rec + 2 * p);
-                if (tan_in) // tangents[indices[i]]: every visit of the pair adds this one
-                    pair_tan[p] = make_float4(__ldg(tan_in + 3 * (size_t)ij.x), __ldg(tan_in + 3 * (size_t)ij.x + 1),
-                                              __ldg(tan_in + 3 * (size_t)ij.x + 2), 0.0f);
+                const uint2 ij = __ldg(J.pairs + p);
+                seg_setup(g, J.v, ij, s, status);
+                seg_store(s, pair_rec + 2 * q);
+                if (J.tan) // tangents[indices[i]]: every visit of the pair adds this one
+                    pair_tan[q] = make_float4(__ldg(J.tan + 3 * (size_t)ij.x), __ldg(J.tan + 3 * (size_t)ij.x + 1),
+                                              __ldg(J.tan + 3 * (size_t)ij.x + 2), 0.0f);
             }
             uint32_t cur = kNoBrick, len = 0;
             uint64_t locals = 0;
@@ -231,18 +279,19 @@ __global__ void bin_kernel(Grid g, const float* __restrict__ v, const uint2* __r
                     locals |= (uint64_t)o.local << (9 * len);
                     ++len;
                 } else {
-                    if (len) emit_run<FILL>(cur, (uint32_t)p, locals, len, visits, cursor, entries, entries_cap, status);
+                    if (len)
+                        emit_run<FILL>(J.brick_base + cur, p, locals, len, visits, cursor, entries, entries_cap, status);
                     cur = ok ? o.brick : kNoBrick;
                     len = ok ? 1u : 0u;
                     locals = ok ? (uint64_t)o.local : 0ull;
                 }
                 seg_advance(s);
             }
-            if (len) emit_run<FILL>(cur, (uint32_t)p, locals, len, visits, cursor, entries, entries_cap, status);
+            if (len) emit_run<FILL>(J.brick_base + cur, p, locals, len, visits, cursor, entries, entries_cap, status);
         } else {
             Visit o;
-            if (vertex_visit(g, v, (uint32_t)p, o))
-                emit_run<FILL>(o.brick, (uint32_t)p, (uint64_t)o.local, 1u, visits, cursor, entries, entries_cap,
+            if (vertex_visit(g, J.v, p, o))
+                emit_run<FILL>(J.brick_base + o.brick, p, (uint64_t)o.local, 1u, visits, cursor, entries, entries_cap,
                                status);
         }
     }
@@ -318,17 +367,27 @@ __global__ void __launch_bounds__(kRangeThreads) bin_ranges_kernel(const uint32_
 }
 
 // Zeroes every voxel of the bricks no visit reached (visited bricks are
-// written by the brick kernel or the global path).  Grid: (x chunks, y, z).
-__global__ void zero_empty_kernel(Grid g, const uint32_t* __restrict__ visits, uint32_t* counts, uint8_t* dens,
-                                  uint32_t* tq)
+// written by the brick kernel or the global path): one block per brick.
+__global__ void zero_empty_kernel(const VoxJob* __restrict__ jobs, int nj, uint32_t total_bricks,
+                                  const uint32_t* __restrict__ visits)
 {
-    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
-    if (x >= g.w) return;
-    if (__ldg(visits + (x >> 3) + g.nbx * ((y >> 3) + g.nby * (z >> 3)))) return;
-    const size_t vi = x + (size_t)g.w * (y + (size_t)g.h * z);
-    counts[vi] = 0u;
-    if (dens) dens[vi] = 0;
-    if (tq) tq[vi] = 0u;
+    __shared__ uint32_t s_brick_base[kMaxJobs];
+    load_bases(jobs, nj, nullptr, s_brick_base);
+    for (uint32_t b = blockIdx.x; b < total_bricks; b += gridDim.x) {
+        if (__ldg(visits + b)) continue;
+        const VoxJob& J = jobs[find_job(s_brick_base, nj, b)];
+        const Grid& g = J.g;
+        const uint32_t lb = b - J.brick_base;
+        const uint32_t bx = lb % g.nbx, by = (lb / g.nbx) % g.nby, bz = lb / (g.nbx * g.nby);
+        for (uint32_t l = threadIdx.x; l < 512u; l += blockDim.x) {
+            const uint32_t x = bx * 8 + (l & 7), y = by * 8 + ((l >> 3) & 7), z = bz * 8 + (l >> 6);
+            if (x >= g.w || y >= g.h || z >= g.d) continue;
+            const size_t vi = x + (size_t)g.w * (y + (size_t)g.h * z);
+            J.counts[vi] = 0u;
+            if (J.dens) J.dens[vi] = 0;
+            if (J.tq) J.tq[vi] = 0u;
+        }
+    }
 }
 
 // Tangent of a visit key: the vertex's own (voxelize_vertices) or the pair's
@@ -411,10 +470,10 @@ __device__ __forceinline__ float4 visit_tangent(const float4* __restrict__ pair_
 
 template <bool SEG, bool TANG>
 __global__ void __launch_bounds__(kBrickThreads, 2)
-brick_kernel(Grid g, const float4* __restrict__ pair_tan, const float* __restrict__ tan,
+brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__ pair_tan_all,
              const uint32_t* __restrict__ visits, const uint32_t* __restrict__ cursor, const uint32_t* __restrict__ list,
-             const uint2* __restrict__ entries, uint32_t* counts, uint8_t* dens, uint32_t* tq, uint4* hdesc,
-             size_t hdesc_cap, uint32_t* hkeys, size_t hkeys_cap, unsigned long long* words)
+             const uint2* __restrict__ entries, size_t entries_cap, uint4* hdesc, size_t hdesc_cap, uint32_t* hkeys,
+             size_t hkeys_cap, unsigned long long* words)
 {
     extern __shared__ uint32_t sm[];
     uint32_t* cnt = sm;                       // visits per local voxel
@@ -423,7 +482,9 @@ brick_kernel(Grid g, const float4* __restrict__ pair_tan, const float* __restric
     uint32_t* wlist = sm + 2 * kBrickThreads + 32;             // voxels for the warp resolve
     float* wtan = reinterpret_cast<float*>(wlist + kBrickThreads); // per warp: 64 x 3 tangents
     uint32_t* keys = wlist + kBrickThreads + kBrickWarps * 3 * 64;
-    __shared__ uint32_t next, wcount;
+    __shared__ uint32_t next, wcount, s_job;
+    __shared__ uint32_t s_brick_base[kMaxJobs];
+    load_bases(jobs, nj, nullptr, s_brick_base);
     const int tid = threadIdx.x;
     unsigned status = 0;
     const uint32_t listed = (uint32_t)words[WORD_BRICK_LIST];
@@ -433,11 +494,26 @@ brick_kernel(Grid g, const float4* __restrict__ pair_tan, const float* __restric
         const uint32_t q = next;
         __syncthreads();
         if (q >= listed) break;
-        const uint32_t b = list[q];              // visited, and within kBrickCap
-        const uint32_t nv = visits[b], start = cursor[b] - nv;
+        const uint32_t gb = list[q];             // visited, and within kBrickCap
+        const uint32_t nv = visits[gb], start = cursor[gb] - nv;
+        if ((uint64_t)start + nv > entries_cap) { // visit budget exceeded: the fill pass flagged it
+            status |= VKHR_DEV_LIST_OVERFLOW;
+            continue;
+        }
         cnt[tid] = 0;
-        if (tid == 0) wcount = 0;
+        if (tid == 0) {
+            wcount = 0;
+            s_job = (uint32_t)find_job(s_brick_base, nj, gb);
+        }
         __syncthreads();
+        const VoxJob& J = jobs[s_job];
+        const Grid& g = J.g;
+        const uint32_t b = gb - J.brick_base;   // brick within the style's grid
+        const float4* pair_tan = pair_tan_all + J.item_base;
+        const float* tan = J.tan;
+        uint32_t* counts = J.counts;
+        uint8_t* dens = J.dens;
+        uint32_t* tq = J.tq;
         for (uint32_t i = tid; i < nv; i += kBrickThreads) atomicAdd(cnt + (__ldg(&entries[start + i].y) & 511u), 1u);
         __syncthreads();
         if (TANG) {
@@ -495,7 +571,7 @@ brick_kernel(Grid g, const float4* __restrict__ pair_tan, const float* __restric
                     if (hb + c <= hkeys_cap && hd < hdesc_cap) {
                         const uint32_t* k = keys + (off[tid] - c);
                         for (uint32_t i = 0; i < c; ++i) hkeys[hb + i] = k[i];
-                        hdesc[hd] = make_uint4(vi, (uint32_t)hb, c, 0u);
+                        hdesc[hd] = make_uint4(vi, (uint32_t)hb, c, s_job);
                     } else {
                         status |= VKHR_DEV_LIST_OVERFLOW;
                     }
@@ -597,10 +673,10 @@ __device__ void resolve_crowded(const uint32_t* src, uint32_t c, const float* __
     __syncthreads();
 }
 
-// One CTA per crowded voxel of the brick path (descriptors: voxel, key offset, count).
-__global__ void __launch_bounds__(256) crowded_kernel(const uint4* __restrict__ hdesc, size_t hdesc_cap,
-                                                      const uint32_t* __restrict__ hkeys, const float* __restrict__ tan,
-                                                      const uint2* __restrict__ pairs, uint32_t* tq,
+// One CTA per crowded voxel of the brick path (descriptors: voxel, key
+// offset, count, style).
+__global__ void __launch_bounds__(256) crowded_kernel(const VoxJob* __restrict__ jobs, const uint4* __restrict__ hdesc,
+                                                      size_t hdesc_cap, const uint32_t* __restrict__ hkeys,
                                                       const unsigned long long* words)
 {
     __shared__ uint32_t keys[kHeavyTile];
@@ -609,7 +685,8 @@ __global__ void __launch_bounds__(256) crowded_kernel(const uint4* __restrict__ 
     if (nh > hdesc_cap) nh = hdesc_cap;
     for (unsigned long long h = blockIdx.x; h < nh; h += gridDim.x) {
         const uint4 d = hdesc[h];
-        resolve_crowded(hkeys + d.y, d.z, tan, pairs, keys, tv, tq + d.x);
+        const VoxJob& J = jobs[d.w];
+        resolve_crowded(hkeys + d.y, d.z, J.tan, J.pairs, keys, tv, J.tq + d.x);
     }
 }
 
@@ -759,8 +836,9 @@ __device__ __forceinline__ uint32_t resolve_registers(uint32_t c, const uint32_t
 // kMediumSort visits go to crowded descriptors over the global list.
 __global__ void global_resolve_kernel(Grid g, const uint32_t* __restrict__ visits, const uint32_t* __restrict__ counts,
                                       const uint32_t* __restrict__ gcursor, const uint32_t* __restrict__ list,
-                                      const float* __restrict__ tan, const uint2* __restrict__ pairs, uint8_t* dens,
-                                      uint32_t* tq, uint4* gdesc, size_t gdesc_cap, unsigned long long* words)
+                                      size_t list_cap, const float* __restrict__ tan, const uint2* __restrict__ pairs,
+                                      uint8_t* dens, uint32_t* tq, uint4* gdesc, size_t gdesc_cap, uint32_t job,
+                                      unsigned long long* words)
 {
     if (!global_path_needed(words)) return;
     for (uint64_t vi = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; vi < g.n; vi += (uint64_t)gridDim.x * blockDim.x) {
@@ -771,20 +849,23 @@ __global__ void global_resolve_kernel(Grid g, const uint32_t* __restrict__ visit
         if (!tq) continue;
         if (c == 0) { tq[vi] = 0u; continue; }
         const uint32_t start = gcursor[vi] - c;
+        if ((uint64_t)start + c > list_cap) { // visit budget exceeded: the fill pass flagged it
+            atomicOr(words + WORD_STATUS, (unsigned long long)VKHR_DEV_LIST_OVERFLOW);
+            continue;
+        }
         if (c <= kSmallSort) tq[vi] = resolve_registers<kSmallSort>(c, list, start, tan, pairs);
         else if (c <= kMediumSort) tq[vi] = resolve_registers<kMediumSort>(c, list, start, tan, pairs);
         else {
             const unsigned long long hd = atomicAdd(words + WORD_HEAVY_COUNT, 1ull);
-            if (hd < gdesc_cap) gdesc[hd] = make_uint4((uint32_t)vi, start, c, 0u);
+            if (hd < gdesc_cap) gdesc[hd] = make_uint4((uint32_t)vi, start, c, job);
             else atomicOr(words + WORD_STATUS, (unsigned long long)VKHR_DEV_LIST_OVERFLOW);
         }
     }
 }
 
-__global__ void __launch_bounds__(256) global_crowded_kernel(const uint4* __restrict__ gdesc, size_t gdesc_cap,
+__global__ void __launch_bounds__(256) global_crowded_kernel(const VoxJob* __restrict__ jobs,
+                                                             const uint4* __restrict__ gdesc, size_t gdesc_cap,
                                                              const uint32_t* __restrict__ list,
-                                                             const float* __restrict__ tan,
-                                                             const uint2* __restrict__ pairs, uint32_t* tq,
                                                              const unsigned long long* words)
 {
     if (!global_path_needed(words)) return;
@@ -794,7 +875,8 @@ __global__ void __launch_bounds__(256) global_crowded_kernel(const uint4* __rest
     if (nh > gdesc_cap) nh = gdesc_cap;
     for (unsigned long long h = blockIdx.x; h < nh; h += gridDim.x) {
         const uint4 d = gdesc[h];
-        resolve_crowded(list + d.y, d.z, tan, pairs, keys, tv, tq + d.x);
+        const VoxJob& J = jobs[d.w];
+        resolve_crowded(list + d.y, d.z, J.tan, J.pairs, keys, tv, J.tq + d.x);
     }
 }
 
@@ -920,86 +1002,132 @@ vkhr_status check_device_status(vkhr_ctx* ctx, unsigned long long s)
 }
 
 template <bool SEG, bool TANG>
-vkhr_status launch_brick(vkhr_ctx* ctx, const Grid& g, const float* tan_in, uint32_t* counts, uint8_t* dens,
-                         uint32_t* tq, cudaStream_t st, unsigned blocks, size_t smem)
+vkhr_status launch_brick(vkhr_ctx* ctx, const VoxJob* d_jobs, int nj, cudaStream_t st, unsigned blocks, size_t smem,
+                         size_t cap_visits)
 {
     VKHR_CUDA_TRY(ctx, cudaFuncSetAttribute(brick_kernel<SEG, TANG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)smem));
-    VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG>), blocks, kBrickThreads, smem, st, g, ctx->pair_tan, tan_in,
-                ctx->brick_visits, ctx->brick_cursor, ctx->brick_list, ctx->items, counts, dens, tq, ctx->hdesc,
-                ctx->hdesc_cap, ctx->hkeys, ctx->hkeys_cap, ctx->d_words);
+    VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG>), blocks, kBrickThreads, smem, st, d_jobs, nj, ctx->pair_tan,
+                ctx->brick_visits, ctx->brick_cursor, ctx->brick_list, ctx->items, cap_visits, ctx->hdesc,
+                ctx->hdesc_cap, ctx->hkeys, cap_visits, ctx->d_words);
     return VKHR_OK;
 }
 
-vkhr_status voxelize_impl(vkhr_ctx* ctx, bool segments, const float* v, const float* tan_in, const uint32_t* idx,
-                          uint64_t n_items, const vkhr_aabb* bounds, int32_t w, int32_t h, int32_t d, int32_t mode,
-                          uint32_t* counts, uint8_t* dens, int8_t* tq, cudaStream_t st)
+// Validates one job and fills its device description.
+vkhr_status make_job(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job& in, VoxJob& out)
+{
+    vkhr_status s = make_grid(ctx, &in.bounds, in.width, in.height, in.depth, in.index_mode, out.g);
+    if (s != VKHR_OK) return s;
+    const uint64_t n_items = segments ? in.item_count / 2 : in.item_count; // floor(n / 2) index pairs
+    if (n_items >= (1ull << 32)) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "more than 2^32 - 1 vertices or pairs");
+    const uint32_t n_in = (uint32_t)n_items;
+    if (!in.d_counts) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_counts is NULL");
+    if (in.d_tangents && !in.d_tangent_in && n_in)
+        return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_tangents requested without d_tangent_in");
+    if (n_in && !in.d_vertices) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_vertices is NULL");
+    if (segments && n_in && !in.d_indices) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_indices is NULL");
+    if (segments && in.d_indices && (reinterpret_cast<uintptr_t>(in.d_indices) & 7u))
+        return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_indices must be 8-byte aligned");
+    if (in.d_tangents && (reinterpret_cast<uintptr_t>(in.d_tangents) & 3u))
+        return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_tangents must be 4-byte aligned");
+    out.v = in.d_vertices;
+    out.tan = in.d_tangents ? in.d_tangent_in : nullptr;
+    out.pairs = segments ? reinterpret_cast<const uint2*>(in.d_indices) : nullptr;
+    out.counts = in.d_counts;
+    out.dens = in.d_densities;
+    out.tq = reinterpret_cast<uint32_t*>(in.d_tangents);
+    out.n_in = n_in;
+    out.pad = 0;
+    return VKHR_OK;
+}
+
+vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* jobs_in, int nj, cudaStream_t st)
 {
     if (!ctx) return VKHR_ERR_INVALID_ARG;
-    Grid g;
-    vkhr_status s = make_grid(ctx, bounds, w, h, d, mode, g);
-    if (s != VKHR_OK) return s;
-    if (!counts) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_counts is NULL");
-    if (n_items >= (1ull << 32)) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "more than 2^32 - 1 vertices or pairs");
-    const uint32_t n_in = (uint32_t)n_items; // vertices, or index pairs
-    if (tq && !tan_in && n_in) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_tangents requested without d_tangent_in");
-    if (n_in && !v) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_vertices is NULL");
-    if (segments && n_in && !idx) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_indices is NULL");
-    if (segments && idx && (reinterpret_cast<uintptr_t>(idx) & 7u))
-        return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_indices must be 8-byte aligned");
-    if (tq && (reinterpret_cast<uintptr_t>(tq) & 3u))
-        return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_tangents must be 4-byte aligned");
+    if (nj <= 0 || nj > kMaxJobs || !jobs_in) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "job count must be in [1, 256]");
+    VoxJob jobs[kMaxJobs];
+    uint64_t items = 0, bricks = 0, max_voxels = 0;
+    const bool tang = jobs_in[0].d_tangents != nullptr;
+    for (int j = 0; j < nj; ++j) {
+        vkhr_status s = make_job(ctx, segments, jobs_in[j], jobs[j]);
+        if (s != VKHR_OK) return s;
+        if ((jobs_in[j].d_tangents != nullptr) != tang)
+            return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "every job of a batch requests tangents, or none does");
+        jobs[j].item_base = (uint32_t)items;
+        jobs[j].brick_base = (uint32_t)bricks;
+        items += jobs[j].n_in;
+        bricks += jobs[j].g.nb;
+        max_voxels = std::max<uint64_t>(max_voxels, jobs[j].g.n);
+        if (items >= (1ull << 32) || bricks >= (1ull << 32))
+            return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "batch too large (2^32 items or bricks)");
+    }
+    const uint32_t total_items = (uint32_t)items, total_bricks = (uint32_t)bricks;
     VKHR_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
-    const uint2* pairs = reinterpret_cast<const uint2*>(idx);
-    const bool tang = tq != nullptr;
-    uint32_t* tq32 = reinterpret_cast<uint32_t*>(tq);
+
+    // job table: pinned staging (reused once the previous upload has run) -> device
+    vkhr_status s = vkhr_reserve(ctx, (void**)&ctx->d_jobs, &ctx->jobs_cap, (size_t)nj * sizeof(VoxJob), 1);
+    if (s != VKHR_OK) return s;
+    // A captured call leaves the copy in the graph, which reads the staging
+    // again at each replay: the staging then keeps this table until the
+    // context's next voxelization.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    VKHR_CUDA_TRY(ctx, cudaStreamIsCapturing(st, &cap));
+    const bool capturing = cap != cudaStreamCaptureStatusNone;
+    if (!capturing) VKHR_CUDA_TRY(ctx, cudaEventSynchronize(ctx->jobs_ev));
+    std::memcpy(ctx->h_jobs, jobs, (size_t)nj * sizeof(VoxJob));
+    VKHR_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_jobs, ctx->h_jobs, (size_t)nj * sizeof(VoxJob), cudaMemcpyHostToDevice, st));
+    if (!capturing) VKHR_CUDA_TRY(ctx, cudaEventRecord(ctx->jobs_ev, st));
+    const VoxJob* d_jobs = reinterpret_cast<const VoxJob*>(ctx->d_jobs);
 
     // per-brick bookkeeping: visits and visit-list cursor
-    s = vkhr_reserve(ctx, (void**)&ctx->brick_runs, &ctx->brick_cap, 3ull * g.nb, sizeof(uint32_t));
+    s = vkhr_reserve(ctx, (void**)&ctx->brick_runs, &ctx->brick_cap, 2ull * total_bricks + 1, sizeof(uint32_t));
     if (s != VKHR_OK) return s;
     ctx->brick_visits = ctx->brick_runs;
-    ctx->brick_cursor = ctx->brick_runs + g.nb;
-    s = vkhr_reserve(ctx, (void**)&ctx->brick_list, &ctx->brick_list_cap, g.nb, sizeof(uint32_t));
+    ctx->brick_cursor = ctx->brick_runs + total_bricks;
+    s = vkhr_reserve(ctx, (void**)&ctx->brick_list, &ctx->brick_list_cap, total_bricks + 1ull, sizeof(uint32_t));
     if (s != VKHR_OK) return s;
-    if (segments && n_in) {
-        s = vkhr_reserve(ctx, (void**)&ctx->pair_rec, &ctx->pair_rec_cap, 2ull * n_in, sizeof(float4));
+    if (segments && total_items) {
+        s = vkhr_reserve(ctx, (void**)&ctx->pair_rec, &ctx->pair_rec_cap, 2ull * total_items, sizeof(float4));
         if (s != VKHR_OK) return s;
         if (tang) {
-            s = vkhr_reserve(ctx, (void**)&ctx->pair_tan, &ctx->pair_tan_cap, n_in, sizeof(float4));
+            s = vkhr_reserve(ctx, (void**)&ctx->pair_tan, &ctx->pair_tan_cap, total_items, sizeof(float4));
             if (s != VKHR_OK) return s;
         }
     }
-    if (!segments) { // vertex mode: every bound is the vertex count, no read-back needed
-        s = vkhr_reserve(ctx, (void**)&ctx->items, &ctx->items_cap, n_in ? n_in : 1, sizeof(uint2));
+    // Capacities that do not depend on the data: vertex mode is bounded by
+    // the vertex count; segment mode by the visit budget when one is set.
+    const bool bounded = !segments || ctx->visit_budget > 0;
+    uint64_t visits_total = segments ? ctx->visit_budget : total_items;
+    if (bounded) {
+        s = vkhr_reserve(ctx, (void**)&ctx->items, &ctx->items_cap, visits_total ? visits_total : 1, sizeof(uint2));
         if (s != VKHR_OK) return s;
     }
     VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_words, 0, WORD_NORM * sizeof(unsigned long long), st));
-    VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->brick_visits, 0, (size_t)g.nb * sizeof(uint32_t), st));
+    VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->brick_visits, 0, (size_t)total_bricks * sizeof(uint32_t), st));
     const unsigned threads = 256;
-    const unsigned in_blocks = std::min(vkhr_blocks(n_in, threads), (unsigned)ctx->sm_count * 16);
-    const float* tan_rec = tang ? tan_in : nullptr;
-    if (n_in) {
+    const unsigned in_blocks = std::min(vkhr_blocks(total_items, threads), (unsigned)ctx->sm_count * 16);
+    if (total_items) {
         if (segments)
-            VKHR_LAUNCH(ctx, (bin_kernel<false, true>), in_blocks, threads, 0, st, g, v, pairs, n_in, tan_rec,
+            VKHR_LAUNCH(ctx, (bin_kernel<false, true>), in_blocks, threads, 0, st, d_jobs, nj, total_items,
                         ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap,
                         ctx->d_words);
         else
-            VKHR_LAUNCH(ctx, (bin_kernel<false, false>), in_blocks, threads, 0, st, g, v, pairs, n_in, tan_rec,
+            VKHR_LAUNCH(ctx, (bin_kernel<false, false>), in_blocks, threads, 0, st, d_jobs, nj, total_items,
                         ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap,
                         ctx->d_words);
     }
-    const unsigned rblocks = std::min(vkhr_blocks(g.nb, kRangeThreads * kRangeItems), (unsigned)ctx->sm_count * 8);
-    VKHR_LAUNCH(ctx, bin_ranges_kernel, rblocks, kRangeThreads, 0, st, ctx->brick_visits, g.nb, ctx->brick_cursor,
-                ctx->brick_list, ctx->d_words);
-    VKHR_LAUNCH(ctx, zero_empty_kernel, dim3((g.w + 255) / 256, g.h, g.d), 256, 0, st, g, ctx->brick_visits, counts,
-                dens, tq32);
+    const unsigned rblocks = std::min(vkhr_blocks(total_bricks, kRangeThreads * kRangeItems), (unsigned)ctx->sm_count * 8);
+    VKHR_LAUNCH(ctx, bin_ranges_kernel, rblocks, kRangeThreads, 0, st, ctx->brick_visits, total_bricks,
+                ctx->brick_cursor, ctx->brick_list, ctx->d_words);
+    VKHR_LAUNCH(ctx, zero_empty_kernel, std::min(total_bricks, (uint32_t)ctx->sm_count * 16), 256, 0, st, d_jobs, nj,
+                total_bricks, ctx->brick_visits);
     VKHR_CUDA_TRY(ctx, cudaGetLastError());
 
-    // Sizes of the visit list and the crowded-voxel buffers.  Vertex mode is
-    // bounded by the vertex count; segment mode reads the total back.
-    uint64_t visits_total = n_in;
-    bool global_path = true; // vertex mode: launched, exits on the device when unneeded
-    if (segments) {
+    bool global_path = true; // when the totals stay on the device, the global path exits there if unneeded
+    if (!bounded) {          // segment mode without a budget: read the visit total back
+        if (capturing)
+            return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG,
+                             "segment voxelization under stream capture needs a visit budget (vkhr_set_visit_budget)");
         VKHR_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->h_words, ctx->d_words, WORD_NORM * sizeof(unsigned long long),
                                            cudaMemcpyDeviceToHost, st));
         VKHR_CUDA_TRY(ctx, cudaStreamSynchronize(st));
@@ -1012,6 +1140,8 @@ vkhr_status voxelize_impl(vkhr_ctx* ctx, bool segments, const float* v, const fl
         s = vkhr_reserve(ctx, (void**)&ctx->items, &ctx->items_cap, visits_total ? visits_total : 1, sizeof(uint2));
         if (s != VKHR_OK) return s;
     }
+    // capacities the kernels check against (the budget, not the grown scratch)
+    const size_t cap_visits = visits_total ? (size_t)visits_total : 1;
     if (tang) {
         s = vkhr_reserve(ctx, (void**)&ctx->hkeys, &ctx->hkeys_cap, visits_total ? visits_total : 1, sizeof(uint32_t));
         if (s != VKHR_OK) return s;
@@ -1019,63 +1149,70 @@ vkhr_status voxelize_impl(vkhr_ctx* ctx, bool segments, const float* v, const fl
                          sizeof(uint4));
         if (s != VKHR_OK) return s;
     }
-    if (global_path && n_in) {
-        s = vkhr_reserve(ctx, (void**)&ctx->cursor, &ctx->cursor_cap, g.n, sizeof(uint32_t));
+    if (global_path && total_items) {
+        s = vkhr_reserve(ctx, (void**)&ctx->cursor, &ctx->cursor_cap, max_voxels, sizeof(uint32_t));
         if (s != VKHR_OK) return s;
         s = vkhr_reserve(ctx, (void**)&ctx->list, &ctx->list_cap, visits_total ? visits_total : 1, sizeof(uint32_t));
         if (s != VKHR_OK) return s;
         s = vkhr_reserve(ctx, (void**)&ctx->gdesc, &ctx->gdesc_cap, visits_total / (kMediumSort + 1) + 1,
                          sizeof(uint4));
         if (s != VKHR_OK) return s;
-        const unsigned vblocks = std::min(vkhr_blocks(g.n, threads), (unsigned)ctx->sm_count * 32);
-        VKHR_LAUNCH(ctx, global_clear_kernel, vblocks, threads, 0, st, counts, g.n, ctx->d_words);
-        if (segments)
-            VKHR_LAUNCH(ctx, (global_visit_kernel<false, true>), in_blocks, threads, 0, st, g, v, pairs, n_in,
-                        ctx->brick_visits, counts, ctx->cursor, ctx->list, ctx->list_cap, ctx->d_words);
-        else
-            VKHR_LAUNCH(ctx, (global_visit_kernel<false, false>), in_blocks, threads, 0, st, g, v, pairs, n_in,
-                        ctx->brick_visits, counts, ctx->cursor, ctx->list, ctx->list_cap, ctx->d_words);
-        const unsigned gr = std::min(vkhr_blocks(g.n, kRangeThreads * kRangeItems), (unsigned)ctx->sm_count * 8);
-        VKHR_LAUNCH(ctx, global_ranges_kernel, gr, kRangeThreads, 0, st, counts, g.n, ctx->cursor, ctx->d_words);
-        if (tang) {
+        for (int j = 0; j < nj; ++j) { // each style's crowded bricks, one after the other
+            const VoxJob& J = jobs[j];
+            if (!J.n_in) continue;
+            const Grid& g = J.g;
+            const uint32_t* jv = ctx->brick_visits + J.brick_base;
+            const unsigned vblocks = std::min(vkhr_blocks(g.n, threads), (unsigned)ctx->sm_count * 32);
+            const unsigned jb = std::min(vkhr_blocks(J.n_in, threads), (unsigned)ctx->sm_count * 16);
+            VKHR_LAUNCH(ctx, global_clear_kernel, vblocks, threads, 0, st, J.counts, g.n, ctx->d_words);
             if (segments)
-                VKHR_LAUNCH(ctx, (global_visit_kernel<true, true>), in_blocks, threads, 0, st, g, v, pairs, n_in,
-                            ctx->brick_visits, counts, ctx->cursor, ctx->list, ctx->list_cap, ctx->d_words);
+                VKHR_LAUNCH(ctx, (global_visit_kernel<false, true>), jb, threads, 0, st, g, J.v, J.pairs, J.n_in, jv,
+                            J.counts, ctx->cursor, ctx->list, cap_visits, ctx->d_words);
             else
-                VKHR_LAUNCH(ctx, (global_visit_kernel<true, false>), in_blocks, threads, 0, st, g, v, pairs, n_in,
-                            ctx->brick_visits, counts, ctx->cursor, ctx->list, ctx->list_cap, ctx->d_words);
+                VKHR_LAUNCH(ctx, (global_visit_kernel<false, false>), jb, threads, 0, st, g, J.v, J.pairs, J.n_in, jv,
+                            J.counts, ctx->cursor, ctx->list, cap_visits, ctx->d_words);
+            const unsigned gr = std::min(vkhr_blocks(g.n, kRangeThreads * kRangeItems), (unsigned)ctx->sm_count * 8);
+            VKHR_LAUNCH(ctx, global_ranges_kernel, gr, kRangeThreads, 0, st, J.counts, g.n, ctx->cursor, ctx->d_words);
+            if (tang) {
+                if (segments)
+                    VKHR_LAUNCH(ctx, (global_visit_kernel<true, true>), jb, threads, 0, st, g, J.v, J.pairs, J.n_in, jv,
+                                J.counts, ctx->cursor, ctx->list, cap_visits, ctx->d_words);
+                else
+                    VKHR_LAUNCH(ctx, (global_visit_kernel<true, false>), jb, threads, 0, st, g, J.v, J.pairs, J.n_in,
+                                jv, J.counts, ctx->cursor, ctx->list, cap_visits, ctx->d_words);
+            }
+            VKHR_LAUNCH(ctx, global_resolve_kernel, vblocks, threads, 0, st, g, jv, J.counts, ctx->cursor, ctx->list,
+                        cap_visits, J.tan, J.pairs, J.dens, J.tq, ctx->gdesc, ctx->gdesc_cap, (uint32_t)j,
+                        ctx->d_words);
         }
-        VKHR_LAUNCH(ctx, global_resolve_kernel, vblocks, threads, 0, st, g, ctx->brick_visits, counts, ctx->cursor,
-                    ctx->list, tan_in, segments ? pairs : nullptr, dens, tang ? tq32 : nullptr, ctx->gdesc,
-                    ctx->gdesc_cap, ctx->d_words);
         if (tang)
-            VKHR_LAUNCH(ctx, global_crowded_kernel, (unsigned)ctx->sm_count * 2, 256, 0, st, ctx->gdesc, ctx->gdesc_cap,
-                        ctx->list, tan_in, segments ? pairs : nullptr, tq32, ctx->d_words);
+            VKHR_LAUNCH(ctx, global_crowded_kernel, (unsigned)ctx->sm_count * 2, 256, 0, st, d_jobs, ctx->gdesc,
+                        ctx->gdesc_cap, ctx->list, ctx->d_words);
         VKHR_CUDA_TRY(ctx, cudaGetLastError());
     }
-    if (n_in) {
+    if (total_items) {
         if (segments)
-            VKHR_LAUNCH(ctx, (bin_kernel<true, true>), in_blocks, threads, 0, st, g, v, pairs, n_in, tan_rec,
-                        ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap,
+            VKHR_LAUNCH(ctx, (bin_kernel<true, true>), in_blocks, threads, 0, st, d_jobs, nj, total_items,
+                        ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->items, cap_visits,
                         ctx->d_words);
         else
-            VKHR_LAUNCH(ctx, (bin_kernel<true, false>), in_blocks, threads, 0, st, g, v, pairs, n_in, tan_rec,
-                        ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap,
+            VKHR_LAUNCH(ctx, (bin_kernel<true, false>), in_blocks, threads, 0, st, d_jobs, nj, total_items,
+                        ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->items, cap_visits,
                         ctx->d_words);
     }
     const size_t smem = (size_t)(2 * kBrickThreads + 32 + kBrickThreads + kBrickWarps * 3 * 64 + (tang ? kBrickCap : 0)) *
                         sizeof(uint32_t);
-    const unsigned bblocks = std::min(g.nb, (unsigned)ctx->sm_count * 2);
+    const unsigned bblocks = std::min(total_bricks, (unsigned)ctx->sm_count * 2);
     if (segments)
-        s = tang ? launch_brick<true, true>(ctx, g, tan_in, counts, dens, tq32, st, bblocks, smem)
-                 : launch_brick<true, false>(ctx, g, tan_in, counts, dens, tq32, st, bblocks, smem);
+        s = tang ? launch_brick<true, true>(ctx, d_jobs, nj, st, bblocks, smem, cap_visits)
+                 : launch_brick<true, false>(ctx, d_jobs, nj, st, bblocks, smem, cap_visits);
     else
-        s = tang ? launch_brick<false, true>(ctx, g, tan_in, counts, dens, tq32, st, bblocks, smem)
-                 : launch_brick<false, false>(ctx, g, tan_in, counts, dens, tq32, st, bblocks, smem);
+        s = tang ? launch_brick<false, true>(ctx, d_jobs, nj, st, bblocks, smem, cap_visits)
+                 : launch_brick<false, false>(ctx, d_jobs, nj, st, bblocks, smem, cap_visits);
     if (s != VKHR_OK) return s;
     if (tang)
-        VKHR_LAUNCH(ctx, crowded_kernel, (unsigned)ctx->sm_count * 2, 256, 0, st, ctx->hdesc, ctx->hdesc_cap, ctx->hkeys,
-                    tan_in, segments ? pairs : nullptr, tq32, ctx->d_words);
+        VKHR_LAUNCH(ctx, crowded_kernel, (unsigned)ctx->sm_count * 2, 256, 0, st, d_jobs, ctx->hdesc, ctx->hdesc_cap,
+                    ctx->hkeys, ctx->d_words);
     VKHR_CUDA_TRY(ctx, cudaGetLastError());
     return VKHR_OK;
 }
@@ -1089,8 +1226,11 @@ vkhr_status vkhr_voxelize_vertices(vkhr_ctx* ctx, const float* d_vertices, const
                                    int32_t depth, int32_t index_mode, uint32_t* d_counts, uint8_t* d_densities,
                                    int8_t* d_tangents, void* stream)
 {
-    return voxelize_impl(ctx, false, d_vertices, d_tangent_in, nullptr, vertex_count, bounds, width, height, depth,
-                         index_mode, d_counts, d_densities, d_tangents, (cudaStream_t)stream);
+    if (!ctx) return VKHR_ERR_INVALID_ARG;
+    if (!bounds) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "bounds is NULL");
+    vkhr_voxel_job j = {d_vertices, d_tangent_in, nullptr, vertex_count, *bounds, width, height, depth, index_mode,
+                        d_counts, d_densities, d_tangents};
+    return voxelize_batch(ctx, false, &j, 1, (cudaStream_t)stream);
 }
 
 vkhr_status vkhr_voxelize_segments(vkhr_ctx* ctx, const float* d_vertices, const float* d_tangent_in,
@@ -1098,9 +1238,25 @@ vkhr_status vkhr_voxelize_segments(vkhr_ctx* ctx, const float* d_vertices, const
                                    int32_t width, int32_t height, int32_t depth, int32_t index_mode,
                                    uint32_t* d_counts, uint8_t* d_densities, int8_t* d_tangents, void* stream)
 {
-    // for (i = 0; i < indices.size() - 1; i += 2): floor(n / 2) pairs
-    return voxelize_impl(ctx, true, d_vertices, d_tangent_in, d_indices, index_count / 2, bounds, width, height,
-                         depth, index_mode, d_counts, d_densities, d_tangents, (cudaStream_t)stream);
+    if (!ctx) return VKHR_ERR_INVALID_ARG;
+    if (!bounds) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "bounds is NULL");
+    vkhr_voxel_job j = {d_vertices, d_tangent_in, d_indices, index_count, *bounds, width, height, depth, index_mode,
+                        d_counts, d_densities, d_tangents};
+    return voxelize_batch(ctx, true, &j, 1, (cudaStream_t)stream);
+}
+
+vkhr_status vkhr_voxelize_batched(vkhr_ctx* ctx, int32_t segments, const vkhr_voxel_job* jobs, int32_t job_count,
+                                  void* stream)
+{
+    return voxelize_batch(ctx, segments != 0, jobs, job_count, (cudaStream_t)stream);
+}
+
+vkhr_status vkhr_set_visit_budget(vkhr_ctx* ctx, uint64_t max_visits)
+{
+    if (!ctx) return VKHR_ERR_INVALID_ARG;
+    if (max_visits >= (1ull << 32)) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "budget must be below 2^32 visits");
+    ctx->visit_budget = max_visits;
+    return VKHR_OK;
 }
 
 vkhr_status vkhr_check_status(vkhr_ctx* ctx, void* stream)
