@@ -49,6 +49,10 @@ WORKLOAD = {
     "density": "u8 unorm (normalized)",
     "l2": "flushed before every timed step (512 MiB write)",
 }
+# DRAM bytes (read + write) per launch from one ncu capture of the production
+# frame (profiles/*_production_frame.md); None until captured for this build.
+TRAFFIC = {}
+
 METRIC = "Msegments/s voxelized + Mpixels/s raymarched, 1 GB300 (frame throughput in Mpixels/s)"
 UNIT = "Mpixels/s"
 
@@ -180,6 +184,173 @@ def reference_arm(args):
     return 0
 
 
+BATCH = {
+    "workload": "16 styles in one batched voxelize + one persistent raymarch launch, CUDA graph: strands "
+                "log-uniform 5k-136k, 8-32 vertices, grids from {64,128,192,256}^3, each in a 3840x2160 view at "
+                "the distance giving a 64-1024 pixel footprint; 512 steps, 64-step shadows, 8-tap AO on uint32 "
+                "counts (isosurface 1 count)",
+    "plain": "per style: vkhr_voxelize_segments (sizes its visit list from a host read) + vkhr_raymarch of "
+             "the whole 3840x2160 view",
+}
+
+
+def batched_comparison(args, dev, stream, rank, world, flush):
+    """The multi-style batch three ways: plain per-style calls, the batched
+    calls, and the batched calls replayed from a CUDA graph.  Returns the
+    JSON object of the comparison (times are maxima over ranks; each rank
+    takes its share of the styles)."""
+    import torch
+
+    from vkhr_gb300 import _abi, _native, replicas, scene, workloads
+
+    specs = workloads.batched_specs()
+    costs = [sp["strands"] * (sp["vertices_per_strand"] - 1) * sp["resolution"] for sp in specs]
+    mine = replicas.shard(costs, rank, world)
+    W, H = workloads.BATCH_TARGET
+    s = stream.cuda_stream
+    ctx_p = _native.Context(dev.index)
+    ctx_b = _native.Context(dev.index)
+    styles = []
+    for i in mine:
+        sp = specs[i]
+        st, t, idx = workloads.grow(sp)
+        res = (sp["resolution"],) * 3
+        n = res[0] ** 3
+        x = {"spec": sp, "segments": st.segment_count, "index_count": int(idx.shape[0]), "res": res,
+             "dv": torch.from_numpy(st.vertices).to(dev), "dt": torch.from_numpy(t).to(dev),
+             "di": torch.from_numpy(idx.view(np.int32)).to(dev),
+             "counts_p": torch.empty(n, dtype=torch.int32, device=dev),
+             "tq_p": torch.empty((n, 4), dtype=torch.int8, device=dev),
+             "counts_b": torch.empty(n, dtype=torch.int32, device=dev),
+             "tq_b": torch.empty((n, 4), dtype=torch.int8, device=dev)}
+        x["b"] = ctx_p.bounding_box(x["dv"].data_ptr(), st.vertex_count, s)
+        dist = workloads.camera_distance(x["b"], sp["footprint"], H)
+        x["p"] = scene.make_params(x["b"], res, W, H, camera_distance=dist, view_direction=sp["view_direction"],
+                                   raycast_steps=512.0, shadow_steps=64.0, isosurface=1.0,
+                                   density_format=_abi.DENSITY_U32_COUNT)
+        x["distance"] = dist
+        x["rect"] = _native.raymarch_footprint(x["p"])
+        styles.append(x)
+    pos, atlas_h = workloads.shelf_pack([(x["rect"][2], x["rect"][3]) for x in styles], W)
+    atlas = torch.zeros((max(atlas_h, 1), W, 4), dtype=torch.float32, device=dev)
+    atlas_d = torch.ones((max(atlas_h, 1), W), dtype=torch.float32, device=dev)
+    full = torch.empty((H, W, 4), dtype=torch.float32, device=dev)
+    full_d = torch.empty((H, W), dtype=torch.float32, device=dev)
+    vjobs, rjobs = [], []
+    for x, (ax, ay) in zip(styles, pos):
+        v = _abi.VoxelJob()
+        v.d_vertices, v.d_tangent_in, v.d_indices = x["dv"].data_ptr(), x["dt"].data_ptr(), x["di"].data_ptr()
+        v.item_count = x["index_count"]
+        v.bounds = x["b"]
+        v.width, v.height, v.depth = x["res"]
+        v.index_mode = _abi.INDEX_REF_FP32
+        v.d_counts, v.d_densities, v.d_tangents = x["counts_b"].data_ptr(), None, x["tq_b"].data_ptr()
+        vjobs.append(v)
+        r = _abi.RaymarchJob()
+        r.params = x["p"]
+        r.d_density, r.d_tangent, r.d_depth_in = x["counts_b"].data_ptr(), x["tq_b"].data_ptr(), None
+        r.d_rgba, r.d_depth_out = atlas[ay, ax].data_ptr(), atlas_d[ay, ax].data_ptr()
+        r.x0, r.y0, r.w, r.h = x["rect"]
+        r.pitch = W
+        rjobs.append(r)
+
+    def plain():
+        for x in styles:
+            ctx_p.voxelize_segments(x["dv"].data_ptr(), x["dt"].data_ptr(), x["di"].data_ptr(), x["index_count"],
+                                    x["b"], x["res"], _abi.INDEX_REF_FP32, x["counts_p"].data_ptr(), None,
+                                    x["tq_p"].data_ptr(), s)
+            ctx_p.raymarch(x["p"], x["counts_p"].data_ptr(), x["tq_p"].data_ptr(), None, full.data_ptr(),
+                           full_d.data_ptr(), s)
+
+    def batched(st_handle):
+        ctx_b.voxelize_batched(True, vjobs, st_handle)
+        ctx_b.raymarch_batched(rjobs, st_handle)
+
+    # the visit budget from one counted run (+25%), then a warm-up at that budget and the capture
+    ctx_b.voxelize_batched(True, vjobs, s)
+    ctx_b.check_status(s)
+    visits = int(sum(int(x["counts_b"].sum(dtype=torch.int64).item()) for x in styles))
+    ctx_b.set_visit_budget(visits + visits // 4 + 4096)
+    side = torch.cuda.Stream(device=dev)
+    side.wait_stream(stream)
+    with torch.cuda.stream(side):
+        batched(side.cuda_stream)
+    ctx_b.check_status(side.cuda_stream)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        batched(torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+
+    variants = {"plain": plain, "batched": lambda: batched(s), "batched_graph": graph.replay}
+    launches = {}
+    for _ in range(max(args.warmup, 3)):
+        for f in variants.values():
+            flush.zero_()
+            f()
+    torch.cuda.synchronize()
+    times = {k: [] for k in variants}
+    walls = {k: [] for k in variants}
+    for _ in range(args.steps):
+        for k, f in variants.items():
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            l0 = ctx_p.launch_count() + ctx_b.launch_count()
+            w0 = time.perf_counter()
+            e0.record(stream)
+            f()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            walls[k].append((time.perf_counter() - w0) * 1e3)
+            times[k].append(e0.elapsed_time(e1))
+            launches[k] = ctx_p.launch_count() + ctx_b.launch_count() - l0
+    ctx_b.check_status(s)
+    # per-kernel device time of the batched calls (event pair per launch, outside the timed runs)
+    ctx_b.set_profiling(True)
+    flush.zero_()
+    batched(s)
+    torch.cuda.synchronize()
+    kern = {}
+    for name, kms in ctx_b.profile():
+        e = kern.setdefault(name, [0, 0.0])
+        e[0] += 1
+        e[1] += kms
+    ctx_b.set_profiling(False)
+    ms = {k: replicas.max_over_ranks(statistics.median(v), device=dev) for k, v in times.items()}
+    wall_ms = {k: replicas.max_over_ranks(statistics.median(v), device=dev) for k, v in walls.items()}
+
+    # identical results: voxels bit-exact, and every region equal to the plain full-view render
+    same = all(torch.equal(x["counts_p"], x["counts_b"]) and torch.equal(x["tq_p"], x["tq_b"]) for x in styles)
+    for x, (ax, ay) in zip(styles, pos):
+        x0, y0, w, h = x["rect"]
+        ctx_p.raymarch(x["p"], x["counts_b"].data_ptr(), x["tq_b"].data_ptr(), None, full.data_ptr(),
+                       full_d.data_ptr(), s)
+        torch.cuda.synchronize()
+        outside = full.clone()
+        outside[y0:y0 + h, x0:x0 + w] = 0.0
+        same = same and torch.equal(atlas[ay:ay + h, ax:ax + w], full[y0:y0 + h, x0:x0 + w])
+        same = same and torch.equal(atlas_d[ay:ay + h, ax:ax + w], full_d[y0:y0 + h, x0:x0 + w])
+        same = same and not bool(outside.any())
+    segs = sum(x["segments"] for x in styles)
+    pixels = sum(x["rect"][2] * x["rect"][3] for x in styles)
+    out = {
+        "config": dict(BATCH, styles=len(specs), ranks=world),
+        "styles_this_rank": [{"strands": x["spec"]["strands"], "vertices": x["spec"]["vertices_per_strand"],
+                              "resolution": x["res"][0], "footprint": list(x["rect"][2:]),
+                              "camera_distance": round(x["distance"], 2)} for x in styles],
+        "segments": segs, "region_pixels": pixels, "visits": visits,
+        "ms": ms, "wall_ms": wall_ms, "launches_per_step": launches,
+        "batched_kernels_ms": {k: round(v[1], 4) for k, v in sorted(kern.items(), key=lambda kv: -kv[1][1])},
+        "speedup_vs_plain": {"batched": ms["plain"] / ms["batched"], "batched_graph": ms["plain"] / ms["batched_graph"]},
+        "batched_graph_msegments_per_s": world * segs / (ms["batched_graph"] / 1e3) / 1e6,
+        "batched_graph_region_mpixels_per_s": world * pixels / (ms["batched_graph"] / 1e3) / 1e6,
+        "identical_to_plain": bool(same),
+    }
+    ctx_b.set_visit_budget(0)
+    return out
+
+
 def gb300_arm(args):
     import torch
 
@@ -272,20 +443,35 @@ def gb300_arm(args):
     top_avg_ms = top_ms / top_n
     S = st.segment_count
     V = st.vertex_count
-    visits = None
+    # algorithmic (compulsory) bytes, each byte once
+    visits = int(counts.sum(dtype=torch.int64).item())
+    R = WORKLOAD["resolution"]
+    occupied = int(counts.view(R // 8, 8, R // 8, 8, R // 8, 8).amax(dim=(1, 3, 5)).gt(0).sum().item())
     alg = {
-        # read voxel-space stepping inputs once (index pairs + both vertices per pair), update counts
-        "count_segments_kernel": 8 * S + 24 * S + 4 * n,
-        "fill_segments_kernel": 8 * S + 24 * S + 4 * n,
-        "resolve_kernel": 4 * n + 4 * n + n + 4 * n,
+        # visit entries (8 B) + the pair tangents once (16 B) + counts, u8 and i8x4 of the occupied bricks
+        "(brick_kernel<SEG, TANG>)": 8 * visits + 16 * S + 9 * 512 * occupied,
+        # index pairs + both vertices of each pair once + the visit entries written
+        "(bin_kernel<true, true>)": 8 * S + 24 * V + 8 * visits,
+        "(bin_kernel<false, true>)": 8 * S + 24 * V + 32 * S,
+        # u8 densities + i8x4 tangents once + the RGBA and depth outputs
         "(raymarch_kernel<DF, TF>)": n * 1 + n * 4 + px * 20,
-        "alloc_ranges_kernel": 8 * n,
     }
     alg_bytes = alg.get(top_name)
     achieved = (alg_bytes / (top_avg_ms / 1e3) / 1e9) if alg_bytes else None
     roofline = {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": (achieved / hbm) if achieved else None, "traffic": None, "peak_kind": peak_kind,
-                "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": top_avg_ms}
+                "frac": (achieved / hbm) if achieved else None, "traffic": TRAFFIC.get(top_name),
+                "peak_kind": peak_kind, "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": top_avg_ms,
+                "visits": visits, "occupied_bricks": occupied}
+    # whole stages against the same peak: inputs once + outputs once
+    vox_alg = 24 * V + 8 * S + 9 * n
+    ray_alg = n * 1 + n * 4 + px * 20
+    vms, rms_ = sum(vox_ms) / args.steps, sum(ray_ms) / args.steps
+    stages = {
+        "voxelize": {"alg_bytes": vox_alg, "ms": vms, "achieved_gbs": vox_alg / (vms / 1e3) / 1e9,
+                     "frac": vox_alg / (vms / 1e3) / 1e9 / hbm},
+        "raymarch": {"alg_bytes": ray_alg, "ms": rms_, "achieved_gbs": ray_alg / (rms_ / 1e3) / 1e9,
+                     "frac": ray_alg / (rms_ / 1e3) / 1e9 / hbm},
+    }
 
     # ---- end to end through the C ABI with host buffers ------------------------
     hv = torch.from_numpy(st.vertices).pin_memory()
@@ -312,6 +498,8 @@ def gb300_arm(args):
     h2d = hv.numel() * 4 + ht.numel() * 4 + hi.numel() * 4
     d2h = ho.numel() * 4 + hd.numel() * 4
 
+    batched = None if args.no_batched else batched_comparison(args, dev, stream, rank, world, flush)
+
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -324,11 +512,14 @@ def gb300_arm(args):
         },
         "kernels": {k: {"launches": v[0], "avg_ms": v[1] / v[0]} for k, v in sorted(per_kernel.items())},
         "roofline": roofline,
+        "roofline_stages": stages,
         "e2e": {"value": world * px / (e2e_ms / 1e3) / 1e6, "unit": UNIT, "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "clocks": clocks.summary(),
     }
+    if batched is not None:
+        line["batched"] = batched
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import oracle as O
 
@@ -356,6 +547,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 16-style batched vs plain comparison")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)

@@ -19,7 +19,7 @@ RES_CHOICES = [(16, 16, 16), (24, 24, 24), (32, 32, 32), (37, 50, 29), (48, 48, 
 def _styles(seed, n_jobs, crowded=True):
     """Uneven styles: strand counts log-uniform in [50, 3000], 8-32 vertices
     per strand, grids from RES_CHOICES; optionally one dense style in an 8^3
-    grid whose bricks exceed the shared-memory capacity (global path)."""
+    grid whose bricks exceed the shared-memory capacity (keys sorted in global scratch)."""
     rng = np.random.default_rng(seed)
     out = []
     for j in range(n_jobs):

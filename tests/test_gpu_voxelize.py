@@ -49,6 +49,24 @@ def test_saturation_and_crowded_voxels(ctx, oracle_lib):
         assert c.max() > 2048
 
 
+def test_bricks_above_shared_capacity(ctx, oracle_lib):
+    """A dense style in a small, ragged grid: many bricks with more visits
+    than a brick sorts in shared memory (keys sorted in the global scratch),
+    next to bricks that fit, in both modes."""
+    st, t, idx = style("hemi", 30_000, 16)
+    b = oracle_lib.bounding_box(st.vertices)
+    for mode in ("vertices", "segments"):
+        c = _check(ctx, oracle_lib, mode, st.vertices, t, idx, b, (20, 17, 23))
+        bricks = np.zeros((3, 3, 3), dtype=np.int64)
+        cz = c.reshape(23, 17, 20)
+        for z in range(3):
+            for y in range(3):
+                for x in range(3):
+                    bricks[z, y, x] = cz[8 * z:8 * z + 8, 8 * y:8 * y + 8, 8 * x:8 * x + 8].sum()
+        if mode == "segments":
+            assert bricks.max() > 22528 and (bricks[bricks > 0] <= 22528).any()
+
+
 def test_exact_index_mode(ctx, oracle_lib):
     st, t, idx = style("hemi", 2048, 12)
     b = oracle_lib.bounding_box(st.vertices)

@@ -21,13 +21,13 @@ enum : unsigned {
 // Slots of the small device word array every context owns.
 enum {
     WORD_TOTAL_VISITS = 0,      // voxel visits of the current voxelization
-    WORD_LIST_CURSOR = 1,       // global path: allocation cursor of the visit list
-    WORD_HEAVY_COUNT = 2,       // global path: crowded-voxel descriptors
+    WORD_BIG_LIST = 1,          // brick path: bricks above the shared-memory capacity
+    WORD_BIG_QUEUE = 2,         // brick path: next entry of that list
     WORD_STATUS = 3,            // VKHR_DEV_* bits
     WORD_BRICK_CURSOR = 4,      // brick path: allocation cursor of the visit list
     WORD_MAX_BRICK_VISITS = 5,  // brick path: largest brick
     WORD_BHEAVY_COUNT = 6,      // brick path: crowded-voxel descriptors
-    WORD_HKEYS_CURSOR = 7,      // brick path: crowded-voxel key buffer cursor
+    WORD_HKEYS_CURSOR = 7,      // brick path: key scratch cursor (crowded voxels, bricks above kBrickCap)
     WORD_BRICK_QUEUE = 8,       // brick path: next entry of the occupied-brick list
     WORD_BRICK_LIST = 9,        // brick path: occupied bricks resolved in shared memory
     WORD_NORM = 10,             // normalize: min, max (2 slots); words below are cleared per voxelization
@@ -40,11 +40,11 @@ struct vkhr_ctx {
     int device;
     int sm_count;
     // grow-only scratch (capacities in elements)
-    uint32_t* brick_runs;      // voxelizer: runs, visits and run-list cursor per brick (3 x bricks)
+    uint32_t* brick_runs;      // voxelizer: visits and visit-list cursor per brick (2 x bricks)
     uint32_t* brick_visits;
     uint32_t* brick_cursor;
     size_t brick_cap;
-    uint2* items;              // voxelizer: run items (pair, first step << 8 | length) or (vertex, voxel)
+    uint2* items;              // voxelizer: visit entries (key, local voxel), grouped by brick
     size_t items_cap;
     uint32_t* brick_list;      // voxelizer: occupied bricks of the shared-memory path
     size_t brick_list_cap;
@@ -52,16 +52,10 @@ struct vkhr_ctx {
     size_t pair_rec_cap;
     float4* pair_tan;          // voxelizer: per index pair, the tangent of its first vertex
     size_t pair_tan_cap;
-    uint32_t* hkeys;           // voxelizer: keys of crowded voxels
+    uint32_t* hkeys;           // voxelizer: key scratch (crowded voxels, bricks above the shared-memory cap)
     size_t hkeys_cap;
-    uint4* hdesc;              // voxelizer: crowded voxels (voxel, key offset, count)
+    uint4* hdesc;              // voxelizer: crowded voxels (voxel, key offset, count, job)
     size_t hdesc_cap;
-    uint32_t* cursor;          // global path: per-voxel list cursor
-    size_t cursor_cap;
-    uint32_t* list;            // global path: visit keys
-    size_t list_cap;
-    uint4* gdesc;              // global path: crowded voxels
-    size_t gdesc_cap;
     void* d_jobs;              // voxelizer: device job table of the current batch
     size_t jobs_cap;           // in bytes
     void* h_jobs;              // pinned staging of the job table

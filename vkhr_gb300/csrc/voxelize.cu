@@ -43,10 +43,8 @@ constexpr int kBrickCap = 22528;       // visits a brick resolves in shared memo
 constexpr int kBrickThread = 16;       // <= this many visits: sorted and summed by the voxel's thread
 constexpr int kBrickSmall = 64;        // <= this many visits: sorted by one warp (2 keys per lane)
 constexpr int kBrickWarps = kBrickThreads / 32;
-constexpr int kSmallSort = 16;         // global path: register-network resolve
-constexpr int kMediumSort = 64;        // global path: 64-key register network
 constexpr int kHeavyTile = 2048;       // crowded voxels: shared-memory sort tile
-constexpr int kKeep = 256;             // smallest keys carried between tiles (>= 255)
+constexpr int kKeep = 256;             // crowded voxels: tangents summed (>= 255)
 constexpr int kRangeThreads = 256;
 constexpr int kRangeItems = 16;
 constexpr uint32_t kNoBrick = 0xffffffffu;
@@ -89,6 +87,7 @@ struct VoxJob {
 };
 
 static_assert(sizeof(VoxJob) * kMaxJobs <= kJobTableBytes, "job table staging too small");
+static_assert(sizeof(VoxJob) % 4 == 0 && (sizeof(VoxJob) + 4) * kMaxJobs <= 48 * 1024, "bin kernels keep the table in shared memory");
 
 // Largest j with base[j] <= x (base ascending, base[0] = 0).
 __device__ __forceinline__ int find_job(const uint32_t* base, int nj, uint32_t x)
@@ -250,12 +249,17 @@ __global__ void bin_kernel(const VoxJob* __restrict__ jobs, int nj, uint32_t tot
                            float4* pair_tan, uint32_t* visits, uint32_t* cursor, uint2* entries, size_t entries_cap,
                            unsigned long long* words)
 {
-    __shared__ uint32_t s_item_base[kMaxJobs];
+    // the job table in shared memory (nj * (sizeof(VoxJob) + 4) bytes of dynamic shared memory)
+    extern __shared__ __align__(16) unsigned char bin_smem[];
+    VoxJob* s_jobs = reinterpret_cast<VoxJob*>(bin_smem);
+    uint32_t* s_item_base = reinterpret_cast<uint32_t*>(s_jobs + nj);
+    for (int i = threadIdx.x; i < nj * (int)(sizeof(VoxJob) / 4); i += blockDim.x)
+        reinterpret_cast<uint32_t*>(s_jobs)[i] = __ldg(reinterpret_cast<const uint32_t*>(jobs) + i);
     load_bases(jobs, nj, s_item_base, nullptr);
     unsigned status = 0;
     for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < total_items;
          q += (uint64_t)gridDim.x * blockDim.x) {
-        const VoxJob& J = jobs[find_job(s_item_base, nj, (uint32_t)q)];
+        const VoxJob& J = s_jobs[find_job(s_item_base, nj, (uint32_t)q)];
         const Grid& g = J.g;
         const uint32_t p = (uint32_t)q - J.item_base;
         if (SEG) {
@@ -354,13 +358,17 @@ __global__ void __launch_bounds__(kRangeThreads) bin_ranges_kernel(const uint32_
             const uint64_t i = base + (uint64_t)j * kRangeThreads + threadIdx.x;
             if (i < nb) cursor[i] = start;
             start += c[j];
-            // bricks for the shared-memory resolve: visited, within capacity
-            const bool listed = c[j] > 0u && c[j] <= (uint32_t)kBrickCap;
-            const unsigned m = __ballot_sync(0xffffffffu, listed);
-            uint32_t at = 0;
+            // visited bricks: up to kBrickCap visits listed from the front, more from the back
+            const bool small = c[j] > 0u && c[j] <= (uint32_t)kBrickCap, big = c[j] > (uint32_t)kBrickCap;
+            const unsigned m = __ballot_sync(0xffffffffu, small), mb = __ballot_sync(0xffffffffu, big);
+            uint32_t at = 0, atb = 0;
             if (lane == 0 && m) at = (uint32_t)atomicAdd(words + WORD_BRICK_LIST, (unsigned long long)__popc(m));
+            if (lane == 0 && mb) atb = (uint32_t)atomicAdd(words + WORD_BIG_LIST, (unsigned long long)__popc(mb));
             at = __shfl_sync(0xffffffffu, at, 0);
-            if (listed) list[at + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
+            atb = __shfl_sync(0xffffffffu, atb, 0);
+            const unsigned below = (1u << lane) - 1u;
+            if (small) list[at + __popc(m & below)] = (uint32_t)i;
+            if (big) list[nb - 1u - (atb + __popc(mb & below))] = (uint32_t)i;
         }
         __syncthreads();
     }
@@ -468,12 +476,130 @@ __device__ __forceinline__ float4 visit_tangent(const float4* __restrict__ pair_
     return make_float4(__ldg(t), __ldg(t + 1), __ldg(t + 2), 0.0f);
 }
 
+// Per-voxel results of one brick whose visit keys are grouped by local voxel
+// at `keys` (shared memory, or the global scratch for bricks above
+// kBrickCap): counts and u8 densities, and the tangents by visit count --
+// up to kBrickThread visits by the voxel's thread, up to kBrickSmall by a
+// warp, more by crowded_kernel through a descriptor.  Block-wide.
 template <bool SEG, bool TANG>
+__device__ __forceinline__ void resolve_brick(const VoxJob& J, const Grid& g, uint32_t b, const float4* pair_tan,
+                                              const uint32_t* cnt, const uint32_t* off, uint32_t* keys,
+                                              bool keys_global, uint32_t keys_at, uint32_t* wlist, uint32_t& wcount,
+                                              float* wtan, uint4* hdesc, size_t hdesc_cap, uint32_t* hkeys,
+                                              size_t hkeys_cap, uint32_t job, unsigned long long* words,
+                                              unsigned& status)
+{
+    const int tid = threadIdx.x;
+    const float* tan = J.tan;
+    uint32_t* tq = J.tq;
+    const uint32_t bx = b % g.nbx, by = (b / g.nbx) % g.nby, bz = b / (g.nbx * g.nby);
+    const uint32_t x = bx * 8 + (tid & 7), y = by * 8 + ((tid >> 3) & 7), z = bz * 8 + (tid >> 6);
+    if (x < g.w && y < g.h && z < g.d) {
+        const uint32_t c = cnt[tid];
+        const uint32_t vi = x + g.w * (y + g.h * z);
+        J.counts[vi] = c;
+        if (J.dens) J.dens[vi] = (uint8_t)(c < 255u ? c : 255u);
+        if (TANG) {
+            if (c == 0) {
+                tq[vi] = 0u;
+            } else if (c > (uint32_t)kBrickThread && c <= (uint32_t)kBrickSmall) {
+                wlist[atomicAdd(&wcount, 1u)] = (uint32_t)tid; // resolved by a warp below
+            } else if (c <= (uint32_t)kBrickThread) {
+                uint32_t* k = keys + (off[tid] - c);
+                for (uint32_t i = 1; i < c; ++i) { // insertion sort: serial order
+                    const uint32_t key = k[i];
+                    uint32_t j = i;
+                    while (j > 0 && k[j - 1] > key) {
+                        k[j] = k[j - 1];
+                        --j;
+                    }
+                    k[j] = key;
+                }
+                // gather 8 tangents at a time (independent loads), then add them in key order
+                float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+                for (uint32_t i0 = 0; i0 < c; i0 += 8) {
+                    float4 tv[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j)
+                        if (i0 + j < c) tv[j] = visit_tangent<SEG>(pair_tan, tan, k[i0 + j]);
+#pragma unroll
+                    for (int j = 0; j < 8; ++j)
+                        if (i0 + j < c) {
+                            sx = __fadd_rn(sx, tv[j].x);
+                            sy = __fadd_rn(sy, tv[j].y);
+                            sz = __fadd_rn(sz, tv[j].z);
+                        }
+                }
+                tq[vi] = pack_tangent(sx, sy, sz, c);
+            } else { // crowded: a CTA of its own sorts the keys
+                const unsigned long long hd = atomicAdd(words + WORD_BHEAVY_COUNT, 1ull);
+                if (keys_global) { // already in the scratch
+                    if (hd < hdesc_cap) hdesc[hd] = make_uint4(vi, keys_at + off[tid] - c, c, job);
+                    else status |= VKHR_DEV_LIST_OVERFLOW;
+                } else {
+                    const unsigned long long hb = atomicAdd(words + WORD_HKEYS_CURSOR, (unsigned long long)c);
+                    if (hb + c <= hkeys_cap && hd < hdesc_cap) {
+                        const uint32_t* k = keys + (off[tid] - c);
+                        for (uint32_t i = 0; i < c; ++i) hkeys[hb + i] = k[i];
+                        hdesc[hd] = make_uint4(vi, (uint32_t)hb, c, job);
+                    } else {
+                        status |= VKHR_DEV_LIST_OVERFLOW;
+                    }
+                }
+            }
+        }
+    }
+    if (TANG) {
+        __syncthreads();
+        // voxels with kBrickThread < count <= kBrickSmall: a warp sorts the keys
+        // (two per lane), gathers the tangents in parallel and lane 0 adds them in order
+        const unsigned lane = lane_id(), warp = (unsigned)tid >> 5;
+        float* wt = wtan + warp * 3 * 64;
+        for (uint32_t m = warp; m < wcount; m += kBrickWarps) {
+            const uint32_t l = wlist[m], c = cnt[l];
+            const uint32_t* k = keys + (off[l] - c);
+            uint32_t ka = lane < c ? k[lane] : 0xffffffffu, kb = lane + 32 < c ? k[lane + 32] : 0xffffffffu;
+            warp_sort64(ka, kb);
+            if (lane < c) {
+                const float4 t = visit_tangent<SEG>(pair_tan, tan, ka);
+                wt[lane] = t.x;
+                wt[64 + lane] = t.y;
+                wt[128 + lane] = t.z;
+            }
+            if (lane + 32 < c) {
+                const float4 t = visit_tangent<SEG>(pair_tan, tan, kb);
+                wt[lane + 32] = t.x;
+                wt[64 + lane + 32] = t.y;
+                wt[128 + lane + 32] = t.z;
+            }
+            __syncwarp();
+            if (lane == 0) {
+                float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+                for (uint32_t i = 0; i < c; ++i) {
+                    sx = __fadd_rn(sx, wt[i]);
+                    sy = __fadd_rn(sy, wt[64 + i]);
+                    sz = __fadd_rn(sz, wt[128 + i]);
+                }
+                const uint32_t lx = bx * 8 + (l & 7), ly = by * 8 + ((l >> 3) & 7), lz = bz * 8 + (l >> 6);
+                tq[lx + g.w * (ly + g.h * lz)] = pack_tangent(sx, sy, sz, c);
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// One CTA per visited brick (a device queue over a list of bricks): counts
+// per local voxel from the brick's visit entries, then, with tangents, a
+// counting sort of the keys by voxel and the per-voxel resolve.  BIG = false
+// takes the bricks of up to kBrickCap visits (keys sorted in shared memory,
+// list from the front); BIG = true the others (keys sorted into a slice of
+// the global key scratch, list from the back).
+template <bool SEG, bool TANG, bool BIG>
 __global__ void __launch_bounds__(kBrickThreads, 2)
 brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__ pair_tan_all,
              const uint32_t* __restrict__ visits, const uint32_t* __restrict__ cursor, const uint32_t* __restrict__ list,
-             const uint2* __restrict__ entries, size_t entries_cap, uint4* hdesc, size_t hdesc_cap, uint32_t* hkeys,
-             size_t hkeys_cap, unsigned long long* words)
+             uint32_t list_n, const uint2* __restrict__ entries, size_t entries_cap, uint4* hdesc, size_t hdesc_cap,
+             uint32_t* hkeys, size_t hkeys_cap, unsigned long long* words)
 {
     extern __shared__ uint32_t sm[];
     uint32_t* cnt = sm;                       // visits per local voxel
@@ -481,20 +607,20 @@ brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__
     uint32_t* warp_sums = sm + 2 * kBrickThreads;
     uint32_t* wlist = sm + 2 * kBrickThreads + 32;             // voxels for the warp resolve
     float* wtan = reinterpret_cast<float*>(wlist + kBrickThreads); // per warp: 64 x 3 tangents
-    uint32_t* keys = wlist + kBrickThreads + kBrickWarps * 3 * 64;
-    __shared__ uint32_t next, wcount, s_job;
+    uint32_t* keys = wlist + kBrickThreads + kBrickWarps * 3 * 64; // (BIG = false only)
+    __shared__ uint32_t next, wcount, s_job, s_hb;
     __shared__ uint32_t s_brick_base[kMaxJobs];
     load_bases(jobs, nj, nullptr, s_brick_base);
     const int tid = threadIdx.x;
     unsigned status = 0;
-    const uint32_t listed = (uint32_t)words[WORD_BRICK_LIST];
+    const uint32_t listed = (uint32_t)words[BIG ? WORD_BIG_LIST : WORD_BRICK_LIST];
     for (;;) {
-        if (tid == 0) next = (uint32_t)atomicAdd(words + WORD_BRICK_QUEUE, 1ull);
+        if (tid == 0) next = (uint32_t)atomicAdd(words + (BIG ? WORD_BIG_QUEUE : WORD_BRICK_QUEUE), 1ull);
         __syncthreads();
         const uint32_t q = next;
         __syncthreads();
         if (q >= listed) break;
-        const uint32_t gb = list[q];             // visited, and within kBrickCap
+        const uint32_t gb = BIG ? list[list_n - 1 - q] : list[q];
         const uint32_t nv = visits[gb], start = cursor[gb] - nv;
         if ((uint64_t)start + nv > entries_cap) { // visit budget exceeded: the fill pass flagged it
             status |= VKHR_DEV_LIST_OVERFLOW;
@@ -504,16 +630,18 @@ brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__
         if (tid == 0) {
             wcount = 0;
             s_job = (uint32_t)find_job(s_brick_base, nj, gb);
+            s_hb = (TANG && BIG) ? (uint32_t)atomicAdd(words + WORD_HKEYS_CURSOR, (unsigned long long)nv) : 0u;
         }
         __syncthreads();
+        if (TANG && BIG && (uint64_t)s_hb + nv > hkeys_cap) { // key scratch exhausted
+            status |= VKHR_DEV_LIST_OVERFLOW;
+            continue;
+        }
         const VoxJob& J = jobs[s_job];
         const Grid& g = J.g;
         const uint32_t b = gb - J.brick_base;   // brick within the style's grid
         const float4* pair_tan = pair_tan_all + J.item_base;
-        const float* tan = J.tan;
-        uint32_t* counts = J.counts;
-        uint8_t* dens = J.dens;
-        uint32_t* tq = J.tq;
+        uint32_t* kbase = BIG ? hkeys + s_hb : keys;
         for (uint32_t i = tid; i < nv; i += kBrickThreads) atomicAdd(cnt + (__ldg(&entries[start + i].y) & 511u), 1u);
         __syncthreads();
         if (TANG) {
@@ -521,100 +649,12 @@ brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__
             __syncthreads();
             for (uint32_t i = tid; i < nv; i += kBrickThreads) {
                 const uint2 e = __ldg(entries + start + i);
-                const uint32_t slot = atomicAdd(off + (e.y & 511u), 1u);
-                if (slot < (uint32_t)kBrickCap) keys[slot] = e.x;
+                kbase[atomicAdd(off + (e.y & 511u), 1u)] = e.x;
             }
-            __syncthreads();
+            __syncthreads(); // also orders the scratch writes before the block's reads
         }
-        const uint32_t bx = b % g.nbx, by = (b / g.nbx) % g.nby, bz = b / (g.nbx * g.nby);
-        const uint32_t x = bx * 8 + (tid & 7), y = by * 8 + ((tid >> 3) & 7), z = bz * 8 + (tid >> 6);
-        if (x < g.w && y < g.h && z < g.d) {
-            const uint32_t c = cnt[tid];
-            const uint32_t vi = x + g.w * (y + g.h * z);
-            counts[vi] = c;
-            if (dens) dens[vi] = (uint8_t)(c < 255u ? c : 255u);
-            if (TANG) {
-                if (c == 0) {
-                    tq[vi] = 0u;
-                } else if (c > (uint32_t)kBrickThread && c <= (uint32_t)kBrickSmall) {
-                    wlist[atomicAdd(&wcount, 1u)] = (uint32_t)tid; // resolved by a warp below
-                } else if (c <= (uint32_t)kBrickThread) {
-                    uint32_t* k = keys + (off[tid] - c);
-                    for (uint32_t i = 1; i < c; ++i) { // insertion sort: serial order
-                        const uint32_t key = k[i];
-                        uint32_t j = i;
-                        while (j > 0 && k[j - 1] > key) {
-                            k[j] = k[j - 1];
-                            --j;
-                        }
-                        k[j] = key;
-                    }
-                    // gather 8 tangents at a time (independent loads), then add them in key order
-                    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-                    for (uint32_t i0 = 0; i0 < c; i0 += 8) {
-                        float4 tv[8];
-#pragma unroll
-                        for (int j = 0; j < 8; ++j)
-                            if (i0 + j < c) tv[j] = visit_tangent<SEG>(pair_tan, tan, k[i0 + j]);
-#pragma unroll
-                        for (int j = 0; j < 8; ++j)
-                            if (i0 + j < c) {
-                                sx = __fadd_rn(sx, tv[j].x);
-                                sy = __fadd_rn(sy, tv[j].y);
-                                sz = __fadd_rn(sz, tv[j].z);
-                            }
-                    }
-                    tq[vi] = pack_tangent(sx, sy, sz, c);
-                } else { // crowded: hand the keys to a CTA of its own
-                    const unsigned long long hb = atomicAdd(words + WORD_HKEYS_CURSOR, (unsigned long long)c);
-                    const unsigned long long hd = atomicAdd(words + WORD_BHEAVY_COUNT, 1ull);
-                    if (hb + c <= hkeys_cap && hd < hdesc_cap) {
-                        const uint32_t* k = keys + (off[tid] - c);
-                        for (uint32_t i = 0; i < c; ++i) hkeys[hb + i] = k[i];
-                        hdesc[hd] = make_uint4(vi, (uint32_t)hb, c, s_job);
-                    } else {
-                        status |= VKHR_DEV_LIST_OVERFLOW;
-                    }
-                }
-            }
-        }
-        if (TANG) {
-            __syncthreads();
-            // voxels with kBrickThread < count <= kBrickSmall: a warp sorts the keys
-            // (two per lane), gathers the tangents in parallel and lane 0 adds them in order
-            const unsigned lane = lane_id(), warp = (unsigned)tid >> 5;
-            float* wt = wtan + warp * 3 * 64;
-            for (uint32_t m = warp; m < wcount; m += kBrickWarps) {
-                const uint32_t l = wlist[m], c = cnt[l];
-                const uint32_t* k = keys + (off[l] - c);
-                uint32_t ka = lane < c ? k[lane] : 0xffffffffu, kb = lane + 32 < c ? k[lane + 32] : 0xffffffffu;
-                warp_sort64(ka, kb);
-                if (lane < c) {
-                    const float4 t = visit_tangent<SEG>(pair_tan, tan, ka);
-                    wt[lane] = t.x;
-                    wt[64 + lane] = t.y;
-                    wt[128 + lane] = t.z;
-                }
-                if (lane + 32 < c) {
-                    const float4 t = visit_tangent<SEG>(pair_tan, tan, kb);
-                    wt[lane + 32] = t.x;
-                    wt[64 + lane + 32] = t.y;
-                    wt[128 + lane + 32] = t.z;
-                }
-                __syncwarp();
-                if (lane == 0) {
-                    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-                    for (uint32_t i = 0; i < c; ++i) {
-                        sx = __fadd_rn(sx, wt[i]);
-                        sy = __fadd_rn(sy, wt[64 + i]);
-                        sz = __fadd_rn(sz, wt[128 + i]);
-                    }
-                    const uint32_t lx = bx * 8 + (l & 7), ly = by * 8 + ((l >> 3) & 7), lz = bz * 8 + (l >> 6);
-                    tq[lx + g.w * (ly + g.h * lz)] = pack_tangent(sx, sy, sz, c);
-                }
-                __syncwarp();
-            }
-        }
+        resolve_brick<SEG, TANG>(J, g, b, pair_tan, cnt, off, kbase, BIG, s_hb, wlist, wcount, wtan, hdesc, hdesc_cap,
+                                 hkeys, hkeys_cap, s_job, words, status);
         __syncthreads();
     }
     if (status) atomicOr(words + WORD_STATUS, (unsigned long long)status);
@@ -636,24 +676,83 @@ __device__ void block_bitonic_sort(uint32_t* s, int n)
         }
 }
 
+// Ascending sort of the first `have` keys of s (padded with 0xffffffff to
+// the next power of two, at most kHeavyTile).  Block-wide.
+__device__ __forceinline__ void sort_prefix(uint32_t* s, uint32_t have)
+{
+    int n = 2;
+    while (n < (int)have) n <<= 1;
+    for (int i = (int)have + threadIdx.x; i < n; i += blockDim.x) s[i] = 0xffffffffu;
+    __syncthreads();
+    block_bitonic_sort(s, n);
+}
+
 // Tangent of a crowded voxel from its c keys at src: the smallest min(c, 255)
-// keys in ascending (serial) order by repeated tile sorts that carry the
-// kKeep smallest forward, then a sequential FP32 sum.  Block-wide.
+// keys in ascending (serial) order, then a sequential FP32 sum.  The keys
+// stream through in chunks of kCrowdThreads * kCrowdPer; only keys below
+// the current 255th-smallest key (thr) are kept, and the buffer is sorted
+// and cut back to 255 keys when a chunk would overflow it.  A key equal to
+// thr can be dropped: the multiset of the 255 smallest values is unchanged
+// (equal keys carry equal tangents).  Block-wide, kCrowdThreads threads.
+constexpr int kCrowdThreads = 256;
+constexpr int kCrowdPer = 4;
+static_assert(kKeep - 1 + kCrowdThreads * kCrowdPer <= kHeavyTile, "a chunk must fit after a cut");
+
 __device__ void resolve_crowded(const uint32_t* src, uint32_t c, const float* __restrict__ tan,
                                 const uint2* __restrict__ pairs, uint32_t* keys, float (*tv)[kKeep], uint32_t* out)
 {
+    __shared__ uint32_t warp_tot[kCrowdThreads / 32];
+    __shared__ uint32_t s_thr;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t m = c < 255u ? c : 255u;
-    uint32_t done = 0;
-    int first = 0;
-    while (done < c) {
-        const uint32_t take = min((uint32_t)(kHeavyTile - first), c - done);
-        for (int i = threadIdx.x; i < kHeavyTile - first; i += blockDim.x)
-            keys[first + i] = (uint32_t)i < take ? src[done + i] : 0xffffffffu;
-        __syncthreads();
-        block_bitonic_sort(keys, kHeavyTile);
-        done += take;
-        first = kKeep;
+    uint32_t have = 0, thr = 0xffffffffu;
+    for (uint32_t base = 0; base < c; base += kCrowdThreads * kCrowdPer) {
+        uint32_t k[kCrowdPer];
+#pragma unroll
+        for (int j = 0; j < kCrowdPer; ++j) {
+            const uint32_t i = base + j * kCrowdThreads + threadIdx.x;
+            k[j] = i < c ? __ldg(src + i) : 0xffffffffu;
+        }
+        for (int pass = 0; pass < 2; ++pass) {
+            uint32_t a = 0;
+#pragma unroll
+            for (int j = 0; j < kCrowdPer; ++j) a += k[j] < thr ? 1u : 0u;
+            if (!__syncthreads_or(a != 0)) break; // nothing below the threshold
+            // block exclusive scan of the accepted counts
+            uint32_t incl = a;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            if (lane == 31) warp_tot[warp] = incl;
+            __syncthreads();
+            uint32_t before = 0, total = 0;
+#pragma unroll
+            for (int w = 0; w < kCrowdThreads / 32; ++w) {
+                const uint32_t t = warp_tot[w];
+                before += w < warp ? t : 0u;
+                total += t;
+            }
+            __syncthreads(); // warp_tot is rewritten by the next scan
+            if (have + total > (uint32_t)kHeavyTile) { // cut back to the 255 smallest, raise the threshold
+                sort_prefix(keys, have);
+                have = 255u;
+                if (threadIdx.x == 0) s_thr = keys[254];
+                __syncthreads();
+                thr = s_thr;
+                continue; // filter the chunk again (it fits now)
+            }
+            uint32_t at = have + before + incl - a;
+#pragma unroll
+            for (int j = 0; j < kCrowdPer; ++j)
+                if (k[j] < thr) keys[at++] = k[j];
+            have += total;
+            __syncthreads();
+            break;
+        }
     }
+    sort_prefix(keys, have);
     for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
         const float* t = tan + 3 * (size_t)key_vertex(keys[i], pairs);
         tv[0][i] = t[0];
@@ -675,7 +774,7 @@ __device__ void resolve_crowded(const uint32_t* src, uint32_t c, const float* __
 
 // One CTA per crowded voxel of the brick path (descriptors: voxel, key
 // offset, count, style).
-__global__ void __launch_bounds__(256) crowded_kernel(const VoxJob* __restrict__ jobs, const uint4* __restrict__ hdesc,
+__global__ void __launch_bounds__(kCrowdThreads) crowded_kernel(const VoxJob* __restrict__ jobs, const uint4* __restrict__ hdesc,
                                                       size_t hdesc_cap, const uint32_t* __restrict__ hkeys,
                                                       const unsigned long long* words)
 {
@@ -687,196 +786,6 @@ __global__ void __launch_bounds__(256) crowded_kernel(const VoxJob* __restrict__
         const uint4 d = hdesc[h];
         const VoxJob& J = jobs[d.w];
         resolve_crowded(hkeys + d.y, d.z, J.tan, J.pairs, keys, tv, J.tq + d.x);
-    }
-}
-
-// ---- global path (bricks with more than kBrickCap visits) ---------------------------
-// Runs only when words[WORD_MAX_BRICK_VISITS] > kBrickCap; visits of other
-// bricks are ignored.
-
-__device__ __forceinline__ bool crowded_brick(const uint32_t* __restrict__ visits, uint32_t b)
-{
-    return __ldg(visits + b) > (uint32_t)kBrickCap;
-}
-
-__device__ __forceinline__ bool global_path_needed(const unsigned long long* words)
-{
-    return words[WORD_MAX_BRICK_VISITS] > (unsigned long long)kBrickCap;
-}
-
-__global__ void global_clear_kernel(uint32_t* counts, uint32_t n, const unsigned long long* words)
-{
-    if (!global_path_needed(words)) return;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-        counts[i] = 0u;
-}
-
-template <bool FILL, bool SEG>
-__global__ void global_visit_kernel(Grid g, const float* __restrict__ v, const uint2* __restrict__ pairs,
-                                    uint32_t n_in, const uint32_t* __restrict__ visits, uint32_t* counts,
-                                    uint32_t* gcursor, uint32_t* list, size_t list_cap, unsigned long long* words)
-{
-    if (!global_path_needed(words)) return;
-    unsigned status = 0;
-    auto visit = [&](const Visit& o, uint32_t key) {
-        if (!crowded_brick(visits, o.brick)) return;
-        if (!FILL) {
-            atomicAdd(counts + o.lin, 1u);
-        } else {
-            const uint32_t slot = atomicAdd(gcursor + o.lin, 1u);
-            if (slot < list_cap) list[slot] = key;
-            else status |= VKHR_DEV_LIST_OVERFLOW;
-        }
-    };
-    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n_in; p += (uint64_t)gridDim.x * blockDim.x) {
-        if (SEG) {
-            Seg s;
-            unsigned ignore = 0;
-            if (!seg_setup(g, v, __ldg(pairs + p), s, ignore)) continue;
-            for (uint32_t k = 0; k < s.n; ++k) {
-                Visit o;
-                if (seg_visit(g, s, o)) visit(o, (uint32_t)p);
-                seg_advance(s);
-            }
-        } else {
-            Visit o;
-            if (vertex_visit(g, v, (uint32_t)p, o)) visit(o, (uint32_t)p);
-        }
-    }
-    if (status) atomicOr(words + WORD_STATUS, (unsigned long long)status);
-}
-
-// Slices [gcursor, gcursor + count) of the global visit list per voxel.
-__global__ void __launch_bounds__(kRangeThreads) global_ranges_kernel(const uint32_t* __restrict__ counts, uint32_t n,
-                                                                    uint32_t* gcursor, unsigned long long* words)
-{
-    if (!global_path_needed(words)) return;
-    __shared__ uint32_t warp_sums[kRangeThreads / 32];
-    __shared__ uint32_t block_base;
-    const uint32_t tile = kRangeThreads * kRangeItems;
-    for (uint64_t base = (uint64_t)blockIdx.x * tile; base < n; base += (uint64_t)gridDim.x * tile) {
-        uint32_t c[kRangeItems];
-        uint32_t sum = 0;
-#pragma unroll
-        for (int j = 0; j < kRangeItems; ++j) {
-            const uint64_t i = base + (uint64_t)j * kRangeThreads + threadIdx.x;
-            c[j] = i < n ? __ldg(counts + i) : 0u;
-            sum += c[j];
-        }
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-        uint32_t incl = sum;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
-        }
-        if (lane == 31) warp_sums[warp] = incl;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            uint32_t run = 0;
-            for (int w = 0; w < kRangeThreads / 32; ++w) {
-                const uint32_t t = warp_sums[w];
-                warp_sums[w] = run;
-                run += t;
-            }
-            block_base = run ? (uint32_t)atomicAdd(words + WORD_LIST_CURSOR, (unsigned long long)run) : 0u;
-        }
-        __syncthreads();
-        uint32_t start = block_base + warp_sums[warp] + (incl - sum);
-#pragma unroll
-        for (int j = 0; j < kRangeItems; ++j) {
-            const uint64_t i = base + (uint64_t)j * kRangeThreads + threadIdx.x;
-            if (i < n) gcursor[i] = start;
-            start += c[j];
-        }
-        __syncthreads();
-    }
-}
-
-template <int N, int CAP>
-__device__ __forceinline__ void sort_network(uint32_t (&x)[CAP])
-{
-#pragma unroll
-    for (int k = 2; k <= N; k <<= 1)
-#pragma unroll
-        for (int j = k >> 1; j > 0; j >>= 1)
-#pragma unroll
-            for (int i = 0; i < N; ++i) {
-                const int l = i ^ j;
-                if (l > i) {
-                    const bool up = (i & k) == 0;
-                    const uint32_t a = x[i], b = x[l];
-                    if ((a > b) == up) { x[i] = b; x[l] = a; }
-                }
-            }
-}
-
-template <int N>
-__device__ __forceinline__ uint32_t resolve_registers(uint32_t c, const uint32_t* __restrict__ list, uint32_t start,
-                                                      const float* __restrict__ tan, const uint2* __restrict__ pairs)
-{
-    uint32_t k[N];
-#pragma unroll
-    for (int i = 0; i < N; ++i) k[i] = (uint32_t)i < c ? __ldg(list + start + i) : 0xffffffffu;
-    sort_network<N, N>(k);
-    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-#pragma unroll
-    for (int i = 0; i < N; ++i)
-        if ((uint32_t)i < c) {
-            const float* t = tan + 3 * (size_t)key_vertex(k[i], pairs);
-            sx = __fadd_rn(sx, __ldg(t + 0));
-            sy = __fadd_rn(sy, __ldg(t + 1));
-            sz = __fadd_rn(sz, __ldg(t + 2));
-        }
-    return pack_tangent(sx, sy, sz, c);
-}
-
-// Resolves the global path's voxels (crowded bricks only; other voxels are
-// written by the brick kernel afterwards).  Voxels with more than
-// kMediumSort visits go to crowded descriptors over the global list.
-__global__ void global_resolve_kernel(Grid g, const uint32_t* __restrict__ visits, const uint32_t* __restrict__ counts,
-                                      const uint32_t* __restrict__ gcursor, const uint32_t* __restrict__ list,
-                                      size_t list_cap, const float* __restrict__ tan, const uint2* __restrict__ pairs,
-                                      uint8_t* dens, uint32_t* tq, uint4* gdesc, size_t gdesc_cap, uint32_t job,
-                                      unsigned long long* words)
-{
-    if (!global_path_needed(words)) return;
-    for (uint64_t vi = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; vi < g.n; vi += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t z = (uint32_t)(vi / g.wh), r = (uint32_t)(vi - (uint64_t)z * g.wh), y = r / g.w, x = r - y * g.w;
-        if (!crowded_brick(visits, (x >> 3) + g.nbx * ((y >> 3) + g.nby * (z >> 3)))) continue;
-        const uint32_t c = counts[vi];
-        if (dens) dens[vi] = (uint8_t)(c < 255u ? c : 255u);
-        if (!tq) continue;
-        if (c == 0) { tq[vi] = 0u; continue; }
-        const uint32_t start = gcursor[vi] - c;
-        if ((uint64_t)start + c > list_cap) { // visit budget exceeded: the fill pass flagged it
-            atomicOr(words + WORD_STATUS, (unsigned long long)VKHR_DEV_LIST_OVERFLOW);
-            continue;
-        }
-        if (c <= kSmallSort) tq[vi] = resolve_registers<kSmallSort>(c, list, start, tan, pairs);
-        else if (c <= kMediumSort) tq[vi] = resolve_registers<kMediumSort>(c, list, start, tan, pairs);
-        else {
-            const unsigned long long hd = atomicAdd(words + WORD_HEAVY_COUNT, 1ull);
-            if (hd < gdesc_cap) gdesc[hd] = make_uint4((uint32_t)vi, start, c, job);
-            else atomicOr(words + WORD_STATUS, (unsigned long long)VKHR_DEV_LIST_OVERFLOW);
-        }
-    }
-}
-
-__global__ void __launch_bounds__(256) global_crowded_kernel(const VoxJob* __restrict__ jobs,
-                                                             const uint4* __restrict__ gdesc, size_t gdesc_cap,
-                                                             const uint32_t* __restrict__ list,
-                                                             const unsigned long long* words)
-{
-    if (!global_path_needed(words)) return;
-    __shared__ uint32_t keys[kHeavyTile];
-    __shared__ float tv[3][kKeep];
-    unsigned long long nh = words[WORD_HEAVY_COUNT];
-    if (nh > gdesc_cap) nh = gdesc_cap;
-    for (unsigned long long h = blockIdx.x; h < nh; h += gridDim.x) {
-        const uint4 d = gdesc[h];
-        const VoxJob& J = jobs[d.w];
-        resolve_crowded(list + d.y, d.z, J.tan, J.pairs, keys, tv, J.tq + d.x);
     }
 }
 
@@ -1002,14 +911,20 @@ vkhr_status check_device_status(vkhr_ctx* ctx, unsigned long long s)
 }
 
 template <bool SEG, bool TANG>
-vkhr_status launch_brick(vkhr_ctx* ctx, const VoxJob* d_jobs, int nj, cudaStream_t st, unsigned blocks, size_t smem,
-                         size_t cap_visits)
+vkhr_status launch_brick(vkhr_ctx* ctx, const VoxJob* d_jobs, int nj, uint32_t total_bricks, cudaStream_t st,
+                         unsigned blocks, size_t cap_visits)
 {
-    VKHR_CUDA_TRY(ctx, cudaFuncSetAttribute(brick_kernel<SEG, TANG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    // bricks above kBrickCap first (their keys go to the global scratch), then the rest
+    const size_t small = (size_t)(2 * kBrickThreads + 32 + kBrickThreads + kBrickWarps * 3 * 64) * sizeof(uint32_t);
+    const size_t smem = small + (TANG ? (size_t)kBrickCap * sizeof(uint32_t) : 0);
+    VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG, true>), (unsigned)ctx->sm_count * 2, kBrickThreads, small, st, d_jobs, nj,
+                ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->brick_list, total_bricks, ctx->items,
+                cap_visits, ctx->hdesc, ctx->hdesc_cap, ctx->hkeys, cap_visits, ctx->d_words);
+    VKHR_CUDA_TRY(ctx, cudaFuncSetAttribute(brick_kernel<SEG, TANG, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)smem));
-    VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG>), blocks, kBrickThreads, smem, st, d_jobs, nj, ctx->pair_tan,
-                ctx->brick_visits, ctx->brick_cursor, ctx->brick_list, ctx->items, cap_visits, ctx->hdesc,
-                ctx->hdesc_cap, ctx->hkeys, cap_visits, ctx->d_words);
+    VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG, false>), blocks, kBrickThreads, smem, st, d_jobs, nj, ctx->pair_tan,
+                ctx->brick_visits, ctx->brick_cursor, ctx->brick_list, total_bricks, ctx->items, cap_visits,
+                ctx->hdesc, ctx->hdesc_cap, ctx->hkeys, cap_visits, ctx->d_words);
     return VKHR_OK;
 }
 
@@ -1046,7 +961,7 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
     if (!ctx) return VKHR_ERR_INVALID_ARG;
     if (nj <= 0 || nj > kMaxJobs || !jobs_in) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "job count must be in [1, 256]");
     VoxJob jobs[kMaxJobs];
-    uint64_t items = 0, bricks = 0, max_voxels = 0;
+    uint64_t items = 0, bricks = 0;
     const bool tang = jobs_in[0].d_tangents != nullptr;
     for (int j = 0; j < nj; ++j) {
         vkhr_status s = make_job(ctx, segments, jobs_in[j], jobs[j]);
@@ -1057,7 +972,6 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
         jobs[j].brick_base = (uint32_t)bricks;
         items += jobs[j].n_in;
         bricks += jobs[j].g.nb;
-        max_voxels = std::max<uint64_t>(max_voxels, jobs[j].g.n);
         if (items >= (1ull << 32) || bricks >= (1ull << 32))
             return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "batch too large (2^32 items or bricks)");
     }
@@ -1106,13 +1020,14 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
     VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->brick_visits, 0, (size_t)total_bricks * sizeof(uint32_t), st));
     const unsigned threads = 256;
     const unsigned in_blocks = std::min(vkhr_blocks(total_items, threads), (unsigned)ctx->sm_count * 16);
+    const size_t bin_smem_bytes = (size_t)nj * (sizeof(VoxJob) + sizeof(uint32_t));
     if (total_items) {
         if (segments)
-            VKHR_LAUNCH(ctx, (bin_kernel<false, true>), in_blocks, threads, 0, st, d_jobs, nj, total_items,
+            VKHR_LAUNCH(ctx, (bin_kernel<false, true>), in_blocks, threads, bin_smem_bytes, st, d_jobs, nj, total_items,
                         ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap,
                         ctx->d_words);
         else
-            VKHR_LAUNCH(ctx, (bin_kernel<false, false>), in_blocks, threads, 0, st, d_jobs, nj, total_items,
+            VKHR_LAUNCH(ctx, (bin_kernel<false, false>), in_blocks, threads, bin_smem_bytes, st, d_jobs, nj, total_items,
                         ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap,
                         ctx->d_words);
     }
@@ -1123,7 +1038,6 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
                 total_bricks, ctx->brick_visits);
     VKHR_CUDA_TRY(ctx, cudaGetLastError());
 
-    bool global_path = true; // when the totals stay on the device, the global path exits there if unneeded
     if (!bounded) {          // segment mode without a budget: read the visit total back
         if (capturing)
             return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG,
@@ -1134,7 +1048,6 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
         s = check_device_status(ctx, ctx->h_words[WORD_STATUS]);
         if (s != VKHR_OK) return s;
         visits_total = ctx->h_words[WORD_TOTAL_VISITS];
-        global_path = ctx->h_words[WORD_MAX_BRICK_VISITS] > (unsigned long long)kBrickCap;
         if (visits_total >= (1ull << 32))
             return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "more than 2^32 - 1 voxel visits in one call");
         s = vkhr_reserve(ctx, (void**)&ctx->items, &ctx->items_cap, visits_total ? visits_total : 1, sizeof(uint2));
@@ -1149,69 +1062,26 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
                          sizeof(uint4));
         if (s != VKHR_OK) return s;
     }
-    if (global_path && total_items) {
-        s = vkhr_reserve(ctx, (void**)&ctx->cursor, &ctx->cursor_cap, max_voxels, sizeof(uint32_t));
-        if (s != VKHR_OK) return s;
-        s = vkhr_reserve(ctx, (void**)&ctx->list, &ctx->list_cap, visits_total ? visits_total : 1, sizeof(uint32_t));
-        if (s != VKHR_OK) return s;
-        s = vkhr_reserve(ctx, (void**)&ctx->gdesc, &ctx->gdesc_cap, visits_total / (kMediumSort + 1) + 1,
-                         sizeof(uint4));
-        if (s != VKHR_OK) return s;
-        for (int j = 0; j < nj; ++j) { // each style's crowded bricks, one after the other
-            const VoxJob& J = jobs[j];
-            if (!J.n_in) continue;
-            const Grid& g = J.g;
-            const uint32_t* jv = ctx->brick_visits + J.brick_base;
-            const unsigned vblocks = std::min(vkhr_blocks(g.n, threads), (unsigned)ctx->sm_count * 32);
-            const unsigned jb = std::min(vkhr_blocks(J.n_in, threads), (unsigned)ctx->sm_count * 16);
-            VKHR_LAUNCH(ctx, global_clear_kernel, vblocks, threads, 0, st, J.counts, g.n, ctx->d_words);
-            if (segments)
-                VKHR_LAUNCH(ctx, (global_visit_kernel<false, true>), jb, threads, 0, st, g, J.v, J.pairs, J.n_in, jv,
-                            J.counts, ctx->cursor, ctx->list, cap_visits, ctx->d_words);
-            else
-                VKHR_LAUNCH(ctx, (global_visit_kernel<false, false>), jb, threads, 0, st, g, J.v, J.pairs, J.n_in, jv,
-                            J.counts, ctx->cursor, ctx->list, cap_visits, ctx->d_words);
-            const unsigned gr = std::min(vkhr_blocks(g.n, kRangeThreads * kRangeItems), (unsigned)ctx->sm_count * 8);
-            VKHR_LAUNCH(ctx, global_ranges_kernel, gr, kRangeThreads, 0, st, J.counts, g.n, ctx->cursor, ctx->d_words);
-            if (tang) {
-                if (segments)
-                    VKHR_LAUNCH(ctx, (global_visit_kernel<true, true>), jb, threads, 0, st, g, J.v, J.pairs, J.n_in, jv,
-                                J.counts, ctx->cursor, ctx->list, cap_visits, ctx->d_words);
-                else
-                    VKHR_LAUNCH(ctx, (global_visit_kernel<true, false>), jb, threads, 0, st, g, J.v, J.pairs, J.n_in,
-                                jv, J.counts, ctx->cursor, ctx->list, cap_visits, ctx->d_words);
-            }
-            VKHR_LAUNCH(ctx, global_resolve_kernel, vblocks, threads, 0, st, g, jv, J.counts, ctx->cursor, ctx->list,
-                        cap_visits, J.tan, J.pairs, J.dens, J.tq, ctx->gdesc, ctx->gdesc_cap, (uint32_t)j,
-                        ctx->d_words);
-        }
-        if (tang)
-            VKHR_LAUNCH(ctx, global_crowded_kernel, (unsigned)ctx->sm_count * 2, 256, 0, st, d_jobs, ctx->gdesc,
-                        ctx->gdesc_cap, ctx->list, ctx->d_words);
-        VKHR_CUDA_TRY(ctx, cudaGetLastError());
-    }
     if (total_items) {
         if (segments)
-            VKHR_LAUNCH(ctx, (bin_kernel<true, true>), in_blocks, threads, 0, st, d_jobs, nj, total_items,
+            VKHR_LAUNCH(ctx, (bin_kernel<true, true>), in_blocks, threads, bin_smem_bytes, st, d_jobs, nj, total_items,
                         ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->items, cap_visits,
                         ctx->d_words);
         else
-            VKHR_LAUNCH(ctx, (bin_kernel<true, false>), in_blocks, threads, 0, st, d_jobs, nj, total_items,
+            VKHR_LAUNCH(ctx, (bin_kernel<true, false>), in_blocks, threads, bin_smem_bytes, st, d_jobs, nj, total_items,
                         ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->items, cap_visits,
                         ctx->d_words);
     }
-    const size_t smem = (size_t)(2 * kBrickThreads + 32 + kBrickThreads + kBrickWarps * 3 * 64 + (tang ? kBrickCap : 0)) *
-                        sizeof(uint32_t);
     const unsigned bblocks = std::min(total_bricks, (unsigned)ctx->sm_count * 2);
     if (segments)
-        s = tang ? launch_brick<true, true>(ctx, d_jobs, nj, st, bblocks, smem, cap_visits)
-                 : launch_brick<true, false>(ctx, d_jobs, nj, st, bblocks, smem, cap_visits);
+        s = tang ? launch_brick<true, true>(ctx, d_jobs, nj, total_bricks, st, bblocks, cap_visits)
+                 : launch_brick<true, false>(ctx, d_jobs, nj, total_bricks, st, bblocks, cap_visits);
     else
-        s = tang ? launch_brick<false, true>(ctx, d_jobs, nj, st, bblocks, smem, cap_visits)
-                 : launch_brick<false, false>(ctx, d_jobs, nj, st, bblocks, smem, cap_visits);
+        s = tang ? launch_brick<false, true>(ctx, d_jobs, nj, total_bricks, st, bblocks, cap_visits)
+                 : launch_brick<false, false>(ctx, d_jobs, nj, total_bricks, st, bblocks, cap_visits);
     if (s != VKHR_OK) return s;
     if (tang)
-        VKHR_LAUNCH(ctx, crowded_kernel, (unsigned)ctx->sm_count * 2, 256, 0, st, d_jobs, ctx->hdesc, ctx->hdesc_cap,
+        VKHR_LAUNCH(ctx, crowded_kernel, (unsigned)ctx->sm_count * 6, kCrowdThreads, 0, st, d_jobs, ctx->hdesc, ctx->hdesc_cap,
                     ctx->hkeys, ctx->d_words);
     VKHR_CUDA_TRY(ctx, cudaGetLastError());
     return VKHR_OK;
