@@ -43,6 +43,7 @@ constexpr int kBrickCap = 22528;       // visits a brick resolves in shared memo
 constexpr int kBrickThread = 16;       // <= this many visits: sorted and summed by the voxel's thread
 constexpr int kBrickSmall = 64;        // <= this many visits: sorted by one warp (2 keys per lane)
 constexpr int kBrickWarps = kBrickThreads / 32;
+constexpr int kGather = 4;             // tangent loads in flight per voxel thread (64 registers at 2 CTAs / SM)
 constexpr int kHeavyTile = 2048;       // crowded voxels: shared-memory sort tile
 constexpr int kKeep = 256;             // crowded voxels: tangents summed (>= 255)
 constexpr int kRangeThreads = 256;
@@ -224,42 +225,71 @@ __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
 // ---- brick path -----------------------------------------------------------------
 
+// A visit entry of the brick path: the visit's serial key (pair or vertex
+// number within its style) and its local voxel in the brick.  PACK = true
+// packs both into 32 bits (key < 2^23), otherwise a uint2.
+template <bool PACK>
+struct Entry;
+template <>
+struct Entry<true> {
+    typedef uint32_t T;
+    static __device__ __forceinline__ T make(uint32_t key, uint32_t local) { return (key << 9) | local; }
+    static __device__ __forceinline__ uint32_t key(T e) { return e >> 9; }
+    static __device__ __forceinline__ uint32_t local(T e) { return e & 511u; }
+};
+template <>
+struct Entry<false> {
+    typedef uint2 T;
+    static __device__ __forceinline__ T make(uint32_t key, uint32_t local) { return make_uint2(key, local); }
+    static __device__ __forceinline__ uint32_t key(T e) { return e.x; }
+    static __device__ __forceinline__ uint32_t local(T e) { return e.y & 511u; }
+};
+constexpr uint32_t kPackedKeyLimit = 1u << 23;
+
 // A run of `len` (<= 7) consecutive visits of one pair / vertex inside brick b,
 // their local voxels packed 9 bits each: counted per brick (FILL = false),
-// or written as (key, local voxel) entries into the
-// brick's slice of the visit list.
-template <bool FILL>
+// or written as (key, local voxel) entries into the brick's slice of the
+// visit list.
+template <bool FILL, bool PACK>
 __device__ __forceinline__ void emit_run(uint32_t b, uint32_t key, uint64_t locals, uint32_t len, uint32_t* visits,
-                                         uint32_t* cursor, uint2* entries, size_t entries_cap, unsigned& status)
+                                         uint32_t* cursor, typename Entry<PACK>::T* entries, size_t entries_cap,
+                                         unsigned& status)
 {
     if (!FILL) {
         atomicAdd(visits + b, len); // fire-and-forget reduction
     } else {
         const uint32_t base = atomicAdd(cursor + b, len);
         if ((uint64_t)base + len <= entries_cap) {
-            for (uint32_t j = 0; j < len; ++j) entries[base + j] = make_uint2(key, (uint32_t)(locals >> (9 * j)) & 511u);
+            for (uint32_t j = 0; j < len; ++j)
+                entries[base + j] = Entry<PACK>::make(key, (uint32_t)(locals >> (9 * j)) & 511u);
         } else {
             status |= VKHR_DEV_LIST_OVERFLOW;
         }
     }
 }
 
-template <bool FILL, bool SEG>
-__global__ void bin_kernel(const VoxJob* __restrict__ jobs, int nj, uint32_t total_items, float4* pair_rec,
-                           float4* pair_tan, uint32_t* visits, uint32_t* cursor, uint2* entries, size_t entries_cap,
-                           unsigned long long* words)
+// SINGLE = true: a one-style call; the style comes as the kernel parameter
+// job0 (constant bank, free to read in the visit loop).  Otherwise the job
+// table is copied into shared memory and each item looks its style up.
+template <bool FILL, bool SEG, bool PACK, bool SINGLE>
+__global__ void bin_kernel(const __grid_constant__ VoxJob job0, const VoxJob* __restrict__ jobs, int nj,
+                           uint32_t total_items, float4* pair_rec, float4* pair_tan, uint32_t* visits,
+                           uint32_t* cursor, void* entries_raw, size_t entries_cap, unsigned long long* words)
 {
+    typename Entry<PACK>::T* entries = reinterpret_cast<typename Entry<PACK>::T*>(entries_raw);
     // the job table in shared memory (nj * (sizeof(VoxJob) + 4) bytes of dynamic shared memory)
     extern __shared__ __align__(16) unsigned char bin_smem[];
     VoxJob* s_jobs = reinterpret_cast<VoxJob*>(bin_smem);
     uint32_t* s_item_base = reinterpret_cast<uint32_t*>(s_jobs + nj);
-    for (int i = threadIdx.x; i < nj * (int)(sizeof(VoxJob) / 4); i += blockDim.x)
-        reinterpret_cast<uint32_t*>(s_jobs)[i] = __ldg(reinterpret_cast<const uint32_t*>(jobs) + i);
-    load_bases(jobs, nj, s_item_base, nullptr);
+    if (!SINGLE) {
+        for (int i = threadIdx.x; i < nj * (int)(sizeof(VoxJob) / 4); i += blockDim.x)
+            reinterpret_cast<uint32_t*>(s_jobs)[i] = __ldg(reinterpret_cast<const uint32_t*>(jobs) + i);
+        load_bases(jobs, nj, s_item_base, nullptr);
+    }
     unsigned status = 0;
     for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < total_items;
          q += (uint64_t)gridDim.x * blockDim.x) {
-        const VoxJob& J = s_jobs[find_job(s_item_base, nj, (uint32_t)q)];
+        const VoxJob& J = SINGLE ? job0 : s_jobs[find_job(s_item_base, nj, (uint32_t)q)];
         const Grid& g = J.g;
         const uint32_t p = (uint32_t)q - J.item_base;
         if (SEG) {
@@ -284,18 +314,18 @@ __global__ void bin_kernel(const VoxJob* __restrict__ jobs, int nj, uint32_t tot
                     ++len;
                 } else {
                     if (len)
-                        emit_run<FILL>(J.brick_base + cur, p, locals, len, visits, cursor, entries, entries_cap, status);
+                        emit_run<FILL, PACK>(J.brick_base + cur, p, locals, len, visits, cursor, entries, entries_cap, status);
                     cur = ok ? o.brick : kNoBrick;
                     len = ok ? 1u : 0u;
                     locals = ok ? (uint64_t)o.local : 0ull;
                 }
                 seg_advance(s);
             }
-            if (len) emit_run<FILL>(J.brick_base + cur, p, locals, len, visits, cursor, entries, entries_cap, status);
+            if (len) emit_run<FILL, PACK>(J.brick_base + cur, p, locals, len, visits, cursor, entries, entries_cap, status);
         } else {
             Visit o;
             if (vertex_visit(g, J.v, p, o))
-                emit_run<FILL>(J.brick_base + o.brick, p, (uint64_t)o.local, 1u, visits, cursor, entries, entries_cap,
+                emit_run<FILL, PACK>(J.brick_base + o.brick, p, (uint64_t)o.local, 1u, visits, cursor, entries, entries_cap,
                                status);
         }
     }
@@ -478,112 +508,97 @@ __device__ __forceinline__ float4 visit_tangent(const float4* __restrict__ pair_
 
 // Per-voxel results of one brick whose visit keys are grouped by local voxel
 // at `keys` (shared memory, or the global scratch for bricks above
-// kBrickCap): counts and u8 densities, and the tangents by visit count --
-// up to kBrickThread visits by the voxel's thread, up to kBrickSmall by a
-// warp, more by crowded_kernel through a descriptor.  Block-wide.
+// kBrickCap): counts and u8 densities, and the tangents.  Each voxel's keys
+// are sorted in place -- up to kBrickThread by the voxel's own thread
+// (insertion sort), up to kBrickSmall by a warp (64-key register bitonic
+// sort) -- and then every voxel's thread adds its tangents in key order, all
+// voxels of the brick at once; more than kBrickSmall visits go to
+// crowded_kernel through a descriptor.  Block-wide.
 template <bool SEG, bool TANG>
 __device__ __forceinline__ void resolve_brick(const VoxJob& J, const Grid& g, uint32_t b, const float4* pair_tan,
                                               const uint32_t* cnt, const uint32_t* off, uint32_t* keys,
                                               bool keys_global, uint32_t keys_at, uint32_t* wlist, uint32_t& wcount,
-                                              float* wtan, uint4* hdesc, size_t hdesc_cap, uint32_t* hkeys,
-                                              size_t hkeys_cap, uint32_t job, unsigned long long* words,
-                                              unsigned& status)
+                                              uint4* hdesc, size_t hdesc_cap, uint32_t* hkeys, size_t hkeys_cap,
+                                              uint32_t job, unsigned long long* words, unsigned& status)
 {
     const int tid = threadIdx.x;
     const float* tan = J.tan;
     uint32_t* tq = J.tq;
     const uint32_t bx = b % g.nbx, by = (b / g.nbx) % g.nby, bz = b / (g.nbx * g.nby);
     const uint32_t x = bx * 8 + (tid & 7), y = by * 8 + ((tid >> 3) & 7), z = bz * 8 + (tid >> 6);
-    if (x < g.w && y < g.h && z < g.d) {
-        const uint32_t c = cnt[tid];
-        const uint32_t vi = x + g.w * (y + g.h * z);
+    const bool inside = x < g.w && y < g.h && z < g.d;
+    const uint32_t c = cnt[tid];
+    const uint32_t vi = x + g.w * (y + g.h * z);
+    uint32_t* k = keys + (off[tid] - c);
+    if (inside) {
         J.counts[vi] = c;
         if (J.dens) J.dens[vi] = (uint8_t)(c < 255u ? c : 255u);
-        if (TANG) {
-            if (c == 0) {
-                tq[vi] = 0u;
-            } else if (c > (uint32_t)kBrickThread && c <= (uint32_t)kBrickSmall) {
-                wlist[atomicAdd(&wcount, 1u)] = (uint32_t)tid; // resolved by a warp below
-            } else if (c <= (uint32_t)kBrickThread) {
-                uint32_t* k = keys + (off[tid] - c);
-                for (uint32_t i = 1; i < c; ++i) { // insertion sort: serial order
-                    const uint32_t key = k[i];
-                    uint32_t j = i;
-                    while (j > 0 && k[j - 1] > key) {
-                        k[j] = k[j - 1];
-                        --j;
-                    }
-                    k[j] = key;
-                }
-                // gather 8 tangents at a time (independent loads), then add them in key order
-                float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-                for (uint32_t i0 = 0; i0 < c; i0 += 8) {
-                    float4 tv[8];
-#pragma unroll
-                    for (int j = 0; j < 8; ++j)
-                        if (i0 + j < c) tv[j] = visit_tangent<SEG>(pair_tan, tan, k[i0 + j]);
-#pragma unroll
-                    for (int j = 0; j < 8; ++j)
-                        if (i0 + j < c) {
-                            sx = __fadd_rn(sx, tv[j].x);
-                            sy = __fadd_rn(sy, tv[j].y);
-                            sz = __fadd_rn(sz, tv[j].z);
-                        }
-                }
-                tq[vi] = pack_tangent(sx, sy, sz, c);
-            } else { // crowded: a CTA of its own sorts the keys
-                const unsigned long long hd = atomicAdd(words + WORD_BHEAVY_COUNT, 1ull);
-                if (keys_global) { // already in the scratch
-                    if (hd < hdesc_cap) hdesc[hd] = make_uint4(vi, keys_at + off[tid] - c, c, job);
-                    else status |= VKHR_DEV_LIST_OVERFLOW;
-                } else {
-                    const unsigned long long hb = atomicAdd(words + WORD_HKEYS_CURSOR, (unsigned long long)c);
-                    if (hb + c <= hkeys_cap && hd < hdesc_cap) {
-                        const uint32_t* k = keys + (off[tid] - c);
-                        for (uint32_t i = 0; i < c; ++i) hkeys[hb + i] = k[i];
-                        hdesc[hd] = make_uint4(vi, (uint32_t)hb, c, job);
-                    } else {
-                        status |= VKHR_DEV_LIST_OVERFLOW;
-                    }
-                }
+    }
+    if (!TANG) return;
+    if (inside && c > (uint32_t)kBrickSmall) { // crowded: a CTA of its own sorts the keys
+        const unsigned long long hd = atomicAdd(words + WORD_BHEAVY_COUNT, 1ull);
+        if (keys_global) { // already in the scratch
+            if (hd < hdesc_cap) hdesc[hd] = make_uint4(vi, keys_at + off[tid] - c, c, job);
+            else status |= VKHR_DEV_LIST_OVERFLOW;
+        } else {
+            const unsigned long long hb = atomicAdd(words + WORD_HKEYS_CURSOR, (unsigned long long)c);
+            if (hb + c <= hkeys_cap && hd < hdesc_cap) {
+                for (uint32_t i = 0; i < c; ++i) hkeys[hb + i] = k[i];
+                hdesc[hd] = make_uint4(vi, (uint32_t)hb, c, job);
+            } else {
+                status |= VKHR_DEV_LIST_OVERFLOW;
             }
         }
+    } else if (inside && c > (uint32_t)kBrickThread) {
+        wlist[atomicAdd(&wcount, 1u)] = (uint32_t)tid; // sorted by a warp below
+    } else if (inside) {
+        for (uint32_t i = 1; i < c; ++i) { // insertion sort: serial order
+            const uint32_t key = k[i];
+            uint32_t j = i;
+            while (j > 0 && k[j - 1] > key) {
+                k[j] = k[j - 1];
+                --j;
+            }
+            k[j] = key;
+        }
     }
-    if (TANG) {
-        __syncthreads();
-        // voxels with kBrickThread < count <= kBrickSmall: a warp sorts the keys
-        // (two per lane), gathers the tangents in parallel and lane 0 adds them in order
+    __syncthreads();
+    {   // voxels with kBrickThread < count <= kBrickSmall: a warp sorts the keys in place (two per lane)
         const unsigned lane = lane_id(), warp = (unsigned)tid >> 5;
-        float* wt = wtan + warp * 3 * 64;
         for (uint32_t m = warp; m < wcount; m += kBrickWarps) {
-            const uint32_t l = wlist[m], c = cnt[l];
-            const uint32_t* k = keys + (off[l] - c);
-            uint32_t ka = lane < c ? k[lane] : 0xffffffffu, kb = lane + 32 < c ? k[lane + 32] : 0xffffffffu;
+            const uint32_t l = wlist[m], cl = cnt[l];
+            uint32_t* kl = keys + (off[l] - cl);
+            uint32_t ka = lane < cl ? kl[lane] : 0xffffffffu, kb = lane + 32 < cl ? kl[lane + 32] : 0xffffffffu;
             warp_sort64(ka, kb);
-            if (lane < c) {
-                const float4 t = visit_tangent<SEG>(pair_tan, tan, ka);
-                wt[lane] = t.x;
-                wt[64 + lane] = t.y;
-                wt[128 + lane] = t.z;
+            if (lane < cl) kl[lane] = ka;
+            if (lane + 32 < cl) kl[lane + 32] = kb;
+        }
+    }
+    __syncthreads();
+    const uint32_t cs = cnt[tid]; // reloaded: fewer registers live across the barriers
+    if (inside && cs <= (uint32_t)kBrickSmall) {
+        const uint32_t c = cs;
+        const uint32_t* k = keys + (off[tid] - c);
+        const uint32_t vi = x + g.w * (y + g.h * z);
+        if (c == 0) {
+            tq[vi] = 0u;
+        } else {
+            // gather kGather tangents at a time (independent loads), then add them in key order
+            float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+            for (uint32_t i0 = 0; i0 < c; i0 += kGather) {
+                float4 tv[kGather];
+#pragma unroll
+                for (int j = 0; j < kGather; ++j)
+                    if (i0 + j < c) tv[j] = visit_tangent<SEG>(pair_tan, tan, k[i0 + j]);
+#pragma unroll
+                for (int j = 0; j < kGather; ++j)
+                    if (i0 + j < c) {
+                        sx = __fadd_rn(sx, tv[j].x);
+                        sy = __fadd_rn(sy, tv[j].y);
+                        sz = __fadd_rn(sz, tv[j].z);
+                    }
             }
-            if (lane + 32 < c) {
-                const float4 t = visit_tangent<SEG>(pair_tan, tan, kb);
-                wt[lane + 32] = t.x;
-                wt[64 + lane + 32] = t.y;
-                wt[128 + lane + 32] = t.z;
-            }
-            __syncwarp();
-            if (lane == 0) {
-                float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-                for (uint32_t i = 0; i < c; ++i) {
-                    sx = __fadd_rn(sx, wt[i]);
-                    sy = __fadd_rn(sy, wt[64 + i]);
-                    sz = __fadd_rn(sz, wt[128 + i]);
-                }
-                const uint32_t lx = bx * 8 + (l & 7), ly = by * 8 + ((l >> 3) & 7), lz = bz * 8 + (l >> 6);
-                tq[lx + g.w * (ly + g.h * lz)] = pack_tangent(sx, sy, sz, c);
-            }
-            __syncwarp();
+            tq[vi] = pack_tangent(sx, sy, sz, c);
         }
     }
 }
@@ -593,68 +608,108 @@ __device__ __forceinline__ void resolve_brick(const VoxJob& J, const Grid& g, ui
 // counting sort of the keys by voxel and the per-voxel resolve.  BIG = false
 // takes the bricks of up to kBrickCap visits (keys sorted in shared memory,
 // list from the front); BIG = true the others (keys sorted into a slice of
-// the global key scratch, list from the back).
-template <bool SEG, bool TANG, bool BIG>
+// the global key scratch, list from the back).  The next brick's queue slot
+// and bounds are fetched while the current one is processed, and the entry
+// passes keep kBrickUnroll loads in flight per thread.
+constexpr int kBrickUnroll = 4;
+
+template <bool SEG, bool TANG, bool BIG, bool PACK>
 __global__ void __launch_bounds__(kBrickThreads, 2)
 brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__ pair_tan_all,
              const uint32_t* __restrict__ visits, const uint32_t* __restrict__ cursor, const uint32_t* __restrict__ list,
-             uint32_t list_n, const uint2* __restrict__ entries, size_t entries_cap, uint4* hdesc, size_t hdesc_cap,
-             uint32_t* hkeys, size_t hkeys_cap, unsigned long long* words)
+             uint32_t list_n, const void* __restrict__ entries_raw, size_t entries_cap, uint4* hdesc,
+             size_t hdesc_cap, uint32_t* hkeys, size_t hkeys_cap, unsigned long long* words)
 {
+    typedef Entry<PACK> E;
+    typedef typename E::T ET;
+    const ET* __restrict__ entries = reinterpret_cast<const ET*>(entries_raw);
     extern __shared__ uint32_t sm[];
     uint32_t* cnt = sm;                       // visits per local voxel
     uint32_t* off = sm + kBrickThreads;       // slice cursor per local voxel
     uint32_t* warp_sums = sm + 2 * kBrickThreads;
-    uint32_t* wlist = sm + 2 * kBrickThreads + 32;             // voxels for the warp resolve
-    float* wtan = reinterpret_cast<float*>(wlist + kBrickThreads); // per warp: 64 x 3 tangents
-    uint32_t* keys = wlist + kBrickThreads + kBrickWarps * 3 * 64; // (BIG = false only)
-    __shared__ uint32_t next, wcount, s_job, s_hb;
+    uint32_t* wlist = sm + 2 * kBrickThreads + 32;             // voxels for the warp sort
+    uint32_t* keys = wlist + kBrickThreads;                    // (BIG = false only)
+    __shared__ uint32_t s_gb, s_nv, s_start, wcount, s_job, s_hb;
     __shared__ uint32_t s_brick_base[kMaxJobs];
     load_bases(jobs, nj, nullptr, s_brick_base);
     const int tid = threadIdx.x;
     unsigned status = 0;
     const uint32_t listed = (uint32_t)words[BIG ? WORD_BIG_LIST : WORD_BRICK_LIST];
+    unsigned long long* queue = words + (BIG ? WORD_BIG_QUEUE : WORD_BRICK_QUEUE);
+    // thread 0 holds the next brick: its queue slot, then its id and bounds
+    uint32_t nq = 0, ngb = 0, nnv = 0, nstart = 0;
+    if (tid == 0) {
+        nq = (uint32_t)atomicAdd(queue, 1ull);
+        if (nq < listed) {
+            ngb = BIG ? list[list_n - 1 - nq] : list[nq];
+            nnv = visits[ngb];
+            nstart = cursor[ngb] - nnv;
+        }
+    }
     for (;;) {
-        if (tid == 0) next = (uint32_t)atomicAdd(words + (BIG ? WORD_BIG_QUEUE : WORD_BRICK_QUEUE), 1ull);
-        __syncthreads();
-        const uint32_t q = next;
-        __syncthreads();
-        if (q >= listed) break;
-        const uint32_t gb = BIG ? list[list_n - 1 - q] : list[q];
-        const uint32_t nv = visits[gb], start = cursor[gb] - nv;
-        if ((uint64_t)start + nv > entries_cap) { // visit budget exceeded: the fill pass flagged it
-            status |= VKHR_DEV_LIST_OVERFLOW;
-            continue;
+        if (tid == 0) {
+            s_gb = nq < listed ? ngb : 0xffffffffu;
+            s_nv = nnv;
+            s_start = nstart;
+            wcount = 0;
+            if (nq < listed) {
+                s_job = (uint32_t)find_job(s_brick_base, nj, ngb);
+                s_hb = (TANG && BIG) ? (uint32_t)atomicAdd(words + WORD_HKEYS_CURSOR, (unsigned long long)nnv) : 0u;
+                nq = (uint32_t)atomicAdd(queue, 1ull); // the brick after: arrives while this one is processed
+            }
         }
         cnt[tid] = 0;
-        if (tid == 0) {
-            wcount = 0;
-            s_job = (uint32_t)find_job(s_brick_base, nj, gb);
-            s_hb = (TANG && BIG) ? (uint32_t)atomicAdd(words + WORD_HKEYS_CURSOR, (unsigned long long)nv) : 0u;
-        }
         __syncthreads();
-        if (TANG && BIG && (uint64_t)s_hb + nv > hkeys_cap) { // key scratch exhausted
+        const uint32_t gb = s_gb, nv = s_nv, start = s_start;
+        if (gb == 0xffffffffu) break;
+        const bool skip = (uint64_t)start + nv > entries_cap ||                 // visit budget exceeded
+                          (TANG && BIG && (uint64_t)s_hb + nv > hkeys_cap);     // key scratch exhausted
+        if (skip) {
             status |= VKHR_DEV_LIST_OVERFLOW;
-            continue;
-        }
-        const VoxJob& J = jobs[s_job];
-        const Grid& g = J.g;
-        const uint32_t b = gb - J.brick_base;   // brick within the style's grid
-        const float4* pair_tan = pair_tan_all + J.item_base;
-        uint32_t* kbase = BIG ? hkeys + s_hb : keys;
-        for (uint32_t i = tid; i < nv; i += kBrickThreads) atomicAdd(cnt + (__ldg(&entries[start + i].y) & 511u), 1u);
-        __syncthreads();
-        if (TANG) {
-            off[tid] = block_exclusive_scan_512(cnt[tid], warp_sums);
-            __syncthreads();
-            for (uint32_t i = tid; i < nv; i += kBrickThreads) {
-                const uint2 e = __ldg(entries + start + i);
-                kbase[atomicAdd(off + (e.y & 511u), 1u)] = e.x;
+            if (tid == 0 && nq < listed) {
+                ngb = BIG ? list[list_n - 1 - nq] : list[nq];
+                nnv = visits[ngb];
+                nstart = cursor[ngb] - nnv;
             }
-            __syncthreads(); // also orders the scratch writes before the block's reads
+        } else {
+            const VoxJob& J = jobs[s_job];
+            const Grid& g = J.g;
+            const uint32_t b = gb - J.brick_base;   // brick within the style's grid
+            const float4* pair_tan = pair_tan_all + J.item_base;
+            uint32_t* kbase = BIG ? hkeys + s_hb : keys;
+            const ET* src = entries + start;
+            for (uint32_t i0 = tid; i0 < nv; i0 += kBrickThreads * kBrickUnroll) {
+                ET e[kBrickUnroll];
+#pragma unroll
+                for (int j = 0; j < kBrickUnroll; ++j)
+                    if (i0 + j * kBrickThreads < nv) e[j] = __ldg(src + i0 + j * kBrickThreads);
+#pragma unroll
+                for (int j = 0; j < kBrickUnroll; ++j)
+                    if (i0 + j * kBrickThreads < nv) atomicAdd(cnt + E::local(e[j]), 1u);
+            }
+            if (tid == 0 && nq < listed) { // the next brick's bounds, while this one's passes run
+                ngb = BIG ? list[list_n - 1 - nq] : list[nq];
+                nnv = visits[ngb];
+                nstart = cursor[ngb] - nnv;
+            }
+            __syncthreads();
+            if (TANG) {
+                off[tid] = block_exclusive_scan_512(cnt[tid], warp_sums);
+                __syncthreads();
+                for (uint32_t i0 = tid; i0 < nv; i0 += kBrickThreads * kBrickUnroll) {
+                    ET e[kBrickUnroll];
+#pragma unroll
+                    for (int j = 0; j < kBrickUnroll; ++j)
+                        if (i0 + j * kBrickThreads < nv) e[j] = __ldg(src + i0 + j * kBrickThreads);
+#pragma unroll
+                    for (int j = 0; j < kBrickUnroll; ++j)
+                        if (i0 + j * kBrickThreads < nv) kbase[atomicAdd(off + E::local(e[j]), 1u)] = E::key(e[j]);
+                }
+                __syncthreads(); // also orders the scratch writes before the block's reads
+            }
+            resolve_brick<SEG, TANG>(J, g, b, pair_tan, cnt, off, kbase, BIG, s_hb, wlist, wcount, hdesc, hdesc_cap,
+                                     hkeys, hkeys_cap, s_job, words, status);
         }
-        resolve_brick<SEG, TANG>(J, g, b, pair_tan, cnt, off, kbase, BIG, s_hb, wlist, wcount, wtan, hdesc, hdesc_cap,
-                                 hkeys, hkeys_cap, s_job, words, status);
         __syncthreads();
     }
     if (status) atomicOr(words + WORD_STATUS, (unsigned long long)status);
@@ -910,21 +965,21 @@ vkhr_status check_device_status(vkhr_ctx* ctx, unsigned long long s)
     return VKHR_OK;
 }
 
-template <bool SEG, bool TANG>
+template <bool SEG, bool TANG, bool PACK>
 vkhr_status launch_brick(vkhr_ctx* ctx, const VoxJob* d_jobs, int nj, uint32_t total_bricks, cudaStream_t st,
                          unsigned blocks, size_t cap_visits)
 {
     // bricks above kBrickCap first (their keys go to the global scratch), then the rest
-    const size_t small = (size_t)(2 * kBrickThreads + 32 + kBrickThreads + kBrickWarps * 3 * 64) * sizeof(uint32_t);
+    const size_t small = (size_t)(2 * kBrickThreads + 32 + kBrickThreads) * sizeof(uint32_t);
     const size_t smem = small + (TANG ? (size_t)kBrickCap * sizeof(uint32_t) : 0);
-    VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG, true>), (unsigned)ctx->sm_count * 2, kBrickThreads, small, st, d_jobs, nj,
+    VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG, true, PACK>), (unsigned)ctx->sm_count * 2, kBrickThreads, small, st,
+                d_jobs, nj, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->brick_list, total_bricks,
+                ctx->items, cap_visits, ctx->hdesc, ctx->hdesc_cap, ctx->hkeys, cap_visits, ctx->d_words);
+    VKHR_CUDA_TRY(ctx, cudaFuncSetAttribute(brick_kernel<SEG, TANG, false, PACK>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG, false, PACK>), blocks, kBrickThreads, smem, st, d_jobs, nj,
                 ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->brick_list, total_bricks, ctx->items,
                 cap_visits, ctx->hdesc, ctx->hdesc_cap, ctx->hkeys, cap_visits, ctx->d_words);
-    VKHR_CUDA_TRY(ctx, cudaFuncSetAttribute(brick_kernel<SEG, TANG, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)smem));
-    VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG, false>), blocks, kBrickThreads, smem, st, d_jobs, nj, ctx->pair_tan,
-                ctx->brick_visits, ctx->brick_cursor, ctx->brick_list, total_bricks, ctx->items, cap_visits,
-                ctx->hdesc, ctx->hdesc_cap, ctx->hkeys, cap_visits, ctx->d_words);
     return VKHR_OK;
 }
 
@@ -976,6 +1031,9 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
             return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "batch too large (2^32 items or bricks)");
     }
     const uint32_t total_items = (uint32_t)items, total_bricks = (uint32_t)bricks;
+    // 4-byte visit entries when every key fits in 23 bits (or keys are not needed)
+    bool pack = true;
+    for (int j = 0; j < nj; ++j) pack = pack && (!tang || jobs[j].n_in <= kPackedKeyLimit);
     VKHR_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
 
     // job table: pinned staging (reused once the previous upload has run) -> device
@@ -1021,15 +1079,24 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
     const unsigned threads = 256;
     const unsigned in_blocks = std::min(vkhr_blocks(total_items, threads), (unsigned)ctx->sm_count * 16);
     const size_t bin_smem_bytes = (size_t)nj * (sizeof(VoxJob) + sizeof(uint32_t));
+    const bool single = nj == 1;
     if (total_items) {
-        if (segments)
-            VKHR_LAUNCH(ctx, (bin_kernel<false, true>), in_blocks, threads, bin_smem_bytes, st, d_jobs, nj, total_items,
-                        ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap,
-                        ctx->d_words);
+        if (segments && single)
+            VKHR_LAUNCH(ctx, (bin_kernel<false, true, false, true>), in_blocks, threads, 0, st, jobs[0], d_jobs, nj,
+                        total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, nullptr,
+                        (size_t)0, ctx->d_words);
+        else if (segments)
+            VKHR_LAUNCH(ctx, (bin_kernel<false, true, false, false>), in_blocks, threads, bin_smem_bytes, st, jobs[0],
+                        d_jobs, nj, total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor,
+                        nullptr, (size_t)0, ctx->d_words);
+        else if (single)
+            VKHR_LAUNCH(ctx, (bin_kernel<false, false, false, true>), in_blocks, threads, 0, st, jobs[0], d_jobs, nj,
+                        total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, nullptr,
+                        (size_t)0, ctx->d_words);
         else
-            VKHR_LAUNCH(ctx, (bin_kernel<false, false>), in_blocks, threads, bin_smem_bytes, st, d_jobs, nj, total_items,
-                        ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->items, ctx->items_cap,
-                        ctx->d_words);
+            VKHR_LAUNCH(ctx, (bin_kernel<false, false, false, false>), in_blocks, threads, bin_smem_bytes, st, jobs[0],
+                        d_jobs, nj, total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor,
+                        nullptr, (size_t)0, ctx->d_words);
     }
     const unsigned rblocks = std::min(vkhr_blocks(total_bricks, kRangeThreads * kRangeItems), (unsigned)ctx->sm_count * 8);
     VKHR_LAUNCH(ctx, bin_ranges_kernel, rblocks, kRangeThreads, 0, st, ctx->brick_visits, total_bricks,
@@ -1063,22 +1130,34 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
         if (s != VKHR_OK) return s;
     }
     if (total_items) {
-        if (segments)
-            VKHR_LAUNCH(ctx, (bin_kernel<true, true>), in_blocks, threads, bin_smem_bytes, st, d_jobs, nj, total_items,
-                        ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->items, cap_visits,
-                        ctx->d_words);
-        else
-            VKHR_LAUNCH(ctx, (bin_kernel<true, false>), in_blocks, threads, bin_smem_bytes, st, d_jobs, nj, total_items,
-                        ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->items, cap_visits,
-                        ctx->d_words);
+        void* ent = ctx->items;
+#define VKHR_FILL(SEG_, PACK_)                                                                                    \
+    do {                                                                                                         \
+        if (single)                                                                                              \
+            VKHR_LAUNCH(ctx, (bin_kernel<true, SEG_, PACK_, true>), in_blocks, threads, 0, st, jobs[0], d_jobs, nj,  \
+                        total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ent,     \
+                        cap_visits, ctx->d_words);                                                                \
+        else                                                                                                     \
+            VKHR_LAUNCH(ctx, (bin_kernel<true, SEG_, PACK_, false>), in_blocks, threads, bin_smem_bytes, st,       \
+                        jobs[0], d_jobs, nj, total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits,        \
+                        ctx->brick_cursor, ent, cap_visits, ctx->d_words);                                        \
+    } while (0)
+        if (segments && pack) VKHR_FILL(true, true);
+        else if (segments) VKHR_FILL(true, false);
+        else if (pack) VKHR_FILL(false, true);
+        else VKHR_FILL(false, false);
+#undef VKHR_FILL
     }
     const unsigned bblocks = std::min(total_bricks, (unsigned)ctx->sm_count * 2);
-    if (segments)
-        s = tang ? launch_brick<true, true>(ctx, d_jobs, nj, total_bricks, st, bblocks, cap_visits)
-                 : launch_brick<true, false>(ctx, d_jobs, nj, total_bricks, st, bblocks, cap_visits);
-    else
-        s = tang ? launch_brick<false, true>(ctx, d_jobs, nj, total_bricks, st, bblocks, cap_visits)
-                 : launch_brick<false, false>(ctx, d_jobs, nj, total_bricks, st, bblocks, cap_visits);
+    if (segments) {
+        if (!tang) s = launch_brick<true, false, true>(ctx, d_jobs, nj, total_bricks, st, bblocks, cap_visits);
+        else if (pack) s = launch_brick<true, true, true>(ctx, d_jobs, nj, total_bricks, st, bblocks, cap_visits);
+        else s = launch_brick<true, true, false>(ctx, d_jobs, nj, total_bricks, st, bblocks, cap_visits);
+    } else {
+        if (!tang) s = launch_brick<false, false, true>(ctx, d_jobs, nj, total_bricks, st, bblocks, cap_visits);
+        else if (pack) s = launch_brick<false, true, true>(ctx, d_jobs, nj, total_bricks, st, bblocks, cap_visits);
+        else s = launch_brick<false, true, false>(ctx, d_jobs, nj, total_bricks, st, bblocks, cap_visits);
+    }
     if (s != VKHR_OK) return s;
     if (tang)
         VKHR_LAUNCH(ctx, crowded_kernel, (unsigned)ctx->sm_count * 6, kCrowdThreads, 0, st, d_jobs, ctx->hdesc, ctx->hdesc_cap,
