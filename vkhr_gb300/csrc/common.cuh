@@ -26,13 +26,14 @@ enum {
     WORD_STATUS = 3,            // VKHR_DEV_* bits
     WORD_BRICK_CURSOR = 4,      // brick path: allocation cursor of the visit list
     WORD_MAX_BRICK_VISITS = 5,  // brick path: largest brick
-    WORD_BHEAVY_COUNT = 6,      // brick path: crowded-voxel descriptors
+    WORD_BHEAVY_COUNT = 6,      // brick path: crowded voxels up to kCrowdWarpMax visits (listed from the front)
     WORD_HKEYS_CURSOR = 7,      // brick path: key scratch cursor (crowded voxels, bricks above kBrickCap)
     WORD_BRICK_QUEUE = 8,       // brick path: next entry of the occupied-brick list
     WORD_BRICK_LIST = 9,        // brick path: occupied bricks resolved in shared memory
-    WORD_NORM = 10,             // normalize: min, max (2 slots); words below are cleared per voxelization
-    WORD_AABB = 12,             // bounding-box scratch (8 slots)
-    WORD_RAY_QUEUE = 20,        // batched raymarch: next tile
+    WORD_BHEAVY_BIG = 10,       // brick path: crowded voxels above kCrowdWarpMax visits (listed from the back)
+    WORD_NORM = 12,             // normalize: min, max (2 slots); words below are cleared per voxelization
+    WORD_AABB = 14,             // bounding-box scratch (8 slots)
+    WORD_RAY_QUEUE = 22,        // batched raymarch: next tile
     WORD_COUNT = 24
 };
 

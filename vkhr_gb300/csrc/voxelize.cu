@@ -43,6 +43,7 @@ constexpr int kBrickCap = 22528;       // visits a brick resolves in shared memo
 constexpr int kBrickThread = 16;       // <= this many visits: sorted and summed by the voxel's thread
 constexpr int kBrickSmall = 64;        // <= this many visits: sorted by one warp (2 keys per lane)
 constexpr int kBrickWarps = kBrickThreads / 32;
+constexpr int kCrowdWarpMax = 256;     // crowded voxels up to this many visits: one warp each
 constexpr int kGather = 4;             // tangent loads in flight per voxel thread (64 registers at 2 CTAs / SM)
 constexpr int kHeavyTile = 2048;       // crowded voxels: shared-memory sort tile
 constexpr int kKeep = 256;             // crowded voxels: tangents summed (>= 255)
@@ -535,16 +536,19 @@ __device__ __forceinline__ void resolve_brick(const VoxJob& J, const Grid& g, ui
         if (J.dens) J.dens[vi] = (uint8_t)(c < 255u ? c : 255u);
     }
     if (!TANG) return;
-    if (inside && c > (uint32_t)kBrickSmall) { // crowded: a CTA of its own sorts the keys
-        const unsigned long long hd = atomicAdd(words + WORD_BHEAVY_COUNT, 1ull);
+    if (inside && c > (uint32_t)kBrickSmall) { // crowded: a warp or a CTA of its own sorts the keys
+        // descriptors of up to kCrowdWarpMax visits from the front, larger ones from the back
+        const bool by_warp = c <= (uint32_t)kCrowdWarpMax;
+        const unsigned long long hd = atomicAdd(words + (by_warp ? WORD_BHEAVY_COUNT : WORD_BHEAVY_BIG), 1ull);
+        const size_t at = by_warp ? (size_t)hd : hdesc_cap - 1 - (size_t)hd;
         if (keys_global) { // already in the scratch
-            if (hd < hdesc_cap) hdesc[hd] = make_uint4(vi, keys_at + off[tid] - c, c, job);
+            if (hd < hdesc_cap) hdesc[at] = make_uint4(vi, keys_at + off[tid] - c, c, job);
             else status |= VKHR_DEV_LIST_OVERFLOW;
         } else {
             const unsigned long long hb = atomicAdd(words + WORD_HKEYS_CURSOR, (unsigned long long)c);
             if (hb + c <= hkeys_cap && hd < hdesc_cap) {
                 for (uint32_t i = 0; i < c; ++i) hkeys[hb + i] = k[i];
-                hdesc[hd] = make_uint4(vi, (uint32_t)hb, c, job);
+                hdesc[at] = make_uint4(vi, (uint32_t)hb, c, job);
             } else {
                 status |= VKHR_DEV_LIST_OVERFLOW;
             }
@@ -827,18 +831,131 @@ __device__ void resolve_crowded(const uint32_t* src, uint32_t c, const float* __
     __syncthreads();
 }
 
-// One CTA per crowded voxel of the brick path (descriptors: voxel, key
-// offset, count, style).
-__global__ void __launch_bounds__(kCrowdThreads) crowded_kernel(const VoxJob* __restrict__ jobs, const uint4* __restrict__ hdesc,
-                                                      size_t hdesc_cap, const uint32_t* __restrict__ hkeys,
-                                                      const unsigned long long* words)
+// Tangent input of a visit key: the pair's stored tangent (segments) or the
+// vertex's own (vertices).
+__device__ __forceinline__ void key_tangent(const VoxJob& J, const float4* __restrict__ pair_tan_all, uint32_t key,
+                                            float& x, float& y, float& z)
+{
+    if (J.pairs) {
+        const float4 t = __ldg(pair_tan_all + J.item_base + key);
+        x = t.x;
+        y = t.y;
+        z = t.z;
+    } else {
+        const float* t = J.tan + 3 * (size_t)key;
+        x = __ldg(t);
+        y = __ldg(t + 1);
+        z = __ldg(t + 2);
+    }
+}
+
+// Ascending bitonic sort of 32 * R keys held R per lane; after it the key at
+// (lane, r) has rank lane * R + r.  Exchanges with partners less than R
+// apart stay in registers, the others go through shuffles.
+template <int R>
+__device__ __forceinline__ void warp_sort(uint32_t (&v)[R])
+{
+    const unsigned lane = lane_id();
+#pragma unroll
+    for (int k = 2; k <= 32 * R; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j < R) {
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const int pr = r ^ j;
+                    if (pr > r) {
+                        const bool up = ((lane * R + r) & k) == 0;
+                        const uint32_t a = v[r], b = v[pr];
+                        if ((a > b) == up) {
+                            v[r] = b;
+                            v[pr] = a;
+                        }
+                    }
+                }
+            } else {
+                const int lj = j / R;
+                const bool lower = (lane & lj) == 0;
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const uint32_t o = __shfl_xor_sync(0xffffffffu, v[r], lj);
+                    const bool up = ((lane * R + r) & k) == 0;
+                    v[r] = (lower == up) ? min(v[r], o) : max(v[r], o);
+                }
+            }
+        }
+    }
+}
+
+// One crowded voxel (c <= 32 * R keys at src) by one warp: sort, gather the
+// first min(c, 255) tangents into shared memory in parallel, then lanes 0..2
+// add the x, y and z components in key order.
+template <int R>
+__device__ __forceinline__ void resolve_warp(const VoxJob& J, const float4* __restrict__ pair_tan_all,
+                                             const uint32_t* __restrict__ src, uint32_t c, float (*wt)[kKeep],
+                                             uint32_t* out)
+{
+    const unsigned lane = lane_id();
+    uint32_t v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) { // coalesced load; a sorting network takes any input order
+        const uint32_t i = (uint32_t)r * 32u + lane;
+        v[r] = i < c ? __ldg(src + i) : 0xffffffffu;
+    }
+    warp_sort<R>(v);
+    const uint32_t m = c < 255u ? c : 255u;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const uint32_t p = lane * R + r;
+        if (p < m) key_tangent(J, pair_tan_all, v[r], wt[0][p], wt[1][p], wt[2][p]);
+    }
+    __syncwarp();
+    float sum = 0.0f;
+    if (lane < 3)
+        for (uint32_t i = 0; i < m; ++i) sum = __fadd_rn(sum, wt[lane][i]);
+    const float sx = __shfl_sync(0xffffffffu, sum, 0), sy = __shfl_sync(0xffffffffu, sum, 1),
+                sz = __shfl_sync(0xffffffffu, sum, 2);
+    if (lane == 0) *out = pack_tangent(sx, sy, sz, m);
+    __syncwarp();
+}
+
+constexpr int kCrowdWarps = 8; // warps per CTA of crowded_warp_kernel
+
+// Crowded voxels of up to kCrowdWarpMax visits, one warp each (descriptors
+// from the front of the list: voxel, key offset, count, style).
+__global__ void __launch_bounds__(32 * kCrowdWarps) crowded_warp_kernel(const VoxJob* __restrict__ jobs,
+                                                                        const float4* __restrict__ pair_tan_all,
+                                                                        const uint4* __restrict__ hdesc,
+                                                                        size_t hdesc_cap,
+                                                                        const uint32_t* __restrict__ hkeys,
+                                                                        const unsigned long long* words)
+{
+    __shared__ float wt[kCrowdWarps][3][kKeep];
+    unsigned long long nh = words[WORD_BHEAVY_COUNT];
+    if (nh > hdesc_cap) nh = hdesc_cap;
+    const unsigned warp = threadIdx.x >> 5;
+    for (unsigned long long h = (unsigned long long)blockIdx.x * kCrowdWarps + warp; h < nh;
+         h += (unsigned long long)gridDim.x * kCrowdWarps) {
+        const uint4 d = hdesc[h];
+        const VoxJob& J = jobs[d.w];
+        if (d.z <= 128u) resolve_warp<4>(J, pair_tan_all, hkeys + d.y, d.z, wt[warp], J.tq + d.x);
+        else resolve_warp<8>(J, pair_tan_all, hkeys + d.y, d.z, wt[warp], J.tq + d.x);
+    }
+}
+
+// Crowded voxels above kCrowdWarpMax visits, one CTA each (descriptors from
+// the back of the list).
+__global__ void __launch_bounds__(kCrowdThreads) crowded_kernel(const VoxJob* __restrict__ jobs,
+                                                                const uint4* __restrict__ hdesc, size_t hdesc_cap,
+                                                                const uint32_t* __restrict__ hkeys,
+                                                                const unsigned long long* words)
 {
     __shared__ uint32_t keys[kHeavyTile];
     __shared__ float tv[3][kKeep];
-    unsigned long long nh = words[WORD_BHEAVY_COUNT];
+    unsigned long long nh = words[WORD_BHEAVY_BIG];
     if (nh > hdesc_cap) nh = hdesc_cap;
     for (unsigned long long h = blockIdx.x; h < nh; h += gridDim.x) {
-        const uint4 d = hdesc[h];
+        const uint4 d = hdesc[hdesc_cap - 1 - h];
         const VoxJob& J = jobs[d.w];
         resolve_crowded(hkeys + d.y, d.z, J.tan, J.pairs, keys, tv, J.tq + d.x);
     }
@@ -1159,9 +1276,12 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
         else s = launch_brick<false, true, false>(ctx, d_jobs, nj, total_bricks, st, bblocks, cap_visits);
     }
     if (s != VKHR_OK) return s;
-    if (tang)
-        VKHR_LAUNCH(ctx, crowded_kernel, (unsigned)ctx->sm_count * 6, kCrowdThreads, 0, st, d_jobs, ctx->hdesc, ctx->hdesc_cap,
-                    ctx->hkeys, ctx->d_words);
+    if (tang) {
+        VKHR_LAUNCH(ctx, crowded_warp_kernel, (unsigned)ctx->sm_count * 8, 32 * kCrowdWarps, 0, st, d_jobs,
+                    ctx->pair_tan, ctx->hdesc, ctx->hdesc_cap, ctx->hkeys, ctx->d_words);
+        VKHR_LAUNCH(ctx, crowded_kernel, (unsigned)ctx->sm_count * 6, kCrowdThreads, 0, st, d_jobs, ctx->hdesc,
+                    ctx->hdesc_cap, ctx->hkeys, ctx->d_words);
+    }
     VKHR_CUDA_TRY(ctx, cudaGetLastError());
     return VKHR_OK;
 }
