@@ -351,6 +351,87 @@ def batched_comparison(args, dev, stream, rank, world, flush):
     return out
 
 
+SCALE = {
+    "workload": "1,048,576 strands x 32 vertices (33,554,432 vertices, 32,505,856 segments; radius-1.2 hemisphere, "
+                "step 0.04) segment-voxelized into 512^3 (u32 counts, u8, i8x4 tangents; 8-byte visit entries), "
+                "normalized, raymarched at 3840x2160 with 1024 steps, 128-step shadows, 8-tap AO; plus 4 views of "
+                "the volume (1920x1080 each) in one batched launch",
+}
+
+
+def scale_section(args, dev, stream, flush):
+    """The scale workload: per-stage device times (median of the steps)."""
+    import torch
+
+    from vkhr_gb300 import _abi, _native, scene, strands
+
+    s = stream.cuda_stream
+    ctx = _native.Context(dev.index)
+    st = strands.hemisphere_style(1_048_576, 32, radius=1.2, step_length=0.04, seed=4)
+    t = strands.generate_tangents(st.vertices, st.segments)
+    idx = strands.generate_indices(st.segments)
+    res = (512, 512, 512)
+    n = 512 ** 3
+    dv = torch.from_numpy(st.vertices).to(dev)
+    dt = torch.from_numpy(t).to(dev)
+    di = torch.from_numpy(idx.view(np.int32)).to(dev)
+    b = ctx.bounding_box(dv.data_ptr(), st.vertex_count, s)
+    counts = torch.empty(n, dtype=torch.int32, device=dev)
+    dens = torch.empty(n, dtype=torch.uint8, device=dev)
+    tq = torch.empty((n, 4), dtype=torch.int8, device=dev)
+    p = scene.make_params(b, res, 3840, 2160, camera_distance=5.0, raycast_steps=1024.0, shadow_steps=128.0)
+    rgba = torch.empty((2160, 3840, 4), dtype=torch.float32, device=dev)
+    depth = torch.empty((2160, 3840), dtype=torch.float32, device=dev)
+    views = [scene.make_params(b, res, 1920, 1080, camera_distance=5.0, raycast_steps=1024.0, shadow_steps=128.0,
+                               view_direction=vd)
+             for vd in ((0.0, 0.0, 1.0), (1.0, 0.3, 0.0), (0.0, 1.0, 0.2), (-0.7, 0.2, -0.7))]
+    rects = [_native.raymarch_footprint(v) for v in views]
+    atlas = torch.empty((max(r[3] for r in rects), sum(r[2] for r in rects), 4), dtype=torch.float32, device=dev)
+    jobs, at = [], 0
+    for v, (x0, y0, w, h) in zip(views, rects):
+        j = _abi.RaymarchJob()
+        j.params = v
+        j.d_density, j.d_tangent = dens.data_ptr(), tq.data_ptr()
+        j.d_rgba = atlas[0, at].data_ptr()
+        j.x0, j.y0, j.w, j.h, j.pitch = x0, y0, w, h, atlas.shape[1]
+        jobs.append(j)
+        at += w
+
+    stages = {
+        "voxelize": lambda: ctx.voxelize_segments(dv.data_ptr(), dt.data_ptr(), di.data_ptr(), idx.shape[0], b, res,
+                                                  _abi.INDEX_REF_FP32, counts.data_ptr(), dens.data_ptr(),
+                                                  tq.data_ptr(), s),
+        "normalize": lambda: ctx.normalize_densities(dens.data_ptr(), n, s),
+        "raymarch": lambda: ctx.raymarch(p, dens.data_ptr(), tq.data_ptr(), None, rgba.data_ptr(),
+                                         depth.data_ptr(), s),
+        "raymarch_4_views_batched": lambda: ctx.raymarch_batched(jobs, s),
+    }
+    times = {k: [] for k in stages}
+    for k in range(max(args.warmup, 3) + args.steps):
+        for name, f in stages.items():
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            f()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if k >= max(args.warmup, 3):
+                times[name].append(e0.elapsed_time(e1))
+    ctx.check_status(s)
+    ms = {k: statistics.median(v) for k, v in times.items()}
+    view_px = sum(r[2] * r[3] for r in rects)
+    out = {
+        "config": SCALE, "ms": ms,
+        "voxelize_msegments_per_s": st.segment_count / (ms["voxelize"] / 1e3) / 1e6,
+        "raymarch_mpixels_per_s": 3840 * 2160 / (ms["raymarch"] / 1e3) / 1e6,
+        "batched_views_region_pixels": view_px,
+        "batched_views_mpixels_per_s": view_px / (ms["raymarch_4_views_batched"] / 1e3) / 1e6,
+        "visits": int(counts.sum(dtype=torch.int64).item()),
+    }
+    ctx.close()
+    return out
+
+
 def gb300_arm(args):
     import torch
 
@@ -364,6 +445,11 @@ def gb300_arm(args):
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream()
     s = stream.cuda_stream
+    if args.section == "scale":  # the scale workload alone (profiling runs)
+        flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+        if rank == 0:
+            print(json.dumps({"section": "scale", "scale": scale_section(args, dev, stream, flush)}))
+        return 0
     if args.section == "batched":  # the multi-style comparison alone (profiling runs)
         flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
         out = batched_comparison(args, dev, stream, rank, world, flush)
@@ -506,6 +592,7 @@ def gb300_arm(args):
 
     batched = None if (args.no_batched or args.section == "frame") else batched_comparison(
         args, dev, stream, rank, world, flush)
+    scale = None if (args.no_scale or args.section == "frame" or world > 1) else scale_section(args, dev, stream, flush)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -527,6 +614,8 @@ def gb300_arm(args):
     }
     if batched is not None:
         line["batched"] = batched
+    if scale is not None:
+        line["scale"] = scale
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import oracle as O
 
@@ -555,8 +644,10 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 16-style batched vs plain comparison")
-    ap.add_argument("--section", default="all", choices=["all", "frame", "batched"],
-                    help="frame: the production frame only; batched: the multi-style comparison only")
+    ap.add_argument("--no-scale", action="store_true", help="skip the 512^3 scale workload")
+    ap.add_argument("--section", default="all", choices=["all", "frame", "batched", "scale"],
+                    help="frame: the production frame only; batched: the multi-style comparison only; "
+                         "scale: the 512^3 workload only")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)

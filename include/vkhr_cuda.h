@@ -265,6 +265,22 @@ vkhr_status vkhr_check_status(vkhr_ctx* ctx, void* stream);
 vkhr_status vkhr_normalize_densities(vkhr_ctx* ctx, uint8_t* d_densities, uint64_t voxel_count, void* stream);
 /* (d_densities must be 16-byte aligned, as cudaMalloc returns.) */
 
+/* Filters of Volume::downsample (hair_style.hh:228-257), which takes any
+ * functor of the 2x2x2 neighbourhood; the ABI offers these. */
+typedef enum vkhr_downsample_filter {
+    VKHR_FILTER_MAX = 0,      /* max of the 8 densities              */
+    VKHR_FILTER_MIN = 1,      /* min of the 8 densities              */
+    VKHR_FILTER_MEAN = 2,     /* floor(sum / 8)                      */
+    VKHR_FILTER_SUM = 3       /* min(sum, 255)                       */
+} vkhr_downsample_filter;
+
+/* Replaces HairStyle::Volume::downsample (hair_style.hh:228-257): u8
+ * densities of a width x height x depth grid reduced 2x2x2 into a
+ * (width/2) x (height/2) x (depth/2) grid.  The dimensions must be even (for
+ * odd ones the reference reads past rows and past the end of the grid). */
+vkhr_status vkhr_downsample_densities(vkhr_ctx* ctx, const uint8_t* d_in, int32_t width, int32_t height,
+                                      int32_t depth, int32_t filter, uint8_t* d_out, void* stream);
+
 /* ---- raymarch ---------------------------------------------------------------
  * Replaces the Vulkan draw of the volume proxy cube (volume.cc:104-112) and
  * the fragment shader volume.frag:31-103 with its includes.  One ray per

@@ -55,6 +55,7 @@ def lib():
         _lib.oracle_segment_visits.argtypes = [P, P, C.c_uint64, C.POINTER(_abi.AABB), C.c_int, C.c_int, C.c_int]
         _lib.oracle_segment_visits.restype = C.c_uint32
         _lib.oracle_normalize.argtypes = [P, C.c_uint64]
+        _lib.oracle_downsample.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, P]
         _lib.oracle_pixel_entry.argtypes = [C.POINTER(_abi.RaymarchParams), C.c_int, C.c_int, P]
         _lib.oracle_raymarch_f64.argtypes = [C.POINTER(_abi.RaymarchParams), P, P, P, P, P, P, C.c_int, C.c_int,
                                              C.c_int]
@@ -78,6 +79,7 @@ def ref():
                                       P, P]
         _ref.ref_raymarch.argtypes = [C.POINTER(_abi.RaymarchParams), P, P, P, P, P, C.c_int, C.c_int, C.c_int]
         _ref.ref_raymarch.restype = C.c_int
+        _ref.ref_downsample.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, P]
     return _ref
 
 
@@ -146,6 +148,14 @@ def normalize(densities):
     return d
 
 
+def downsample(densities, res, filt):
+    w, h, d = (int(x) for x in res)
+    src = np.ascontiguousarray(densities, dtype=np.uint8)
+    out = np.zeros((w // 2) * (h // 2) * (d // 2), dtype=np.uint8)
+    lib().oracle_downsample(_p(src), w, h, d, int(filt), _p(out))
+    return out
+
+
 # ---- raymarch ----------------------------------------------------------------
 
 def raymarch(params, density, tangent, depth_in=None, precision="f64", rows=None, threads=0, diag=False):
@@ -193,6 +203,14 @@ def ref_voxelize(mode, vertices, tangents, indices, res, normalize=False):
     ref().ref_voxelize(1 if mode == "segments" else 0, _p(v), v.shape[0], _p(t), _p(idx), idx.shape[0], w, h, d,
                        1 if normalize else 0, _p(dens), _p(tq))
     return dens, tq
+
+
+def ref_downsample(densities, res, filt):
+    w, h, d = (int(x) for x in res)
+    src = np.ascontiguousarray(densities, dtype=np.uint8)
+    out = np.zeros((w // 2) * (h // 2) * (d // 2), dtype=np.uint8)
+    ref().ref_downsample(_p(src), w, h, d, int(filt), _p(out))
+    return out
 
 
 def ref_raymarch(params, density, tangent, depth_in=None, rows=None, threads=0):

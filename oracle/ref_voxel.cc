@@ -5,6 +5,7 @@
 // compare the C oracle with the reference code on the same inputs.
 #include <vkhr/scene_graph/hair_style.hh>
 
+#include <array>
 #include <cstdint>
 #include <cstring>
 
@@ -62,4 +63,24 @@ extern "C" void ref_voxelize(int segments_mode, const float* vertices, uint32_t 
         tangents_out[4 * i + 2] = v.tangents[i].z;
         tangents_out[4 * i + 3] = v.tangents[i].w;
     }
+}
+
+// Volume::downsample with the filters the ABI offers (0 max, 1 min, 2 floor
+// of the mean, 3 saturating sum); the reference itself has no call site.
+extern "C" void ref_downsample(const uint8_t* in, int w, int h, int d, int filter, uint8_t* out)
+{
+    vkhr::HairStyle::Volume v{glm::vec3(w, h, d), vkhr::AABB{}};
+    v.densities.assign(in, in + (std::size_t)w * h * d);
+    auto run = [&](auto f) {
+        vkhr::HairStyle::Volume r = v.downsample(f);
+        std::memcpy(out, r.densities.data(), r.densities.size());
+    };
+    if (filter == 0)
+        run([](const std::array<unsigned char, 8>& n) { unsigned char m = 0; for (auto x : n) m = x > m ? x : m; return m; });
+    else if (filter == 1)
+        run([](const std::array<unsigned char, 8>& n) { unsigned char m = 255; for (auto x : n) m = x < m ? x : m; return m; });
+    else if (filter == 2)
+        run([](const std::array<unsigned char, 8>& n) { unsigned s = 0; for (auto x : n) s += x; return (unsigned char)(s / 8u); });
+    else
+        run([](const std::array<unsigned char, 8>& n) { unsigned s = 0; for (auto x : n) s += x; return (unsigned char)(s < 255u ? s : 255u); });
 }

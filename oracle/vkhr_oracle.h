@@ -52,6 +52,7 @@ uint32_t oracle_segment_visits(const float* vertices, const uint32_t* indices, u
 
 /* hair_style.cc:344-357 (constant volume -> 0, the reference divides by 0). */
 void oracle_normalize(uint8_t* densities, uint64_t n);
+void oracle_downsample(const uint8_t* in, int w, int h, int d, int filter, uint8_t* out);
 
 /* Rasterizer stand-in for the proxy cube (volume.vert:17-25, volume.cc:60-102,
  * back-face culling): world-space entry point of the ray through the centre

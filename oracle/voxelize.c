@@ -250,3 +250,26 @@ void oracle_normalize(uint8_t* dens, uint64_t n)
         dens[i] = (uint8_t)(x * scaling);
     }
 }
+
+/* HairStyle::Volume::downsample (hair_style.hh:228-257) with the ABI's
+ * filters: max, min, floor(sum / 8), min(sum, 255); even dimensions. */
+void oracle_downsample(const uint8_t* in, int w, int h, int d, int filter, uint8_t* out)
+{
+    const int ow = w / 2, oh = h / 2, od = d / 2;
+    for (int k = 0; k < od; ++k)
+        for (int j = 0; j < oh; ++j)
+            for (int i = 0; i < ow; ++i) {
+                unsigned mx = 0, mn = 255, sum = 0;
+                for (int z = 0; z < 2; ++z)
+                    for (int y = 0; y < 2; ++y)
+                        for (int x = 0; x < 2; ++x) {
+                            const unsigned v = in[(size_t)(2 * i + x) + (size_t)(2 * j + y) * w +
+                                                  (size_t)(2 * k + z) * w * h];
+                            if (v > mx) mx = v;
+                            if (v < mn) mn = v;
+                            sum += v;
+                        }
+                unsigned r = filter == 0 ? mx : filter == 1 ? mn : filter == 2 ? sum / 8u : (sum < 255u ? sum : 255u);
+                out[(size_t)i + (size_t)j * ow + (size_t)k * ow * oh] = (uint8_t)r;
+            }
+}

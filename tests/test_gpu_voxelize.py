@@ -174,3 +174,22 @@ def test_prepare_kernels(ctx, oracle_lib):
     ctx.generate_indices(st.segments, di.data_ptr(), torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
     assert np.array_equal(di.cpu().numpy().view(np.uint32), oracle_lib.generate_indices(st.segments))
+
+
+@pytest.mark.parametrize("filt", [_abi.FILTER_MAX, _abi.FILTER_MIN, _abi.FILTER_MEAN, _abi.FILTER_SUM])
+def test_downsample(ctx, oracle_lib, filt):
+    """Volume::downsample (hair_style.hh:228-257) on the GPU against the oracle."""
+    import torch
+
+    st, t, idx = style("hemi", 4096, 16)
+    b = oracle_lib.bounding_box(st.vertices)
+    res = (64, 38, 50)
+    _, d, _, _ = oracle_lib.voxelize("segments", st.vertices, t, idx, b, res)
+    ref = oracle_lib.downsample(d, res, filt)
+    din = torch.from_numpy(d).cuda()
+    out = torch.full((ref.size,), 7, dtype=torch.uint8, device="cuda")
+    ctx.downsample_densities(din.data_ptr(), res, filt, out.data_ptr())
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy(), ref)
+    with pytest.raises(Exception):
+        ctx.downsample_densities(din.data_ptr(), (63, 38, 50), filt, out.data_ptr())  # odd width

@@ -40,3 +40,13 @@ def test_raymarch_against_reference_shader(oracle_lib):
     rgba, depth, diag = O.raymarch(p, dn, tq, diag=True)
     assert (ref[..., 3] > 0).sum() > 100
     assert np.abs(rgba - ref).max() <= 1e-4
+
+
+@pytest.mark.parametrize("filt", [0, 1, 2, 3])
+def test_downsample_against_reference(oracle_lib, filt):
+    """Volume::downsample (hair_style.hh:228-257) with each filter the ABI offers."""
+    O = oracle_lib
+    st = strands.hemisphere_style(2500, 12, seed=7)
+    t, idx, b = O.ref_prepare(st.vertices, st.segments)
+    d_ref, _ = O.ref_voxelize("segments", st.vertices, t, idx, (32, 18, 40))
+    assert np.array_equal(O.downsample(d_ref, (32, 18, 40), filt), O.ref_downsample(d_ref, (32, 18, 40), filt))

@@ -30,6 +30,11 @@ STATUS_NAMES = {
 INDEX_REF_FP32 = 0
 INDEX_EXACT = 1
 
+FILTER_MAX = 0
+FILTER_MIN = 1
+FILTER_MEAN = 2
+FILTER_SUM = 3
+
 DENSITY_U8_UNORM = 0
 DENSITY_U32_COUNT = 1
 DENSITY_F32 = 2

@@ -19,6 +19,7 @@ EXPORTS = [
     "vkhr_malloc", "vkhr_free", "vkhr_upload", "vkhr_download", "vkhr_sync", "vkhr_check_status",
     "vkhr_voxelize_batched", "vkhr_set_visit_budget", "vkhr_sizeof_voxel_job",
     "vkhr_raymarch_batched", "vkhr_raymarch_footprint", "vkhr_sizeof_raymarch_job",
+    "vkhr_downsample_densities",
 ]
 
 _lib = None
@@ -59,6 +60,7 @@ def load():
     lib.vkhr_raymarch_batched.argtypes = [P, C.POINTER(_abi.RaymarchJob), C.c_int32, P]
     lib.vkhr_raymarch_footprint.argtypes = [C.POINTER(_abi.RaymarchParams), C.POINTER(C.c_int32)]
     lib.vkhr_normalize_densities.argtypes = [P, P, C.c_uint64, P]
+    lib.vkhr_downsample_densities.argtypes = [P, P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P, P]
     lib.vkhr_check_status.argtypes = [P, P]
     lib.vkhr_raymarch.argtypes = [P, C.POINTER(_abi.RaymarchParams), P, P, P, P, P, P]
     lib.vkhr_malloc.argtypes = [P, C.c_size_t, C.POINTER(C.c_void_p)]
@@ -170,6 +172,10 @@ class Context:
 
     def normalize_densities(self, d_densities, n, stream=None):
         self.check(self.lib.vkhr_normalize_densities(self.handle, d_densities, n, stream))
+
+    def downsample_densities(self, d_in, res, filt, d_out, stream=None):
+        w, h, d = res
+        self.check(self.lib.vkhr_downsample_densities(self.handle, d_in, w, h, d, filt, d_out, stream))
 
     def raymarch(self, params, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, stream=None):
         self.check(self.lib.vkhr_raymarch(self.handle, C.byref(params), d_density, d_tangent, d_depth_in, d_rgba,

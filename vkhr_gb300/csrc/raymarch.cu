@@ -184,27 +184,105 @@ __device__ Vec3 sample_tangent(const RayConsts& c, const void* t, Vec3 p)
 // (u = s * N - 0.5 per axis) reads texels i0 and i0 + 1; shifting to
 // cell = i0 + 1 in [0, N], brick k covers cells [8k, 8k + 8), i.e. texels
 // [8k - 1, 8k + 7].  A brick is occupied when any of those texels is nonzero;
-// every sample whose cell lies in an empty brick is exactly 0.  One warp per brick.
+// every sample whose cell lies in an empty brick is exactly 0.
+//
+// One thread per column: the chunk of 8 texels along x at x0 = 8 * cx (one
+// vector load when aligned) in each of the 8 x 8 rows y in [8a, 8a + 8),
+// z in [8c, 8c + 8).  Texel x0 + i belongs to cell brick cx (i <= 7) and
+// texel x0 + 7 also to cx + 1; along y (and z) row 8a + i belongs to cell
+// brick a, and row 8a + 7 also to a + 1.  The thread ORs its rows' masks in
+// registers and marks at most 8 bricks.
+template <int DF>
+__device__ __forceinline__ uint32_t chunk_mask(const typename DensityTexel<DF>::T* __restrict__ p, int n)
+{
+    typedef DensityTexel<DF> TX;
+    uint32_t m = 0;
+    if (n == 8 && DF == VKHR_DENSITY_U8_UNORM && !(reinterpret_cast<uintptr_t>(p) & 7u)) {
+        const uint2 v = __ldg(reinterpret_cast<const uint2*>(p));
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            m |= ((v.x >> (8 * i)) & 0xffu) ? (1u << i) : 0u;
+            m |= ((v.y >> (8 * i)) & 0xffu) ? (1u << (i + 4)) : 0u;
+        }
+    } else if (n == 8 && DF != VKHR_DENSITY_U8_UNORM && !(reinterpret_cast<uintptr_t>(p) & 15u)) {
+        const float4* q = reinterpret_cast<const float4*>(p);
+        const float4 a = __ldg(q), b = __ldg(q + 1);
+        const float f[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+        const uint32_t* w = reinterpret_cast<const uint32_t*>(f);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) // u32 counts: nonzero bits; f32: nonzero value (-0 is zero)
+            m |= (DF == VKHR_DENSITY_F32 ? f[i] != 0.0f : w[i] != 0u) ? (1u << i) : 0u;
+    } else {
+        for (int i = 0; i < n; ++i) m |= TX::load(p, i) != 0.0f ? (1u << i) : 0u;
+    }
+    return m;
+}
+
+__device__ __forceinline__ void occupancy_mark(uint32_t* bits, int nbx, int nby, int kx, int ky, int kz)
+{
+    const uint32_t b = (uint32_t)kx + (uint32_t)nbx * ((uint32_t)ky + (uint32_t)nby * (uint32_t)kz);
+    atomicOr(bits + (b >> 5), 1u << (b & 31)); // result unused: a fire-and-forget reduction
+}
+
+template <int DF>
+__device__ __forceinline__ void occupancy_column(const typename DensityTexel<DF>::T* __restrict__ d, int nx, int ny,
+                                                 int nz, int nbx, int nby, uint32_t* bits, int cx, int a, int c)
+{
+    const int x0 = 8 * cx, n = min(8, nx - x0);
+    uint32_t m_all = 0, m_y = 0, m_z = 0, m_yz = 0; // rows of brick (a, c); last y row; last z row; both
+    for (int zz = 0; zz < 8; ++zz) {
+        const int z = 8 * c + zz;
+        if (z >= nz) break;
+        uint32_t mz = 0, my = 0;
+#pragma unroll
+        for (int yy = 0; yy < 8; ++yy) {
+            const int y = 8 * a + yy;
+            if (y < ny) {
+                const uint32_t m = chunk_mask<DF>(d + (size_t)nx * ((size_t)y + (size_t)ny * z) + x0, n);
+                mz |= m;
+                if (yy == 7) my = m;
+            }
+        }
+        m_all |= mz;
+        m_y |= my;
+        if (zz == 7) {
+            m_z = mz;
+            m_yz = my;
+        }
+    }
+    const uint32_t ms[4] = {m_all, m_y, m_z, m_yz};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (!ms[k]) continue;
+        const int ky = a + (k & 1), kz = c + (k >> 1);
+        occupancy_mark(bits, nbx, nby, cx, ky, kz);
+        if (ms[k] & 0x80u) occupancy_mark(bits, nbx, nby, cx + 1, ky, kz);
+    }
+}
+
 template <int DF>
 __global__ void occupancy_kernel(const typename DensityTexel<DF>::T* __restrict__ d, int nx, int ny, int nz, int bx,
                                  int by, int bz, uint32_t* __restrict__ bits)
 {
-    typedef DensityTexel<DF> TX;
-    const int lane = threadIdx.x & 31;
-    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
-    const uint64_t total = (uint64_t)bx * by * bz;
-    for (uint64_t b = blockIdx.x * (uint64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); b < total; b += warps) {
-        const int kx = (int)(b % bx), ky = (int)((b / bx) % by), kz = (int)(b / ((uint64_t)bx * by));
-        bool nz_found = false;
-        for (int i = lane; i < (kBrick + 1) * (kBrick + 1) * (kBrick + 1) && !nz_found; i += 32) {
-            const int x = kBrick * kx - 1 + i % (kBrick + 1);
-            const int y = kBrick * ky - 1 + (i / (kBrick + 1)) % (kBrick + 1);
-            const int z = kBrick * kz - 1 + i / ((kBrick + 1) * (kBrick + 1));
-            if (x >= 0 && y >= 0 && z >= 0 && x < nx && y < ny && z < nz)
-                nz_found = TX::load(d, (size_t)x + (size_t)nx * ((size_t)y + (size_t)ny * z)) != 0.0f;
-        }
-        if (__any_sync(0xffffffffu, nz_found) && lane == 0) atomicOr(bits + (b >> 5), 1u << (b & 31));
+    // columns with cx fastest (a warp reads consecutive chunks of a row)
+    const uint32_t cxn = (uint32_t)(nx + 7) / 8, an = (uint32_t)(ny + 7) / 8, cn = (uint32_t)(nz + 7) / 8;
+    const uint32_t total = cxn * an * cn;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const uint32_t r = i / cxn, cx = i - r * cxn;
+        const uint32_t c = r / an, a = r - c * an;
+        occupancy_column<DF>(d, nx, ny, nz, bx, by, bits, (int)cx, (int)a, (int)c);
     }
+}
+
+static inline uint64_t occupancy_columns(int nx, int ny, int nz)
+{
+    return (uint64_t)((nx + 7) / 8) * ((ny + 7) / 8) * ((nz + 7) / 8);
+}
+
+static inline unsigned occupancy_blocks(int nx, int ny, int nz, int sm_count)
+{
+    const uint64_t cols = occupancy_columns(nx, ny, nz);
+    return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((cols + 127) / 128, (uint64_t)sm_count * 16));
 }
 
 // Classifies one sample position (texel coordinates u).  Returns 1 when the
@@ -441,7 +519,7 @@ struct RayJob {
     uint32_t* occ;         // this view's occupancy bitmap
     int x0, y0, w, h, pitch, tiles_x;
     uint32_t tile_base;    // first tile of the job in the batch
-    uint32_t brick_base;   // first occupancy brick of the job in the batch
+    uint32_t column_base;  // first occupancy column of the job's volume in the batch
 };
 
 static_assert(sizeof(RayJob) % 4 == 0, "RayJob is copied as 32-bit words");
@@ -460,31 +538,19 @@ __device__ __forceinline__ int find_base(const uint32_t* base, int nj, uint32_t 
 }
 
 template <int DF>
-__global__ void occupancy_batched_kernel(const RayJob* __restrict__ jobs, int nj, uint32_t total_bricks)
+__global__ void occupancy_batched_kernel(const RayJob* __restrict__ jobs, int nj, uint32_t total_columns)
 {
-    typedef DensityTexel<DF> TX;
     __shared__ uint32_t s_base[kMaxRayJobs];
-    for (int j = threadIdx.x; j < nj; j += blockDim.x) s_base[j] = jobs[j].brick_base;
+    for (int j = threadIdx.x; j < nj; j += blockDim.x) s_base[j] = jobs[j].column_base;
     __syncthreads();
-    const int lane = threadIdx.x & 31;
-    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-    for (uint32_t b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); b < total_bricks; b += warps) {
-        const RayJob& J = jobs[find_base(s_base, nj, b)];
-        const uint32_t lb = b - J.brick_base;
-        const int bx = J.c.nb[0], by = J.c.nb[1];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total_columns; i += gridDim.x * blockDim.x) {
+        const RayJob& J = jobs[find_base(s_base, nj, i)];
+        const uint32_t li = i - J.column_base;
         const int nx = J.c.res[0], ny = J.c.res[1], nz = J.c.res[2];
-        const int kx = (int)(lb % (uint32_t)bx), ky = (int)((lb / (uint32_t)bx) % (uint32_t)by),
-                  kz = (int)(lb / ((uint32_t)bx * (uint32_t)by));
-        const typename TX::T* d = (const typename TX::T*)J.dens;
-        bool nz_found = false;
-        for (int i = lane; i < (kBrick + 1) * (kBrick + 1) * (kBrick + 1) && !nz_found; i += 32) {
-            const int x = kBrick * kx - 1 + i % (kBrick + 1);
-            const int y = kBrick * ky - 1 + (i / (kBrick + 1)) % (kBrick + 1);
-            const int z = kBrick * kz - 1 + i / ((kBrick + 1) * (kBrick + 1));
-            if (x >= 0 && y >= 0 && z >= 0 && x < nx && y < ny && z < nz)
-                nz_found = TX::load(d, (size_t)x + (size_t)nx * ((size_t)y + (size_t)ny * z)) != 0.0f;
-        }
-        if (__any_sync(0xffffffffu, nz_found) && lane == 0) atomicOr(J.occ + (lb >> 5), 1u << (lb & 31));
+        const uint32_t cxn = (uint32_t)(nx + 7) / 8, an = (uint32_t)(ny + 7) / 8;
+        const uint32_t r = li / cxn, cx = li - r * cxn, c = r / an, a = r - c * an;
+        occupancy_column<DF>((const typename DensityTexel<DF>::T*)J.dens, nx, ny, nz, J.c.nb[0], J.c.nb[1], J.occ,
+                             (int)cx, (int)a, (int)c);
     }
 }
 
@@ -641,8 +707,7 @@ vkhr_status launch(vkhr_ctx* ctx, const RayConsts& c, const void* dens, const vo
     vkhr_status s = vkhr_reserve(ctx, (void**)&ctx->occ, &ctx->occ_cap, words, sizeof(uint32_t));
     if (s != VKHR_OK) return s;
     VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->occ, 0, words * sizeof(uint32_t), st));
-    const unsigned oblocks = (unsigned)std::min<size_t>((bricks + 7) / 8, (size_t)ctx->sm_count * 32);
-    VKHR_LAUNCH(ctx, occupancy_kernel<DF>, oblocks, 256, 0, st, (const typename DensityTexel<DF>::T*)dens, c.res[0],
+    VKHR_LAUNCH(ctx, occupancy_kernel<DF>, occupancy_blocks(c.res[0], c.res[1], c.res[2], ctx->sm_count), 128, 0, st, (const typename DensityTexel<DF>::T*)dens, c.res[0],
                 c.res[1], c.res[2], c.nb[0], c.nb[1], c.nb[2], ctx->occ);
     const dim3 block(32 * kWarpsX * kWarpsY);
     const dim3 grid((c.W + kTileW * kWarpsX - 1) / (kTileW * kWarpsX), (c.H + kTileH * kWarpsY - 1) / (kTileH * kWarpsY));
@@ -690,12 +755,12 @@ extern "C" vkhr_status vkhr_raymarch(vkhr_ctx* ctx, const vkhr_raymarch_params* 
 namespace {
 
 template <int DF, int TF>
-vkhr_status launch_batched(vkhr_ctx* ctx, const RayJob* d_jobs, int nj, uint32_t total_bricks, uint32_t total_tiles,
+vkhr_status launch_batched(vkhr_ctx* ctx, const RayJob* d_jobs, int nj, uint32_t total_columns, uint32_t total_tiles,
                            cudaStream_t st)
 {
-    const unsigned oblocks = (unsigned)std::min<size_t>((total_bricks + 7) / 8, (size_t)ctx->sm_count * 32);
-    if (total_bricks)
-        VKHR_LAUNCH(ctx, occupancy_batched_kernel<DF>, oblocks ? oblocks : 1, 256, 0, st, d_jobs, nj, total_bricks);
+    const unsigned oblocks = (unsigned)std::min<size_t>((total_columns + 127) / 128, (size_t)ctx->sm_count * 16);
+    if (total_columns)
+        VKHR_LAUNCH(ctx, occupancy_batched_kernel<DF>, oblocks ? oblocks : 1, 128, 0, st, d_jobs, nj, total_columns);
     if (!total_tiles) return VKHR_OK;
     static int per_sm = 0; // resident CTAs per SM of this instantiation
     if (!per_sm) {
@@ -748,7 +813,7 @@ extern "C" vkhr_status vkhr_raymarch_batched(vkhr_ctx* ctx, const vkhr_raymarch_
     VKHR_CUDA_TRY(ctx, cudaStreamIsCapturing(st, &cap));
     const bool capturing = cap != cudaStreamCaptureStatusNone;
     if (!capturing) VKHR_CUDA_TRY(ctx, cudaEventSynchronize(ctx->rjobs_ev));
-    uint64_t tiles = 0, bricks = 0, words = 0;
+    uint64_t tiles = 0, chunks = 0, words = 0;
     size_t occ_at[kMaxRayJobs];
     for (int k = 0; k < job_count; ++k) {
         const vkhr_raymarch_job& in = jobs[order[k]];
@@ -767,14 +832,14 @@ extern "C" vkhr_status vkhr_raymarch_batched(vkhr_ctx* ctx, const vkhr_raymarch_
         J.pitch = in.pitch;
         J.tiles_x = (in.w + kRegionTileW - 1) / kRegionTileW;
         J.tile_base = (uint32_t)tiles;
-        J.brick_base = (uint32_t)bricks;
+        J.column_base = (uint32_t)chunks;
         tiles += (uint64_t)J.tiles_x * ((in.h + kRegionTileH - 1) / kRegionTileH);
         const uint64_t nb = (uint64_t)J.c.nb[0] * J.c.nb[1] * J.c.nb[2];
-        bricks += nb;
+        chunks += occupancy_columns(J.c.res[0], J.c.res[1], J.c.res[2]);
         occ_at[k] = (size_t)words;
         words += (nb + 31) / 32;
-        if (tiles >= (1ull << 32) || bricks >= (1ull << 32))
-            return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "batch too large (2^32 tiles or bricks)");
+        if (tiles >= (1ull << 32) || chunks >= (1ull << 32))
+            return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "batch too large (2^32 tiles or texel chunks)");
     }
     vkhr_status s = vkhr_reserve(ctx, (void**)&ctx->occ, &ctx->occ_cap, (size_t)words, sizeof(uint32_t));
     if (s != VKHR_OK) return s;
@@ -789,7 +854,7 @@ extern "C" vkhr_status vkhr_raymarch_batched(vkhr_ctx* ctx, const vkhr_raymarch_
     VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->occ, 0, (size_t)words * sizeof(uint32_t), st));
     VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_words + WORD_RAY_QUEUE, 0, sizeof(unsigned long long), st));
     const RayJob* d_jobs = reinterpret_cast<const RayJob*>(ctx->d_rjobs);
-    const uint32_t nbk = (uint32_t)bricks, nt = (uint32_t)tiles;
+    const uint32_t nbk = (uint32_t)chunks, nt = (uint32_t)tiles;
     if (df == VKHR_DENSITY_U8_UNORM && tf == VKHR_TANGENT_I8_SNORM)
         s = launch_batched<VKHR_DENSITY_U8_UNORM, VKHR_TANGENT_I8_SNORM>(ctx, d_jobs, job_count, nbk, nt, st);
     else if (df == VKHR_DENSITY_U8_UNORM)
@@ -881,9 +946,7 @@ cudaError_t launch_static(const RayConsts& c, const void* dens, const void* tang
     // the array keeps the previous call's bits: clear the part this grid uses
     cudaError_t e = cudaMemsetAsync(occ, 0, words * sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
-    const size_t bricks = (size_t)c.nb[0] * c.nb[1] * c.nb[2];
-    const unsigned oblocks = (unsigned)std::min<size_t>((bricks + 7) / 8, (size_t)sm_count * 32);
-    occupancy_kernel<DF><<<oblocks, 256, 0, st>>>((const typename DensityTexel<DF>::T*)dens, c.res[0], c.res[1],
+    occupancy_kernel<DF><<<occupancy_blocks(c.res[0], c.res[1], c.res[2], sm_count), 128, 0, st>>>((const typename DensityTexel<DF>::T*)dens, c.res[0], c.res[1],
                                                    c.res[2], c.nb[0], c.nb[1], c.nb[2], occ);
     const dim3 block(32 * kWarpsX * kWarpsY);
     const dim3 grid((c.W + kTileW * kWarpsX - 1) / (kTileW * kWarpsX), (c.H + kTileH * kWarpsY - 1) / (kTileH * kWarpsY));

@@ -85,7 +85,7 @@ struct VoxJob {
     uint32_t item_base;
     uint32_t n_in;
     uint32_t brick_base;
-    uint32_t pad;
+    uint32_t zero_base; // first 4-voxel group of the style (empty-brick zeroing)
 };
 
 static_assert(sizeof(VoxJob) * kMaxJobs <= kJobTableBytes, "job table staging too small");
@@ -406,25 +406,39 @@ __global__ void __launch_bounds__(kRangeThreads) bin_ranges_kernel(const uint32_
 }
 
 // Zeroes every voxel of the bricks no visit reached (visited bricks are
-// written by the brick kernel or the global path): one block per brick.
-__global__ void zero_empty_kernel(const VoxJob* __restrict__ jobs, int nj, uint32_t total_bricks,
+// written by the brick kernel).  A streaming pass in the volumes' own order:
+// one thread per group of 4 voxels along x (16-byte stores of counts and
+// tangents, 4-byte stores of densities when aligned), so that a warp writes
+// contiguous memory wherever neighbouring bricks are empty.
+__global__ void zero_empty_kernel(const VoxJob* __restrict__ jobs, int nj, uint32_t total_groups,
                                   const uint32_t* __restrict__ visits)
 {
-    __shared__ uint32_t s_brick_base[kMaxJobs];
-    load_bases(jobs, nj, nullptr, s_brick_base);
-    for (uint32_t b = blockIdx.x; b < total_bricks; b += gridDim.x) {
-        if (__ldg(visits + b)) continue;
-        const VoxJob& J = jobs[find_job(s_brick_base, nj, b)];
+    __shared__ uint32_t s_base[kMaxJobs];
+    for (int j = threadIdx.x; j < nj; j += blockDim.x) s_base[j] = jobs[j].zero_base;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total_groups; i += gridDim.x * blockDim.x) {
+        const VoxJob& J = jobs[find_job(s_base, nj, i)];
         const Grid& g = J.g;
-        const uint32_t lb = b - J.brick_base;
-        const uint32_t bx = lb % g.nbx, by = (lb / g.nbx) % g.nby, bz = lb / (g.nbx * g.nby);
-        for (uint32_t l = threadIdx.x; l < 512u; l += blockDim.x) {
-            const uint32_t x = bx * 8 + (l & 7), y = by * 8 + ((l >> 3) & 7), z = bz * 8 + (l >> 6);
-            if (x >= g.w || y >= g.h || z >= g.d) continue;
-            const size_t vi = x + (size_t)g.w * (y + (size_t)g.h * z);
-            J.counts[vi] = 0u;
-            if (J.dens) J.dens[vi] = 0;
-            if (J.tq) J.tq[vi] = 0u;
+        const uint32_t li = i - J.zero_base, gw = (g.w + 3) / 4;
+        const uint32_t row = li / gw, x0 = 4 * (li - row * gw);
+        const uint32_t z = row / g.h, y = row - z * g.h;
+        if (__ldg(visits + J.brick_base + (x0 >> 3) + g.nbx * ((y >> 3) + g.nby * (z >> 3)))) continue;
+        const size_t vi = x0 + (size_t)g.w * (y + (size_t)g.h * z);
+        uint32_t* c = J.counts + vi;
+        uint32_t* t = J.tq ? J.tq + vi : nullptr;
+        uint8_t* d = J.dens ? J.dens + vi : nullptr;
+        const uint32_t n = min(4u, g.w - x0);
+        if (n == 4 && !(reinterpret_cast<uintptr_t>(c) & 15u) && (!t || !(reinterpret_cast<uintptr_t>(t) & 15u)) &&
+            (!d || !(reinterpret_cast<uintptr_t>(d) & 3u))) {
+            *reinterpret_cast<uint4*>(c) = make_uint4(0u, 0u, 0u, 0u);
+            if (t) *reinterpret_cast<uint4*>(t) = make_uint4(0u, 0u, 0u, 0u);
+            if (d) *reinterpret_cast<uint32_t*>(d) = 0u;
+        } else {
+            for (uint32_t k = 0; k < n; ++k) {
+                c[k] = 0u;
+                if (t) t[k] = 0u;
+                if (d) d[k] = 0;
+            }
         }
     }
 }
@@ -1035,6 +1049,37 @@ __global__ void rescale_u8_kernel(uint8_t* d, uint64_t n, const unsigned long lo
         d[i] = (uint8_t)rescale1(d[i], lo, hi, scaling);
 }
 
+// ---- Volume::downsample ----------------------------------------------------------------
+
+// One output voxel per thread: the 2x2x2 neighbourhood of the input in the
+// reference's order (x fastest), reduced by the filter.
+__global__ void downsample_kernel(const uint8_t* __restrict__ in, uint32_t w, uint32_t h, uint32_t d, int filter,
+                                  uint8_t* __restrict__ out)
+{
+    const uint32_t ow = w / 2, oh = h / 2, od = d / 2;
+    const uint64_t n = (uint64_t)ow * oh * od;
+    for (uint64_t o = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; o < n; o += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t i = (uint32_t)(o % ow), j = (uint32_t)((o / ow) % oh), k = (uint32_t)(o / ((uint64_t)ow * oh));
+        uint32_t mx = 0, mn = 255, sum = 0;
+#pragma unroll
+        for (int z = 0; z < 2; ++z)
+#pragma unroll
+            for (int y = 0; y < 2; ++y)
+#pragma unroll
+                for (int x = 0; x < 2; ++x) {
+                    const uint32_t v =
+                        __ldg(in + (2 * i + x) + (size_t)w * ((2 * j + y) + (size_t)h * (2 * k + z)));
+                    mx = max(mx, v);
+                    mn = min(mn, v);
+                    sum += v;
+                }
+        out[o] = (uint8_t)(filter == VKHR_FILTER_MAX ? mx
+                           : filter == VKHR_FILTER_MIN ? mn
+                           : filter == VKHR_FILTER_MEAN ? sum / 8u
+                                                        : min(sum, 255u));
+    }
+}
+
 // ---- host ----------------------------------------------------------------------------------
 
 vkhr_status make_grid(vkhr_ctx* ctx, const vkhr_aabb* b, int32_t w, int32_t h, int32_t d, int32_t mode, Grid& g)
@@ -1124,7 +1169,7 @@ vkhr_status make_job(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job& in, Vox
     out.dens = in.d_densities;
     out.tq = reinterpret_cast<uint32_t*>(in.d_tangents);
     out.n_in = n_in;
-    out.pad = 0;
+    out.zero_base = 0;
     return VKHR_OK;
 }
 
@@ -1133,7 +1178,7 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
     if (!ctx) return VKHR_ERR_INVALID_ARG;
     if (nj <= 0 || nj > kMaxJobs || !jobs_in) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "job count must be in [1, 256]");
     VoxJob jobs[kMaxJobs];
-    uint64_t items = 0, bricks = 0;
+    uint64_t items = 0, bricks = 0, groups = 0;
     const bool tang = jobs_in[0].d_tangents != nullptr;
     for (int j = 0; j < nj; ++j) {
         vkhr_status s = make_job(ctx, segments, jobs_in[j], jobs[j]);
@@ -1142,12 +1187,14 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
             return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "every job of a batch requests tangents, or none does");
         jobs[j].item_base = (uint32_t)items;
         jobs[j].brick_base = (uint32_t)bricks;
+        jobs[j].zero_base = (uint32_t)groups;
         items += jobs[j].n_in;
         bricks += jobs[j].g.nb;
-        if (items >= (1ull << 32) || bricks >= (1ull << 32))
-            return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "batch too large (2^32 items or bricks)");
+        groups += (uint64_t)((jobs[j].g.w + 3) / 4) * jobs[j].g.h * jobs[j].g.d;
+        if (items >= (1ull << 32) || bricks >= (1ull << 32) || groups >= (1ull << 32))
+            return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "batch too large (2^32 items, bricks or 4-voxel groups)");
     }
-    const uint32_t total_items = (uint32_t)items, total_bricks = (uint32_t)bricks;
+    const uint32_t total_items = (uint32_t)items, total_bricks = (uint32_t)bricks, total_groups = (uint32_t)groups;
     // 4-byte visit entries when every key fits in 23 bits (or keys are not needed)
     bool pack = true;
     for (int j = 0; j < nj; ++j) pack = pack && (!tang || jobs[j].n_in <= kPackedKeyLimit);
@@ -1218,8 +1265,8 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
     const unsigned rblocks = std::min(vkhr_blocks(total_bricks, kRangeThreads * kRangeItems), (unsigned)ctx->sm_count * 8);
     VKHR_LAUNCH(ctx, bin_ranges_kernel, rblocks, kRangeThreads, 0, st, ctx->brick_visits, total_bricks,
                 ctx->brick_cursor, ctx->brick_list, ctx->d_words);
-    VKHR_LAUNCH(ctx, zero_empty_kernel, std::min(total_bricks, (uint32_t)ctx->sm_count * 16), 256, 0, st, d_jobs, nj,
-                total_bricks, ctx->brick_visits);
+    VKHR_LAUNCH(ctx, zero_empty_kernel, std::min(vkhr_blocks(total_groups, 256), (unsigned)ctx->sm_count * 16), 256, 0,
+                st, d_jobs, nj, total_groups, ctx->brick_visits);
     VKHR_CUDA_TRY(ctx, cudaGetLastError());
 
     if (!bounded) {          // segment mode without a budget: read the visit total back
@@ -1325,6 +1372,25 @@ vkhr_status vkhr_set_visit_budget(vkhr_ctx* ctx, uint64_t max_visits)
     if (!ctx) return VKHR_ERR_INVALID_ARG;
     if (max_visits >= (1ull << 32)) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "budget must be below 2^32 visits");
     ctx->visit_budget = max_visits;
+    return VKHR_OK;
+}
+
+vkhr_status vkhr_downsample_densities(vkhr_ctx* ctx, const uint8_t* d_in, int32_t width, int32_t height,
+                                      int32_t depth, int32_t filter, uint8_t* d_out, void* stream)
+{
+    if (!ctx) return VKHR_ERR_INVALID_ARG;
+    if (!d_in || !d_out) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_in and d_out are required");
+    if (width <= 0 || height <= 0 || depth <= 0 || (width | height | depth) & 1)
+        return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "dimensions must be positive and even");
+    if (filter < VKHR_FILTER_MAX || filter > VKHR_FILTER_SUM)
+        return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "unknown filter");
+    if ((uint64_t)width * height * depth >= (1ull << 32))
+        return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "more than 2^32 - 1 voxels");
+    VKHR_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    const uint64_t n = (uint64_t)(width / 2) * (height / 2) * (depth / 2);
+    VKHR_LAUNCH(ctx, downsample_kernel, std::min(vkhr_blocks(n, 256), (unsigned)ctx->sm_count * 32), 256, 0,
+                (cudaStream_t)stream, d_in, (uint32_t)width, (uint32_t)height, (uint32_t)depth, filter, d_out);
+    VKHR_CUDA_TRY(ctx, cudaGetLastError());
     return VKHR_OK;
 }
 
