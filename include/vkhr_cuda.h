@@ -333,6 +333,47 @@ vkhr_status vkhr_raymarch_batched(vkhr_ctx* ctx, const vkhr_raymarch_job* jobs, 
  * the camera; w = h = 0 when the box is off screen.  Host-only. */
 vkhr_status vkhr_raymarch_footprint(const vkhr_raymarch_params* params, int32_t rect[4]);
 
+/* ---- differentiable path ----------------------------------------------------
+ * No reference counterpart: gradients of an image loss with respect to an FP32
+ * density volume (VKHR_DENSITY_F32), an FP32 tangent field (VKHR_TANGENT_F32X4,
+ * w ignored), kd and hair_exponent, and -- through the trilinear splat below --
+ * the strand vertex positions.  The forward is the raymarch of vkhr_raymarch
+ * (same results, bit for bit); the isosurface point, the early exit and the
+ * zero tests are constants of the derivative, the clamps of the output pass
+ * gradient only strictly inside (0, 1).  No depth buffer. */
+
+/* Bytes of the per-ray tape of vkhr_raymarch_train: 32 bytes of state per
+ * pixel plus the march's t every checkpoint_interval iterations (0 for
+ * invalid parameters). */
+size_t vkhr_raymarch_tape_bytes(const vkhr_raymarch_params* params, int32_t checkpoint_interval);
+
+/* vkhr_raymarch that also records the tape (16-byte aligned, caller-owned)
+ * vkhr_raymarch_adjoint replays. */
+vkhr_status vkhr_raymarch_train(vkhr_ctx* ctx, const vkhr_raymarch_params* params, const float* d_density,
+                                const float* d_tangent, float* d_rgba, float* d_depth_out, void* d_tape,
+                                size_t tape_bytes, int32_t checkpoint_interval, void* stream);
+
+/* Adds dL/d(density), dL/d(tangent) (float4 per voxel, w left alone) and
+ * [dL/d kd, dL/d hair_exponent] (two doubles) to the caller's buffers, given
+ * dL/d(rgba) (float4 per pixel) and the tape of the training forward on the
+ * same inputs.  The primary march is replayed from the tape's checkpoints,
+ * one thread per ray segment of checkpoint_interval iterations. */
+vkhr_status vkhr_raymarch_adjoint(vkhr_ctx* ctx, const vkhr_raymarch_params* params, const float* d_density,
+                                  const float* d_tangent, const void* d_tape, int32_t checkpoint_interval,
+                                  const float* d_grad_rgba, float* d_grad_density, float* d_grad_tangent,
+                                  double* d_grad_params, void* stream);
+
+/* Continuous trilinear-splat voxelization: every vertex adds its trilinear
+ * weights (in the raymarch's texel convention: texel centres at
+ * origin + (i + 0.5) * size / N) to the FP32 density (accumulated into). */
+vkhr_status vkhr_splat_vertices(vkhr_ctx* ctx, const float* d_vertices, uint32_t vertex_count, const vkhr_aabb* bounds,
+                                int32_t width, int32_t height, int32_t depth, float* d_density, void* stream);
+
+/* dL/d(vertex) (float3 per vertex, written) of the splat, given dL/d(density). */
+vkhr_status vkhr_splat_vertices_adjoint(vkhr_ctx* ctx, const float* d_vertices, uint32_t vertex_count,
+                                        const vkhr_aabb* bounds, int32_t width, int32_t height, int32_t depth,
+                                        const float* d_grad_density, float* d_grad_vertices, void* stream);
+
 /* Allocation-free raymarch.  No counterpart in the reference: it exists for
  * callers that may not allocate device memory at all -- a real-time frame
  * loop that forbids cudaMalloc (which synchronises the device and takes an

@@ -56,6 +56,10 @@ def lib():
         _lib.oracle_segment_visits.restype = C.c_uint32
         _lib.oracle_normalize.argtypes = [P, C.c_uint64]
         _lib.oracle_downsample.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, P]
+        _lib.oracle_diff_loss.argtypes = [C.POINTER(_abi.RaymarchParams), P, P, P, P, P, P, C.c_int]
+        _lib.oracle_diff_loss.restype = C.c_double
+        _lib.oracle_splat.argtypes = [P, C.c_uint32, C.POINTER(_abi.AABB), C.c_int, C.c_int, C.c_int, P]
+        _lib.oracle_splat_adjoint.argtypes = [P, C.c_uint32, C.POINTER(_abi.AABB), C.c_int, C.c_int, C.c_int, P, P]
         _lib.oracle_pixel_entry.argtypes = [C.POINTER(_abi.RaymarchParams), C.c_int, C.c_int, P]
         _lib.oracle_raymarch_f64.argtypes = [C.POINTER(_abi.RaymarchParams), P, P, P, P, P, P, C.c_int, C.c_int,
                                              C.c_int]
@@ -174,6 +178,41 @@ def raymarch(params, density, tangent, depth_in=None, precision="f64", rows=None
         return (rgba, depth, dg) if diag else (rgba, depth)
     lib().oracle_raymarch_f32(C.byref(params), _p(dens), _p(tan), _p(din), _p(rgba), _p(depth), r0, r1, threads)
     return rgba, depth
+
+
+# ---- differentiable path (FP64) ------------------------------------------------
+
+def diff_loss(params, density, tangent, target, grads=False, threads=0):
+    """Loss sum((rgba - target)^2) of the FP64 differentiable raymarch; with
+    grads=True also (g_density, g_tangent (n, 4), g_params [kd, exponent]).
+    density (n,) and tangent (n, 4) are converted to float64."""
+    d = np.ascontiguousarray(density, dtype=np.float64).reshape(-1)
+    t = np.ascontiguousarray(tangent, dtype=np.float64).reshape(-1, 4)
+    tg = _f32(target)
+    if not grads:
+        return float(lib().oracle_diff_loss(C.byref(params), _p(d), _p(t), _p(tg), None, None, None, threads))
+    gd = np.zeros_like(d)
+    gt = np.zeros_like(t)
+    gp = np.zeros(2, dtype=np.float64)
+    loss = lib().oracle_diff_loss(C.byref(params), _p(d), _p(t), _p(tg), _p(gd), _p(gt), _p(gp), threads)
+    return float(loss), gd, gt, gp
+
+
+def splat(vertices, bounds, res):
+    v = _f32(vertices)
+    w, h, d = (int(x) for x in res)
+    out = np.zeros(w * h * d, dtype=np.float64)
+    lib().oracle_splat(_p(v), v.shape[0], C.byref(bounds), w, h, d, _p(out))
+    return out
+
+
+def splat_adjoint(vertices, bounds, res, g_density):
+    v = _f32(vertices)
+    w, h, d = (int(x) for x in res)
+    g = np.ascontiguousarray(g_density, dtype=np.float64)
+    out = np.zeros((v.shape[0], 3), dtype=np.float64)
+    lib().oracle_splat_adjoint(_p(v), v.shape[0], C.byref(bounds), w, h, d, _p(g), _p(out))
+    return out
 
 
 def max_threads():

@@ -47,6 +47,7 @@ static inline REAL SFX(texel_density)(const SFX(vol)* v, long i, long j, long k)
     switch (v->fmt) {
     case VKHR_DENSITY_U8_UNORM: return (REAL)((const uint8_t*)v->data)[at] / (REAL)255; /* UNORM: c/255 */
     case VKHR_DENSITY_U32_COUNT: return (REAL)((const uint32_t*)v->data)[at];
+    case ORACLE_F64: return (REAL)((const double*)v->data)[at];
     default: return (REAL)((const float*)v->data)[at];
     }
 }
@@ -63,6 +64,10 @@ static inline SFX(vec3) SFX(texel_tangent)(const SFX(vol)* v, long i, long j, lo
             if (c[a] < (REAL)-1) c[a] = (REAL)-1;
         }
         return SFX(v3)(c[0], c[1], c[2]);
+    }
+    if (v->fmt == ORACLE_F64) {
+        const double* g = (const double*)v->data + 4 * at;
+        return SFX(v3)((REAL)g[0], (REAL)g[1], (REAL)g[2]);
     }
     const float* f = (const float*)v->data + 4 * at;
     return SFX(v3)((REAL)f[0], (REAL)f[1], (REAL)f[2]);

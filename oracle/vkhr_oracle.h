@@ -54,6 +54,21 @@ uint32_t oracle_segment_visits(const float* vertices, const uint32_t* indices, u
 void oracle_normalize(uint8_t* densities, uint64_t n);
 void oracle_downsample(const uint8_t* in, int w, int h, int d, int filter, uint8_t* out);
 
+/* Texel format of the differentiable oracle: double densities, double x4
+ * tangents (so that finite-difference perturbations are exact). */
+#define ORACLE_F64 100
+
+/* The differentiable raymarch in FP64 (adjoint.c): the loss
+ * sum((rgba - target)^2) with rgba kept in double, and its analytic
+ * gradient (accumulated into g_density, g_tangent (4 per voxel), g_params
+ * [kd, hair_exponent]; any may be NULL).  density / tangent in ORACLE_F64. */
+double oracle_diff_loss(const vkhr_raymarch_params* p, const double* density, const double* tangent,
+                        const float* target, double* g_density, double* g_tangent, double* g_params, int threads);
+/* Trilinear splat of vertices in FP64 (accumulated into density) and its adjoint. */
+void oracle_splat(const float* vertices, uint32_t n, const vkhr_aabb* b, int w, int h, int d, double* density);
+void oracle_splat_adjoint(const float* vertices, uint32_t n, const vkhr_aabb* b, int w, int h, int d,
+                          const double* g_density, double* g_vertices);
+
 /* Rasterizer stand-in for the proxy cube (volume.vert:17-25, volume.cc:60-102,
  * back-face culling): world-space entry point of the ray through the centre
  * of pixel (px, py) into the AABB.  Returns 0 when no front face covers it. */

@@ -1,0 +1,175 @@
+"""The differentiable path on the GPU: the training forward equals
+vkhr_raymarch bit for bit; the adjoint (vkhr_raymarch_adjoint) against FP64
+central finite differences (h = 1e-3) of the FP64 oracle's loss on 256
+random coordinates (densities of nonzero voxels, tangent components, kd and
+the exponent; ill-conditioned coordinates excluded as in
+tests/test_oracle_adjoint.py) and against the oracle's FP64 analytic
+gradient on every coordinate; the result does not depend on the checkpoint
+interval; the splat and its adjoint against the FP64 oracle, and the chained
+vertex gradient through torch.autograd (the check harness)."""
+import numpy as np
+import pytest
+
+from vkhr_gb300 import _abi, adjoint, scene
+from tests.test_oracle_adjoint import FLOOR, H, TOL, central, diff_scene
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).cuda()
+
+
+def _gpu_grads(ctx, torch, p, dens, tan, target, K):
+    """GPU loss gradient: (loss, g_density, g_tangent, g_params, rgba)."""
+    d = _dev(torch, dens).requires_grad_(True)
+    t = _dev(torch, tan).requires_grad_(True)
+    kp = torch.tensor([p.kd, p.hair_exponent], dtype=torch.float64, device="cuda", requires_grad=True)
+    rgba = adjoint.raymarch(d, t, kp, p, ctx, K)
+    loss = ((rgba.double() - _dev(torch, target).double()) ** 2).sum()
+    loss.backward()
+    torch.cuda.synchronize()
+    return (float(loss.detach()), d.grad.double().cpu().numpy(), t.grad.double().cpu().numpy(), kp.grad.cpu().numpy(),
+            rgba.detach().cpu().numpy())
+
+
+@pytest.mark.parametrize("steps", [64.0, 100.0])
+def test_train_forward_equals_raymarch(ctx, oracle_lib, steps):
+    import torch
+
+    st, b, p, dens, tan, target = diff_scene(oracle_lib, size=(96, 72), steps=steps)
+    d, t = _dev(torch, dens), _dev(torch, tan)
+    ref = torch.empty((p.height, p.width, 4), dtype=torch.float32, device="cuda")
+    ctx.raymarch(p, d.data_ptr(), t.data_ptr(), None, ref.data_ptr(), None)
+    for K in (7, 16):
+        out = torch.empty_like(ref)
+        nbytes = ctx.tape_bytes(p, K)
+        tape = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+        ctx.raymarch_train(p, d.data_ptr(), t.data_ptr(), out.data_ptr(), None, tape.data_ptr(), nbytes, K)
+        torch.cuda.synchronize()
+        assert torch.equal(out, ref)
+    assert (ref[..., 3] > 0).sum().item() > 100
+
+
+@pytest.mark.parametrize("steps", [64.0, 100.0])
+def test_adjoint_vs_finite_differences(ctx, oracle_lib, steps):
+    """256 coordinates: 200 densities of nonzero voxels, 54 tangent components,
+    kd and the exponent."""
+    import torch
+
+    O = oracle_lib
+    st, b, p, dens, tan, target = diff_scene(O, steps=steps)
+    d32, t32 = dens.astype(np.float32).astype(np.float64), tan.astype(np.float32).astype(np.float64)
+    loss, gd, gt, gp, rgba = _gpu_grads(ctx, torch, p, d32, t32, target, 16)
+    rng = np.random.default_rng(11)
+    dcoords = rng.choice(np.nonzero((gd != 0) & (d32 > 0))[0], size=200, replace=False)
+    tt = np.nonzero(np.abs(gt[:, :3]).sum(axis=1))[0]
+    tcoords = list(zip(rng.choice(tt, size=54, replace=False).tolist(), rng.integers(0, 3, 54).tolist()))
+
+    def fd(kind, c, h):
+        if kind == "d":
+            def f(x):
+                dd = d32.copy()
+                dd[c] = x
+                return O.diff_loss(p, dd, t32, target)
+            return central(f, d32[c], h)
+        v, k = c
+        def f(x):
+            tt2 = t32.copy()
+            tt2[v, k] = x
+            return O.diff_loss(p, d32, tt2, target)
+        return central(f, t32[v, k], h)
+
+    got, want, ill, n = [], [], 0, 0
+    for kind, coords, g in (("d", dcoords, lambda c: gd[c]), ("t", tcoords, lambda c: gt[c[0], c[1]])):
+        for c in coords:
+            n += 1
+            (f1, dev1), (f2, dev2) = fd(kind, c, H), fd(kind, c, H / 2)
+            if (dev1 > 1e-13 and dev2 > 0.5 * dev1) or abs(f1 - f2) > max(TOL * max(abs(f1), abs(f2)), FLOOR):
+                ill += 1
+                continue
+            got.append(g(c))
+            want.append(f1)
+    assert n == 254 and ill <= 0.1 * n, ill
+    got, want = np.array(got), np.array(want)
+    # 1e-3 relative, normwise over the coordinates: the FP32 forward's image
+    # (which dL/drgba is formed from) differs from the FP64 one by ~1e-5
+    rel = np.linalg.norm(got - want) / np.linalg.norm(want)
+    assert rel <= TOL, rel
+    # each coordinate within 1e-2, but for a few whose pixels take another
+    # discrete decision (surface point) in FP32 than in FP64
+    far = np.abs(got - want) > np.maximum(1e-2 * np.abs(want), FLOOR)
+    assert far.sum() <= 0.02 * n, (far.sum(), got[far][:4], want[far][:4])
+    # kd and the exponent (global: compared with the oracle's analytic value)
+    _, _, _, gp_ref = O.diff_loss(p, d32, t32, target, grads=True)
+    assert np.allclose(gp, gp_ref, rtol=1e-3, atol=FLOOR), (gp, gp_ref)
+
+
+def test_adjoint_vs_oracle_gradient(ctx, oracle_lib):
+    """Every coordinate against the oracle's FP64 analytic gradient (relative L2)."""
+    import torch
+
+    O = oracle_lib
+    st, b, p, dens, tan, target = diff_scene(O, res=(40, 40, 40), size=(128, 96), steps=128.0, seed=6)
+    d32, t32 = dens.astype(np.float32).astype(np.float64), tan.astype(np.float32).astype(np.float64)
+    loss, gd, gt, gp, rgba = _gpu_grads(ctx, torch, p, d32, t32, target, 32)
+    lref, gd_ref, gt_ref, gp_ref = O.diff_loss(p, d32, t32, target, grads=True)
+    assert abs(loss - lref) <= 1e-4 * lref
+    for g, r in ((gd, gd_ref), (gt[:, :3], gt_ref[:, :3])):
+        assert np.linalg.norm(g - r) <= 1e-3 * np.linalg.norm(r), np.linalg.norm(g - r) / np.linalg.norm(r)
+    # kd and the exponent are sums over 12,288 pixels of terms of both signs;
+    # the cancellation amplifies the FP32 image's error (dL/drgba is formed
+    # from it) to a few 1e-3 of the net sum
+    assert np.allclose(gp, gp_ref, rtol=5e-3), (gp, gp_ref)
+
+
+def test_checkpoint_interval_does_not_matter(ctx, oracle_lib):
+    import torch
+
+    st, b, p, dens, tan, target = diff_scene(oracle_lib, size=(96, 72), steps=128.0)
+    res = [_gpu_grads(ctx, torch, p, dens, tan, target, K) for K in (16, 32, 64)]
+    for r in res[1:]:
+        assert r[0] == res[0][0]
+        assert np.linalg.norm(r[1] - res[0][1]) <= 1e-5 * np.linalg.norm(res[0][1])
+        assert np.linalg.norm(r[2] - res[0][2]) <= 1e-5 * np.linalg.norm(res[0][2])
+
+
+def test_splat_and_vertex_gradient(ctx, oracle_lib):
+    """splat(V) on the GPU against the FP64 oracle, and dL/dV of the loss of
+    raymarch(splat(V)) through torch.autograd against the oracle's chain
+    (FP64 loss gradient -> FP64 splat adjoint)."""
+    import torch
+
+    O = oracle_lib
+    st, b, p, dens, tan, target = diff_scene(O, size=(96, 72), steps=64.0)
+    res = tuple(p.volume_resolution)
+    V = torch.from_numpy(st.vertices).cuda().requires_grad_(True)
+    dg = adjoint.splat(V, b, res, ctx)
+    d_ref = O.splat(st.vertices, b, res)
+    assert np.abs(dg.detach().double().cpu().numpy() - d_ref).max() <= 1e-4 * max(1.0, d_ref.max())
+    t = _dev(torch, tan)
+    kp = torch.tensor([p.kd, p.hair_exponent], dtype=torch.float64, device="cuda")
+    rgba = adjoint.raymarch(dg, t, kp, p, ctx, 16)
+    loss = ((rgba.double() - _dev(torch, target).double()) ** 2).sum()
+    loss.backward()
+    gv = V.grad.double().cpu().numpy()
+    _, gd_ref, _, _ = O.diff_loss(p, dg.detach().double().cpu().numpy(), tan.astype(np.float32), target, grads=True)
+    gv_ref = O.splat_adjoint(st.vertices, b, res, gd_ref)
+    assert np.linalg.norm(gv_ref) > 0
+    assert np.linalg.norm(gv - gv_ref) <= 2e-3 * np.linalg.norm(gv_ref), np.linalg.norm(gv - gv_ref) / np.linalg.norm(gv_ref)
+
+
+def test_rejects_other_formats(ctx, oracle_lib):
+    import torch
+    from vkhr_gb300._native import VkhrError
+
+    st, b, p, dens, tan, target = diff_scene(oracle_lib, size=(32, 24))
+    q = _abi.RaymarchParams.from_buffer_copy(p)
+    q.density_format = _abi.DENSITY_U8_UNORM
+    buf = torch.empty(1 << 20, dtype=torch.uint8, device="cuda")
+    with pytest.raises(VkhrError) as e:
+        ctx.raymarch_train(q, buf.data_ptr(), buf.data_ptr(), buf.data_ptr(), None, buf.data_ptr(), 1 << 20, 16)
+    assert e.value.status == _abi.VKHR_ERR_NOT_SUPPORTED
+    with pytest.raises(VkhrError) as e:
+        ctx.raymarch_train(p, buf.data_ptr(), buf.data_ptr(), buf.data_ptr(), None, buf.data_ptr(), 16, 16)
+    assert e.value.status == _abi.VKHR_ERR_CAPACITY

@@ -19,7 +19,8 @@ EXPORTS = [
     "vkhr_malloc", "vkhr_free", "vkhr_upload", "vkhr_download", "vkhr_sync", "vkhr_check_status",
     "vkhr_voxelize_batched", "vkhr_set_visit_budget", "vkhr_sizeof_voxel_job",
     "vkhr_raymarch_batched", "vkhr_raymarch_footprint", "vkhr_sizeof_raymarch_job",
-    "vkhr_downsample_densities",
+    "vkhr_downsample_densities", "vkhr_raymarch_tape_bytes", "vkhr_raymarch_train", "vkhr_raymarch_adjoint",
+    "vkhr_splat_vertices", "vkhr_splat_vertices_adjoint",
 ]
 
 _lib = None
@@ -61,6 +62,14 @@ def load():
     lib.vkhr_raymarch_footprint.argtypes = [C.POINTER(_abi.RaymarchParams), C.POINTER(C.c_int32)]
     lib.vkhr_normalize_densities.argtypes = [P, P, C.c_uint64, P]
     lib.vkhr_downsample_densities.argtypes = [P, P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P, P]
+    lib.vkhr_raymarch_tape_bytes.argtypes = [C.POINTER(_abi.RaymarchParams), C.c_int32]
+    lib.vkhr_raymarch_tape_bytes.restype = C.c_size_t
+    lib.vkhr_raymarch_train.argtypes = [P, C.POINTER(_abi.RaymarchParams), P, P, P, P, P, C.c_size_t, C.c_int32, P]
+    lib.vkhr_raymarch_adjoint.argtypes = [P, C.POINTER(_abi.RaymarchParams), P, P, P, C.c_int32, P, P, P, P, P]
+    lib.vkhr_splat_vertices.argtypes = [P, P, C.c_uint32, C.POINTER(_abi.AABB), C.c_int32, C.c_int32, C.c_int32, P,
+                                        P]
+    lib.vkhr_splat_vertices_adjoint.argtypes = [P, P, C.c_uint32, C.POINTER(_abi.AABB), C.c_int32, C.c_int32,
+                                                C.c_int32, P, P, P]
     lib.vkhr_check_status.argtypes = [P, P]
     lib.vkhr_raymarch.argtypes = [P, C.POINTER(_abi.RaymarchParams), P, P, P, P, P, P]
     lib.vkhr_malloc.argtypes = [P, C.c_size_t, C.POINTER(C.c_void_p)]
@@ -78,7 +87,8 @@ def load():
     lib.vkhr_sizeof_voxel_job.restype = C.c_size_t
     lib.vkhr_sizeof_raymarch_job.restype = C.c_size_t
     for name in EXPORTS:
-        getattr(lib, name).restype = getattr(lib, name).restype or C.c_int
+        if getattr(lib, name).restype is C.c_int or getattr(lib, name).restype is None:
+            getattr(lib, name).restype = C.c_int
     _lib = lib
     return lib
 
@@ -176,6 +186,32 @@ class Context:
     def downsample_densities(self, d_in, res, filt, d_out, stream=None):
         w, h, d = res
         self.check(self.lib.vkhr_downsample_densities(self.handle, d_in, w, h, d, filt, d_out, stream))
+
+    # differentiable path
+    def tape_bytes(self, params, checkpoint_interval):
+        return int(self.lib.vkhr_raymarch_tape_bytes(C.byref(params), checkpoint_interval))
+
+    def raymarch_train(self, params, d_density, d_tangent, d_rgba, d_depth_out, d_tape, tape_bytes,
+                       checkpoint_interval, stream=None):
+        self.check(self.lib.vkhr_raymarch_train(self.handle, C.byref(params), d_density, d_tangent, d_rgba,
+                                                d_depth_out, d_tape, tape_bytes, checkpoint_interval, stream))
+
+    def raymarch_adjoint(self, params, d_density, d_tangent, d_tape, checkpoint_interval, d_grad_rgba,
+                         d_grad_density, d_grad_tangent, d_grad_params, stream=None):
+        self.check(self.lib.vkhr_raymarch_adjoint(self.handle, C.byref(params), d_density, d_tangent, d_tape,
+                                                  checkpoint_interval, d_grad_rgba, d_grad_density, d_grad_tangent,
+                                                  d_grad_params, stream))
+
+    def splat_vertices(self, d_vertices, vertex_count, bounds, res, d_density, stream=None):
+        w, h, d = res
+        self.check(self.lib.vkhr_splat_vertices(self.handle, d_vertices, vertex_count, C.byref(bounds), w, h, d,
+                                                d_density, stream))
+
+    def splat_vertices_adjoint(self, d_vertices, vertex_count, bounds, res, d_grad_density, d_grad_vertices,
+                               stream=None):
+        w, h, d = res
+        self.check(self.lib.vkhr_splat_vertices_adjoint(self.handle, d_vertices, vertex_count, C.byref(bounds), w,
+                                                        h, d, d_grad_density, d_grad_vertices, stream))
 
     def raymarch(self, params, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, stream=None):
         self.check(self.lib.vkhr_raymarch(self.handle, C.byref(params), d_density, d_tangent, d_depth_in, d_rgba,

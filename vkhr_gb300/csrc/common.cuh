@@ -66,6 +66,8 @@ struct vkhr_ctx {
     size_t rjobs_cap;          // in bytes
     void* h_rjobs;             // pinned staging of the raymarch job table
     cudaEvent_t rjobs_ev;      // recorded after the staging was copied out
+    float* g_acc;              // adjoint: per-pixel gradient of the accumulated density
+    size_t g_acc_cap;
     uint32_t* occ;             // raymarch brick-occupancy bitmap
     size_t occ_cap;            // in 32-bit words
     unsigned long long* d_words;

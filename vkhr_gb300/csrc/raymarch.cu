@@ -15,473 +15,11 @@
 //     no later sample can change any output (coverage is clamped to 1);
 //   * texture filtering is a software trilinear with FP32 weights at Vulkan's
 //     texel centres, CLAMP_TO_BORDER reading 0.
-#include "common.cuh"
+#include "march.cuh"
 
-#include <algorithm>
-#include <cmath>
 #include <mutex>
 
 namespace {
-
-constexpr int kTileW = 8, kTileH = 4;         // pixels per warp
-constexpr int kWarpsX = 2, kWarpsY = 2;       // warps per block
-constexpr float kMaxSteps = 1048576.0f;       // 2^20: t += 1/steps still advances below 1
-
-struct RayConsts {
-    int W, H;
-    float inv_vp[16];
-    float pv[16];
-    float cam[3];
-    float radius;
-    float lo[3], hi[3];
-    int res[3];
-    float tsc[3], tbias[3];   // texel coordinate u = P * tsc + tbias = (P - origin) / size * N - 0.5
-    float voxel_space[3];
-    float light[3], intensity[3], color[3];
-    float alpha, exponent, iso, kd;
-    float steps, shadow_steps, thickness, ao_kernel, ao_radius, ao_exp, ao_max;
-    float lod;
-    int shading_model, deep_shadows_on;
-    int steps_pow2, shadow_pow2;  // 1/steps is exact and t = i * step: empty space may be jumped
-    int nb[3];                    // occupancy bricks per axis, (res + 8) / 8
-};
-
-constexpr int kBrick = 8;          // occupancy brick edge in texel cells
-constexpr float kSkipMargin = 0.01f; // texels kept between a predicted sample and a brick face
-
-template <int DF>
-struct DensityTexel;
-template <>
-struct DensityTexel<VKHR_DENSITY_U8_UNORM> {
-    typedef uint8_t T;
-    static __device__ __forceinline__ float load(const T* p, size_t i) { return (float)__ldg(p + i); }
-    static constexpr float scale = 1.0f / 255.0f; // UNORM c / 255
-};
-template <>
-struct DensityTexel<VKHR_DENSITY_U32_COUNT> {
-    typedef uint32_t T;
-    static __device__ __forceinline__ float load(const T* p, size_t i) { return (float)__ldg(p + i); }
-    static constexpr float scale = 1.0f;
-};
-template <>
-struct DensityTexel<VKHR_DENSITY_F32> {
-    typedef float T;
-    static __device__ __forceinline__ float load(const T* p, size_t i) { return __ldg(p + i); }
-    static constexpr float scale = 1.0f;
-};
-
-struct Vec3 {
-    float x, y, z;
-};
-__device__ __forceinline__ Vec3 v3(float x, float y, float z) { return Vec3{x, y, z}; }
-__device__ __forceinline__ Vec3 operator+(Vec3 a, Vec3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
-__device__ __forceinline__ Vec3 operator-(Vec3 a, Vec3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
-__device__ __forceinline__ Vec3 operator*(Vec3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
-__device__ __forceinline__ float dot(Vec3 a, Vec3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__device__ __forceinline__ Vec3 normalize(Vec3 a)
-{
-    float l = sqrtf(dot(a, a));
-    return v3(a.x / l, a.y / l, a.z / l); // 0/0 -> NaN for a zero vector, as on the GPU
-}
-// GLSL mix(x, y, a) = x * (1 - a) + y * a
-__device__ __forceinline__ Vec3 mix(Vec3 a, Vec3 b, float t)
-{
-    const float u = 1.0f - t;
-    return v3(fmaf(b.x, t, a.x * u), fmaf(b.y, t, a.y * u), fmaf(b.z, t, a.z * u));
-}
-__device__ __forceinline__ float clip_depth(const RayConsts& c, Vec3 p)
-{
-    float z = fmaf(c.pv[2], p.x, fmaf(c.pv[6], p.y, fmaf(c.pv[10], p.z, c.pv[14])));
-    float w = fmaf(c.pv[3], p.x, fmaf(c.pv[7], p.y, fmaf(c.pv[11], p.z, c.pv[15])));
-    return z / w;
-}
-
-// Texel-space set-up; false when all eight taps read the border.
-__device__ __forceinline__ bool tex_setup(const RayConsts& c, Vec3 p, int i0[3], float a[3])
-{
-    const float pp[3] = {p.x, p.y, p.z};
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        float u = fmaf(pp[k], c.tsc[k], c.tbias[k]);
-        if (!(u > -2.0f && u < (float)(c.res[k] + 1))) return false;
-        float f = floorf(u);
-        i0[k] = (int)f;
-        a[k] = u - f;
-    }
-    return true;
-}
-
-template <int DF>
-__device__ __forceinline__ float sample_density(const RayConsts& c, const typename DensityTexel<DF>::T* __restrict__ d,
-                                                Vec3 p)
-{
-    typedef DensityTexel<DF> TX;
-    int i0[3];
-    float a[3];
-    if (!tex_setup(c, p, i0, a)) return 0.0f;
-    const int nx = c.res[0], ny = c.res[1], nz = c.res[2];
-    float v[8];
-    if (i0[0] >= 0 && i0[0] + 1 < nx && i0[1] >= 0 && i0[1] + 1 < ny && i0[2] >= 0 && i0[2] + 1 < nz) {
-        const size_t sy = (size_t)nx, sz = (size_t)nx * ny;
-        const size_t b = (size_t)i0[0] + sy * i0[1] + sz * i0[2];
-        v[0] = TX::load(d, b);
-        v[1] = TX::load(d, b + 1);
-        v[2] = TX::load(d, b + sy);
-        v[3] = TX::load(d, b + sy + 1);
-        v[4] = TX::load(d, b + sz);
-        v[5] = TX::load(d, b + sz + 1);
-        v[6] = TX::load(d, b + sz + sy);
-        v[7] = TX::load(d, b + sz + sy + 1);
-    } else {
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const int x = i0[0] + (k & 1), y = i0[1] + ((k >> 1) & 1), z = i0[2] + (k >> 2);
-            v[k] = (x >= 0 && y >= 0 && z >= 0 && x < nx && y < ny && z < nz)
-                       ? TX::load(d, (size_t)x + (size_t)nx * ((size_t)y + (size_t)ny * z))
-                       : 0.0f;
-        }
-    }
-    const float x00 = fmaf(a[0], v[1] - v[0], v[0]);
-    const float x10 = fmaf(a[0], v[3] - v[2], v[2]);
-    const float x01 = fmaf(a[0], v[5] - v[4], v[4]);
-    const float x11 = fmaf(a[0], v[7] - v[6], v[6]);
-    const float y0 = fmaf(a[1], x10 - x00, x00);
-    const float y1 = fmaf(a[1], x11 - x01, x01);
-    return fmaf(a[2], y1 - y0, y0) * TX::scale;
-}
-
-template <int TF>
-__device__ __forceinline__ Vec3 tangent_texel(const void* t, int x, int y, int z, const int* n)
-{
-    if (x < 0 || y < 0 || z < 0 || x >= n[0] || y >= n[1] || z >= n[2]) return v3(0.0f, 0.0f, 0.0f);
-    const size_t i = (size_t)x + (size_t)n[0] * ((size_t)y + (size_t)n[1] * z);
-    if (TF == VKHR_TANGENT_I8_SNORM) {
-        const char4 q = __ldg(reinterpret_cast<const char4*>(t) + i);
-        return v3(fmaxf((float)q.x / 127.0f, -1.0f), fmaxf((float)q.y / 127.0f, -1.0f),
-                  fmaxf((float)q.z / 127.0f, -1.0f));
-    }
-    const float4 f = __ldg(reinterpret_cast<const float4*>(t) + i);
-    return v3(f.x, f.y, f.z);
-}
-
-template <int TF>
-__device__ Vec3 sample_tangent(const RayConsts& c, const void* t, Vec3 p)
-{
-    int i0[3];
-    float a[3];
-    Vec3 acc = v3(0.0f, 0.0f, 0.0f);
-    if (!tex_setup(c, p, i0, a)) return acc;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        const int dx = k & 1, dy = (k >> 1) & 1, dz = k >> 2;
-        const float w = (dx ? a[0] : 1.0f - a[0]) * (dy ? a[1] : 1.0f - a[1]) * (dz ? a[2] : 1.0f - a[2]);
-        acc = acc + tangent_texel<TF>(t, i0[0] + dx, i0[1] + dy, i0[2] + dz, c.res) * w;
-    }
-    return acc;
-}
-
-// Occupancy of the texel-cell grid.  A sample with lower tap i0 = floor(u)
-// (u = s * N - 0.5 per axis) reads texels i0 and i0 + 1; shifting to
-// cell = i0 + 1 in [0, N], brick k covers cells [8k, 8k + 8), i.e. texels
-// [8k - 1, 8k + 7].  A brick is occupied when any of those texels is nonzero;
-// every sample whose cell lies in an empty brick is exactly 0.
-//
-// One thread per column: the chunk of 8 texels along x at x0 = 8 * cx (one
-// vector load when aligned) in each of the 8 x 8 rows y in [8a, 8a + 8),
-// z in [8c, 8c + 8).  Texel x0 + i belongs to cell brick cx (i <= 7) and
-// texel x0 + 7 also to cx + 1; along y (and z) row 8a + i belongs to cell
-// brick a, and row 8a + 7 also to a + 1.  The thread ORs its rows' masks in
-// registers and marks at most 8 bricks.
-template <int DF>
-__device__ __forceinline__ uint32_t chunk_mask(const typename DensityTexel<DF>::T* __restrict__ p, int n)
-{
-    typedef DensityTexel<DF> TX;
-    uint32_t m = 0;
-    if (n == 8 && DF == VKHR_DENSITY_U8_UNORM && !(reinterpret_cast<uintptr_t>(p) & 7u)) {
-        const uint2 v = __ldg(reinterpret_cast<const uint2*>(p));
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            m |= ((v.x >> (8 * i)) & 0xffu) ? (1u << i) : 0u;
-            m |= ((v.y >> (8 * i)) & 0xffu) ? (1u << (i + 4)) : 0u;
-        }
-    } else if (n == 8 && DF != VKHR_DENSITY_U8_UNORM && !(reinterpret_cast<uintptr_t>(p) & 15u)) {
-        const float4* q = reinterpret_cast<const float4*>(p);
-        const float4 a = __ldg(q), b = __ldg(q + 1);
-        const float f[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
-        const uint32_t* w = reinterpret_cast<const uint32_t*>(f);
-#pragma unroll
-        for (int i = 0; i < 8; ++i) // u32 counts: nonzero bits; f32: nonzero value (-0 is zero)
-            m |= (DF == VKHR_DENSITY_F32 ? f[i] != 0.0f : w[i] != 0u) ? (1u << i) : 0u;
-    } else {
-        for (int i = 0; i < n; ++i) m |= TX::load(p, i) != 0.0f ? (1u << i) : 0u;
-    }
-    return m;
-}
-
-__device__ __forceinline__ void occupancy_mark(uint32_t* bits, int nbx, int nby, int kx, int ky, int kz)
-{
-    const uint32_t b = (uint32_t)kx + (uint32_t)nbx * ((uint32_t)ky + (uint32_t)nby * (uint32_t)kz);
-    atomicOr(bits + (b >> 5), 1u << (b & 31)); // result unused: a fire-and-forget reduction
-}
-
-template <int DF>
-__device__ __forceinline__ void occupancy_column(const typename DensityTexel<DF>::T* __restrict__ d, int nx, int ny,
-                                                 int nz, int nbx, int nby, uint32_t* bits, int cx, int a, int c)
-{
-    const int x0 = 8 * cx, n = min(8, nx - x0);
-    uint32_t m_all = 0, m_y = 0, m_z = 0, m_yz = 0; // rows of brick (a, c); last y row; last z row; both
-    for (int zz = 0; zz < 8; ++zz) {
-        const int z = 8 * c + zz;
-        if (z >= nz) break;
-        uint32_t mz = 0, my = 0;
-#pragma unroll
-        for (int yy = 0; yy < 8; ++yy) {
-            const int y = 8 * a + yy;
-            if (y < ny) {
-                const uint32_t m = chunk_mask<DF>(d + (size_t)nx * ((size_t)y + (size_t)ny * z) + x0, n);
-                mz |= m;
-                if (yy == 7) my = m;
-            }
-        }
-        m_all |= mz;
-        m_y |= my;
-        if (zz == 7) {
-            m_z = mz;
-            m_yz = my;
-        }
-    }
-    const uint32_t ms[4] = {m_all, m_y, m_z, m_yz};
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        if (!ms[k]) continue;
-        const int ky = a + (k & 1), kz = c + (k >> 1);
-        occupancy_mark(bits, nbx, nby, cx, ky, kz);
-        if (ms[k] & 0x80u) occupancy_mark(bits, nbx, nby, cx + 1, ky, kz);
-    }
-}
-
-template <int DF>
-__global__ void occupancy_kernel(const typename DensityTexel<DF>::T* __restrict__ d, int nx, int ny, int nz, int bx,
-                                 int by, int bz, uint32_t* __restrict__ bits)
-{
-    // columns with cx fastest (a warp reads consecutive chunks of a row)
-    const uint32_t cxn = (uint32_t)(nx + 7) / 8, an = (uint32_t)(ny + 7) / 8, cn = (uint32_t)(nz + 7) / 8;
-    const uint32_t total = cxn * an * cn;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-        const uint32_t r = i / cxn, cx = i - r * cxn;
-        const uint32_t c = r / an, a = r - c * an;
-        occupancy_column<DF>(d, nx, ny, nz, bx, by, bits, (int)cx, (int)a, (int)c);
-    }
-}
-
-static inline uint64_t occupancy_columns(int nx, int ny, int nz)
-{
-    return (uint64_t)((nx + 7) / 8) * ((ny + 7) / 8) * ((nz + 7) / 8);
-}
-
-static inline unsigned occupancy_blocks(int nx, int ny, int nz, int sm_count)
-{
-    const uint64_t cols = occupancy_columns(nx, ny, nz);
-    return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((cols + 127) / 128, (uint64_t)sm_count * 16));
-}
-
-// Classifies one sample position (texel coordinates u).  Returns 1 when the
-// sample is exactly zero (border, or an empty brick), 2 when it is zero and
-// the ray has left the grid for good (moving away along every such axis),
-// 0 when it must be sampled.  box_lo/box_hi receive the current brick's
-// texel-coordinate extent for the empty-space jump.
-__device__ __forceinline__ int classify(const RayConsts& c, const uint32_t* __restrict__ occ, const float u[3],
-                                        const float du[3], float box_lo[3], float box_hi[3])
-{
-    int cell[3];
-    bool outside = false, leaving = false;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const float f = floorf(u[k]);
-        if (!(f >= -1.0f && f <= (float)(c.res[k] - 1))) {
-            outside = true;
-            if ((u[k] < -1.0f - kSkipMargin && du[k] <= 0.0f) || (u[k] > (float)c.res[k] + kSkipMargin && du[k] >= 0.0f) ||
-                !(u[k] == u[k]))
-                leaving = true;
-            cell[k] = 0;
-        } else {
-            cell[k] = (int)f + 1;
-        }
-    }
-    if (outside) { // zero, but no brick to jump across: step singly
-#pragma unroll
-        for (int k = 0; k < 3; ++k) box_lo[k] = box_hi[k] = u[k];
-        return leaving ? 2 : 1;
-    }
-    const int bxk = cell[0] / kBrick, byk = cell[1] / kBrick, bzk = cell[2] / kBrick;
-    const uint32_t b = (uint32_t)bxk + (uint32_t)c.nb[0] * ((uint32_t)byk + (uint32_t)c.nb[1] * (uint32_t)bzk);
-    if (__ldg(occ + (b >> 5)) & (1u << (b & 31))) return 0;
-    box_lo[0] = (float)(kBrick * bxk - 1);
-    box_lo[1] = (float)(kBrick * byk - 1);
-    box_lo[2] = (float)(kBrick * bzk - 1);
-    box_hi[0] = box_lo[0] + (float)kBrick;
-    box_hi[1] = box_lo[1] + (float)kBrick;
-    box_hi[2] = box_lo[2] + (float)kBrick;
-    return 1;
-}
-
-// Whole steps that stay inside the empty brick [lo, hi) from u along du
-// (per unit t), keeping kSkipMargin texels from its faces.
-__device__ __forceinline__ float steps_inside(const float u[3], const float du[3], const float lo[3], const float hi[3],
-                                              float step)
-{
-    float te = INFINITY;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        if (du[k] > 0.0f) te = fminf(te, (hi[k] - kSkipMargin - u[k]) / du[k]);
-        else if (du[k] < 0.0f) te = fminf(te, (lo[k] + kSkipMargin - u[k]) / du[k]);
-    }
-    return floorf(te / step);
-}
-
-__device__ __forceinline__ void texel_coords(const RayConsts& c, Vec3 p, float u[3])
-{
-    u[0] = fmaf(p.x, c.tsc[0], c.tbias[0]);
-    u[1] = fmaf(p.y, c.tsc[1], c.tbias[1]);
-    u[2] = fmaf(p.z, c.tsc[2], c.tbias[2]);
-}
-
-// The fragment of pixel (px, py) of the c.W x c.H view: colour + coverage
-// and depth.  depth_at points at the pixel's depth-buffer value (NULL: 1.0).
-template <int DF, int TF>
-__device__ __forceinline__ void march_pixel(const RayConsts& c, const typename DensityTexel<DF>::T* __restrict__ dens,
-                                            const void* __restrict__ tang, const uint32_t* __restrict__ occ,
-                                            const float* depth_at, int px, int py, float4& out, float& out_depth)
-{
-    // ---- proxy cube: entry point of the pixel-centre ray ---------------------
-    const float nx = 2.0f * ((float)px + 0.5f) / (float)c.W - 1.0f;
-    const float ny = 2.0f * ((float)py + 0.5f) / (float)c.H - 1.0f;
-    float f[4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) f[r] = c.inv_vp[r] * nx + c.inv_vp[4 + r] * ny + c.inv_vp[8 + r] + c.inv_vp[12 + r];
-    const float dir[3] = {f[0] / f[3] - c.cam[0], f[1] / f[3] - c.cam[1], f[2] / f[3] - c.cam[2]};
-    float tmin = -INFINITY, tmax = INFINITY;
-    bool hit = true;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        if (dir[k] == 0.0f) {
-            if (c.cam[k] < c.lo[k] || c.cam[k] > c.hi[k]) hit = false;
-            continue;
-        }
-        float t0 = (c.lo[k] - c.cam[k]) / dir[k], t1 = (c.hi[k] - c.cam[k]) / dir[k];
-        tmin = fmaxf(tmin, fminf(t0, t1));
-        tmax = fminf(tmax, fmaxf(t0, t1));
-    }
-    out = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    out_depth = 1.0f;
-    if (hit && tmin > 0.0f && tmin <= tmax) {
-        const Vec3 cam = v3(c.cam[0], c.cam[1], c.cam[2]);
-        const Vec3 start = v3(fmaf(tmin, dir[0], c.cam[0]), fmaf(tmin, dir[1], c.cam[1]), fmaf(tmin, dir[2], c.cam[2]));
-        const Vec3 end = start + normalize(start - cam) * c.radius;
-        const float db = depth_at ? *depth_at : 1.0f;
-        const bool depth_test = !(clip_depth(c, end) < db);
-
-        // ---- volume_surface (volume_rendering.glsl:19-52) --------------------
-        const float step = 1.0f / c.steps;
-        const bool jump = c.steps_pow2 && !depth_test;
-        float us[3], ue[3], du[3];
-        texel_coords(c, start, us);
-        texel_coords(c, end, ue);
-        du[0] = ue[0] - us[0];
-        du[1] = ue[1] - us[1];
-        du[2] = ue[2] - us[2];
-        float acc = 0.0f;
-        Vec3 surf = v3(0.0f, 0.0f, 0.0f), entry = v3(0.0f, 0.0f, 0.0f);
-        bool found = false, entered = false;
-        for (float t = 0.0f; t < 1.0f;) {
-            const Vec3 P = mix(start, end, t);
-            if (depth_test && db < clip_depth(c, P)) break;
-            float u[3], lo[3], hi[3];
-            texel_coords(c, P, u);
-            const int z = classify(c, occ, u, du, lo, hi);
-            if (z == 2) break; // left the grid: every later sample adds exactly 0
-            if (z == 1) {      // exactly 0: acc and the decisions are unchanged
-                const float n = jump ? steps_inside(u, du, lo, hi, step) : 0.0f;
-                t = n >= 1.0f ? fmaf(n, step, t) : t + step;
-                continue;
-            }
-            const float rho = sample_density<DF>(c, dens, P);
-            acc += rho;
-            if (rho != 0.0f) {
-                if (acc <= c.iso) surf = P;
-                if (acc >= c.iso) found = true;
-                if (!entered) { entry = P; entered = true; }
-                if (acc > c.iso && c.lod * (acc / c.iso) * c.alpha >= 1.0f) break; // outputs final
-            }
-            t += step;
-        }
-        if (!found && entered) surf = entry;
-        const float a = acc / c.iso;
-        if (a != 0.0f) {
-            const float coverage = c.lod * a * c.alpha;
-            // ---- shading (volume.frag:50-67, kajiya-kay.glsl:7-24) ------------
-            Vec3 shading = v3(1.0f, 1.0f, 1.0f);
-            const Vec3 light = v3(c.light[0], c.light[1], c.light[2]);
-            if (c.shading_model == VKHR_SHADING_KAJIYA_KAY) {
-                const Vec3 L = normalize(light - surf);
-                const Vec3 E = normalize(surf - cam);
-                const Vec3 T = normalize(sample_tangent<TF>(c, tang, surf));
-                const float cosTL = dot(T, L), cosTE = dot(T, E);
-                const float sinTL = sqrtf(fmaxf(1.0f - cosTL * cosTL, 0.0f));
-                const float sinTE = sqrtf(fmaxf(1.0f - cosTE * cosTE, 0.0f));
-                const float spec = powf(fmaxf(cosTL * cosTE + sinTL * sinTE, 0.0f), c.exponent);
-                const float dk = c.kd * sinTL;
-                shading = v3(c.color[0] * dk + c.intensity[0] * spec, c.color[1] * dk + c.intensity[1] * spec,
-                             c.color[2] * dk + c.intensity[2] * spec);
-            }
-            float occlusion = 1.0f;
-            // ---- volume_approximated_deep_shadows (approximate_deep_shadows.glsl:24-36)
-            if (c.deep_shadows_on == 1 && c.shading_model != VKHR_SHADING_LAO) {
-                const float sstep = 1.0f / c.shadow_steps;
-                float ls[3], le[3], dl[3];
-                texel_coords(c, surf, ls);
-                texel_coords(c, light, le);
-                dl[0] = le[0] - ls[0];
-                dl[1] = le[1] - ls[1];
-                dl[2] = le[2] - ls[2];
-                float strands = 0.0f;
-                for (float t = 0.0f; t < 1.0f;) {
-                    const Vec3 Q = mix(surf, light, t);
-                    float u[3], lo[3], hi[3];
-                    texel_coords(c, Q, u);
-                    const int z = classify(c, occ, u, dl, lo, hi);
-                    if (z == 2) break;
-                    if (z == 1) {
-                        const float n = c.shadow_pow2 ? steps_inside(u, dl, lo, hi, sstep) : 0.0f;
-                        t = n >= 1.0f ? fmaf(n, sstep, t) : t + sstep;
-                        continue;
-                    }
-                    strands += sample_density<DF>(c, dens, Q) * c.thickness;
-                    t += sstep;
-                }
-                occlusion *= powf(1.0f - c.alpha, strands);
-            }
-            // ---- local_ambient_occlusion (local_ambient_occlusion.glsl:9-30)
-            if (c.shading_model != VKHR_SHADING_ADSM) {
-                const float kr = (c.ao_kernel - 1.0f) / 2.0f;
-                const float scale = c.ao_radius / kr;
-                const Vec3 sc = v3(c.voxel_space[0] * scale, c.voxel_space[1] * scale, c.voxel_space[2] * scale);
-                float dsum = 0.0f;
-                for (float z = -kr; z <= kr; z += 1.0f)
-                    for (float y = -kr; y <= kr; y += 1.0f)
-                        for (float x = -kr; x <= kr; x += 1.0f) {
-                            const Vec3 q = v3(surf.x + x * sc.x, surf.y + y * sc.y, surf.z + z * sc.z);
-                            dsum += fminf(sample_density<DF>(c, dens, q), c.ao_max);
-                        }
-                occlusion *= powf(1.0f - dsum / (c.ao_kernel * c.ao_kernel * c.ao_kernel), c.ao_exp);
-            }
-            // packUnorm4x8 clamp (ppll.glsl:32); NaN -> 0
-            out = make_float4(__saturatef(shading.x * occlusion), __saturatef(shading.y * occlusion),
-                              __saturatef(shading.z * occlusion), __saturatef(coverage));
-            out_depth = clip_depth(c, surf);
-        }
-    }
-}
 
 template <int DF, int TF>
 __global__ void __launch_bounds__(32 * kWarpsX * kWarpsY)
@@ -592,110 +130,6 @@ raymarch_batched_kernel(const RayJob* __restrict__ jobs, int nj, uint32_t total_
             if (sj.depth_out) sj.depth_out[at] = out_depth;
         }
     }
-}
-
-bool invert4(const double m[16], double inv[16])
-{
-    double a[4][8];
-    for (int r = 0; r < 4; ++r)
-        for (int k = 0; k < 4; ++k) {
-            a[r][k] = m[k * 4 + r];
-            a[r][k + 4] = r == k ? 1.0 : 0.0;
-        }
-    for (int k = 0; k < 4; ++k) {
-        int piv = k;
-        for (int r = k + 1; r < 4; ++r)
-            if (std::fabs(a[r][k]) > std::fabs(a[piv][k])) piv = r;
-        if (a[piv][k] == 0.0) return false;
-        if (piv != k)
-            for (int j = 0; j < 8; ++j) std::swap(a[k][j], a[piv][j]);
-        const double d = a[k][k];
-        for (int j = 0; j < 8; ++j) a[k][j] /= d;
-        for (int r = 0; r < 4; ++r)
-            if (r != k) {
-                const double f = a[r][k];
-                for (int j = 0; j < 8; ++j) a[r][j] -= f * a[k][j];
-            }
-    }
-    for (int r = 0; r < 4; ++r)
-        for (int k = 0; k < 4; ++k) inv[k * 4 + r] = a[r][k + 4];
-    return true;
-}
-
-vkhr_status make_consts(vkhr_ctx* ctx, const vkhr_raymarch_params* p, RayConsts& c)
-{
-    if (p->width <= 0 || p->height <= 0) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "width/height must be > 0");
-    if (!(p->raycast_steps > 0.0f) || !(p->raycast_steps <= kMaxSteps))
-        return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "raycast_steps must be in (0, 2^20]");
-    const float sst = p->shadow_steps > 0.0f ? p->shadow_steps : p->raycast_steps;
-    if (!(sst <= kMaxSteps)) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "shadow_steps must be <= 2^20");
-    if (!(p->ao_kernel_size >= 2.0f && p->ao_kernel_size <= 16.0f))
-        return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "ao_kernel_size must be in [2, 16]");
-    if (!(p->isosurface > 0.0f)) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "isosurface must be > 0");
-    if (p->density_format < 0 || p->density_format > 2 || p->tangent_format < 0 || p->tangent_format > 1)
-        return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "unknown texel format");
-    for (int k = 0; k < 3; ++k) {
-        if (p->volume_resolution[k] <= 0) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "volume_resolution must be > 0");
-        if (!(p->volume_bounds.size[k] > 0.0f) || !std::isfinite(p->volume_bounds.size[k]))
-            return vkhr_fail(ctx, VKHR_ERR_DEGENERATE_AABB, "every AABB extent must be finite and > 0");
-    }
-    c.W = p->width;
-    c.H = p->height;
-    double pv[16], inv[16];
-    for (int col = 0; col < 4; ++col)
-        for (int r = 0; r < 4; ++r) {
-            double s = 0.0;
-            for (int k = 0; k < 4; ++k) s += (double)p->projection[k * 4 + r] * (double)p->view[col * 4 + k];
-            pv[col * 4 + r] = s;
-        }
-    if (!invert4(pv, inv)) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "projection * view is singular");
-    for (int i = 0; i < 16; ++i) {
-        c.pv[i] = (float)pv[i];
-        c.inv_vp[i] = (float)inv[i];
-    }
-    for (int k = 0; k < 3; ++k) {
-        c.cam[k] = p->camera_position[k];
-        c.lo[k] = p->volume_bounds.origin[k];
-        c.hi[k] = p->volume_bounds.origin[k] + p->volume_bounds.size[k];
-        c.res[k] = p->volume_resolution[k];
-        const double s = (double)p->volume_resolution[k] / (double)p->volume_bounds.size[k];
-        c.tsc[k] = (float)s;
-        c.tbias[k] = (float)(-(double)p->volume_bounds.origin[k] * s - 0.5);
-        c.voxel_space[k] = p->volume_bounds.size[k] / (float)p->volume_resolution[k];
-        c.light[k] = p->light_origin[k];
-        c.intensity[k] = p->light_intensity[k];
-        c.color[k] = p->hair_color[k];
-    }
-    c.radius = p->volume_bounds.radius;
-    c.alpha = p->hair_alpha;
-    c.exponent = p->hair_exponent;
-    c.iso = p->isosurface;
-    c.kd = p->kd;
-    c.steps = p->raycast_steps;
-    c.shadow_steps = sst;
-    c.thickness = p->shadow_thickness;
-    c.ao_kernel = p->ao_kernel_size;
-    c.ao_radius = p->occlusion_radius;
-    c.ao_exp = p->ao_exponent;
-    c.ao_max = p->ao_max;
-    // lod() of scheme.glsl:7-11 for the camera's look-at distance
-    if (p->renderer == VKHR_RENDERER_RASTERIZER) c.lod = 0.0f;
-    else if (p->renderer == VKHR_RENDERER_RAYMARCHER) c.lod = 1.0f;
-    else {
-        float t = (p->look_at_distance - p->magnified_distance) / (p->minified_distance - p->magnified_distance);
-        t = std::min(std::max(t, 0.0f), 1.0f);
-        c.lod = t * t * (3.0f - 2.0f * t);
-    }
-    c.shading_model = p->shading_model;
-    c.deep_shadows_on = p->deep_shadows_on;
-    auto pow2 = [](float x) {
-        int e;
-        return std::frexp(x, &e) == 0.5f;
-    };
-    c.steps_pow2 = pow2(c.steps) ? 1 : 0;
-    c.shadow_pow2 = pow2(c.shadow_steps) ? 1 : 0;
-    for (int k = 0; k < 3; ++k) c.nb[k] = (c.res[k] + kBrick) / kBrick;
-    return VKHR_OK;
 }
 
 template <int DF, int TF>
