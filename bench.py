@@ -432,6 +432,91 @@ def scale_section(args, dev, stream, flush):
     return out
 
 
+DIFF = {
+    "workload": "differentiable view: the 136,320 x 13 style (1,772,160 vertices) trilinearly splatted into an FP32 "
+                "256^3 density, FP32 tangents, 960x540 with 512 steps, 64-step shadows, 8-tap AO; L2 loss against a "
+                "target from log-normally perturbed densities (sigma 0.2) with exponent 60; gradients with respect "
+                "to density, tangents, kd, the exponent and (through the splat) the vertices",
+}
+
+
+def diff_section(args, dev, stream, flush):
+    """Forward vs adjoint cost of the differentiable path (median device ms)."""
+    import torch
+
+    from vkhr_gb300 import _abi, _native, scene
+
+    s = stream.cuda_stream
+    ctx = _native.Context(dev.index)
+    st, t, idx = make_style()
+    res = (256, 256, 256)
+    n = 256 ** 3
+    V = torch.from_numpy(st.vertices).to(dev)
+    b = ctx.bounding_box(V.data_ptr(), st.vertex_count, s)
+    dens = torch.zeros(n, dtype=torch.float32, device=dev)
+    ctx.splat_vertices(V.data_ptr(), st.vertex_count, b, res, dens.data_ptr(), s)
+    counts = torch.empty(n, dtype=torch.int32, device=dev)
+    tq = torch.empty((n, 4), dtype=torch.int8, device=dev)
+    dt = torch.from_numpy(t).to(dev)
+    di = torch.from_numpy(idx.view(np.int32)).to(dev)
+    ctx.voxelize_segments(V.data_ptr(), dt.data_ptr(), di.data_ptr(), idx.shape[0], b, res, _abi.INDEX_REF_FP32,
+                          counts.data_ptr(), None, tq.data_ptr(), s)
+    tan = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+    tan[:, :3] = torch.clamp(tq[:, :3].float() / 127.0, min=-1.0)
+    kw = dict(camera_distance=4.0, raycast_steps=512.0, shadow_steps=64.0, isosurface=1.0, kd=0.4,
+              density_format=_abi.DENSITY_F32, tangent_format=_abi.TANGENT_F32X4)
+    p = scene.make_params(b, res, 960, 540, hair_exponent=80.0, **kw)
+    pt = scene.make_params(b, res, 960, 540, hair_exponent=60.0, **kw)
+    gen = torch.Generator(device=dev).manual_seed(3)
+    noisy = dens * torch.exp(0.2 * torch.randn(n, generator=gen, device=dev))
+    target = torch.empty((540, 960, 4), dtype=torch.float32, device=dev)
+    ctx.raymarch(pt, noisy.data_ptr(), tan.data_ptr(), None, target.data_ptr(), None, s)
+    rgba = torch.empty_like(target)
+    out = {"config": DIFF, "ms": {}}
+    for K in (16, 32, 64):
+        nbytes = ctx.tape_bytes(p, K)
+        tape = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        g_rgba = torch.empty_like(target)
+        gd = torch.empty_like(dens)
+        gt = torch.empty_like(tan)
+        gp = torch.empty(2, dtype=torch.float64, device=dev)
+        gv = torch.empty_like(V)
+
+        def adjoint_pass():
+            torch.mul(rgba - target, 2.0, out=g_rgba)  # dL/drgba of the L2 loss
+            gd.zero_()
+            gt.zero_()
+            gp.zero_()
+            ctx.raymarch_adjoint(p, dens.data_ptr(), tan.data_ptr(), tape.data_ptr(), K, g_rgba.data_ptr(),
+                                 gd.data_ptr(), gt.data_ptr(), gp.data_ptr(), s)
+            ctx.splat_vertices_adjoint(V.data_ptr(), st.vertex_count, b, res, gd.data_ptr(), gv.data_ptr(), s)
+
+        stages = {
+            "forward": lambda: ctx.raymarch(p, dens.data_ptr(), tan.data_ptr(), None, rgba.data_ptr(), None, s),
+            "forward_train": lambda: ctx.raymarch_train(p, dens.data_ptr(), tan.data_ptr(), rgba.data_ptr(), None,
+                                                        tape.data_ptr(), nbytes, K, s),
+            "adjoint": adjoint_pass,
+        }
+        times = {k: [] for k in stages}
+        for k in range(max(args.warmup, 3) + args.steps):
+            for name, f in stages.items():
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                f()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                if k >= max(args.warmup, 3):
+                    times[name].append(e0.elapsed_time(e1))
+        ms = {k: statistics.median(v) for k, v in times.items()}
+        out["ms"]["K=%d" % K] = ms
+        out["adjoint_over_forward_K%d" % K] = ms["adjoint"] / ms["forward"]
+        out["train_plus_adjoint_over_forward_K%d" % K] = (ms["forward_train"] + ms["adjoint"]) / ms["forward"]
+        out["tape_bytes_K%d" % K] = nbytes
+    ctx.close()
+    return out
+
+
 def gb300_arm(args):
     import torch
 
@@ -449,6 +534,11 @@ def gb300_arm(args):
         flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
         if rank == 0:
             print(json.dumps({"section": "scale", "scale": scale_section(args, dev, stream, flush)}))
+        return 0
+    if args.section == "diff":  # the differentiable workload alone (profiling runs)
+        flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+        if rank == 0:
+            print(json.dumps({"section": "diff", "diff": diff_section(args, dev, stream, flush)}))
         return 0
     if args.section == "batched":  # the multi-style comparison alone (profiling runs)
         flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
@@ -593,6 +683,7 @@ def gb300_arm(args):
     batched = None if (args.no_batched or args.section == "frame") else batched_comparison(
         args, dev, stream, rank, world, flush)
     scale = None if (args.no_scale or args.section == "frame" or world > 1) else scale_section(args, dev, stream, flush)
+    diff = None if (args.no_diff or args.section == "frame" or world > 1) else diff_section(args, dev, stream, flush)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -616,6 +707,8 @@ def gb300_arm(args):
         line["batched"] = batched
     if scale is not None:
         line["scale"] = scale
+    if diff is not None:
+        line["diff"] = diff
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import oracle as O
 
@@ -645,9 +738,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 16-style batched vs plain comparison")
     ap.add_argument("--no-scale", action="store_true", help="skip the 512^3 scale workload")
-    ap.add_argument("--section", default="all", choices=["all", "frame", "batched", "scale"],
+    ap.add_argument("--no-diff", action="store_true", help="skip the differentiable workload")
+    ap.add_argument("--section", default="all", choices=["all", "frame", "batched", "scale", "diff"],
                     help="frame: the production frame only; batched: the multi-style comparison only; "
-                         "scale: the 512^3 workload only")
+                         "scale: the 512^3 workload only; diff: the differentiable workload only")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)

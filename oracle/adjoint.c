@@ -202,7 +202,8 @@ static double diff_pixel(const vkhr_raymarch_params* p, const vol_ad* dv, const 
 }
 
 double oracle_diff_loss(const vkhr_raymarch_params* p, const double* density, const double* tangent,
-                        const float* target, double* g_density, double* g_tangent, double* g_params, int threads)
+                        const float* target, const uint8_t* mask, double* g_density, double* g_tangent,
+                        double* g_params, int threads)
 {
     vol_ad dv, tv;
     dv.data = density;
@@ -223,6 +224,7 @@ double oracle_diff_loss(const vkhr_raymarch_params* p, const double* density, co
     for (int y = 0; y < H; ++y)
         for (int x = 0; x < W; ++x) {
             const size_t at = (size_t)y * W + x;
+            if (mask && !mask[at]) continue; /* excluded from the loss */
             double st[3];
             if (!oracle_pixel_entry_inv(p, inv, x, y, st)) {
                 for (int c = 0; c < 4; ++c) loss += (double)target[4 * at + c] * (double)target[4 * at + c];

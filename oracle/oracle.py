@@ -56,7 +56,7 @@ def lib():
         _lib.oracle_segment_visits.restype = C.c_uint32
         _lib.oracle_normalize.argtypes = [P, C.c_uint64]
         _lib.oracle_downsample.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, P]
-        _lib.oracle_diff_loss.argtypes = [C.POINTER(_abi.RaymarchParams), P, P, P, P, P, P, C.c_int]
+        _lib.oracle_diff_loss.argtypes = [C.POINTER(_abi.RaymarchParams), P, P, P, P, P, P, P, C.c_int]
         _lib.oracle_diff_loss.restype = C.c_double
         _lib.oracle_splat.argtypes = [P, C.c_uint32, C.POINTER(_abi.AABB), C.c_int, C.c_int, C.c_int, P]
         _lib.oracle_splat_adjoint.argtypes = [P, C.c_uint32, C.POINTER(_abi.AABB), C.c_int, C.c_int, C.c_int, P, P]
@@ -182,19 +182,21 @@ def raymarch(params, density, tangent, depth_in=None, precision="f64", rows=None
 
 # ---- differentiable path (FP64) ------------------------------------------------
 
-def diff_loss(params, density, tangent, target, grads=False, threads=0):
-    """Loss sum((rgba - target)^2) of the FP64 differentiable raymarch; with
-    grads=True also (g_density, g_tangent (n, 4), g_params [kd, exponent]).
-    density (n,) and tangent (n, 4) are converted to float64."""
+def diff_loss(params, density, tangent, target, grads=False, threads=0, mask=None):
+    """Loss sum((rgba - target)^2) of the FP64 differentiable raymarch over
+    the pixels where mask (H, W) is true (None: all); with grads=True also
+    (g_density, g_tangent (n, 4), g_params [kd, exponent]).  density (n,)
+    and tangent (n, 4) are converted to float64."""
     d = np.ascontiguousarray(density, dtype=np.float64).reshape(-1)
     t = np.ascontiguousarray(tangent, dtype=np.float64).reshape(-1, 4)
     tg = _f32(target)
+    m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
     if not grads:
-        return float(lib().oracle_diff_loss(C.byref(params), _p(d), _p(t), _p(tg), None, None, None, threads))
+        return float(lib().oracle_diff_loss(C.byref(params), _p(d), _p(t), _p(tg), _p(m), None, None, None, threads))
     gd = np.zeros_like(d)
     gt = np.zeros_like(t)
     gp = np.zeros(2, dtype=np.float64)
-    loss = lib().oracle_diff_loss(C.byref(params), _p(d), _p(t), _p(tg), _p(gd), _p(gt), _p(gp), threads)
+    loss = lib().oracle_diff_loss(C.byref(params), _p(d), _p(t), _p(tg), _p(m), _p(gd), _p(gt), _p(gp), threads)
     return float(loss), gd, gt, gp
 
 

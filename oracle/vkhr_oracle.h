@@ -59,11 +59,13 @@ void oracle_downsample(const uint8_t* in, int w, int h, int d, int filter, uint8
 #define ORACLE_F64 100
 
 /* The differentiable raymarch in FP64 (adjoint.c): the loss
- * sum((rgba - target)^2) with rgba kept in double, and its analytic
- * gradient (accumulated into g_density, g_tangent (4 per voxel), g_params
+ * sum((rgba - target)^2) with rgba kept in double, over the pixels whose
+ * mask byte is nonzero (mask NULL: all), and its analytic gradient
+ * (accumulated into g_density, g_tangent (4 per voxel), g_params
  * [kd, hair_exponent]; any may be NULL).  density / tangent in ORACLE_F64. */
 double oracle_diff_loss(const vkhr_raymarch_params* p, const double* density, const double* tangent,
-                        const float* target, double* g_density, double* g_tangent, double* g_params, int threads);
+                        const float* target, const uint8_t* mask, double* g_density, double* g_tangent,
+                        double* g_params, int threads);
 /* Trilinear splat of vertices in FP64 (accumulated into density) and its adjoint. */
 void oracle_splat(const float* vertices, uint32_t n, const vkhr_aabb* b, int w, int h, int d, double* density);
 void oracle_splat_adjoint(const float* vertices, uint32_t n, const vkhr_aabb* b, int w, int h, int d,
