@@ -50,8 +50,14 @@ WORKLOAD = {
     "l2": "flushed before every timed step (512 MiB write)",
 }
 # DRAM bytes (read + write) per launch from one ncu capture of the production
-# frame (profiles/*_production_frame.md); None until captured for this build.
-TRAFFIC = {}
+# frame (profiles/voxelizer_kernels_production_frame.md and
+# profiles/raymarch_kernel_production_frame.md), by kernel family.
+TRAFFIC = {
+    "brick_kernel<SEG, TANG, false": 155_667_968 + 37_609_728,
+    "bin_kernel<true": 55_134_208 + 72_237_312,
+    "bin_kernel<false": 55_694_080 + 24_500_992,
+    "raymarch_kernel": 8_216_576 + 51_968,
+}
 
 METRIC = "Msegments/s voxelized + Mpixels/s raymarched, 1 GB300 (frame throughput in Mpixels/s)"
 UNIT = "Mpixels/s"
@@ -577,6 +583,8 @@ def gb300_arm(args):
         voxelize()
         raymarch()
     torch.cuda.synchronize()
+    # the ray-packet variant for this view (vkhr_autotune_raymarch), kept in the context
+    tuned, tuned_ms = ctx.autotune_raymarch(p, dens.data_ptr(), tq.data_ptr(), rgba.data_ptr(), s)
 
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
            torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
@@ -629,19 +637,27 @@ def gb300_arm(args):
     visits = int(counts.sum(dtype=torch.int64).item())
     R = WORKLOAD["resolution"]
     occupied = int(counts.view(R // 8, 8, R // 8, 8, R // 8, 8).amax(dim=(1, 3, 5)).gt(0).sum().item())
-    alg = {
-        # visit entries (8 B) + the pair tangents once (16 B) + counts, u8 and i8x4 of the occupied bricks
-        "(brick_kernel<SEG, TANG>)": 8 * visits + 16 * S + 9 * 512 * occupied,
-        # index pairs + both vertices of each pair once + the visit entries written
-        "(bin_kernel<true, true>)": 8 * S + 24 * V + 8 * visits,
-        "(bin_kernel<false, true>)": 8 * S + 24 * V + 32 * S,
-        # u8 densities + i8x4 tangents once + the RGBA and depth outputs
-        "(raymarch_kernel<DF, TF>)": n * 1 + n * 4 + px * 20,
-    }
-    alg_bytes = alg.get(top_name)
+    def alg_bytes_of(name):
+        """Algorithmic bytes per launch of a kernel of the frame, by kernel family."""
+        if "brick_kernel" in name and "false" in name:
+            # 4-byte visit entries + the pair tangents once + counts, u8 and i8x4 of the occupied bricks
+            return 4 * visits + 16 * S + 9 * 512 * occupied
+        if name.startswith("(bin_kernel<true"):
+            # index pairs + both vertices of each pair once + the 4-byte visit entries written
+            return 8 * S + 24 * V + 4 * visits
+        if name.startswith("(bin_kernel<false"):
+            # index pairs + vertices once + the pair records and tangents written
+            return 8 * S + 24 * V + 48 * S
+        if "raymarch_kernel" in name:
+            # u8 densities + i8x4 tangents once + the RGBA and depth outputs
+            return n * 1 + n * 4 + px * 20
+        return None
+
+    alg_bytes = alg_bytes_of(top_name)
     achieved = (alg_bytes / (top_avg_ms / 1e3) / 1e9) if alg_bytes else None
     roofline = {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": (achieved / hbm) if achieved else None, "traffic": TRAFFIC.get(top_name),
+                "frac": (achieved / hbm) if achieved else None,
+                "traffic": next((v for k, v in TRAFFIC.items() if k in top_name), None),
                 "peak_kind": peak_kind, "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": top_avg_ms,
                 "visits": visits, "occupied_bricks": occupied}
     # whole stages against the same peak: inputs once + outputs once
@@ -702,6 +718,8 @@ def gb300_arm(args):
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "clocks": clocks.summary(),
+        "autotune": {"raymarch_variant": tuned, "variant_ms": tuned_ms,
+                     "variants": ["8x4 tiles", "16x2 tiles", "4x8 tiles", "8x4 tiles, 64 registers"]},
     }
     if batched is not None:
         line["batched"] = batched

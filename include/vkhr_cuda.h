@@ -298,6 +298,24 @@ vkhr_status vkhr_raymarch(vkhr_ctx* ctx, const vkhr_raymarch_params* params,
                           const void* d_density, const void* d_tangent, const float* d_depth_in,
                           float* d_rgba, float* d_depth_out, void* stream);
 
+/* Ray-packet variants of vkhr_raymarch: 0 = 8x4-pixel warp tiles (default),
+ * 1 = 16x2, 2 = 4x8, 3 = 8x4 with 8 resident CTAs per SM (fewer registers).
+ * Every variant computes the same pixels. */
+#define VKHR_RAYMARCH_VARIANTS 4
+
+/* Autotuner (no reference counterpart): times each variant of vkhr_raymarch
+ * on these inputs (one warm-up and three timed runs each, d_rgba receiving
+ * the image) and keeps the fastest in the context for params' texel
+ * formats; later vkhr_raymarch calls with those formats use it.  Writes the
+ * choice to *chosen and, when variant_ms is not NULL, the median time of
+ * each variant (VKHR_RAYMARCH_VARIANTS floats).  Synchronises the stream. */
+vkhr_status vkhr_autotune_raymarch(vkhr_ctx* ctx, const vkhr_raymarch_params* params, const void* d_density,
+                                   const void* d_tangent, float* d_rgba, int32_t* chosen, float* variant_ms,
+                                   void* stream);
+
+/* Selects a variant for a pair of texel formats without timing. */
+vkhr_status vkhr_set_raymarch_variant(vkhr_ctx* ctx, int32_t density_format, int32_t tangent_format, int32_t variant);
+
 /* One view of a batched raymarch: its parameters (width x height is the whole
  * view the camera projects to), its volume, and the region [x0, x0 + w) x
  * [y0, y0 + h) of the view to render.  Outputs use the region's layout: pixel

@@ -30,6 +30,8 @@ STATUS_NAMES = {
 INDEX_REF_FP32 = 0
 INDEX_EXACT = 1
 
+RAYMARCH_VARIANTS = 4
+
 FILTER_MAX = 0
 FILTER_MIN = 1
 FILTER_MEAN = 2

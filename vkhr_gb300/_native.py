@@ -20,7 +20,7 @@ EXPORTS = [
     "vkhr_voxelize_batched", "vkhr_set_visit_budget", "vkhr_sizeof_voxel_job",
     "vkhr_raymarch_batched", "vkhr_raymarch_footprint", "vkhr_sizeof_raymarch_job",
     "vkhr_downsample_densities", "vkhr_raymarch_tape_bytes", "vkhr_raymarch_train", "vkhr_raymarch_adjoint",
-    "vkhr_splat_vertices", "vkhr_splat_vertices_adjoint",
+    "vkhr_splat_vertices", "vkhr_splat_vertices_adjoint", "vkhr_autotune_raymarch", "vkhr_set_raymarch_variant",
 ]
 
 _lib = None
@@ -62,6 +62,9 @@ def load():
     lib.vkhr_raymarch_footprint.argtypes = [C.POINTER(_abi.RaymarchParams), C.POINTER(C.c_int32)]
     lib.vkhr_normalize_densities.argtypes = [P, P, C.c_uint64, P]
     lib.vkhr_downsample_densities.argtypes = [P, P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P, P]
+    lib.vkhr_autotune_raymarch.argtypes = [P, C.POINTER(_abi.RaymarchParams), P, P, P, C.POINTER(C.c_int32),
+                                           C.POINTER(C.c_float), P]
+    lib.vkhr_set_raymarch_variant.argtypes = [P, C.c_int32, C.c_int32, C.c_int32]
     lib.vkhr_raymarch_tape_bytes.argtypes = [C.POINTER(_abi.RaymarchParams), C.c_int32]
     lib.vkhr_raymarch_tape_bytes.restype = C.c_size_t
     lib.vkhr_raymarch_train.argtypes = [P, C.POINTER(_abi.RaymarchParams), P, P, P, P, P, C.c_size_t, C.c_int32, P]
@@ -186,6 +189,17 @@ class Context:
     def downsample_densities(self, d_in, res, filt, d_out, stream=None):
         w, h, d = res
         self.check(self.lib.vkhr_downsample_densities(self.handle, d_in, w, h, d, filt, d_out, stream))
+
+    def autotune_raymarch(self, params, d_density, d_tangent, d_rgba, stream=None):
+        """(chosen variant, [median ms of each variant])."""
+        chosen = C.c_int32(-1)
+        ms = (C.c_float * 4)()
+        self.check(self.lib.vkhr_autotune_raymarch(self.handle, C.byref(params), d_density, d_tangent, d_rgba,
+                                                   C.byref(chosen), ms, stream))
+        return int(chosen.value), [float(x) for x in ms]
+
+    def set_raymarch_variant(self, density_format, tangent_format, variant):
+        self.check(self.lib.vkhr_set_raymarch_variant(self.handle, density_format, tangent_format, variant))
 
     # differentiable path
     def tape_bytes(self, params, checkpoint_interval):

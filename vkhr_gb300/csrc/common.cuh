@@ -66,6 +66,7 @@ struct vkhr_ctx {
     size_t rjobs_cap;          // in bytes
     void* h_rjobs;             // pinned staging of the raymarch job table
     cudaEvent_t rjobs_ev;      // recorded after the staging was copied out
+    int ray_variant[3][2];     // raymarch packet variant per (density format, tangent format)
     float* g_acc;              // adjoint: per-pixel gradient of the accumulated density
     size_t g_acc_cap;
     uint32_t* occ;             // raymarch brick-occupancy bitmap

@@ -21,15 +21,26 @@
 
 namespace {
 
-template <int DF, int TF>
-__global__ void __launch_bounds__(32 * kWarpsX * kWarpsY)
+// Ray packets: a warp marches a TW x (32 / TW) pixel tile, and MINB
+// resident CTAs per SM are asked for (6: at most 85 registers per thread,
+// 8: at most 64).  The
+// variants compute the same pixels; the autotuner picks one per context
+// and texel format.
+struct RayVariant {
+    int tw, minb;
+};
+constexpr RayVariant kRayVariants[VKHR_RAYMARCH_VARIANTS] = {{8, 6}, {16, 6}, {4, 6}, {8, 8}};
+
+template <int DF, int TF, int TW = 8, int MINB = 6>
+__global__ void __launch_bounds__(32 * kWarpsX * kWarpsY, MINB)
 raymarch_kernel(const __grid_constant__ RayConsts c, const typename DensityTexel<DF>::T* __restrict__ dens,
                 const void* __restrict__ tang, const uint32_t* __restrict__ occ, const float* __restrict__ depth_in,
                 float4* __restrict__ rgba, float* __restrict__ depth_out)
 {
+    constexpr int TH = 32 / TW;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int px = (blockIdx.x * kWarpsX + (warp % kWarpsX)) * kTileW + (lane % kTileW);
-    const int py = (blockIdx.y * kWarpsY + (warp / kWarpsX)) * kTileH + (lane / kTileW);
+    const int px = (blockIdx.x * kWarpsX + (warp % kWarpsX)) * TW + (lane % TW);
+    const int py = (blockIdx.y * kWarpsY + (warp / kWarpsX)) * TH + (lane / TW);
     if (px >= c.W || py >= c.H) return;
     const size_t at = (size_t)py * c.W + px;
     float4 out;
@@ -143,10 +154,18 @@ vkhr_status launch(vkhr_ctx* ctx, const RayConsts& c, const void* dens, const vo
     VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->occ, 0, words * sizeof(uint32_t), st));
     VKHR_LAUNCH(ctx, occupancy_kernel<DF>, occupancy_blocks(c.res[0], c.res[1], c.res[2], ctx->sm_count), 128, 0, st, (const typename DensityTexel<DF>::T*)dens, c.res[0],
                 c.res[1], c.res[2], c.nb[0], c.nb[1], c.nb[2], ctx->occ);
+    const int v = ctx->ray_variant[DF][TF];
     const dim3 block(32 * kWarpsX * kWarpsY);
-    const dim3 grid((c.W + kTileW * kWarpsX - 1) / (kTileW * kWarpsX), (c.H + kTileH * kWarpsY - 1) / (kTileH * kWarpsY));
-    VKHR_LAUNCH(ctx, (raymarch_kernel<DF, TF>), grid, block, 0, st, c, (const typename DensityTexel<DF>::T*)dens, tang,
-                ctx->occ, din, reinterpret_cast<float4*>(rgba), dout);
+    const int tw = kRayVariants[v].tw, th = 32 / tw;
+    const dim3 grid((c.W + tw * kWarpsX - 1) / (tw * kWarpsX), (c.H + th * kWarpsY - 1) / (th * kWarpsY));
+    const typename DensityTexel<DF>::T* d = (const typename DensityTexel<DF>::T*)dens;
+    float4* out = reinterpret_cast<float4*>(rgba);
+    switch (v) {
+    case 1: VKHR_LAUNCH(ctx, (raymarch_kernel<DF, TF, 16, 6>), grid, block, 0, st, c, d, tang, ctx->occ, din, out, dout); break;
+    case 2: VKHR_LAUNCH(ctx, (raymarch_kernel<DF, TF, 4, 6>), grid, block, 0, st, c, d, tang, ctx->occ, din, out, dout); break;
+    case 3: VKHR_LAUNCH(ctx, (raymarch_kernel<DF, TF, 8, 8>), grid, block, 0, st, c, d, tang, ctx->occ, din, out, dout); break;
+    default: VKHR_LAUNCH(ctx, (raymarch_kernel<DF, TF, 8, 6>), grid, block, 0, st, c, d, tang, ctx->occ, din, out, dout);
+    }
     return VKHR_OK;
 }
 
@@ -182,6 +201,65 @@ extern "C" vkhr_status vkhr_raymarch(vkhr_ctx* ctx, const vkhr_raymarch_params* 
     else
         s = launch<VKHR_DENSITY_F32, VKHR_TANGENT_F32X4>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
     VKHR_CUDA_TRY(ctx, cudaGetLastError());
+    return VKHR_OK;
+}
+
+extern "C" vkhr_status vkhr_set_raymarch_variant(vkhr_ctx* ctx, int32_t density_format, int32_t tangent_format,
+                                                 int32_t variant)
+{
+    if (!ctx) return VKHR_ERR_INVALID_ARG;
+    if (density_format < 0 || density_format > 2 || tangent_format < 0 || tangent_format > 1)
+        return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "unknown texel format");
+    if (variant < 0 || variant >= VKHR_RAYMARCH_VARIANTS) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "unknown variant");
+    ctx->ray_variant[density_format][tangent_format] = variant;
+    return VKHR_OK;
+}
+
+extern "C" vkhr_status vkhr_autotune_raymarch(vkhr_ctx* ctx, const vkhr_raymarch_params* params, const void* d_density,
+                                              const void* d_tangent, float* d_rgba, int32_t* chosen, float* variant_ms,
+                                              void* stream)
+{
+    if (!ctx) return VKHR_ERR_INVALID_ARG;
+    if (!params || !chosen) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "params and chosen are required");
+    const int df = params->density_format, tf = params->tangent_format;
+    if (df < 0 || df > 2 || tf < 0 || tf > 1) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "unknown texel format");
+    VKHR_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaEvent_t e[2];
+    VKHR_CUDA_TRY(ctx, cudaEventCreate(&e[0]));
+    if (cudaEventCreate(&e[1]) != cudaSuccess) {
+        cudaEventDestroy(e[0]);
+        return vkhr_fail(ctx, VKHR_ERR_CUDA, "cudaEventCreate failed");
+    }
+    const int previous = ctx->ray_variant[df][tf];
+    float ms[VKHR_RAYMARCH_VARIANTS];
+    int best = 0;
+    vkhr_status s = VKHR_OK;
+    for (int v = 0; v < VKHR_RAYMARCH_VARIANTS && s == VKHR_OK; ++v) {
+        ctx->ray_variant[df][tf] = v;
+        float t[3] = {0.0f, 0.0f, 0.0f};
+        for (int r = -1; r < 3 && s == VKHR_OK; ++r) { // one warm-up, three timed runs
+            if (cudaEventRecord(e[0], st) != cudaSuccess) s = vkhr_fail(ctx, VKHR_ERR_CUDA, "cudaEventRecord failed");
+            if (s == VKHR_OK) s = vkhr_raymarch(ctx, params, d_density, d_tangent, nullptr, d_rgba, nullptr, stream);
+            if (s == VKHR_OK && (cudaEventRecord(e[1], st) != cudaSuccess || cudaEventSynchronize(e[1]) != cudaSuccess))
+                s = vkhr_fail(ctx, VKHR_ERR_CUDA, "timing the autotune runs failed");
+            if (s == VKHR_OK && r >= 0 && cudaEventElapsedTime(&t[r], e[0], e[1]) != cudaSuccess)
+                s = vkhr_fail(ctx, VKHR_ERR_CUDA, "cudaEventElapsedTime failed");
+        }
+        std::sort(t, t + 3);
+        ms[v] = t[1];
+        if (v > 0 && ms[v] < ms[best]) best = v;
+    }
+    cudaEventDestroy(e[0]);
+    cudaEventDestroy(e[1]);
+    if (s != VKHR_OK) {
+        ctx->ray_variant[df][tf] = previous;
+        return s;
+    }
+    ctx->ray_variant[df][tf] = best;
+    *chosen = best;
+    if (variant_ms)
+        for (int v = 0; v < VKHR_RAYMARCH_VARIANTS; ++v) variant_ms[v] = ms[v];
     return VKHR_OK;
 }
 
