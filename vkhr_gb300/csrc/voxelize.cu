@@ -512,6 +512,38 @@ __device__ __forceinline__ void warp_sort64(uint32_t& a, uint32_t& b)
     }
 }
 
+// Ascending sort of a voxel's c <= N keys at k (shared memory) in registers:
+// a bitonic network (compile-time indices, so every compare-exchange is a
+// min and a max), the slots past c padded with the largest key.  The loads
+// and stores are independent of one another, unlike an insertion sort's
+// chain of dependent shared-memory reads.
+template <int N>
+__device__ __forceinline__ void sort_keys(uint32_t* k, uint32_t c)
+{
+    uint32_t r[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) r[i] = (uint32_t)i < c ? k[i] : 0xffffffffu;
+#pragma unroll
+    for (int s = 2; s <= N; s <<= 1) {
+#pragma unroll
+        for (int j = s >> 1; j > 0; j >>= 1) {
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const uint32_t a = r[i], b = r[l];
+                    const bool up = (i & s) == 0;
+                    r[i] = up ? min(a, b) : max(a, b);
+                    r[l] = up ? max(a, b) : min(a, b);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+        if ((uint32_t)i < c) k[i] = r[i];
+}
+
 template <bool SEG>
 __device__ __forceinline__ float4 visit_tangent(const float4* __restrict__ pair_tan, const float* __restrict__ tan,
                                                 uint32_t key)
@@ -525,7 +557,7 @@ __device__ __forceinline__ float4 visit_tangent(const float4* __restrict__ pair_
 // at `keys` (shared memory, or the global scratch for bricks above
 // kBrickCap): counts and u8 densities, and the tangents.  Each voxel's keys
 // are sorted in place -- up to kBrickThread by the voxel's own thread
-// (insertion sort), up to kBrickSmall by a warp (64-key register bitonic
+// (register sorting network), up to kBrickSmall by a warp (64-key register bitonic
 // sort) -- and then every voxel's thread adds its tangents in key order, all
 // voxels of the brick at once; more than kBrickSmall visits go to
 // crowded_kernel through a descriptor.  Block-wide.
@@ -569,16 +601,14 @@ __device__ __forceinline__ void resolve_brick(const VoxJob& J, const Grid& g, ui
         }
     } else if (inside && c > (uint32_t)kBrickThread) {
         wlist[atomicAdd(&wcount, 1u)] = (uint32_t)tid; // sorted by a warp below
-    } else if (inside) {
-        for (uint32_t i = 1; i < c; ++i) { // insertion sort: serial order
-            const uint32_t key = k[i];
-            uint32_t j = i;
-            while (j > 0 && k[j - 1] > key) {
-                k[j] = k[j - 1];
-                --j;
-            }
-            k[j] = key;
-        }
+    }
+    {   // up to kBrickThread keys: sorted by the voxel's thread in registers, with the
+        // network of the warp's largest such voxel (a voxel outside the grid has none)
+        const uint32_t ct = c <= (uint32_t)kBrickThread ? c : 0u;
+        const uint32_t nmax = __reduce_max_sync(0xffffffffu, ct);
+        if (nmax > 8) sort_keys<16>(k, ct);
+        else if (nmax > 4) sort_keys<8>(k, ct);
+        else if (nmax > 1) sort_keys<4>(k, ct);
     }
     __syncthreads();
     {   // voxels with kBrickThread < count <= kBrickSmall: a warp sorts the keys in place (two per lane)
