@@ -40,6 +40,7 @@ enum {
 struct vkhr_ctx {
     int device;
     int sm_count;
+    int l2_bytes;              // L2 cache size
     // grow-only scratch (capacities in elements)
     uint32_t* brick_runs;      // voxelizer: visits and visit-list cursor per brick (2 x bricks)
     uint32_t* brick_visits;

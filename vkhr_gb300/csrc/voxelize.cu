@@ -11,7 +11,7 @@
 // Brick path (every voxel whose 8^3 brick receives <= kBrickCap visits):
 //   1. bin (count)  one thread per vertex / index pair walks its visits and
 //                   splits them into runs of consecutive visits inside one
-//                   brick; warp-aggregated atomics count visits per brick
+//                   brick; one reduction per run counts visits per brick
 //                   (32K bricks at 256^3, hot in L2).  A pair's set-up (its
 //                   root, direction and step count: nine IEEE divisions) and
 //                   its first vertex's tangent are stored once;
@@ -22,14 +22,16 @@
 //                   writes (serial key, local voxel) entries into it;
 //   4. brick        one CTA per occupied brick reads its entries twice: counts
 //                   per voxel in shared memory, then the keys bucketed per
-//                   voxel; each voxel's keys are sorted in shared memory and
-//                   its tangents summed in that order; the brick's 512
+//                   voxel; each voxel's keys are sorted (up to 16 in the
+//                   voxel's thread's registers by a bitonic network, up to 64
+//                   by a warp) and its tangents summed in that order; the brick's 512
 //                   counts, u8 densities and int8x4 tangents are written once;
-//   5. crowded      voxels with > 64 visits: one CTA each sorts its keys in
-//                   shared-memory tiles (carrying the 256 smallest forward).
-// Global path (only bricks above kBrickCap): per-voxel global atomics, a
-// visit list and the same ordered resolve; it runs before step 4 and only
-// when such a brick exists.
+//   5. crowded      voxels with 65..256 visits: one warp each sorts its keys
+//                   in registers; above 256 visits one CTA each selects the
+//                   256 smallest keys in shared-memory tiles.
+// Bricks above kBrickCap visits take the same brick kernel (a separate
+// launch) with their keys bucketed into a slice of a global scratch instead
+// of shared memory.
 #include "common.cuh"
 
 #include <algorithm>
@@ -272,7 +274,7 @@ __device__ __forceinline__ void emit_run(uint32_t b, uint32_t key, uint64_t loca
 // SINGLE = true: a one-style call; the style comes as the kernel parameter
 // job0 (constant bank, free to read in the visit loop).  Otherwise the job
 // table is copied into shared memory and each item looks its style up.
-template <bool FILL, bool SEG, bool PACK, bool SINGLE>
+template <bool FILL, bool SEG, bool PACK, bool SINGLE, bool SPREAD = false>
 __global__ void bin_kernel(const __grid_constant__ VoxJob job0, const VoxJob* __restrict__ jobs, int nj,
                            uint32_t total_items, float4* pair_rec, float4* pair_tan, uint32_t* visits,
                            uint32_t* cursor, void* entries_raw, size_t entries_cap, unsigned long long* words)
@@ -288,8 +290,20 @@ __global__ void bin_kernel(const __grid_constant__ VoxJob job0, const VoxJob* __
         load_bases(jobs, nj, s_item_base, nullptr);
     }
     unsigned status = 0;
-    for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < total_items;
-         q += (uint64_t)gridDim.x * blockDim.x) {
+    // Fill pass of one style whose visit list is near the L2 size (SPREAD): lane l of
+    // global warp w takes item l * cols + w, so a warp's 32 walks come from
+    // distant strands and its slice reservations spread over many bricks
+    // instead of queueing on one brick's counter.  The scattered entry stores
+    // merge in L2 there; a much larger list would reach DRAM as partial sectors,
+    // so it keeps consecutive items per warp, as do the counting pass
+    // (coalesced index and vertex reads) and a batch (one style per warp).
+    constexpr bool sp = FILL && SINGLE && SEG && SPREAD;
+    const uint64_t cols = (total_items + 31) / 32;
+    const uint64_t span = sp ? cols * 32 : total_items;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < span;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t q = sp ? (i & 31) * cols + (i >> 5) : i;
+        if (q >= total_items) continue;
         const VoxJob& J = SINGLE ? job0 : s_jobs[find_job(s_item_base, nj, (uint32_t)q)];
         const Grid& g = J.g;
         const uint32_t p = (uint32_t)q - J.item_base;
@@ -1271,7 +1285,11 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
     VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_words, 0, WORD_NORM * sizeof(unsigned long long), st));
     VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->brick_visits, 0, (size_t)total_bricks * sizeof(uint32_t), st));
     const unsigned threads = 256;
-    const unsigned in_blocks = std::min(vkhr_blocks(total_items, threads), (unsigned)ctx->sm_count * 16);
+    // one style: one item per thread (blocks retire and start staggered, so
+    // their set-up loads overlap other blocks' walks); a batch caps the grid,
+    // as every block copies the job table into shared memory
+    const unsigned in_blocks = nj == 1 ? vkhr_blocks(total_items, threads)
+                                       : std::min(vkhr_blocks(total_items, threads), (unsigned)ctx->sm_count * 16);
     const size_t bin_smem_bytes = (size_t)nj * (sizeof(VoxJob) + sizeof(uint32_t));
     const bool single = nj == 1;
     if (total_items) {
@@ -1325,9 +1343,18 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
     }
     if (total_items) {
         void* ent = ctx->items;
+        // spread a one-style fill's warps over distant strands when its visit
+        // list is within twice the L2 size: most scattered entry stores still
+        // merge in L2 (measured: a 123 MB list gains, a 1.8 GB list loses)
+        const bool spread = single && segments && (uint64_t)cap_visits * (pack ? sizeof(uint32_t) : sizeof(uint2)) <=
+                                                      2ull * (uint64_t)ctx->l2_bytes;
 #define VKHR_FILL(SEG_, PACK_)                                                                                    \
     do {                                                                                                         \
-        if (single)                                                                                              \
+        if (single && SEG_ && spread)                                                                            \
+            VKHR_LAUNCH(ctx, (bin_kernel<true, SEG_, PACK_, true, true>), in_blocks, threads, 0, st, jobs[0],      \
+                        d_jobs, nj, total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits,                 \
+                        ctx->brick_cursor, ent, cap_visits, ctx->d_words);                                        \
+        else if (single)                                                                                         \
             VKHR_LAUNCH(ctx, (bin_kernel<true, SEG_, PACK_, true>), in_blocks, threads, 0, st, jobs[0], d_jobs, nj,  \
                         total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ent,     \
                         cap_visits, ctx->d_words);                                                                \
