@@ -29,6 +29,36 @@ def test_small_style(ctx, oracle_lib, mode, res):
     assert c.sum() > 0
 
 
+def test_one_walk_slices_and_compact_fallback(native_lib, oracle_lib):
+    """Segment calls without a visit budget: the first call on a context walks
+    twice (count, then fill) and learns a per-brick capacity from its largest
+    brick; later calls walk once, writing each run into its brick's fixed
+    slice (one kernel fewer); a style whose largest brick outgrows the
+    capacity fills again in the compact layout.  Every call is bit-exact."""
+    from vkhr_gb300 import _native
+
+    c = _native.Context(0)
+    try:
+        sparse = style("hemi", 2048, 12)
+        dense = style("disk", 40_000, 13)  # bricks far above the sparse style's largest
+        res = (96, 96, 96)
+
+        def run(s):
+            st, t, idx = s
+            b = oracle_lib.bounding_box(st.vertices)
+            n0 = c.launch_count()
+            _check(c, oracle_lib, "segments", st.vertices, t, idx, b, res)
+            return c.launch_count() - n0
+
+        two_walks = run(sparse)
+        assert run(sparse) == two_walks - 1      # one walk into the learned slices
+        assert run(dense) == two_walks           # a brick past its slice: compact fill
+        assert run(dense) == two_walks - 1       # capacity grown from that call
+        assert run(sparse) == two_walks - 1      # grow-only: still fits
+    finally:
+        c.close()
+
+
 @pytest.mark.parametrize("mode", ["vertices", "segments"])
 def test_production_style_256(ctx, oracle_lib, mode):
     """136,320 strands x 13 vertices (1,635,840 segments) into 256^3, full size."""

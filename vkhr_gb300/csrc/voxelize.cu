@@ -32,6 +32,11 @@
 // Bricks above kBrickCap visits take the same brick kernel (a separate
 // launch) with their keys bucketed into a slice of a global scratch instead
 // of shared memory.
+// One-walk calls (segment mode without a visit budget, once the context has
+// seen a call's largest brick): step 1 also writes every run into a fixed
+// slice of its brick (capacity: the largest brick seen + 25%) and step 3 is
+// skipped; a brick past its slice shows in the visit read-back the call
+// makes anyway, and that call runs step 3 in the compact layout.
 #include "common.cuh"
 
 #include <algorithm>
@@ -248,17 +253,28 @@ struct Entry<false> {
     static __device__ __forceinline__ uint32_t local(T e) { return e.y & 511u; }
 };
 constexpr uint32_t kPackedKeyLimit = 1u << 23;
+constexpr uint64_t kDirectBytes = 8ull << 30; // fixed per-brick slices of a one-walk call: at most 8 GB
 
 // A run of `len` (<= 7) consecutive visits of one pair / vertex inside brick b,
 // their local voxels packed 9 bits each: counted per brick (FILL = false),
 // or written as (key, local voxel) entries into the brick's slice of the
 // visit list.
-template <bool FILL, bool PACK>
+// DIRECT (a counting walk that also fills): the brick's count is its cursor
+// and the entries go to the brick's fixed slice of entries_cap entries; a
+// run past the slice is counted but not written (the caller sees the
+// brick's count above the capacity and fills again in the compact layout).
+template <bool FILL, bool PACK, bool DIRECT = false>
 __device__ __forceinline__ void emit_run(uint32_t b, uint32_t key, uint64_t locals, uint32_t len, uint32_t* visits,
                                          uint32_t* cursor, typename Entry<PACK>::T* entries, size_t entries_cap,
                                          unsigned& status)
 {
-    if (!FILL) {
+    if (DIRECT) {
+        const uint32_t at = atomicAdd(visits + b, len);
+        if ((uint64_t)at + len <= entries_cap) {
+            typename Entry<PACK>::T* e = entries + (size_t)b * entries_cap + at;
+            for (uint32_t j = 0; j < len; ++j) e[j] = Entry<PACK>::make(key, (uint32_t)(locals >> (9 * j)) & 511u);
+        }
+    } else if (!FILL) {
         atomicAdd(visits + b, len); // fire-and-forget reduction
     } else {
         const uint32_t base = atomicAdd(cursor + b, len);
@@ -274,7 +290,9 @@ __device__ __forceinline__ void emit_run(uint32_t b, uint32_t key, uint64_t loca
 // SINGLE = true: a one-style call; the style comes as the kernel parameter
 // job0 (constant bank, free to read in the visit loop).  Otherwise the job
 // table is copied into shared memory and each item looks its style up.
-template <bool FILL, bool SEG, bool PACK, bool SINGLE, bool SPREAD = false>
+// DIRECT (with FILL = false): the counting walk also writes the entries
+// into fixed per-brick slices of entries_cap entries (see emit_run).
+template <bool FILL, bool SEG, bool PACK, bool SINGLE, bool SPREAD = false, bool DIRECT = false>
 __global__ void bin_kernel(const __grid_constant__ VoxJob job0, const VoxJob* __restrict__ jobs, int nj,
                            uint32_t total_items, float4* pair_rec, float4* pair_tan, uint32_t* visits,
                            uint32_t* cursor, void* entries_raw, size_t entries_cap, unsigned long long* words)
@@ -290,13 +308,14 @@ __global__ void bin_kernel(const __grid_constant__ VoxJob job0, const VoxJob* __
         load_bases(jobs, nj, s_item_base, nullptr);
     }
     unsigned status = 0;
-    // Fill pass of one style whose visit list is near the L2 size (SPREAD): lane l of
-    // global warp w takes item l * cols + w, so a warp's 32 walks come from
-    // distant strands and its slice reservations spread over many bricks
-    // instead of queueing on one brick's counter.  The scattered entry stores
-    // merge in L2 there; a much larger list would reach DRAM as partial sectors,
-    // so it keeps consecutive items per warp, as do the counting pass
-    // (coalesced index and vertex reads) and a batch (one style per warp).
+    // Fill pass of one style whose visit list is near the L2 size (SPREAD):
+    // lane l of global warp w takes item l * cols + w, so a warp's 32 walks
+    // come from distant strands and its slice reservations spread over many
+    // bricks instead of queueing on one brick's counter.  The scattered entry
+    // stores merge in L2 there; a much larger list would reach DRAM as
+    // partial sectors, so it keeps consecutive items per warp, as do the
+    // counting and one-walk passes (coalesced index and vertex reads, pair
+    // record stores) and a batch (one style per warp).
     constexpr bool sp = FILL && SINGLE && SEG && SPREAD;
     const uint64_t cols = (total_items + 31) / 32;
     const uint64_t span = sp ? cols * 32 : total_items;
@@ -329,14 +348,17 @@ __global__ void bin_kernel(const __grid_constant__ VoxJob job0, const VoxJob* __
                     ++len;
                 } else {
                     if (len)
-                        emit_run<FILL, PACK>(J.brick_base + cur, p, locals, len, visits, cursor, entries, entries_cap, status);
+                        emit_run<FILL, PACK, DIRECT>(J.brick_base + cur, p, locals, len, visits, cursor, entries,
+                                                     entries_cap, status);
                     cur = ok ? o.brick : kNoBrick;
                     len = ok ? 1u : 0u;
                     locals = ok ? (uint64_t)o.local : 0ull;
                 }
                 seg_advance(s);
             }
-            if (len) emit_run<FILL, PACK>(J.brick_base + cur, p, locals, len, visits, cursor, entries, entries_cap, status);
+            if (len)
+                emit_run<FILL, PACK, DIRECT>(J.brick_base + cur, p, locals, len, visits, cursor, entries, entries_cap,
+                                             status);
         } else {
             Visit o;
             if (vertex_visit(g, J.v, p, o))
@@ -670,7 +692,9 @@ __device__ __forceinline__ void resolve_brick(const VoxJob& J, const Grid& g, ui
 // counting sort of the keys by voxel and the per-voxel resolve.  BIG = false
 // takes the bricks of up to kBrickCap visits (keys sorted in shared memory,
 // list from the front); BIG = true the others (keys sorted into a slice of
-// the global key scratch, list from the back).  The next brick's queue slot
+// the global key scratch, list from the back).  A brick's entries are the
+// slice its fill reserved (compact layout), or with direct_cap > 0 the fixed
+// slice [brick * direct_cap, + count) of a one-walk call.  The next brick's queue slot
 // and bounds are fetched while the current one is processed, and the entry
 // passes keep kBrickUnroll loads in flight per thread.
 constexpr int kBrickUnroll = 4;
@@ -679,8 +703,8 @@ template <bool SEG, bool TANG, bool BIG, bool PACK>
 __global__ void __launch_bounds__(kBrickThreads, 2)
 brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__ pair_tan_all,
              const uint32_t* __restrict__ visits, const uint32_t* __restrict__ cursor, const uint32_t* __restrict__ list,
-             uint32_t list_n, const void* __restrict__ entries_raw, size_t entries_cap, uint4* hdesc,
-             size_t hdesc_cap, uint32_t* hkeys, size_t hkeys_cap, unsigned long long* words)
+             uint32_t list_n, const void* __restrict__ entries_raw, size_t entries_cap, uint32_t direct_cap,
+             uint4* hdesc, size_t hdesc_cap, uint32_t* hkeys, size_t hkeys_cap, unsigned long long* words)
 {
     typedef Entry<PACK> E;
     typedef typename E::T ET;
@@ -705,7 +729,7 @@ brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__
         if (nq < listed) {
             ngb = BIG ? list[list_n - 1 - nq] : list[nq];
             nnv = visits[ngb];
-            nstart = cursor[ngb] - nnv;
+            nstart = direct_cap ? ngb * direct_cap : cursor[ngb] - nnv;
         }
     }
     for (;;) {
@@ -725,13 +749,14 @@ brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__
         const uint32_t gb = s_gb, nv = s_nv, start = s_start;
         if (gb == 0xffffffffu) break;
         const bool skip = (uint64_t)start + nv > entries_cap ||                 // visit budget exceeded
+                          (direct_cap && nv > direct_cap) ||                    // past its fixed slice
                           (TANG && BIG && (uint64_t)s_hb + nv > hkeys_cap);     // key scratch exhausted
         if (skip) {
             status |= VKHR_DEV_LIST_OVERFLOW;
             if (tid == 0 && nq < listed) {
                 ngb = BIG ? list[list_n - 1 - nq] : list[nq];
                 nnv = visits[ngb];
-                nstart = cursor[ngb] - nnv;
+                nstart = direct_cap ? ngb * direct_cap : cursor[ngb] - nnv;
             }
         } else {
             const VoxJob& J = jobs[s_job];
@@ -752,7 +777,7 @@ brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__
             if (tid == 0 && nq < listed) { // the next brick's bounds, while this one's passes run
                 ngb = BIG ? list[list_n - 1 - nq] : list[nq];
                 nnv = visits[ngb];
-                nstart = cursor[ngb] - nnv;
+                nstart = direct_cap ? ngb * direct_cap : cursor[ngb] - nnv;
             }
             __syncthreads();
             if (TANG) {
@@ -1173,19 +1198,19 @@ vkhr_status check_device_status(vkhr_ctx* ctx, unsigned long long s)
 
 template <bool SEG, bool TANG, bool PACK>
 vkhr_status launch_brick(vkhr_ctx* ctx, const VoxJob* d_jobs, int nj, uint32_t total_bricks, cudaStream_t st,
-                         unsigned blocks, size_t cap_visits)
+                         unsigned blocks, size_t entries_cap, size_t keys_cap, uint32_t direct_cap)
 {
     // bricks above kBrickCap first (their keys go to the global scratch), then the rest
     const size_t small = (size_t)(2 * kBrickThreads + 32 + kBrickThreads) * sizeof(uint32_t);
     const size_t smem = small + (TANG ? (size_t)kBrickCap * sizeof(uint32_t) : 0);
     VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG, true, PACK>), (unsigned)ctx->sm_count * 2, kBrickThreads, small, st,
                 d_jobs, nj, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->brick_list, total_bricks,
-                ctx->items, cap_visits, ctx->hdesc, ctx->hdesc_cap, ctx->hkeys, cap_visits, ctx->d_words);
+                ctx->items, entries_cap, direct_cap, ctx->hdesc, ctx->hdesc_cap, ctx->hkeys, keys_cap, ctx->d_words);
     VKHR_CUDA_TRY(ctx, cudaFuncSetAttribute(brick_kernel<SEG, TANG, false, PACK>,
                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG, false, PACK>), blocks, kBrickThreads, smem, st, d_jobs, nj,
                 ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->brick_list, total_bricks, ctx->items,
-                cap_visits, ctx->hdesc, ctx->hdesc_cap, ctx->hkeys, cap_visits, ctx->d_words);
+                entries_cap, direct_cap, ctx->hdesc, ctx->hdesc_cap, ctx->hkeys, keys_cap, ctx->d_words);
     return VKHR_OK;
 }
 
@@ -1282,6 +1307,22 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
         s = vkhr_reserve(ctx, (void**)&ctx->items, &ctx->items_cap, visits_total ? visits_total : 1, sizeof(uint2));
         if (s != VKHR_OK) return s;
     }
+    // One walk instead of two: segment mode without a budget reads its visit
+    // total back anyway, so when the context knows a per-brick capacity (from
+    // its earlier calls' largest brick) and the fixed slices fit in memory,
+    // the counting walk also writes every run into its brick's slice
+    // [brick * capacity, + count).  A brick past the capacity shows in the
+    // read-back; the call then fills again in the compact layout.
+    const size_t entry_bytes = pack ? sizeof(uint32_t) : sizeof(uint2);
+    uint32_t direct_cap = 0;
+    if (!bounded && total_items && ctx->direct_cap) {
+        const uint64_t slots = (uint64_t)total_bricks * ctx->direct_cap;
+        if (slots < (1ull << 32) && slots * entry_bytes <= kDirectBytes) {
+            s = vkhr_reserve(ctx, (void**)&ctx->items, &ctx->items_cap, (slots * entry_bytes + 7) / 8, sizeof(uint2));
+            if (s != VKHR_OK) return s;
+            direct_cap = ctx->direct_cap;
+        }
+    }
     VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_words, 0, WORD_NORM * sizeof(unsigned long long), st));
     VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->brick_visits, 0, (size_t)total_bricks * sizeof(uint32_t), st));
     const unsigned threads = 256;
@@ -1292,7 +1333,21 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
                                        : std::min(vkhr_blocks(total_items, threads), (unsigned)ctx->sm_count * 16);
     const size_t bin_smem_bytes = (size_t)nj * (sizeof(VoxJob) + sizeof(uint32_t));
     const bool single = nj == 1;
-    if (total_items) {
+#define VKHR_DIRECT(PACK_)                                                                                        \
+    do {                                                                                                         \
+        if (single)                                                                                              \
+            VKHR_LAUNCH(ctx, (bin_kernel<false, true, PACK_, true, false, true>), in_blocks, threads, 0, st,       \
+                        jobs[0], d_jobs, nj, total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits,        \
+                        ctx->brick_cursor, ctx->items, (size_t)direct_cap, ctx->d_words);                         \
+        else                                                                                                     \
+            VKHR_LAUNCH(ctx, (bin_kernel<false, true, PACK_, false, false, true>), in_blocks, threads,             \
+                        bin_smem_bytes, st, jobs[0], d_jobs, nj, total_items, ctx->pair_rec, ctx->pair_tan,       \
+                        ctx->brick_visits, ctx->brick_cursor, ctx->items, (size_t)direct_cap, ctx->d_words);      \
+    } while (0)
+    if (total_items && direct_cap) {
+        if (pack) VKHR_DIRECT(true);
+        else VKHR_DIRECT(false);
+    } else if (total_items) {
         if (segments && single)
             VKHR_LAUNCH(ctx, (bin_kernel<false, true, false, true>), in_blocks, threads, 0, st, jobs[0], d_jobs, nj,
                         total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, nullptr,
@@ -1310,6 +1365,7 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
                         d_jobs, nj, total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor,
                         nullptr, (size_t)0, ctx->d_words);
     }
+#undef VKHR_DIRECT
     const unsigned rblocks = std::min(vkhr_blocks(total_bricks, kRangeThreads * kRangeItems), (unsigned)ctx->sm_count * 8);
     VKHR_LAUNCH(ctx, bin_ranges_kernel, rblocks, kRangeThreads, 0, st, ctx->brick_visits, total_bricks,
                 ctx->brick_cursor, ctx->brick_list, ctx->d_words);
@@ -1329,8 +1385,15 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
         visits_total = ctx->h_words[WORD_TOTAL_VISITS];
         if (visits_total >= (1ull << 32))
             return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "more than 2^32 - 1 voxel visits in one call");
-        s = vkhr_reserve(ctx, (void**)&ctx->items, &ctx->items_cap, visits_total ? visits_total : 1, sizeof(uint2));
-        if (s != VKHR_OK) return s;
+        // the next calls' per-brick capacity: this call's largest brick + 25%, grow-only
+        const uint64_t largest = ctx->h_words[WORD_MAX_BRICK_VISITS];
+        const uint64_t want = (largest + largest / 4 + 63) / 64 * 64;
+        if (want > ctx->direct_cap && want < (1ull << 31)) ctx->direct_cap = (uint32_t)want;
+        if (direct_cap && largest > direct_cap) direct_cap = 0; // a brick outgrew its slice: fill compactly
+        if (!direct_cap) {
+            s = vkhr_reserve(ctx, (void**)&ctx->items, &ctx->items_cap, visits_total ? visits_total : 1, sizeof(uint2));
+            if (s != VKHR_OK) return s;
+        }
     }
     // capacities the kernels check against (the budget, not the grown scratch)
     const size_t cap_visits = visits_total ? (size_t)visits_total : 1;
@@ -1341,7 +1404,7 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
                          sizeof(uint4));
         if (s != VKHR_OK) return s;
     }
-    if (total_items) {
+    if (total_items && !direct_cap) {
         void* ent = ctx->items;
         // spread a one-style fill's warps over distant strands when its visit
         // list is within twice the L2 size: most scattered entry stores still
@@ -1370,15 +1433,19 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
 #undef VKHR_FILL
     }
     const unsigned bblocks = std::min(total_bricks, (unsigned)ctx->sm_count * 2);
+    const size_t entries_cap = direct_cap ? (size_t)total_bricks * direct_cap : cap_visits;
+#define VKHR_BRICK(SEG_, TANG_, PACK_)                                                                            \
+    launch_brick<SEG_, TANG_, PACK_>(ctx, d_jobs, nj, total_bricks, st, bblocks, entries_cap, cap_visits, direct_cap)
     if (segments) {
-        if (!tang) s = launch_brick<true, false, true>(ctx, d_jobs, nj, total_bricks, st, bblocks, cap_visits);
-        else if (pack) s = launch_brick<true, true, true>(ctx, d_jobs, nj, total_bricks, st, bblocks, cap_visits);
-        else s = launch_brick<true, true, false>(ctx, d_jobs, nj, total_bricks, st, bblocks, cap_visits);
+        if (!tang) s = VKHR_BRICK(true, false, true);
+        else if (pack) s = VKHR_BRICK(true, true, true);
+        else s = VKHR_BRICK(true, true, false);
     } else {
-        if (!tang) s = launch_brick<false, false, true>(ctx, d_jobs, nj, total_bricks, st, bblocks, cap_visits);
-        else if (pack) s = launch_brick<false, true, true>(ctx, d_jobs, nj, total_bricks, st, bblocks, cap_visits);
-        else s = launch_brick<false, true, false>(ctx, d_jobs, nj, total_bricks, st, bblocks, cap_visits);
+        if (!tang) s = VKHR_BRICK(false, false, true);
+        else if (pack) s = VKHR_BRICK(false, true, true);
+        else s = VKHR_BRICK(false, true, false);
     }
+#undef VKHR_BRICK
     if (s != VKHR_OK) return s;
     if (tang) {
         VKHR_LAUNCH(ctx, crowded_warp_kernel, (unsigned)ctx->sm_count * 8, 32 * kCrowdWarps, 0, st, d_jobs,
