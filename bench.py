@@ -53,7 +53,8 @@ WORKLOAD = {
 # frame (profiles/voxelizer_kernels_production_frame.md and
 # profiles/raymarch_kernel_production_frame.md), by kernel family.
 TRAFFIC = {
-    "brick_kernel<SEG, TANG, false": 155_667_968 + 37_609_728,
+    "bin_kernel<false, true, true, true, false, true": 57_419_008 + 149_499_904,  # one walk
+    "brick_kernel<SEG, TANG, false": 158_595_328 + 38_296_576,
     "bin_kernel<true": 55_134_208 + 72_237_312,
     "bin_kernel<false": 55_694_080 + 24_500_992,
     "raymarch_kernel": 8_216_576 + 51_968,
@@ -645,6 +646,9 @@ def gb300_arm(args):
         if name.startswith("(bin_kernel<true"):
             # index pairs + both vertices of each pair once + the 4-byte visit entries written
             return 8 * S + 24 * V + 4 * visits
+        if name.startswith("(bin_kernel<false") and name.count(",") == 5 and name.endswith("true>)"):
+            # one walk: index pairs + vertices once + the pair records and tangents + the 4-byte visit entries written
+            return 8 * S + 24 * V + 48 * S + 4 * visits
         if name.startswith("(bin_kernel<false"):
             # index pairs + vertices once + the pair records and tangents written
             return 8 * S + 24 * V + 48 * S
