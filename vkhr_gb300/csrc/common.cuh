@@ -76,6 +76,10 @@ struct vkhr_ctx {
     unsigned long long* d_words;
     unsigned long long* h_words; // pinned mirror
     cudaEvent_t ev;
+    // side stream for kernels that overlap the main chain (fork/join by events,
+    // so a captured call captures both streams)
+    cudaStream_t side;
+    cudaEvent_t fork_ev, join_ev;
     unsigned long long launches; // kernels this context has launched
     // kernel tracer (vkhr_set_profiling): an event pair around every launch
     int profiling;
@@ -108,6 +112,10 @@ void vkhr_prof_end(vkhr_ctx* ctx, cudaStream_t st);
     } while (0)
 
 vkhr_status vkhr_fail(vkhr_ctx* ctx, vkhr_status s, const char* msg);
+// The side stream waits for the work queued so far on st / st waits for the
+// work queued so far on the side stream.
+vkhr_status vkhr_fork_side(vkhr_ctx* ctx, cudaStream_t st);
+vkhr_status vkhr_join_side(vkhr_ctx* ctx, cudaStream_t st);
 vkhr_status vkhr_fail_cuda(vkhr_ctx* ctx, cudaError_t e, const char* what, const char* file, int line);
 
 // Grow-only device buffer; contents are not preserved on growth.

@@ -56,6 +56,20 @@ void vkhr_prof_end(vkhr_ctx* ctx, cudaStream_t st)
     ++ctx->prof_n;
 }
 
+vkhr_status vkhr_fork_side(vkhr_ctx* ctx, cudaStream_t st)
+{
+    VKHR_CUDA_TRY(ctx, cudaEventRecord(ctx->fork_ev, st));
+    VKHR_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->side, ctx->fork_ev, 0));
+    return VKHR_OK;
+}
+
+vkhr_status vkhr_join_side(vkhr_ctx* ctx, cudaStream_t st)
+{
+    VKHR_CUDA_TRY(ctx, cudaEventRecord(ctx->join_ev, ctx->side));
+    VKHR_CUDA_TRY(ctx, cudaStreamWaitEvent(st, ctx->join_ev, 0));
+    return VKHR_OK;
+}
+
 extern "C" {
 
 int vkhr_abi_version(void) { return VKHR_CUDA_ABI_VERSION; }
@@ -120,6 +134,9 @@ vkhr_status vkhr_create(int device, vkhr_ctx** out)
     if (e == cudaSuccess) e = cudaMemset(ctx->d_words, 0, WORD_COUNT * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_words, WORD_COUNT * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->join_ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->jobs_ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_jobs, kJobTableBytes);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->rjobs_ev, cudaEventDisableTiming);
@@ -146,6 +163,9 @@ vkhr_status vkhr_destroy(vkhr_ctx* ctx)
     if (ctx->d_words) cudaFree(ctx->d_words);
     if (ctx->h_words) cudaFreeHost(ctx->h_words);
     if (ctx->ev) cudaEventDestroy(ctx->ev);
+    if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
+    if (ctx->join_ev) cudaEventDestroy(ctx->join_ev);
+    if (ctx->side) cudaStreamDestroy(ctx->side);
     if (ctx->jobs_ev) cudaEventDestroy(ctx->jobs_ev);
     if (ctx->h_jobs) cudaFreeHost(ctx->h_jobs);
     if (ctx->rjobs_ev) cudaEventDestroy(ctx->rjobs_ev);

@@ -1200,10 +1200,13 @@ template <bool SEG, bool TANG, bool PACK>
 vkhr_status launch_brick(vkhr_ctx* ctx, const VoxJob* d_jobs, int nj, uint32_t total_bricks, cudaStream_t st,
                          unsigned blocks, size_t entries_cap, size_t keys_cap, uint32_t direct_cap)
 {
-    // bricks above kBrickCap first (their keys go to the global scratch), then the rest
+    // bricks above kBrickCap (their keys go to the global scratch) on the side
+    // stream, alongside the rest on st; the caller joins the side stream
     const size_t small = (size_t)(2 * kBrickThreads + 32 + kBrickThreads) * sizeof(uint32_t);
     const size_t smem = small + (TANG ? (size_t)kBrickCap * sizeof(uint32_t) : 0);
-    VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG, true, PACK>), (unsigned)ctx->sm_count * 2, kBrickThreads, small, st,
+    vkhr_status s = vkhr_fork_side(ctx, st); // after the fill
+    if (s != VKHR_OK) return s;
+    VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG, true, PACK>), (unsigned)ctx->sm_count * 2, kBrickThreads, small, ctx->side,
                 d_jobs, nj, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->brick_list, total_bricks,
                 ctx->items, entries_cap, direct_cap, ctx->hdesc, ctx->hdesc_cap, ctx->hkeys, keys_cap, ctx->d_words);
     VKHR_CUDA_TRY(ctx, cudaFuncSetAttribute(brick_kernel<SEG, TANG, false, PACK>,
@@ -1369,8 +1372,6 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
     const unsigned rblocks = std::min(vkhr_blocks(total_bricks, kRangeThreads * kRangeItems), (unsigned)ctx->sm_count * 8);
     VKHR_LAUNCH(ctx, bin_ranges_kernel, rblocks, kRangeThreads, 0, st, ctx->brick_visits, total_bricks,
                 ctx->brick_cursor, ctx->brick_list, ctx->d_words);
-    VKHR_LAUNCH(ctx, zero_empty_kernel, std::min(vkhr_blocks(total_groups, 256), (unsigned)ctx->sm_count * 16), 256, 0,
-                st, d_jobs, nj, total_groups, ctx->brick_visits);
     VKHR_CUDA_TRY(ctx, cudaGetLastError());
 
     if (!bounded) {          // segment mode without a budget: read the visit total back
@@ -1404,6 +1405,12 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
                          sizeof(uint4));
         if (s != VKHR_OK) return s;
     }
+    // Unvisited bricks are zeroed on the side stream, alongside the fill and
+    // the brick kernel (disjoint voxels); every return below joins it.
+    s = vkhr_fork_side(ctx, st);
+    if (s != VKHR_OK) return s;
+    VKHR_LAUNCH(ctx, zero_empty_kernel, std::min(vkhr_blocks(total_groups, 256), (unsigned)ctx->sm_count * 16), 256, 0,
+                ctx->side, d_jobs, nj, total_groups, ctx->brick_visits);
     if (total_items && !direct_cap) {
         void* ent = ctx->items;
         // spread a one-style fill's warps over distant strands when its visit
@@ -1446,12 +1453,18 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
         else s = VKHR_BRICK(false, true, false);
     }
 #undef VKHR_BRICK
+    const vkhr_status joined = vkhr_join_side(ctx, st); // zeroing and big bricks done before the crowded voxels
     if (s != VKHR_OK) return s;
-    if (tang) {
+    if (joined != VKHR_OK) return joined;
+    if (tang) { // crowded voxels of up to / above kCrowdWarpMax visits: independent descriptor lists
+        s = vkhr_fork_side(ctx, st);
+        if (s != VKHR_OK) return s;
+        VKHR_LAUNCH(ctx, crowded_kernel, (unsigned)ctx->sm_count * 6, kCrowdThreads, 0, ctx->side, d_jobs, ctx->hdesc,
+                    ctx->hdesc_cap, ctx->hkeys, ctx->d_words);
         VKHR_LAUNCH(ctx, crowded_warp_kernel, (unsigned)ctx->sm_count * 8, 32 * kCrowdWarps, 0, st, d_jobs,
                     ctx->pair_tan, ctx->hdesc, ctx->hdesc_cap, ctx->hkeys, ctx->d_words);
-        VKHR_LAUNCH(ctx, crowded_kernel, (unsigned)ctx->sm_count * 6, kCrowdThreads, 0, st, d_jobs, ctx->hdesc,
-                    ctx->hdesc_cap, ctx->hkeys, ctx->d_words);
+        s = vkhr_join_side(ctx, st);
+        if (s != VKHR_OK) return s;
     }
     VKHR_CUDA_TRY(ctx, cudaGetLastError());
     return VKHR_OK;
