@@ -277,7 +277,8 @@ static inline unsigned occupancy_blocks(int nx, int ny, int nz, int sm_count)
 // sample is exactly zero (border, or an empty brick), 2 when it is zero and
 // the ray has left the grid for good (moving away along every such axis),
 // 0 when it must be sampled.  box_lo/box_hi receive the current brick's
-// texel-coordinate extent for the empty-space jump.
+// texel-coordinate extent for the empty-space jump.  du only needs the ray
+// direction's sign per axis (its reciprocal serves).
 __device__ __forceinline__ int classify(const RayConsts& c, const uint32_t* __restrict__ occ, const float u[3],
                                         const float du[3], float box_lo[3], float box_hi[3])
 {
@@ -314,17 +315,29 @@ __device__ __forceinline__ int classify(const RayConsts& c, const uint32_t* __re
 }
 
 // Whole steps that stay inside the empty brick [lo, hi) from u along du
-// (per unit t), keeping kSkipMargin texels from its faces.
-__device__ __forceinline__ float steps_inside(const float u[3], const float du[3], const float lo[3], const float hi[3],
-                                              float step)
+// (per unit t), keeping kSkipMargin texels from its faces.  inv holds 1/du
+// per axis (0 where du is 0; computed once per ray, and it carries du's
+// sign, which is all classify needs) and steps_per_t = 1/step, exact because
+// jumps run for power-of-two step counts only.  The reciprocal's rounding
+// moves the predicted exit by about 1e-6 texel, far inside the margin; and
+// even one step more than the exact count would leave every skipped sample
+// inside the margin-shrunk brick (the first sample past the jump is taken).
+__device__ __forceinline__ float steps_inside(const float u[3], const float inv[3], const float lo[3], const float hi[3],
+                                              float steps_per_t)
 {
     float te = INFINITY;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        if (du[k] > 0.0f) te = fminf(te, (hi[k] - kSkipMargin - u[k]) / du[k]);
-        else if (du[k] < 0.0f) te = fminf(te, (lo[k] + kSkipMargin - u[k]) / du[k]);
+        if (inv[k] > 0.0f) te = fminf(te, (hi[k] - kSkipMargin - u[k]) * inv[k]);
+        else if (inv[k] < 0.0f) te = fminf(te, (lo[k] + kSkipMargin - u[k]) * inv[k]);
     }
-    return floorf(te / step);
+    return floorf(te * steps_per_t);
+}
+
+__device__ __forceinline__ void reciprocals(const float d[3], float inv[3])
+{
+#pragma unroll
+    for (int k = 0; k < 3; ++k) inv[k] = d[k] != 0.0f ? 1.0f / d[k] : 0.0f;
 }
 
 __device__ __forceinline__ void texel_coords(const RayConsts& c, Vec3 p, float u[3])
@@ -411,6 +424,8 @@ __device__ __forceinline__ void march_pixel(const RayConsts& c, const typename D
         du[0] = ue[0] - us[0];
         du[1] = ue[1] - us[1];
         du[2] = ue[2] - us[2];
+        float inv_du[3];
+        reciprocals(du, inv_du);
         float acc = 0.0f;
         Vec3 surf = v3(0.0f, 0.0f, 0.0f), entry = v3(0.0f, 0.0f, 0.0f);
         bool found = false, entered = false;
@@ -421,10 +436,10 @@ __device__ __forceinline__ void march_pixel(const RayConsts& c, const typename D
             if (depth_test && db < clip_depth(c, P)) break;
             float u[3], lo[3], hi[3];
             texel_coords(c, P, u);
-            const int z = classify(c, occ, u, du, lo, hi);
+            const int z = classify(c, occ, u, inv_du, lo, hi);
             if (z == 2) break; // left the grid: every later sample adds exactly 0
             if (z == 1) {      // exactly 0: acc and the decisions are unchanged
-                const float n = jump ? steps_inside(u, du, lo, hi, step) : 0.0f;
+                const float n = jump ? steps_inside(u, inv_du, lo, hi, c.steps) : 0.0f;
                 t = n >= 1.0f ? fmaf(n, step, t) : t + step;
                 if (TAPE) k += n >= 1.0f ? (uint32_t)n : 1u;
                 continue;
@@ -483,15 +498,17 @@ __device__ __forceinline__ void march_pixel(const RayConsts& c, const typename D
                 dl[0] = le[0] - ls[0];
                 dl[1] = le[1] - ls[1];
                 dl[2] = le[2] - ls[2];
+                float inv_dl[3];
+                reciprocals(dl, inv_dl);
                 float strands = 0.0f;
                 for (float t = 0.0f; t < 1.0f;) {
                     const Vec3 Q = mix(surf, light, t);
                     float u[3], lo[3], hi[3];
                     texel_coords(c, Q, u);
-                    const int z = classify(c, occ, u, dl, lo, hi);
+                    const int z = classify(c, occ, u, inv_dl, lo, hi);
                     if (z == 2) break;
                     if (z == 1) {
-                        const float n = c.shadow_pow2 ? steps_inside(u, dl, lo, hi, sstep) : 0.0f;
+                        const float n = c.shadow_pow2 ? steps_inside(u, inv_dl, lo, hi, c.shadow_steps) : 0.0f;
                         t = n >= 1.0f ? fmaf(n, sstep, t) : t + sstep;
                         continue;
                     }
