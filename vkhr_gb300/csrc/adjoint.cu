@@ -364,8 +364,16 @@ vkhr_status vkhr_raymarch_train(vkhr_ctx* ctx, const vkhr_raymarch_params* param
     s = vkhr_reserve(ctx, (void**)&ctx->occ, &ctx->occ_cap, words, sizeof(uint32_t));
     if (s != VKHR_OK) return s;
     VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->occ, 0, words * sizeof(uint32_t), st));
-    VKHR_LAUNCH(ctx, occupancy_kernel<VKHR_DENSITY_F32>, occupancy_blocks(c.res[0], c.res[1], c.res[2], ctx->sm_count),
-                128, 0, st, d_density, c.res[0], c.res[1], c.res[2], c.nb[0], c.nb[1], c.nb[2], ctx->occ);
+    {
+        const int L = occupancy_lanes(c.res[0], c.res[1], c.res[2], ctx->sm_count);
+        const unsigned ob = occupancy_blocks(c.res[0], c.res[1], c.res[2], ctx->sm_count, L);
+        if (L == 8)
+            VKHR_LAUNCH(ctx, (occupancy_kernel<VKHR_DENSITY_F32, 8>), ob, 128, 0, st, d_density, c.res[0], c.res[1],
+                        c.res[2], c.nb[0], c.nb[1], c.nb[2], ctx->occ);
+        else
+            VKHR_LAUNCH(ctx, (occupancy_kernel<VKHR_DENSITY_F32, 1>), ob, 128, 0, st, d_density, c.res[0], c.res[1],
+                        c.res[2], c.nb[0], c.nb[1], c.nb[2], ctx->occ);
+    }
     const size_t px = (size_t)c.W * c.H;
     const uint32_t nckpt = tape_checkpoints(params, checkpoint_interval);
     PixelTape* tape = reinterpret_cast<PixelTape*>(d_tape);

@@ -174,12 +174,12 @@ __device__ Vec3 sample_tangent(const RayConsts& c, const void* t, Vec3 p)
 // [8k - 1, 8k + 7].  A brick is occupied when any of those texels is nonzero;
 // every sample whose cell lies in an empty brick is exactly 0.
 //
-// One thread per column: the chunk of 8 texels along x at x0 = 8 * cx (one
-// vector load when aligned) in each of the 8 x 8 rows y in [8a, 8a + 8),
-// z in [8c, 8c + 8).  Texel x0 + i belongs to cell brick cx (i <= 7) and
-// texel x0 + 7 also to cx + 1; along y (and z) row 8a + i belongs to cell
-// brick a, and row 8a + 7 also to a + 1.  The thread ORs its rows' masks in
-// registers and marks at most 8 bricks.
+// A column: the chunk of 8 texels along x at x0 = 8 * cx (one vector load
+// when aligned) in each of the 8 x 8 rows y in [8a, 8a + 8), z in [8c, 8c + 8).
+// Texel x0 + i belongs to cell brick cx (i <= 7) and texel x0 + 7 also to
+// cx + 1; along y (and z) row 8a + i belongs to cell brick a, and row 8a + 7
+// also to a + 1.  The column's rows' masks are ORed (in registers and across
+// its 8 lanes) and it marks at most 8 bricks.
 template <int DF>
 __device__ __forceinline__ uint32_t chunk_mask(const typename DensityTexel<DF>::T* __restrict__ p, int n)
 {
@@ -212,32 +212,52 @@ __device__ __forceinline__ void occupancy_mark(uint32_t* bits, int nbx, int nby,
     atomicOr(bits + (b >> 5), 1u << (b & 31)); // result unused: a fire-and-forget reduction
 }
 
-template <int DF>
+// One 8x8x8 column of texels (chunk cx of rows 8a..8a+7 of planes 8c..8c+7)
+// with L lanes (L = 1 or 8): lane sub = lane % L reads the z rows
+// zz = sub, sub + L, ...; the masks are ORed across the column's L lanes by
+// shuffles (only the lane holding zz = 7 contributes the last-plane masks)
+// and lane sub = 0 marks.  With L > 1 all 32 lanes of the warp call it
+// (valid = false for lanes past the last column); for a given zz the warp's
+// 32 / L columns read consecutive chunks of one row.
+template <int DF, int L>
 __device__ __forceinline__ void occupancy_column(const typename DensityTexel<DF>::T* __restrict__ d, int nx, int ny,
-                                                 int nz, int nbx, int nby, uint32_t* bits, int cx, int a, int c)
+                                                 int nz, int nbx, int nby, uint32_t* bits, int cx, int a, int c,
+                                                 bool valid)
 {
-    const int x0 = 8 * cx, n = min(8, nx - x0);
+    const int sub = (int)(threadIdx.x & 31u) & (L - 1);
     uint32_t m_all = 0, m_y = 0, m_z = 0, m_yz = 0; // rows of brick (a, c); last y row; last z row; both
-    for (int zz = 0; zz < 8; ++zz) {
-        const int z = 8 * c + zz;
-        if (z >= nz) break;
-        uint32_t mz = 0, my = 0;
+    if (valid) {
+        const int x0 = 8 * cx, n = min(8, nx - x0);
 #pragma unroll
-        for (int yy = 0; yy < 8; ++yy) {
-            const int y = 8 * a + yy;
-            if (y < ny) {
-                const uint32_t m = chunk_mask<DF>(d + (size_t)nx * ((size_t)y + (size_t)ny * z) + x0, n);
-                mz |= m;
-                if (yy == 7) my = m;
+        for (int k = 0; k < 8 / L; ++k) {
+            const int zz = sub + k * L, z = 8 * c + zz;
+            if (z >= nz) break;
+            uint32_t mz = 0, my = 0;
+#pragma unroll
+            for (int yy = 0; yy < 8; ++yy) {
+                const int y = 8 * a + yy;
+                if (y < ny) {
+                    const uint32_t m = chunk_mask<DF>(d + (size_t)nx * ((size_t)y + (size_t)ny * z) + x0, n);
+                    mz |= m;
+                    if (yy == 7) my = m;
+                }
+            }
+            m_all |= mz;
+            m_y |= my;
+            if (zz == 7) {
+                m_z = mz;
+                m_yz = my;
             }
         }
-        m_all |= mz;
-        m_y |= my;
-        if (zz == 7) {
-            m_z = mz;
-            m_yz = my;
-        }
     }
+#pragma unroll
+    for (int o = 1; o < L; o <<= 1) {
+        m_all |= __shfl_xor_sync(0xffffffffu, m_all, o);
+        m_y |= __shfl_xor_sync(0xffffffffu, m_y, o);
+        m_z |= __shfl_xor_sync(0xffffffffu, m_z, o);
+        m_yz |= __shfl_xor_sync(0xffffffffu, m_yz, o);
+    }
+    if (!valid || sub != 0) return;
     const uint32_t ms[4] = {m_all, m_y, m_z, m_yz};
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
@@ -248,17 +268,20 @@ __device__ __forceinline__ void occupancy_column(const typename DensityTexel<DF>
     }
 }
 
-template <int DF>
+template <int DF, int L>
 __global__ void occupancy_kernel(const typename DensityTexel<DF>::T* __restrict__ d, int nx, int ny, int nz, int bx,
                                  int by, int bz, uint32_t* __restrict__ bits)
 {
-    // columns with cx fastest (a warp reads consecutive chunks of a row)
+    // L lanes per column, columns with cx fastest; the loop is warp-uniform
     const uint32_t cxn = (uint32_t)(nx + 7) / 8, an = (uint32_t)(ny + 7) / 8, cn = (uint32_t)(nz + 7) / 8;
-    const uint32_t total = cxn * an * cn;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    const uint64_t lanes = (uint64_t)L * cxn * an * cn;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g - (threadIdx.x & 31u) < lanes; g += stride) {
+        const bool valid = g < lanes;
+        const uint32_t i = valid ? (uint32_t)(g / L) : 0u;
         const uint32_t r = i / cxn, cx = i - r * cxn;
         const uint32_t c = r / an, a = r - c * an;
-        occupancy_column<DF>(d, nx, ny, nz, bx, by, bits, (int)cx, (int)a, (int)c);
+        occupancy_column<DF, L>(d, nx, ny, nz, bx, by, bits, (int)cx, (int)a, (int)c, valid);
     }
 }
 
@@ -267,10 +290,18 @@ static inline uint64_t occupancy_columns(int nx, int ny, int nz)
     return (uint64_t)((nx + 7) / 8) * ((ny + 7) / 8) * ((nz + 7) / 8);
 }
 
-static inline unsigned occupancy_blocks(int nx, int ny, int nz, int sm_count)
+// Lanes per column: 8 when that grid still fits in 16 blocks of 128 threads
+// per SM (a small volume has too few columns to fill the GPU one per
+// thread), else 1.
+static inline int occupancy_lanes(int nx, int ny, int nz, int sm_count)
 {
-    const uint64_t cols = occupancy_columns(nx, ny, nz);
-    return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((cols + 127) / 128, (uint64_t)sm_count * 16));
+    return 8 * occupancy_columns(nx, ny, nz) <= (uint64_t)sm_count * 16 * 128 ? 8 : 1;
+}
+
+static inline unsigned occupancy_blocks(int nx, int ny, int nz, int sm_count, int lanes_per_column)
+{
+    const uint64_t lanes = (uint64_t)lanes_per_column * occupancy_columns(nx, ny, nz);
+    return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((lanes + 127) / 128, (uint64_t)sm_count * 16));
 }
 
 // Classifies one sample position (texel coordinates u).  Returns 1 when the

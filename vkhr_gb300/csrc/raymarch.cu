@@ -35,19 +35,36 @@ template <int DF, int TF, int TW = 8, int MINB = 6>
 __global__ void __launch_bounds__(32 * kWarpsX * kWarpsY, MINB)
 raymarch_kernel(const __grid_constant__ RayConsts c, const typename DensityTexel<DF>::T* __restrict__ dens,
                 const void* __restrict__ tang, const uint32_t* __restrict__ occ, const float* __restrict__ depth_in,
-                float4* __restrict__ rgba, float* __restrict__ depth_out)
+                float4* __restrict__ rgba, float* __restrict__ depth_out, int x0, int y0, int x1, int y1)
 {
+    // the pixels [x0, x1) x [y0, y1): the volume's footprint (background_kernel writes the rest)
     constexpr int TH = 32 / TW;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int px = (blockIdx.x * kWarpsX + (warp % kWarpsX)) * TW + (lane % TW);
-    const int py = (blockIdx.y * kWarpsY + (warp / kWarpsX)) * TH + (lane / TW);
-    if (px >= c.W || py >= c.H) return;
+    const int px = x0 + (blockIdx.x * kWarpsX + (warp % kWarpsX)) * TW + (lane % TW);
+    const int py = y0 + (blockIdx.y * kWarpsY + (warp / kWarpsX)) * TH + (lane / TW);
+    if (px >= x1 || py >= y1) return;
     const size_t at = (size_t)py * c.W + px;
     float4 out;
     float out_depth;
     march_pixel<DF, TF>(c, dens, tang, occ, depth_in ? depth_in + at : nullptr, px, py, out, out_depth);
     rgba[at] = out;
     if (depth_out) depth_out[at] = out_depth;
+}
+
+// Background (RGBA 0, depth 1: what march_pixel gives a ray that misses the
+// volume's box) for the pixels outside [x0, x1) x [y0, y1).  A pixel outside
+// the footprint rectangle misses the box, so the march launch covers the
+// rectangle only instead of one CTA per tile of the whole view.
+__global__ void background_kernel(float4* __restrict__ rgba, float* __restrict__ depth, int W, int H, int x0, int y0,
+                                  int x1, int y1)
+{
+    const size_t n = (size_t)W * H;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const int py = (int)(i / (size_t)W), px = (int)(i - (size_t)py * W);
+        if (px >= x0 && px < x1 && py >= y0 && py < y1) continue;
+        rgba[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (depth) depth[i] = 1.0f;
+    }
 }
 
 // ---- batched raymarch ------------------------------------------------------------
@@ -92,14 +109,18 @@ __global__ void occupancy_batched_kernel(const RayJob* __restrict__ jobs, int nj
     __shared__ uint32_t s_base[kMaxRayJobs];
     for (int j = threadIdx.x; j < nj; j += blockDim.x) s_base[j] = jobs[j].column_base;
     __syncthreads();
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total_columns; i += gridDim.x * blockDim.x) {
+    // one thread per column (a batch has columns enough to fill the GPU)
+    const uint64_t lanes = total_columns, stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < lanes; g += stride) {
+        const bool valid = true;
+        const uint32_t i = (uint32_t)g;
         const RayJob& J = jobs[find_base(s_base, nj, i)];
         const uint32_t li = i - J.column_base;
         const int nx = J.c.res[0], ny = J.c.res[1], nz = J.c.res[2];
         const uint32_t cxn = (uint32_t)(nx + 7) / 8, an = (uint32_t)(ny + 7) / 8;
         const uint32_t r = li / cxn, cx = li - r * cxn, c = r / an, a = r - c * an;
-        occupancy_column<DF>((const typename DensityTexel<DF>::T*)J.dens, nx, ny, nz, J.c.nb[0], J.c.nb[1], J.occ,
-                             (int)cx, (int)a, (int)c);
+        occupancy_column<DF, 1>((const typename DensityTexel<DF>::T*)J.dens, nx, ny, nz, J.c.nb[0], J.c.nb[1], J.occ,
+                                (int)cx, (int)a, (int)c, valid);
     }
 }
 
@@ -145,28 +166,50 @@ raymarch_batched_kernel(const RayJob* __restrict__ jobs, int nj, uint32_t total_
 
 template <int DF, int TF>
 vkhr_status launch(vkhr_ctx* ctx, const RayConsts& c, const void* dens, const void* tang, const float* din, float* rgba,
-                   float* dout, cudaStream_t st)
+                   float* dout, const int32_t rect[4], cudaStream_t st)
 {
     const size_t bricks = (size_t)c.nb[0] * c.nb[1] * c.nb[2];
     const size_t words = (bricks + 31) / 32;
     vkhr_status s = vkhr_reserve(ctx, (void**)&ctx->occ, &ctx->occ_cap, words, sizeof(uint32_t));
     if (s != VKHR_OK) return s;
     VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->occ, 0, words * sizeof(uint32_t), st));
-    VKHR_LAUNCH(ctx, occupancy_kernel<DF>, occupancy_blocks(c.res[0], c.res[1], c.res[2], ctx->sm_count), 128, 0, st, (const typename DensityTexel<DF>::T*)dens, c.res[0],
-                c.res[1], c.res[2], c.nb[0], c.nb[1], c.nb[2], ctx->occ);
+    {
+        const typename DensityTexel<DF>::T* dd = (const typename DensityTexel<DF>::T*)dens;
+        const int L = occupancy_lanes(c.res[0], c.res[1], c.res[2], ctx->sm_count);
+        const unsigned ob = occupancy_blocks(c.res[0], c.res[1], c.res[2], ctx->sm_count, L);
+        if (L == 8)
+            VKHR_LAUNCH(ctx, (occupancy_kernel<DF, 8>), ob, 128, 0, st, dd, c.res[0], c.res[1], c.res[2], c.nb[0], c.nb[1],
+                        c.nb[2], ctx->occ);
+        else
+            VKHR_LAUNCH(ctx, (occupancy_kernel<DF, 1>), ob, 128, 0, st, dd, c.res[0], c.res[1], c.res[2], c.nb[0], c.nb[1],
+                        c.nb[2], ctx->occ);
+    }
+    const int x0 = rect[0], y0 = rect[1], x1 = rect[0] + rect[2], y1 = rect[1] + rect[3];
+    float4* out = reinterpret_cast<float4*>(rgba);
+    const bool background = rect[2] < c.W || rect[3] < c.H;
+    if (background) { // disjoint pixels: on the side stream, alongside the march
+        s = vkhr_fork_side(ctx, st);
+        if (s != VKHR_OK) return s;
+        VKHR_LAUNCH(ctx, background_kernel, (unsigned)ctx->sm_count * 8, 256, 0, ctx->side, out, dout, c.W, c.H, x0, y0,
+                    x1, y1);
+    }
+    if (rect[2] <= 0 || rect[3] <= 0) return background ? vkhr_join_side(ctx, st) : VKHR_OK;
     const int v = ctx->ray_variant[DF][TF];
     const dim3 block(32 * kWarpsX * kWarpsY);
     const int tw = kRayVariants[v].tw, th = 32 / tw;
-    const dim3 grid((c.W + tw * kWarpsX - 1) / (tw * kWarpsX), (c.H + th * kWarpsY - 1) / (th * kWarpsY));
+    const dim3 grid((rect[2] + tw * kWarpsX - 1) / (tw * kWarpsX), (rect[3] + th * kWarpsY - 1) / (th * kWarpsY));
     const typename DensityTexel<DF>::T* d = (const typename DensityTexel<DF>::T*)dens;
-    float4* out = reinterpret_cast<float4*>(rgba);
+#define VKHR_RAY(TW_, MINB_)                                                                                      \
+    VKHR_LAUNCH(ctx, (raymarch_kernel<DF, TF, TW_, MINB_>), grid, block, 0, st, c, d, tang, ctx->occ, din, out, dout, x0, \
+                y0, x1, y1)
     switch (v) {
-    case 1: VKHR_LAUNCH(ctx, (raymarch_kernel<DF, TF, 16, 6>), grid, block, 0, st, c, d, tang, ctx->occ, din, out, dout); break;
-    case 2: VKHR_LAUNCH(ctx, (raymarch_kernel<DF, TF, 4, 6>), grid, block, 0, st, c, d, tang, ctx->occ, din, out, dout); break;
-    case 3: VKHR_LAUNCH(ctx, (raymarch_kernel<DF, TF, 8, 8>), grid, block, 0, st, c, d, tang, ctx->occ, din, out, dout); break;
-    default: VKHR_LAUNCH(ctx, (raymarch_kernel<DF, TF, 8, 6>), grid, block, 0, st, c, d, tang, ctx->occ, din, out, dout);
+    case 1: VKHR_RAY(16, 6); break;
+    case 2: VKHR_RAY(4, 6); break;
+    case 3: VKHR_RAY(8, 8); break;
+    default: VKHR_RAY(8, 6);
     }
-    return VKHR_OK;
+#undef VKHR_RAY
+    return background ? vkhr_join_side(ctx, st) : VKHR_OK;
 }
 
 } // namespace
@@ -187,19 +230,22 @@ extern "C" vkhr_status vkhr_raymarch(vkhr_ctx* ctx, const vkhr_raymarch_params* 
         return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_tangent is misaligned for its format");
     VKHR_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     cudaStream_t st = (cudaStream_t)stream;
+    int32_t rect[4]; // pixels outside it miss the volume's box
+    s = vkhr_raymarch_footprint(params, rect);
+    if (s != VKHR_OK) return vkhr_fail(ctx, s, "footprint of the view");
     const int df = params->density_format, tf = params->tangent_format;
     if (df == VKHR_DENSITY_U8_UNORM && tf == VKHR_TANGENT_I8_SNORM)
-        s = launch<VKHR_DENSITY_U8_UNORM, VKHR_TANGENT_I8_SNORM>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
+        s = launch<VKHR_DENSITY_U8_UNORM, VKHR_TANGENT_I8_SNORM>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, rect, st);
     else if (df == VKHR_DENSITY_U8_UNORM)
-        s = launch<VKHR_DENSITY_U8_UNORM, VKHR_TANGENT_F32X4>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
+        s = launch<VKHR_DENSITY_U8_UNORM, VKHR_TANGENT_F32X4>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, rect, st);
     else if (df == VKHR_DENSITY_U32_COUNT && tf == VKHR_TANGENT_I8_SNORM)
-        s = launch<VKHR_DENSITY_U32_COUNT, VKHR_TANGENT_I8_SNORM>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
+        s = launch<VKHR_DENSITY_U32_COUNT, VKHR_TANGENT_I8_SNORM>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, rect, st);
     else if (df == VKHR_DENSITY_U32_COUNT)
-        s = launch<VKHR_DENSITY_U32_COUNT, VKHR_TANGENT_F32X4>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
+        s = launch<VKHR_DENSITY_U32_COUNT, VKHR_TANGENT_F32X4>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, rect, st);
     else if (tf == VKHR_TANGENT_I8_SNORM)
-        s = launch<VKHR_DENSITY_F32, VKHR_TANGENT_I8_SNORM>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
+        s = launch<VKHR_DENSITY_F32, VKHR_TANGENT_I8_SNORM>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, rect, st);
     else
-        s = launch<VKHR_DENSITY_F32, VKHR_TANGENT_F32X4>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, st);
+        s = launch<VKHR_DENSITY_F32, VKHR_TANGENT_F32X4>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, rect, st);
     VKHR_CUDA_TRY(ctx, cudaGetLastError());
     return VKHR_OK;
 }
@@ -453,17 +499,29 @@ cudaError_t g_static_error[kMaxStaticDevices];
 
 template <int DF, int TF>
 cudaError_t launch_static(const RayConsts& c, const void* dens, const void* tang, const float* din, float* rgba,
-                          float* dout, uint32_t* occ, size_t words, int sm_count, cudaStream_t st)
+                          float* dout, uint32_t* occ, size_t words, int sm_count, const int32_t rect[4], cudaStream_t st)
 {
     // the array keeps the previous call's bits: clear the part this grid uses
     cudaError_t e = cudaMemsetAsync(occ, 0, words * sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
-    occupancy_kernel<DF><<<occupancy_blocks(c.res[0], c.res[1], c.res[2], sm_count), 128, 0, st>>>((const typename DensityTexel<DF>::T*)dens, c.res[0], c.res[1],
-                                                   c.res[2], c.nb[0], c.nb[1], c.nb[2], occ);
-    const dim3 block(32 * kWarpsX * kWarpsY);
-    const dim3 grid((c.W + kTileW * kWarpsX - 1) / (kTileW * kWarpsX), (c.H + kTileH * kWarpsY - 1) / (kTileH * kWarpsY));
-    raymarch_kernel<DF, TF><<<grid, block, 0, st>>>(c, (const typename DensityTexel<DF>::T*)dens, tang, occ, din,
-                                                     reinterpret_cast<float4*>(rgba), dout);
+    const typename DensityTexel<DF>::T* dd = (const typename DensityTexel<DF>::T*)dens;
+    const int L = occupancy_lanes(c.res[0], c.res[1], c.res[2], sm_count);
+    const unsigned ob = occupancy_blocks(c.res[0], c.res[1], c.res[2], sm_count, L);
+    if (L == 8)
+        occupancy_kernel<DF, 8><<<ob, 128, 0, st>>>(dd, c.res[0], c.res[1], c.res[2], c.nb[0], c.nb[1], c.nb[2], occ);
+    else
+        occupancy_kernel<DF, 1><<<ob, 128, 0, st>>>(dd, c.res[0], c.res[1], c.res[2], c.nb[0], c.nb[1], c.nb[2], occ);
+    const int x0 = rect[0], y0 = rect[1], x1 = rect[0] + rect[2], y1 = rect[1] + rect[3];
+    float4* out = reinterpret_cast<float4*>(rgba);
+    if (rect[2] < c.W || rect[3] < c.H)
+        background_kernel<<<(unsigned)sm_count * 8, 256, 0, st>>>(out, dout, c.W, c.H, x0, y0, x1, y1);
+    if (rect[2] > 0 && rect[3] > 0) {
+        const dim3 block(32 * kWarpsX * kWarpsY);
+        const dim3 grid((rect[2] + kTileW * kWarpsX - 1) / (kTileW * kWarpsX),
+                        (rect[3] + kTileH * kWarpsY - 1) / (kTileH * kWarpsY));
+        raymarch_kernel<DF, TF><<<grid, block, 0, st>>>(c, (const typename DensityTexel<DF>::T*)dens, tang, occ, din,
+                                                         out, dout, x0, y0, x1, y1);
+    }
     return cudaGetLastError();
 }
 
@@ -494,22 +552,24 @@ extern "C" vkhr_status vkhr_raymarch_static(const vkhr_raymarch_params* params, 
         g_static_error[dev] = e;
     });
     if (g_static_error[dev] != cudaSuccess) return VKHR_ERR_CUDA;
+    int32_t rect[4]; // pixels outside it miss the volume's box
+    if (vkhr_raymarch_footprint(params, rect) != VKHR_OK) return VKHR_ERR_INVALID_ARG;
     uint32_t* occ = g_static_occupancy_ptr[dev];
     const int sms = g_static_sm_count[dev];
     cudaStream_t st = (cudaStream_t)stream;
     const int df = params->density_format, tf = params->tangent_format;
     cudaError_t e;
     if (df == VKHR_DENSITY_U8_UNORM && tf == VKHR_TANGENT_I8_SNORM)
-        e = launch_static<VKHR_DENSITY_U8_UNORM, VKHR_TANGENT_I8_SNORM>(c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, occ, words, sms, st);
+        e = launch_static<VKHR_DENSITY_U8_UNORM, VKHR_TANGENT_I8_SNORM>(c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, occ, words, sms, rect, st);
     else if (df == VKHR_DENSITY_U8_UNORM)
-        e = launch_static<VKHR_DENSITY_U8_UNORM, VKHR_TANGENT_F32X4>(c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, occ, words, sms, st);
+        e = launch_static<VKHR_DENSITY_U8_UNORM, VKHR_TANGENT_F32X4>(c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, occ, words, sms, rect, st);
     else if (df == VKHR_DENSITY_U32_COUNT && tf == VKHR_TANGENT_I8_SNORM)
-        e = launch_static<VKHR_DENSITY_U32_COUNT, VKHR_TANGENT_I8_SNORM>(c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, occ, words, sms, st);
+        e = launch_static<VKHR_DENSITY_U32_COUNT, VKHR_TANGENT_I8_SNORM>(c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, occ, words, sms, rect, st);
     else if (df == VKHR_DENSITY_U32_COUNT)
-        e = launch_static<VKHR_DENSITY_U32_COUNT, VKHR_TANGENT_F32X4>(c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, occ, words, sms, st);
+        e = launch_static<VKHR_DENSITY_U32_COUNT, VKHR_TANGENT_F32X4>(c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, occ, words, sms, rect, st);
     else if (tf == VKHR_TANGENT_I8_SNORM)
-        e = launch_static<VKHR_DENSITY_F32, VKHR_TANGENT_I8_SNORM>(c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, occ, words, sms, st);
+        e = launch_static<VKHR_DENSITY_F32, VKHR_TANGENT_I8_SNORM>(c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, occ, words, sms, rect, st);
     else
-        e = launch_static<VKHR_DENSITY_F32, VKHR_TANGENT_F32X4>(c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, occ, words, sms, st);
+        e = launch_static<VKHR_DENSITY_F32, VKHR_TANGENT_F32X4>(c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, occ, words, sms, rect, st);
     return e == cudaSuccess ? VKHR_OK : VKHR_ERR_CUDA;
 }
