@@ -57,7 +57,7 @@ TRAFFIC = {
     "brick_kernel<SEG, TANG, false": 158_595_328 + 38_296_576,
     "bin_kernel<true": 55_134_208 + 72_237_312,
     "bin_kernel<false": 55_694_080 + 24_500_992,
-    "raymarch_kernel": 8_216_576 + 51_968,
+    "raymarch_kernel": 8_215_040 + 0,
 }
 
 METRIC = "Msegments/s voxelized + Mpixels/s raymarched, 1 GB300 (frame throughput in Mpixels/s)"
