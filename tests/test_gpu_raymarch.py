@@ -122,6 +122,33 @@ def test_depth_buffer_breaks_rays(ctx, oracle_lib):
     _compare(gpu, gdepth, ref, rdepth, diag)
 
 
+@pytest.mark.parametrize("shift", [(0.0, 0.0, 0.0), (0.9, 0.4, 0.0)])
+def test_footprint_launch_every_pixel(ctx, oracle_lib, shift):
+    """The march kernel covers only the volume's screen footprint and a
+    background kernel writes the other pixels: every pixel is written, those
+    outside the footprint are background (RGBA 0, depth 1), and the whole
+    image matches the oracle, which marches every pixel -- also for a view
+    whose volume straddles the image's edge (shifted look-at point)."""
+    from vkhr_gb300 import _native
+
+    res = (48, 48, 48)
+    b, c, dn, tq = _volume(oracle_lib, "hemi", 3000, 12, res)
+    o, sz = np.asarray(b.origin, dtype=np.float64), np.asarray(b.size, dtype=np.float64)
+    target = o + 0.5 * sz + np.asarray(shift) * sz
+    p = scene.make_params(b, res, 160, 120, raycast_steps=128.0, shadow_steps=32.0, view_direction=(0.3, 0.2, 1.0),
+                          target=target)
+    x0, y0, w, h = _native.raymarch_footprint(p)
+    assert 0 < w * h < 160 * 120  # a proper part of the view
+    gpu, gdepth = _gpu_raymarch(ctx, p, dn, tq)
+    assert (gpu != -7.0).all() and (gdepth != -7.0).all()
+    outside = np.ones((120, 160), dtype=bool)
+    outside[y0:y0 + h, x0:x0 + w] = False
+    assert not gpu[outside].any() and np.all(gdepth[outside] == 1.0)
+    ref, rdepth, diag = oracle_lib.raymarch(p, dn, tq, diag=True)
+    assert not ref[outside].any()
+    _compare(gpu, gdepth, ref, rdepth, diag)
+
+
 def test_camera_inside_volume_covers_nothing(ctx, oracle_lib):
     b, c, dn, tq = _volume(oracle_lib, "hemi", 1024, 8, (32, 32, 32))
     p = scene.make_params(b, (32, 32, 32), 64, 48, camera_distance=0.1, raycast_steps=64.0)
