@@ -524,6 +524,81 @@ def diff_section(args, dev, stream, flush):
     return out
 
 
+def frame_graph_section(args, dev, stream, flush, st, t, idx, b, res, p):
+    """The per-frame path as one CUDA graph (vkhr_frame_graph_*): the
+    production style voxelized under a visit budget, normalized and
+    raymarched, replayed per frame.  Device time with inputs resident, and
+    end to end with each frame's swayed vertices and tangents uploaded and
+    the image read back (serial)."""
+    import torch
+
+    from vkhr_gb300 import _abi, _native, strands, workloads
+
+    ctx = _native.Context(dev.index)
+    s = stream.cuda_stream
+    n = res[0] * res[1] * res[2]
+    W, H = p.width, p.height
+    dv = torch.from_numpy(st.vertices).to(dev)
+    dt = torch.from_numpy(t).to(dev)
+    di = torch.from_numpy(idx.view(np.int32)).to(dev)
+    counts = torch.empty(n, dtype=torch.int32, device=dev)
+    dens = torch.empty(n, dtype=torch.uint8, device=dev)
+    tq = torch.empty((n, 4), dtype=torch.int8, device=dev)
+    rgba = torch.empty((H, W, 4), dtype=torch.float32, device=dev)
+    depth = torch.empty((H, W), dtype=torch.float32, device=dev)
+    job = _abi.VoxelJob()
+    job.d_vertices, job.d_tangent_in, job.d_indices = dv.data_ptr(), dt.data_ptr(), di.data_ptr()
+    job.item_count = idx.shape[0]
+    job.bounds = b
+    job.width, job.height, job.depth = res
+    job.index_mode = _abi.INDEX_REF_FP32
+    job.d_counts, job.d_densities, job.d_tangents = counts.data_ptr(), dens.data_ptr(), tq.data_ptr()
+    graph = ctx.frame_graph(True, job, p, rgba.data_ptr(), depth.data_ptr(), stream=s)
+    # two frames of motion, alternated: the style as loaded and swayed (inside the same bounds)
+    v1 = workloads.sway(st.vertices, 0.02)
+    v1 = np.clip(v1, np.asarray(b.origin, dtype=np.float32),
+                 (np.asarray(b.origin, dtype=np.float64) + np.asarray(b.size, dtype=np.float64)).astype(np.float32))
+    hv = [torch.from_numpy(st.vertices).pin_memory(), torch.from_numpy(v1).pin_memory()]
+    ht = [torch.from_numpy(t).pin_memory(), torch.from_numpy(strands.generate_tangents(v1, st.segments)).pin_memory()]
+    ho = torch.empty((H, W, 4), dtype=torch.float32).pin_memory()
+    hd = torch.empty((H, W), dtype=torch.float32).pin_memory()
+    for _ in range(max(args.warmup, 3)):
+        flush.zero_()
+        graph.launch(s)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for k in range(args.steps):
+        flush.zero_()
+        ev[k][0].record(stream)
+        graph.launch(s)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    dev_ms = sum(a.elapsed_time(z) for a, z in ev) / args.steps
+    for k in range(args.steps + 2):
+        if k >= 2:
+            ev[k - 2][0].record(stream)
+        dv.copy_(hv[k % 2], non_blocking=True)
+        dt.copy_(ht[k % 2], non_blocking=True)
+        graph.launch(s)
+        ho.copy_(rgba, non_blocking=True)
+        hd.copy_(depth, non_blocking=True)
+        if k >= 2:
+            ev[k - 2][1].record(stream)
+        torch.cuda.synchronize()
+    e2e_ms = sum(a.elapsed_time(z) for a, z in ev) / args.steps
+    ctx.check_status(s)
+    graph.close()
+    ctx.close()
+    return {
+        "config": {"workload": "the production frame as one CUDA graph per frame: voxelize (segments, visit budget = "
+                               "1.25x the first frame's visits), normalize, occupancy, raymarch 1920x1080; e2e: "
+                               "each frame uploads its swayed vertices and tangents and reads the image back, serial"},
+        "ms": dev_ms, "mpixels_per_s": W * H / dev_ms / 1e3,
+        "e2e_ms": e2e_ms, "e2e_mpixels_per_s": W * H / e2e_ms / 1e3,
+        "h2d_bytes_per_step": hv[0].numel() * 4 + ht[0].numel() * 4, "d2h_bytes_per_step": ho.numel() * 4 + hd.numel() * 4,
+    }
+
+
 def gb300_arm(args):
     import torch
 
@@ -754,6 +829,8 @@ def gb300_arm(args):
 
     batched = None if (args.no_batched or args.section == "frame") else batched_comparison(
         args, dev, stream, rank, world, flush)
+    frame_graph = None if (args.section == "frame" or world > 1) else frame_graph_section(
+        args, dev, stream, flush, st, t, idx, b, res, p)
     scale = None if (args.no_scale or args.section == "frame" or world > 1) else scale_section(args, dev, stream, flush)
     diff = None if (args.no_diff or args.section == "frame" or world > 1) else diff_section(args, dev, stream, flush)
 
@@ -784,6 +861,8 @@ def gb300_arm(args):
     }
     if batched is not None:
         line["batched"] = batched
+    if frame_graph is not None:
+        line["frame_graph"] = frame_graph
     if scale is not None:
         line["scale"] = scale
     if diff is not None:

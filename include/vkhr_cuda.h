@@ -412,6 +412,32 @@ vkhr_status vkhr_splat_vertices_adjoint(vkhr_ctx* ctx, const float* d_vertices, 
 vkhr_status vkhr_raymarch_static(const vkhr_raymarch_params* params, const void* d_density, const void* d_tangent,
                                  const float* d_depth_in, float* d_rgba, float* d_depth_out, void* stream);
 
+/* Per-frame voxelization feeding the raymarcher without a host round trip:
+ * one CUDA graph of a style's voxelization (rasterizer.cc:216-230, the
+ * per-frame voxelize pass of the paper), optionally Volume::normalize, the
+ * brick-occupancy pass and the raymarch of one view (volume.cc:104-112).
+ * Create captures the three calls once; launch replays them on a stream.
+ * Between launches the caller rewrites the job's input buffers in place (a
+ * hair simulation moving the vertices and tangents); every pointer, the
+ * bounds, the sizes and the view stay those of create.
+ *   - visit_budget: the visit capacity of every frame (see
+ *     vkhr_set_visit_budget); 0 counts this frame's visits once (a host read)
+ *     and uses 1.25x that.  A frame above it reports VKHR_ERR_CAPACITY from
+ *     vkhr_check_status.  The context keeps the budget.
+ *   - Create makes one uncaptured frame (so every scratch buffer has its
+ *     size) and synchronises `stream`; launch never allocates or syncs.
+ *   - The graph reads the context's staged job table at every replay: while
+ *     it is in use the context runs no other voxelization.
+ *   - No reference counterpart as an API (the reference re-records command
+ *     buffers per frame). */
+typedef struct vkhr_frame_graph vkhr_frame_graph;
+
+vkhr_status vkhr_frame_graph_create(vkhr_ctx* ctx, int32_t segments, const vkhr_voxel_job* job, int32_t normalize,
+                                    uint64_t visit_budget, const vkhr_raymarch_params* params, const float* d_depth_in,
+                                    float* d_rgba, float* d_depth_out, void* stream, vkhr_frame_graph** out);
+vkhr_status vkhr_frame_graph_launch(vkhr_frame_graph* graph, void* stream);
+vkhr_status vkhr_frame_graph_destroy(vkhr_frame_graph* graph);
+
 #ifdef __cplusplus
 }
 #endif

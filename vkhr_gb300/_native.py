@@ -21,6 +21,7 @@ EXPORTS = [
     "vkhr_raymarch_batched", "vkhr_raymarch_footprint", "vkhr_sizeof_raymarch_job",
     "vkhr_downsample_densities", "vkhr_raymarch_tape_bytes", "vkhr_raymarch_train", "vkhr_raymarch_adjoint",
     "vkhr_splat_vertices", "vkhr_splat_vertices_adjoint", "vkhr_autotune_raymarch", "vkhr_set_raymarch_variant",
+    "vkhr_frame_graph_create", "vkhr_frame_graph_launch", "vkhr_frame_graph_destroy",
 ]
 
 _lib = None
@@ -74,6 +75,10 @@ def load():
     lib.vkhr_splat_vertices_adjoint.argtypes = [P, P, C.c_uint32, C.POINTER(_abi.AABB), C.c_int32, C.c_int32,
                                                 C.c_int32, P, P, P]
     lib.vkhr_check_status.argtypes = [P, P]
+    lib.vkhr_frame_graph_create.argtypes = [P, C.c_int32, C.POINTER(_abi.VoxelJob), C.c_int32, C.c_uint64,
+                                            C.POINTER(_abi.RaymarchParams), P, P, P, P, C.POINTER(C.c_void_p)]
+    lib.vkhr_frame_graph_launch.argtypes = [P, P]
+    lib.vkhr_frame_graph_destroy.argtypes = [P]
     lib.vkhr_raymarch.argtypes = [P, C.POINTER(_abi.RaymarchParams), P, P, P, P, P, P]
     lib.vkhr_malloc.argtypes = [P, C.c_size_t, C.POINTER(C.c_void_p)]
     lib.vkhr_free.argtypes = [P, P]
@@ -94,6 +99,27 @@ def load():
             getattr(lib, name).restype = C.c_int
     _lib = lib
     return lib
+
+
+class FrameGraph:
+    """A captured frame (vkhr_frame_graph_*): launch() replays it on a stream."""
+
+    def __init__(self, ctx, handle):
+        self.ctx, self.handle = ctx, handle
+
+    def launch(self, stream=None):
+        self.ctx.check(self.ctx.lib.vkhr_frame_graph_launch(self.handle, stream))
+
+    def close(self):
+        if self.handle:
+            self.ctx.lib.vkhr_frame_graph_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Context:
@@ -171,6 +197,16 @@ class Context:
         """jobs: a sequence of _abi.VoxelJob (item_count = vertex or index count)."""
         arr = (_abi.VoxelJob * len(jobs))(*jobs)
         self.check(self.lib.vkhr_voxelize_batched(self.handle, 1 if segments else 0, arr, len(jobs), stream))
+
+    def frame_graph(self, segments, job, params, d_rgba, d_depth_out=None, d_depth_in=None, normalize=True,
+                    visit_budget=0, stream=None):
+        """vkhr_frame_graph_create: one CUDA graph of the job's voxelization,
+        Volume::normalize and the view's raymarch; FrameGraph.launch replays it."""
+        h = C.c_void_p()
+        self.check(self.lib.vkhr_frame_graph_create(self.handle, 1 if segments else 0, C.byref(job),
+                                                    1 if normalize else 0, int(visit_budget), C.byref(params),
+                                                    d_depth_in, d_rgba, d_depth_out, stream, C.byref(h)))
+        return FrameGraph(self, h)
 
     def raymarch_batched(self, jobs, stream=None):
         """jobs: a sequence of _abi.RaymarchJob."""

@@ -61,3 +61,16 @@ def shelf_pack(rects, width):
         x += w
         row_h = max(row_h, h)
     return pos, y + row_h
+
+
+def sway(vertices, amount):
+    """One step of simulated motion: the strands swayed along x by `amount`
+    (world units) times the square of each vertex's relative height."""
+    import numpy as np
+
+    v = np.asarray(vertices, dtype=np.float64)
+    y = v[:, 1]
+    h = (y - y.min()) / max(float(y.max() - y.min()), 1e-6)
+    out = v.copy()
+    out[:, 0] += amount * h * h
+    return out.astype(np.float32)
