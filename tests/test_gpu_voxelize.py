@@ -59,6 +59,34 @@ def test_one_walk_slices_and_compact_fallback(native_lib, oracle_lib):
         c.close()
 
 
+def test_budgeted_one_walk_device_fallback(native_lib, oracle_lib):
+    """Under a visit budget (no read-back; capturable) a context that knows a
+    per-brick capacity still walks once, and the device picks the layout: a
+    style whose largest brick fits reads the fixed slices, one whose largest
+    brick outgrew them is filled compactly by the (otherwise idle) fill pass.
+    Both bit-exact."""
+    from vkhr_gb300 import _native
+
+    c = _native.Context(0)
+    try:
+        sparse = style("hemi", 2048, 12)
+        dense = style("disk", 40_000, 13)  # largest brick 30,553 visits: far above the learned capacity
+        res = (96, 96, 96)
+
+        def run(s):
+            st, t, idx = s
+            b = oracle_lib.bounding_box(st.vertices)
+            _check(c, oracle_lib, "segments", st.vertices, t, idx, b, res)
+
+        run(sparse)                  # no budget: learns a capacity of 384 visits per brick
+        c.set_visit_budget(4_000_000)
+        run(sparse)                  # budgeted, fits: the fixed slices
+        run(dense)                   # budgeted, a brick outgrew its slice: the device fills compactly
+        run(sparse)
+    finally:
+        c.close()
+
+
 @pytest.mark.parametrize("mode", ["vertices", "segments"])
 def test_production_style_256(ctx, oracle_lib, mode):
     """136,320 strands x 13 vertices (1,635,840 segments) into 256^3, full size."""

@@ -295,8 +295,12 @@ __device__ __forceinline__ void emit_run(uint32_t b, uint32_t key, uint64_t loca
 template <bool FILL, bool SEG, bool PACK, bool SINGLE, bool SPREAD = false, bool DIRECT = false>
 __global__ void bin_kernel(const __grid_constant__ VoxJob job0, const VoxJob* __restrict__ jobs, int nj,
                            uint32_t total_items, float4* pair_rec, float4* pair_tan, uint32_t* visits,
-                           uint32_t* cursor, void* entries_raw, size_t entries_cap, unsigned long long* words)
+                           uint32_t* cursor, void* entries_raw, size_t entries_cap, unsigned long long* words,
+                           uint32_t skip_if_fits)
 {
+    // a budgeted one-walk call's fill: needed only when a brick outgrew the
+    // fixed slices of capacity skip_if_fits (0: always fill)
+    if (FILL && skip_if_fits && words[WORD_MAX_BRICK_VISITS] <= skip_if_fits) return;
     typename Entry<PACK>::T* entries = reinterpret_cast<typename Entry<PACK>::T*>(entries_raw);
     // the job table in shared memory (nj * (sizeof(VoxJob) + 4) bytes of dynamic shared memory)
     extern __shared__ __align__(16) unsigned char bin_smem[];
@@ -703,12 +707,25 @@ template <bool SEG, bool TANG, bool BIG, bool PACK>
 __global__ void __launch_bounds__(kBrickThreads, 2)
 brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__ pair_tan_all,
              const uint32_t* __restrict__ visits, const uint32_t* __restrict__ cursor, const uint32_t* __restrict__ list,
-             uint32_t list_n, const void* __restrict__ entries_raw, size_t entries_cap, uint32_t direct_cap,
-             uint4* hdesc, size_t hdesc_cap, uint32_t* hkeys, size_t hkeys_cap, unsigned long long* words)
+             uint32_t list_n, const void* __restrict__ entries_raw, size_t entries_cap,
+             const void* __restrict__ slots_raw, uint32_t direct_cap, int speculative, uint4* hdesc, size_t hdesc_cap,
+             uint32_t* hkeys, size_t hkeys_cap, unsigned long long* words)
 {
     typedef Entry<PACK> E;
     typedef typename E::T ET;
-    const ET* __restrict__ entries = reinterpret_cast<const ET*>(entries_raw);
+    // The layout, chosen once into shared memory (kept out of registers).
+    // speculative: a budgeted one-walk call, whose largest brick only the
+    // device knows -- the fixed slices hold every brick's entries when it
+    // fits their capacity, else the fill pass has laid them out compactly.
+    __shared__ const ET* s_entries;
+    __shared__ unsigned long long s_entries_cap;
+    __shared__ uint32_t s_dcap;
+    if (threadIdx.x == 0) {
+        const uint32_t d = speculative && words[WORD_MAX_BRICK_VISITS] > direct_cap ? 0u : direct_cap;
+        s_dcap = d;
+        s_entries = reinterpret_cast<const ET*>(d ? slots_raw : entries_raw);
+        s_entries_cap = d ? (unsigned long long)list_n * d : (unsigned long long)entries_cap; // fixed slices
+    }
     extern __shared__ uint32_t sm[];
     uint32_t* cnt = sm;                       // visits per local voxel
     uint32_t* off = sm + kBrickThreads;       // slice cursor per local voxel
@@ -729,7 +746,7 @@ brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__
         if (nq < listed) {
             ngb = BIG ? list[list_n - 1 - nq] : list[nq];
             nnv = visits[ngb];
-            nstart = direct_cap ? ngb * direct_cap : cursor[ngb] - nnv;
+            nstart = s_dcap ? ngb * s_dcap : cursor[ngb] - nnv;
         }
     }
     for (;;) {
@@ -748,15 +765,15 @@ brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__
         __syncthreads();
         const uint32_t gb = s_gb, nv = s_nv, start = s_start;
         if (gb == 0xffffffffu) break;
-        const bool skip = (uint64_t)start + nv > entries_cap ||                 // visit budget exceeded
-                          (direct_cap && nv > direct_cap) ||                    // past its fixed slice
+        const bool skip = (uint64_t)start + nv > s_entries_cap ||               // visit budget exceeded
+                          (s_dcap && nv > s_dcap) ||                            // past its fixed slice
                           (TANG && BIG && (uint64_t)s_hb + nv > hkeys_cap);     // key scratch exhausted
         if (skip) {
             status |= VKHR_DEV_LIST_OVERFLOW;
             if (tid == 0 && nq < listed) {
                 ngb = BIG ? list[list_n - 1 - nq] : list[nq];
                 nnv = visits[ngb];
-                nstart = direct_cap ? ngb * direct_cap : cursor[ngb] - nnv;
+                nstart = s_dcap ? ngb * s_dcap : cursor[ngb] - nnv;
             }
         } else {
             const VoxJob& J = jobs[s_job];
@@ -764,7 +781,7 @@ brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__
             const uint32_t b = gb - J.brick_base;   // brick within the style's grid
             const float4* pair_tan = pair_tan_all + J.item_base;
             uint32_t* kbase = BIG ? hkeys + s_hb : keys;
-            const ET* src = entries + start;
+            const ET* src = s_entries + start;
             for (uint32_t i0 = tid; i0 < nv; i0 += kBrickThreads * kBrickUnroll) {
                 ET e[kBrickUnroll];
 #pragma unroll
@@ -777,7 +794,7 @@ brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__
             if (tid == 0 && nq < listed) { // the next brick's bounds, while this one's passes run
                 ngb = BIG ? list[list_n - 1 - nq] : list[nq];
                 nnv = visits[ngb];
-                nstart = direct_cap ? ngb * direct_cap : cursor[ngb] - nnv;
+                nstart = s_dcap ? ngb * s_dcap : cursor[ngb] - nnv;
             }
             __syncthreads();
             if (TANG) {
@@ -1198,8 +1215,9 @@ vkhr_status check_device_status(vkhr_ctx* ctx, unsigned long long s)
 
 template <bool SEG, bool TANG, bool PACK>
 vkhr_status launch_brick(vkhr_ctx* ctx, const VoxJob* d_jobs, int nj, uint32_t total_bricks, cudaStream_t st,
-                         unsigned blocks, size_t entries_cap, size_t keys_cap, uint32_t direct_cap)
+                         unsigned blocks, size_t entries_cap, size_t keys_cap, uint32_t direct_cap, bool speculative)
 {
+    const int spec = speculative ? 1 : 0;
     // bricks above kBrickCap (their keys go to the global scratch) on the side
     // stream, alongside the rest on st; the caller joins the side stream
     const size_t small = (size_t)(2 * kBrickThreads + 32 + kBrickThreads) * sizeof(uint32_t);
@@ -1208,12 +1226,13 @@ vkhr_status launch_brick(vkhr_ctx* ctx, const VoxJob* d_jobs, int nj, uint32_t t
     if (s != VKHR_OK) return s;
     VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG, true, PACK>), (unsigned)ctx->sm_count * 2, kBrickThreads, small, ctx->side,
                 d_jobs, nj, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->brick_list, total_bricks,
-                ctx->items, entries_cap, direct_cap, ctx->hdesc, ctx->hdesc_cap, ctx->hkeys, keys_cap, ctx->d_words);
+                ctx->items, entries_cap, ctx->slots, direct_cap, spec, ctx->hdesc, ctx->hdesc_cap, ctx->hkeys, keys_cap,
+                ctx->d_words);
     VKHR_CUDA_TRY(ctx, cudaFuncSetAttribute(brick_kernel<SEG, TANG, false, PACK>,
                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG, false, PACK>), blocks, kBrickThreads, smem, st, d_jobs, nj,
                 ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->brick_list, total_bricks, ctx->items,
-                entries_cap, direct_cap, ctx->hdesc, ctx->hdesc_cap, ctx->hkeys, keys_cap, ctx->d_words);
+                entries_cap, ctx->slots, direct_cap, spec, ctx->hdesc, ctx->hdesc_cap, ctx->hkeys, keys_cap, ctx->d_words);
     return VKHR_OK;
 }
 
@@ -1310,22 +1329,26 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
         s = vkhr_reserve(ctx, (void**)&ctx->items, &ctx->items_cap, visits_total ? visits_total : 1, sizeof(uint2));
         if (s != VKHR_OK) return s;
     }
-    // One walk instead of two: segment mode without a budget reads its visit
-    // total back anyway, so when the context knows a per-brick capacity (from
-    // its earlier calls' largest brick) and the fixed slices fit in memory,
+    // One walk instead of two: when the context knows a per-brick capacity
+    // (its earlier calls' largest brick) and the fixed slices fit in memory,
     // the counting walk also writes every run into its brick's slice
-    // [brick * capacity, + count).  A brick past the capacity shows in the
-    // read-back; the call then fills again in the compact layout.
+    // [brick * capacity, + count) of a separate buffer.  A brick past the
+    // capacity is counted but not written.  Without a budget the visit
+    // read-back shows it and the call fills again compactly; with a budget
+    // (one style; no read-back, the call may be captured) the device decides:
+    // the fill pass runs only if the largest brick outgrew the capacity, and
+    // the brick kernel reads whichever layout holds the entries.
     const size_t entry_bytes = pack ? sizeof(uint32_t) : sizeof(uint2);
     uint32_t direct_cap = 0;
-    if (!bounded && total_items && ctx->direct_cap) {
+    if (segments && total_items && ctx->direct_cap && (!bounded || nj == 1)) {
         const uint64_t slots = (uint64_t)total_bricks * ctx->direct_cap;
         if (slots < (1ull << 32) && slots * entry_bytes <= kDirectBytes) {
-            s = vkhr_reserve(ctx, (void**)&ctx->items, &ctx->items_cap, (slots * entry_bytes + 7) / 8, sizeof(uint2));
+            s = vkhr_reserve(ctx, (void**)&ctx->slots, &ctx->slots_cap, (slots * entry_bytes + 7) / 8, sizeof(uint2));
             if (s != VKHR_OK) return s;
             direct_cap = ctx->direct_cap;
         }
     }
+    const bool speculative = bounded && direct_cap != 0; // the device picks the layout
     VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_words, 0, WORD_NORM * sizeof(unsigned long long), st));
     VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->brick_visits, 0, (size_t)total_bricks * sizeof(uint32_t), st));
     const unsigned threads = 256;
@@ -1341,11 +1364,11 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
         if (single)                                                                                              \
             VKHR_LAUNCH(ctx, (bin_kernel<false, true, PACK_, true, false, true>), in_blocks, threads, 0, st,       \
                         jobs[0], d_jobs, nj, total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits,        \
-                        ctx->brick_cursor, ctx->items, (size_t)direct_cap, ctx->d_words);                         \
+                        ctx->brick_cursor, ctx->slots, (size_t)direct_cap, ctx->d_words, 0u);                         \
         else                                                                                                     \
             VKHR_LAUNCH(ctx, (bin_kernel<false, true, PACK_, false, false, true>), in_blocks, threads,             \
                         bin_smem_bytes, st, jobs[0], d_jobs, nj, total_items, ctx->pair_rec, ctx->pair_tan,       \
-                        ctx->brick_visits, ctx->brick_cursor, ctx->items, (size_t)direct_cap, ctx->d_words);      \
+                        ctx->brick_visits, ctx->brick_cursor, ctx->slots, (size_t)direct_cap, ctx->d_words, 0u);      \
     } while (0)
     if (total_items && direct_cap) {
         if (pack) VKHR_DIRECT(true);
@@ -1354,19 +1377,19 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
         if (segments && single)
             VKHR_LAUNCH(ctx, (bin_kernel<false, true, false, true>), in_blocks, threads, 0, st, jobs[0], d_jobs, nj,
                         total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, nullptr,
-                        (size_t)0, ctx->d_words);
+                        (size_t)0, ctx->d_words, 0u);
         else if (segments)
             VKHR_LAUNCH(ctx, (bin_kernel<false, true, false, false>), in_blocks, threads, bin_smem_bytes, st, jobs[0],
                         d_jobs, nj, total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor,
-                        nullptr, (size_t)0, ctx->d_words);
+                        nullptr, (size_t)0, ctx->d_words, 0u);
         else if (single)
             VKHR_LAUNCH(ctx, (bin_kernel<false, false, false, true>), in_blocks, threads, 0, st, jobs[0], d_jobs, nj,
                         total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, nullptr,
-                        (size_t)0, ctx->d_words);
+                        (size_t)0, ctx->d_words, 0u);
         else
             VKHR_LAUNCH(ctx, (bin_kernel<false, false, false, false>), in_blocks, threads, bin_smem_bytes, st, jobs[0],
                         d_jobs, nj, total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor,
-                        nullptr, (size_t)0, ctx->d_words);
+                        nullptr, (size_t)0, ctx->d_words, 0u);
     }
 #undef VKHR_DIRECT
     const unsigned rblocks = std::min(vkhr_blocks(total_bricks, kRangeThreads * kRangeItems), (unsigned)ctx->sm_count * 8);
@@ -1411,8 +1434,9 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
     if (s != VKHR_OK) return s;
     VKHR_LAUNCH(ctx, zero_empty_kernel, std::min(vkhr_blocks(total_groups, 256), (unsigned)ctx->sm_count * 16), 256, 0,
                 ctx->side, d_jobs, nj, total_groups, ctx->brick_visits);
-    if (total_items && !direct_cap) {
+    if (total_items && (!direct_cap || speculative)) {
         void* ent = ctx->items;
+        const uint32_t skip_if_fits = speculative ? direct_cap : 0u; // the fill is the fallback
         // spread a one-style fill's warps over distant strands when its visit
         // list is within twice the L2 size: most scattered entry stores still
         // merge in L2 (measured: a 123 MB list gains, a 1.8 GB list loses)
@@ -1423,15 +1447,15 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
         if (single && SEG_ && spread)                                                                            \
             VKHR_LAUNCH(ctx, (bin_kernel<true, SEG_, PACK_, true, true>), in_blocks, threads, 0, st, jobs[0],      \
                         d_jobs, nj, total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits,                 \
-                        ctx->brick_cursor, ent, cap_visits, ctx->d_words);                                        \
+                        ctx->brick_cursor, ent, cap_visits, ctx->d_words, skip_if_fits);                          \
         else if (single)                                                                                         \
             VKHR_LAUNCH(ctx, (bin_kernel<true, SEG_, PACK_, true>), in_blocks, threads, 0, st, jobs[0], d_jobs, nj,  \
                         total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ent,     \
-                        cap_visits, ctx->d_words);                                                                \
+                        cap_visits, ctx->d_words, skip_if_fits);                                                  \
         else                                                                                                     \
             VKHR_LAUNCH(ctx, (bin_kernel<true, SEG_, PACK_, false>), in_blocks, threads, bin_smem_bytes, st,       \
                         jobs[0], d_jobs, nj, total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits,        \
-                        ctx->brick_cursor, ent, cap_visits, ctx->d_words);                                        \
+                        ctx->brick_cursor, ent, cap_visits, ctx->d_words, skip_if_fits);                          \
     } while (0)
         if (segments && pack) VKHR_FILL(true, true);
         else if (segments) VKHR_FILL(true, false);
@@ -1440,9 +1464,9 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
 #undef VKHR_FILL
     }
     const unsigned bblocks = std::min(total_bricks, (unsigned)ctx->sm_count * 2);
-    const size_t entries_cap = direct_cap ? (size_t)total_bricks * direct_cap : cap_visits;
 #define VKHR_BRICK(SEG_, TANG_, PACK_)                                                                            \
-    launch_brick<SEG_, TANG_, PACK_>(ctx, d_jobs, nj, total_bricks, st, bblocks, entries_cap, cap_visits, direct_cap)
+    launch_brick<SEG_, TANG_, PACK_>(ctx, d_jobs, nj, total_bricks, st, bblocks, cap_visits, cap_visits, direct_cap,     \
+                                     speculative)
     if (segments) {
         if (!tang) s = VKHR_BRICK(true, false, true);
         else if (pack) s = VKHR_BRICK(true, true, true);
