@@ -438,6 +438,65 @@ vkhr_status vkhr_frame_graph_create(vkhr_ctx* ctx, int32_t segments, const vkhr_
 vkhr_status vkhr_frame_graph_launch(vkhr_frame_graph* graph, void* stream);
 vkhr_status vkhr_frame_graph_destroy(vkhr_frame_graph* graph);
 
+/* ---- .hair files and strand reduction ------------------------------------- */
+
+/* The 128-byte header of a `.hair` file, byte for byte
+ * (HairStyle::FileHeader, hair_style.hh:147-174; the field bit-field as one
+ * little-endian word of VKHR_HAIR_* bits). */
+typedef struct vkhr_hair_header {
+    char signature[4]; /* 'H', 'A', 'I', 'R' */
+    uint32_t strand_count, vertex_count;
+    uint32_t fields;
+    uint32_t default_segment_count;
+    float default_thickness, default_transparency;
+    float default_color[3];
+    char information[64];
+    float bounding_box_min[3], bounding_box_max[3];
+} vkhr_hair_header;
+
+#define VKHR_HAIR_SEGMENTS 1u
+#define VKHR_HAIR_VERTICES 2u
+#define VKHR_HAIR_THICKNESS 4u
+#define VKHR_HAIR_TRANSPARENCY 8u
+#define VKHR_HAIR_COLOR 16u
+#define VKHR_HAIR_TANGENTS 32u
+#define VKHR_HAIR_INDICES 64u
+#define VKHR_HAIR_BOUNDING_BOX 128u
+
+/* Reads a file's header (no CUDA call).  VKHR_ERR_INVALID_ARG when the file
+ * cannot be opened or read, or its signature is not HAIR. */
+vkhr_status vkhr_hair_read_header(const char* path, vkhr_hair_header* header);
+
+/* HairStyle::load (hair_style.cc:24-45, field readers :576-623) into device
+ * memory: the segment count of every strand to h_segments (host, strand_count
+ * of them; may be NULL), the vertices (float3) to d_vertices, and, when the
+ * file holds them, the tangents (float3) to d_tangents and the indices (u32,
+ * 2 per segment, 2 * (vertex_count - strand_count)) to d_indices (each may
+ * be NULL).  The arrays stream through two pinned chunks with asynchronous
+ * copies on `stream`; the call returns once they are done.  Thickness,
+ * transparency and colour are skipped (nothing on the path reads them).
+ * Errors (VKHR_ERR_INVALID_ARG, with the reference's error name in
+ * vkhr_last_error): OpeningFile, ReadingFileHeader, InvalidSignature,
+ * Reading<Field> for a short file, InvalidFormat for a file without
+ * vertices. */
+vkhr_status vkhr_hair_load(vkhr_ctx* ctx, const char* path, vkhr_hair_header* header, uint16_t* h_segments,
+                           float* d_vertices, float* d_tangents, uint32_t* d_indices, void* stream);
+
+/* HairStyle::reduce(ratio) (hair_style.cc:375-449) on device-resident
+ * strands.  The choice of strands is the reference's, made on the host over
+ * h_segments (NULL: every strand has default_segment_count segments): its
+ * xorshift64 sequence from *seed (updated), its FP32 count arithmetic (ratio
+ * 1 keeps every strand, shuffled: HairStyle::shuffle).  A kernel then gathers
+ * the kept strands' vertices and tangents (d_tangents may be NULL), in the
+ * order kept, to the outputs (capacity: the input's vertex count).  The kept
+ * strands' segment counts go to h_segments_out (capacity strand_count), the
+ * kept counts to *strands_out / *vertices_out.  Returns once the gather is
+ * done.  Indices: vkhr_generate_indices over the kept segments. */
+vkhr_status vkhr_reduce_strands(vkhr_ctx* ctx, float ratio, uint64_t* seed, const uint16_t* h_segments,
+                                uint32_t strand_count, uint32_t default_segment_count, const float* d_vertices,
+                                const float* d_tangents, uint16_t* h_segments_out, uint32_t* strands_out,
+                                uint32_t* vertices_out, float* d_vertices_out, float* d_tangents_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

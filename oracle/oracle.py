@@ -84,7 +84,53 @@ def ref():
         _ref.ref_raymarch.argtypes = [C.POINTER(_abi.RaymarchParams), P, P, P, P, P, C.c_int, C.c_int, C.c_int]
         _ref.ref_raymarch.restype = C.c_int
         _ref.ref_downsample.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, P]
+        U32P = C.POINTER(C.c_uint32)
+        _ref.ref_hair_load.argtypes = [C.c_char_p, U32P, U32P, U32P, U32P, P, C.c_uint32, P, P, C.c_uint32, P, C.c_uint32]
+        _ref.ref_hair_load.restype = C.c_int
+        _ref.ref_hair_save.argtypes = [C.c_char_p, P, C.c_uint32, P, P, C.c_uint32]
+        _ref.ref_hair_save.restype = C.c_int
+        _ref.ref_reduce.argtypes = [P, P, C.c_uint32, P, C.c_uint32, C.c_uint32, C.c_float, C.POINTER(C.c_uint64), P,
+                                    P, P, U32P, U32P]
     return _ref
+
+
+def ref_hair_load(path):
+    """The reference's HairStyle::load of `path`: (error state, dict of arrays)."""
+    r = ref()
+    n, v, bits, ni = C.c_uint32(), C.c_uint32(), C.c_uint32(), C.c_uint32()
+    err = r.ref_hair_load(path.encode(), C.byref(n), C.byref(v), C.byref(bits), C.byref(ni), None, 0, None, None, 0,
+                          None, 0)
+    segs = np.zeros(n.value, dtype=np.uint16)
+    verts = np.zeros((v.value, 3), dtype=np.float32)
+    tans = np.zeros((v.value, 3), dtype=np.float32)
+    idx = np.zeros(ni.value, dtype=np.uint32)
+    err = r.ref_hair_load(path.encode(), C.byref(n), C.byref(v), C.byref(bits), C.byref(ni), _p(segs), n.value,
+                          _p(verts), _p(tans), v.value, _p(idx), ni.value)
+    return err, {"fields": bits.value, "segments": segs, "vertices": verts, "tangents": tans, "indices": idx}
+
+
+def ref_hair_save(path, segments, vertices, tangents=None):
+    """The reference's HairStyle::save of the given arrays; 0 on success."""
+    segs = np.ascontiguousarray(segments, dtype=np.uint16)
+    v = _f32(vertices)
+    t = None if tangents is None else _f32(tangents)
+    return ref().ref_hair_save(path.encode(), _p(segs), len(segs), _p(v), _p(t), len(v))
+
+
+def ref_reduce(vertices, tangents, segments, strand_count, ratio, seed, default_segment_count=0):
+    """The reference's HairStyle::reduce(ratio) with the seed fixed: (kept
+    vertices, kept tangents, kept segment counts, seed after)."""
+    v = _f32(vertices)
+    t = None if tangents is None else _f32(tangents)
+    segs = None if segments is None else np.ascontiguousarray(segments, dtype=np.uint16)
+    vo = np.zeros_like(v)
+    to = None if t is None else np.zeros_like(t)
+    so = np.zeros(max(strand_count, 1), dtype=np.uint16)
+    sd = C.c_uint64(seed)
+    ns, nv = C.c_uint32(), C.c_uint32()
+    ref().ref_reduce(_p(v), _p(t), len(v), _p(segs), strand_count, default_segment_count, ratio, C.byref(sd), _p(vo),
+                     _p(to), _p(so), C.byref(ns), C.byref(nv))
+    return vo[:nv.value], None if to is None else to[:nv.value], so[:ns.value], sd.value
 
 
 def _p(a):

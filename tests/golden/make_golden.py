@@ -7,6 +7,7 @@ seeded synthetic styles, and stores inputs and outputs as .npz files.
 Needs the reference sources; run from the repository root:
 
     make -C oracle ref && python tests/golden/make_golden.py
+    python tests/golden/make_golden.py reduce   # the strand-reduction fixtures only
 """
 import os
 import sys
@@ -50,7 +51,28 @@ def raymarch_case(name, st, res, W, H, **kw):
                         depth=depth)
 
 
+def reduce_case(name, st, seed, ratios):
+    """HairStyle::reduce (and its .hair saver) of the reference on a style
+    with an even strand count: reduce's offset array copy writes one element
+    past its end (hair_style.cc:392), which stays inside the allocation's
+    slack for an even count."""
+    assert len(st.segments) % 2 == 0
+    t, idx, b = O.ref_prepare(st.vertices, st.segments)
+    out = {"vertices": st.vertices, "segments": st.segments.astype(np.uint16), "tangents": t, "seed": np.uint64(seed),
+           "ratios": np.array(ratios, dtype=np.float32)}
+    for k, r in enumerate(ratios):
+        v, tt, sg, sd = O.ref_reduce(st.vertices, t, st.segments, len(st.segments), float(r), seed)
+        out["r%d_vertices" % k], out["r%d_tangents" % k], out["r%d_segments" % k] = v, tt, sg
+        out["r%d_seed" % k] = np.uint64(sd)
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), **out)
+    assert O.ref_hair_save(os.path.join(OUT, name + ".hair"), st.segments, st.vertices, t) == 0
+
+
 def main():
+    if sys.argv[1:] == ["reduce"]:  # only the strand-reduction fixtures
+        reduce_case("reduce_hemisphere", strands.hemisphere_style(256, 8, seed=16), 0x9E3779B97F4A7C15,
+                    [1.0, 0.5, 0.984375, 0.015625])
+        return
     voxel_case("voxel_hemisphere", strands.hemisphere_style(256, 8, seed=11), [(16, 16, 16), (13, 9, 21)])
     voxel_case("voxel_ragged", strands.ragged_style([2, 0, 3, 9, 1, 17, 0, 5, 30, 2], seed=12), [(8, 8, 8), (20, 7, 11)])
     crowded = strands.disk_style(1500, 6, disk_radius=0.02, step_length=0.01, seed=13)

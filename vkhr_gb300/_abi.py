@@ -72,6 +72,28 @@ class AABB(C.Structure):
         }
 
 
+class HairHeader(C.Structure):
+    """vkhr_hair_header: a `.hair` file's 128-byte header (hair_style.hh:147-174)."""
+
+    _fields_ = [
+        ("signature", C.c_char * 4),
+        ("strand_count", C.c_uint32),
+        ("vertex_count", C.c_uint32),
+        ("fields", C.c_uint32),
+        ("default_segment_count", C.c_uint32),
+        ("default_thickness", C.c_float),
+        ("default_transparency", C.c_float),
+        ("default_color", C.c_float * 3),
+        ("information", C.c_char * 64),
+        ("bounding_box_min", C.c_float * 3),
+        ("bounding_box_max", C.c_float * 3),
+    ]
+
+
+HAIR_SEGMENTS, HAIR_VERTICES, HAIR_THICKNESS, HAIR_TRANSPARENCY = 1, 2, 4, 8
+HAIR_COLOR, HAIR_TANGENTS, HAIR_INDICES, HAIR_BOUNDING_BOX = 16, 32, 64, 128
+
+
 class VoxelJob(C.Structure):
     """vkhr_voxel_job: one style of a batched voxelization."""
 

@@ -22,6 +22,7 @@ EXPORTS = [
     "vkhr_downsample_densities", "vkhr_raymarch_tape_bytes", "vkhr_raymarch_train", "vkhr_raymarch_adjoint",
     "vkhr_splat_vertices", "vkhr_splat_vertices_adjoint", "vkhr_autotune_raymarch", "vkhr_set_raymarch_variant",
     "vkhr_frame_graph_create", "vkhr_frame_graph_launch", "vkhr_frame_graph_destroy",
+    "vkhr_hair_read_header", "vkhr_hair_load", "vkhr_reduce_strands",
 ]
 
 _lib = None
@@ -78,6 +79,11 @@ def load():
     lib.vkhr_frame_graph_create.argtypes = [P, C.c_int32, C.POINTER(_abi.VoxelJob), C.c_int32, C.c_uint64,
                                             C.POINTER(_abi.RaymarchParams), P, P, P, P, C.POINTER(C.c_void_p)]
     lib.vkhr_frame_graph_launch.argtypes = [P, P]
+    lib.vkhr_hair_read_header.argtypes = [C.c_char_p, C.POINTER(_abi.HairHeader)]
+    lib.vkhr_hair_load.argtypes = [P, C.c_char_p, C.POINTER(_abi.HairHeader), P, P, P, P, P]
+    U32P = C.POINTER(C.c_uint32)
+    lib.vkhr_reduce_strands.argtypes = [P, C.c_float, C.POINTER(C.c_uint64), P, C.c_uint32, C.c_uint32, P, P, P, U32P,
+                                        U32P, P, P, P]
     lib.vkhr_frame_graph_destroy.argtypes = [P]
     lib.vkhr_raymarch.argtypes = [P, C.POINTER(_abi.RaymarchParams), P, P, P, P, P, P]
     lib.vkhr_malloc.argtypes = [P, C.c_size_t, C.POINTER(C.c_void_p)]
@@ -208,6 +214,34 @@ class Context:
                                                     d_depth_in, d_rgba, d_depth_out, stream, C.byref(h)))
         return FrameGraph(self, h)
 
+    def hair_load(self, path, d_vertices, d_tangents=None, d_indices=None, want_segments=True, stream=None):
+        """vkhr_hair_load: (header, host segment counts or None)."""
+        import numpy as np
+
+        hdr = hair_read_header(path)
+        segs = np.zeros(hdr.strand_count, dtype=np.uint16) if want_segments else None
+        out = _abi.HairHeader()
+        self.check(self.lib.vkhr_hair_load(self.handle, path.encode(), C.byref(out),
+                                           None if segs is None else segs.ctypes.data_as(C.c_void_p), d_vertices,
+                                           d_tangents, d_indices, stream))
+        return out, segs
+
+    def reduce_strands(self, ratio, seed, segments, strand_count, d_vertices, d_tangents, d_vertices_out,
+                       d_tangents_out=None, default_segment_count=0, stream=None):
+        """vkhr_reduce_strands: (kept segment counts, kept vertex count, seed after)."""
+        import numpy as np
+
+        segs = None if segments is None else np.ascontiguousarray(segments, dtype=np.uint16)
+        out = np.zeros(max(strand_count, 1), dtype=np.uint16)
+        sd = C.c_uint64(seed)
+        ns, nv = C.c_uint32(), C.c_uint32()
+        self.check(self.lib.vkhr_reduce_strands(self.handle, ratio, C.byref(sd),
+                                                None if segs is None else segs.ctypes.data_as(C.c_void_p),
+                                                strand_count, default_segment_count, d_vertices, d_tangents,
+                                                out.ctypes.data_as(C.c_void_p), C.byref(ns), C.byref(nv),
+                                                d_vertices_out, d_tangents_out, stream))
+        return out[:ns.value], nv.value, sd.value
+
     def raymarch_batched(self, jobs, stream=None):
         """jobs: a sequence of _abi.RaymarchJob."""
         arr = (_abi.RaymarchJob * len(jobs))(*jobs)
@@ -266,6 +300,16 @@ class Context:
     def raymarch(self, params, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, stream=None):
         self.check(self.lib.vkhr_raymarch(self.handle, C.byref(params), d_density, d_tangent, d_depth_in, d_rgba,
                                           d_depth_out, stream))
+
+
+def hair_read_header(path):
+    """vkhr_hair_read_header (no CUDA call)."""
+    lib = load()
+    h = _abi.HairHeader()
+    st = lib.vkhr_hair_read_header(path.encode(), C.byref(h))
+    if st != 0:
+        raise VkhrError(st, "vkhr_hair_read_header(%s)" % path)
+    return h
 
 
 def raymarch_footprint(params):

@@ -42,6 +42,8 @@ struct vkhr_ctx {
     int sm_count;
     int l2_bytes;              // L2 cache size
     uint32_t direct_cap;       // voxelizer: per-brick slice capacity of one-walk calls (0: not yet known)
+    uint4* d_gather;           // strand reduction: the kept strands' (source, destination, vertices)
+    size_t d_gather_cap;
     void* slots;               // voxelizer: the fixed per-brick slices of one-walk calls
     size_t slots_cap;          // (in 8-byte units)
     // grow-only scratch (capacities in elements)
