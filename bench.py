@@ -599,6 +599,88 @@ def frame_graph_section(args, dev, stream, flush, st, t, idx, b, res, p):
     }
 
 
+def schedule_section(args, dev, stream):
+    """The reference's benchmark schedule for the raymarcher (benchmark.hh:
+    12-140, run by rasterizer.cc:599-772) restated headlessly on the synthetic
+    ponytail at 1280x720: distance 200..2000 (step 1800/64), raymarch samples
+    512..64 (step 448/64 = 7), strand ratio 1..1/64 (step 1/64) around the
+    defaults (distance 226, ratio 1, 512 samples).  Distances map to this
+    scene's units by 4.0 / 226 (the default camera distance here over the
+    reference's).  Distance and samples time the raymarch of the loaded
+    volume; each strand ratio applies HairStyle::reduce (vkhr_reduce_strands,
+    the reference's seeded choice) to the loaded style and times the
+    voxelization (segments, normalized) plus the raymarch."""
+    import torch
+
+    from vkhr_gb300 import _abi, _native, scene, strands
+
+    ctx = _native.Context(dev.index)
+    s = stream.cuda_stream
+    st, t, idx = make_style()
+    res = (WORKLOAD["resolution"],) * 3
+    n = res[0] * res[1] * res[2]
+    W, H = 1280, 720
+    dv = torch.from_numpy(st.vertices).to(dev)
+    dt = torch.from_numpy(t).to(dev)
+    b = ctx.bounding_box(dv.data_ptr(), st.vertex_count, s)
+    counts = torch.empty(n, dtype=torch.int32, device=dev)
+    dens = torch.empty(n, dtype=torch.uint8, device=dev)
+    tq = torch.empty((n, 4), dtype=torch.int8, device=dev)
+    rgba = torch.empty((H, W, 4), dtype=torch.float32, device=dev)
+    depth = torch.empty((H, W), dtype=torch.float32, device=dev)
+    scale = 4.0 / 226.0
+    reps = max(args.steps, 3)
+
+    def params(distance=226.0, samples=512):
+        return scene.make_params(b, res, W, H, camera_distance=distance * scale, raycast_steps=float(samples),
+                                 renderer=_abi.RENDERER_RAYMARCHER)
+
+    def voxelize(v_ptr, t_ptr, di, count):
+        ctx.voxelize_segments(v_ptr, t_ptr, di.data_ptr(), count, b, res, _abi.INDEX_REF_FP32, counts.data_ptr(),
+                              dens.data_ptr(), tq.data_ptr(), s)
+        ctx.normalize_densities(dens.data_ptr(), n, s)
+
+    def timed(fn):
+        for _ in range(2):
+            fn()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        for a, z in ev:
+            a.record(stream)
+            fn()
+            z.record(stream)
+        torch.cuda.synchronize()
+        return sorted(a.elapsed_time(z) for a, z in ev)[reps // 2]
+
+    di_full = torch.from_numpy(idx.view(np.int32)).to(dev)
+    voxelize(dv.data_ptr(), dt.data_ptr(), di_full, idx.shape[0])
+    torch.cuda.synchronize()
+
+    def march(p):
+        return lambda: ctx.raymarch(p, dens.data_ptr(), tq.data_ptr(), None, rgba.data_ptr(), depth.data_ptr(), s)
+
+    out = {"config": {"workload": "the reference's raymarcher benchmark schedule on the synthetic ponytail "
+                                  "(136,320 x 13, 256^3), 1280x720; median of %d runs per point" % reps,
+                      "distance_scale": scale}}
+    out["distance"] = [[d, timed(march(params(distance=d)))]
+                       for d in (200.0 + k * (1800.0 / 64.0) for k in range(64))]
+    out["samples"] = [[k, timed(march(params(samples=k)))] for k in range(512, 63, -(448 // 64))]
+    ov, ot = torch.empty_like(dv), torch.empty_like(dt)
+    segs = st.segments.astype(np.uint16)
+    rows = []
+    for k in range(64):
+        ratio = 1.0 - k / 64.0
+        kept, nv, _ = ctx.reduce_strands(ratio, 0x9E3779B97F4A7C15, segs, len(segs), dv.data_ptr(), dt.data_ptr(),
+                                         ov.data_ptr(), ot.data_ptr(), stream=s)
+        kidx = strands.generate_indices(kept)
+        di = torch.from_numpy(kidx.view(np.int32)).to(dev)
+        p = params()
+        vox_ms = timed(lambda: voxelize(ov.data_ptr(), ot.data_ptr(), di, kidx.shape[0]))
+        rows.append([ratio, int(len(kept)), vox_ms, timed(march(p))])
+    out["strands"] = rows
+    ctx.close()
+    return out
+
+
 def gb300_arm(args):
     import torch
 
@@ -616,6 +698,10 @@ def gb300_arm(args):
         flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
         if rank == 0:
             print(json.dumps({"section": "scale", "scale": scale_section(args, dev, stream, flush)}))
+        return 0
+    if args.section == "schedule":  # the reference's benchmark schedule (opt-in)
+        if rank == 0:
+            print(json.dumps({"section": "schedule", "schedule": schedule_section(args, dev, stream)}))
         return 0
     if args.section == "diff":  # the differentiable workload alone (profiling runs)
         flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
@@ -897,7 +983,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the 16-style batched vs plain comparison")
     ap.add_argument("--no-scale", action="store_true", help="skip the 512^3 scale workload")
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiable workload")
-    ap.add_argument("--section", default="all", choices=["all", "frame", "batched", "scale", "diff"],
+    ap.add_argument("--section", default="all", choices=["all", "frame", "batched", "scale", "diff", "schedule"],
                     help="frame: the production frame only; batched: the multi-style comparison only; "
                          "scale: the 512^3 workload only; diff: the differentiable workload only")
     args = ap.parse_args()
