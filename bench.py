@@ -681,6 +681,137 @@ def schedule_section(args, dev, stream):
     return out
 
 
+def composite_section(args, dev, stream, flush, st, t, idx, b, res):
+    """The colour pass's transparency without a linked list (vkhr_composite):
+    the production style at 1280x720 (the reference's window) under the
+    hybrid LoD renderer, at the reference's default LoD band (magnified 400,
+    minified 800; distances scaled to this scene by 4.0 / 226).  Two views:
+    the close-up at the reference's default distance 226 (lod 0: strands
+    only) and the band's middle, 600 (lod 0.5: strands at half coverage plus
+    the raymarched volume's fragments).  Strand fragments come from the
+    synthetic one-pixel-line rasterizer of workloads.strand_fragments (the
+    strand rasterizer is not part of this library), in primitive order.
+    Device time of the composite with its inputs resident (L2 flushed, the
+    white background restored before each step, outside the timed region);
+    e2e: the fragments uploaded from pinned memory, the raymarch, the
+    composite and the image read back, serial, per frame."""
+    import torch
+
+    from vkhr_gb300 import _abi, _native, scene, workloads
+
+    ctx = _native.Context(dev.index)
+    s = stream.cuda_stream
+    W, H = 1280, 720
+    npix = W * H
+    scale = 4.0 / 226.0
+    n = res[0] * res[1] * res[2]
+    dv = torch.from_numpy(st.vertices).to(dev)
+    dt = torch.from_numpy(t).to(dev)
+    di = torch.from_numpy(idx.view(np.int32)).to(dev)
+    counts = torch.empty(n, dtype=torch.int32, device=dev)
+    dens = torch.empty(n, dtype=torch.uint8, device=dev)
+    tq = torch.empty((n, 4), dtype=torch.int8, device=dev)
+    ctx.voxelize_segments(dv.data_ptr(), dt.data_ptr(), di.data_ptr(), idx.shape[0], b, res, _abi.INDEX_REF_FP32,
+                          counts.data_ptr(), dens.data_ptr(), tq.data_ptr(), s)
+    ctx.normalize_densities(dens.data_ptr(), n, s)
+    rgba = torch.empty((H, W, 4), dtype=torch.float32, device=dev)
+    depth = torch.empty((H, W), dtype=torch.float32, device=dev)
+    color = torch.empty((H, W), dtype=torch.int32, device=dev)
+    hbm, peak_kind = peaks()
+    reps = max(args.steps, 3)
+    out = {"config": {"workload": "hybrid-LoD compositing of the production style (136,320 x 13) at 1280x720: "
+                                  "synthetic one-pixel strand fragments in primitive order + the raymarched "
+                                  "volume's fragments, resolved per pixel (16-node k-buffer + 1024 blended)",
+                      "lod_band": [400.0, 800.0], "distance_scale": scale}}
+    for name, distance in (("close", 226.0), ("hybrid", 600.0)):
+        p = scene.make_params(b, res, W, H, camera_distance=distance * scale, raycast_steps=512.0,
+                              renderer=_abi.RENDERER_HYBRID_LOD)
+        p.magnified_distance, p.minified_distance = 400.0 * scale, 800.0 * scale
+        lod = _native.level_of_detail(p.magnified_distance, p.minified_distance, p.look_at_distance)
+        strands_on = _native.rasterizer_enabled(_abi.RENDERER_HYBRID_LOD, lod)
+        volume_on = _native.raymarcher_enabled(_abi.RENDERER_HYBRID_LOD, lod)
+        frags = workloads.strand_fragments(st.vertices, t, idx, p, lod, dev) if strands_on else \
+            torch.zeros((0, 3), dtype=torch.int32, device=dev)
+        F = frags.shape[0]
+        vr, vd = (rgba.data_ptr(), depth.data_ptr()) if volume_on else (None, None)
+        if volume_on:
+            ctx.raymarch(p, dens.data_ptr(), tq.data_ptr(), None, rgba.data_ptr(), depth.data_ptr(), s)
+
+        def composite():
+            ctx.composite(frags.data_ptr() if F else None, F, W, H, color.data_ptr(), vr, vd, s)
+
+        for _ in range(3):
+            color.fill_(-1)
+            composite()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        for a, z in ev:
+            flush.zero_()
+            color.fill_(-1)
+            a.record(stream)
+            composite()
+            z.record(stream)
+        torch.cuda.synchronize()
+        ms = sorted(a.elapsed_time(z) for a, z in ev)[reps // 2]
+        ctx.set_profiling(True)
+        for _ in range(reps):
+            flush.zero_()
+            color.fill_(-1)
+            composite()
+        torch.cuda.synchronize()
+        kern = {}
+        for kname, kms in ctx.profile():
+            e = kern.setdefault(kname, [0, 0.0])
+            e[0] += 1
+            e[1] += kms
+        ctx.set_profiling(False)
+        ctx.check_status(s)
+        changed = int(((color != -1).sum()).item())
+        # e2e: upload the fragments, raymarch (when on), composite, read the image back
+        hf = frags.cpu().pin_memory()
+        hc = torch.empty((H, W), dtype=torch.int32).pin_memory()
+        e2e = []
+        for k in range(reps + 2):
+            a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            color.fill_(-1)
+            a.record(stream)
+            frags.copy_(hf, non_blocking=True)
+            if volume_on:
+                ctx.raymarch(p, dens.data_ptr(), tq.data_ptr(), None, rgba.data_ptr(), depth.data_ptr(), s)
+            composite()
+            hc.copy_(color, non_blocking=True)
+            z.record(stream)
+            torch.cuda.synchronize()
+            if k >= 2:
+                e2e.append(a.elapsed_time(z))
+        e2e_ms = sorted(e2e)[len(e2e) // 2]
+        alg = F * 12 + npix * 8 + (npix * 20 if volume_on else 0)
+        row = {"distance": distance, "lod": lod, "strand_fragments": F, "volume": bool(volume_on),
+               "pixels_changed": changed, "ms": ms, "mfragments_per_s": F / ms / 1e3,
+               "algorithmic_bytes": alg, "achieved_gbs": alg / ms / 1e6, "peak_gbs": hbm, "peak": peak_kind,
+               "frac": alg / ms / 1e6 / hbm,
+               "kernels": {k: {"launches": v[0], "avg_ms": v[1] / v[0]} for k, v in sorted(kern.items())},
+               "e2e_ms": e2e_ms, "h2d_bytes_per_step": F * 12, "d2h_bytes_per_step": npix * 4}
+        if not args.no_cpu_baseline:
+            from oracle import oracle as O
+
+            if not os.path.exists(O.LIB):
+                O.build(with_reference=False)
+            hfr = frags.cpu().numpy().view(_abi.FRAGMENT_DTYPE).reshape(-1)
+            bg = np.full((H, W), 0xFFFFFFFF, dtype=np.uint32)
+            vra = rgba.cpu().numpy() if volume_on else None
+            vda = depth.cpu().numpy() if volume_on else None
+            t0 = time.perf_counter()
+            O.composite(hfr, bg, vra, vda)
+            cpu_s = time.perf_counter() - t0
+            row["cpu_baseline"] = {"value": F / cpu_s / 1e6, "unit": "Mfragments/s", "cores": O.max_threads(),
+                                   "kind": "port", "sample": "the whole composite once (%.2f s)" % cpu_s}
+        out[name] = row
+        del frags, hf
+    ctx.close()
+    return out
+
+
 def gb300_arm(args):
     import torch
 
@@ -707,6 +838,16 @@ def gb300_arm(args):
         flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
         if rank == 0:
             print(json.dumps({"section": "diff", "diff": diff_section(args, dev, stream, flush)}))
+        return 0
+    if args.section == "composite":  # the compositing workload alone (profiling runs)
+        flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+        if rank == 0:
+            st, t, idx = make_style()
+            res = (WORKLOAD["resolution"],) * 3
+            dv = torch.from_numpy(st.vertices).to(dev)
+            b = ctx.bounding_box(dv.data_ptr(), st.vertex_count, s)
+            print(json.dumps({"section": "composite",
+                              "composite": composite_section(args, dev, stream, flush, st, t, idx, b, res)}))
         return 0
     if args.section == "batched":  # the multi-style comparison alone (profiling runs)
         flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
@@ -919,6 +1060,8 @@ def gb300_arm(args):
         args, dev, stream, flush, st, t, idx, b, res, p)
     scale = None if (args.no_scale or args.section == "frame" or world > 1) else scale_section(args, dev, stream, flush)
     diff = None if (args.no_diff or args.section == "frame" or world > 1) else diff_section(args, dev, stream, flush)
+    composite = None if (args.no_composite or args.section == "frame" or world > 1) else composite_section(
+        args, dev, stream, flush, st, t, idx, b, res)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -953,6 +1096,8 @@ def gb300_arm(args):
         line["scale"] = scale
     if diff is not None:
         line["diff"] = diff
+    if composite is not None:
+        line["composite"] = composite
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import oracle as O
 
@@ -983,9 +1128,12 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the 16-style batched vs plain comparison")
     ap.add_argument("--no-scale", action="store_true", help="skip the 512^3 scale workload")
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiable workload")
-    ap.add_argument("--section", default="all", choices=["all", "frame", "batched", "scale", "diff", "schedule"],
+    ap.add_argument("--no-composite", action="store_true", help="skip the hybrid-LoD compositing workload")
+    ap.add_argument("--section", default="all",
+                    choices=["all", "frame", "batched", "scale", "diff", "schedule", "composite"],
                     help="frame: the production frame only; batched: the multi-style comparison only; "
-                         "scale: the 512^3 workload only; diff: the differentiable workload only")
+                         "scale: the 512^3 workload only; diff: the differentiable workload only; "
+                         "composite: the hybrid-LoD compositing only")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)

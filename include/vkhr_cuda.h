@@ -18,6 +18,8 @@
  *   vkhr::HairStyle::Volume::normalize   src/vkhr/scene_graph/hair_style.cc:344-357
  *   vulkan::Volume::draw + volume.frag   src/vkhr/rasterizer/volume.cc:104-112,
  *                                        share/shaders/volumes/volume.frag:31-103
+ *   vulkan::LinkedList::resolve          src/vkhr/rasterizer/linked_list.cc:21-41,
+ *     + resolve.comp                     share/shaders/transparency/resolve.comp:15-101
  */
 #ifndef VKHR_CUDA_H
 #define VKHR_CUDA_H
@@ -85,11 +87,14 @@ enum {
     VKHR_SHADING_LAO = 3
 };
 
-/* Renderer::Type (include/vkhr/renderer.hh:14): 0 rasterizer, 1 hybrid, 2 raymarcher. */
+/* Renderer::Type (include/vkhr/renderer.hh:13-17).  lod() of scheme.glsl:7-11
+ * is 0 for the rasterizer, 1 for the raymarcher and the smoothstep blend for
+ * every other value (the ray tracer's and the hybrid's). */
 enum {
     VKHR_RENDERER_RASTERIZER = 0,
-    VKHR_RENDERER_HYBRID = 1,
-    VKHR_RENDERER_RAYMARCHER = 2
+    VKHR_RENDERER_RAY_TRACER = 1,
+    VKHR_RENDERER_RAYMARCHER = 2,
+    VKHR_RENDERER_HYBRID_LOD = 3
 };
 
 /* Every scalar the raymarch reads.  Field groups mirror the reference UBOs:
@@ -256,7 +261,9 @@ vkhr_status vkhr_voxelize_batched(vkhr_ctx* ctx, int32_t segments, const vkhr_vo
 vkhr_status vkhr_set_visit_budget(vkhr_ctx* ctx, uint64_t max_visits);
 
 /* Waits for the stream and reports errors that kernels recorded on the device
- * since the last voxelization started (e.g. a capacity overflow). */
+ * since the last voxelization started or the last check that reported one
+ * (e.g. a capacity overflow, a fragment outside the image); reporting clears
+ * them. */
 vkhr_status vkhr_check_status(vkhr_ctx* ctx, void* stream);
 
 /* Replaces HairStyle::Volume::normalize (hair_style.cc:344-357): u8 min-max
@@ -496,6 +503,82 @@ vkhr_status vkhr_reduce_strands(vkhr_ctx* ctx, float ratio, uint64_t* seed, cons
                                 uint32_t strand_count, uint32_t default_segment_count, const float* d_vertices,
                                 const float* d_tangents, uint16_t* h_segments_out, uint32_t* strands_out,
                                 uint32_t* vertices_out, float* d_vertices_out, float* d_tangents_out, void* stream);
+
+/* ---- compositing: the PPLL resolve and its PPLL-free form ---------------------
+ * Colour images are width*height RGBA8 words, red in the low byte: the
+ * colour attachment resolve.comp reads as the background and overwrites
+ * (share/shaders/transparency/resolve.comp:6, :39, :101).  Loads convert
+ * c / 255; stores clamp to [0, 1] and take the nearest code, ties to even
+ * (Vulkan's UNORM conversions, whose ties the specs leave open).  Blends are
+ * mix(x, y, a) = x * (1 - a) + y * a in FP32 without contraction. */
+#define VKHR_PPLL_NULL 0xffffffffu  /* PPLL_NULL_NODE, ppll.glsl:4 */
+#define VKHR_K_BUFFER_SIZE 16       /* resolve.comp:12 */
+#define VKHR_MAX_FRAGMENTS 1024     /* resolve.comp:13 */
+
+/* Node of the reference's per-pixel linked list (ppll.glsl:7-11;
+ * LinkedList::NodeSize, include/vkhr/rasterizer/linked_list.hh:29):
+ * color = packUnorm4x8(rgba), depth unpacked, prev = next node of the list. */
+typedef struct vkhr_ppll_node {
+    uint32_t color;
+    float depth;
+    uint32_t prev;
+} vkhr_ppll_node;
+
+/* A fragment for the PPLL-free composite: a node whose link is replaced by
+ * its pixel, y * width + x. */
+typedef struct vkhr_fragment {
+    uint32_t color;
+    float depth;
+    uint32_t pixel;
+} vkhr_fragment;
+
+/* Replaces LinkedList::resolve (src/vkhr/rasterizer/linked_list.cc:21-41)
+ * and resolve.comp:15-101: every pixel whose head is not VKHR_PPLL_NULL
+ * blends its list over d_color: the first 16 nodes fill a k-buffer, up to
+ * 1024 more are blended as they come (each swapped with the k-buffer's
+ * furthest node when nearer), then the k-buffer back to front.
+ *   d_heads  width*height words;  d_nodes  node_count nodes.
+ * A link outside [0, node_count) ends its list (the reference reads past
+ * its buffer there); vkhr_check_status reports it as VKHR_ERR_INVALID_ARG.
+ * Never waits on the host. */
+vkhr_status vkhr_resolve_ppll(vkhr_ctx* ctx, const uint32_t* d_heads, const vkhr_ppll_node* d_nodes,
+                              uint32_t node_count, int32_t width, int32_t height, uint32_t* d_color, void* stream);
+
+/* The colour pass's transparency without a linked list (strand.frag:81-84,
+ * volume.frag:97-100, resolve.comp:15-101).  Each pixel resolves exactly the
+ * list a PPLL would hold had the strand fragments been linked in buffer order
+ * and the volume fragment after them (the raymarch runs in the subpass after
+ * the strands, src/vkhr/rasterizer.cc:245-257): the volume fragment first,
+ * then the strand fragments last-in first.  The result equals
+ * vkhr_resolve_ppll on that PPLL, without its node pool: no fragment is
+ * dropped for capacity (the reference keeps at most 32 per pixel on average,
+ * ppll.glsl:25, linked_list.hh:28).
+ *   d_fragments     fragment_count strand fragments (device memory);
+ *   d_volume_rgba,  vkhr_raymarch's outputs (width*height float4 and floats)
+ *   d_volume_depth  or both NULL: a pixel holds a volume fragment where its
+ *                   depth is below 1 (vkhr_raymarch writes 1 where none
+ *                   survives), coloured packUnorm4x8(rgba);
+ *   d_color         the background, overwritten where a pixel has fragments.
+ * A fragment whose pixel is outside the image is skipped and reported by
+ * vkhr_check_status (VKHR_ERR_INVALID_ARG).  Scratch: 12 bytes per fragment
+ * and about 8 per pixel, grow-only in the context; the call never waits on
+ * the host and can be captured into a CUDA graph after one uncaptured call
+ * at the same sizes. */
+vkhr_status vkhr_composite(vkhr_ctx* ctx, const vkhr_fragment* d_fragments, uint32_t fragment_count,
+                           const float* d_volume_rgba, const float* d_volume_depth, int32_t width, int32_t height,
+                           uint32_t* d_color, void* stream);
+
+/* Level of detail on the host.  vkhr_level_of_detail is Rasterizer::update's
+ * glm::smoothstep(magnified, minified, distance) (rasterizer.cc:165-167);
+ * vkhr_lod is scheme.glsl:7-11's lod(), which scales the raymarch's coverage
+ * by lod and the strands' by 1 - lod (volume.frag:48, strand.frag:42); the
+ * two predicates are Interface::rasterizer_enabled / raymarcher_enabled
+ * (src/vkhr/rasterizer/interface.cc:534-540), which decide whether the
+ * strands and the volume are drawn at all. */
+float vkhr_level_of_detail(float magnified_distance, float minified_distance, float distance);
+float vkhr_lod(int32_t renderer, float magnified_distance, float minified_distance, float distance);
+int32_t vkhr_rasterizer_enabled(int32_t renderer, float level_of_detail);
+int32_t vkhr_raymarcher_enabled(int32_t renderer, float level_of_detail);
 
 #ifdef __cplusplus
 }

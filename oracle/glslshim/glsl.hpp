@@ -1,8 +1,10 @@
 // glslshim/glsl.hpp -- TEST INFRASTRUCTURE ONLY.
 //
-// Just enough of GLSL 4.60 (types, built-ins, a software sampler3D) for the
-// reference's raymarch shader (share/shaders/volumes/volume.frag and its
-// includes) to compile as C++17 and run on the CPU in strict FP32.  Written
+// Just enough of GLSL 4.60 (types, built-ins, a software sampler3D, storage
+// images) for the reference's raymarch shader (share/shaders/volumes/
+// volume.frag and its includes) and its PPLL resolve (share/shaders/
+// transparency/resolve.comp, ppll.glsl) to compile as C++17 and run on the
+// CPU in strict FP32.  Written
 // for this project; everything lives in namespace glsl so that unqualified
 // calls inside the shader code resolve to these overloads only.
 //
@@ -31,6 +33,7 @@ struct vec2 {
 
 struct ivec2;
 struct ivec3;
+struct uvec2;
 
 struct vec3 {
     union {
@@ -64,6 +67,7 @@ struct ivec2 {
     ivec2() = default;
     ivec2(int a, int b) : x(a), y(b) {}
     explicit ivec2(const vec2& v) : x((int)v.x), y((int)v.y) {}
+    explicit ivec2(const uvec2& v);
     operator vec2() const { return vec2((float)x, (float)y); }
 };
 
@@ -191,6 +195,80 @@ inline vec4 texture(const sampler2D&, vec2) { return vec4(1.0f); }
 inline ivec2 textureSize(const sampler2D& s, int) { return ivec2(s.n[0], s.n[1]); }
 
 struct subpassInput { int unused; };
+
+// ---- compute shaders and storage images --------------------------------------
+// Enough for share/shaders/transparency/resolve.comp and ppll.glsl.  An
+// rgba8 image holds one 32-bit word per texel, red in the low byte; its
+// loads and stores convert as unpackUnorm4x8 / packUnorm4x8 do (Vulkan's
+// UNORM conversions: c / 255, and clamp to [0, 1] then the nearest of the
+// two closest codes -- ties, which the specs leave open, go to even here).
+struct uvec2 {
+    uint x, y;
+};
+struct uvec3 {
+    union {
+        struct { uint x, y, z; };
+        uvec2 xy;
+    };
+    uvec3() = default;
+    uvec3(uint a, uint b, uint c) : x(a), y(b), z(c) {}
+};
+struct uvec4 {
+    union {
+        struct { uint x, y, z, w; };
+        struct { uint r, g, b, a; };
+    };
+    uvec4() = default;
+    uvec4(uint p, uint q, uint s, uint t) : x(p), y(q), z(s), w(t) {}
+};
+inline ivec2::ivec2(const uvec2& v) : x((int)v.x), y((int)v.y) {}
+
+inline vec4 mix(vec4 x, vec4 y, float a) { return x * (1.0f - a) + y * a; }
+
+inline vec4 unpackUnorm4x8(uint c)
+{
+    return vec4((float)(c & 0xffu) / 255.0f, (float)((c >> 8) & 0xffu) / 255.0f, (float)((c >> 16) & 0xffu) / 255.0f,
+                (float)((c >> 24) & 0xffu) / 255.0f);
+}
+
+inline uint unorm8_code(float x)
+{
+    x = x > 0.0f ? (x < 1.0f ? x : 1.0f) : 0.0f;
+    return (uint)std::nearbyint(x * 255.0f);
+}
+
+inline uint packUnorm4x8(vec4 v)
+{
+    return unorm8_code(v.x) | unorm8_code(v.y) << 8 | unorm8_code(v.z) << 16 | unorm8_code(v.w) << 24;
+}
+
+struct uimage2D { // r32ui
+    uint* data;
+    int width, height;
+};
+struct image2D { // rgba8
+    uint* data;
+    int width, height;
+};
+
+inline std::size_t texel_at(int width, ivec2 p) { return (std::size_t)p.y * (std::size_t)width + (std::size_t)p.x; }
+inline uvec4 imageLoad(const uimage2D& im, ivec2 p) { return uvec4(im.data[texel_at(im.width, p)], 0u, 0u, 1u); }
+inline uint imageAtomicExchange(uimage2D& im, ivec2 p, uint v)
+{
+    uint& t = im.data[texel_at(im.width, p)];
+    const uint old = t;
+    t = v;
+    return old;
+}
+inline vec4 imageLoad(const image2D& im, ivec2 p) { return unpackUnorm4x8(im.data[texel_at(im.width, p)]); }
+inline void imageStore(image2D& im, ivec2 p, vec4 v) { im.data[texel_at(im.width, p)] = packUnorm4x8(v); }
+
+inline uint atomicAdd(uint& mem, uint v)
+{
+    const uint old = mem;
+    mem += v;
+    return old;
+}
 
 } // namespace glsl
 

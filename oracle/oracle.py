@@ -66,6 +66,12 @@ def lib():
         _lib.oracle_raymarch_f32.argtypes = [C.POINTER(_abi.RaymarchParams), P, P, P, P, P, C.c_int, C.c_int,
                                              C.c_int]
         _lib.oracle_max_threads.restype = C.c_int
+        _lib.oracle_pack_unorm8x4.argtypes = [P]
+        _lib.oracle_pack_unorm8x4.restype = C.c_uint32
+        _lib.oracle_resolve_ppll.argtypes = [P, P, C.c_uint32, C.c_int, C.c_int, P, C.c_int]
+        _lib.oracle_resolve_ppll.restype = C.c_int
+        _lib.oracle_composite.argtypes = [P, C.c_uint32, P, P, C.c_int, C.c_int, P, C.c_int]
+        _lib.oracle_composite.restype = C.c_int
     return _lib
 
 
@@ -91,6 +97,10 @@ def ref():
         _ref.ref_hair_save.restype = C.c_int
         _ref.ref_reduce.argtypes = [P, P, C.c_uint32, P, C.c_uint32, C.c_uint32, C.c_float, C.POINTER(C.c_uint64), P,
                                     P, P, U32P, U32P]
+        _ref.ref_resolve_ppll.argtypes = [P, P, C.c_uint32, C.c_int, C.c_int, P, C.c_int]
+        _ref.ref_resolve_ppll.restype = C.c_int
+        _ref.ref_build_ppll.argtypes = [P, C.c_uint32, P, P, C.c_int, C.c_int, C.c_uint32, P, P]
+        _ref.ref_build_ppll.restype = C.c_uint32
     return _ref
 
 
@@ -312,3 +322,66 @@ def ref_raymarch(params, density, tangent, depth_in=None, rows=None, threads=0):
     if rc != 0:
         raise ValueError("the reference shader supports reference semantics only (shadow_steps <= 0, kd == 1)")
     return rgba, depth
+
+
+# ---- compositing -------------------------------------------------------------
+
+def _frags(fragments):
+    return np.ascontiguousarray(fragments, dtype=_abi.FRAGMENT_DTYPE)
+
+
+def _volume(volume_rgba, volume_depth):
+    if volume_rgba is None:
+        return None, None
+    return _f32(volume_rgba), _f32(volume_depth)
+
+
+def pack_unorm8x4(rgba):
+    v = _f32(rgba)
+    return int(lib().oracle_pack_unorm8x4(_p(v)))
+
+
+def resolve_ppll(heads, nodes, color, threads=0):
+    """resolve.comp over a PPLL (restatement): returns (status, new colour image)."""
+    out = np.array(color, dtype=np.uint32, copy=True)
+    h = np.ascontiguousarray(heads, dtype=np.uint32)
+    n = np.ascontiguousarray(nodes, dtype=_abi.PPLL_NODE_DTYPE)
+    H, W = out.shape
+    rc = lib().oracle_resolve_ppll(_p(h), _p(n), len(n), W, H, _p(out), threads)
+    return rc, out
+
+
+def composite(fragments, color, volume_rgba=None, volume_depth=None, threads=0):
+    """The PPLL-free composite (restatement): the new colour image; ValueError
+    when a fragment's pixel is outside the image."""
+    out = np.array(color, dtype=np.uint32, copy=True)
+    f = _frags(fragments)
+    vr, vd = _volume(volume_rgba, volume_depth)
+    H, W = out.shape
+    rc = lib().oracle_composite(_p(f), len(f), _p(vr), _p(vd), W, H, _p(out), threads)
+    if rc != 0:
+        raise ValueError("fragment pixel outside the image" if rc == -1 else "out of memory")
+    return out
+
+
+def ref_build_ppll(fragments, width, height, volume_rgba=None, volume_depth=None, capacity=None):
+    """The reference's ppll.glsl appends (strand fragments in buffer order, then
+    the volume fragments): (heads, nodes, node counter)."""
+    f = _frags(fragments)
+    vr, vd = _volume(volume_rgba, volume_depth)
+    if capacity is None:
+        capacity = len(f) + width * height
+    heads = np.zeros((height, width), dtype=np.uint32)
+    nodes = np.zeros(capacity + 1, dtype=_abi.PPLL_NODE_DTYPE)
+    used = ref().ref_build_ppll(_p(f), len(f), _p(vr), _p(vd), width, height, capacity, _p(heads), _p(nodes))
+    return heads, nodes, int(used)
+
+
+def ref_resolve_ppll(heads, nodes, color, threads=0):
+    """The reference's resolve.comp (compiled as C++) over a PPLL: the new colour image."""
+    out = np.array(color, dtype=np.uint32, copy=True)
+    h = np.ascontiguousarray(heads, dtype=np.uint32)
+    n = np.ascontiguousarray(nodes, dtype=_abi.PPLL_NODE_DTYPE)
+    H, W = out.shape
+    ref().ref_resolve_ppll(_p(h), _p(n), len(n), W, H, _p(out), threads)
+    return out

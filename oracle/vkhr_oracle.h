@@ -102,6 +102,28 @@ void oracle_raymarch_f32(const vkhr_raymarch_params* p, const void* density, con
 
 int oracle_max_threads(void);
 
+/* ---- compositing (resolve.c) ---------------------------------------------
+ * Colours are RGBA8 words, red in the low byte (packUnorm4x8's order). */
+
+/* Vulkan's float -> UNORM8 conversion of 4 channels: clamp to [0, 1] (NaN to
+ * 0), scale by 255, nearest code with ties to even. */
+uint32_t oracle_pack_unorm8x4(const float v[4]);
+
+/* resolve.comp:15-101 over the reference's PPLL: heads (width*height words,
+ * 0xffffffff = empty), nodes of 3 words {color, depth bits, prev}.  color is
+ * read as the background and written where a list is non-empty.  Returns 0,
+ * or -1 when a list links a node index >= node_count (that list ends there). */
+int oracle_resolve_ppll(const uint32_t* heads, const uint32_t* nodes, uint32_t node_count, int width, int height,
+                        uint32_t* color, int threads);
+
+/* The PPLL-free composite: fragments of 3 words {color, depth bits, pixel};
+ * a pixel holds a volume fragment where volume_depth < 1 (volume_rgba /
+ * volume_depth may be NULL).  Each pixel resolves the list a PPLL holds after
+ * the fragments were linked in buffer order and the volume fragment last.
+ * Returns 0, or -1 (nothing written) when a pixel index is out of range. */
+int oracle_composite(const uint32_t* fragments, uint32_t fragment_count, const float* volume_rgba,
+                     const float* volume_depth, int width, int height, uint32_t* color, int threads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -68,3 +68,78 @@ def image_errors(gpu, ref, diag, **kw):
     rms = np.sqrt((d[ok] ** 2).mean(axis=0)) if ok.any() else np.zeros(4)
     mx = d[ok].max(axis=0) if ok.any() else np.zeros(4)
     return rms, mx, int(ill.sum()), int(emitted.sum())
+
+
+# ---- compositing cases -----------------------------------------------------------
+# Depths the k-buffer treats specially: 0 and below never count as "furthest"
+# (resolve.comp:48-57 starts from 0), NaN compares false, 3e38 is the empty
+# slots' depth, above it and +inf beat the empty slots.
+SPECIAL_DEPTHS = np.array([0.0, -0.25, np.nan, np.inf, np.float32(3e38), np.float32(3.2e38), 0.5, 1.0],
+                          dtype=np.float32)
+
+# per-pixel fragment counts that reach every slice tier and both resolve
+# phases (k-buffer only, tail, past the 1040 nodes a pixel resolves)
+TIER_COUNTS = [0, 1, 2, 5, 8, 9, 16, 17, 32, 33, 100, 128, 129, 400, 512, 513, 1039, 1040, 1041, 2048, 2049, 3000]
+
+
+def fragment_case(width, height, counts, seed, tie_levels=None, special_rate=0.02):
+    """Strand fragments, counts[p] of them at pixel p, in a shuffled buffer
+    order; random RGBA8 colours; depths in [0, 1), rounded to tie_levels
+    levels when given (so that equal depths occur), a few special values."""
+    rng = np.random.default_rng(seed)
+    counts = np.asarray(counts, dtype=np.int64)
+    assert counts.size == width * height
+    pix = np.repeat(np.arange(width * height, dtype=np.uint32), counts)
+    rng.shuffle(pix)
+    f = np.zeros(len(pix), dtype=_abi.FRAGMENT_DTYPE)
+    f["pixel"] = pix
+    f["color"] = rng.integers(0, 1 << 32, len(pix), dtype=np.uint64).astype(np.uint32)
+    d = rng.random(len(pix), dtype=np.float32)
+    if tie_levels:
+        d = (np.floor(d * tie_levels) / tie_levels).astype(np.float32)
+    if special_rate and len(pix):
+        sel = rng.random(len(pix)) < special_rate
+        d[sel] = rng.choice(SPECIAL_DEPTHS, int(sel.sum()))
+    f["depth"] = d
+    return f
+
+
+def volume_case(width, height, seed, coverage=0.5):
+    """A raymarch-like volume image: RGBA a little outside [0, 1] (packing
+    clamps), depth below 1 on about `coverage` of the pixels, 1 elsewhere,
+    a few NaN depths (no fragment)."""
+    rng = np.random.default_rng(seed)
+    rgba = rng.uniform(-0.1, 1.1, (height, width, 4)).astype(np.float32)
+    depth = rng.random((height, width), dtype=np.float32)
+    depth[rng.random((height, width)) >= coverage] = 1.0
+    depth[rng.random((height, width)) < 0.01] = np.nan
+    return rgba, depth
+
+
+def background_case(width, height, seed):
+    rng = np.random.default_rng(seed)
+    return rng.integers(0, 1 << 32, (height, width), dtype=np.uint64).astype(np.uint32)
+
+
+def build_ppll(fragments, width, height, seed=None):
+    """The PPLL that linking `fragments` in buffer order builds (each new node
+    becomes its pixel's head, its `prev` the old head).  With a seed the nodes
+    are stored in a shuffled order (node indices are arbitrary in a PPLL)."""
+    n = len(fragments)
+    pix = fragments["pixel"].astype(np.int64)
+    slot = np.arange(n, dtype=np.int64)
+    if seed is not None:
+        slot = np.random.default_rng(seed).permutation(n)
+    order = np.argsort(pix, kind="stable")
+    prev = np.full(n, _abi.PPLL_NULL, dtype=np.uint32)
+    same = pix[order][1:] == pix[order][:-1]
+    prev[order[1:][same]] = slot[order[:-1][same]]
+    nodes = np.zeros(n, dtype=_abi.PPLL_NODE_DTYPE)
+    nodes["color"][slot] = fragments["color"]
+    nodes["depth"][slot] = fragments["depth"]
+    nodes["prev"][slot] = prev
+    heads = np.full(width * height, _abi.PPLL_NULL, dtype=np.uint32)
+    last = np.ones(n, dtype=bool)
+    last[order[:-1][same]] = False
+    heads[pix[last]] = slot[last]
+    return heads.reshape(height, width), nodes

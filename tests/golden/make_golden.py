@@ -3,11 +3,14 @@
 Runs the reference's voxelizer (src/vkhr/scene_graph/hair_style.cc, compiled
 unmodified into oracle/_ref by `make -C oracle ref`) and its raymarch shader
 (share/shaders/volumes/volume.frag and includes, compiled as C++) on small
-seeded synthetic styles, and stores inputs and outputs as .npz files.
+seeded synthetic styles, and its PPLL appends and resolve (ppll.glsl,
+resolve.comp, compiled as C++) on seeded fragments, and stores inputs and
+outputs as .npz files.
 Needs the reference sources; run from the repository root:
 
     make -C oracle ref && python tests/golden/make_golden.py
-    python tests/golden/make_golden.py reduce   # the strand-reduction fixtures only
+    python tests/golden/make_golden.py reduce     # the strand-reduction fixtures only
+    python tests/golden/make_golden.py composite  # the PPLL resolve fixture only
 """
 import os
 import sys
@@ -68,7 +71,28 @@ def reduce_case(name, st, seed, ratios):
     assert O.ref_hair_save(os.path.join(OUT, name + ".hair"), st.segments, st.vertices, t) == 0
 
 
+def composite_case(name, width, height, counts, seed):
+    """The reference's PPLL appends (ppll.glsl's ppll_next_node / node_data /
+    link_node, strand fragments in buffer order, then the volume fragments)
+    and its resolve.comp on that PPLL, both compiled as C++."""
+    from tests._helpers import background_case, fragment_case, volume_case
+
+    f = fragment_case(width, height, counts, seed, tie_levels=256)
+    bg = background_case(width, height, seed + 1)
+    vr, vd = volume_case(width, height, seed + 2)
+    heads, nodes, used = O.ref_build_ppll(f, width, height, vr, vd)
+    nodes = nodes[:used]
+    color = O.ref_resolve_ppll(heads, nodes, bg)
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), fragments=f, background=bg, volume_rgba=vr,
+                        volume_depth=vd, heads=heads, nodes=nodes, color=color)
+
+
 def main():
+    if sys.argv[1:] == ["composite"]:  # only the compositing fixture
+        from tests._helpers import TIER_COUNTS
+
+        composite_case("composite_tiers", 11, 2, TIER_COUNTS, 21)
+        return
     if sys.argv[1:] == ["reduce"]:  # only the strand-reduction fixtures
         reduce_case("reduce_hemisphere", strands.hemisphere_style(256, 8, seed=16), 0x9E3779B97F4A7C15,
                     [1.0, 0.5, 0.984375, 0.015625])

@@ -73,7 +73,7 @@ def test_extension_knobs(ctx, oracle_lib):
     """kd 0.4, 32-step shadows, a hybrid-renderer LoD blend and non-power-of-two steps."""
     b, c, dn, tq = _volume(oracle_lib, "hemi", 4096, 16, (64, 64, 64))
     p = scene.make_params(b, (64, 64, 64), 320, 240, raycast_steps=201.0, shadow_steps=32.0, kd=0.4,
-                          renderer=_abi.RENDERER_HYBRID, hair_alpha=0.8)
+                          renderer=_abi.RENDERER_HYBRID_LOD, hair_alpha=0.8)
     p.magnified_distance, p.minified_distance = 2.0, 6.0
     ref, rdepth, diag = oracle_lib.raymarch(p, dn, tq, diag=True)
     gpu, gdepth = _gpu_raymarch(ctx, p, dn, tq)

@@ -5,6 +5,8 @@ library exports ``vkhr_sizeof_*`` helpers and the tests compare them.
 """
 import ctypes as C
 
+import numpy as np
+
 VKHR_OK = 0
 VKHR_ERR_INVALID_ARG = 1
 VKHR_ERR_DEGENERATE_AABB = 2
@@ -49,8 +51,17 @@ SHADING_ADSM = 2
 SHADING_LAO = 3
 
 RENDERER_RASTERIZER = 0
-RENDERER_HYBRID = 1
+RENDERER_RAY_TRACER = 1
 RENDERER_RAYMARCHER = 2
+RENDERER_HYBRID_LOD = 3
+
+
+# vkhr_ppll_node (ppll.glsl:7-11) and vkhr_fragment: 12 bytes each
+PPLL_NULL = 0xFFFFFFFF
+K_BUFFER_SIZE = 16
+MAX_FRAGMENTS = 1024
+PPLL_NODE_DTYPE = np.dtype([("color", "<u4"), ("depth", "<f4"), ("prev", "<u4")])
+FRAGMENT_DTYPE = np.dtype([("color", "<u4"), ("depth", "<f4"), ("pixel", "<u4")])
 
 
 class AABB(C.Structure):

@@ -23,6 +23,8 @@ EXPORTS = [
     "vkhr_splat_vertices", "vkhr_splat_vertices_adjoint", "vkhr_autotune_raymarch", "vkhr_set_raymarch_variant",
     "vkhr_frame_graph_create", "vkhr_frame_graph_launch", "vkhr_frame_graph_destroy",
     "vkhr_hair_read_header", "vkhr_hair_load", "vkhr_reduce_strands",
+    "vkhr_resolve_ppll", "vkhr_composite", "vkhr_level_of_detail", "vkhr_lod", "vkhr_rasterizer_enabled",
+    "vkhr_raymarcher_enabled",
 ]
 
 _lib = None
@@ -85,6 +87,14 @@ def load():
     lib.vkhr_reduce_strands.argtypes = [P, C.c_float, C.POINTER(C.c_uint64), P, C.c_uint32, C.c_uint32, P, P, P, U32P,
                                         U32P, P, P, P]
     lib.vkhr_frame_graph_destroy.argtypes = [P]
+    lib.vkhr_resolve_ppll.argtypes = [P, P, P, C.c_uint32, C.c_int32, C.c_int32, P, P]
+    lib.vkhr_composite.argtypes = [P, P, C.c_uint32, P, P, C.c_int32, C.c_int32, P, P]
+    lib.vkhr_level_of_detail.argtypes = [C.c_float, C.c_float, C.c_float]
+    lib.vkhr_level_of_detail.restype = C.c_float
+    lib.vkhr_lod.argtypes = [C.c_int32, C.c_float, C.c_float, C.c_float]
+    lib.vkhr_lod.restype = C.c_float
+    lib.vkhr_rasterizer_enabled.argtypes = [C.c_int32, C.c_float]
+    lib.vkhr_raymarcher_enabled.argtypes = [C.c_int32, C.c_float]
     lib.vkhr_raymarch.argtypes = [P, C.POINTER(_abi.RaymarchParams), P, P, P, P, P, P]
     lib.vkhr_malloc.argtypes = [P, C.c_size_t, C.POINTER(C.c_void_p)]
     lib.vkhr_free.argtypes = [P, P]
@@ -242,6 +252,18 @@ class Context:
                                                 d_vertices_out, d_tangents_out, stream))
         return out[:ns.value], nv.value, sd.value
 
+    def resolve_ppll(self, d_heads, d_nodes, node_count, width, height, d_color, stream=None):
+        """vkhr_resolve_ppll: resolve.comp over the reference's PPLL onto d_color."""
+        self.check(self.lib.vkhr_resolve_ppll(self.handle, d_heads, d_nodes, node_count, width, height, d_color,
+                                              stream))
+
+    def composite(self, d_fragments, fragment_count, width, height, d_color, d_volume_rgba=None,
+                  d_volume_depth=None, stream=None):
+        """vkhr_composite: the PPLL-free resolve of strand fragments (and the
+        raymarched volume's fragments) onto d_color."""
+        self.check(self.lib.vkhr_composite(self.handle, d_fragments, fragment_count, d_volume_rgba, d_volume_depth,
+                                           width, height, d_color, stream))
+
     def raymarch_batched(self, jobs, stream=None):
         """jobs: a sequence of _abi.RaymarchJob."""
         arr = (_abi.RaymarchJob * len(jobs))(*jobs)
@@ -310,6 +332,24 @@ def hair_read_header(path):
     if st != 0:
         raise VkhrError(st, "vkhr_hair_read_header(%s)" % path)
     return h
+
+
+def level_of_detail(magnified_distance, minified_distance, distance):
+    """vkhr_level_of_detail: Rasterizer::update's smoothstep (no CUDA call)."""
+    return load().vkhr_level_of_detail(magnified_distance, minified_distance, distance)
+
+
+def lod(renderer, magnified_distance, minified_distance, distance):
+    """vkhr_lod: scheme.glsl's lod() (no CUDA call)."""
+    return load().vkhr_lod(renderer, magnified_distance, minified_distance, distance)
+
+
+def rasterizer_enabled(renderer, level):
+    return bool(load().vkhr_rasterizer_enabled(renderer, level))
+
+
+def raymarcher_enabled(renderer, level):
+    return bool(load().vkhr_raymarcher_enabled(renderer, level))
 
 
 def raymarch_footprint(params):

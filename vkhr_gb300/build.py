@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libvkhr_cuda.so")
 BUILD = os.path.join(HERE, "_build")
-SOURCES = ["context.cu", "prepare.cu", "voxelize.cu", "raymarch.cu", "adjoint.cu", "frame.cu", "hair.cu"]
+SOURCES = ["context.cu", "prepare.cu", "voxelize.cu", "raymarch.cu", "adjoint.cu", "frame.cu", "hair.cu", "composite.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -16,6 +16,7 @@ enum : unsigned {
     VKHR_DEV_LIST_OVERFLOW = 2u,    // fixed-capacity visit list too small
     VKHR_DEV_TIMEOUT = 4u,          // a bounded device wait gave up
     VKHR_DEV_REPLAY_MISMATCH = 8u,  // a brick replay disagreed with its binning (internal error)
+    VKHR_DEV_BAD_INDEX = 16u,       // compositing: a fragment's pixel or a PPLL link outside its array
 };
 
 // Slots of the small device word array every context owns.
@@ -43,6 +44,8 @@ struct vkhr_ctx {
     int l2_bytes;              // L2 cache size
     uint32_t direct_cap;       // voxelizer: per-brick slice capacity of one-walk calls (0: not yet known)
     uint4* d_gather;           // strand reduction: the kept strands' (source, destination, vertices)
+    uint32_t* comp;            // compositing: per-pixel counts, slice starts, sort queues, fragment keys
+    size_t comp_cap;           // (in 32-bit words)
     size_t d_gather_cap;
     void* slots;               // voxelizer: the fixed per-brick slices of one-walk calls
     size_t slots_cap;          // (in 8-byte units)

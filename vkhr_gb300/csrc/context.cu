@@ -156,7 +156,7 @@ vkhr_status vkhr_destroy(vkhr_ctx* ctx)
     cudaSetDevice(ctx->device);
     cudaDeviceSynchronize();
     void* bufs[] = {ctx->brick_runs, ctx->items, ctx->brick_list, ctx->pair_rec, ctx->pair_tan, ctx->hkeys, ctx->hdesc,
-                    ctx->d_jobs, ctx->d_rjobs, ctx->g_acc, ctx->slots, ctx->d_gather};
+                    ctx->d_jobs, ctx->d_rjobs, ctx->g_acc, ctx->slots, ctx->d_gather, ctx->comp};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (ctx->occ) cudaFree(ctx->occ);

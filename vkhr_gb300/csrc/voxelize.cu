@@ -1210,6 +1210,8 @@ vkhr_status check_device_status(vkhr_ctx* ctx, unsigned long long s)
                          "a segment spans more than 2^24 voxels (vertices far outside the bounds)");
     if (s & VKHR_DEV_LIST_OVERFLOW) return vkhr_fail(ctx, VKHR_ERR_CAPACITY, "visit list overflow");
     if (s & VKHR_DEV_REPLAY_MISMATCH) return vkhr_fail(ctx, VKHR_ERR_CUDA, "brick replay disagreed with binning");
+    if (s & VKHR_DEV_BAD_INDEX)
+        return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "a fragment's pixel or a PPLL node link is out of range");
     return VKHR_OK;
 }
 
@@ -1562,7 +1564,11 @@ vkhr_status vkhr_check_status(vkhr_ctx* ctx, void* stream)
     VKHR_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->h_words, ctx->d_words, WORD_NORM * sizeof(unsigned long long),
                                        cudaMemcpyDeviceToHost, (cudaStream_t)stream));
     VKHR_CUDA_TRY(ctx, cudaStreamSynchronize((cudaStream_t)stream));
-    return check_device_status(ctx, ctx->h_words[WORD_STATUS]);
+    const unsigned long long status = ctx->h_words[WORD_STATUS];
+    if (status) // reported once: the next check starts clean
+        VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_words + WORD_STATUS, 0, sizeof(unsigned long long),
+                                           (cudaStream_t)stream));
+    return check_device_status(ctx, status);
 }
 
 vkhr_status vkhr_normalize_densities(vkhr_ctx* ctx, uint8_t* d, uint64_t n, void* stream)

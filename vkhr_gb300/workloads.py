@@ -74,3 +74,54 @@ def sway(vertices, amount):
     out = v.copy()
     out[:, 0] += amount * h * h
     return out.astype(np.float32)
+
+
+def strand_fragments(vertices, tangents, indices, params, lod, device):
+    """Synthetic strand-rasterizer output for the compositing step, on the
+    device: each segment projected with params' camera and sampled once per
+    pixel step along its major screen axis (at most 64 samples), in segment
+    order, like one-pixel lines rasterized in primitive order.  Colour: the
+    hair colour lit by |tangent . light| (a stand-in for strand.frag's shading),
+    coverage hair_alpha * (1 - lod) (strand.frag:39-42); depth is the clip-space
+    z / w the rasterizer interpolates.  Samples outside the image or the depth
+    range are dropped.  Returns a (fragment_count, 3) int32 tensor laid out as
+    vkhr_fragment {color, depth bits, pixel}."""
+    import torch
+
+    W, H = params.width, params.height
+    view = np.asarray(params.view, dtype=np.float64).reshape(4, 4).T
+    proj = np.asarray(params.projection, dtype=np.float64).reshape(4, 4).T
+    m = torch.as_tensor((proj @ view).astype(np.float32), device=device)
+    v = torch.as_tensor(np.ascontiguousarray(vertices, dtype=np.float32), device=device)
+    clip = v @ m[:3, :3].T + m[:3, 3]
+    w = v @ m[3, :3] + m[3, 3]
+    sx = (clip[:, 0] / w * 0.5 + 0.5) * W
+    sy = (clip[:, 1] / w * 0.5 + 0.5) * H
+    sz = clip[:, 2] / w
+    idx = torch.as_tensor(np.ascontiguousarray(indices).view(np.int32).astype(np.int64), device=device)
+    a, b = idx[0::2], idx[1::2]
+    length = torch.maximum((sx[b] - sx[a]).abs(), (sy[b] - sy[a]).abs())
+    n = torch.clamp(torch.ceil(length), 1, 64).to(torch.int64)
+    seg = torch.repeat_interleave(torch.arange(len(a), device=device), n)
+    first = torch.cumsum(n, 0) - n
+    k = torch.arange(len(seg), device=device) - first[seg]
+    t = (k.to(torch.float32) + 0.5) / n[seg].to(torch.float32)
+    x = sx[a[seg]] + t * (sx[b[seg]] - sx[a[seg]])
+    y = sy[a[seg]] + t * (sy[b[seg]] - sy[a[seg]])
+    z = sz[a[seg]] + t * (sz[b[seg]] - sz[a[seg]])
+    keep = (x >= 0) & (x < W) & (y >= 0) & (y < H) & (z >= 0) & (z <= 1)
+    seg, x, y, z = seg[keep], x[keep], y[keep], z[keep]
+    tan = torch.as_tensor(np.ascontiguousarray(tangents, dtype=np.float32), device=device)[a[seg]]
+    ld = np.asarray(params.light_origin, dtype=np.float64) - np.asarray(params.camera_position, dtype=np.float64)
+    ld = torch.as_tensor((ld / np.linalg.norm(ld)).astype(np.float32), device=device)
+    shade = 0.35 + 0.65 * (tan @ ld).abs()
+    hc = torch.as_tensor(np.asarray(params.hair_color, dtype=np.float32), device=device)
+    rgb = torch.clamp(hc[None, :] * shade[:, None] * 2.0, 0, 1)
+    alpha = torch.full_like(shade, float(params.hair_alpha) * (1.0 - float(lod)))
+    q = torch.round(torch.cat([rgb, alpha[:, None]], 1) * 255.0).to(torch.int64)
+    color = q[:, 0] | (q[:, 1] << 8) | (q[:, 2] << 16) | (q[:, 3] << 24)
+    out = torch.empty((len(seg), 3), dtype=torch.int32, device=device)
+    out[:, 0] = (color - ((color >> 31) << 32)).to(torch.int32)
+    out[:, 1] = z.contiguous().view(torch.int32)
+    out[:, 2] = (y.to(torch.int64) * W + x.to(torch.int64)).to(torch.int32)
+    return out
