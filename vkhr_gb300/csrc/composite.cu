@@ -32,7 +32,6 @@ constexpr int kK = VKHR_K_BUFFER_SIZE;     // 16
 constexpr int kTail = VKHR_MAX_FRAGMENTS;  // 1024
 constexpr uint32_t kList = kK + kTail;     // nodes one pixel can resolve
 constexpr uint32_t kNull = VKHR_PPLL_NULL;
-constexpr float kMaxDepth = 3.e+38f;       // PPLL_MAXIMUM_DEPTH
 
 constexpr int kScanThreads = 1024;
 constexpr int kScanItems = 4 * kScanThreads;  // values per scan block
@@ -297,33 +296,43 @@ __global__ void __launch_bounds__(256) slice_bounds_kernel(const uint32_t* __res
 }
 
 // ---- resolve --------------------------------------------------------------------------
-// resolve.comp:15-101 for one pixel, the k-buffer in registers.  Empty slots
-// (depth 3e38, colour 0) blend as no-ops, so the back-to-front pass runs once
-// per filled slot only: the filled slots keep their order among themselves,
-// and once no depth above 0 is left the shader blends slot 0 again, as here.
+// resolve.comp:15-101 for one pixel.  The k-buffer lives in shared memory,
+// slot k of thread t at [k * kResolveThreads + t]: a lane's dynamic slot always
+// falls in its own bank, and a swap is three accesses.  Empty slots (depth
+// 3e38, colour 0) blend as no-ops, so the back-to-front pass runs once per
+// filled slot only: the filled slots keep their order among themselves, and
+// once no depth above 0 is left the shader blends slot 0 again, as here.
 // During the tail the furthest slot is a function of the k-buffer alone, so
 // it is searched again only after a swap changed the k-buffer.
+constexpr int kResolveThreads = 256;
+
 struct KBuffer {
-    float kd[kK];
-    uint32_t kc[kK];
+    float* kd;     // this thread's slot 0 (stride kResolveThreads)
+    uint32_t* kc;
     int m;         // filled slots
     float fd;      // furthest depth and slot (valid unless stale)
     int fi;
     bool stale;
     float4 r;      // the blended colour
 
-    __device__ __forceinline__ void init(uint32_t background, const float* tab)
+    __device__ __forceinline__ float& d(int k) { return kd[k * kResolveThreads]; }
+    __device__ __forceinline__ uint32_t& c(int k) { return kc[k * kResolveThreads]; }
+
+    __device__ __forceinline__ void init(float* sd, uint32_t* sc, uint32_t background, const float* tab)
     {
-#pragma unroll
-        for (int k = 0; k < kK; ++k) {
-            kd[k] = kMaxDepth;
-            kc[k] = 0u;
-        }
+        kd = sd + threadIdx.x;
+        kc = sc + threadIdx.x;
         m = 0;
         fd = 0.0f;
         fi = 0;
         stale = true;
         r = unpack(tab, background);
+    }
+
+    __device__ __forceinline__ void put(int k, Frag f)
+    {
+        d(k) = f.d;
+        c(k) = f.c;
     }
 
     // later nodes: blended as they come, each swapped first with the
@@ -334,24 +343,20 @@ struct KBuffer {
             fd = 0.0f;
             fi = 0;
 #pragma unroll
-            for (int k = 0; k < kK; ++k)
-                if (kd[k] > fd) {
-                    fd = kd[k];
+            for (int k = 0; k < kK; ++k) {
+                const float x = d(k);
+                if (x > fd) {
+                    fd = x;
                     fi = k;
                 }
+            }
             stale = false;
         }
         uint32_t bc = f.c;
         if (f.d < fd) {
-            // one-hot slot mask: selects by bit keep the k-buffer in registers
-            const uint32_t hot = 1u << fi;
-#pragma unroll
-            for (int k = 0; k < kK; ++k)
-                if (hot & (1u << k)) {
-                    bc = kc[k];
-                    kc[k] = f.c;
-                    kd[k] = f.d;
-                }
+            bc = c(fi);
+            c(fi) = f.c;
+            d(fi) = f.d;
             stale = true;
         }
         blend(r, tab, bc);
@@ -361,66 +366,116 @@ struct KBuffer {
     __device__ __forceinline__ uint32_t finish(const float* tab)
     {
         for (int it = 0; it < m; ++it) {
-            float d = 0.0f;
+            float x = 0.0f;
             int i = 0;
 #pragma unroll
             for (int k = 0; k < kK; ++k)
-                if (k < m && kd[k] > d) {
-                    d = kd[k];
-                    i = k;
+                if (k < m) {
+                    const float y = d(k);
+                    if (y > x) {
+                        x = y;
+                        i = k;
+                    }
                 }
-            uint32_t bc = 0u;
-            const uint32_t hot = 1u << i;
-#pragma unroll
-            for (int k = 0; k < kK; ++k)
-                if (hot & (1u << k)) {
-                    bc = kc[k];
-                    kd[k] = 0.0f;
-                }
-            blend(r, tab, bc);
+            d(i) = 0.0f;
+            blend(r, tab, c(i));
         }
         return pack(r);
     }
 };
 
+// ---- work list: pixels with fragments, longest lists first -----------------------
+// Lists longer than kList resolve kList nodes; lengths are bucketed by 65
+// (kList / 16) so that the lanes of a resolve warp run about as long.
+constexpr int kBuckets = 16;
+__device__ __forceinline__ uint32_t list_length(const uint32_t* start, const float* vol_depth, uint32_t p)
+{
+    uint32_t n = start ? start[p + 1] - start[p] : 0u;
+    if (vol_depth && vol_depth[p] < 1.0f) ++n;
+    return min(n, kList);
+}
+__device__ __forceinline__ int bucket_of(uint32_t len) { return kBuckets - 1 - min(kBuckets - 1, (int)((len - 1) / 65u)); }
+
+// words[0..15]: pixels per bucket; words[16..31]: fill cursors; words[32]: total
+__global__ void __launch_bounds__(256) worklist_count_kernel(const uint32_t* __restrict__ start,
+                                                             const float* __restrict__ vol_depth, uint32_t npix,
+                                                             uint32_t* __restrict__ words)
+{
+    __shared__ uint32_t h[kBuckets];
+    if (threadIdx.x < kBuckets) h[threadIdx.x] = 0u;
+    __syncthreads();
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < npix) {
+        const uint32_t len = list_length(start, vol_depth, p);
+        if (len) atomicAdd(&h[bucket_of(len)], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x < kBuckets && h[threadIdx.x]) atomicAdd(&words[threadIdx.x], h[threadIdx.x]);
+}
+
+__global__ void __launch_bounds__(256) worklist_fill_kernel(const uint32_t* __restrict__ start,
+                                                            const float* __restrict__ vol_depth, uint32_t npix,
+                                                            uint32_t* __restrict__ words, uint32_t* __restrict__ list)
+{
+    __shared__ uint32_t h[kBuckets], base[kBuckets];
+    if (threadIdx.x < kBuckets) h[threadIdx.x] = 0u;
+    __syncthreads();
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    int b = -1;
+    uint32_t rank = 0;
+    if (p < npix) {
+        const uint32_t len = list_length(start, vol_depth, p);
+        if (len) {
+            b = bucket_of(len);
+            rank = atomicAdd(&h[b], 1u);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < kBuckets) {
+        uint32_t off = 0;
+        for (int k = 0; k < (int)threadIdx.x; ++k) off += words[k];
+        base[threadIdx.x] = h[threadIdx.x] ? off + atomicAdd(&words[kBuckets + threadIdx.x], h[threadIdx.x]) : 0u;
+        if (threadIdx.x == kBuckets - 1 && blockIdx.x == 0) words[2 * kBuckets] = off + words[kBuckets - 1];
+    }
+    __syncthreads();
+    if (b >= 0) list[base[b] + rank] = p;
+}
+
 // A pixel's list without links: its volume fragment (when it has one), then
 // its slice of the pixel-sorted payloads from the last entry back.
 template <bool VOL>
-__global__ void __launch_bounds__(256) composite_resolve_kernel(const uint32_t* __restrict__ start,
-                                                                const unsigned long long* __restrict__ vals,
-                                                                const float4* __restrict__ vol_rgba,
-                                                                const float* __restrict__ vol_depth, uint32_t npix,
-                                                                uint32_t* __restrict__ color)
+__global__ void __launch_bounds__(kResolveThreads) composite_resolve_kernel(
+    const uint32_t* __restrict__ list, const uint32_t* __restrict__ list_words, const uint32_t* __restrict__ start,
+    const unsigned long long* __restrict__ vals, const float4* __restrict__ vol_rgba,
+    const float* __restrict__ vol_depth, uint32_t* __restrict__ color)
 {
     __shared__ float tab[256];
+    __shared__ float sd[kK * kResolveThreads];
+    __shared__ uint32_t sc[kK * kResolveThreads];
     fill_unorm_table(tab);
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= npix) return;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= list_words[2 * kBuckets]) return;
+    const uint32_t p = list[t];
     const uint32_t lo = start ? start[p] : 0u;
     const uint32_t hi = start ? start[p + 1] : 0u;
     int v = 0;
     Frag vf{0u, 0.0f};
     if (VOL) {
-        const float d = vol_depth[p];
-        if (d < 1.0f) {
+        const float dv = vol_depth[p];
+        if (dv < 1.0f) {
             v = 1;
-            vf = Frag{pack(vol_rgba[p]), d};
+            vf = Frag{pack(vol_rgba[p]), dv};
         }
     }
     const uint32_t total = min(hi - lo + (uint32_t)v, kList);
-    if (total == 0) return;
     KBuffer kb;
-    kb.init(color[p], tab);
+    kb.init(sd, sc, color[p], tab);
     // list entry e >= v is the slice's entry top - e, top = hi - 1 + v (>= lo)
     const uint32_t top = hi - 1u + (uint32_t)v;
     kb.m = (int)min(total, (uint32_t)kK);
 #pragma unroll
     for (int k = 0; k < kK; ++k)
-        if (k < kb.m) {
-            const Frag f = (VOL && k == 0 && v) ? vf : unpack_payload(__ldg(vals + (top - k)));
-            kb.kd[k] = f.d;
-            kb.kc[k] = f.c;
-        }
+        if (k < kb.m) kb.put(k, (VOL && k == 0 && v) ? vf : unpack_payload(__ldg(vals + (top - k))));
     // the tail in batches of 8, the next batch loading while one blends
     constexpr int kBatch = 8;
     unsigned long long cur[kBatch], nxt[kBatch];
@@ -440,12 +495,15 @@ __global__ void __launch_bounds__(256) composite_resolve_kernel(const uint32_t* 
 }
 
 // A PPLL list; a link outside the node array ends it and is recorded.
-__global__ void __launch_bounds__(256) ppll_resolve_kernel(const uint32_t* __restrict__ heads,
-                                                           const vkhr_ppll_node* __restrict__ nodes, uint32_t count,
-                                                           uint32_t npix, uint32_t* __restrict__ color,
-                                                           unsigned long long* words)
+__global__ void __launch_bounds__(kResolveThreads) ppll_resolve_kernel(const uint32_t* __restrict__ heads,
+                                                                       const vkhr_ppll_node* __restrict__ nodes,
+                                                                       uint32_t count, uint32_t npix,
+                                                                       uint32_t* __restrict__ color,
+                                                                       unsigned long long* words)
 {
     __shared__ float tab[256];
+    __shared__ float sd[kK * kResolveThreads];
+    __shared__ uint32_t sc[kK * kResolveThreads];
     fill_unorm_table(tab);
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npix) return;
@@ -453,20 +511,17 @@ __global__ void __launch_bounds__(256) ppll_resolve_kernel(const uint32_t* __res
     if (node == kNull) return; // resolve.comp:19-20
     bool bad = false;
     KBuffer kb;
-    kb.init(color[p], tab);
-#pragma unroll
-    for (int k = 0; k < kK; ++k) // resolve.comp:31-36
-        if (node != kNull && !bad) {
-            if (node >= count) {
-                bad = true;
-            } else {
-                const vkhr_ppll_node* nd = nodes + node;
-                kb.kd[k] = __ldg(&nd->depth);
-                kb.kc[k] = __ldg(&nd->color);
-                node = __ldg(&nd->prev);
-                kb.m = k + 1;
-            }
+    kb.init(sd, sc, color[p], tab);
+    for (int k = 0; k < kK && node != kNull; ++k) { // resolve.comp:31-36
+        if (node >= count) {
+            bad = true;
+            break;
         }
+        const vkhr_ppll_node* nd = nodes + node;
+        kb.put(k, Frag{__ldg(&nd->color), __ldg(&nd->depth)});
+        node = __ldg(&nd->prev);
+        kb.m = k + 1;
+    }
     for (int t = 0; t < kTail && node != kNull && !bad; ++t) {
         if (node >= count) {
             bad = true;
@@ -510,8 +565,8 @@ vkhr_status vkhr_resolve_ppll(vkhr_ctx* ctx, const uint32_t* d_heads, const vkhr
         return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "d_nodes is NULL or misaligned");
     cudaStream_t st = (cudaStream_t)stream;
     VKHR_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
-    VKHR_LAUNCH(ctx, ppll_resolve_kernel, vkhr_blocks(npix, 256), 256, 0, st, d_heads, d_nodes, node_count, npix,
-                d_color, ctx->d_words);
+    VKHR_LAUNCH(ctx, ppll_resolve_kernel, vkhr_blocks(npix, kResolveThreads), kResolveThreads, 0, st, d_heads, d_nodes,
+                node_count, npix, d_color, ctx->d_words);
     VKHR_CUDA_TRY(ctx, cudaGetLastError());
     return VKHR_OK;
 }
@@ -536,6 +591,9 @@ vkhr_status vkhr_composite(vkhr_ctx* ctx, const vkhr_fragment* d_fragments, uint
 
     const uint32_t* start = nullptr;
     const unsigned long long* vals = nullptr;
+    // work list: 64 words (bucket counts, cursors, total) and one entry a pixel
+    const size_t list_words_at = 0, list_at = 64;
+    const size_t list_need = list_at + ((size_t)npix + 3) / 4 * 4;
     if (fragment_count) {
         const uint32_t F = fragment_count;
         const uint32_t tiles = (F + kTile - 1) / kTile;
@@ -549,7 +607,7 @@ vkhr_status vkhr_composite(vkhr_ctx* ctx, const vkhr_fragment* d_fragments, uint
         auto round4 = [](size_t x) { return (x + 3) / 4 * 4; };
         // scratch (32-bit words, 16-byte aligned pieces):
         //   hist | partials | start | keys x2 | payloads x2
-        const size_t partials_at = round4(hist_n);
+        const size_t partials_at = list_need + round4(hist_n);
         const size_t start_at = partials_at + round4(nb);
         const size_t keys_at = start_at + round4((size_t)npix + 1);
         const size_t vals_at = keys_at + 2 * round4(F);
@@ -557,7 +615,7 @@ vkhr_status vkhr_composite(vkhr_ctx* ctx, const vkhr_fragment* d_fragments, uint
         s = vkhr_reserve(ctx, (void**)&ctx->comp, &ctx->comp_cap, need, sizeof(uint32_t));
         if (s != VKHR_OK) return s;
         uint32_t* w = ctx->comp;
-        uint32_t* d_hist = w;
+        uint32_t* d_hist = w + list_need;
         uint32_t* d_partials = w + partials_at;
         uint32_t* d_start = w + start_at;
         uint32_t* d_keys[2] = {w + keys_at, w + keys_at + round4(F)};
@@ -590,14 +648,23 @@ vkhr_status vkhr_composite(vkhr_ctx* ctx, const vkhr_fragment* d_fragments, uint
                     d_start);
         start = d_start;
         vals = d_vals[last];
+    } else {
+        s = vkhr_reserve(ctx, (void**)&ctx->comp, &ctx->comp_cap, list_need, sizeof(uint32_t));
+        if (s != VKHR_OK) return s;
     }
-    const unsigned rb = vkhr_blocks(npix, 256);
+    uint32_t* d_list_words = ctx->comp + list_words_at;
+    uint32_t* d_list = ctx->comp + list_at;
+    VKHR_CUDA_TRY(ctx, cudaMemsetAsync(d_list_words, 0, 64 * sizeof(uint32_t), st));
+    const unsigned pb = vkhr_blocks(npix, 256);
+    VKHR_LAUNCH(ctx, worklist_count_kernel, pb, 256, 0, st, start, d_volume_depth, npix, d_list_words);
+    VKHR_LAUNCH(ctx, worklist_fill_kernel, pb, 256, 0, st, start, d_volume_depth, npix, d_list_words, d_list);
+    const unsigned rb = vkhr_blocks(npix, kResolveThreads);
     if (d_volume_rgba)
-        VKHR_LAUNCH(ctx, composite_resolve_kernel<true>, rb, 256, 0, st, start, vals,
-                    reinterpret_cast<const float4*>(d_volume_rgba), d_volume_depth, npix, d_color);
+        VKHR_LAUNCH(ctx, composite_resolve_kernel<true>, rb, kResolveThreads, 0, st, d_list, d_list_words, start, vals,
+                    reinterpret_cast<const float4*>(d_volume_rgba), d_volume_depth, d_color);
     else
-        VKHR_LAUNCH(ctx, composite_resolve_kernel<false>, rb, 256, 0, st, start, vals, nullptr, nullptr, npix,
-                    d_color);
+        VKHR_LAUNCH(ctx, composite_resolve_kernel<false>, rb, kResolveThreads, 0, st, d_list, d_list_words, start,
+                    vals, nullptr, nullptr, d_color);
     VKHR_CUDA_TRY(ctx, cudaGetLastError());
     return VKHR_OK;
 }
