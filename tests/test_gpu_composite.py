@@ -204,3 +204,32 @@ def test_production_hybrid_frame(ctx, distance):
     want = O.composite(f, bg, vr, vd)
     assert np.array_equal(got, want)
     assert (got != bg).sum() > 3000
+
+
+def test_composite_in_a_cuda_graph(ctx):
+    """After one call at the same sizes the composite allocates nothing and
+    can be captured; the replayed graph gives the oracle's image."""
+    import torch
+
+    W, H = 97, 61
+    rng = np.random.default_rng(19)
+    f = fragment_case(W, H, rng.choice([0, 1, 4, 17, 60], W * H), 20)
+    bg = background_case(W, H, 21)
+    vr, vd = volume_case(W, H, 22)
+    df, dbg = _dev_u32(f, torch), _dev_u32(bg, torch)
+    dc = dbg.clone()
+    dvr, dvd = to_dev(vr, torch), to_dev(vd, torch)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        ctx.composite(df.data_ptr(), len(f), W, H, dc.data_ptr(), dvr.data_ptr(), dvd.data_ptr(), stream=s.cuda_stream)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        ctx.composite(df.data_ptr(), len(f), W, H, dc.data_ptr(), dvr.data_ptr(), dvd.data_ptr(),
+                      stream=torch.cuda.current_stream().cuda_stream)
+    want = O.composite(f, bg, vr, vd)
+    for _ in range(2):
+        dc.copy_(dbg)
+        g.replay()
+        torch.cuda.synchronize()
+        assert np.array_equal(dc.cpu().numpy().view(np.uint32).reshape(H, W), want)
