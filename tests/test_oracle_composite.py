@@ -154,3 +154,31 @@ def test_level_of_detail_helpers(native_lib):
         for lv in (0.0, 0.5, 1.0):
             assert N.rasterizer_enabled(r, lv) == (r == 0 or (r == 3 and lv != 1.0))
             assert N.raymarcher_enabled(r, lv) == (r == 2 or (r == 3 and lv != 0.0))
+
+
+def test_rasterized_strands_match_reference():
+    """Fragments as a strand rasterizer emits them: the synthetic one-pixel
+    lines of workloads.strand_fragments (primitive order, tens of fragments
+    on a pixel), composited over a raymarch-like volume image; the oracle's
+    PPLL-free composite equals the reference's own appends and resolve."""
+    R = _ref()
+    from vkhr_gb300 import scene, workloads
+    from tests._helpers import style
+
+    st, t, idx = style("hemi", 1500, 10, seed=23)
+    b = O.bounding_box(st.vertices)
+    W, H = 96, 64
+    p = scene.make_params(b, (32, 32, 32), W, H, camera_distance=6.0, renderer=_abi.RENDERER_HYBRID_LOD)
+    f = workloads.strand_fragments(st.vertices, t, idx, p, 0.25, "cpu").numpy().view(_abi.FRAGMENT_DTYPE).reshape(-1)
+    assert len(f) > 2000
+    assert f["pixel"].max() < W * H and np.all((f["depth"] >= 0) & (f["depth"] <= 1))
+    # alpha = hair_alpha * (1 - lod) = 0.375, packed
+    assert np.all(f["color"] >> 24 == round(0.5 * 0.75 * 255))
+    counts = np.bincount(f["pixel"], minlength=W * H)
+    assert counts.max() > 16  # some pixels reach the k-buffer's tail
+    vr, vd = volume_case(W, H, 24, coverage=0.3)
+    bg = np.full((H, W), 0xFFFFFFFF, dtype=np.uint32)
+    heads, nodes, _ = R.ref_build_ppll(f, W, H, vr, vd)
+    want = R.ref_resolve_ppll(heads, nodes, bg)
+    assert np.array_equal(O.composite(f, bg, vr, vd), want)
+    assert (want != bg).sum() > 500
