@@ -233,3 +233,18 @@ def test_composite_in_a_cuda_graph(ctx):
         g.replay()
         torch.cuda.synchronize()
         assert np.array_equal(dc.cpu().numpy().view(np.uint32).reshape(H, W), want)
+
+
+def test_three_radix_passes(ctx):
+    """1920x1080 has 2,073,600 pixels: 21-bit keys, three 7-bit radix passes
+    (every other case here takes one or two)."""
+    W, H = 1920, 1080
+    rng = np.random.default_rng(25)
+    counts = np.zeros(W * H, dtype=np.int64)
+    hit = rng.choice(W * H, 40_000, replace=False)
+    counts[hit] = rng.choice([1, 2, 5, 17, 40], len(hit))
+    counts[[0, W * H - 1, 1 << 20, (1 << 20) - 1]] = [3, 30, 20, 1100]
+    f = fragment_case(W, H, counts, 26, tie_levels=512)
+    bg = background_case(W, H, 27)
+    vr, vd = volume_case(W, H, 28, coverage=0.05)
+    assert np.array_equal(_composite(ctx, f, bg, vr, vd), O.composite(f, bg, vr, vd))
