@@ -13,7 +13,11 @@
 //   * vkhr::cuda::voxelize_vertices likewise for HairStyle::voxelize_vertices
 //     (src/vkhr/scene_graph/hair_style.cc:257-294);
 //   * vkhr::Raymarcher::draw renders the volume.frag raymarch
-//     (share/shaders/volumes/volume.frag:31-103) headlessly into RGBA + depth.
+//     (share/shaders/volumes/volume.frag:31-103) headlessly into RGBA + depth;
+//   * vkhr::LinkedList::resolve replaces vulkan::LinkedList::resolve
+//     (src/vkhr/rasterizer/linked_list.cc:21-41, share/shaders/transparency/
+//     resolve.comp:15-101) over the same per-pixel linked lists, and
+//     LinkedList::composite resolves fragments without building the lists.
 // The templates accept the reference's own vkhr::HairStyle (any type with
 // `vertices`, `tangents`, `indices` vectors of 12-byte vec3 / uint32 and a
 // get_bounding_box() returning an AABB-shaped struct).
@@ -240,6 +244,85 @@ public:
 
 private:
     cuda::Context& ctx_;
+};
+
+// The per-pixel linked list of the colour pass (include/vkhr/rasterizer/
+// linked_list.hh, src/vkhr/rasterizer/linked_list.cc) without Vulkan.  The
+// colour image is width*height RGBA8 words (red in the low byte): the
+// background going in, the resolved frame coming out.
+class LinkedList {
+public:
+    static constexpr std::size_t AverageFragmentsPerPixel = 32; // linked_list.hh:28
+    static constexpr std::size_t NodeSize = 12;                  // ppll.glsl's Node
+    static constexpr std::uint32_t Null = VKHR_PPLL_NULL;
+
+    LinkedList(cuda::Context& ctx, std::uint32_t width, std::uint32_t height)
+        : ctx_(ctx), width_(width), height_(height)
+    {
+    }
+
+    std::uint32_t width() const { return width_; }
+    std::uint32_t height() const { return height_; }
+
+    // resolve.comp over a PPLL: `heads` (width*height, Null = empty) and `nodes`.
+    std::vector<std::uint32_t> resolve(const std::vector<std::uint32_t>& heads,
+                                       const std::vector<vkhr_ppll_node>& nodes,
+                                       const std::vector<std::uint32_t>& color)
+    {
+        check_image(heads.size());
+        check_image(color.size());
+        cuda::Context::Buffer h = ctx_.upload(heads);
+        cuda::Context::Buffer c = ctx_.upload(color);
+        cuda::Context::Buffer n;
+        if (!nodes.empty()) n = ctx_.upload(nodes);
+        ctx_.check(vkhr_resolve_ppll(ctx_.get(), static_cast<const std::uint32_t*>(h.data()),
+                                     static_cast<const vkhr_ppll_node*>(n.data()), (std::uint32_t)nodes.size(),
+                                     (std::int32_t)width_, (std::int32_t)height_,
+                                     static_cast<std::uint32_t*>(c.data()), nullptr));
+        return finish(c);
+    }
+
+    // The same step without lists: strand fragments in the order they were
+    // emitted, and optionally the raymarched volume's fragments (a pixel holds
+    // one where its depth is below 1), resolved as if linked in that order.
+    std::vector<std::uint32_t> composite(const std::vector<vkhr_fragment>& fragments,
+                                         const std::vector<std::uint32_t>& color,
+                                         const Raymarcher::Image* volume = nullptr)
+    {
+        check_image(color.size());
+        cuda::Context::Buffer c = ctx_.upload(color);
+        cuda::Context::Buffer f, vr, vd;
+        if (!fragments.empty()) f = ctx_.upload(fragments);
+        if (volume) {
+            if ((std::uint32_t)volume->width != width_ || (std::uint32_t)volume->height != height_)
+                throw cuda::Error(VKHR_ERR_INVALID_ARG, "LinkedList::composite: volume image size differs");
+            vr = ctx_.upload(volume->rgba);
+            vd = ctx_.upload(volume->depth);
+        }
+        ctx_.check(vkhr_composite(ctx_.get(), static_cast<const vkhr_fragment*>(f.data()),
+                                  (std::uint32_t)fragments.size(), static_cast<const float*>(vr.data()),
+                                  static_cast<const float*>(vd.data()), (std::int32_t)width_, (std::int32_t)height_,
+                                  static_cast<std::uint32_t*>(c.data()), nullptr));
+        return finish(c);
+    }
+
+private:
+    void check_image(std::size_t n) const
+    {
+        if (n != (std::size_t)width_ * height_)
+            throw cuda::Error(VKHR_ERR_INVALID_ARG, "LinkedList: an image array is not width * height long");
+    }
+
+    std::vector<std::uint32_t> finish(const cuda::Context::Buffer& c)
+    {
+        std::vector<std::uint32_t> out((std::size_t)width_ * height_);
+        c.download(out.data(), out.size() * sizeof(std::uint32_t));
+        ctx_.check(vkhr_check_status(ctx_.get(), nullptr)); // waits; reports indices out of range
+        return out;
+    }
+
+    cuda::Context& ctx_;
+    std::uint32_t width_, height_;
 };
 
 } // namespace vkhr

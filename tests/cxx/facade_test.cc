@@ -54,6 +54,18 @@ int main(int argc, char** argv)
     in.read(reinterpret_cast<char*>(s.indices.data()), 4 * nidx);
     vkhr_raymarch_params p;
     in.read(reinterpret_cast<char*>(&p), sizeof(p));
+    // compositing inputs: strand fragments, the background, a PPLL
+    const size_t px = (size_t)p.width * (size_t)p.height;
+    uint32_t nf = 0, nn = 0;
+    in.read(reinterpret_cast<char*>(&nf), 4);
+    std::vector<vkhr_fragment> frags(nf);
+    in.read(reinterpret_cast<char*>(frags.data()), 12 * (size_t)nf);
+    std::vector<uint32_t> background(px), heads(px);
+    in.read(reinterpret_cast<char*>(background.data()), 4 * px);
+    in.read(reinterpret_cast<char*>(&nn), 4);
+    std::vector<vkhr_ppll_node> nodes(nn);
+    in.read(reinterpret_cast<char*>(heads.data()), 4 * px);
+    in.read(reinterpret_cast<char*>(nodes.data()), 12 * (size_t)nn);
     if (!in) return 3;
     try {
         vkhr::cuda::Context ctx(0);
@@ -70,6 +82,16 @@ int main(int argc, char** argv)
         vkhr::Raymarcher::Image img = rm.draw(vs, p);
         write(std::string(argv[2]) + "_rgba.bin", img.rgba);
         write(std::string(argv[2]) + "_depth.bin", img.depth);
+        // the colour pass's resolve: over the reference's lists, and without them
+        vkhr::LinkedList ll(ctx, (uint32_t)p.width, (uint32_t)p.height);
+        write(std::string(argv[2]) + "_ppll.bin", ll.resolve(heads, nodes, background));
+        write(std::string(argv[2]) + "_composite.bin", ll.composite(frags, background, &img));
+        try {
+            ll.composite(frags, std::vector<uint32_t>(px + 1));
+            return 6;
+        } catch (const vkhr::cuda::Error& e) {
+            if (e.status != VKHR_ERR_INVALID_ARG) return 7;
+        }
         // errors surface as exceptions with the ABI status
         try {
             vkhr::cuda::voxelize_vertices(ctx, s, 0, res[1], res[2]);
