@@ -182,3 +182,30 @@ def test_rasterized_strands_match_reference():
     want = R.ref_resolve_ppll(heads, nodes, bg)
     assert np.array_equal(O.composite(f, bg, vr, vd), want)
     assert (want != bg).sum() > 500
+
+
+def test_random_lists_match_reference():
+    """Property: for random images (1..6 x 1..6 pixels), list lengths 0..40,
+    depths mixing ties, specials and uniform values, colours and volume
+    images, the oracle's composite and PPLL resolve equal the reference's."""
+    hyp = pytest.importorskip("hypothesis")
+    st = pytest.importorskip("hypothesis.strategies")
+    R = _ref()
+
+    @hyp.settings(max_examples=150, deadline=None)
+    @hyp.given(w=st.integers(1, 6), h=st.integers(1, 6), seed=st.integers(0, 2**31 - 1),
+               ties=st.sampled_from([None, 4, 64]), special=st.sampled_from([0.0, 0.1, 0.5]),
+               volume=st.booleans(), deep=st.integers(0, 40))
+    def check(w, h, seed, ties, special, volume, deep):
+        rng = np.random.default_rng(seed)
+        counts = rng.integers(0, deep + 1, w * h)
+        f = fragment_case(w, h, counts, seed, tie_levels=ties, special_rate=special)
+        bg = background_case(w, h, seed + 1)
+        vr, vd = volume_case(w, h, seed + 2) if volume else (None, None)
+        heads, nodes, _ = R.ref_build_ppll(f, w, h, vr, vd)
+        want = R.ref_resolve_ppll(heads, nodes, bg)
+        assert np.array_equal(O.composite(f, bg, vr, vd), want)
+        rc, got = O.resolve_ppll(heads, nodes, bg)
+        assert rc == 0 and np.array_equal(got, want)
+
+    check()
