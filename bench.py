@@ -6,7 +6,8 @@ One step = one frame of the path at production size: segment-voxelize a
 roots on a 0.3-radius disk tilted 30 degrees, 12 steps of 0.08) into a
 256^3 grid (uint32 counts, u8 densities, int8 tangents), normalize the
 densities, then raymarch a 1920x1080 view with 512 steps, 64-step density
-shadows and 8-tap ambient occlusion.
+shadows, 8-tap ambient occlusion and the workloads' dual-lobe Kajiya-Kay
+(kd 0.4, specular exponents 80 / 8, tangent shifts +0.1 / -0.1).
 
 `value` is frame throughput in Mpixels/s (1920*1080 / step time) with the
 inputs resident in HBM; the per-stage rates (Msegments/s voxelized, Mpixels/s
@@ -17,8 +18,9 @@ read of the frame (RGBA + depth) are inside the timed region.
 
 --impl reference times the reference's CPU algorithm for the same frame on
 the host cores (the oracle's restatement of HairStyle::voxelize_segments,
-serial as in the reference, plus the FP32 raymarch of volume.frag on a
-sample of rows, all threads).
+serial as in the reference, plus the FP32 raymarch of volume.frag over every
+pixel row of the volume's screen footprint -- the proxy cube's fragments,
+volume.vert:17-25 -- with all threads).
 """
 import argparse
 import json
@@ -37,7 +39,8 @@ import numpy as np  # noqa: E402
 
 WORKLOAD = {
     "workload": "production frame: 136,320 strands x 13 vertices (1,635,840 segments) segment-voxelized into "
-                "256^3, raymarched at 1920x1080, 512 steps, 64-step shadows, 8-tap AO",
+                "256^3, raymarched at 1920x1080, 512 steps, 64-step shadows, 8-tap AO, Kajiya-Kay kd 0.4, "
+                "exponents 80/8, shifts +-0.1",
     "strands": 136_320,
     "vertices_per_strand": 13,
     "resolution": 256,
@@ -46,6 +49,7 @@ WORKLOAD = {
     "raycast_steps": 512,
     "shadow_steps": 64,
     "ao_taps": 8,
+    "shading": "Kajiya-Kay: kd 0.4, specular exponents 80 / 8, tangent shifts +0.1 / -0.1",
     "density": "u8 unorm (normalized)",
     "l2": "flushed before every timed step (512 MiB write)",
 }
@@ -130,26 +134,29 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def cpu_frame(O, st, t, idx, b, rows_sample):
-    """One CPU frame: the serial voxelizer + normalize, then the FP32 raymarch
-    on `rows_sample` evenly spread rows (all threads); returns seconds for a
-    full frame (raymarch time scaled by H / rows)."""
+def frame_params(b, res):
     from vkhr_gb300 import scene
 
+    return scene.make_params(b, res, WORKLOAD["width"], WORKLOAD["height"],
+                             raycast_steps=float(WORKLOAD["raycast_steps"]), shadow_steps=float(WORKLOAD["shadow_steps"]),
+                             **scene.CONFIG_SHADING)
+
+
+def cpu_frame(O, st, t, idx, b):
+    """One CPU frame: the serial voxelizer + normalize, then the FP32 raymarch
+    of every pixel with all threads (a pixel whose ray misses the volume's
+    box, which the proxy cube does not cover, costs only its box test).
+    Returns the seconds of both parts."""
     res = (WORKLOAD["resolution"],) * 3
     t0 = time.perf_counter()
     _, d, tq, _ = O.voxelize("segments", st.vertices, t, idx, b, res)
     dn = O.normalize(d)
     t1 = time.perf_counter()
-    p = scene.make_params(b, res, WORKLOAD["width"], WORKLOAD["height"], raycast_steps=float(WORKLOAD["raycast_steps"]),
-                          shadow_steps=float(WORKLOAD["shadow_steps"]))
-    H = WORKLOAD["height"]
-    rows = np.linspace(0, H - 1, rows_sample).astype(int)
+    p = frame_params(b, res)
     t2 = time.perf_counter()
-    for r in rows:
-        O.raymarch(p, dn, tq, precision="f32", rows=(int(r), int(r) + 1))
+    O.raymarch(p, dn, tq, precision="f32")
     t3 = time.perf_counter()
-    return (t1 - t0), (t3 - t2) * H / len(rows)
+    return (t1 - t0), (t3 - t2)
 
 
 def reference_arm(args):
@@ -164,26 +171,26 @@ def reference_arm(args):
         O.build(with_reference=False)
     st, t, idx = make_style()
     b = O.bounding_box(st.vertices)
-    rows = 36
     for _ in range(args.warmup):
-        cpu_frame(O, st, t, idx, b, rows)
+        cpu_frame(O, st, t, idx, b)
     vox, ray = [], []
     for _ in range(args.steps):
-        a, r = cpu_frame(O, st, t, idx, b, rows)
+        a, r = cpu_frame(O, st, t, idx, b)
         vox.append(a)
         ray.append(r)
     step_s = (sum(vox) + sum(ray)) / args.steps
     px = WORKLOAD["width"] * WORKLOAD["height"]
     value = px / step_s / 1e6
     cores = O.max_threads()
-    sample = ("per step: the full serial voxelization (1,635,840 segments -> 256^3) + normalize, and the FP32 "
-              "raymarch of %d of 1080 evenly spread rows, scaled to the frame" % rows)
+    sample = ("every step is the whole frame: the serial voxelization (1,635,840 segments -> 256^3) + normalize, "
+              "and the FP32 raymarch of all 1920x1080 pixels (all threads)")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": WORKLOAD,
         "components": {"voxelize_msegments_per_s": st.segment_count / (sum(vox) / args.steps) / 1e6,
-                       "raymarch_mpixels_per_s": px / (sum(ray) / args.steps) / 1e6},
+                       "raymarch_mpixels_per_s": px / (sum(ray) / args.steps) / 1e6,
+                       "voxelize_s": sum(vox) / args.steps, "raymarch_s": sum(ray) / args.steps},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -361,8 +368,9 @@ def batched_comparison(args, dev, stream, rank, world, flush):
 SCALE = {
     "workload": "1,048,576 strands x 32 vertices (33,554,432 vertices, 32,505,856 segments; radius-1.2 hemisphere, "
                 "step 0.04) segment-voxelized into 512^3 (u32 counts, u8, i8x4 tangents; 8-byte visit entries), "
-                "normalized, raymarched at 3840x2160 with 1024 steps, 128-step shadows, 8-tap AO; plus 4 views of "
-                "the volume (1920x1080 each) in one batched launch",
+                "normalized, raymarched at 3840x2160 with 1024 steps, 128-step shadows, 16-direction AO, Kajiya-Kay "
+                "kd 0.4, exponents 80/8, shifts +-0.1; plus 4 views of the volume (3840x2160 each) in one batched "
+                "launch",
 }
 
 
@@ -386,11 +394,11 @@ def scale_section(args, dev, stream, flush):
     counts = torch.empty(n, dtype=torch.int32, device=dev)
     dens = torch.empty(n, dtype=torch.uint8, device=dev)
     tq = torch.empty((n, 4), dtype=torch.int8, device=dev)
-    p = scene.make_params(b, res, 3840, 2160, camera_distance=5.0, raycast_steps=1024.0, shadow_steps=128.0)
+    kw = dict(camera_distance=5.0, raycast_steps=1024.0, shadow_steps=128.0, ao_directions=16, **scene.CONFIG_SHADING)
+    p = scene.make_params(b, res, 3840, 2160, **kw)
     rgba = torch.empty((2160, 3840, 4), dtype=torch.float32, device=dev)
     depth = torch.empty((2160, 3840), dtype=torch.float32, device=dev)
-    views = [scene.make_params(b, res, 1920, 1080, camera_distance=5.0, raycast_steps=1024.0, shadow_steps=128.0,
-                               view_direction=vd)
+    views = [scene.make_params(b, res, 3840, 2160, view_direction=vd, **kw)
              for vd in ((0.0, 0.0, 1.0), (1.0, 0.3, 0.0), (0.0, 1.0, 0.2), (-0.7, 0.2, -0.7))]
     rects = [_native.raymarch_footprint(v) for v in views]
     atlas = torch.empty((max(r[3] for r in rects), sum(r[2] for r in rects), 4), dtype=torch.float32, device=dev)
@@ -442,8 +450,9 @@ def scale_section(args, dev, stream, flush):
 DIFF = {
     "workload": "differentiable view: the 136,320 x 13 style (1,772,160 vertices) trilinearly splatted into an FP32 "
                 "256^3 density, FP32 tangents, 960x540 with 512 steps, 64-step shadows, 8-tap AO; L2 loss against a "
-                "target from log-normally perturbed densities (sigma 0.2) with exponent 60; gradients with respect "
-                "to density, tangents, kd, the exponent and (through the splat) the vertices",
+                "target from log-normally perturbed densities (sigma 0.2) with first exponent 60; Kajiya-Kay kd 0.4, "
+                "exponents 80/8, shifts +-0.1; gradients with respect to density, tangents, kd, both exponents and "
+                "(through the splat) the vertices",
 }
 
 
@@ -470,8 +479,9 @@ def diff_section(args, dev, stream, flush):
                           counts.data_ptr(), None, tq.data_ptr(), s)
     tan = torch.zeros((n, 4), dtype=torch.float32, device=dev)
     tan[:, :3] = torch.clamp(tq[:, :3].float() / 127.0, min=-1.0)
-    kw = dict(camera_distance=4.0, raycast_steps=512.0, shadow_steps=64.0, isosurface=1.0, kd=0.4,
-              density_format=_abi.DENSITY_F32, tangent_format=_abi.TANGENT_F32X4)
+    kw = dict(camera_distance=4.0, raycast_steps=512.0, shadow_steps=64.0, isosurface=1.0,
+              density_format=_abi.DENSITY_F32, tangent_format=_abi.TANGENT_F32X4,
+              **{k: v for k, v in scene.CONFIG_SHADING.items() if k != "hair_exponent"})
     p = scene.make_params(b, res, 960, 540, hair_exponent=80.0, **kw)
     pt = scene.make_params(b, res, 960, 540, hair_exponent=60.0, **kw)
     gen = torch.Generator(device=dev).manual_seed(3)
@@ -486,7 +496,7 @@ def diff_section(args, dev, stream, flush):
         g_rgba = torch.empty_like(target)
         gd = torch.empty_like(dens)
         gt = torch.empty_like(tan)
-        gp = torch.empty(2, dtype=torch.float64, device=dev)
+        gp = torch.empty(3, dtype=torch.float64, device=dev)  # kd and the two exponents
         gv = torch.empty_like(V)
 
         def adjoint_pass():
@@ -869,8 +879,7 @@ def gb300_arm(args):
     tq = torch.empty((n, 4), dtype=torch.int8, device=dev)
     rgba = torch.empty((H, W, 4), dtype=torch.float32, device=dev)
     depth = torch.empty((H, W), dtype=torch.float32, device=dev)
-    p = scene.make_params(b, res, W, H, raycast_steps=float(WORKLOAD["raycast_steps"]),
-                          shadow_steps=float(WORKLOAD["shadow_steps"]))
+    p = frame_params(b, res)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
     # two sets of device inputs and outputs (the streamed end-to-end loop below
     # double-buffers them; every other measurement uses set 0)
@@ -941,27 +950,26 @@ def gb300_arm(args):
     top_avg_ms = top_ms / top_n
     S = st.segment_count
     V = st.vertex_count
-    # algorithmic (compulsory) bytes, each byte once
+    # algorithmic (compulsory) bytes, each byte once: the inputs read (index
+    # pairs 8 B per segment, vertices and tangents 12 B each per vertex) and
+    # the outputs written (counts 4 B, u8 1 B, i8x4 tangents 4 B per voxel);
+    # the visit entries, pair records and key scratch are the design's own
+    # traffic (reported as ncu-measured `traffic`), not algorithmic bytes
     visits = int(counts.sum(dtype=torch.int64).item())
     R = WORKLOAD["resolution"]
     occupied = int(counts.view(R // 8, 8, R // 8, 8, R // 8, 8).amax(dim=(1, 3, 5)).gt(0).sum().item())
+    covered = int((rgba != 0).any(dim=2).sum().item())  # image.cc:259-271: pixels not the background
+
     def alg_bytes_of(name):
         """Algorithmic bytes per launch of a kernel of the frame, by kernel family."""
-        if "brick_kernel" in name and "false" in name:
-            # 4-byte visit entries + the pair tangents once + counts, u8 and i8x4 of the occupied bricks
-            return 4 * visits + 16 * S + 9 * 512 * occupied
-        if name.startswith("(bin_kernel<true"):
-            # index pairs + both vertices of each pair once + the 4-byte visit entries written
-            return 8 * S + 24 * V + 4 * visits
-        if name.startswith("(bin_kernel<false") and name.count(",") == 5 and name.endswith("true>)"):
-            # one walk: index pairs + vertices once + the pair records and tangents + the 4-byte visit entries written
-            return 8 * S + 24 * V + 48 * S + 4 * visits
+        if "brick_kernel" in name:
+            return 9 * 512 * occupied              # counts, u8, i8x4 of the occupied bricks
+        if "zero_empty_kernel" in name:
+            return 9 * (n - 512 * occupied)        # the same outputs of the unvisited bricks
         if name.startswith("(bin_kernel<false"):
-            # index pairs + vertices once + the pair records and tangents written
-            return 8 * S + 24 * V + 48 * S
+            return 8 * S + 24 * V                  # index pairs, vertices and tangents read
         if "raymarch_kernel" in name:
-            # u8 densities + i8x4 tangents once + the RGBA and depth outputs
-            return n * 1 + n * 4 + px * 20
+            return n * 1 + n * 4 + px * 20         # u8 densities + i8x4 tangents + RGBA and depth out
         return None
 
     alg_bytes = alg_bytes_of(top_name)
@@ -981,6 +989,26 @@ def gb300_arm(args):
         "raymarch": {"alg_bytes": ray_alg, "ms": rms_, "achieved_gbs": ray_alg / (rms_ / 1e3) / 1e9,
                      "frac": ray_alg / (rms_ / 1e3) / 1e9 / hbm},
     }
+    per_kernel_roofline = {}
+    for name, (cnt, kms) in per_kernel.items():
+        ab = alg_bytes_of(name)
+        if ab:
+            per_kernel_roofline[name] = {"alg_bytes": ab, "avg_ms": kms / cnt,
+                                         "frac": ab / (kms / cnt / 1e3) / 1e9 / hbm}
+
+    # ---- vertex mode: the same style by vertex counts (HairStyle::voxelize_vertices) ----
+    vtimes = []
+    for k in range(max(args.warmup, 3) + args.steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.voxelize_vertices(dv.data_ptr(), dt.data_ptr(), V, b, res, _abi.INDEX_REF_FP32, counts.data_ptr(),
+                              dens.data_ptr(), tq.data_ptr(), s)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if k >= max(args.warmup, 3):
+            vtimes.append(e0.elapsed_time(e1))
+    vertex_ms = statistics.median(vtimes)
 
     # ---- end to end through the C ABI with host buffers ------------------------
     hv = torch.from_numpy(st.vertices).pin_memory()
@@ -1066,16 +1094,21 @@ def gb300_arm(args):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic", "config": dict(WORKLOAD, parallelism="replicas" if world > 1 else "single"),
+        "data": "synthetic", "config": WORKLOAD,
         "components": {
             "voxelize_ms": sum(vox_ms) / args.steps, "raymarch_ms": sum(ray_ms) / args.steps,
             "voxelize_msegments_per_s": S / (sum(vox_ms) / args.steps / 1e3) / 1e6,
             "raymarch_mpixels_per_s": px / (sum(ray_ms) / args.steps / 1e3) / 1e6,
+            "covered_pixels": covered,
+            "raymarch_covered_mpixels_per_s": covered / (sum(ray_ms) / args.steps / 1e3) / 1e6,
+            "voxelize_vertices_ms": vertex_ms,
+            "voxelize_vertices_mvertices_per_s": V / (vertex_ms / 1e3) / 1e6,
             "wall_ms_per_step_incl_flush": wall * 1e3 / args.steps,
         },
         "kernels": {k: {"launches": v[0], "avg_ms": v[1] / v[0]} for k, v in sorted(per_kernel.items())},
         "roofline": roofline,
         "roofline_stages": stages,
+        "roofline_kernels": per_kernel_roofline,
         "e2e": {"value": world * px / (e2e_ms / 1e3) / 1e6, "unit": UNIT, "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "copies": "streamed: step k+1's upload and step k-1's read-back overlap step k's compute "
@@ -1086,8 +1119,16 @@ def gb300_arm(args):
         "gpu_launches": launches,
         "clocks": clocks.summary(),
         "autotune": {"raymarch_variant": tuned, "variant_ms": tuned_ms,
-                     "variants": ["8x4 tiles", "16x2 tiles", "4x8 tiles", "8x4 tiles, 64 registers"]},
+                     "variants": ["8x4 tiles", "16x2 tiles", "4x8 tiles", "8x4 tiles, 64 registers",
+                                  "8x4 tiles, density bricks staged in shared memory by TMA",
+                                  "8x4 tiles, density through the texture unit (not tuned: 8-bit filter weights)"]},
     }
+    if batched is not None:
+        line["batched_speedup_vs_plain"] = round(batched["speedup_vs_plain"]["batched_graph"], 3)
+    if diff is not None:
+        line["adjoint_over_forward"] = round(diff["adjoint_over_forward_K16"], 3)
+    if scale is not None:
+        line["scale_frame_ms"] = round(scale["ms"]["voxelize"] + scale["ms"]["normalize"] + scale["ms"]["raymarch"], 3)
     if batched is not None:
         line["batched"] = batched
     if frame_graph is not None:
@@ -1103,12 +1144,11 @@ def gb300_arm(args):
 
         if not os.path.exists(O.LIB):
             O.build(with_reference=False)
-        rows = 36
-        a, r = cpu_frame(O, st, t, idx, b, rows)
+        a, r = cpu_frame(O, st, t, idx, b)
         line["cpu_baseline"] = {
             "value": px / (a + r) / 1e6, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
-            "sample": "one frame: the full serial voxelization + normalize (%.2f s) and the FP32 raymarch of %d of "
-                      "1080 rows scaled to the frame (%.2f s)" % (a, rows, r)}
+            "sample": "one whole frame: the serial voxelization + normalize (%.2f s) and the FP32 raymarch of all "
+                      "1920x1080 pixels, all threads (%.2f s)" % (a, r)}
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

@@ -162,19 +162,28 @@ Volume voxelize(Context& ctx, const Style& style, bool segments, int w, int h, i
     Context::Buffer v = ctx.upload(style.vertices);
     Context::Buffer t = ctx.upload(style.tangents);
     Context::Buffer counts(ctx, n * 4), dens(ctx, n), tq(ctx, n * 4);
-    if (segments) {
-        Context::Buffer idx = ctx.upload(style.indices);
-        ctx.check(vkhr_voxelize_segments(ctx.get(), static_cast<const float*>(v.data()),
-                                         static_cast<const float*>(t.data()), static_cast<const uint32_t*>(idx.data()),
-                                         style.indices.size(), &vol.bounds, w, h, d, index_mode,
-                                         static_cast<uint32_t*>(counts.data()), static_cast<uint8_t*>(dens.data()),
-                                         static_cast<int8_t*>(tq.data()), nullptr));
-        ctx.sync();
-    } else {
-        ctx.check(vkhr_voxelize_vertices(ctx.get(), static_cast<const float*>(v.data()),
-                                         static_cast<const float*>(t.data()), (uint32_t)style.vertices.size(),
-                                         &vol.bounds, w, h, d, index_mode, static_cast<uint32_t*>(counts.data()),
-                                         static_cast<uint8_t*>(dens.data()), static_cast<int8_t*>(tq.data()), nullptr));
+    Context::Buffer idx;
+    if (segments) idx = ctx.upload(style.indices);
+    for (int attempt = 0;; ++attempt) {
+        if (segments)
+            ctx.check(vkhr_voxelize_segments(
+                ctx.get(), static_cast<const float*>(v.data()), static_cast<const float*>(t.data()),
+                static_cast<const uint32_t*>(idx.data()), style.indices.size(), &vol.bounds, w, h, d, index_mode,
+                static_cast<uint32_t*>(counts.data()), static_cast<uint8_t*>(dens.data()),
+                static_cast<int8_t*>(tq.data()), nullptr));
+        else
+            ctx.check(vkhr_voxelize_vertices(ctx.get(), static_cast<const float*>(v.data()),
+                                             static_cast<const float*>(t.data()), (uint32_t)style.vertices.size(),
+                                             &vol.bounds, w, h, d, index_mode, static_cast<uint32_t*>(counts.data()),
+                                             static_cast<uint8_t*>(dens.data()), static_cast<int8_t*>(tq.data()),
+                                             nullptr));
+        // waits, and reports what the kernels recorded: a visit list sized
+        // from an earlier call at this size that proved too small makes the
+        // context count again, which the one retry does
+        const vkhr_status s = vkhr_check_status(ctx.get(), nullptr);
+        if (s == VKHR_ERR_CAPACITY && attempt == 0) continue;
+        ctx.check(s);
+        break;
     }
     vol.densities.resize(n);
     vol.tangents.resize(4 * n);
@@ -186,6 +195,30 @@ Volume voxelize(Context& ctx, const Style& style, bool segments, int w, int h, i
     return vol;
 }
 } // namespace detail
+
+// The reference's own HairStyle::Volume (include/vkhr/scene_graph/hair_style.hh:89-101:
+// glm::vec3 resolution, AABB bounds, std::vector<unsigned char> densities,
+// std::vector<glm::i8vec4> tangents) from a Volume, so that the loader's call
+// site (src/vkhr/rasterizer/hair_style.cc:75) changes in one line:
+//   auto strand_volume = vkhr::cuda::to_reference<vkhr::HairStyle::Volume>(
+//       vkhr::cuda::voxelize_segments(ctx, hair_style, 256, 256, 256));
+template <class RefVolume>
+RefVolume to_reference(const Volume& v)
+{
+    RefVolume r;
+    r.resolution = decltype(r.resolution)((float)v.resolution[0], (float)v.resolution[1], (float)v.resolution[2]);
+    r.bounds.origin = decltype(r.bounds.origin)(v.bounds.origin[0], v.bounds.origin[1], v.bounds.origin[2]);
+    r.bounds.radius = v.bounds.radius;
+    r.bounds.size = decltype(r.bounds.size)(v.bounds.size[0], v.bounds.size[1], v.bounds.size[2]);
+    r.bounds.volume = v.bounds.volume;
+    r.densities.assign(v.densities.begin(), v.densities.end());
+    typedef typename decltype(r.tangents)::value_type Tangent;
+    const size_t n = v.tangents.size() / 4;
+    r.tangents.reserve(n);
+    for (size_t i = 0; i < n; ++i)
+        r.tangents.push_back(Tangent(v.tangents[4 * i], v.tangents[4 * i + 1], v.tangents[4 * i + 2], v.tangents[4 * i + 3]));
+    return r;
+}
 
 // HairStyle::voxelize_vertices (hair_style.cc:257-294) on the GPU.
 template <class Style>

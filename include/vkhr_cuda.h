@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define VKHR_CUDA_ABI_VERSION 1
+#define VKHR_CUDA_ABI_VERSION 2
 
 typedef enum vkhr_status {
     VKHR_OK = 0,
@@ -140,7 +140,36 @@ typedef struct vkhr_raymarch_params {
     float kd;                           /* ext: diffuse scale, 1 = reference         */
     int32_t density_format;             /* vkhr_density_format                       */
     int32_t tangent_format;             /* vkhr_tangent_format                       */
+
+    float spec_exponent2;               /* ext: second lobe's exponent; <= 0 = none  */
+    float spec_shift[2];                /* ext: tangent shift of lobe 1 / lobe 2     */
+    int32_t ao_directions;              /* ext: 0 = the ao_kernel_size^3 cube, else
+                                           that many directions (1..32)             */
 } vkhr_raymarch_params;
+
+/* The extension knobs, exactly (all zero: the reference's shading):
+ *
+ * Dual-lobe Kajiya-Kay.  With T the normalised surface tangent, L and E as in
+ * kajiya-kay.glsl:7-24 (E points from the camera to the surface), V = -E and
+ * N = normalize(V - (T.V) T) (the unit direction towards the camera
+ * perpendicular to the strand; N = 0 when T is parallel to E), lobe j uses
+ * the shifted tangent T_j = normalize(T + spec_shift[j] * N):
+ *   spec_j  = max(cos(T_j,L) cos(T_j,E) + sin(T_j,L) sin(T_j,E), 0)^p_j,
+ *   shading = kd * sin(T,L) * hair_color + spec_1 * light_intensity
+ *             + spec_2 * light_intensity * hair_color        (second lobe),
+ * p_1 = hair_exponent, p_2 = spec_exponent2; the second lobe exists when
+ * spec_exponent2 > 0.  A positive shift turns the strand towards the viewer
+ * by atan(shift).
+ *
+ * Directional ambient occlusion.  ao_directions = n > 0 replaces the
+ * ao_kernel_size^3 cube of local_ambient_occlusion.glsl:9-30 by n taps at
+ *   s + d_i * (occlusion_radius * sqrt(3)) * voxel_size   (per axis),
+ * d_i the Fibonacci-sphere directions (y the polar axis):
+ *   y_i = 1 - (2i + 1) / n,  r_i = sqrt(1 - y_i^2),  phi_i = i * pi * (3 - sqrt(5)),
+ *   d_i = (r_i cos phi_i, y_i, r_i sin phi_i),
+ * and occlusion = (1 - sum_i min(density_i, ao_max) / n)^ao_exponent.  The
+ * radius factor sqrt(3) puts the taps at the distance of the reference's
+ * 8-tap cube (kernel 2), whose taps are the 8 directions (+-1, +-1, +-1)/sqrt(3). */
 
 /* Opaque library context: one per host thread (or externally synchronised).
  * It pins a device and owns grow-only scratch buffers. */
@@ -209,8 +238,22 @@ vkhr_status vkhr_generate_indices(vkhr_ctx* ctx, const uint16_t* h_segments, uin
  *                including the reference's serial summation order and its
  *                stop-at-255 rule (optional, may be NULL; needs d_tangent_in).
  * d_vertices / d_tangent_in are float3 arrays (12-byte stride, glm::vec3).
- * bounds is host memory.  Scratch comes from the context; the first call at
- * a new size may allocate and reads one 8-byte count back to the host. */
+ * bounds is host memory.  Scratch comes from the context and grows on
+ * demand (a growth allocates, which synchronises the device).
+ *
+ * Host waits.  Vertex mode never waits on the host.  Segment mode sizes its
+ * visit list from the number of voxel visits:
+ *   - with a visit budget (vkhr_set_visit_budget) from the budget: no wait;
+ *   - without one, a one-style call at a size (index count, grid, index mode,
+ *     tangents or not) that this context has voxelized before sizes it from
+ *     twice that earlier call's visits: no wait.  A call whose visits exceed
+ *     that records VKHR_ERR_CAPACITY, which vkhr_check_status reports (its
+ *     outputs are then incomplete); the context then forgets the sizes it
+ *     learned, and the next call at each size counts again;
+ *   - otherwise (the first call at a size, and every batch of two or more
+ *     styles) the call reads its visit total back: one 8-byte copy and a
+ *     wait for `stream`.
+ * A call under stream capture must not need the read-back. */
 
 /* Replaces HairStyle::voxelize_vertices (hair_style.cc:257-294). */
 vkhr_status vkhr_voxelize_vertices(vkhr_ctx* ctx, const float* d_vertices, const float* d_tangent_in,
@@ -261,9 +304,9 @@ vkhr_status vkhr_voxelize_batched(vkhr_ctx* ctx, int32_t segments, const vkhr_vo
 vkhr_status vkhr_set_visit_budget(vkhr_ctx* ctx, uint64_t max_visits);
 
 /* Waits for the stream and reports errors that kernels recorded on the device
- * since the last voxelization started or the last check that reported one
- * (e.g. a capacity overflow, a fragment outside the image); reporting clears
- * them. */
+ * since the last report (e.g. a capacity overflow, a fragment outside the
+ * image); reporting clears them.  A segment voxelization that reads its
+ * visit total back reports them the same way. */
 vkhr_status vkhr_check_status(vkhr_ctx* ctx, void* stream);
 
 /* Replaces HairStyle::Volume::normalize (hair_style.cc:344-357): u8 min-max
@@ -306,16 +349,26 @@ vkhr_status vkhr_raymarch(vkhr_ctx* ctx, const vkhr_raymarch_params* params,
                           float* d_rgba, float* d_depth_out, void* stream);
 
 /* Ray-packet variants of vkhr_raymarch: 0 = 8x4-pixel warp tiles (default),
- * 1 = 16x2, 2 = 4x8, 3 = 8x4 with 8 resident CTAs per SM (fewer registers).
- * Every variant computes the same pixels. */
-#define VKHR_RAYMARCH_VARIANTS 4
+ * 1 = 16x2, 2 = 4x8, 3 = 8x4 with 8 resident CTAs per SM (fewer registers),
+ * 4 = 8x4 tiles whose primary march reads density texels from shared memory,
+ * each occupied 8^3 brick a warp's rays need staged by one TMA tensor copy
+ * (used where TMA can address the grid: a 16-byte aligned base and a row
+ * pitch of whole 16 bytes; variant 0 elsewhere).  Variants 0-4 compute the
+ * same pixels, bit for bit.  5 = 8x4 tiles sampling the density through the
+ * texture unit: the call copies it into a 3D array of the context (LINEAR
+ * filtering, border 0) and the hardware filters it with 8-bit weights, so its
+ * pixels differ from the others by that filter's precision; u8 and FP32
+ * densities only (variant 0 for counts).  The autotuner does not try it. */
+#define VKHR_RAYMARCH_VARIANTS 6
 
 /* Autotuner (no reference counterpart): times each variant of vkhr_raymarch
- * on these inputs (one warm-up and three timed runs each, d_rgba receiving
- * the image) and keeps the fastest in the context for params' texel
- * formats; later vkhr_raymarch calls with those formats use it.  Writes the
- * choice to *chosen and, when variant_ms is not NULL, the median time of
- * each variant (VKHR_RAYMARCH_VARIANTS floats).  Synchronises the stream. */
+ * that computes the reference's pixels (0-4) on these inputs (one warm-up
+ * and three timed runs each, d_rgba receiving the image) and keeps the
+ * fastest in the context for params' texel formats; later vkhr_raymarch
+ * calls with those formats use it.  Writes the choice to *chosen and, when
+ * variant_ms is not NULL, the median time of each variant
+ * (VKHR_RAYMARCH_VARIANTS floats; 0 for variant 5, not timed).  Synchronises
+ * the stream. */
 vkhr_status vkhr_autotune_raymarch(vkhr_ctx* ctx, const vkhr_raymarch_params* params, const void* d_density,
                                    const void* d_tangent, float* d_rgba, int32_t* chosen, float* variant_ms,
                                    void* stream);
@@ -361,7 +414,7 @@ vkhr_status vkhr_raymarch_footprint(const vkhr_raymarch_params* params, int32_t 
 /* ---- differentiable path ----------------------------------------------------
  * No reference counterpart: gradients of an image loss with respect to an FP32
  * density volume (VKHR_DENSITY_F32), an FP32 tangent field (VKHR_TANGENT_F32X4,
- * w ignored), kd and hair_exponent, and -- through the trilinear splat below --
+ * w ignored), kd and the specular exponents, and -- through the trilinear splat below --
  * the strand vertex positions.  The forward is the raymarch of vkhr_raymarch
  * (same results, bit for bit); the isosurface point, the early exit and the
  * zero tests are constants of the derivative, the clamps of the output pass
@@ -379,7 +432,8 @@ vkhr_status vkhr_raymarch_train(vkhr_ctx* ctx, const vkhr_raymarch_params* param
                                 size_t tape_bytes, int32_t checkpoint_interval, void* stream);
 
 /* Adds dL/d(density), dL/d(tangent) (float4 per voxel, w left alone) and
- * [dL/d kd, dL/d hair_exponent] (two doubles) to the caller's buffers, given
+ * [dL/d kd, dL/d hair_exponent, dL/d spec_exponent2] (three doubles; the last
+ * stays 0 without a second lobe) to the caller's buffers, given
  * dL/d(rgba) (float4 per pixel) and the tape of the training forward on the
  * same inputs.  The primary march is replayed from the tape's checkpoints,
  * one thread per ray segment of checkpoint_interval iterations. */
@@ -409,8 +463,12 @@ vkhr_status vkhr_splat_vertices_adjoint(vkhr_ctx* ctx, const float* d_vertices, 
  * every device loading the library holds until the process exits.
  *   - Limit: ((w+8)/8) * ((h+8)/8) * ((d+8)/8) <= 1,048,576 occupancy bricks
  *     (volumes up to about 800^3); larger grids return VKHR_ERR_CAPACITY.
+ *   - It runs on the current device (cudaSetDevice): the pointers and the
+ *     stream must belong to that device.
  *   - The first call on a device looks up the array's device address (and
- *     the SM count); make that first call before any stream capture.
+ *     the SM count); make that first call before any stream capture.  A
+ *     lookup that fails returns VKHR_ERR_CUDA and is tried again by the
+ *     next call.
  *   - All calls share the one array and it keeps the previous call's bits
  *     (each call clears the part it uses): calls that can overlap on the GPU
  *     (different streams, or different host threads) race; order them.
@@ -435,6 +493,10 @@ vkhr_status vkhr_raymarch_static(const vkhr_raymarch_params* params, const void*
  *     size) and synchronises `stream`; launch never allocates or syncs.
  *   - The graph reads the context's staged job table at every replay: while
  *     it is in use the context runs no other voxelization.
+ *   - The graph holds the addresses of the context's scratch buffers: until
+ *     it is destroyed, a call on the context that would have to grow a
+ *     scratch buffer fails with VKHR_ERR_CAPACITY instead of moving it.
+ *     Destroy the graph before its context.
  *   - No reference counterpart as an API (the reference re-records command
  *     buffers per frame). */
 typedef struct vkhr_frame_graph vkhr_frame_graph;

@@ -9,9 +9,13 @@
  * constants and differentiates the rest:
  *   coverage = lod * acc / iso * alpha (acc = sum of all primary samples),
  *   rgb = clamp(KK(T(surf)) * (1 - alpha)^(thickness * sum shadow samples)
- *              * (1 - sum min(rho, ao_max) / k^3)^ao_exp),
+ *              * (1 - sum min(rho, ao_max) / taps)^ao_exp),
  *   T = normalize(trilinear tangent), samples trilinear in their 8 texels;
- * the clamps pass gradient strictly inside (0, 1).
+ * the clamps pass gradient strictly inside (0, 1).  KK is the dual-lobe,
+ * shifted form of the vkhr_raymarch_params extension (one unshifted lobe
+ * with its knobs at zero); its gradient goes through the scalar form of the
+ * shift (lobe_grad below), while the forward evaluates the vector definition
+ * (raymarch_body.h), so the finite-difference tests check one against the other.
  */
 #include "vkhr_oracle.h"
 
@@ -29,8 +33,44 @@
 typedef struct grads {
     double* density; /* per voxel */
     double* tangent; /* 4 per voxel */
-    double params[2];
+    double params[3];
 } grads;
+
+/* One specular lobe as a function of a = T.L and b = T.E, with c = L.E
+ * fixed.  Shifting T by s towards the camera (normalize(T + s N), N the unit
+ * component of -E perpendicular to T) gives
+ *   a_s = k (a + s (a b - c) / sb),  b_s = k (b - s sb),
+ *   sb = sqrt(1 - b^2) = sin(T, E),  k = 1 / sqrt(1 + s^2),
+ * and the lobe is max(a_s b_s + sqrt(1 - a_s^2) sqrt(1 - b_s^2), 0)^p.
+ * Returns the lobe; *da, *db and *dp receive its partials. */
+static double lobe_grad(double a, double b, double c, double s, double p, double* da, double* db, double* dp)
+{
+    double as = a, bs = b, j00 = 1, j01 = 0, j11 = 1; /* d(a_s, b_s) / d(a, b); d b_s / d a = 0 */
+    const double sb = sqrt(1 - b * b > 0 ? 1 - b * b : 0);
+    if (s != 0 && sb > 0) {
+        const double k = 1 / sqrt(1 + s * s);
+        as = k * (a + s * (a * b - c) / sb);
+        bs = k * (b - s * sb);
+        j00 = k * (1 + s * b / sb);
+        j01 = k * s * (a / sb + (a * b - c) * b / (sb * sb * sb));
+        j11 = k * (1 + s * b / sb);
+    }
+    const double sa2 = sqrt(1 - as * as > 0 ? 1 - as * as : 0), sb2 = sqrt(1 - bs * bs > 0 ? 1 - bs * bs : 0);
+    double base = as * bs + sa2 * sb2;
+    base = base > 0 ? base : 0;
+    const double spec = pow(base, p);
+    *da = *db = *dp = 0;
+    if (base > 0) {
+        const double ds = p * pow(base, p - 1);
+        double gas = bs, gbs = as; /* d base / d a_s, d base / d b_s */
+        if (sa2 > 0) gas -= sb2 * as / sa2;
+        if (sb2 > 0) gbs -= sa2 * bs / sb2;
+        *da = ds * gas * j00;
+        *db = ds * (gas * j01 + gbs * j11);
+        *dp = spec * log(base);
+    }
+    return spec;
+}
 
 static void scatter_density(const vol_ad* v, vec3_ad P, double g, double* grad)
 {
@@ -65,6 +105,15 @@ static void scatter_tangent(const vol_ad* v, vec3_ad P, vec3_ad g, double* grad)
 
 static double clamp01_d(double x) { return x > 0 ? (x < 1 ? x : 1) : 0; }
 static double clamp_grad(double x, double g) { return (x > 0 && x < 1) ? g : 0; }
+
+/* Position of directional AO tap i (the extension of local_ambient_occlusion.glsl). */
+static vec3_ad ao_tap(const vkhr_raymarch_params* p, vec3_ad s, vec3_ad voxel_space, int i)
+{
+    double d[3];
+    ao_direction_ad(i, p->ao_directions, d);
+    const double reach = (double)p->occlusion_radius * sqrt(3.0);
+    return add_ad(s, mul_ad(v3_ad(d[0] * reach, d[1] * reach, d[2] * reach), voxel_space));
+}
 
 /* One pixel: returns its loss sum_c (rgba_c - target_c)^2 and, with gr,
  * adds its gradient. */
@@ -105,8 +154,9 @@ static double diff_pixel(const vkhr_raymarch_params* p, const vol_ad* dv, const 
     const int kk = p->shading_model == VKHR_SHADING_KAJIYA_KAY;
     vec3_ad shading = v3_ad(1, 1, 1), L = v3_ad(0, 0, 0), E = v3_ad(0, 0, 0), T = v3_ad(0, 0, 0);
     vec3_ad Tr = v3_ad(0, 0, 0);
-    double cosTL = 0, cosTE = 0, sinTL = 0, sinTE = 0, base = 0, spec = 0, tlen = 0;
+    double cosTL = 0, cosTE = 0, sinTL = 0, tlen = 0;
     const vec3_ad color = from_ad(p->hair_color), inten = from_ad(p->light_intensity);
+    const double p2 = p->spec_exponent2 > 0 ? (double)p->spec_exponent2 : 0;
     if (kk) {
         L = normalize_ad(sub_ad(light, surf), NULL);
         E = normalize_ad(sub_ad(surf, cam), NULL);
@@ -115,11 +165,8 @@ static double diff_pixel(const vkhr_raymarch_params* p, const vol_ad* dv, const 
         cosTL = dot_ad(T, L);
         cosTE = dot_ad(T, E);
         sinTL = sqrt(1 - cosTL * cosTL > 0 ? 1 - cosTL * cosTL : 0);
-        sinTE = sqrt(1 - cosTE * cosTE > 0 ? 1 - cosTE * cosTE : 0);
-        base = cosTL * cosTE + sinTL * sinTE;
-        base = base > 0 ? base : 0;
-        spec = pow(base, (double)p->hair_exponent);
-        shading = add_ad(scale_ad(color, (double)p->kd * sinTL), scale_ad(inten, spec));
+        shading = kajiya_kay_ad(color, inten, (double)p->hair_exponent, T, L, E, (double)p->kd, p2,
+                                (double)p->spec_shift[0], (double)p->spec_shift[1]);
     }
     const int shadows = p->deep_shadows_on == 1 && p->shading_model != VKHR_SHADING_LAO;
     const int lao = p->shading_model != VKHR_SHADING_ADSM;
@@ -132,13 +179,21 @@ static double diff_pixel(const vkhr_raymarch_params* p, const vol_ad* dv, const 
         occl_s = pow(1 - alpha, strands);
     }
     const float kr = (p->ao_kernel_size - 1.0f) / 2.0f;
-    const double k3 = (double)p->ao_kernel_size * (double)p->ao_kernel_size * (double)p->ao_kernel_size;
+    const int ndir = p->ao_directions;
+    const double k3 = ndir > 0 ? (double)ndir
+                               : (double)p->ao_kernel_size * (double)p->ao_kernel_size * (double)p->ao_kernel_size;
     const vec3_ad vs = v3_ad((double)p->volume_bounds.size[0] / p->volume_resolution[0],
                              (double)p->volume_bounds.size[1] / p->volume_resolution[1],
                              (double)p->volume_bounds.size[2] / p->volume_resolution[2]);
     const vec3_ad sc = scale_ad(vs, (double)p->occlusion_radius / (double)kr);
     double dsum = 0, occl_a = 1;
-    if (lao) {
+    if (lao && ndir > 0) { /* the directional taps */
+        for (int i = 0; i < ndir; ++i) {
+            const double r = sample_density_ad(dv, ao_tap(p, surf, vs, i));
+            dsum += r < p->ao_max ? r : (double)p->ao_max;
+        }
+        occl_a = pow(1 - dsum / k3, (double)p->ao_exponent);
+    } else if (lao) {
         for (float z = -kr; z <= kr; z += 1.0f)
             for (float y = -kr; y <= kr; y += 1.0f)
                 for (float x = -kr; x <= kr; x += 1.0f) {
@@ -165,17 +220,20 @@ static double diff_pixel(const vkhr_raymarch_params* p, const vol_ad* dv, const 
     const double gocc = gx[0] * shading.x + gx[1] * shading.y + gx[2] * shading.z;
     if (kk) {
         const double gi = dot_ad(gsh, inten), gc = dot_ad(gsh, color);
+        const double gic = gsh.x * inten.x * color.x + gsh.y * inten.y * color.y + gsh.z * inten.z * color.z;
+        const double cosLE = dot_ad(L, E);
         gr->params[0] += gc * sinTL;
-        double dspec = 0;
-        if (base > 0) {
-            gr->params[1] += gi * spec * log(base);
-            dspec = (double)p->hair_exponent * pow(base, (double)p->hair_exponent - 1);
+        double da, db, dp;
+        lobe_grad(cosTL, cosTE, cosLE, (double)p->spec_shift[0], (double)p->hair_exponent, &da, &db, &dp);
+        double gcosTL = gi * da, gcosTE = gi * db;
+        gr->params[1] += gi * dp;
+        if (p2 > 0) {
+            lobe_grad(cosTL, cosTE, cosLE, (double)p->spec_shift[1], p2, &da, &db, &dp);
+            gcosTL += gic * da;
+            gcosTE += gic * db;
+            gr->params[2] += gic * dp;
         }
-        const double gbase = gi * dspec;
-        const double gsinTL = gc * (double)p->kd + gbase * sinTE, gsinTE = gbase * sinTL;
-        double gcosTL = gbase * cosTE, gcosTE = gbase * cosTL;
-        if (sinTL > 0) gcosTL -= gsinTL * cosTL / sinTL;
-        if (sinTE > 0) gcosTE -= gsinTE * cosTE / sinTE;
+        if (sinTL > 0) gcosTL -= gc * (double)p->kd * cosTL / sinTL; /* the diffuse kd sin(T, L) */
         const vec3_ad gT = add_ad(scale_ad(L, gcosTL), scale_ad(E, gcosTE));
         if (tlen > 0) {
             const vec3_ad gTr = scale_ad(sub_ad(gT, scale_ad(T, dot_ad(gT, T))), 1 / tlen);
@@ -189,7 +247,11 @@ static double diff_pixel(const vkhr_raymarch_params* p, const vol_ad* dv, const 
     if (lao && gocc != 0) {
         const double gd = -gocc * occl_s * (double)p->ao_exponent *
                           pow(1 - dsum / k3, (double)p->ao_exponent - 1) / k3;
-        for (float z = -kr; z <= kr; z += 1.0f)
+        for (int i = 0; i < ndir; ++i) {
+            const vec3_ad q = ao_tap(p, surf, vs, i);
+            if (sample_density_ad(dv, q) < p->ao_max) scatter_density(dv, q, gd, gr->density);
+        }
+        for (float z = -kr; ndir <= 0 && z <= kr; z += 1.0f) /* the cube's taps */
             for (float y = -kr; y <= kr; y += 1.0f)
                 for (float x = -kr; x <= kr; x += 1.0f) {
                     const vec3_ad q = add_ad(surf, mul_ad(v3_ad(x, y, z), sc));
@@ -215,7 +277,7 @@ double oracle_diff_loss(const vkhr_raymarch_params* p, const double* density, co
     double inv[16];
     if (!oracle_vp_inverse(p, inv)) return NAN;
     const int want = g_density || g_tangent || g_params;
-    grads gr = {g_density, g_tangent, {0, 0}};
+    grads gr = {g_density, g_tangent, {0, 0, 0}};
     if (threads <= 0) threads = oracle_max_threads();
     if (want) threads = 1; /* the gradient scatter is serial */
     double loss = 0;
@@ -235,6 +297,7 @@ double oracle_diff_loss(const vkhr_raymarch_params* p, const double* density, co
     if (g_params) {
         g_params[0] += gr.params[0];
         g_params[1] += gr.params[1];
+        g_params[2] += gr.params[2];
     }
     return loss;
 }

@@ -16,7 +16,7 @@ from vkhr_gb300 import _abi
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libvkhr_ref.so")
-REFERENCE_ROOT = "/root/reference"
+REFERENCE_ROOT = os.environ.get("VKHR_REFERENCE_ROOT", "/root/reference")
 
 _lib = None
 _ref = None
@@ -32,7 +32,8 @@ def build(with_reference=None):
 
 
 DIAG_DTYPE = np.dtype([("iso_margin", np.float64), ("support_margin", np.float64), ("tangent_len", np.float64),
-                       ("steps_taken", np.int32), ("covered", np.int32)])
+                       ("iso_shift", np.float64), ("fp32_res", np.float64), ("steps_taken", np.int32),
+                       ("covered", np.int32)])
 
 P = C.c_void_p
 
@@ -241,7 +242,7 @@ def raymarch(params, density, tangent, depth_in=None, precision="f64", rows=None
 def diff_loss(params, density, tangent, target, grads=False, threads=0, mask=None):
     """Loss sum((rgba - target)^2) of the FP64 differentiable raymarch over
     the pixels where mask (H, W) is true (None: all); with grads=True also
-    (g_density, g_tangent (n, 4), g_params [kd, exponent]).  density (n,)
+    (g_density, g_tangent (n, 4), g_params [kd, exponent, exponent2]).  density (n,)
     and tangent (n, 4) are converted to float64."""
     d = np.ascontiguousarray(density, dtype=np.float64).reshape(-1)
     t = np.ascontiguousarray(tangent, dtype=np.float64).reshape(-1, 4)
@@ -251,7 +252,7 @@ def diff_loss(params, density, tangent, target, grads=False, threads=0, mask=Non
         return float(lib().oracle_diff_loss(C.byref(params), _p(d), _p(t), _p(tg), _p(m), None, None, None, threads))
     gd = np.zeros_like(d)
     gt = np.zeros_like(t)
-    gp = np.zeros(2, dtype=np.float64)
+    gp = np.zeros(3, dtype=np.float64)
     loss = lib().oracle_diff_loss(C.byref(params), _p(d), _p(t), _p(tg), _p(m), _p(gd), _p(gt), _p(gp), threads)
     return float(loss), gd, gt, gp
 

@@ -149,6 +149,28 @@ static REAL SFX(sample_density)(const SFX(vol)* v, SFX(vec3) P)
     return acc;
 }
 
+/* |grad rho|_1 of the trilinear density at P in texel units: how much the
+ * sample can change per texel of movement.  Test-side only. */
+static double SFX(density_slope)(const SFX(vol)* v, SFX(vec3) P)
+{
+    long i0[3];
+    REAL a[3];
+    if (!SFX(tex_setup)(v, P, i0, a)) return 0.0;
+    double g[3] = {0, 0, 0};
+    for (int dz = 0; dz < 2; ++dz)
+        for (int dy = 0; dy < 2; ++dy)
+            for (int dx = 0; dx < 2; ++dx) {
+                const double t = (double)SFX(texel_density)(v, i0[0] + dx, i0[1] + dy, i0[2] + dz);
+                const double wx = dx ? (double)a[0] : 1.0 - (double)a[0];
+                const double wy = dy ? (double)a[1] : 1.0 - (double)a[1];
+                const double wz = dz ? (double)a[2] : 1.0 - (double)a[2];
+                g[0] += (dx ? 1.0 : -1.0) * wy * wz * t;
+                g[1] += wx * (dy ? 1.0 : -1.0) * wz * t;
+                g[2] += wx * wy * (dz ? 1.0 : -1.0) * t;
+            }
+    return fabs(g[0]) + fabs(g[1]) + fabs(g[2]);
+}
+
 static SFX(vec3) SFX(sample_tangent)(const SFX(vol)* v, SFX(vec3) P)
 {
     long i0[3];
@@ -175,9 +197,10 @@ static inline REAL SFX(clip_depth)(const REAL pv[16], SFX(vec3) P)
 /* volume_rendering.glsl:19-52 (volume_surface). */
 static void SFX(volume_surface)(const SFX(vol)* dv, const REAL pv[16], SFX(vec3) start, SFX(vec3) end,
                                 float steps, REAL iso, float depth_buffer, SFX(vec3)* surf_out,
-                                REAL* a_out, double* margin, int* taken, double* support_margin)
+                                REAL* a_out, double* margin, int* taken, double* support_margin,
+                                double* iso_shift)
 {
-    double sm = 1.0 / 0.0;
+    double sm = 1.0 / 0.0, shift = 1.0 / 0.0, slope = 0.0;
     REAL acc = 0;
     float step_size = 1.0f / steps;
     SFX(vec3) surface_point = SFX(v3)(0, 0, 0);
@@ -197,10 +220,15 @@ static void SFX(volume_surface)(const SFX(vol)* dv, const REAL pv[16], SFX(vec3)
             double sup = SFX(support_margin)(dv, P);
             if (sup < sm) sm = sup;
         }
+        if (iso_shift && !(acc > iso)) slope += SFX(density_slope)(dv, P);
         acc += density;
         if (density != (REAL)0) {
             double dm = fabs((double)acc - (double)iso) / (double)iso;
             if (dm < m) m = dm;
+            if (iso_shift && slope > 0.0) {
+                double sh = fabs((double)acc - (double)iso) / slope;
+                if (sh < shift) shift = sh;
+            }
             if (acc <= iso) surface_point = P;
             if (acc >= iso) surface_point_found = 1;
             if (!entry_point_found) {
@@ -215,11 +243,11 @@ static void SFX(volume_surface)(const SFX(vol)* dv, const REAL pv[16], SFX(vec3)
     if (margin) *margin = m;
     if (taken) *taken = k;
     if (support_margin) *support_margin = sm;
+    if (iso_shift) *iso_shift = shift;
 }
 
-/* kajiya-kay.glsl:7-24; `kd` scales the diffuse term (1 = reference). */
-static SFX(vec3) SFX(kajiya_kay)(SFX(vec3) diffuse, SFX(vec3) specular, REAL p, SFX(vec3) tangent,
-                                  SFX(vec3) light, SFX(vec3) eye, REAL kd)
+/* One Kajiya-Kay specular lobe (kajiya-kay.glsl:15-21) of unit tangent t. */
+static REAL SFX(kk_lobe)(SFX(vec3) tangent, SFX(vec3) light, SFX(vec3) eye, REAL p)
 {
     REAL cosTL = SFX(dot)(tangent, light);
     REAL cosTE = SFX(dot)(tangent, eye);
@@ -227,8 +255,45 @@ static SFX(vec3) SFX(kajiya_kay)(SFX(vec3) diffuse, SFX(vec3) specular, REAL p, 
     REAL sinTL = SQRT_FN(a > 0 ? a : 0); /* sqrt of a negative rounding residue: 0 */
     REAL sinTE = SQRT_FN(b > 0 ? b : 0);
     REAL c = cosTL * cosTE + sinTL * sinTE;
-    REAL spec = POW_FN(c > 0 ? c : 0, p);
-    return SFX(add)(SFX(scale)(diffuse, kd * sinTL), SFX(scale)(specular, spec));
+    return POW_FN(c > 0 ? c : 0, p);
+}
+
+/* Extension: the tangent of a shifted lobe, normalize(t + shift * N) with N
+ * the unit direction towards the camera perpendicular to t (eye points from
+ * the camera to the surface); t itself where N is undefined (t || eye). */
+static SFX(vec3) SFX(shift_tangent)(SFX(vec3) t, SFX(vec3) eye, REAL shift)
+{
+    SFX(vec3) v = SFX(scale)(eye, (REAL)-1);
+    SFX(vec3) n = SFX(sub)(v, SFX(scale)(t, SFX(dot)(t, v)));
+    REAL len = SQRT_FN(SFX(dot)(n, n));
+    if (!(len > 0)) return t;
+    return SFX(normalize)(SFX(add)(t, SFX(scale)(n, shift / len)), NULL);
+}
+
+/* kajiya-kay.glsl:7-24; `kd` scales the diffuse term (1 = reference).
+ * Extension (all zero: the reference): a second, hair-coloured lobe of
+ * exponent p2 > 0 and per-lobe tangent shifts. */
+static SFX(vec3) SFX(kajiya_kay)(SFX(vec3) diffuse, SFX(vec3) specular, REAL p, SFX(vec3) tangent,
+                                  SFX(vec3) light, SFX(vec3) eye, REAL kd, REAL p2, REAL shift1, REAL shift2)
+{
+    REAL cosTL = SFX(dot)(tangent, light);
+    REAL cosTE = SFX(dot)(tangent, eye);
+    REAL a = (REAL)1 - cosTL * cosTL, b = (REAL)1 - cosTE * cosTE;
+    REAL sinTL = SQRT_FN(a > 0 ? a : 0); /* sqrt of a negative rounding residue: 0 */
+    REAL sinTE = SQRT_FN(b > 0 ? b : 0);
+    REAL spec;
+    if (shift1 == 0) {
+        REAL c = cosTL * cosTE + sinTL * sinTE;
+        spec = POW_FN(c > 0 ? c : 0, p);
+    } else {
+        spec = SFX(kk_lobe)(SFX(shift_tangent)(tangent, eye, shift1), light, eye, p);
+    }
+    SFX(vec3) out = SFX(add)(SFX(scale)(diffuse, kd * sinTL), SFX(scale)(specular, spec));
+    if (p2 > 0) {
+        SFX(vec3) t2 = shift2 == 0 ? tangent : SFX(shift_tangent)(tangent, eye, shift2);
+        out = SFX(add)(out, SFX(scale)(SFX(mul)(specular, diffuse), SFX(kk_lobe)(t2, light, eye, p2)));
+    }
+    return out;
 }
 
 /* approximate_deep_shadows.glsl:24-36. */
@@ -244,14 +309,40 @@ static REAL SFX(deep_shadows)(const SFX(vol)* dv, SFX(vec3) s, SFX(vec3) light, 
     return POW_FN((REAL)1 - alpha, strands);
 }
 
-/* local_ambient_occlusion.glsl:9-30. */
+/* Extension: AO direction i of n, the Fibonacci-sphere point with y as the
+ * polar axis (the directional AO of vkhr_raymarch_params). */
+static inline void SFX(ao_direction)(int i, int n, double d[3])
+{
+    const double pi = 3.14159265358979323846;
+    double y = 1.0 - (2.0 * i + 1.0) / (double)n;
+    double r = sqrt(1.0 - y * y);
+    double phi = (double)i * pi * (3.0 - sqrt(5.0));
+    d[0] = r * cos(phi);
+    d[1] = y;
+    d[2] = r * sin(phi);
+}
+
+/* local_ambient_occlusion.glsl:9-30; directions > 0: the directional
+ * extension, taps at s + d_i * radius * sqrt(3) * voxel size. */
 static REAL SFX(lao)(const SFX(vol)* dv, SFX(vec3) s, float kernel_size, REAL radius, REAL intensity,
-                     REAL min_intensity)
+                     REAL min_intensity, int directions)
 {
     REAL density = 0;
-    float kernel_radius = (kernel_size - 1.0f) / 2.0f;
     SFX(vec3) voxel_space = SFX(v3)(dv->size.x / (REAL)dv->n[0], dv->size.y / (REAL)dv->n[1],
                                     dv->size.z / (REAL)dv->n[2]);
+    if (directions > 0) {
+        for (int i = 0; i < directions; ++i) {
+            double d[3];
+            SFX(ao_direction)(i, directions, d);
+            const double reach = (double)radius * sqrt(3.0);
+            SFX(vec3) q = SFX(add)(s, SFX(mul)(SFX(v3)((REAL)(d[0] * reach), (REAL)(d[1] * reach),
+                                                       (REAL)(d[2] * reach)), voxel_space));
+            REAL r = SFX(sample_density)(dv, q);
+            density += r < min_intensity ? r : min_intensity;
+        }
+        return POW_FN((REAL)1 - density / (REAL)directions, intensity);
+    }
+    float kernel_radius = (kernel_size - 1.0f) / 2.0f;
     REAL voxel_scaling = radius / (REAL)kernel_radius;
     SFX(vec3) sc = SFX(scale)(voxel_space, voxel_scaling);
     for (float z = -kernel_radius; z <= +kernel_radius; z += 1.0f)
@@ -293,13 +384,22 @@ static void SFX(shade_pixel)(const vkhr_raymarch_params* p, const SFX(vol)* dv, 
     REAL a;
     double margin, support;
     int taken;
+    double shift;
     SFX(volume_surface)(dv, pv, start, end, p->raycast_steps, (REAL)p->isosurface, depth_buffer, &surf, &a,
-                        &margin, &taken, diag ? &support : NULL);
+                        &margin, &taken, diag ? &support : NULL, diag ? &shift : NULL);
     if (diag) {
         diag->iso_margin = margin;
         diag->steps_taken = taken;
         diag->tangent_len = 0;
         diag->support_margin = support;
+        diag->iso_shift = shift;
+        double tsc = 0, sc = 0;
+        for (int c = 0; c < 3; ++c) {
+            const double t = (double)p->volume_resolution[c] / (double)p->volume_bounds.size[c];
+            if (t > tsc) tsc = t;
+        }
+        sc = sqrt((double)(start.x * start.x + start.y * start.y + start.z * start.z));
+        diag->fp32_res = ldexp(sc + (double)p->volume_bounds.radius, -24) * tsc;
     }
     rgba[0] = rgba[1] = rgba[2] = rgba[3] = 0.0f;
     if (depth_out) *depth_out = 1.0f;
@@ -316,7 +416,8 @@ static void SFX(shade_pixel)(const vkhr_raymarch_params* p, const SFX(vol)* dv, 
     if (diag) diag->tangent_len = (double)tlen;
     if (p->shading_model == VKHR_SHADING_KAJIYA_KAY)
         shading = SFX(kajiya_kay)(SFX(from)(p->hair_color), SFX(from)(p->light_intensity), (REAL)p->hair_exponent,
-                                  T, L, E, (REAL)p->kd);
+                                  T, L, E, (REAL)p->kd, (REAL)p->spec_exponent2, (REAL)p->spec_shift[0],
+                                  (REAL)p->spec_shift[1]);
     REAL occlusion = 1;
     if (p->deep_shadows_on == 1 && p->shading_model != VKHR_SHADING_LAO) {
         float ss = p->shadow_steps > 0.0f ? p->shadow_steps : p->raycast_steps;
@@ -324,7 +425,7 @@ static void SFX(shade_pixel)(const vkhr_raymarch_params* p, const SFX(vol)* dv, 
     }
     if (p->shading_model != VKHR_SHADING_ADSM)
         occlusion *= SFX(lao)(dv, surf, p->ao_kernel_size, (REAL)p->occlusion_radius, (REAL)p->ao_exponent,
-                              (REAL)p->ao_max);
+                              (REAL)p->ao_max, p->ao_directions);
     rgba[0] = SFX(clamp01)(shading.x * occlusion);
     rgba[1] = SFX(clamp01)(shading.y * occlusion);
     rgba[2] = SFX(clamp01)(shading.z * occlusion);
@@ -353,7 +454,9 @@ static void SFX(raymarch_rows)(const vkhr_raymarch_params* p, const void* densit
     double inv[16];
     int invertible = oracle_vp_inverse(p, inv);
     if (threads <= 0) threads = oracle_max_threads();
-#pragma omp parallel for schedule(dynamic) num_threads(threads)
+    /* pixels, not rows, are the unit of work: a call over a few rows (or the
+     * footprint of a small volume) still uses every thread */
+#pragma omp parallel for collapse(2) schedule(dynamic, 64) num_threads(threads)
     for (int y = row_begin; y < row_end; ++y) {
         for (int x = 0; x < W; ++x) {
             size_t at = (size_t)y * (size_t)W + (size_t)x;
@@ -362,6 +465,8 @@ static void SFX(raymarch_rows)(const vkhr_raymarch_params* p, const void* densit
             if (dg) {
                 dg->iso_margin = 1.0 / 0.0;
                 dg->support_margin = 1.0 / 0.0;
+                dg->iso_shift = 1.0 / 0.0;
+                dg->fp32_res = 0;
                 dg->tangent_len = 0;
                 dg->steps_taken = 0;
                 dg->covered = 0;

@@ -86,6 +86,13 @@ typedef struct oracle_pixel_diag {
                               distance in texels to flipping `density != 0` (see
                               support_margin in raymarch_body.h; inf if none)          */
     double tangent_len;  /* length of the sampled tangent before normalisation         */
+    double iso_shift;    /* min over nonzero samples k of |acc_k - iso| / sum_{i<=k} |grad rho_i|_1:
+                            how far, in texels, every sample up to k would have to
+                            move to flip that sample's isosurface test (inf if none)  */
+    double fp32_res;     /* FP32 position resolution of the ray's samples, in texels:
+                            2^-24 (|start| + radius) max_k N_k / size_k (the samples
+                            mix(start, end, t) of an entry point and end point
+                            that are exact up to their own rounding)           */
     int32_t steps_taken; /* primary-loop iterations executed                          */
     int32_t covered;     /* 1 if the pixel spawned a ray                              */
 } oracle_pixel_diag;

@@ -46,16 +46,50 @@ def gpu_voxelize(ctx, mode, vertices, tangents, indices, bounds, res, index_mode
             None if tq is None else tq.cpu().numpy())
 
 
-def ill_conditioned(ref, diag, margin=1e-4, support=2e-4, tangent_floor=1e-4):
+def ill_conditioned(ref, diag, margin=1e-4, support=2e-4, tangent_floor=1e-4, shift_factor=0.5):
     """Pixels whose shader result hinges on a decision FP32 cannot resolve:
-    the isosurface test within `margin` (relative) of the threshold, a
-    `density != 0` test on a sample whose nonzero taps carry less than
-    `support` trilinear weight (about FP32's position resolution in texels),
-    or a surface tangent shorter than `tangent_floor` (normalisation
-    amplifies rounding)."""
+    the isosurface test within `margin` (relative) of the threshold, or
+    within `shift_factor` times the view's FP32 position resolution (in
+    texels) of flipping when the samples move (iso_shift: the margin over
+    the accumulated density slope); a `density != 0` test on a sample whose
+    nonzero taps carry less than `support` trilinear weight (or less than one
+    position resolution); or a surface tangent shorter than `tangent_floor`
+    (normalisation amplifies rounding).  The FP32 position resolution
+    (fp32_res) grows with the camera's distance and the grid's resolution."""
     emitted = ref[..., 3] > 0
-    return ((diag["iso_margin"] < margin) | (diag["support_margin"] < support)
+    res = diag["fp32_res"]
+    return ((diag["iso_margin"] < margin) | (diag["support_margin"] < np.maximum(support, res))
+            | (diag["iso_shift"] < shift_factor * res)
             | (emitted & (diag["tangent_len"] < tangent_floor) & (diag["tangent_len"] > 0)))
+
+
+RMS_TOL = 1e-3  # per channel, over well-conditioned pixels
+MAX_TOL = 2e-2
+
+
+def compare_images(gpu, gdepth, ref, rdepth, diag, label="", depth_tol=1e-4, max_excluded=0.01):
+    """The raymarch parity bar: per channel RMS <= 1e-3 and max <= 2e-2 over
+    well-conditioned pixels, at most `max_excluded` of the emitted fragments
+    excluded (1% of a frame; a test over many views or row bands allows 3%
+    in one of them and checks 1% over all of them), and every
+    well-conditioned depth within `depth_tol`.  Prints the counts (pytest -s
+    shows them); returns (rms, max, excluded, emitted)."""
+    rms, mx, excluded, emitted = image_errors(gpu, ref, diag)
+    print("%s: %d emitted fragments, %d excluded (%.3f%%), rms %s, max %s"
+          % (label, emitted, excluded, 100.0 * excluded / max(emitted, 1), np.round(rms, 6).tolist(),
+             np.round(mx, 5).tolist()))
+    assert emitted > 0, label
+    assert excluded <= max(2, max_excluded * emitted), (label, excluded, emitted)
+    assert np.all(rms <= RMS_TOL), (label, rms)
+    assert np.all(mx <= MAX_TOL), (label, mx)
+    ok = ~ill_conditioned(ref, diag)
+    dd = np.abs(gdepth - rdepth)
+    bad = np.argwhere(ok & (dd > depth_tol))
+    info = [(int(y), int(x), float(diag["iso_margin"][y, x]), float(diag["support_margin"][y, x]),
+             float(diag["tangent_len"][y, x]), float(rdepth[y, x]), float(gdepth[y, x]), ref[y, x].tolist(),
+             gpu[y, x].tolist()) for y, x in bad[:8]]
+    assert len(bad) == 0, (label, len(bad), info)
+    return rms, mx, excluded, emitted
 
 
 def image_errors(gpu, ref, diag, **kw):

@@ -27,7 +27,7 @@ def test_struct_layouts(native_lib):
     assert native_lib.vkhr_sizeof_raymarch_params() == C.sizeof(_abi.RaymarchParams)
     assert native_lib.vkhr_sizeof_voxel_job() == C.sizeof(_abi.VoxelJob) == 104
     assert native_lib.vkhr_sizeof_raymarch_job() == C.sizeof(_abi.RaymarchJob)
-    assert native_lib.vkhr_abi_version() == 1
+    assert native_lib.vkhr_abi_version() == 2
 
 
 def test_status_strings_and_null_context(native_lib):

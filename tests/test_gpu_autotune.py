@@ -1,6 +1,7 @@
-"""The raymarch autotuner: every ray-packet variant renders the same image
-(same per-pixel device code), and vkhr_autotune_raymarch keeps a variant
-that later calls use."""
+"""The raymarch autotuner: every ray-packet variant it tunes renders the same
+image (same per-pixel device code), and vkhr_autotune_raymarch keeps a
+variant that later calls use.  The TMA-staged variant equals the L2 march
+bit for bit; the texture-unit variant is measured against the FP64 oracle."""
 import numpy as np
 import pytest
 
@@ -22,7 +23,7 @@ def test_variants_render_the_same_image(ctx, oracle_lib):
     p = scene.make_params(b, res, 333, 251, raycast_steps=256.0, shadow_steps=32.0)
     dd, dt = to_dev(dn, torch), to_dev(tq, torch)
     imgs = []
-    for v in range(_abi.RAYMARCH_VARIANTS):
+    for v in range(_abi.TUNED_RAYMARCH_VARIANTS):
         ctx.set_raymarch_variant(p.density_format, p.tangent_format, v)
         rgba = torch.full((p.height, p.width, 4), -7.0, dtype=torch.float32, device="cuda")
         ctx.raymarch(p, dd.data_ptr(), dt.data_ptr(), None, rgba.data_ptr(), None)
@@ -33,8 +34,120 @@ def test_variants_render_the_same_image(ctx, oracle_lib):
     assert (imgs[0][..., 3] > 0).sum() > 1000
     rgba = torch.empty((p.height, p.width, 4), dtype=torch.float32, device="cuda")
     chosen, ms = ctx.autotune_raymarch(p, dd.data_ptr(), dt.data_ptr(), rgba.data_ptr())
-    assert 0 <= chosen < _abi.RAYMARCH_VARIANTS and min(ms) > 0 and ms[chosen] == min(ms)
+    tuned = ms[:_abi.TUNED_RAYMARCH_VARIANTS]
+    assert 0 <= chosen < _abi.TUNED_RAYMARCH_VARIANTS and min(tuned) > 0 and ms[chosen] == min(tuned)
+    assert ms[_abi.RAYMARCH_TEXTURE_VARIANT] == 0.0  # not a candidate
     assert np.array_equal(rgba.cpu().numpy(), imgs[0])
     with pytest.raises(VkhrError):
         ctx.set_raymarch_variant(p.density_format, p.tangent_format, _abi.RAYMARCH_VARIANTS)
     ctx.set_raymarch_variant(p.density_format, p.tangent_format, 0)
+
+
+@pytest.mark.parametrize("fmt,tfmt,res,view,depth", [
+    (_abi.DENSITY_U8_UNORM, _abi.TANGENT_I8_SNORM, (64, 64, 64), (0.0, 0.0, 1.0), False),
+    (_abi.DENSITY_U8_UNORM, _abi.TANGENT_F32X4, (48, 32, 40), (0.6, 0.3, 1.0), True),
+    (_abi.DENSITY_U32_COUNT, _abi.TANGENT_I8_SNORM, (40, 44, 36), (-0.4, 0.8, 0.5), False),
+    (_abi.DENSITY_F32, _abi.TANGENT_F32X4, (36, 28, 52), (0.2, -0.5, -1.0), True),
+    (_abi.DENSITY_U8_UNORM, _abi.TANGENT_I8_SNORM, (37, 50, 29), (0.3, 0.2, 1.0), False),  # pitch: no TMA
+])
+def test_staged_variant_equals_l2_march(ctx, oracle_lib, fmt, tfmt, res, view, depth):
+    """Variant 4 (each occupied brick a warp's rays need staged into shared
+    memory by one TMA copy) against variant 0 (texels from L2): the same
+    pixels bit for bit, with and without a depth buffer, for every density
+    format, for a view whose volume straddles the image's edge, and for a
+    grid whose row pitch TMA cannot address (which falls back to variant 0);
+    and against the FP64 oracle."""
+    import torch
+
+    from tests._helpers import compare_images
+
+    st, t, idx = style("hemi", 3000, 14, seed=17)
+    b = oracle_lib.bounding_box(st.vertices)
+    c, d, tq, _ = oracle_lib.voxelize("segments", st.vertices, t, idx, b, res)
+    if fmt == _abi.DENSITY_U8_UNORM:
+        dens, iso = oracle_lib.normalize(d), 0.115
+    elif fmt == _abi.DENSITY_U32_COUNT:
+        dens, iso = c, 1.0
+    else:
+        dens, iso = c.astype(np.float32) * np.float32(0.25), 0.25
+    tan = tq if tfmt == _abi.TANGENT_I8_SNORM else np.maximum(tq.astype(np.float32) / 127.0, -1.0)
+    o, sz = np.asarray(b.origin, dtype=np.float64), np.asarray(b.size, dtype=np.float64)
+    p = scene.make_params(b, res, 300, 220, raycast_steps=256.0, shadow_steps=32.0, isosurface=iso,
+                          view_direction=view, target=o + 0.5 * sz + np.array([0.45, 0.1, 0.0]) * sz,
+                          density_format=fmt, tangent_format=tfmt, **scene.CONFIG_SHADING)
+    dd, dt = to_dev(dens, torch), to_dev(tan, torch)
+    din = None
+    depth_np = None
+    if depth:
+        base = torch.full((p.height, p.width, 4), -7.0, dtype=torch.float32, device="cuda")
+        bd = torch.empty((p.height, p.width), dtype=torch.float32, device="cuda")
+        ctx.raymarch(p, dd.data_ptr(), dt.data_ptr(), None, base.data_ptr(), bd.data_ptr())
+        torch.cuda.synchronize()
+        depth_np = np.where(bd.cpu().numpy() < 1.0, bd.cpu().numpy() + 1e-3, 0.5).astype(np.float32)
+        depth_np[:, : p.width // 2] = 1.0
+        din = torch.from_numpy(depth_np).cuda()
+    imgs = []
+    for v in (0, 4):
+        ctx.set_raymarch_variant(fmt, tfmt, v)
+        rgba = torch.full((p.height, p.width, 4), -7.0, dtype=torch.float32, device="cuda")
+        dep = torch.full((p.height, p.width), -7.0, dtype=torch.float32, device="cuda")
+        ctx.raymarch(p, dd.data_ptr(), dt.data_ptr(), None if din is None else din.data_ptr(), rgba.data_ptr(),
+                     dep.data_ptr())
+        ctx.check_status(None)
+        torch.cuda.synchronize()
+        imgs.append((rgba.cpu().numpy(), dep.cpu().numpy()))
+    ctx.set_raymarch_variant(fmt, tfmt, 0)
+    assert np.array_equal(imgs[0][0], imgs[1][0]), int((imgs[0][0] != imgs[1][0]).any(axis=2).sum())
+    assert np.array_equal(imgs[0][1], imgs[1][1])
+    assert (imgs[1][0][..., 3] > 0).sum() > 200
+    ref, rdepth, diag = oracle_lib.raymarch(p, dens, tan, depth_in=depth_np, diag=True)
+    # small views (300x220) whose depth buffer cuts rays mid-volume: up to 2% excluded
+    compare_images(imgs[1][0], imgs[1][1], ref, rdepth, diag, label="staged variant", max_excluded=0.02)
+
+
+@pytest.mark.parametrize("fmt", [_abi.DENSITY_U8_UNORM, _abi.DENSITY_F32])
+def test_texture_unit_variant(ctx, oracle_lib, fmt):
+    """Variant 5 samples the density through the texture unit (a 3D array with
+    hardware LINEAR filtering and border 0).  Its filter weights have 8
+    fractional bits, so it is measured, not required to match: the errors
+    against the FP64 oracle are printed, and bounded only loosely (the same
+    surfaces: coverage within 0.1, colour within 0.25).  Counts fall back to
+    the memory path, bit for bit."""
+    import torch
+
+    st, t, idx = style("hemi", 4096, 16)
+    b = oracle_lib.bounding_box(st.vertices)
+    res = (64, 64, 64)
+    c, d, tq, _ = oracle_lib.voxelize("segments", st.vertices, t, idx, b, res)
+    if fmt == _abi.DENSITY_U8_UNORM:
+        dens, iso = oracle_lib.normalize(d), 0.115
+    else:
+        dens, iso = (oracle_lib.normalize(d).astype(np.float32) / 255.0), 0.115
+    p = scene.make_params(b, res, 320, 240, raycast_steps=256.0, shadow_steps=32.0, isosurface=iso,
+                          density_format=fmt)
+    dd, dt = to_dev(dens, torch), to_dev(tq, torch)
+    ctx.set_raymarch_variant(fmt, p.tangent_format, _abi.RAYMARCH_TEXTURE_VARIANT)
+    rgba = torch.full((p.height, p.width, 4), -7.0, dtype=torch.float32, device="cuda")
+    ctx.raymarch(p, dd.data_ptr(), dt.data_ptr(), None, rgba.data_ptr(), None)
+    torch.cuda.synchronize()
+    ctx.set_raymarch_variant(fmt, p.tangent_format, 0)
+    img = rgba.cpu().numpy()
+    ref, rdepth, diag = oracle_lib.raymarch(p, dens, tq, diag=True)
+    from tests._helpers import image_errors
+    rms, mx, excluded, emitted = image_errors(img, ref, diag)
+    print("texture-unit variant, density format %d: rms %s max %s (memory path bar: rms 1e-3, max 2e-2)"
+          % (fmt, np.round(rms, 5).tolist(), np.round(mx, 4).tolist()))
+    assert (img != -7.0).all() and emitted > 1000
+    assert np.all(mx[:3] <= 0.25) and mx[3] <= 0.1
+    # counts cannot be filtered by the texture unit: variant 5 runs the memory path
+    pc = scene.make_params(b, res, 320, 240, raycast_steps=256.0, isosurface=1.0, density_format=_abi.DENSITY_U32_COUNT)
+    dc = to_dev(c, torch)
+    outs = []
+    for v in (0, _abi.RAYMARCH_TEXTURE_VARIANT):
+        ctx.set_raymarch_variant(_abi.DENSITY_U32_COUNT, pc.tangent_format, v)
+        o = torch.empty((pc.height, pc.width, 4), dtype=torch.float32, device="cuda")
+        ctx.raymarch(pc, dc.data_ptr(), dt.data_ptr(), None, o.data_ptr(), None)
+        torch.cuda.synchronize()
+        outs.append(o.cpu().numpy())
+    ctx.set_raymarch_variant(_abi.DENSITY_U32_COUNT, pc.tangent_format, 0)
+    assert np.array_equal(outs[0], outs[1])

@@ -89,3 +89,60 @@ def test_frame_graph_follows_moving_strands(native_lib, oracle_lib, budget):
         graph.close()
     finally:
         ctx.close()
+
+
+def test_live_frame_graph_keeps_scratch_in_place(native_lib, oracle_lib):
+    """A frame graph holds the addresses of its context's scratch: while it
+    exists, a call on that context that would have to grow a scratch buffer
+    (here the raymarch's occupancy bitmap, for a larger grid) fails with
+    VKHR_ERR_CAPACITY instead of moving it, and the graph still renders the
+    frame it captured; once the graph is destroyed the call succeeds."""
+    import torch
+
+    from vkhr_gb300 import _native
+    from vkhr_gb300._native import VkhrError
+
+    res = (32, 32, 32)
+    n = res[0] * res[1] * res[2]
+    W, H = 96, 72
+    st, t, idx = style("hemi", 1500, 10)
+    b = oracle_lib.bounding_box(st.vertices)
+    dv, dt = to_dev(st.vertices, torch), to_dev(t, torch)
+    di = to_dev(np.asarray(idx, dtype=np.uint32), torch)
+    counts = torch.zeros(n, dtype=torch.int32, device="cuda")
+    dens = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    tq = torch.zeros((n, 4), dtype=torch.int8, device="cuda")
+    rgba = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    job = _abi.VoxelJob()
+    job.d_vertices, job.d_tangent_in, job.d_indices = dv.data_ptr(), dt.data_ptr(), di.data_ptr()
+    job.item_count = len(idx)
+    job.bounds = b
+    job.width, job.height, job.depth = res
+    job.index_mode = _abi.INDEX_REF_FP32
+    job.d_counts, job.d_densities, job.d_tangents = counts.data_ptr(), dens.data_ptr(), tq.data_ptr()
+    p = scene.make_params(b, res, W, H, raycast_steps=128.0, shadow_steps=32.0)
+    # a larger grid the context has not raymarched yet
+    big = (264, 264, 264)  # more occupancy bricks than the scratch the graph holds (grown with headroom)
+    pb = scene.make_params(b, big, W, H, raycast_steps=64.0)
+    bd = torch.zeros(big[0] * big[1] * big[2], dtype=torch.uint8, device="cuda")
+    bt = torch.zeros((big[0] * big[1] * big[2], 4), dtype=torch.int8, device="cuda")
+    out = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    ctx = _native.Context(0)
+    s = torch.cuda.current_stream().cuda_stream
+    try:
+        graph = ctx.frame_graph(True, job, p, rgba.data_ptr(), None, stream=s)
+        with pytest.raises(VkhrError) as e:
+            ctx.raymarch(pb, bd.data_ptr(), bt.data_ptr(), None, out.data_ptr(), None, s)
+        assert e.value.status == _abi.VKHR_ERR_CAPACITY
+        rgba.zero_()
+        graph.launch(s)
+        torch.cuda.synchronize()
+        ctx.check_status(s)
+        c_ref, d_ref, t_ref, _ = oracle_lib.voxelize("segments", st.vertices, t, idx, b, res)
+        assert np.array_equal(counts.cpu().numpy().view(np.uint32), c_ref)
+        assert (rgba[..., 3] > 0).sum().item() > 50
+        graph.close()
+        ctx.raymarch(pb, bd.data_ptr(), bt.data_ptr(), None, out.data_ptr(), None, s)  # may grow now
+        torch.cuda.synchronize()
+    finally:
+        ctx.close()

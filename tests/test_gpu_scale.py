@@ -1,18 +1,20 @@
 """The scale workload: 1,048,576 strands x 32 vertices (33,554,432 vertices,
 32,505,856 segments) grown on a radius-1.2 hemisphere with step 0.04,
-segment-voxelized into 512^3 and raymarched at 3840x2160 with 1024 steps and
-128-step shadows, plus four views of the volume in one batched launch.
+segment-voxelized into 512^3 and raymarched at 3840x2160 with 1024 steps,
+128-step shadows, 16-direction AO and the workloads' dual-lobe Kajiya-Kay,
+plus four 3840x2160 views of the volume in one batched launch.
 
 The voxelization is checked bit for bit against the oracle over the whole
 grid (counts, u8 densities, int8 tangents) in the reference's FP32 index
 mode, which at 512^3 (> 2^24 voxels) reproduces the reference's rounded
 indices (hair_style.cc:321).  The frame is checked against the FP64 oracle
-on row bands; the four batched views equal their single-view renders."""
+on row bands; the four batched views equal their single-view renders, and
+each is checked against the FP64 oracle on a row band."""
 import numpy as np
 import pytest
 
 from vkhr_gb300 import _abi, _native, scene, strands
-from tests._helpers import image_errors, to_dev
+from tests._helpers import compare_images, to_dev
 
 pytestmark = pytest.mark.gpu
 
@@ -67,7 +69,8 @@ def test_scale_voxelization_bit_exact(scale_volume):
 
 
 def _params(b, w, h, **kw):
-    return scene.make_params(b, RES, w, h, camera_distance=5.0, raycast_steps=1024.0, shadow_steps=128.0, **kw)
+    return scene.make_params(b, RES, w, h, camera_distance=5.0, raycast_steps=1024.0, shadow_steps=128.0,
+                             ao_directions=16, **scene.CONFIG_SHADING, **kw)
 
 
 def test_scale_frame_rows(ctx, oracle_lib, scale_volume):
@@ -85,23 +88,27 @@ def test_scale_frame_rows(ctx, oracle_lib, scale_volume):
     assert lit.size > 200
     lo, hi = int(lit.min()), int(lit.max())
     dn, tqn = dens.cpu().numpy(), tq.cpu().numpy()
-    for f in (0.2, 0.5, 0.8):
+    excluded = emitted = 0
+    for f in (0.2, 0.35, 0.5, 0.65, 0.8):  # inside the lit span: grazing rows at its edges are mostly ill-conditioned
         r0 = int(lo + f * (hi - lo))
-        rows = (r0, r0 + 8)
+        rows = (r0, r0 + 16)
         ref, rdepth, diag = oracle_lib.raymarch(p, dn, tqn, diag=True, rows=rows)
-        rms, mx, excluded, emitted = image_errors(gpu[r0:r0 + 8], ref[r0:r0 + 8], diag[r0:r0 + 8])
-        assert emitted > 0 and excluded <= max(2, 0.01 * emitted), (excluded, emitted)
-        assert np.all(rms <= 1e-3) and np.all(mx <= 2e-2), (rms, mx)
+        _, _, ex, em = compare_images(gpu[r0:r0 + 16], gdepth[r0:r0 + 16], ref[r0:r0 + 16], rdepth[r0:r0 + 16],
+                                      diag[r0:r0 + 16], label="scale frame rows %d..%d" % rows, max_excluded=0.03)
+        excluded += ex
+        emitted += em
+    assert excluded <= 0.01 * emitted, (excluded, emitted)
 
 
-def test_scale_four_views_batched(ctx, scale_volume):
-    """Four views of the 512^3 volume in one batched launch equal the four
-    single-view renders, pixel for pixel."""
+def test_scale_four_views_batched(ctx, oracle_lib, scale_volume):
+    """Four 3840x2160 views of the 512^3 volume in one batched launch equal
+    the four single-view renders, pixel for pixel, and each matches the FP64
+    oracle on a band of rows through its middle."""
     import torch
 
     b, dens, tq = scale_volume
     s = torch.cuda.current_stream().cuda_stream
-    views = [_params(b, 1920, 1080, view_direction=vd) for vd in
+    views = [_params(b, 3840, 2160, view_direction=vd) for vd in
              ((0.0, 0.0, 1.0), (1.0, 0.3, 0.0), (0.0, 1.0, 0.2), (-0.7, 0.2, -0.7))]
     rects = [_native.raymarch_footprint(p) for p in views]
     pitch = sum(r[2] for r in rects)
@@ -119,12 +126,22 @@ def test_scale_four_views_batched(ctx, scale_volume):
     ctx.raymarch_batched(jobs, s)
     torch.cuda.synchronize()
     A = atlas.cpu().numpy()
-    full = torch.empty((1080, 1920, 4), dtype=torch.float32, device="cuda")
-    at = 0
-    for p, (x0, y0, w, h) in zip(views, rects):
-        ctx.raymarch(p, dens.data_ptr(), tq.data_ptr(), None, full.data_ptr(), None, s)
+    full = torch.empty((2160, 3840, 4), dtype=torch.float32, device="cuda")
+    full_d = torch.empty((2160, 3840), dtype=torch.float32, device="cuda")
+    dn, tqn = dens.cpu().numpy(), tq.cpu().numpy()
+    at = excluded = emitted = 0
+    for k, (p, (x0, y0, w, h)) in enumerate(zip(views, rects)):
+        ctx.raymarch(p, dens.data_ptr(), tq.data_ptr(), None, full.data_ptr(), full_d.data_ptr(), s)
         torch.cuda.synchronize()
-        F = full.cpu().numpy()
+        F, FD = full.cpu().numpy(), full_d.cpu().numpy()
         assert np.array_equal(A[:h, at:at + w], F[y0:y0 + h, x0:x0 + w])
         assert (F[..., 3] > 0).any()
+        r0 = y0 + h // 2 - 8
+        ref, rdepth, diag = oracle_lib.raymarch(p, dn, tqn, diag=True, rows=(r0, r0 + 16))
+        sl = slice(r0, r0 + 16)
+        _, _, ex, em = compare_images(F[sl], FD[sl], ref[sl], rdepth[sl], diag[sl],
+                                      label="scale view %d rows %d..%d" % (k, r0, r0 + 16), max_excluded=0.03)
+        excluded += ex
+        emitted += em
         at += w
+    assert excluded <= 0.01 * emitted, (excluded, emitted)

@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 from vkhr_gb300 import _abi, strands
-from tests._helpers import gpu_voxelize, style
+from tests._helpers import gpu_voxelize, style, to_dev
 
 pytestmark = pytest.mark.gpu
 
@@ -29,32 +29,92 @@ def test_small_style(ctx, oracle_lib, mode, res):
     assert c.sum() > 0
 
 
-def test_one_walk_slices_and_compact_fallback(native_lib, oracle_lib):
-    """Segment calls without a visit budget: the first call on a context walks
-    twice (count, then fill) and learns a per-brick capacity from its largest
-    brick; later calls walk once, writing each run into its brick's fixed
-    slice (one kernel fewer); a style whose largest brick outgrows the
-    capacity fills again in the compact layout.  Every call is bit-exact."""
+def test_unbudgeted_calls_learn_their_size(native_lib, oracle_lib):
+    """Segment calls without a visit budget.  The first call at a size (index
+    count, grid, index mode, tangents) reads its visit total back, which a
+    stream capture refuses; a later call at that size sizes its scratch from
+    it, walks once into per-brick slices with the device choosing the
+    layout, and waits on nothing, so it can be captured.  A call at a known
+    size that needs more than twice the learned visits in its visit list
+    records a capacity overflow (reported by vkhr_check_status); the next
+    call at that size counts again.  Every result that is not reported as
+    overflowed is bit-exact."""
+    import torch
+
     from vkhr_gb300 import _native
+    from vkhr_gb300._native import VkhrError
 
     c = _native.Context(0)
     try:
-        sparse = style("hemi", 2048, 12)
-        dense = style("disk", 40_000, 13)  # bricks far above the sparse style's largest
+        sparse = style("hemi", 2048, 12)    # 56,145 visits into 96^3
+        dense = style("disk", 2048, 12)     # the same index count: 177,814 visits
+        big = style("disk", 40_000, 13)     # bricks far above the sparse style's largest
         res = (96, 96, 96)
+
+        def captured(s):
+            """The call under stream capture: True if it captured (no host wait)."""
+            st, t, idx = s
+            b = oracle_lib.bounding_box(st.vertices)
+            n = res[0] * res[1] * res[2]
+            dv, dt, di = to_dev(st.vertices, torch), to_dev(t, torch), to_dev(idx, torch)
+            out = [torch.full((n,), -1, dtype=torch.int32, device="cuda"),
+                   torch.full((n,), 77, dtype=torch.uint8, device="cuda"),
+                   torch.full((n, 4), 55, dtype=torch.int8, device="cuda")]
+            torch.cuda.synchronize()
+            graph = torch.cuda.CUDAGraph()
+            ok = True
+            try:
+                with torch.cuda.graph(graph):
+                    c.voxelize_segments(dv.data_ptr(), dt.data_ptr(), di.data_ptr(), len(idx), b, res,
+                                        _abi.INDEX_REF_FP32, out[0].data_ptr(), out[1].data_ptr(), out[2].data_ptr(),
+                                        torch.cuda.current_stream().cuda_stream)
+            except VkhrError as e:
+                assert e.status == _abi.VKHR_ERR_INVALID_ARG  # needs its visit total: not capturable
+                ok = False
+            if ok:
+                graph.replay()
+                torch.cuda.synchronize()
+                c.check_status(None)
+                c_ref, d_ref, t_ref, _ = oracle_lib.voxelize("segments", st.vertices, t, idx, b, res)
+                assert np.array_equal(out[0].cpu().numpy().view(np.uint32), c_ref)
+                assert np.array_equal(out[1].cpu().numpy(), d_ref)
+                assert np.array_equal(out[2].cpu().numpy(), t_ref)
+            return ok
 
         def run(s):
             st, t, idx = s
-            b = oracle_lib.bounding_box(st.vertices)
-            n0 = c.launch_count()
-            _check(c, oracle_lib, "segments", st.vertices, t, idx, b, res)
-            return c.launch_count() - n0
+            _check(c, oracle_lib, "segments", st.vertices, t, idx, oracle_lib.bounding_box(st.vertices), res)
 
-        two_walks = run(sparse)
-        assert run(sparse) == two_walks - 1      # one walk into the learned slices
-        assert run(dense) == two_walks           # a brick past its slice: compact fill
-        assert run(dense) == two_walks - 1       # capacity grown from that call
-        assert run(sparse) == two_walks - 1      # grow-only: still fits
+        # (a capture must not allocate either: the larger style sizes the scratch first)
+        run(big)                      # counted: the context learns the size and a per-brick capacity
+        run(big)                      # known size: scratch for twice its visits
+        assert captured(big)          # known size: no host wait
+        assert not captured(sparse)   # a new size: reads its visits back
+        run(sparse)                   # counted: the context learns the size
+        assert captured(sparse)
+    finally:
+        c.close()
+    # A context that has seen only the sparse style: its per-brick slices are
+    # too small for the dense style's bricks, so a dense call at the sparse
+    # style's size is laid out compactly in a visit list sized for twice the
+    # sparse style's visits, which is too small: a reported overflow.
+    c = _native.Context(0)
+    try:
+        run(sparse)
+        st, t, idx = dense
+        b = oracle_lib.bounding_box(st.vertices)
+        dv, dt, di = to_dev(st.vertices, torch), to_dev(t, torch), to_dev(idx, torch)
+        n = res[0] * res[1] * res[2]
+        counts = torch.empty(n, dtype=torch.int32, device="cuda")
+        dens = torch.empty(n, dtype=torch.uint8, device="cuda")
+        tq = torch.empty((n, 4), dtype=torch.int8, device="cuda")
+        c.voxelize_segments(dv.data_ptr(), dt.data_ptr(), di.data_ptr(), len(idx), b, res, _abi.INDEX_REF_FP32,
+                            counts.data_ptr(), dens.data_ptr(), tq.data_ptr(), torch.cuda.current_stream().cuda_stream)
+        with pytest.raises(VkhrError) as e:
+            c.check_status(None)
+        assert e.value.status == _abi.VKHR_ERR_CAPACITY
+        run(dense)                    # the context forgot its sizes: this call counts again, bit-exact
+        run(dense)                    # and the next one sizes from that count
     finally:
         c.close()
 

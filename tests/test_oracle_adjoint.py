@@ -1,6 +1,8 @@
 """The FP64 oracle of the differentiable path against FP64 central finite
 differences (h = 1e-3): the analytic gradient with respect to densities,
-tangent components, kd and the specular exponent, and the splat's adjoint.
+tangent components, kd and the specular exponents, and the splat's adjoint;
+for the reference's shading, for the workloads' dual-lobe Kajiya-Kay with
+tangent shifts, and for the directional ambient occlusion.
 A coordinate is ill-conditioned, and excluded (at most 10% of them), when
 the loss is not smooth there at the scale of h: the central differences
 at h and h/2 disagree by more than 1e-3 relative, or the loss at the point
@@ -20,7 +22,14 @@ TOL = 1e-3
 FLOOR = 1e-10  # |dL/dx| below this is rounding noise of the loss (~1e-16 L / h)
 
 
-def diff_scene(O, res=(24, 24, 24), size=(40, 30), steps=64.0, seed=3):
+SHADINGS = {
+    "reference": {},
+    "dual_lobe": {"spec_exponent2": 8.0, "spec_shift": (0.1, -0.1)},
+    "dual_lobe_ao16": {"spec_exponent2": 8.0, "spec_shift": (0.1, -0.1), "ao_directions": 16},
+}
+
+
+def diff_scene(O, res=(24, 24, 24), size=(40, 30), steps=64.0, seed=3, shading=None):
     """A splatted style, a smooth random tangent field, and a target image
     rendered from log-normally perturbed densities with exponent 60."""
     st, t, idx = style("hemi", 1500, 12, seed=seed)
@@ -31,7 +40,7 @@ def diff_scene(O, res=(24, 24, 24), size=(40, 30), steps=64.0, seed=3):
     tan = np.zeros((n, 4))
     tan[:, :3] = np.array([1.0, 0.3, 0.2]) + 0.3 * rng.normal(size=(n, 3))
     kw = dict(camera_distance=5.0, raycast_steps=steps, shadow_steps=32.0, isosurface=1.0, kd=0.4,
-              density_format=_abi.DENSITY_F32, tangent_format=_abi.TANGENT_F32X4)
+              density_format=_abi.DENSITY_F32, tangent_format=_abi.TANGENT_F32X4, **(shading or {}))
     p = scene.make_params(b, res, size[0], size[1], hair_exponent=80.0, **kw)
     pt = scene.make_params(b, res, size[0], size[1], hair_exponent=60.0, **kw)
     noisy = (dens * rng.lognormal(0.0, 0.2, size=n)).astype(np.float32)
@@ -60,9 +69,10 @@ def check(fd_of, analytic, coords):
     assert not bad, bad[:5]
 
 
-def test_density_tangent_and_params(oracle_lib):
+@pytest.mark.parametrize("shading", sorted(SHADINGS))
+def test_density_tangent_and_params(oracle_lib, shading):
     O = oracle_lib
-    st, b, p, dens, tan, target = diff_scene(O)
+    st, b, p, dens, tan, target = diff_scene(O, shading=SHADINGS[shading])
     loss, gd, gt, gp = O.diff_loss(p, dens, tan, target, grads=True)
     assert np.abs(gd).max() > 0 and np.abs(gt).max() > 0
     rng = np.random.default_rng(1)
@@ -93,19 +103,20 @@ def test_density_tangent_and_params(oracle_lib):
 
     def fd_param(k, h):
         # the parameter block holds float32: difference over the stored values
+        field = ("kd", "hair_exponent", "spec_exponent2")[k]
+
         def at(x):
             q = _abi.RaymarchParams.from_buffer_copy(p)
-            if k == 0:
-                q.kd = x
-            else:
-                q.hair_exponent = x
-            return q, (q.kd if k == 0 else q.hair_exponent)
-        x0 = p.kd if k == 0 else p.hair_exponent
+            setattr(q, field, x)
+            return q, getattr(q, field)
+        x0 = getattr(p, field)
         (qm, xm), (qp, xp) = at(x0 - h), at(x0 + h)
         lo, mid, hi = (O.diff_loss(q, dens, tan, target) for q in (qm, p, qp))
         return (hi - lo) / (xp - xm), abs(mid - (lo * (xp - x0) + hi * (x0 - xm)) / (xp - xm))
 
-    check(fd_param, lambda k: gp[k], [0, 1])
+    check(fd_param, lambda k: gp[k], [0, 1, 2] if p.spec_exponent2 > 0 else [0, 1])
+    if p.spec_exponent2 <= 0:
+        assert gp[2] == 0
 
 
 def test_splat_adjoint(oracle_lib):
@@ -135,12 +146,13 @@ def test_splat_adjoint(oracle_lib):
     assert skipped <= 3
 
 
-def test_forward_matches_raymarch_oracle(oracle_lib):
+@pytest.mark.parametrize("shading", sorted(SHADINGS))
+def test_forward_matches_raymarch_oracle(oracle_lib, shading):
     """The differentiable oracle's forward is the FP64 raymarch oracle
     (volume.frag:31-103): with that oracle's image as the target the loss is
     only the rounding of the target to float32."""
     O = oracle_lib
-    st, b, p, dens, tan, target = diff_scene(O)
+    st, b, p, dens, tan, target = diff_scene(O, shading=SHADINGS[shading])
     d32, t32 = dens.astype(np.float32), tan.astype(np.float32)
     ref, _ = O.raymarch(p, d32, t32, precision="f64")
     assert (ref[..., 3] > 0).sum() > 100

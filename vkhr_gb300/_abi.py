@@ -32,7 +32,10 @@ STATUS_NAMES = {
 INDEX_REF_FP32 = 0
 INDEX_EXACT = 1
 
-RAYMARCH_VARIANTS = 4
+RAYMARCH_VARIANTS = 6
+TUNED_RAYMARCH_VARIANTS = 5  # variants 0-4 compute the same pixels; 5 samples through the texture unit
+RAYMARCH_TEXTURE_VARIANT = 5
+MAX_AO_DIRECTIONS = 32
 
 FILTER_MAX = 0
 FILTER_MIN = 1
@@ -157,6 +160,9 @@ class RaymarchParams(C.Structure):
         ("kd", C.c_float),
         ("density_format", C.c_int32),
         ("tangent_format", C.c_int32),
+        ("spec_exponent2", C.c_float),
+        ("spec_shift", C.c_float * 2),
+        ("ao_directions", C.c_int32),
     ]
 
 

@@ -285,7 +285,7 @@ class Context:
     def autotune_raymarch(self, params, d_density, d_tangent, d_rgba, stream=None):
         """(chosen variant, [median ms of each variant])."""
         chosen = C.c_int32(-1)
-        ms = (C.c_float * 4)()
+        ms = (C.c_float * _abi.RAYMARCH_VARIANTS)()
         self.check(self.lib.vkhr_autotune_raymarch(self.handle, C.byref(params), d_density, d_tangent, d_rgba,
                                                    C.byref(chosen), ms, stream))
         return int(chosen.value), [float(x) for x in ms]

@@ -11,22 +11,24 @@ import torch
 from . import _abi
 
 
-def _params_with(params, kd, exponent):
+def _params_with(params, kd, exponent, exponent2=None):
     p = _abi.RaymarchParams.from_buffer_copy(params)
     p.kd = float(kd)
     p.hair_exponent = float(exponent)
+    if exponent2 is not None:
+        p.spec_exponent2 = float(exponent2)
     p.density_format = _abi.DENSITY_F32
     p.tangent_format = _abi.TANGENT_F32X4
     return p
 
 
 class RaymarchFunction(torch.autograd.Function):
-    """rgba (H, W, 4) = raymarch(density (n,), tangent (n, 4), kd_exp (2,))."""
+    """rgba (H, W, 4) = raymarch(density (n,), tangent (n, 4), kd_exp), kd_exp
+    = (kd, hair_exponent) or (kd, hair_exponent, spec_exponent2)."""
 
     @staticmethod
     def forward(fctx, density, tangent, kd_exp, params, native, K):
-        kd, exponent = (float(x) for x in kd_exp.detach().cpu())
-        p = _params_with(params, kd, exponent)
+        p = _params_with(params, *(float(x) for x in kd_exp.detach().cpu()))
         density = density.contiguous()
         tangent = tangent.contiguous()
         dev = density.device
@@ -37,7 +39,7 @@ class RaymarchFunction(torch.autograd.Function):
         native.raymarch_train(p, density.data_ptr(), tangent.data_ptr(), rgba.data_ptr(), None, tape.data_ptr(),
                               nbytes, K, s)
         fctx.save_for_backward(density, tangent, tape)
-        fctx.params, fctx.native, fctx.K = p, native, K
+        fctx.params, fctx.native, fctx.K, fctx.nparams = p, native, K, kd_exp.numel()
         return rgba
 
     @staticmethod
@@ -46,11 +48,11 @@ class RaymarchFunction(torch.autograd.Function):
         g_rgba = g_rgba.contiguous().float()
         gd = torch.zeros_like(density)
         gt = torch.zeros_like(tangent)
-        gp = torch.zeros(2, dtype=torch.float64, device=density.device)
+        gp = torch.zeros(3, dtype=torch.float64, device=density.device)  # kd, exponent, exponent2
         s = torch.cuda.current_stream(density.device).cuda_stream
         fctx.native.raymarch_adjoint(fctx.params, density.data_ptr(), tangent.data_ptr(), tape.data_ptr(), fctx.K,
                                      g_rgba.data_ptr(), gd.data_ptr(), gt.data_ptr(), gp.data_ptr(), s)
-        return gd, gt, gp, None, None, None
+        return gd, gt, gp[:fctx.nparams], None, None, None
 
 
 class SplatFunction(torch.autograd.Function):

@@ -3,17 +3,17 @@
 // device code as vkhr_raymarch) and records a per-ray tape with checkpoints,
 // the hand-written adjoint of that raymarch with respect to an FP32 density
 // volume, an FP32 tangent field and the Kajiya-Kay parameters (kd and the
-// specular exponent), and a continuous trilinear-splat voxelizer of strand
-// vertices with its adjoint.
+// specular exponents of both lobes), and a continuous trilinear-splat
+// voxelizer of strand vertices with its adjoint.
 //
 // The model's discrete decisions (the isosurface point, the early exit, the
 // zero tests) are constants of the derivative; everything else is
 // differentiated exactly:
 //   coverage = lod * acc / iso * alpha, acc = sum of the primary samples;
-//   rgb = clamp(shading * occl_s * occl_a), with shading Kajiya-Kay of the
-//   normalised trilinear tangent at the surface point, occl_s =
-//   (1 - alpha)^(thickness * sum of the shadow samples) and occl_a =
-//   (1 - sum(min(rho, ao_max)) / k^3)^ao_exp;
+//   rgb = clamp(shading * occl_s * occl_a), with shading the (dual-lobe,
+//   shifted) Kajiya-Kay of the normalised trilinear tangent at the surface
+//   point, occl_s = (1 - alpha)^(thickness * sum of the shadow samples) and
+//   occl_a = (1 - sum(min(rho, ao_max)) / taps)^ao_exp;
 //   every sample is trilinear in its 8 texels.
 // The primary march is replayed from checkpoints of t stored every K
 // iterations: one thread per (ray, K-iteration segment).
@@ -82,10 +82,40 @@ __device__ __forceinline__ void scatter_tangent(const RayConsts& c, float4* __re
 
 __device__ __forceinline__ float clamp_grad(float x, float g) { return (x > 0.0f && x < 1.0f) ? g : 0.0f; }
 
+// kk_lobe and its partials with respect to a = T.L (da), b = T.E (db) and
+// the exponent (dp), through the shifted cosines of shift_cosines (c = L.E
+// is a constant of the derivative: L and E depend on the surface point only).
+__device__ __forceinline__ float kk_lobe_grad(float a, float b, float sa, float sb, float cab, float s, float p,
+                                              float& da, float& db, float& dp)
+{
+    float as = a, bs = b, sas = sa, sbs = sb, j00 = 1.0f, j01 = 0.0f, j11 = 1.0f;
+    if (s != 0.0f && sb > 0.0f) {
+        shift_cosines(a, b, sb, cab, s, as, bs);
+        const float k = 1.0f / sqrtf(fmaf(s, s, 1.0f));
+        j00 = j11 = k * (1.0f + s * b / sb);
+        j01 = k * s * (a / sb + (a * b - cab) * b / (sb * sb * sb));
+        sas = sqrtf(fmaxf(1.0f - as * as, 0.0f));
+        sbs = sqrtf(fmaxf(1.0f - bs * bs, 0.0f));
+    }
+    const float base = fmaxf(as * bs + sas * sbs, 0.0f);
+    const float spec = powf(base, p);
+    da = db = dp = 0.0f;
+    if (base > 0.0f) {
+        const float ds = p * powf(base, p - 1.0f);
+        float gas = bs, gbs = as; // d base / d a_s, d base / d b_s
+        if (sas > 0.0f) gas -= sbs * as / sas;
+        if (sbs > 0.0f) gbs -= sas * bs / sbs;
+        da = ds * gas * j00;
+        db = ds * (gas * j01 + gbs * j11);
+        dp = spec * logf(base);
+    }
+    return spec;
+}
+
 // Per pixel: the gradient of the pixel's accumulated density (g_acc, for
 // the segment replay below), and the shading, shadow and LAO parts of the
 // adjoint, which depend on the surface point only.  kd and the specular
-// exponent are reduced per warp into double accumulators.
+// exponents are reduced per warp into double accumulators.
 template <int DF, int TF>
 __global__ void __launch_bounds__(128) adjoint_pixel_kernel(const __grid_constant__ RayConsts c,
                                                             const float* __restrict__ dens,
@@ -97,7 +127,7 @@ __global__ void __launch_bounds__(128) adjoint_pixel_kernel(const __grid_constan
 {
     const uint32_t pixels = (uint32_t)c.W * (uint32_t)c.H;
     const uint32_t at = blockIdx.x * blockDim.x + threadIdx.x;
-    float gkd = 0.0f, gexp = 0.0f;
+    float gkd = 0.0f, gexp = 0.0f, gexp2 = 0.0f;
     if (at < pixels) {
         const PixelTape tp = tape[at];
         float ga = 0.0f;
@@ -112,7 +142,8 @@ __global__ void __launch_bounds__(128) adjoint_pixel_kernel(const __grid_constan
             // forward quantities at the surface point
             Vec3 shading = v3(1.0f, 1.0f, 1.0f);
             Vec3 L, E, T, Tr;
-            float cosTL = 0.0f, cosTE = 0.0f, sinTL = 0.0f, sinTE = 0.0f, base = 0.0f, spec = 0.0f;
+            float cosTL = 0.0f, cosTE = 0.0f, sinTL = 0.0f, sinTE = 0.0f, cosLE = 0.0f;
+            float da1 = 0.0f, db1 = 0.0f, dp1 = 0.0f, da2 = 0.0f, db2 = 0.0f, dp2 = 0.0f;
             const bool kk = c.shading_model == VKHR_SHADING_KAJIYA_KAY;
             if (kk) {
                 L = normalize(light - surf);
@@ -123,15 +154,21 @@ __global__ void __launch_bounds__(128) adjoint_pixel_kernel(const __grid_constan
                 cosTE = dot(T, E);
                 sinTL = sqrtf(fmaxf(1.0f - cosTL * cosTL, 0.0f));
                 sinTE = sqrtf(fmaxf(1.0f - cosTE * cosTE, 0.0f));
-                base = fmaxf(cosTL * cosTE + sinTL * sinTE, 0.0f);
-                spec = powf(base, c.exponent);
+                cosLE = dot(L, E);
+                const float spec = kk_lobe_grad(cosTL, cosTE, sinTL, sinTE, cosLE, c.shift[0], c.exponent, da1, db1, dp1);
                 const float dk = c.kd * sinTL;
                 shading = v3(c.color[0] * dk + c.intensity[0] * spec, c.color[1] * dk + c.intensity[1] * spec,
                              c.color[2] * dk + c.intensity[2] * spec);
+                if (c.exponent2 > 0.0f) {
+                    const float spec2 =
+                        kk_lobe_grad(cosTL, cosTE, sinTL, sinTE, cosLE, c.shift[1], c.exponent2, da2, db2, dp2);
+                    shading = shading + v3(c.intensity[0] * c.color[0] * spec2, c.intensity[1] * c.color[1] * spec2,
+                                           c.intensity[2] * c.color[2] * spec2);
+                }
             }
             const bool shadows = c.deep_shadows_on == 1 && c.shading_model != VKHR_SHADING_LAO;
             const bool lao = c.shading_model != VKHR_SHADING_ADSM;
-            const float k3 = c.ao_kernel * c.ao_kernel * c.ao_kernel;
+            const float k3 = c.ao_n > 0 ? (float)c.ao_n : c.ao_kernel * c.ao_kernel * c.ao_kernel; // taps
             const float ao_base = 1.0f - tp.dsum / k3;
             const float occl_a = lao ? powf(ao_base, c.ao_exp) : 1.0f;
             const float occl = (shadows ? tp.occl_s : 1.0f) * occl_a;
@@ -143,17 +180,17 @@ __global__ void __launch_bounds__(128) adjoint_pixel_kernel(const __grid_constan
             if (kk) {
                 const float gi = gsh.x * c.intensity[0] + gsh.y * c.intensity[1] + gsh.z * c.intensity[2];
                 const float gc = gsh.x * c.color[0] + gsh.y * c.color[1] + gsh.z * c.color[2];
+                const float gic = gsh.x * c.intensity[0] * c.color[0] + gsh.y * c.intensity[1] * c.color[1] +
+                                  gsh.z * c.intensity[2] * c.color[2];
                 gkd = gc * sinTL;
-                float dspec = 0.0f;
-                if (base > 0.0f) {
-                    gexp = gi * spec * logf(base);
-                    dspec = c.exponent * powf(base, c.exponent - 1.0f);
+                gexp = gi * dp1;
+                float gcosTL = gi * da1, gcosTE = gi * db1;
+                if (c.exponent2 > 0.0f) {
+                    gexp2 = gic * dp2;
+                    gcosTL += gic * da2;
+                    gcosTE += gic * db2;
                 }
-                const float gbase = gi * dspec;
-                const float gsinTL = gc * c.kd + gbase * sinTE, gsinTE = gbase * sinTL;
-                float gcosTL = gbase * cosTE, gcosTE = gbase * cosTL;
-                if (sinTL > 0.0f) gcosTL -= gsinTL * cosTL / sinTL;
-                if (sinTE > 0.0f) gcosTE -= gsinTE * cosTE / sinTE;
+                if (sinTL > 0.0f) gcosTL -= gc * c.kd * cosTL / sinTL; // the diffuse kd sin(T, L)
                 const Vec3 gT = L * gcosTL + E * gcosTE;
                 const float len = sqrtf(dot(Tr, Tr));
                 if (len > 0.0f) { // through T = Tr / |Tr|
@@ -168,28 +205,36 @@ __global__ void __launch_bounds__(128) adjoint_pixel_kernel(const __grid_constan
             }
             if (lao && gocc != 0.0f && ao_base > 0.0f) {
                 const float gd = -gocc * (shadows ? tp.occl_s : 1.0f) * c.ao_exp * powf(ao_base, c.ao_exp - 1.0f) / k3;
-                const float kr = (c.ao_kernel - 1.0f) / 2.0f;
-                const float scale = c.ao_radius / kr;
-                const Vec3 sc = v3(c.voxel_space[0] * scale, c.voxel_space[1] * scale, c.voxel_space[2] * scale);
-                for (float z = -kr; z <= kr; z += 1.0f)
-                    for (float y = -kr; y <= kr; y += 1.0f)
-                        for (float x = -kr; x <= kr; x += 1.0f) {
-                            const Vec3 q = v3(surf.x + x * sc.x, surf.y + y * sc.y, surf.z + z * sc.z);
-                            if (sample_density<DF>(c, dens, q) < c.ao_max) scatter_density(c, g_dens, q, gd);
-                        }
+                for (int i = 0; i < c.ao_n; ++i) { // the directional taps
+                    const Vec3 q = v3(surf.x + c.ao_off[i][0], surf.y + c.ao_off[i][1], surf.z + c.ao_off[i][2]);
+                    if (sample_density<DF>(c, dens, q) < c.ao_max) scatter_density(c, g_dens, q, gd);
+                }
+                if (c.ao_n == 0) { // the cube's taps
+                    const float kr = (c.ao_kernel - 1.0f) / 2.0f;
+                    const float scale = c.ao_radius / kr;
+                    const Vec3 sc = v3(c.voxel_space[0] * scale, c.voxel_space[1] * scale, c.voxel_space[2] * scale);
+                    for (float z = -kr; z <= kr; z += 1.0f)
+                        for (float y = -kr; y <= kr; y += 1.0f)
+                            for (float x = -kr; x <= kr; x += 1.0f) {
+                                const Vec3 q = v3(surf.x + x * sc.x, surf.y + y * sc.y, surf.z + z * sc.z);
+                                if (sample_density<DF>(c, dens, q) < c.ao_max) scatter_density(c, g_dens, q, gd);
+                            }
+                }
             }
         }
         g_acc[at] = ga;
     }
-    // kd and exponent: warp sums, one double atomic per warp
+    // kd and the exponents: warp sums, one double atomic per warp and parameter
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         gkd += __shfl_down_sync(0xffffffffu, gkd, o);
         gexp += __shfl_down_sync(0xffffffffu, gexp, o);
+        gexp2 += __shfl_down_sync(0xffffffffu, gexp2, o);
     }
-    if ((threadIdx.x & 31) == 0 && (gkd != 0.0f || gexp != 0.0f)) {
+    if ((threadIdx.x & 31) == 0 && (gkd != 0.0f || gexp != 0.0f || gexp2 != 0.0f)) {
         atomicAdd(g_par + 0, (double)gkd);
         atomicAdd(g_par + 1, (double)gexp);
+        atomicAdd(g_par + 2, (double)gexp2);
     }
 }
 

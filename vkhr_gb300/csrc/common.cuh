@@ -38,6 +38,15 @@ enum {
     WORD_COUNT = 24
 };
 
+// Visit total of an earlier unbudgeted one-style segment voxelization, by
+// the call's size (index count, grid, index mode, tangents requested).
+struct vkhr_learned_visits {
+    uint64_t items;
+    int32_t w, h, d, mode;
+    uint64_t visits;           // 0: empty slot
+};
+constexpr int kLearnedSizes = 16;
+
 struct vkhr_ctx {
     int device;
     int sm_count;
@@ -71,6 +80,9 @@ struct vkhr_ctx {
     void* h_jobs;              // pinned staging of the job table
     cudaEvent_t jobs_ev;       // recorded after the staging was copied out
     uint64_t visit_budget;     // segment mode: fixed visit capacity (0 = size from the counted total)
+    vkhr_learned_visits learned[kLearnedSizes]; // segment mode without a budget: earlier calls' visits
+    int learned_next;          // slot the next new size replaces
+    int live_graphs;           // frame graphs holding pointers into this context's scratch
     void* d_rjobs;             // raymarch: device job table of the current batch
     size_t rjobs_cap;          // in bytes
     void* h_rjobs;             // pinned staging of the raymarch job table
@@ -80,6 +92,9 @@ struct vkhr_ctx {
     size_t g_acc_cap;
     uint32_t* occ;             // raymarch brick-occupancy bitmap
     size_t occ_cap;            // in 32-bit words
+    cudaArray_t tex_array;     // raymarch, texture-unit variant: the density copied into a 3D array
+    cudaTextureObject_t tex_obj; // (LINEAR filter, border 0) and its texture object
+    int tex_res[3], tex_fmt;   // the array's extent and density format
     unsigned long long* d_words;
     unsigned long long* h_words; // pinned mirror
     cudaEvent_t ev;
@@ -98,7 +113,7 @@ struct vkhr_ctx {
 
 constexpr int kProfileMax = 4096;
 constexpr size_t kJobTableBytes = 64 * 1024;  // pinned staging of a voxelizer batch's job table
-constexpr size_t kRayTableBytes = 128 * 1024; // pinned staging of a raymarch batch's job table
+constexpr size_t kRayTableBytes = 256 * 1024; // pinned staging of a raymarch batch's job table
 
 void vkhr_prof_begin(vkhr_ctx* ctx, const char* name, cudaStream_t st);
 void vkhr_prof_end(vkhr_ctx* ctx, cudaStream_t st);
@@ -125,8 +140,14 @@ vkhr_status vkhr_fork_side(vkhr_ctx* ctx, cudaStream_t st);
 vkhr_status vkhr_join_side(vkhr_ctx* ctx, cudaStream_t st);
 vkhr_status vkhr_fail_cuda(vkhr_ctx* ctx, cudaError_t e, const char* what, const char* file, int line);
 
-// Grow-only device buffer; contents are not preserved on growth.
+// Grow-only device buffer; contents are not preserved on growth.  While a
+// frame graph of the context exists, a buffer that would have to grow is
+// refused (VKHR_ERR_CAPACITY): the graph holds its address.
 vkhr_status vkhr_reserve(vkhr_ctx* ctx, void** ptr, size_t* cap_elems, size_t need_elems, size_t elem_bytes);
+
+// One-style segment voxelization that reads its visit total back (into
+// *visits) whatever the context has learned; the context's budget is kept.
+vkhr_status vkhr_voxelize_counted(vkhr_ctx* ctx, const vkhr_voxel_job* job, void* stream, uint64_t* visits);
 
 static inline unsigned vkhr_blocks(size_t n, unsigned threads)
 {

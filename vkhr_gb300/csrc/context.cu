@@ -23,6 +23,9 @@ vkhr_status vkhr_fail_cuda(vkhr_ctx* ctx, cudaError_t e, const char* what, const
 vkhr_status vkhr_reserve(vkhr_ctx* ctx, void** ptr, size_t* cap_elems, size_t need_elems, size_t elem_bytes)
 {
     if (need_elems <= *cap_elems && *ptr) return VKHR_OK;
+    if (*ptr && ctx->live_graphs > 0)
+        return vkhr_fail(ctx, VKHR_ERR_CAPACITY,
+                         "scratch would have to grow while a frame graph holds it: destroy the graph first");
     size_t grow = need_elems + need_elems / 8 + 1024; // headroom against creeping sizes
     if (*ptr) {
         // the old buffer may still be read by work queued on any stream
@@ -160,6 +163,8 @@ vkhr_status vkhr_destroy(vkhr_ctx* ctx)
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (ctx->occ) cudaFree(ctx->occ);
+    if (ctx->tex_obj) cudaDestroyTextureObject(ctx->tex_obj);
+    if (ctx->tex_array) cudaFreeArray(ctx->tex_array);
     if (ctx->d_words) cudaFree(ctx->d_words);
     if (ctx->h_words) cudaFreeHost(ctx->h_words);
     if (ctx->ev) cudaEventDestroy(ctx->ev);

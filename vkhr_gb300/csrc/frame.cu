@@ -64,14 +64,9 @@ vkhr_status vkhr_frame_graph_create(vkhr_ctx* ctx, int32_t segments, const vkhr_
     if (segments) { // a capacity for every frame: no visit total is read back inside the graph
         uint64_t budget = visit_budget;
         if (!budget) { // count this frame's visits once
-            const uint64_t keep = ctx->visit_budget;
-            ctx->visit_budget = 0;
-            s = vkhr_voxelize_batched(ctx, 1, job, 1, stream);
-            if (s != VKHR_OK) {
-                ctx->visit_budget = keep;
-                return s;
-            }
-            const uint64_t v = ctx->h_words[WORD_TOTAL_VISITS];
+            uint64_t v = 0;
+            s = vkhr_voxelize_counted(ctx, job, stream, &v);
+            if (s != VKHR_OK) return s;
             budget = v + v / 4 + 4096;
         }
         s = vkhr_set_visit_budget(ctx, budget);
@@ -114,6 +109,7 @@ vkhr_status vkhr_frame_graph_create(vkhr_ctx* ctx, int32_t segments, const vkhr_
         cudaGraphDestroy(graph);
         return vkhr_fail(ctx, VKHR_ERR_OOM, "frame graph");
     }
+    ++ctx->live_graphs; // the context's scratch may no longer move
     *out = fg;
     return VKHR_OK;
 }
@@ -130,6 +126,7 @@ vkhr_status vkhr_frame_graph_destroy(vkhr_frame_graph* fg)
 {
     if (!fg) return VKHR_OK;
     cudaSetDevice(fg->device);
+    if (fg->ctx && fg->ctx->live_graphs > 0) --fg->ctx->live_graphs;
     if (fg->exec) cudaGraphExecDestroy(fg->exec);
     if (fg->graph) cudaGraphDestroy(fg->graph);
     delete fg;

@@ -14,10 +14,14 @@ namespace {
 constexpr int kTileW = 8, kTileH = 4;         // pixels per warp
 constexpr int kWarpsX = 2, kWarpsY = 2;       // warps per block
 constexpr float kMaxSteps = 1048576.0f;       // 2^20: t += 1/steps still advances below 1
+constexpr int kMaxAoDirections = 32;          // directional AO taps (vkhr_raymarch_params::ao_directions)
 
 struct RayConsts {
     int W, H;
-    float inv_vp[16];
+    float ray_dir[3][3][2];   // ray direction of pixel (px, py), up to a positive scale, as an unevaluated
+                              // sum hi + lo per coefficient: component k = [k][0] + [k][1] px + [k][2] py
+    float ray_w[3];           // homogeneous w of the unprojected far-plane point: w0 + wx px + wy py (its sign
+                              // orients the direction)
     float pv[16];
     float cam[3];
     float radius;
@@ -32,7 +36,17 @@ struct RayConsts {
     int shading_model, deep_shadows_on;
     int steps_pow2, shadow_pow2;  // 1/steps is exact and t = i * step: empty space may be jumped
     int nb[3];                    // occupancy bricks per axis, (res + 8) / 8
+    float exponent2;              // second specular lobe's exponent (0: one lobe)
+    float shift[2];               // tangent shift of each lobe (0: the reference's unshifted lobe)
+    int ao_n;                     // directional AO taps (0: the ao_kernel^3 cube)
+    float ao_off[kMaxAoDirections][3]; // world-space offsets of the directional taps
+    unsigned long long tex;       // the density as a 3D texture object (texture-unit variant only; else 0)
 };
+
+// Where the march's density samples come from: the texels in memory with the
+// software trilinear below (every variant but one), or the texture unit's
+// hardware trilinear filter, whose weights have 8 fractional bits.
+constexpr int kSampleMemory = 0, kSampleTexture = 1;
 
 constexpr int kBrick = 8;          // occupancy brick edge in texel cells
 constexpr float kSkipMargin = 0.01f; // texels kept between a predicted sample and a brick face
@@ -136,6 +150,18 @@ __device__ __forceinline__ float sample_density(const RayConsts& c, const typena
     const float y0 = fmaf(a[1], x10 - x00, x00);
     const float y1 = fmaf(a[1], x11 - x01, x01);
     return fmaf(a[2], y1 - y0, y0) * TX::scale;
+}
+
+template <int DF, int SRC>
+__device__ __forceinline__ float density_at(const RayConsts& c, const typename DensityTexel<DF>::T* __restrict__ d,
+                                            Vec3 p)
+{
+    if (SRC == kSampleTexture) { // texel centres at integer + 0.5 in the texture's unnormalised coordinates
+        const float u = fmaf(p.x, c.tsc[0], c.tbias[0]), v = fmaf(p.y, c.tsc[1], c.tbias[1]),
+                    w = fmaf(p.z, c.tsc[2], c.tbias[2]);
+        return tex3D<float>((cudaTextureObject_t)c.tex, u + 0.5f, v + 0.5f, w + 0.5f);
+    }
+    return sample_density<DF>(c, d, p);
 }
 
 template <int TF>
@@ -304,6 +330,15 @@ static inline unsigned occupancy_blocks(int nx, int ny, int nz, int sm_count, in
     return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((lanes + 127) / 128, (uint64_t)sm_count * 16));
 }
 
+// The occupancy brick of a sample's texel cell (cell = floor(u) + 1 per axis,
+// in [0, N]; classify's index), for a sample inside the cell grid.
+__device__ __forceinline__ uint32_t cell_brick(const RayConsts& c, const float u[3])
+{
+    const int bxk = ((int)floorf(u[0]) + 1) / kBrick, byk = ((int)floorf(u[1]) + 1) / kBrick,
+              bzk = ((int)floorf(u[2]) + 1) / kBrick;
+    return (uint32_t)bxk + (uint32_t)c.nb[0] * ((uint32_t)byk + (uint32_t)c.nb[1] * (uint32_t)bzk);
+}
+
 // Classifies one sample position (texel coordinates u).  Returns 1 when the
 // sample is exactly zero (border, or an empty brick), 2 when it is zero and
 // the ray has left the grid for good (moving away along every such axis),
@@ -378,6 +413,36 @@ __device__ __forceinline__ void texel_coords(const RayConsts& c, Vec3 p, float u
     u[2] = fmaf(p.z, c.tsc[2], c.tbias[2]);
 }
 
+// Tangent of a Kajiya-Kay lobe shifted by s towards the camera,
+// normalize(T + s N) with N the unit component of -E perpendicular to T,
+// as its cosines with L and E: with a = T.L, b = T.E, c = L.E, sb = sin(T, E)
+// and k = 1 / sqrt(1 + s^2),
+//   a_s = k (a + s (a b - c) / sb),   b_s = k (b - s sb)
+// (T itself where N is undefined, sb = 0).  s = 0 leaves a and b unchanged.
+__device__ __forceinline__ void shift_cosines(float a, float b, float sb, float cab, float s, float& as, float& bs)
+{
+    as = a;
+    bs = b;
+    if (s != 0.0f && sb > 0.0f) {
+        const float k = 1.0f / sqrtf(fmaf(s, s, 1.0f));
+        as = k * (a + s * (a * b - cab) / sb);
+        bs = k * (b - s * sb);
+    }
+}
+
+// One Kajiya-Kay specular lobe (kajiya-kay.glsl:15-21) of the tangent
+// shifted by s: max(cos(T_s,L) cos(T_s,E) + sin(T_s,L) sin(T_s,E), 0)^p.  For
+// s = 0 it is the reference's expression of the unshifted cosines and sines.
+__device__ __forceinline__ float kk_lobe(float cosTL, float cosTE, float sinTL, float sinTE, float cosLE, float s,
+                                         float p)
+{
+    if (s == 0.0f) return powf(fmaxf(cosTL * cosTE + sinTL * sinTE, 0.0f), p);
+    float a, b;
+    shift_cosines(cosTL, cosTE, sinTE, cosLE, s, a, b);
+    const float sa = sqrtf(fmaxf(1.0f - a * a, 0.0f)), sb = sqrtf(fmaxf(1.0f - b * b, 0.0f));
+    return powf(fmaxf(a * b + sa * sb, 0.0f), p);
+}
+
 // What the differentiable path keeps of a pixel's forward march (32 bytes).
 struct PixelTape {
     float surf[3];   // surface point
@@ -389,17 +454,73 @@ struct PixelTape {
 };
 constexpr uint32_t kTapeEmitted = 1u, kTapeHit = 2u;
 
+// Double-float arithmetic: a value as an unevaluated sum hi + lo of two
+// floats (|lo| <= ulp(hi) / 2), with error-free FMA products and two-sums
+// (T. J. Dekker, "A floating-point technique for extending the available
+// precision", 1971; the FMA form of the product).  The intrinsics keep the
+// compiler from contracting the steps whose rounding errors they capture.
+struct DF {
+    float hi, lo;
+};
+__device__ __forceinline__ DF df_fast_sum(float a, float b) // |a| >= |b|
+{
+    const float s = __fadd_rn(a, b);
+    return DF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ DF df_two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+    return DF{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ DF df_add(DF x, DF y)
+{
+    const DF s = df_two_sum(x.hi, y.hi);
+    return df_fast_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo)));
+}
+__device__ __forceinline__ DF df_mul_f(DF x, float f)
+{
+    const float p = __fmul_rn(x.hi, f);
+    return df_fast_sum(p, __fmaf_rn(x.lo, f, __fmaf_rn(x.hi, f, -p)));
+}
+__device__ __forceinline__ DF df_mul(DF x, DF y)
+{
+    const float p = __fmul_rn(x.hi, y.hi);
+    return df_fast_sum(p, __fmaf_rn(x.hi, y.lo, __fmaf_rn(x.lo, y.hi, __fmaf_rn(x.hi, y.hi, -p))));
+}
+__device__ __forceinline__ DF df_div(DF n, DF d)
+{
+    const float q1 = __fdiv_rn(n.hi, d.hi);
+    const DF r = df_add(n, df_mul_f(d, -q1)); // n - q1 d
+    return df_fast_sum(q1, __fdiv_rn(r.hi, d.hi));
+}
+
 // Entry of the pixel-centre ray into the volume's AABB (the front faces of
 // the proxy cube, volume.vert:17-25), and the march's end point
-// start + normalize(start - camera) * radius (volume.frag:32-34).
+// start + normalize(start - camera) * radius (volume.frag:32-34).  The ray
+// points from the camera at the pixel's far-plane point, inverse(P V)
+// (nx, ny, 1, 1) dehomogenised.  That point's w is about 1/far, the
+// difference of nearly equal terms, so the direction is taken as
+// num - camera * w (num the xyz of the unprojection): the same ray up to the
+// positive factor w, affine in the pixel's integer coordinates, with
+// coefficients folded in double on the host and kept as float pairs.  The
+// direction and the entry on the hit face are evaluated in double-float:
+// for a camera tens of units away, FP32 alone would place the entry a few
+// 1e-5 texel off, enough to flip the shader's isosurface and zero tests.
 __device__ __forceinline__ bool ray_entry(const RayConsts& c, int px, int py, Vec3& start, Vec3& end)
 {
-    const float nx = 2.0f * ((float)px + 0.5f) / (float)c.W - 1.0f;
-    const float ny = 2.0f * ((float)py + 0.5f) / (float)c.H - 1.0f;
-    float f[4];
+    const float fx = (float)px, fy = (float)py; // exact
+    const float w = fmaf(c.ray_w[1], fx, fmaf(c.ray_w[2], fy, c.ray_w[0]));
+    DF D[3];
+    float dir[3];
 #pragma unroll
-    for (int r = 0; r < 4; ++r) f[r] = c.inv_vp[r] * nx + c.inv_vp[4 + r] * ny + c.inv_vp[8 + r] + c.inv_vp[12 + r];
-    const float dir[3] = {f[0] / f[3] - c.cam[0], f[1] / f[3] - c.cam[1], f[2] / f[3] - c.cam[2]};
+    for (int k = 0; k < 3; ++k) {
+        const DF a = DF{c.ray_dir[k][0][0], c.ray_dir[k][0][1]};
+        const DF b = df_mul_f(DF{c.ray_dir[k][1][0], c.ray_dir[k][1][1]}, fx);
+        const DF e = df_mul_f(DF{c.ray_dir[k][2][0], c.ray_dir[k][2][1]}, fy);
+        D[k] = df_add(df_add(a, b), e);
+        if (w < 0.0f) D[k] = DF{-D[k].hi, -D[k].lo}; // a far-plane point behind the camera flips the ray
+        dir[k] = D[k].hi;
+    }
     float tmin = -INFINITY, tmax = INFINITY;
     bool hit = true;
 #pragma unroll
@@ -413,17 +534,135 @@ __device__ __forceinline__ bool ray_entry(const RayConsts& c, int px, int py, Ve
         tmax = fminf(tmax, fmaxf(t0, t1));
     }
     if (!(hit && tmin > 0.0f && tmin <= tmax)) return false;
+    // the entry on the face of the axis whose slab is entered last, in double-float
+    int ke = 0;
+    float best = -INFINITY;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        if (dir[k] == 0.0f) continue;
+        const float near = fminf((c.lo[k] - c.cam[k]) / dir[k], (c.hi[k] - c.cam[k]) / dir[k]);
+        if (near > best) {
+            best = near;
+            ke = k;
+        }
+    }
+    const float face = dir[ke] > 0.0f ? c.lo[ke] : c.hi[ke];
+    const DF t = df_div(df_two_sum(face, -c.cam[ke]), D[ke]);
+    float p[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const DF q = df_add(df_mul(t, D[k]), DF{c.cam[k], 0.0f});
+        p[k] = k == ke ? face : __fadd_rn(q.hi, q.lo);
+    }
     const Vec3 cam = v3(c.cam[0], c.cam[1], c.cam[2]);
-    start = v3(fmaf(tmin, dir[0], c.cam[0]), fmaf(tmin, dir[1], c.cam[1]), fmaf(tmin, dir[2], c.cam[2]));
+    start = v3(p[0], p[1], p[2]);
     end = start + normalize(start - cam) * c.radius;
     return true;
+}
+
+// The fragment of a ray whose primary march ended with accumulated density
+// acc and surface point surf (volume.frag:45-103): shading, density shadows,
+// ambient occlusion, coverage and depth.  Leaves out / out_depth (background)
+// alone when acc is 0 (the shader's discard).
+template <int DF, int TF, bool TAPE = false, int SRC = kSampleMemory>
+__device__ __forceinline__ void shade_fragment(const RayConsts& c, const typename DensityTexel<DF>::T* __restrict__ dens,
+                                               const void* __restrict__ tang, const uint32_t* __restrict__ occ,
+                                               Vec3 surf, float acc, float4& out, float& out_depth,
+                                               PixelTape* tape = nullptr)
+{
+    const Vec3 cam = v3(c.cam[0], c.cam[1], c.cam[2]);
+    const float a = acc / c.iso;
+    if (a != 0.0f) {
+        if (TAPE) tape->flags |= kTapeEmitted;
+        const float coverage = c.lod * a * c.alpha;
+        // ---- shading (volume.frag:50-67, kajiya-kay.glsl:7-24) ------------
+        Vec3 shading = v3(1.0f, 1.0f, 1.0f);
+        const Vec3 light = v3(c.light[0], c.light[1], c.light[2]);
+        if (c.shading_model == VKHR_SHADING_KAJIYA_KAY) {
+            const Vec3 L = normalize(light - surf);
+            const Vec3 E = normalize(surf - cam);
+            const Vec3 T = normalize(sample_tangent<TF>(c, tang, surf));
+            const float cosTL = dot(T, L), cosTE = dot(T, E);
+            const float sinTL = sqrtf(fmaxf(1.0f - cosTL * cosTL, 0.0f));
+            const float sinTE = sqrtf(fmaxf(1.0f - cosTE * cosTE, 0.0f));
+            const float cosLE = c.shift[0] != 0.0f || c.exponent2 > 0.0f ? dot(L, E) : 0.0f;
+            const float spec = kk_lobe(cosTL, cosTE, sinTL, sinTE, cosLE, c.shift[0], c.exponent);
+            const float dk = c.kd * sinTL;
+            shading = v3(c.color[0] * dk + c.intensity[0] * spec, c.color[1] * dk + c.intensity[1] * spec,
+                         c.color[2] * dk + c.intensity[2] * spec);
+            if (c.exponent2 > 0.0f) { // the second, hair-coloured lobe
+                const float spec2 = kk_lobe(cosTL, cosTE, sinTL, sinTE, cosLE, c.shift[1], c.exponent2);
+                shading = shading + v3(c.intensity[0] * c.color[0] * spec2, c.intensity[1] * c.color[1] * spec2,
+                                       c.intensity[2] * c.color[2] * spec2);
+            }
+        }
+        float occlusion = 1.0f;
+        // ---- volume_approximated_deep_shadows (approximate_deep_shadows.glsl:24-36)
+        if (c.deep_shadows_on == 1 && c.shading_model != VKHR_SHADING_LAO) {
+            const float sstep = 1.0f / c.shadow_steps;
+            float ls[3], le[3], dl[3];
+            texel_coords(c, surf, ls);
+            texel_coords(c, light, le);
+            dl[0] = le[0] - ls[0];
+            dl[1] = le[1] - ls[1];
+            dl[2] = le[2] - ls[2];
+            float inv_dl[3];
+            reciprocals(dl, inv_dl);
+            float strands = 0.0f;
+            for (float t = 0.0f; t < 1.0f;) {
+                const Vec3 Q = mix(surf, light, t);
+                float u[3], lo[3], hi[3];
+                texel_coords(c, Q, u);
+                const int z = classify(c, occ, u, inv_dl, lo, hi);
+                if (z == 2) break;
+                if (z == 1) {
+                    const float n = c.shadow_pow2 ? steps_inside(u, inv_dl, lo, hi, c.shadow_steps) : 0.0f;
+                    t = n >= 1.0f ? fmaf(n, sstep, t) : t + sstep;
+                    continue;
+                }
+                strands += density_at<DF, SRC>(c, dens, Q) * c.thickness;
+                t += sstep;
+            }
+            const float os = powf(1.0f - c.alpha, strands);
+            if (TAPE) tape->occl_s = os;
+            occlusion *= os;
+        }
+        // ---- local_ambient_occlusion (local_ambient_occlusion.glsl:9-30)
+        if (c.shading_model != VKHR_SHADING_ADSM) {
+            float dsum = 0.0f, taps;
+            if (c.ao_n > 0) { // the directional extension
+                for (int i = 0; i < c.ao_n; ++i) {
+                    const Vec3 q = v3(surf.x + c.ao_off[i][0], surf.y + c.ao_off[i][1], surf.z + c.ao_off[i][2]);
+                    dsum += fminf(density_at<DF, SRC>(c, dens, q), c.ao_max);
+                }
+                taps = (float)c.ao_n;
+            } else {
+                const float kr = (c.ao_kernel - 1.0f) / 2.0f;
+                const float scale = c.ao_radius / kr;
+                const Vec3 sc = v3(c.voxel_space[0] * scale, c.voxel_space[1] * scale, c.voxel_space[2] * scale);
+                for (float z = -kr; z <= kr; z += 1.0f)
+                    for (float y = -kr; y <= kr; y += 1.0f)
+                        for (float x = -kr; x <= kr; x += 1.0f) {
+                            const Vec3 q = v3(surf.x + x * sc.x, surf.y + y * sc.y, surf.z + z * sc.z);
+                            dsum += fminf(density_at<DF, SRC>(c, dens, q), c.ao_max);
+                        }
+                taps = c.ao_kernel * c.ao_kernel * c.ao_kernel;
+            }
+            if (TAPE) tape->dsum = dsum;
+            occlusion *= powf(1.0f - dsum / taps, c.ao_exp);
+        }
+        // packUnorm4x8 clamp (ppll.glsl:32); NaN -> 0
+        out = make_float4(__saturatef(shading.x * occlusion), __saturatef(shading.y * occlusion),
+                          __saturatef(shading.z * occlusion), __saturatef(coverage));
+        out_depth = clip_depth(c, surf);
+    }
 }
 
 // The fragment of pixel (px, py) of the c.W x c.H view: colour + coverage
 // and depth.  depth_at points at the pixel's depth-buffer value (NULL: 1.0).
 // TAPE = true also records the pixel's PixelTape and the march's t every K
 // iterations into ckpt[0, nckpt) (the checkpoints the adjoint replays from).
-template <int DF, int TF, bool TAPE = false>
+template <int DF, int TF, bool TAPE = false, int SRC = kSampleMemory>
 __device__ __forceinline__ void march_pixel(const RayConsts& c, const typename DensityTexel<DF>::T* __restrict__ dens,
                                             const void* __restrict__ tang, const uint32_t* __restrict__ occ,
                                             const float* depth_at, int px, int py, float4& out, float& out_depth,
@@ -442,7 +681,6 @@ __device__ __forceinline__ void march_pixel(const RayConsts& c, const typename D
     }
     Vec3 start, end;
     if (ray_entry(c, px, py, start, end)) {
-        const Vec3 cam = v3(c.cam[0], c.cam[1], c.cam[2]);
         const float db = depth_at ? *depth_at : 1.0f;
         const bool depth_test = !(clip_depth(c, end) < db);
 
@@ -475,7 +713,7 @@ __device__ __forceinline__ void march_pixel(const RayConsts& c, const typename D
                 if (TAPE) k += n >= 1.0f ? (uint32_t)n : 1u;
                 continue;
             }
-            const float rho = sample_density<DF>(c, dens, P);
+            const float rho = density_at<DF, SRC>(c, dens, P);
             acc += rho;
             if (rho != 0.0f) {
                 if (acc <= c.iso) surf = P;
@@ -500,76 +738,7 @@ __device__ __forceinline__ void march_pixel(const RayConsts& c, const typename D
             tape->n = k;
             tape->flags = kTapeHit;
         }
-        const float a = acc / c.iso;
-        if (a != 0.0f) {
-            if (TAPE) tape->flags |= kTapeEmitted;
-            const float coverage = c.lod * a * c.alpha;
-            // ---- shading (volume.frag:50-67, kajiya-kay.glsl:7-24) ------------
-            Vec3 shading = v3(1.0f, 1.0f, 1.0f);
-            const Vec3 light = v3(c.light[0], c.light[1], c.light[2]);
-            if (c.shading_model == VKHR_SHADING_KAJIYA_KAY) {
-                const Vec3 L = normalize(light - surf);
-                const Vec3 E = normalize(surf - cam);
-                const Vec3 T = normalize(sample_tangent<TF>(c, tang, surf));
-                const float cosTL = dot(T, L), cosTE = dot(T, E);
-                const float sinTL = sqrtf(fmaxf(1.0f - cosTL * cosTL, 0.0f));
-                const float sinTE = sqrtf(fmaxf(1.0f - cosTE * cosTE, 0.0f));
-                const float spec = powf(fmaxf(cosTL * cosTE + sinTL * sinTE, 0.0f), c.exponent);
-                const float dk = c.kd * sinTL;
-                shading = v3(c.color[0] * dk + c.intensity[0] * spec, c.color[1] * dk + c.intensity[1] * spec,
-                             c.color[2] * dk + c.intensity[2] * spec);
-            }
-            float occlusion = 1.0f;
-            // ---- volume_approximated_deep_shadows (approximate_deep_shadows.glsl:24-36)
-            if (c.deep_shadows_on == 1 && c.shading_model != VKHR_SHADING_LAO) {
-                const float sstep = 1.0f / c.shadow_steps;
-                float ls[3], le[3], dl[3];
-                texel_coords(c, surf, ls);
-                texel_coords(c, light, le);
-                dl[0] = le[0] - ls[0];
-                dl[1] = le[1] - ls[1];
-                dl[2] = le[2] - ls[2];
-                float inv_dl[3];
-                reciprocals(dl, inv_dl);
-                float strands = 0.0f;
-                for (float t = 0.0f; t < 1.0f;) {
-                    const Vec3 Q = mix(surf, light, t);
-                    float u[3], lo[3], hi[3];
-                    texel_coords(c, Q, u);
-                    const int z = classify(c, occ, u, inv_dl, lo, hi);
-                    if (z == 2) break;
-                    if (z == 1) {
-                        const float n = c.shadow_pow2 ? steps_inside(u, inv_dl, lo, hi, c.shadow_steps) : 0.0f;
-                        t = n >= 1.0f ? fmaf(n, sstep, t) : t + sstep;
-                        continue;
-                    }
-                    strands += sample_density<DF>(c, dens, Q) * c.thickness;
-                    t += sstep;
-                }
-                const float os = powf(1.0f - c.alpha, strands);
-                if (TAPE) tape->occl_s = os;
-                occlusion *= os;
-            }
-            // ---- local_ambient_occlusion (local_ambient_occlusion.glsl:9-30)
-            if (c.shading_model != VKHR_SHADING_ADSM) {
-                const float kr = (c.ao_kernel - 1.0f) / 2.0f;
-                const float scale = c.ao_radius / kr;
-                const Vec3 sc = v3(c.voxel_space[0] * scale, c.voxel_space[1] * scale, c.voxel_space[2] * scale);
-                float dsum = 0.0f;
-                for (float z = -kr; z <= kr; z += 1.0f)
-                    for (float y = -kr; y <= kr; y += 1.0f)
-                        for (float x = -kr; x <= kr; x += 1.0f) {
-                            const Vec3 q = v3(surf.x + x * sc.x, surf.y + y * sc.y, surf.z + z * sc.z);
-                            dsum += fminf(sample_density<DF>(c, dens, q), c.ao_max);
-                        }
-                if (TAPE) tape->dsum = dsum;
-                occlusion *= powf(1.0f - dsum / (c.ao_kernel * c.ao_kernel * c.ao_kernel), c.ao_exp);
-            }
-            // packUnorm4x8 clamp (ppll.glsl:32); NaN -> 0
-            out = make_float4(__saturatef(shading.x * occlusion), __saturatef(shading.y * occlusion),
-                              __saturatef(shading.z * occlusion), __saturatef(coverage));
-            out_depth = clip_depth(c, surf);
-        }
+        shade_fragment<DF, TF, TAPE, SRC>(c, dens, tang, occ, surf, acc, out, out_depth, tape);
     }
 }
 
@@ -608,8 +777,12 @@ inline vkhr_status make_consts(vkhr_ctx* ctx, const vkhr_raymarch_params* p, Ray
         return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "raycast_steps must be in (0, 2^20]");
     const float sst = p->shadow_steps > 0.0f ? p->shadow_steps : p->raycast_steps;
     if (!(sst <= kMaxSteps)) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "shadow_steps must be <= 2^20");
-    if (!(p->ao_kernel_size >= 2.0f && p->ao_kernel_size <= 16.0f))
+    if (p->ao_directions < 0 || p->ao_directions > kMaxAoDirections)
+        return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "ao_directions must be in [0, 32]");
+    if (p->ao_directions == 0 && !(p->ao_kernel_size >= 2.0f && p->ao_kernel_size <= 16.0f))
         return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "ao_kernel_size must be in [2, 16]");
+    if (!std::isfinite(p->spec_exponent2) || !std::isfinite(p->spec_shift[0]) || !std::isfinite(p->spec_shift[1]))
+        return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "spec_exponent2 and spec_shift must be finite");
     if (!(p->isosurface > 0.0f)) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "isosurface must be > 0");
     if (p->density_format < 0 || p->density_format > 2 || p->tangent_format < 0 || p->tangent_format > 1)
         return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "unknown texel format");
@@ -628,9 +801,31 @@ inline vkhr_status make_consts(vkhr_ctx* ctx, const vkhr_raymarch_params* p, Ray
             pv[col * 4 + r] = s;
         }
     if (!invert4(pv, inv)) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "projection * view is singular");
-    for (int i = 0; i < 16; ++i) {
-        c.pv[i] = (float)pv[i];
-        c.inv_vp[i] = (float)inv[i];
+    for (int i = 0; i < 16; ++i) c.pv[i] = (float)pv[i];
+    // rays: inverse(P V) (nx, ny, 1, 1) = (num, w), affine in (nx, ny), with
+    // nx = 2 (px + 0.5) / W - 1 (likewise ny); the direction num - camera * w
+    // (inv is column-major: inv[col * 4 + row]), in the pixel basis, each
+    // coefficient split into float hi + lo
+    {
+        const double sx = 2.0 / (double)p->width, ox = 1.0 / (double)p->width - 1.0;
+        const double sy = 2.0 / (double)p->height, oy = 1.0 / (double)p->height - 1.0;
+        auto split = [](double v, float out[2]) {
+            out[0] = (float)v;
+            out[1] = (float)(v - (double)out[0]);
+        };
+        for (int k = 0; k < 3; ++k) {
+            const double cam = (double)p->camera_position[k];
+            const double an = inv[0 * 4 + k] - cam * inv[0 * 4 + 3];                            // d/dnx
+            const double am = inv[1 * 4 + k] - cam * inv[1 * 4 + 3];                            // d/dny
+            const double a0 = inv[2 * 4 + k] + inv[3 * 4 + k] - cam * (inv[2 * 4 + 3] + inv[3 * 4 + 3]);
+            split(a0 + an * ox + am * oy, c.ray_dir[k][0]);
+            split(an * sx, c.ray_dir[k][1]);
+            split(am * sy, c.ray_dir[k][2]);
+        }
+        const double wn = inv[0 * 4 + 3], wm = inv[1 * 4 + 3], w0 = inv[2 * 4 + 3] + inv[3 * 4 + 3];
+        c.ray_w[0] = (float)(w0 + wn * ox + wm * oy);
+        c.ray_w[1] = (float)(wn * sx);
+        c.ray_w[2] = (float)(wm * sy);
     }
     for (int k = 0; k < 3; ++k) {
         c.cam[k] = p->camera_position[k];
@@ -674,6 +869,24 @@ inline vkhr_status make_consts(vkhr_ctx* ctx, const vkhr_raymarch_params* p, Ray
     c.steps_pow2 = pow2(c.steps) ? 1 : 0;
     c.shadow_pow2 = pow2(c.shadow_steps) ? 1 : 0;
     for (int k = 0; k < 3; ++k) c.nb[k] = (c.res[k] + kBrick) / kBrick;
+    c.tex = 0;
+    c.exponent2 = p->spec_exponent2 > 0.0f ? p->spec_exponent2 : 0.0f;
+    c.shift[0] = p->spec_shift[0];
+    c.shift[1] = p->spec_shift[1];
+    // directional AO: Fibonacci-sphere directions (y polar) at the reach of
+    // the reference's 8-tap cube, radius * sqrt(3) voxels, in world units
+    c.ao_n = p->ao_directions;
+    const double pi = 3.14159265358979323846;
+    for (int i = 0; i < kMaxAoDirections; ++i)
+        for (int k = 0; k < 3; ++k) c.ao_off[i][k] = 0.0f;
+    for (int i = 0; i < c.ao_n; ++i) {
+        const double y = 1.0 - (2.0 * i + 1.0) / (double)c.ao_n, r = std::sqrt(1.0 - y * y);
+        const double phi = (double)i * pi * (3.0 - std::sqrt(5.0));
+        const double d[3] = {r * std::cos(phi), y, r * std::sin(phi)};
+        const double reach = (double)p->occlusion_radius * std::sqrt(3.0);
+        for (int k = 0; k < 3; ++k)
+            c.ao_off[i][k] = (float)(d[k] * reach * (double)p->volume_bounds.size[k] / (double)p->volume_resolution[k]);
+    }
     return VKHR_OK;
 }
 

@@ -17,6 +17,8 @@
 //     texel centres, CLAMP_TO_BORDER reading 0.
 #include "march.cuh"
 
+#include <cuda.h> // CUtensorMap and its enums (the encoder is looked up in the driver at run time)
+
 #include <mutex>
 
 namespace {
@@ -29,9 +31,14 @@ namespace {
 struct RayVariant {
     int tw, minb;
 };
-constexpr RayVariant kRayVariants[VKHR_RAYMARCH_VARIANTS] = {{8, 6}, {16, 6}, {4, 6}, {8, 8}};
+constexpr int kPacketVariants = 4;   // raymarch_kernel instantiations; variant 4 is the staged kernel
+constexpr int kStagedVariant = 4;
+constexpr int kTextureVariant = 5;   // the texture unit's filter: other pixels, never autotuned
+constexpr int kTunedVariants = 5;    // the variants that compute the same pixels
+static_assert(VKHR_RAYMARCH_VARIANTS == kTextureVariant + 1, "variant table");
+constexpr RayVariant kRayVariants[kPacketVariants] = {{8, 6}, {16, 6}, {4, 6}, {8, 8}};
 
-template <int DF, int TF, int TW = 8, int MINB = 6>
+template <int DF, int TF, int TW = 8, int MINB = 6, int SRC = kSampleMemory>
 __global__ void __launch_bounds__(32 * kWarpsX * kWarpsY, MINB)
 raymarch_kernel(const __grid_constant__ RayConsts c, const typename DensityTexel<DF>::T* __restrict__ dens,
                 const void* __restrict__ tang, const uint32_t* __restrict__ occ, const float* __restrict__ depth_in,
@@ -47,6 +54,237 @@ raymarch_kernel(const __grid_constant__ RayConsts c, const typename DensityTexel
     float4 out;
     float out_depth;
     march_pixel<DF, TF>(c, dens, tang, occ, depth_in ? depth_in + at : nullptr, px, py, out, out_depth);
+    rgba[at] = out;
+    if (depth_out) depth_out[at] = out_depth;
+}
+
+// ---- TMA-staged primary march ----------------------------------------------------
+// raymarch_kernel with the primary march's density texels read from shared
+// memory.  Each warp marches its 8x4 rays in rounds: every live ray advances
+// through the samples that need no texel (exactly zero in an empty brick,
+// jumped as in march_pixel) to its next sample in an occupied brick; the warp
+// takes the brick the first such ray needs, one lane loads the brick's texels
+// -- cells [8b, 8b + 8) reach texels [8b - 1, 8b + 7] per axis -- with one
+// cp.async.bulk.tensor.3d into the warp's slot (the tensor map's zero fill
+// outside the grid is the sampler's border 0), and every ray whose sample lies
+// in that brick takes its samples from the slot until it leaves the brick.
+// The samples, their order and their arithmetic are march_pixel's, so the
+// image is the same bit for bit; shading (tangent, shadows, AO) reads global
+// memory as before.  Needs a tensor map of the density grid (row pitch a
+// multiple of 16 bytes, 16-byte aligned base).
+
+template <int DF>
+struct Stage {
+    typedef typename DensityTexel<DF>::T T;
+    static constexpr int kAlign = 16 / (int)sizeof(T); // a box's x start is a whole 16 bytes
+    // x extent from the aligned start down from 8b - 1 through 8b + 7, in whole 16 bytes
+    static constexpr int kX = sizeof(T) == 1 ? 32 : 12;
+    static constexpr int kY = 9, kZ = 9;
+    static constexpr uint32_t kBytes = (uint32_t)(kX * kY * kZ * sizeof(T));
+    static constexpr uint32_t kSlot = (kBytes + 127u) / 128u * 128u;
+};
+constexpr int kStageWarps = kWarpsX * kWarpsY;
+constexpr uint32_t kStageWaitLimit = 1u << 20; // try_wait rounds before a brick load counts as lost
+
+template <int DF>
+constexpr size_t staged_smem_bytes() { return (size_t)kStageWarps * (Stage<DF>::kSlot + 8); }
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n\tfence.mbarrier_init.release.cluster;" ::"r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
+{
+    for (uint32_t i = 0; i < kStageWaitLimit; ++i) {
+        uint32_t ok;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(ok)
+                     : "r"(bar), "r"(parity)
+                     : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+// One lane: the box of brick b's texels, origin (ox, oy, oz), into the slot.
+__device__ __forceinline__ void load_box(const CUtensorMap* map, uint32_t slot, uint32_t bar, uint32_t bytes, int ox,
+                                         int oy, int oz)
+{
+    // the warp's earlier reads of the slot (generic proxy) before the copy's writes (async proxy)
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+                 ::"r"(slot), "l"(reinterpret_cast<uint64_t>(map)), "r"(ox), "r"(oy), "r"(oz), "r"(bar)
+                 : "memory");
+}
+
+// sample_density from the staged box (origin ox, oy, oz) of the sample's brick.
+template <int DF>
+__device__ __forceinline__ float sample_box(const RayConsts& c, const typename DensityTexel<DF>::T* box, int ox, int oy,
+                                            int oz, Vec3 p)
+{
+    typedef Stage<DF> S;
+    int i0[3];
+    float a[3];
+    tex_setup(c, p, i0, a); // true for every sample inside the cell grid
+    constexpr int sy = S::kX, sz = S::kX * S::kY;
+    const int b = ((i0[2] - oz) * S::kY + (i0[1] - oy)) * S::kX + (i0[0] - ox);
+    float v[8];
+    v[0] = (float)box[b];
+    v[1] = (float)box[b + 1];
+    v[2] = (float)box[b + sy];
+    v[3] = (float)box[b + sy + 1];
+    v[4] = (float)box[b + sz];
+    v[5] = (float)box[b + sz + 1];
+    v[6] = (float)box[b + sz + sy];
+    v[7] = (float)box[b + sz + sy + 1];
+    const float x00 = fmaf(a[0], v[1] - v[0], v[0]);
+    const float x10 = fmaf(a[0], v[3] - v[2], v[2]);
+    const float x01 = fmaf(a[0], v[5] - v[4], v[4]);
+    const float x11 = fmaf(a[0], v[7] - v[6], v[6]);
+    const float y0 = fmaf(a[1], x10 - x00, x00);
+    const float y1 = fmaf(a[1], x11 - x01, x01);
+    return fmaf(a[2], y1 - y0, y0) * DensityTexel<DF>::scale;
+}
+
+__device__ __forceinline__ int floor_to(int x, int m) { return (x >= 0 ? x / m : -((-x + m - 1) / m)) * m; }
+
+template <int DF, int TF>
+__global__ void __launch_bounds__(32 * kWarpsX * kWarpsY, 6)
+raymarch_staged_kernel(const __grid_constant__ RayConsts c, const __grid_constant__ CUtensorMap map,
+                       const typename DensityTexel<DF>::T* __restrict__ dens, const void* __restrict__ tang,
+                       const uint32_t* __restrict__ occ, const float* __restrict__ depth_in,
+                       float4* __restrict__ rgba, float* __restrict__ depth_out, int x0, int y0, int x1, int y1,
+                       unsigned long long* __restrict__ words)
+{
+    typedef Stage<DF> S;
+    typedef typename DensityTexel<DF>::T T;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const T* box = reinterpret_cast<const T*>(smem + (size_t)warp * S::kSlot);
+    const uint32_t slot = smem_addr(box);
+    const uint32_t bar = smem_addr(smem + (size_t)kStageWarps * S::kSlot + 8 * warp);
+    if (lane == 0) mbar_init(bar);
+    __syncwarp();
+
+    // the warp's 8x4 pixels, as raymarch_kernel's default packet; every lane
+    // stays to the end (the warp loads bricks together)
+    const int px = x0 + (blockIdx.x * kWarpsX + (warp % kWarpsX)) * kTileW + (lane % kTileW);
+    const int py = y0 + (blockIdx.y * kWarpsY + (warp / kWarpsX)) * kTileH + (lane / kTileW);
+    const bool valid = px < x1 && py < y1;
+    const size_t at = valid ? (size_t)py * c.W + px : 0;
+    Vec3 start = v3(0.0f, 0.0f, 0.0f), end = start;
+    const bool hit = valid && ray_entry(c, px, py, start, end);
+    const float db = (hit && depth_in) ? depth_in[at] : 1.0f;
+    const bool depth_test = hit && !(clip_depth(c, end) < db);
+    const float step = 1.0f / c.steps;
+    const bool jump = c.steps_pow2 && !depth_test;
+    float inv_du[3] = {0.0f, 0.0f, 0.0f};
+    if (hit) {
+        float us[3], ue[3], du[3];
+        texel_coords(c, start, us);
+        texel_coords(c, end, ue);
+        du[0] = ue[0] - us[0];
+        du[1] = ue[1] - us[1];
+        du[2] = ue[2] - us[2];
+        reciprocals(du, inv_du);
+    }
+    float t = 0.0f, acc = 0.0f;
+    Vec3 surf = v3(0.0f, 0.0f, 0.0f), entry = surf;
+    bool found = false, entered = false, live = hit, lost = false;
+    uint32_t parity = 0;
+    for (;;) {
+        // ---- to the ray's next sample that reads texels (volume_rendering.glsl:28-47)
+        int need = -1;
+        while (live) {
+            if (!(t < 1.0f)) {
+                live = false;
+                break;
+            }
+            const Vec3 P = mix(start, end, t);
+            if (depth_test && db < clip_depth(c, P)) {
+                live = false;
+                break;
+            }
+            float u[3], lo[3], hi[3];
+            texel_coords(c, P, u);
+            const int z = classify(c, occ, u, inv_du, lo, hi);
+            if (z == 2) {
+                live = false;
+                break;
+            }
+            if (z == 1) {
+                const float n = jump ? steps_inside(u, inv_du, lo, hi, c.steps) : 0.0f;
+                t = n >= 1.0f ? fmaf(n, step, t) : t + step;
+                continue;
+            }
+            need = (int)cell_brick(c, u);
+            break;
+        }
+        const unsigned want = __ballot_sync(0xffffffffu, need >= 0);
+        if (!want) break;
+        // ---- the brick of the first waiting ray, staged
+        const int b = __shfl_sync(0xffffffffu, need, __ffs(want) - 1);
+        const int bx = b % c.nb[0], by = (b / c.nb[0]) % c.nb[1], bz = b / (c.nb[0] * c.nb[1]);
+        const int ox = floor_to(kBrick * bx - 1, S::kAlign), oy = kBrick * by - 1, oz = kBrick * bz - 1;
+        if (lane == 0) load_box(&map, slot, bar, S::kBytes, ox, oy, oz);
+        const bool arrived = mbar_wait(bar, parity);
+        if (__any_sync(0xffffffffu, !arrived)) { // a load that never lands: report it and stop marching
+            if (lane == 0) {
+                atomicOr(words + WORD_STATUS, (unsigned long long)VKHR_DEV_TIMEOUT);
+                mbar_wait(bar, parity); // give the copy one more bounded wait before the slot is let go
+            }
+            lost = true;
+            break;
+        }
+        parity ^= 1u;
+        // ---- the samples of the rays inside that brick
+        if (need == b) {
+            for (;;) {
+                const Vec3 P = mix(start, end, t);
+                const float rho = sample_box<DF>(c, box, ox, oy, oz, P);
+                acc += rho;
+                if (rho != 0.0f) {
+                    if (acc <= c.iso) surf = P;
+                    if (acc >= c.iso) found = true;
+                    if (!entered) {
+                        entry = P;
+                        entered = true;
+                    }
+                    if (acc > c.iso && c.lod * (acc / c.iso) * c.alpha >= 1.0f) { // outputs final
+                        live = false;
+                        break;
+                    }
+                }
+                t += step;
+                if (!(t < 1.0f)) {
+                    live = false;
+                    break;
+                }
+                const Vec3 Q = mix(start, end, t);
+                if (depth_test && db < clip_depth(c, Q)) {
+                    live = false;
+                    break;
+                }
+                float u[3], lo[3], hi[3];
+                texel_coords(c, Q, u);
+                if (classify(c, occ, u, inv_du, lo, hi) != 0 || (int)cell_brick(c, u) != b) break;
+            }
+        }
+        __syncwarp(); // every lane is done with the slot before the next load
+    }
+    if (!valid) return;
+    float4 out = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float out_depth = 1.0f;
+    if (hit && !lost) {
+        if (!found && entered) surf = entry;
+        shade_fragment<DF, TF>(c, dens, tang, occ, surf, acc, out, out_depth);
+    }
     rgba[at] = out;
     if (depth_out) depth_out[at] = out_depth;
 }
@@ -164,6 +402,97 @@ raymarch_batched_kernel(const RayJob* __restrict__ jobs, int nj, uint32_t total_
     }
 }
 
+// The density as a 3D texture for the texture-unit variant: a CUDA array of
+// the grid's extent (kept in the context, re-made when the extent or format
+// changes), LINEAR filtering, border 0 (CLAMP_TO_BORDER), u8 read as UNORM;
+// the call copies the density into it on the stream.  Integer counts cannot
+// be filtered by the texture unit (false: the caller marches from memory).
+template <int DF>
+vkhr_status texture_density(vkhr_ctx* ctx, const RayConsts& c, const void* dens, cudaStream_t st, bool& ok)
+{
+    ok = false;
+    if (DF == VKHR_DENSITY_U32_COUNT) return VKHR_OK;
+    const size_t es = sizeof(typename DensityTexel<DF>::T);
+    if (!ctx->tex_array || ctx->tex_fmt != DF || ctx->tex_res[0] != c.res[0] || ctx->tex_res[1] != c.res[1] ||
+        ctx->tex_res[2] != c.res[2]) {
+        if (ctx->tex_array && ctx->live_graphs > 0)
+            return vkhr_fail(ctx, VKHR_ERR_CAPACITY, "the density texture would have to change while a frame graph lives");
+        if (ctx->tex_obj) cudaDestroyTextureObject(ctx->tex_obj);
+        if (ctx->tex_array) {
+            VKHR_CUDA_TRY(ctx, cudaDeviceSynchronize()); // earlier launches may still read it
+            cudaFreeArray(ctx->tex_array);
+        }
+        ctx->tex_obj = 0;
+        ctx->tex_array = nullptr;
+        const cudaChannelFormatDesc fd =
+            DF == VKHR_DENSITY_U8_UNORM ? cudaCreateChannelDesc<unsigned char>() : cudaCreateChannelDesc<float>();
+        VKHR_CUDA_TRY(ctx, cudaMalloc3DArray(&ctx->tex_array, &fd, make_cudaExtent(c.res[0], c.res[1], c.res[2])));
+        cudaResourceDesc rd = {};
+        rd.resType = cudaResourceTypeArray;
+        rd.res.array.array = ctx->tex_array;
+        cudaTextureDesc td = {};
+        for (int k = 0; k < 3; ++k) td.addressMode[k] = cudaAddressModeBorder; // border colour 0
+        td.filterMode = cudaFilterModeLinear;
+        td.readMode = DF == VKHR_DENSITY_U8_UNORM ? cudaReadModeNormalizedFloat : cudaReadModeElementType;
+        td.normalizedCoords = 0;
+        VKHR_CUDA_TRY(ctx, cudaCreateTextureObject(&ctx->tex_obj, &rd, &td, nullptr));
+        for (int k = 0; k < 3; ++k) ctx->tex_res[k] = c.res[k];
+        ctx->tex_fmt = DF;
+    }
+    cudaMemcpy3DParms cp = {};
+    cp.srcPtr = make_cudaPitchedPtr(const_cast<void*>(dens), (size_t)c.res[0] * es, (size_t)c.res[0], (size_t)c.res[1]);
+    cp.dstArray = ctx->tex_array;
+    cp.extent = make_cudaExtent(c.res[0], c.res[1], c.res[2]);
+    cp.kind = cudaMemcpyDeviceToDevice;
+    VKHR_CUDA_TRY(ctx, cudaMemcpy3DAsync(&cp, st));
+    ok = true;
+    return VKHR_OK;
+}
+
+// cuTensorMapEncodeTiled from the driver (looked up once; NULL if unavailable).
+typedef CUresult (*TensorMapEncoder)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                     const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                     CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+TensorMapEncoder tensor_map_encoder()
+{
+    static std::once_flag once;
+    static TensorMapEncoder fn = nullptr;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<TensorMapEncoder>(p);
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
+// The tensor map of a density grid for the staged march: 3D, the grid's own
+// extent (texels outside it read as zero), box Stage<DF>::kX x 9 x 9.  False
+// when TMA cannot address the grid: a base not 16-byte aligned, or a row
+// pitch not a multiple of 16 bytes.
+template <int DF>
+bool density_tensor_map(const RayConsts& c, const void* dens, CUtensorMap* map)
+{
+    typedef Stage<DF> S;
+    const size_t es = sizeof(typename S::T);
+    const TensorMapEncoder enc = tensor_map_encoder();
+    if (!enc || (reinterpret_cast<uintptr_t>(dens) & 15u) || ((size_t)c.res[0] * es) % 16 != 0) return false;
+    const CUtensorMapDataType type = DF == VKHR_DENSITY_U8_UNORM ? CU_TENSOR_MAP_DATA_TYPE_UINT8
+                                     : DF == VKHR_DENSITY_U32_COUNT ? CU_TENSOR_MAP_DATA_TYPE_UINT32
+                                                                    : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    const cuuint64_t dim[3] = {(cuuint64_t)c.res[0], (cuuint64_t)c.res[1], (cuuint64_t)c.res[2]};
+    const cuuint64_t stride[2] = {(cuuint64_t)c.res[0] * es, (cuuint64_t)c.res[0] * c.res[1] * es};
+    const cuuint32_t box[3] = {(cuuint32_t)S::kX, (cuuint32_t)S::kY, (cuuint32_t)S::kZ};
+    const cuuint32_t elem[3] = {1, 1, 1};
+    return enc(map, type, 3, const_cast<void*>(dens), dim, stride, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 template <int DF, int TF>
 vkhr_status launch(vkhr_ctx* ctx, const RayConsts& c, const void* dens, const void* tang, const float* din, float* rgba,
                    float* dout, const int32_t rect[4], cudaStream_t st)
@@ -194,8 +523,35 @@ vkhr_status launch(vkhr_ctx* ctx, const RayConsts& c, const void* dens, const vo
                     x1, y1);
     }
     if (rect[2] <= 0 || rect[3] <= 0) return background ? vkhr_join_side(ctx, st) : VKHR_OK;
-    const int v = ctx->ray_variant[DF][TF];
+    int v = ctx->ray_variant[DF][TF];
     const dim3 block(32 * kWarpsX * kWarpsY);
+    if (v == kStagedVariant) {
+        CUtensorMap map;
+        if (density_tensor_map<DF>(c, dens, &map)) {
+            const dim3 grid((rect[2] + kTileW * kWarpsX - 1) / (kTileW * kWarpsX),
+                            (rect[3] + kTileH * kWarpsY - 1) / (kTileH * kWarpsY));
+            VKHR_LAUNCH(ctx, (raymarch_staged_kernel<DF, TF>), grid, block, staged_smem_bytes<DF>(), st, c, map,
+                        (const typename DensityTexel<DF>::T*)dens, tang, ctx->occ, din, out, dout, x0, y0, x1, y1,
+                        ctx->d_words);
+            return background ? vkhr_join_side(ctx, st) : VKHR_OK;
+        }
+        v = 0; // TMA cannot address this grid: the default packets
+    }
+    if (v == kTextureVariant) {
+        bool ok = false;
+        vkhr_status ts = texture_density<DF>(ctx, c, dens, st, ok);
+        if (ts != VKHR_OK) return ts;
+        if (ok) {
+            RayConsts ct = c;
+            ct.tex = (unsigned long long)ctx->tex_obj;
+            const dim3 grid((rect[2] + kTileW * kWarpsX - 1) / (kTileW * kWarpsX),
+                            (rect[3] + kTileH * kWarpsY - 1) / (kTileH * kWarpsY));
+            VKHR_LAUNCH(ctx, (raymarch_kernel<DF, TF, 8, 6, kSampleTexture>), grid, block, 0, st, ct,
+                        (const typename DensityTexel<DF>::T*)dens, tang, ctx->occ, din, out, dout, x0, y0, x1, y1);
+            return background ? vkhr_join_side(ctx, st) : VKHR_OK;
+        }
+        v = 0; // integer counts: the default packets
+    }
     const int tw = kRayVariants[v].tw, th = 32 / tw;
     const dim3 grid((rect[2] + tw * kWarpsX - 1) / (tw * kWarpsX), (rect[3] + th * kWarpsY - 1) / (th * kWarpsY));
     const typename DensityTexel<DF>::T* d = (const typename DensityTexel<DF>::T*)dens;
@@ -246,6 +602,7 @@ extern "C" vkhr_status vkhr_raymarch(vkhr_ctx* ctx, const vkhr_raymarch_params* 
         s = launch<VKHR_DENSITY_F32, VKHR_TANGENT_I8_SNORM>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, rect, st);
     else
         s = launch<VKHR_DENSITY_F32, VKHR_TANGENT_F32X4>(ctx, c, d_density, d_tangent, d_depth_in, d_rgba, d_depth_out, rect, st);
+    if (s != VKHR_OK) return s; // e.g. scratch that could not grow: nothing was launched
     VKHR_CUDA_TRY(ctx, cudaGetLastError());
     return VKHR_OK;
 }
@@ -281,7 +638,8 @@ extern "C" vkhr_status vkhr_autotune_raymarch(vkhr_ctx* ctx, const vkhr_raymarch
     float ms[VKHR_RAYMARCH_VARIANTS];
     int best = 0;
     vkhr_status s = VKHR_OK;
-    for (int v = 0; v < VKHR_RAYMARCH_VARIANTS && s == VKHR_OK; ++v) {
+    for (int v = 0; v < VKHR_RAYMARCH_VARIANTS; ++v) ms[v] = 0.0f;
+    for (int v = 0; v < kTunedVariants && s == VKHR_OK; ++v) {
         ctx->ray_variant[df][tf] = v;
         float t[3] = {0.0f, 0.0f, 0.0f};
         for (int r = -1; r < 3 && s == VKHR_OK; ++r) { // one warm-up, three timed runs
@@ -492,10 +850,12 @@ constexpr int kMaxStaticDevices = 64;
 
 __device__ __align__(256) uint32_t g_static_occupancy[kStaticOccupancyWords];
 
-std::once_flag g_static_once[kMaxStaticDevices];
+// Per device: the array's device address and the SM count, resolved by the
+// first call on the device that succeeds (a failed lookup is retried).
+std::mutex g_static_mutex;
+bool g_static_resolved[kMaxStaticDevices];
 uint32_t* g_static_occupancy_ptr[kMaxStaticDevices];
 int g_static_sm_count[kMaxStaticDevices];
-cudaError_t g_static_error[kMaxStaticDevices];
 
 template <int DF, int TF>
 cudaError_t launch_static(const RayConsts& c, const void* dens, const void* tang, const float* din, float* rgba,
@@ -511,18 +871,22 @@ cudaError_t launch_static(const RayConsts& c, const void* dens, const void* tang
         occupancy_kernel<DF, 8><<<ob, 128, 0, st>>>(dd, c.res[0], c.res[1], c.res[2], c.nb[0], c.nb[1], c.nb[2], occ);
     else
         occupancy_kernel<DF, 1><<<ob, 128, 0, st>>>(dd, c.res[0], c.res[1], c.res[2], c.nb[0], c.nb[1], c.nb[2], occ);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const int x0 = rect[0], y0 = rect[1], x1 = rect[0] + rect[2], y1 = rect[1] + rect[3];
     float4* out = reinterpret_cast<float4*>(rgba);
-    if (rect[2] < c.W || rect[3] < c.H)
+    if (rect[2] < c.W || rect[3] < c.H) {
         background_kernel<<<(unsigned)sm_count * 8, 256, 0, st>>>(out, dout, c.W, c.H, x0, y0, x1, y1);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
     if (rect[2] > 0 && rect[3] > 0) {
         const dim3 block(32 * kWarpsX * kWarpsY);
         const dim3 grid((rect[2] + kTileW * kWarpsX - 1) / (kTileW * kWarpsX),
                         (rect[3] + kTileH * kWarpsY - 1) / (kTileH * kWarpsY));
         raymarch_kernel<DF, TF><<<grid, block, 0, st>>>(c, (const typename DensityTexel<DF>::T*)dens, tang, occ, din,
                                                          out, dout, x0, y0, x1, y1);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
-    return cudaGetLastError();
+    return cudaSuccess;
 }
 
 } // namespace
@@ -544,14 +908,24 @@ extern "C" vkhr_status vkhr_raymarch_static(const vkhr_raymarch_params* params, 
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return VKHR_ERR_CUDA;
     if (dev < 0 || dev >= kMaxStaticDevices) return VKHR_ERR_NOT_SUPPORTED;
-    // first call on this device: resolve the array's device address (host
-    // code cannot use the symbol itself) and the SM count
-    std::call_once(g_static_once[dev], [dev]() {
-        cudaError_t e = cudaGetSymbolAddress((void**)&g_static_occupancy_ptr[dev], g_static_occupancy);
-        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g_static_sm_count[dev], cudaDevAttrMultiProcessorCount, dev);
-        g_static_error[dev] = e;
-    });
-    if (g_static_error[dev] != cudaSuccess) return VKHR_ERR_CUDA;
+    // first successful call on this device: resolve the array's device
+    // address (host code cannot use the symbol itself) and the SM count
+    {
+        std::lock_guard<std::mutex> lock(g_static_mutex);
+        if (!g_static_resolved[dev]) {
+            uint32_t* ptr = nullptr;
+            int sms = 0;
+            cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_static_occupancy);
+            if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            if (e != cudaSuccess) {
+                cudaGetLastError(); // leave no error of the failed lookup behind; a later call retries
+                return VKHR_ERR_CUDA;
+            }
+            g_static_occupancy_ptr[dev] = ptr;
+            g_static_sm_count[dev] = sms;
+            g_static_resolved[dev] = true;
+        }
+    }
     int32_t rect[4]; // pixels outside it miss the volume's box
     if (vkhr_raymarch_footprint(params, rect) != VKHR_OK) return VKHR_ERR_INVALID_ARG;
     uint32_t* occ = g_static_occupancy_ptr[dev];

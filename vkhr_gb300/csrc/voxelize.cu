@@ -1210,9 +1210,49 @@ vkhr_status check_device_status(vkhr_ctx* ctx, unsigned long long s)
                          "a segment spans more than 2^24 voxels (vertices far outside the bounds)");
     if (s & VKHR_DEV_LIST_OVERFLOW) return vkhr_fail(ctx, VKHR_ERR_CAPACITY, "visit list overflow");
     if (s & VKHR_DEV_REPLAY_MISMATCH) return vkhr_fail(ctx, VKHR_ERR_CUDA, "brick replay disagreed with binning");
+    if (s & VKHR_DEV_TIMEOUT) return vkhr_fail(ctx, VKHR_ERR_TIMEOUT, "a bounded device wait ran out (a brick load never landed)");
     if (s & VKHR_DEV_BAD_INDEX)
         return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "a fragment's pixel or a PPLL node link is out of range");
     return VKHR_OK;
+}
+
+// Reports (and clears) the device status bits; a visit-list overflow also
+// forgets the learned visit totals, so the next unbudgeted call at each size
+// counts its visits again.
+vkhr_status report_status(vkhr_ctx* ctx, unsigned long long status, cudaStream_t st)
+{
+    if (!status) return VKHR_OK;
+    VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_words + WORD_STATUS, 0, sizeof(unsigned long long), st));
+    if (status & VKHR_DEV_LIST_OVERFLOW)
+        for (int i = 0; i < kLearnedSizes; ++i) ctx->learned[i].visits = 0;
+    return check_device_status(ctx, status);
+}
+
+bool same_size(const vkhr_learned_visits& l, const vkhr_voxel_job& j, bool tang)
+{
+    return l.visits && l.items == j.item_count && l.w == j.width && l.h == j.height && l.d == j.depth &&
+           l.mode == (j.index_mode | (tang ? 2 : 0));
+}
+
+// Visit total of the last counted call at this size (0: none).
+uint64_t learned_visits(const vkhr_ctx* ctx, const vkhr_voxel_job& j, bool tang)
+{
+    for (int i = 0; i < kLearnedSizes; ++i)
+        if (same_size(ctx->learned[i], j, tang)) return ctx->learned[i].visits;
+    return 0;
+}
+
+void learn_visits(vkhr_ctx* ctx, const vkhr_voxel_job& j, bool tang, uint64_t visits)
+{
+    int at = -1;
+    for (int i = 0; i < kLearnedSizes && at < 0; ++i)
+        if (same_size(ctx->learned[i], j, tang)) at = i;
+    if (at < 0) {
+        at = ctx->learned_next;
+        ctx->learned_next = (ctx->learned_next + 1) % kLearnedSizes;
+    }
+    ctx->learned[at] = vkhr_learned_visits{j.item_count, j.width, j.height, j.depth, j.index_mode | (tang ? 2 : 0),
+                                           visits ? visits : 1};
 }
 
 template <bool SEG, bool TANG, bool PACK>
@@ -1266,7 +1306,10 @@ vkhr_status make_job(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job& in, Vox
     return VKHR_OK;
 }
 
-vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* jobs_in, int nj, cudaStream_t st)
+// count_visits: a segment call without a budget reads its visit total back
+// even when an earlier call at its size taught the context one.
+vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* jobs_in, int nj, cudaStream_t st,
+                           bool count_visits = false)
 {
     if (!ctx) return VKHR_ERR_INVALID_ARG;
     if (nj <= 0 || nj > kMaxJobs || !jobs_in) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "job count must be in [1, 256]");
@@ -1324,9 +1367,18 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
         }
     }
     // Capacities that do not depend on the data: vertex mode is bounded by
-    // the vertex count; segment mode by the visit budget when one is set.
-    const bool bounded = !segments || ctx->visit_budget > 0;
-    uint64_t visits_total = segments ? ctx->visit_budget : total_items;
+    // the vertex count; segment mode by the visit budget when one is set,
+    // and a one-style call without a budget, at a size the context counted
+    // before, by twice that count (a call above it records a list overflow).
+    // Only the first call at a size reads its visit total back.
+    uint64_t learned = 0;
+    if (segments && !ctx->visit_budget && nj == 1 && ctx->direct_cap && total_items && !count_visits)
+        learned = learned_visits(ctx, jobs_in[0], tang);
+    const bool bounded = !segments || ctx->visit_budget > 0 || learned > 0;
+    uint64_t visits_total = 0; // unbounded: the count read back below
+    if (!segments) visits_total = total_items;
+    else if (ctx->visit_budget) visits_total = ctx->visit_budget;
+    else if (learned) visits_total = std::min<uint64_t>(2 * learned + 4096, (1ull << 32) - 1);
     if (bounded) {
         s = vkhr_reserve(ctx, (void**)&ctx->items, &ctx->items_cap, visits_total ? visits_total : 1, sizeof(uint2));
         if (s != VKHR_OK) return s;
@@ -1351,7 +1403,10 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
         }
     }
     const bool speculative = bounded && direct_cap != 0; // the device picks the layout
-    VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_words, 0, WORD_NORM * sizeof(unsigned long long), st));
+    // per-call words; the status bits stay until a check reports them
+    VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_words, 0, WORD_STATUS * sizeof(unsigned long long), st));
+    VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_words + WORD_STATUS + 1, 0,
+                                       (WORD_NORM - WORD_STATUS - 1) * sizeof(unsigned long long), st));
     VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->brick_visits, 0, (size_t)total_bricks * sizeof(uint32_t), st));
     const unsigned threads = 256;
     // one style: one item per thread (blocks retire and start staggered, so
@@ -1406,11 +1461,12 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
         VKHR_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->h_words, ctx->d_words, WORD_NORM * sizeof(unsigned long long),
                                            cudaMemcpyDeviceToHost, st));
         VKHR_CUDA_TRY(ctx, cudaStreamSynchronize(st));
-        s = check_device_status(ctx, ctx->h_words[WORD_STATUS]);
+        s = report_status(ctx, ctx->h_words[WORD_STATUS], st); // this call's, or earlier unreported errors
         if (s != VKHR_OK) return s;
         visits_total = ctx->h_words[WORD_TOTAL_VISITS];
         if (visits_total >= (1ull << 32))
             return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "more than 2^32 - 1 voxel visits in one call");
+        if (nj == 1) learn_visits(ctx, jobs_in[0], tang, visits_total);
         // the next calls' per-brick capacity: this call's largest brick + 25%, grow-only
         const uint64_t largest = ctx->h_words[WORD_MAX_BRICK_VISITS];
         const uint64_t want = (largest + largest / 4 + 63) / 64 * 64;
@@ -1530,6 +1586,20 @@ vkhr_status vkhr_voxelize_batched(vkhr_ctx* ctx, int32_t segments, const vkhr_vo
     return voxelize_batch(ctx, segments != 0, jobs, job_count, (cudaStream_t)stream);
 }
 
+} // extern "C"
+
+vkhr_status vkhr_voxelize_counted(vkhr_ctx* ctx, const vkhr_voxel_job* job, void* stream, uint64_t* visits)
+{
+    const uint64_t keep = ctx->visit_budget;
+    ctx->visit_budget = 0;
+    const vkhr_status s = voxelize_batch(ctx, true, job, 1, (cudaStream_t)stream, true);
+    ctx->visit_budget = keep;
+    if (s == VKHR_OK) *visits = ctx->h_words[WORD_TOTAL_VISITS];
+    return s;
+}
+
+extern "C" {
+
 vkhr_status vkhr_set_visit_budget(vkhr_ctx* ctx, uint64_t max_visits)
 {
     if (!ctx) return VKHR_ERR_INVALID_ARG;
@@ -1564,11 +1634,8 @@ vkhr_status vkhr_check_status(vkhr_ctx* ctx, void* stream)
     VKHR_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->h_words, ctx->d_words, WORD_NORM * sizeof(unsigned long long),
                                        cudaMemcpyDeviceToHost, (cudaStream_t)stream));
     VKHR_CUDA_TRY(ctx, cudaStreamSynchronize((cudaStream_t)stream));
-    const unsigned long long status = ctx->h_words[WORD_STATUS];
-    if (status) // reported once: the next check starts clean
-        VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_words + WORD_STATUS, 0, sizeof(unsigned long long),
-                                           (cudaStream_t)stream));
-    return check_device_status(ctx, status);
+    return report_status(ctx, ctx->h_words[WORD_STATUS], (cudaStream_t)stream); // reported once
+
 }
 
 vkhr_status vkhr_normalize_densities(vkhr_ctx* ctx, uint8_t* d, uint64_t n, void* stream)

@@ -58,13 +58,17 @@ def make_params(bounds, resolution, width, height, camera_distance=4.0, fov_degr
                 hair_color=(0.40, 0.32, 0.24), hair_alpha=0.5, hair_exponent=80.0,
                 shading_model=_abi.SHADING_KAJIYA_KAY, deep_shadows_on=1, occlusion_radius=2.5,
                 ao_exponent=10.0, ao_max=0.16, renderer=_abi.RENDERER_RAYMARCHER, shadow_steps=0.0, kd=1.0,
-                density_format=_abi.DENSITY_U8_UNORM, tangent_format=_abi.TANGENT_I8_SNORM, target=None):
+                density_format=_abi.DENSITY_U8_UNORM, tangent_format=_abi.TANGENT_I8_SNORM, target=None,
+                spec_exponent2=0.0, spec_shift=(0.0, 0.0), ao_directions=0):
     """Reference-semantics raymarch parameters for a style with AABB `bounds`.
 
     The camera looks at the AABB centre (or `target`) from `camera_distance`
     along `view_direction`, up = +y; the light and intensity default to the
     reference's ponytail scene (share/scenes/ponytail.vkhr: direction
-    (1, 2, 1), intensity (0.43, 0.38, 0.28)).
+    (1, 2, 1), intensity (0.43, 0.38, 0.28)).  spec_exponent2, spec_shift and
+    ao_directions are the extension knobs of vkhr_raymarch_params (a second,
+    hair-coloured specular lobe, tangent shifts per lobe, directional AO);
+    their defaults give the reference's shading.
     """
     p = _abi.RaymarchParams()
     p.width, p.height = int(width), int(height)
@@ -107,5 +111,13 @@ def make_params(bounds, resolution, width, height, camera_distance=4.0, fov_degr
     p.kd = kd
     p.density_format = density_format
     p.tangent_format = tangent_format
+    p.spec_exponent2 = spec_exponent2
+    p.spec_shift[:] = [float(x) for x in spec_shift]
+    p.ao_directions = int(ao_directions)
     return p
+
+
+# The shading the workloads name: Kajiya-Kay with kd 0.4, specular exponents
+# 80 / 8 and tangent shifts +0.1 / -0.1.
+CONFIG_SHADING = {"kd": 0.4, "hair_exponent": 80.0, "spec_exponent2": 8.0, "spec_shift": (0.1, -0.1)}
 
