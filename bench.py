@@ -822,6 +822,98 @@ def composite_section(args, dev, stream, flush, st, t, idx, b, res):
     return out
 
 
+RAY_AB = {
+    "workload": "raymarch variants on two views: the production frame's 1920x1080 view of its normalized 256^3 "
+                "volume (512 steps, 64-step shadows, 8-tap AO), and a 3840x2160 view of the 512^3 scale volume "
+                "(1024 steps, 128-step shadows, 16-direction AO); workloads' Kajiya-Kay",
+    "variants": {"0-3": "ray packets reading texels from L2/HBM (8x4, 16x2, 4x8, 8x4 at 64 registers)",
+                 "4": "8x4 packets, each occupied density brick a warp's rays need staged into shared memory by one "
+                      "TMA tensor copy",
+                 "5": "8x4 packets sampling through the texture unit (3D array copy + hardware trilinear, "
+                      "8-bit weights)"},
+    "warm": "the volume L2-resident, as right after the voxelizer wrote it; cold: L2 flushed (512 MiB write) first",
+}
+
+
+def raymarch_ab_section(args, dev, stream, flush):
+    """Time every raymarch variant on the headline view and a 512^3 view."""
+    import torch
+
+    from vkhr_gb300 import _abi, _native, scene, strands
+
+    s = stream.cuda_stream
+    ctx = _native.Context(dev.index)
+    views = {}
+    st, t, idx = make_style()
+    res = (WORKLOAD["resolution"],) * 3
+    dv, dt, di = (torch.from_numpy(a).to(dev) for a in (st.vertices, t, idx.view(np.int32)))
+    b = ctx.bounding_box(dv.data_ptr(), st.vertex_count, s)
+    n = res[0] ** 3
+    counts = torch.empty(n, dtype=torch.int32, device=dev)
+    dens = torch.empty(n, dtype=torch.uint8, device=dev)
+    tq = torch.empty((n, 4), dtype=torch.int8, device=dev)
+    ctx.voxelize_segments(dv.data_ptr(), dt.data_ptr(), di.data_ptr(), idx.shape[0], b, res, _abi.INDEX_REF_FP32,
+                          counts.data_ptr(), dens.data_ptr(), tq.data_ptr(), s)
+    ctx.normalize_densities(dens.data_ptr(), n, s)
+    views["production 1920x1080, 256^3"] = (frame_params(b, res), dens, tq)
+    if not args.no_scale:
+        sst = strands.hemisphere_style(1_048_576, 32, radius=1.2, step_length=0.04, seed=4)
+        st_t = strands.generate_tangents(sst.vertices, sst.segments)
+        s_idx = strands.generate_indices(sst.segments)
+        r5 = (512, 512, 512)
+        n5 = 512 ** 3
+        v5, t5, i5 = (torch.from_numpy(a).to(dev) for a in (sst.vertices, st_t, s_idx.view(np.int32)))
+        b5 = ctx.bounding_box(v5.data_ptr(), sst.vertex_count, s)
+        c5 = torch.empty(n5, dtype=torch.int32, device=dev)
+        d5 = torch.empty(n5, dtype=torch.uint8, device=dev)
+        q5 = torch.empty((n5, 4), dtype=torch.int8, device=dev)
+        ctx.voxelize_segments(v5.data_ptr(), t5.data_ptr(), i5.data_ptr(), s_idx.shape[0], b5, r5,
+                              _abi.INDEX_REF_FP32, c5.data_ptr(), d5.data_ptr(), q5.data_ptr(), s)
+        ctx.normalize_densities(d5.data_ptr(), n5, s)
+        del v5, t5, i5, c5
+        p5 = scene.make_params(b5, r5, 3840, 2160, camera_distance=5.0, raycast_steps=1024.0, shadow_steps=128.0,
+                               ao_directions=16, **scene.CONFIG_SHADING)
+        views["scale 3840x2160, 512^3"] = (p5, d5, q5)
+    torch.cuda.synchronize()
+    out = {"config": RAY_AB, "views": {}}
+    for name, (p, d, q) in views.items():
+        rgba = torch.empty((p.height, p.width, 4), dtype=torch.float32, device=dev)
+        base = None
+        rows = {}
+        for v in range(_abi.RAYMARCH_VARIANTS):
+            ctx.set_raymarch_variant(p.density_format, p.tangent_format, v)
+            res_v = {}
+            for mode in ("warm", "cold"):
+                ms = []
+                for k in range(max(args.warmup, 3) + max(args.steps, 5)):
+                    if mode == "cold":
+                        flush.zero_()
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    ctx.raymarch(p, d.data_ptr(), q.data_ptr(), None, rgba.data_ptr(), None, s)
+                    e1.record(stream)
+                    torch.cuda.synchronize()
+                    if k >= max(args.warmup, 3):
+                        ms.append(e0.elapsed_time(e1))
+                res_v[mode + "_ms"] = statistics.median(ms)
+            ctx.set_profiling(True)
+            ctx.raymarch(p, d.data_ptr(), q.data_ptr(), None, rgba.data_ptr(), None, s)
+            torch.cuda.synchronize()
+            res_v["kernels_warm_ms"] = {k_: round(m_, 4) for k_, m_ in ctx.profile()}
+            ctx.set_profiling(False)
+            img = rgba.clone()
+            if base is None:
+                base = img
+            diff = (img - base).abs()
+            res_v["max_diff_vs_variant0"] = float(diff.max().item())
+            res_v["rms_diff_vs_variant0"] = float(diff.pow(2).mean().sqrt().item())
+            rows[str(v)] = res_v
+        ctx.set_raymarch_variant(p.density_format, p.tangent_format, 0)
+        out["views"][name] = rows
+    ctx.close()
+    return out
+
+
 def gb300_arm(args):
     import torch
 
@@ -858,6 +950,11 @@ def gb300_arm(args):
             b = ctx.bounding_box(dv.data_ptr(), st.vertex_count, s)
             print(json.dumps({"section": "composite",
                               "composite": composite_section(args, dev, stream, flush, st, t, idx, b, res)}))
+        return 0
+    if args.section == "raymarch_ab":  # the raymarch variants' A/B (opt-in)
+        flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+        if rank == 0:
+            print(json.dumps({"section": "raymarch_ab", "raymarch_ab": raymarch_ab_section(args, dev, stream, flush)}))
         return 0
     if args.section == "batched":  # the multi-style comparison alone (profiling runs)
         flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
@@ -1170,10 +1267,10 @@ def main():
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiable workload")
     ap.add_argument("--no-composite", action="store_true", help="skip the hybrid-LoD compositing workload")
     ap.add_argument("--section", default="all",
-                    choices=["all", "frame", "batched", "scale", "diff", "schedule", "composite"],
+                    choices=["all", "frame", "batched", "scale", "diff", "schedule", "composite", "raymarch_ab"],
                     help="frame: the production frame only; batched: the multi-style comparison only; "
                          "scale: the 512^3 workload only; diff: the differentiable workload only; "
-                         "composite: the hybrid-LoD compositing only")
+                         "composite: the hybrid-LoD compositing only; raymarch_ab: the raymarch variants' A/B")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)

@@ -593,13 +593,33 @@ __device__ __forceinline__ float4 visit_tangent(const float4* __restrict__ pair_
     return make_float4(__ldg(t), __ldg(t + 1), __ldg(t + 2), 0.0f);
 }
 
+// The reference's tangent of a voxel with c <= 255 visits is
+// trunc(fl(fl(S / c) * 127)) per component, S the serial FP32 sum of its
+// visits' tangents in key order (hair_style.cc:311-335).  That map is
+// monotone in S, and any other order of the same additions gives a sum F with
+// |S - F| <= 2 gamma(c - 1) sum |t_i| (recursive summation, N. J. Higham,
+// "Accuracy and Stability of Numerical Algorithms", 2nd ed., 4.2).  So when
+// the map agrees at both ends of [F - B, F + B] (B that bound, with the ends
+// rounded outward), it is the reference's value, whatever S is; only the
+// voxels where it does not are sorted and summed in key order.  c <= 2: every
+// order gives the same sum.
+__device__ __forceinline__ bool certify(float f, float a, float bound_scale, float m, int& q)
+{
+    if (!(a < INFINITY)) return false;                 // inf or NaN tangents: the ordered sum decides
+    const float b = __fmul_ru(a, bound_scale);
+    const int lo = quantize1(__fsub_rd(f, b), m), hi = quantize1(__fadd_ru(f, b), m);
+    q = lo;
+    return lo == hi;
+}
+
 // Per-voxel results of one brick whose visit keys are grouped by local voxel
 // at `keys` (shared memory, or the global scratch for bricks above
-// kBrickCap): counts and u8 densities, and the tangents.  Each voxel's keys
-// are sorted in place -- up to kBrickThread by the voxel's own thread
-// (register sorting network), up to kBrickSmall by a warp (64-key register bitonic
-// sort) -- and then every voxel's thread adds its tangents in key order, all
-// voxels of the brick at once; more than kBrickSmall visits go to
+// kBrickCap): counts and u8 densities, and the tangents.  Every voxel's thread
+// adds its tangents in the order its keys were grouped and certifies the
+// quantized result (certify); the voxels it cannot certify have their keys
+// sorted in place -- up to kBrickThread by the voxel's own thread (register
+// sorting network), up to kBrickSmall by a warp (64-key register bitonic
+// sort) -- and summed again in key order; more than kBrickSmall visits go to
 // crowded_kernel through a descriptor.  Block-wide.
 template <bool SEG, bool TANG>
 __device__ __forceinline__ void resolve_brick(const VoxJob& J, const Grid& g, uint32_t b, const float4* pair_tan,
@@ -622,6 +642,42 @@ __device__ __forceinline__ void resolve_brick(const VoxJob& J, const Grid& g, ui
         if (J.dens) J.dens[vi] = (uint8_t)(c < 255u ? c : 255u);
     }
     if (!TANG) return;
+    // ---- every voxel of up to kBrickSmall visits: its sum in grouped order, certified
+    bool sorted_needed = false;
+    if (inside && c <= (uint32_t)kBrickSmall) {
+        if (c == 0) {
+            tq[vi] = 0u;
+        } else {
+            float sx = 0.0f, sy = 0.0f, sz = 0.0f, am = 0.0f; // am: sum of max |t_i| over the components
+            for (uint32_t i0 = 0; i0 < c; i0 += kGather) {
+                float4 tv[kGather];
+#pragma unroll
+                for (int j = 0; j < kGather; ++j)
+                    if (i0 + j < c) tv[j] = visit_tangent<SEG>(pair_tan, tan, k[i0 + j]);
+#pragma unroll
+                for (int j = 0; j < kGather; ++j)
+                    if (i0 + j < c) {
+                        sx = __fadd_rn(sx, tv[j].x);
+                        sy = __fadd_rn(sy, tv[j].y);
+                        sz = __fadd_rn(sz, tv[j].z);
+                        am = __fadd_ru(am, fmaxf(fmaxf(fabsf(tv[j].x), fabsf(tv[j].y)), fabsf(tv[j].z)));
+                    }
+            }
+            if (c <= 2u) { // one addition at most: the same sum in every order
+                tq[vi] = pack_tangent(sx, sy, sz, c);
+            } else {
+                // B = 2 gamma(c - 1) sum |t| per component, gamma(n) = n u / (1 - n u) <= 1.01 n u for
+                // n < 256 (u = 2^-24); am (rounded up) bounds every component's sum |t|; 2.05 covers both
+                const float scale = __fmul_ru((float)(c - 1), 2.05f * 5.9604645e-8f);
+                const float fm = (float)c;
+                int qx, qy, qz;
+                if (certify(sx, am, scale, fm, qx) && certify(sy, am, scale, fm, qy) && certify(sz, am, scale, fm, qz))
+                    tq[vi] = ((uint32_t)(qx & 0xff)) | ((uint32_t)(qy & 0xff) << 8) | ((uint32_t)(qz & 0xff) << 16);
+                else
+                    sorted_needed = true;
+            }
+        }
+    }
     if (inside && c > (uint32_t)kBrickSmall) { // crowded: a warp or a CTA of its own sorts the keys
         // descriptors of up to kCrowdWarpMax visits from the front, larger ones from the back
         const bool by_warp = c <= (uint32_t)kCrowdWarpMax;
@@ -639,19 +695,19 @@ __device__ __forceinline__ void resolve_brick(const VoxJob& J, const Grid& g, ui
                 status |= VKHR_DEV_LIST_OVERFLOW;
             }
         }
-    } else if (inside && c > (uint32_t)kBrickThread) {
+    } else if (sorted_needed && c > (uint32_t)kBrickThread) {
         wlist[atomicAdd(&wcount, 1u)] = (uint32_t)tid; // sorted by a warp below
     }
     {   // up to kBrickThread keys: sorted by the voxel's thread in registers, with the
-        // network of the warp's largest such voxel (a voxel outside the grid has none)
-        const uint32_t ct = c <= (uint32_t)kBrickThread ? c : 0u;
+        // network of the warp's largest such voxel (only voxels that need it)
+        const uint32_t ct = sorted_needed && c <= (uint32_t)kBrickThread ? c : 0u;
         const uint32_t nmax = __reduce_max_sync(0xffffffffu, ct);
         if (nmax > 8) sort_keys<16>(k, ct);
         else if (nmax > 4) sort_keys<8>(k, ct);
         else if (nmax > 1) sort_keys<4>(k, ct);
     }
     __syncthreads();
-    {   // voxels with kBrickThread < count <= kBrickSmall: a warp sorts the keys in place (two per lane)
+    {   // kBrickThread < count <= kBrickSmall, uncertified: a warp sorts the keys in place (two per lane)
         const unsigned lane = lane_id(), warp = (unsigned)tid >> 5;
         for (uint32_t m = warp; m < wcount; m += kBrickWarps) {
             const uint32_t l = wlist[m], cl = cnt[l];
@@ -663,31 +719,23 @@ __device__ __forceinline__ void resolve_brick(const VoxJob& J, const Grid& g, ui
         }
     }
     __syncthreads();
-    const uint32_t cs = cnt[tid]; // reloaded: fewer registers live across the barriers
-    if (inside && cs <= (uint32_t)kBrickSmall) {
-        const uint32_t c = cs;
-        const uint32_t* k = keys + (off[tid] - c);
-        const uint32_t vi = x + g.w * (y + g.h * z);
-        if (c == 0) {
-            tq[vi] = 0u;
-        } else {
-            // gather kGather tangents at a time (independent loads), then add them in key order
-            float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-            for (uint32_t i0 = 0; i0 < c; i0 += kGather) {
-                float4 tv[kGather];
+    if (sorted_needed) { // the uncertified voxels: their tangents added in key order
+        const uint32_t* ks = keys + (off[tid] - c);
+        float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+        for (uint32_t i0 = 0; i0 < c; i0 += kGather) {
+            float4 tv[kGather];
 #pragma unroll
-                for (int j = 0; j < kGather; ++j)
-                    if (i0 + j < c) tv[j] = visit_tangent<SEG>(pair_tan, tan, k[i0 + j]);
+            for (int j = 0; j < kGather; ++j)
+                if (i0 + j < c) tv[j] = visit_tangent<SEG>(pair_tan, tan, ks[i0 + j]);
 #pragma unroll
-                for (int j = 0; j < kGather; ++j)
-                    if (i0 + j < c) {
-                        sx = __fadd_rn(sx, tv[j].x);
-                        sy = __fadd_rn(sy, tv[j].y);
-                        sz = __fadd_rn(sz, tv[j].z);
-                    }
-            }
-            tq[vi] = pack_tangent(sx, sy, sz, c);
+            for (int j = 0; j < kGather; ++j)
+                if (i0 + j < c) {
+                    sx = __fadd_rn(sx, tv[j].x);
+                    sy = __fadd_rn(sy, tv[j].y);
+                    sz = __fadd_rn(sz, tv[j].z);
+                }
         }
+        tq[vi] = pack_tangent(sx, sy, sz, c);
     }
 }
 
