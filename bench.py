@@ -412,6 +412,11 @@ def scale_section(args, dev, stream, flush):
         jobs.append(j)
         at += w
 
+    # the ray-packet variant for the 3840x2160 view (vkhr_autotune_raymarch), after one voxelization
+    ctx.voxelize_segments(dv.data_ptr(), dt.data_ptr(), di.data_ptr(), idx.shape[0], b, res, _abi.INDEX_REF_FP32,
+                          counts.data_ptr(), dens.data_ptr(), tq.data_ptr(), s)
+    ctx.normalize_densities(dens.data_ptr(), n, s)
+    tuned, tuned_ms = ctx.autotune_raymarch(p, dens.data_ptr(), tq.data_ptr(), rgba.data_ptr(), s)
     stages = {
         "voxelize": lambda: ctx.voxelize_segments(dv.data_ptr(), dt.data_ptr(), di.data_ptr(), idx.shape[0], b, res,
                                                   _abi.INDEX_REF_FP32, counts.data_ptr(), dens.data_ptr(),
@@ -442,6 +447,7 @@ def scale_section(args, dev, stream, flush):
         "batched_views_region_pixels": view_px,
         "batched_views_mpixels_per_s": view_px / (ms["raymarch_4_views_batched"] / 1e3) / 1e6,
         "visits": int(counts.sum(dtype=torch.int64).item()),
+        "autotune": {"raymarch_variant": tuned, "variant_ms": tuned_ms},
     }
     ctx.close()
     return out
@@ -830,7 +836,9 @@ RAY_AB = {
                  "4": "8x4 packets, each occupied density brick a warp's rays need staged into shared memory by one "
                       "TMA tensor copy",
                  "5": "8x4 packets sampling through the texture unit (3D array copy + hardware trilinear, "
-                      "8-bit weights)"},
+                      "8-bit weights)",
+                 "6": "variant 5's texture for the deep-shadow and AO samples only; the isosurface search reads "
+                      "memory"},
     "warm": "the volume L2-resident, as right after the voxelizer wrote it; cold: L2 flushed (512 MiB write) first",
 }
 
@@ -881,6 +889,8 @@ def raymarch_ab_section(args, dev, stream, flush):
         base = None
         rows = {}
         for v in range(_abi.RAYMARCH_VARIANTS):
+            if args.variant >= 0 and v not in (0, args.variant):
+                continue
             ctx.set_raymarch_variant(p.density_format, p.tangent_format, v)
             res_v = {}
             for mode in ("warm", "cold"):
@@ -1218,7 +1228,8 @@ def gb300_arm(args):
         "autotune": {"raymarch_variant": tuned, "variant_ms": tuned_ms,
                      "variants": ["8x4 tiles", "16x2 tiles", "4x8 tiles", "8x4 tiles, 64 registers",
                                   "8x4 tiles, density bricks staged in shared memory by TMA",
-                                  "8x4 tiles, density through the texture unit (not tuned: 8-bit filter weights)"]},
+                                  "8x4 tiles, density through the texture unit (not tuned: 8-bit filter weights)",
+                                  "8x4 tiles, shadow and AO samples through the texture unit (not tuned)"]},
     }
     if batched is not None:
         line["batched_speedup_vs_plain"] = round(batched["speedup_vs_plain"]["batched_graph"], 3)
@@ -1266,6 +1277,8 @@ def main():
     ap.add_argument("--no-scale", action="store_true", help="skip the 512^3 scale workload")
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiable workload")
     ap.add_argument("--no-composite", action="store_true", help="skip the hybrid-LoD compositing workload")
+    ap.add_argument("--variant", type=int, default=-1,
+                    help="raymarch_ab: time only variant 0 and this raymarch variant (profiling runs)")
     ap.add_argument("--section", default="all",
                     choices=["all", "frame", "batched", "scale", "diff", "schedule", "composite", "raymarch_ab"],
                     help="frame: the production frame only; batched: the multi-style comparison only; "

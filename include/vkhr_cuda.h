@@ -358,8 +358,11 @@ vkhr_status vkhr_raymarch(vkhr_ctx* ctx, const vkhr_raymarch_params* params,
  * texture unit: the call copies it into a 3D array of the context (LINEAR
  * filtering, border 0) and the hardware filters it with 8-bit weights, so its
  * pixels differ from the others by that filter's precision; u8 and FP32
- * densities only (variant 0 for counts).  The autotuner does not try it. */
-#define VKHR_RAYMARCH_VARIANTS 6
+ * densities only (variant 0 for counts).  6 = variant 5's texture for the
+ * shading's samples only (deep-shadow march and ambient-occlusion taps),
+ * while the isosurface search reads the texels in memory as variant 0 does.
+ * The autotuner tries neither 5 nor 6. */
+#define VKHR_RAYMARCH_VARIANTS 7
 
 /* Autotuner (no reference counterpart): times each variant of vkhr_raymarch
  * that computes the reference's pixels (0-4) on these inputs (one warm-up
@@ -367,7 +370,7 @@ vkhr_status vkhr_raymarch(vkhr_ctx* ctx, const vkhr_raymarch_params* params,
  * fastest in the context for params' texel formats; later vkhr_raymarch
  * calls with those formats use it.  Writes the choice to *chosen and, when
  * variant_ms is not NULL, the median time of each variant
- * (VKHR_RAYMARCH_VARIANTS floats; 0 for variant 5, not timed).  Synchronises
+ * (VKHR_RAYMARCH_VARIANTS floats; 0 for variants 5 and 6, not timed).  Synchronises
  * the stream. */
 vkhr_status vkhr_autotune_raymarch(vkhr_ctx* ctx, const vkhr_raymarch_params* params, const void* d_density,
                                    const void* d_tangent, float* d_rgba, int32_t* chosen, float* variant_ms,

@@ -36,7 +36,7 @@ def test_variants_render_the_same_image(ctx, oracle_lib):
     chosen, ms = ctx.autotune_raymarch(p, dd.data_ptr(), dt.data_ptr(), rgba.data_ptr())
     tuned = ms[:_abi.TUNED_RAYMARCH_VARIANTS]
     assert 0 <= chosen < _abi.TUNED_RAYMARCH_VARIANTS and min(tuned) > 0 and ms[chosen] == min(tuned)
-    assert ms[_abi.RAYMARCH_TEXTURE_VARIANT] == 0.0  # not a candidate
+    assert ms[_abi.RAYMARCH_TEXTURE_VARIANT] == 0.0 and ms[_abi.RAYMARCH_SHADE_TEXTURE_VARIANT] == 0.0  # not candidates
     assert np.array_equal(rgba.cpu().numpy(), imgs[0])
     with pytest.raises(VkhrError):
         ctx.set_raymarch_variant(p.density_format, p.tangent_format, _abi.RAYMARCH_VARIANTS)
@@ -105,14 +105,18 @@ def test_staged_variant_equals_l2_march(ctx, oracle_lib, fmt, tfmt, res, view, d
     compare_images(imgs[1][0], imgs[1][1], ref, rdepth, diag, label="staged variant", max_excluded=0.02)
 
 
+@pytest.mark.parametrize("variant", [_abi.RAYMARCH_TEXTURE_VARIANT, _abi.RAYMARCH_SHADE_TEXTURE_VARIANT])
 @pytest.mark.parametrize("fmt", [_abi.DENSITY_U8_UNORM, _abi.DENSITY_F32])
-def test_texture_unit_variant(ctx, oracle_lib, fmt):
+def test_texture_unit_variant(ctx, oracle_lib, fmt, variant):
     """Variant 5 samples the density through the texture unit (a 3D array with
-    hardware LINEAR filtering and border 0).  Its filter weights have 8
-    fractional bits, so it is measured, not required to match: the errors
-    against the FP64 oracle are printed, and bounded only loosely (the same
-    surfaces: coverage within 0.1, colour within 0.25).  Counts fall back to
-    the memory path, bit for bit."""
+    hardware LINEAR filtering and border 0), variant 6 only the shading's
+    (deep-shadow and AO) samples.  The filter's weights have 8 fractional
+    bits, which moves isosurface hits by a step here and there: variant 5
+    does not meet the raymarch bar (measured on a GB300: colour RMS 9e-3,
+    max 0.70) and neither is autotuned.  The errors against the FP64 oracle
+    and the share of pixels past the bar are printed and bounded loosely
+    (coverage within 0.05, colour RMS within 0.02).  Counts fall back to the
+    memory path, bit for bit."""
     import torch
 
     st, t, idx = style("hemi", 4096, 16)
@@ -126,7 +130,7 @@ def test_texture_unit_variant(ctx, oracle_lib, fmt):
     p = scene.make_params(b, res, 320, 240, raycast_steps=256.0, shadow_steps=32.0, isosurface=iso,
                           density_format=fmt)
     dd, dt = to_dev(dens, torch), to_dev(tq, torch)
-    ctx.set_raymarch_variant(fmt, p.tangent_format, _abi.RAYMARCH_TEXTURE_VARIANT)
+    ctx.set_raymarch_variant(fmt, p.tangent_format, variant)
     rgba = torch.full((p.height, p.width, 4), -7.0, dtype=torch.float32, device="cuda")
     ctx.raymarch(p, dd.data_ptr(), dt.data_ptr(), None, rgba.data_ptr(), None)
     torch.cuda.synchronize()
@@ -135,15 +139,23 @@ def test_texture_unit_variant(ctx, oracle_lib, fmt):
     ref, rdepth, diag = oracle_lib.raymarch(p, dens, tq, diag=True)
     from tests._helpers import image_errors
     rms, mx, excluded, emitted = image_errors(img, ref, diag)
-    print("texture-unit variant, density format %d: rms %s max %s (memory path bar: rms 1e-3, max 2e-2)"
-          % (fmt, np.round(rms, 5).tolist(), np.round(mx, 4).tolist()))
+    past = (np.abs(img.astype(np.float64) - ref)[..., :3].max(axis=2) > 2e-2) & (ref[..., 3] > 0)
+    print("texture-unit variant %d, density format %d: rms %s max %s, %d of %d fragments past 2e-2 "
+          "(memory path bar: rms 1e-3, max 2e-2)"
+          % (variant, fmt, np.round(rms, 5).tolist(), np.round(mx, 4).tolist(), int(past.sum()), emitted))
     assert (img != -7.0).all() and emitted > 1000
-    assert np.all(mx[:3] <= 0.25) and mx[3] <= 0.1
-    # counts cannot be filtered by the texture unit: variant 5 runs the memory path
+    assert np.all(rms[:3] <= 0.02) and mx[3] <= 0.05
+    # the texture unit's filter is not the exact trilinear: the images differ
+    ctx.set_raymarch_variant(fmt, p.tangent_format, 0)
+    mem = torch.empty_like(rgba)
+    ctx.raymarch(p, dd.data_ptr(), dt.data_ptr(), None, mem.data_ptr(), None)
+    torch.cuda.synchronize()
+    assert (mem.cpu().numpy() != img).any(), "variant %d rendered the memory path's image" % variant
+    # counts cannot be filtered by the texture unit: the variant runs the memory path
     pc = scene.make_params(b, res, 320, 240, raycast_steps=256.0, isosurface=1.0, density_format=_abi.DENSITY_U32_COUNT)
     dc = to_dev(c, torch)
     outs = []
-    for v in (0, _abi.RAYMARCH_TEXTURE_VARIANT):
+    for v in (0, variant):
         ctx.set_raymarch_variant(_abi.DENSITY_U32_COUNT, pc.tangent_format, v)
         o = torch.empty((pc.height, pc.width, 4), dtype=torch.float32, device="cuda")
         ctx.raymarch(pc, dc.data_ptr(), dt.data_ptr(), None, o.data_ptr(), None)

@@ -181,3 +181,89 @@ def test_batched_graph_replay(ctx, oracle_lib, segments):
             batch.check(oracle_lib, vertices=moved)
     finally:
         ctx.set_visit_budget(0)
+
+
+def test_batch_learns_one_walk_layout(oracle_lib):
+    """A batch without a budget counts its visits (two walks) and learns a
+    layout: a slice per visited brick of its count + 25%.  The next call of
+    the same shape walks once, writing every brick's entries into its slice.
+    A call whose bricks outgrow their slices fills again compactly and
+    learns the layout anew; under a budget (captured) the device takes that
+    fallback itself.  Every result is bit-exact."""
+    import torch
+
+    from vkhr_gb300 import _native
+
+    c = _native.Context(0)
+    styles = _styles(6, 8)
+    batch = _Batch(torch, oracle_lib, styles, True)
+    s = torch.cuda.current_stream().cuda_stream
+
+    def kernels():
+        """Kernel names of one unbudgeted call."""
+        batch.poison()
+        c.set_profiling(True)
+        c.voxelize_batched(True, batch.jobs, s)
+        c.check_status(s)
+        torch.cuda.synchronize()
+        names = [n for n, _ in c.profile()]
+        c.set_profiling(False)
+        return names
+
+    def walks(names):
+        direct = sum(1 for n in names if n.startswith("(bin_kernel<false") and n.endswith("true>)"))
+        counting = sum(1 for n in names if n.startswith("(bin_kernel<false") and not n.endswith("true>)"))
+        fill = sum(1 for n in names if n.startswith("(bin_kernel<true"))
+        return direct, counting, fill, sum(1 for n in names if "layout_kernel" in n)
+
+    def move(contract):
+        """Every style's vertices pulled towards its box centre (same bounds)."""
+        out = []
+        for k, ((st, t, idx), res, mode) in enumerate(styles):
+            lo, hi = st.vertices.min(axis=0), st.vertices.max(axis=0)
+            v = st.vertices if contract == 1.0 else ((st.vertices - 0.5 * (lo + hi)) * contract + 0.5 * (lo + hi))
+            v = v.astype(np.float32)
+            batch.keep[3 * k].copy_(torch.from_numpy(v))
+            out.append(v)
+        torch.cuda.synchronize()
+        return out
+
+    try:
+        names = kernels()                                  # counted: two walks, learns the layout
+        assert walks(names) == (0, 1, 1, 1), names
+        batch.check(oracle_lib)
+        names = kernels()                                  # the same shape: one walk
+        assert walks(names) == (1, 0, 0, 0), names
+        batch.check(oracle_lib)
+        moved = move(0.4)                                  # crowded bricks outgrow their slices
+        names = kernels()
+        assert walks(names) == (1, 0, 1, 1), names         # compact fill, layout learned again
+        batch.check(oracle_lib, vertices=moved)
+        names = kernels()
+        assert walks(names) == (1, 0, 0, 0), names
+        batch.check(oracle_lib, vertices=moved)
+
+        # under a budget, captured: one walk, the fill a device-side fallback
+        visits = sum(int(x.cpu().numpy().view(np.uint32).sum(dtype=np.uint64)) for x, _, _ in batch.outs)
+        c.set_visit_budget(4 * visits + 4096)
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            c.voxelize_batched(True, batch.jobs, side.cuda_stream)  # sizes the scratch for the budget
+        c.check_status(side.cuda_stream)
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            c.voxelize_batched(True, batch.jobs, torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        for contract in (0.4, 1.0, 0.4):                   # fits; outgrows (fallback); fits
+            moved = move(contract)
+            batch.poison()
+            graph.replay()
+            torch.cuda.synchronize()
+            c.check_status(None)
+            batch.check(oracle_lib, vertices=moved)
+        del graph
+    finally:
+        c.set_visit_budget(0)
+        c.close()

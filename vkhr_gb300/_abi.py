@@ -32,9 +32,10 @@ STATUS_NAMES = {
 INDEX_REF_FP32 = 0
 INDEX_EXACT = 1
 
-RAYMARCH_VARIANTS = 6
-TUNED_RAYMARCH_VARIANTS = 5  # variants 0-4 compute the same pixels; 5 samples through the texture unit
+RAYMARCH_VARIANTS = 7
+TUNED_RAYMARCH_VARIANTS = 5  # variants 0-4 compute the same pixels; 5 and 6 sample through the texture unit
 RAYMARCH_TEXTURE_VARIANT = 5
+RAYMARCH_SHADE_TEXTURE_VARIANT = 6  # the texture unit for the shadow and AO samples only
 MAX_AO_DIRECTIONS = 32
 
 FILTER_MAX = 0

@@ -32,10 +32,12 @@ enum {
     WORD_BRICK_QUEUE = 8,       // brick path: next entry of the occupied-brick list
     WORD_BRICK_LIST = 9,        // brick path: occupied bricks resolved in shared memory
     WORD_BHEAVY_BIG = 10,       // brick path: crowded voxels above kCrowdWarpMax visits (listed from the back)
+    WORD_DIRECT_OVERFLOW = 11,  // one-walk call: a brick outgrew its fixed slice (the fill pass lays it out)
     WORD_NORM = 12,             // normalize: min, max (2 slots); words below are cleared per voxelization
     WORD_AABB = 14,             // bounding-box scratch (8 slots)
     WORD_RAY_QUEUE = 22,        // batched raymarch: next tile
-    WORD_COUNT = 24
+    WORD_LAYOUT_CURSOR = 24,    // voxelizer: slice cursor of a learned batch layout
+    WORD_COUNT = 26
 };
 
 // Visit total of an earlier unbudgeted one-style segment voxelization, by
@@ -58,6 +60,11 @@ struct vkhr_ctx {
     size_t d_gather_cap;
     void* slots;               // voxelizer: the fixed per-brick slices of one-walk calls
     size_t slots_cap;          // (in 8-byte units)
+    uint2* layout;             // voxelizer: learned {first slot, capacity} per brick of a batch's one walk
+    size_t layout_cap;         // (in bricks)
+    uint64_t layout_shape;     // the batch shape it was learned for (0: none)
+    uint32_t layout_bricks;    // bricks of that batch
+    uint64_t layout_slots;     // slots its slices span
     // grow-only scratch (capacities in elements)
     uint32_t* brick_runs;      // voxelizer: visits and visit-list cursor per brick (2 x bricks)
     uint32_t* brick_visits;
@@ -67,8 +74,6 @@ struct vkhr_ctx {
     size_t items_cap;
     uint32_t* brick_list;      // voxelizer: occupied bricks of the shared-memory path
     size_t brick_list_cap;
-    float4* pair_rec;          // voxelizer: per index pair {root.xyz, steps}, {direction.xyz, 0}
-    size_t pair_rec_cap;
     float4* pair_tan;          // voxelizer: per index pair, the tangent of its first vertex
     size_t pair_tan_cap;
     uint32_t* hkeys;           // voxelizer: key scratch (crowded voxels, bricks above the shared-memory cap)

@@ -158,8 +158,8 @@ vkhr_status vkhr_destroy(vkhr_ctx* ctx)
     if (!ctx) return VKHR_OK;
     cudaSetDevice(ctx->device);
     cudaDeviceSynchronize();
-    void* bufs[] = {ctx->brick_runs, ctx->items, ctx->brick_list, ctx->pair_rec, ctx->pair_tan, ctx->hkeys, ctx->hdesc,
-                    ctx->d_jobs, ctx->d_rjobs, ctx->g_acc, ctx->slots, ctx->d_gather, ctx->comp};
+    void* bufs[] = {ctx->brick_runs, ctx->items, ctx->brick_list, ctx->pair_tan, ctx->hkeys, ctx->hdesc,
+                    ctx->d_jobs, ctx->d_rjobs, ctx->g_acc, ctx->slots, ctx->layout, ctx->d_gather, ctx->comp};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (ctx->occ) cudaFree(ctx->occ);

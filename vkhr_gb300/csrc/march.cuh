@@ -44,9 +44,13 @@ struct RayConsts {
 };
 
 // Where the march's density samples come from: the texels in memory with the
-// software trilinear below (every variant but one), or the texture unit's
-// hardware trilinear filter, whose weights have 8 fractional bits.
-constexpr int kSampleMemory = 0, kSampleTexture = 1;
+// software trilinear below, or the texture unit's hardware trilinear filter,
+// whose weights have 8 fractional bits -- for every sample (kSampleTexture),
+// or for the shadow and ambient-occlusion samples of the shading only while
+// the isosurface search reads memory (kSampleShadeTexture).
+constexpr int kSampleMemory = 0, kSampleTexture = 1, kSampleShadeTexture = 2;
+__host__ __device__ constexpr int march_source(int src) { return src == kSampleTexture ? kSampleTexture : kSampleMemory; }
+__host__ __device__ constexpr int shade_source(int src) { return src == kSampleMemory ? kSampleMemory : kSampleTexture; }
 
 constexpr int kBrick = 8;          // occupancy brick edge in texel cells
 constexpr float kSkipMargin = 0.01f; // texels kept between a predicted sample and a brick face
@@ -620,7 +624,7 @@ __device__ __forceinline__ void shade_fragment(const RayConsts& c, const typenam
                     t = n >= 1.0f ? fmaf(n, sstep, t) : t + sstep;
                     continue;
                 }
-                strands += density_at<DF, SRC>(c, dens, Q) * c.thickness;
+                strands += density_at<DF, shade_source(SRC)>(c, dens, Q) * c.thickness;
                 t += sstep;
             }
             const float os = powf(1.0f - c.alpha, strands);
@@ -633,7 +637,7 @@ __device__ __forceinline__ void shade_fragment(const RayConsts& c, const typenam
             if (c.ao_n > 0) { // the directional extension
                 for (int i = 0; i < c.ao_n; ++i) {
                     const Vec3 q = v3(surf.x + c.ao_off[i][0], surf.y + c.ao_off[i][1], surf.z + c.ao_off[i][2]);
-                    dsum += fminf(density_at<DF, SRC>(c, dens, q), c.ao_max);
+                    dsum += fminf(density_at<DF, shade_source(SRC)>(c, dens, q), c.ao_max);
                 }
                 taps = (float)c.ao_n;
             } else {
@@ -644,7 +648,7 @@ __device__ __forceinline__ void shade_fragment(const RayConsts& c, const typenam
                     for (float y = -kr; y <= kr; y += 1.0f)
                         for (float x = -kr; x <= kr; x += 1.0f) {
                             const Vec3 q = v3(surf.x + x * sc.x, surf.y + y * sc.y, surf.z + z * sc.z);
-                            dsum += fminf(density_at<DF, SRC>(c, dens, q), c.ao_max);
+                            dsum += fminf(density_at<DF, shade_source(SRC)>(c, dens, q), c.ao_max);
                         }
                 taps = c.ao_kernel * c.ao_kernel * c.ao_kernel;
             }
@@ -713,7 +717,7 @@ __device__ __forceinline__ void march_pixel(const RayConsts& c, const typename D
                 if (TAPE) k += n >= 1.0f ? (uint32_t)n : 1u;
                 continue;
             }
-            const float rho = density_at<DF, SRC>(c, dens, P);
+            const float rho = density_at<DF, march_source(SRC)>(c, dens, P);
             acc += rho;
             if (rho != 0.0f) {
                 if (acc <= c.iso) surf = P;

@@ -34,8 +34,9 @@ struct RayVariant {
 constexpr int kPacketVariants = 4;   // raymarch_kernel instantiations; variant 4 is the staged kernel
 constexpr int kStagedVariant = 4;
 constexpr int kTextureVariant = 5;   // the texture unit's filter: other pixels, never autotuned
+constexpr int kShadeTextureVariant = 6; // the same filter for the shading's samples only
 constexpr int kTunedVariants = 5;    // the variants that compute the same pixels
-static_assert(VKHR_RAYMARCH_VARIANTS == kTextureVariant + 1, "variant table");
+static_assert(VKHR_RAYMARCH_VARIANTS == kShadeTextureVariant + 1, "variant table");
 constexpr RayVariant kRayVariants[kPacketVariants] = {{8, 6}, {16, 6}, {4, 6}, {8, 8}};
 
 template <int DF, int TF, int TW = 8, int MINB = 6, int SRC = kSampleMemory>
@@ -53,7 +54,7 @@ raymarch_kernel(const __grid_constant__ RayConsts c, const typename DensityTexel
     const size_t at = (size_t)py * c.W + px;
     float4 out;
     float out_depth;
-    march_pixel<DF, TF>(c, dens, tang, occ, depth_in ? depth_in + at : nullptr, px, py, out, out_depth);
+    march_pixel<DF, TF, false, SRC>(c, dens, tang, occ, depth_in ? depth_in + at : nullptr, px, py, out, out_depth);
     rgba[at] = out;
     if (depth_out) depth_out[at] = out_depth;
 }
@@ -537,7 +538,7 @@ vkhr_status launch(vkhr_ctx* ctx, const RayConsts& c, const void* dens, const vo
         }
         v = 0; // TMA cannot address this grid: the default packets
     }
-    if (v == kTextureVariant) {
+    if (v == kTextureVariant || v == kShadeTextureVariant) {
         bool ok = false;
         vkhr_status ts = texture_density<DF>(ctx, c, dens, st, ok);
         if (ts != VKHR_OK) return ts;
@@ -546,8 +547,13 @@ vkhr_status launch(vkhr_ctx* ctx, const RayConsts& c, const void* dens, const vo
             ct.tex = (unsigned long long)ctx->tex_obj;
             const dim3 grid((rect[2] + kTileW * kWarpsX - 1) / (kTileW * kWarpsX),
                             (rect[3] + kTileH * kWarpsY - 1) / (kTileH * kWarpsY));
-            VKHR_LAUNCH(ctx, (raymarch_kernel<DF, TF, 8, 6, kSampleTexture>), grid, block, 0, st, ct,
-                        (const typename DensityTexel<DF>::T*)dens, tang, ctx->occ, din, out, dout, x0, y0, x1, y1);
+            const typename DensityTexel<DF>::T* d = (const typename DensityTexel<DF>::T*)dens;
+            if (v == kTextureVariant)
+                VKHR_LAUNCH(ctx, (raymarch_kernel<DF, TF, 8, 6, kSampleTexture>), grid, block, 0, st, ct, d, tang,
+                            ctx->occ, din, out, dout, x0, y0, x1, y1);
+            else
+                VKHR_LAUNCH(ctx, (raymarch_kernel<DF, TF, 8, 6, kSampleShadeTexture>), grid, block, 0, st, ct, d, tang,
+                            ctx->occ, din, out, dout, x0, y0, x1, y1);
             return background ? vkhr_join_side(ctx, st) : VKHR_OK;
         }
         v = 0; // integer counts: the default packets

@@ -210,25 +210,6 @@ __device__ __forceinline__ void seg_advance(Seg& s)
     for (int a = 0; a < 3; ++a) s.root[a] = __fadd_rn(s.root[a], s.dir[a]); // root += direction
 }
 
-// The set-up of a pair, stored once by the counting bin pass.
-__device__ __forceinline__ void seg_store(const Seg& s, float4* rec)
-{
-    rec[0] = make_float4(s.root[0], s.root[1], s.root[2], __uint_as_float(s.n));
-    rec[1] = make_float4(s.dir[0], s.dir[1], s.dir[2], 0.0f);
-}
-
-__device__ __forceinline__ void seg_load(const float4* __restrict__ rec, Seg& s)
-{
-    const float4 a = __ldg(rec), b = __ldg(rec + 1);
-    s.root[0] = a.x;
-    s.root[1] = a.y;
-    s.root[2] = a.z;
-    s.n = __float_as_uint(a.w);
-    s.dir[0] = b.x;
-    s.dir[1] = b.y;
-    s.dir[2] = b.z;
-}
-
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
 // ---- brick path -----------------------------------------------------------------
@@ -260,19 +241,28 @@ constexpr uint64_t kDirectBytes = 8ull << 30; // fixed per-brick slices of a one
 // or written as (key, local voxel) entries into the brick's slice of the
 // visit list.
 // DIRECT (a counting walk that also fills): the brick's count is its cursor
-// and the entries go to the brick's fixed slice of entries_cap entries; a
-// run past the slice is counted but not written (the caller sees the
-// brick's count above the capacity and fills again in the compact layout).
+// and the entries go to the brick's fixed slice -- [b * entries_cap, + entries_cap)
+// or, with a learned layout, {first slot, capacity} = layout[b]; a run past
+// the slice is counted but not written, and raises the call's overflow word
+// (the fill pass then lays the call out compactly from the exact counts).
 template <bool FILL, bool PACK, bool DIRECT = false>
 __device__ __forceinline__ void emit_run(uint32_t b, uint32_t key, uint64_t locals, uint32_t len, uint32_t* visits,
                                          uint32_t* cursor, typename Entry<PACK>::T* entries, size_t entries_cap,
-                                         unsigned& status)
+                                         const uint2* __restrict__ layout, unsigned long long* words, unsigned& status)
 {
     if (DIRECT) {
         const uint32_t at = atomicAdd(visits + b, len);
-        if ((uint64_t)at + len <= entries_cap) {
-            typename Entry<PACK>::T* e = entries + (size_t)b * entries_cap + at;
+        uint64_t first = (uint64_t)b * entries_cap, cap = entries_cap;
+        if (layout) {
+            const uint2 sl = __ldg(layout + b);
+            first = sl.x;
+            cap = sl.y;
+        }
+        if ((uint64_t)at + len <= cap) {
+            typename Entry<PACK>::T* e = entries + first + at;
             for (uint32_t j = 0; j < len; ++j) e[j] = Entry<PACK>::make(key, (uint32_t)(locals >> (9 * j)) & 511u);
+        } else {
+            *reinterpret_cast<volatile unsigned long long*>(words + WORD_DIRECT_OVERFLOW) = 1ull;
         }
     } else if (!FILL) {
         atomicAdd(visits + b, len); // fire-and-forget reduction
@@ -291,16 +281,16 @@ __device__ __forceinline__ void emit_run(uint32_t b, uint32_t key, uint64_t loca
 // job0 (constant bank, free to read in the visit loop).  Otherwise the job
 // table is copied into shared memory and each item looks its style up.
 // DIRECT (with FILL = false): the counting walk also writes the entries
-// into fixed per-brick slices of entries_cap entries (see emit_run).
+// into fixed per-brick slices (see emit_run).
 template <bool FILL, bool SEG, bool PACK, bool SINGLE, bool SPREAD = false, bool DIRECT = false>
 __global__ void bin_kernel(const __grid_constant__ VoxJob job0, const VoxJob* __restrict__ jobs, int nj,
-                           uint32_t total_items, float4* pair_rec, float4* pair_tan, uint32_t* visits,
-                           uint32_t* cursor, void* entries_raw, size_t entries_cap, unsigned long long* words,
-                           uint32_t skip_if_fits)
+                           uint32_t total_items, float4* pair_tan, uint32_t* visits,
+                           uint32_t* cursor, void* entries_raw, size_t entries_cap, const uint2* __restrict__ layout,
+                           unsigned long long* words, int fallback)
 {
-    // a budgeted one-walk call's fill: needed only when a brick outgrew the
-    // fixed slices of capacity skip_if_fits (0: always fill)
-    if (FILL && skip_if_fits && words[WORD_MAX_BRICK_VISITS] <= skip_if_fits) return;
+    // a budgeted one-walk call's fill (fallback != 0): needed only when a
+    // brick outgrew its fixed slice
+    if (FILL && fallback && !words[WORD_DIRECT_OVERFLOW]) return;
     typename Entry<PACK>::T* entries = reinterpret_cast<typename Entry<PACK>::T*>(entries_raw);
     // the job table in shared memory (nj * (sizeof(VoxJob) + 4) bytes of dynamic shared memory)
     extern __shared__ __align__(16) unsigned char bin_smem[];
@@ -331,17 +321,13 @@ __global__ void bin_kernel(const __grid_constant__ VoxJob job0, const VoxJob* __
         const Grid& g = J.g;
         const uint32_t p = (uint32_t)q - J.item_base;
         if (SEG) {
+            // the pair's set-up (the fill pass recomputes it: the same bytes as a stored record, no store)
             Seg s;
-            if (FILL) {
-                seg_load(pair_rec + 2 * q, s);
-            } else {
-                const uint2 ij = __ldg(J.pairs + p);
-                seg_setup(g, J.v, ij, s, status);
-                seg_store(s, pair_rec + 2 * q);
-                if (J.tan) // tangents[indices[i]]: every visit of the pair adds this one
-                    pair_tan[q] = make_float4(__ldg(J.tan + 3 * (size_t)ij.x), __ldg(J.tan + 3 * (size_t)ij.x + 1),
-                                              __ldg(J.tan + 3 * (size_t)ij.x + 2), 0.0f);
-            }
+            const uint2 ij = __ldg(J.pairs + p);
+            seg_setup(g, J.v, ij, s, status);
+            if (!FILL && J.tan) // tangents[indices[i]]: every visit of the pair adds this one
+                pair_tan[q] = make_float4(__ldg(J.tan + 3 * (size_t)ij.x), __ldg(J.tan + 3 * (size_t)ij.x + 1),
+                                          __ldg(J.tan + 3 * (size_t)ij.x + 2), 0.0f);
             uint32_t cur = kNoBrick, len = 0;
             uint64_t locals = 0;
             for (uint32_t k = 0; k < s.n; ++k) {
@@ -353,7 +339,7 @@ __global__ void bin_kernel(const __grid_constant__ VoxJob job0, const VoxJob* __
                 } else {
                     if (len)
                         emit_run<FILL, PACK, DIRECT>(J.brick_base + cur, p, locals, len, visits, cursor, entries,
-                                                     entries_cap, status);
+                                                     entries_cap, layout, words, status);
                     cur = ok ? o.brick : kNoBrick;
                     len = ok ? 1u : 0u;
                     locals = ok ? (uint64_t)o.local : 0ull;
@@ -362,12 +348,12 @@ __global__ void bin_kernel(const __grid_constant__ VoxJob job0, const VoxJob* __
             }
             if (len)
                 emit_run<FILL, PACK, DIRECT>(J.brick_base + cur, p, locals, len, visits, cursor, entries, entries_cap,
-                                             status);
+                                             layout, words, status);
         } else {
             Visit o;
             if (vertex_visit(g, J.v, p, o))
                 emit_run<FILL, PACK>(J.brick_base + o.brick, p, (uint64_t)o.local, 1u, visits, cursor, entries, entries_cap,
-                               status);
+                                     layout, words, status);
         }
     }
     if (status) atomicOr(words + WORD_STATUS, (unsigned long long)status);
@@ -440,6 +426,64 @@ __global__ void __launch_bounds__(kRangeThreads) bin_ranges_kernel(const uint32_
             const unsigned below = (1u << lane) - 1u;
             if (small) list[at + __popc(m & below)] = (uint32_t)i;
             if (big) list[nb - 1u - (atb + __popc(mb & below))] = (uint32_t)i;
+        }
+        __syncthreads();
+    }
+}
+
+// Slice capacity a learned batch layout gives a brick the counted call saw
+// `v` visits in: v + 25% + 32, rounded up to 8 entries (unvisited: none).
+__host__ __device__ __forceinline__ uint32_t layout_slice(uint32_t v)
+{
+    return v ? (v + (v >> 2) + 32u + 7u) & ~7u : 0u;
+}
+
+// The learned layout of a batch's one-walk calls from a counted call's
+// per-brick visits: {first slot, capacity} per brick, the slices disjoint
+// (tiles of kRangeThreads * kRangeItems bricks take their ranges with one
+// atomic each, so the slices of a tile are contiguous, the tiles in any
+// order).  The next calls with the same bricks walk once, each brick's
+// entries going to its slice.
+__global__ void __launch_bounds__(kRangeThreads) layout_kernel(const uint32_t* __restrict__ visits, uint32_t nb,
+                                                             uint2* __restrict__ layout, unsigned long long* words)
+{
+    __shared__ uint32_t warp_sums[kRangeThreads / 32];
+    __shared__ uint32_t block_base;
+    const uint32_t tile = kRangeThreads * kRangeItems;
+    for (uint64_t base = (uint64_t)blockIdx.x * tile; base < nb; base += (uint64_t)gridDim.x * tile) {
+        uint32_t c[kRangeItems];
+        uint32_t sum = 0;
+#pragma unroll
+        for (int j = 0; j < kRangeItems; ++j) {
+            const uint64_t i = base + (uint64_t)j * kRangeThreads + threadIdx.x;
+            c[j] = i < nb ? layout_slice(__ldg(visits + i)) : 0u;
+            sum += c[j];
+        }
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        uint32_t incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) warp_sums[warp] = incl;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t run = 0;
+            for (int w = 0; w < kRangeThreads / 32; ++w) {
+                const uint32_t t = warp_sums[w];
+                warp_sums[w] = run;
+                run += t;
+            }
+            block_base = run ? (uint32_t)atomicAdd(words + WORD_LAYOUT_CURSOR, (unsigned long long)run) : 0u;
+        }
+        __syncthreads();
+        uint32_t start = block_base + warp_sums[warp] + (incl - sum);
+#pragma unroll
+        for (int j = 0; j < kRangeItems; ++j) {
+            const uint64_t i = base + (uint64_t)j * kRangeThreads + threadIdx.x;
+            if (i < nb) layout[i] = make_uint2(start, c[j]);
+            start += c[j];
         }
         __syncthreads();
     }
@@ -745,8 +789,9 @@ __device__ __forceinline__ void resolve_brick(const VoxJob& J, const Grid& g, ui
 // takes the bricks of up to kBrickCap visits (keys sorted in shared memory,
 // list from the front); BIG = true the others (keys sorted into a slice of
 // the global key scratch, list from the back).  A brick's entries are the
-// slice its fill reserved (compact layout), or with direct_cap > 0 the fixed
-// slice [brick * direct_cap, + count) of a one-walk call.  The next brick's queue slot
+// slice its fill reserved (compact layout), or the fixed slice of a one-walk
+// call: [brick * direct_cap, + count), or with a learned layout
+// [layout[brick].x, + count).  The next brick's queue slot
 // and bounds are fetched while the current one is processed, and the entry
 // passes keep kBrickUnroll loads in flight per thread.
 constexpr int kBrickUnroll = 4;
@@ -756,23 +801,26 @@ __global__ void __launch_bounds__(kBrickThreads, 2)
 brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__ pair_tan_all,
              const uint32_t* __restrict__ visits, const uint32_t* __restrict__ cursor, const uint32_t* __restrict__ list,
              uint32_t list_n, const void* __restrict__ entries_raw, size_t entries_cap,
-             const void* __restrict__ slots_raw, uint32_t direct_cap, int speculative, uint4* hdesc, size_t hdesc_cap,
-             uint32_t* hkeys, size_t hkeys_cap, unsigned long long* words)
+             const void* __restrict__ slots_raw, size_t slots_n, uint32_t direct_cap, const uint2* __restrict__ layout,
+             int speculative, uint4* hdesc, size_t hdesc_cap, uint32_t* hkeys, size_t hkeys_cap,
+             unsigned long long* words)
 {
     typedef Entry<PACK> E;
     typedef typename E::T ET;
     // The layout, chosen once into shared memory (kept out of registers).
-    // speculative: a budgeted one-walk call, whose largest brick only the
-    // device knows -- the fixed slices hold every brick's entries when it
-    // fits their capacity, else the fill pass has laid them out compactly.
+    // speculative: a budgeted one-walk call, whose overflow only the device
+    // knows -- the fixed slices hold every brick's entries when none outgrew
+    // its slice, else the fill pass has laid them out compactly.
     __shared__ const ET* s_entries;
+    __shared__ const uint2* s_layout;
     __shared__ unsigned long long s_entries_cap;
     __shared__ uint32_t s_dcap;
     if (threadIdx.x == 0) {
-        const uint32_t d = speculative && words[WORD_MAX_BRICK_VISITS] > direct_cap ? 0u : direct_cap;
-        s_dcap = d;
-        s_entries = reinterpret_cast<const ET*>(d ? slots_raw : entries_raw);
-        s_entries_cap = d ? (unsigned long long)list_n * d : (unsigned long long)entries_cap; // fixed slices
+        const bool direct = (direct_cap || layout) && !(speculative && words[WORD_DIRECT_OVERFLOW]);
+        s_dcap = direct && !layout ? direct_cap : 0u;
+        s_layout = direct ? layout : nullptr;
+        s_entries = reinterpret_cast<const ET*>(direct ? slots_raw : entries_raw);
+        s_entries_cap = direct ? (unsigned long long)slots_n : (unsigned long long)entries_cap;
     }
     extern __shared__ uint32_t sm[];
     uint32_t* cnt = sm;                       // visits per local voxel
@@ -780,7 +828,7 @@ brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__
     uint32_t* warp_sums = sm + 2 * kBrickThreads;
     uint32_t* wlist = sm + 2 * kBrickThreads + 32;             // voxels for the warp sort
     uint32_t* keys = wlist + kBrickThreads;                    // (BIG = false only)
-    __shared__ uint32_t s_gb, s_nv, s_start, wcount, s_job, s_hb;
+    __shared__ uint32_t s_gb, s_nv, s_start, s_cap, wcount, s_job, s_hb;
     __shared__ uint32_t s_brick_base[kMaxJobs];
     load_bases(jobs, nj, nullptr, s_brick_base);
     const int tid = threadIdx.x;
@@ -788,13 +836,27 @@ brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__
     const uint32_t listed = (uint32_t)words[BIG ? WORD_BIG_LIST : WORD_BRICK_LIST];
     unsigned long long* queue = words + (BIG ? WORD_BIG_QUEUE : WORD_BRICK_QUEUE);
     // thread 0 holds the next brick: its queue slot, then its id and bounds
-    uint32_t nq = 0, ngb = 0, nnv = 0, nstart = 0;
+    uint32_t nq = 0, ngb = 0, nnv = 0, nstart = 0, ncap = 0;
+    // a brick's entries: its first one and the capacity of its slice
+    auto bounds = [&](uint32_t b, uint32_t nv) {
+        if (s_layout) {
+            const uint2 sl = s_layout[b];
+            nstart = sl.x;
+            ncap = sl.y;
+        } else if (s_dcap) {
+            nstart = b * s_dcap;
+            ncap = s_dcap;
+        } else {
+            nstart = cursor[b] - nv;
+            ncap = 0xffffffffu;
+        }
+    };
     if (tid == 0) {
         nq = (uint32_t)atomicAdd(queue, 1ull);
         if (nq < listed) {
             ngb = BIG ? list[list_n - 1 - nq] : list[nq];
             nnv = visits[ngb];
-            nstart = s_dcap ? ngb * s_dcap : cursor[ngb] - nnv;
+            bounds(ngb, nnv);
         }
     }
     for (;;) {
@@ -802,6 +864,7 @@ brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__
             s_gb = nq < listed ? ngb : 0xffffffffu;
             s_nv = nnv;
             s_start = nstart;
+            s_cap = ncap;
             wcount = 0;
             if (nq < listed) {
                 s_job = (uint32_t)find_job(s_brick_base, nj, ngb);
@@ -814,14 +877,14 @@ brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__
         const uint32_t gb = s_gb, nv = s_nv, start = s_start;
         if (gb == 0xffffffffu) break;
         const bool skip = (uint64_t)start + nv > s_entries_cap ||               // visit budget exceeded
-                          (s_dcap && nv > s_dcap) ||                            // past its fixed slice
+                          nv > s_cap ||                                         // past its fixed slice
                           (TANG && BIG && (uint64_t)s_hb + nv > hkeys_cap);     // key scratch exhausted
         if (skip) {
             status |= VKHR_DEV_LIST_OVERFLOW;
             if (tid == 0 && nq < listed) {
                 ngb = BIG ? list[list_n - 1 - nq] : list[nq];
                 nnv = visits[ngb];
-                nstart = s_dcap ? ngb * s_dcap : cursor[ngb] - nnv;
+                bounds(ngb, nnv);
             }
         } else {
             const VoxJob& J = jobs[s_job];
@@ -842,7 +905,7 @@ brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__
             if (tid == 0 && nq < listed) { // the next brick's bounds, while this one's passes run
                 ngb = BIG ? list[list_n - 1 - nq] : list[nq];
                 nnv = visits[ngb];
-                nstart = s_dcap ? ngb * s_dcap : cursor[ngb] - nnv;
+                bounds(ngb, nnv);
             }
             __syncthreads();
             if (TANG) {
@@ -1305,7 +1368,8 @@ void learn_visits(vkhr_ctx* ctx, const vkhr_voxel_job& j, bool tang, uint64_t vi
 
 template <bool SEG, bool TANG, bool PACK>
 vkhr_status launch_brick(vkhr_ctx* ctx, const VoxJob* d_jobs, int nj, uint32_t total_bricks, cudaStream_t st,
-                         unsigned blocks, size_t entries_cap, size_t keys_cap, uint32_t direct_cap, bool speculative)
+                         unsigned blocks, size_t entries_cap, size_t keys_cap, uint32_t direct_cap,
+                         const uint2* layout, size_t slots_n, bool speculative)
 {
     const int spec = speculative ? 1 : 0;
     // bricks above kBrickCap (their keys go to the global scratch) on the side
@@ -1316,13 +1380,14 @@ vkhr_status launch_brick(vkhr_ctx* ctx, const VoxJob* d_jobs, int nj, uint32_t t
     if (s != VKHR_OK) return s;
     VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG, true, PACK>), (unsigned)ctx->sm_count * 2, kBrickThreads, small, ctx->side,
                 d_jobs, nj, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->brick_list, total_bricks,
-                ctx->items, entries_cap, ctx->slots, direct_cap, spec, ctx->hdesc, ctx->hdesc_cap, ctx->hkeys, keys_cap,
-                ctx->d_words);
+                ctx->items, entries_cap, ctx->slots, slots_n, direct_cap, layout, spec, ctx->hdesc, ctx->hdesc_cap,
+                ctx->hkeys, keys_cap, ctx->d_words);
     VKHR_CUDA_TRY(ctx, cudaFuncSetAttribute(brick_kernel<SEG, TANG, false, PACK>,
                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG, false, PACK>), blocks, kBrickThreads, smem, st, d_jobs, nj,
                 ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->brick_list, total_bricks, ctx->items,
-                entries_cap, ctx->slots, direct_cap, spec, ctx->hdesc, ctx->hdesc_cap, ctx->hkeys, keys_cap, ctx->d_words);
+                entries_cap, ctx->slots, slots_n, direct_cap, layout, spec, ctx->hdesc, ctx->hdesc_cap, ctx->hkeys, keys_cap,
+                ctx->d_words);
     return VKHR_OK;
 }
 
@@ -1351,6 +1416,50 @@ vkhr_status make_job(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job& in, Vox
     out.tq = reinterpret_cast<uint32_t*>(in.d_tangents);
     out.n_in = n_in;
     out.zero_base = 0;
+    return VKHR_OK;
+}
+
+// The shape a learned batch layout is kept for: the styles' grids and pair
+// counts, tangents requested, entry size.
+uint64_t batch_shape(const VoxJob* jobs, int nj, bool tang, bool pack)
+{
+    uint64_t h = 1469598103934665603ull; // FNV-1a over the fields
+    auto mix = [&h](uint64_t x) { h = (h ^ x) * 1099511628211ull; };
+    mix((uint64_t)nj);
+    mix(tang ? 1 : 0);
+    mix(pack ? 1 : 0);
+    for (int j = 0; j < nj; ++j) {
+        mix(jobs[j].g.w);
+        mix(jobs[j].g.h);
+        mix(jobs[j].g.d);
+        mix(jobs[j].n_in);
+    }
+    return h | 1u; // 0 means "no layout"
+}
+
+// Learns a batch's one-walk layout from the exact per-brick visits of this
+// call's counting walk (queued after it on st): each visited brick gets a
+// slice of layout_slice(visits) entries.  The slices span at most
+// visits + visits / 4 + 39 per visited brick; a batch whose span would pass
+// kDirectBytes (or 2^32 entries), or a context with live frame graphs, keeps
+// two walks.
+vkhr_status learn_layout(vkhr_ctx* ctx, uint64_t shape, uint32_t nb, uint64_t visits, uint64_t visited,
+                         size_t entry_bytes, cudaStream_t st)
+{
+    ctx->layout_shape = 0;
+    const uint64_t slots = visits + visits / 4 + 39 * visited + 8;
+    if (slots >= (1ull << 32) || slots * entry_bytes > kDirectBytes || ctx->live_graphs) return VKHR_OK;
+    vkhr_status s = vkhr_reserve(ctx, (void**)&ctx->layout, &ctx->layout_cap, nb ? nb : 1, sizeof(uint2));
+    if (s != VKHR_OK) return s;
+    s = vkhr_reserve(ctx, (void**)&ctx->slots, &ctx->slots_cap, (slots * entry_bytes + 7) / 8, sizeof(uint2));
+    if (s != VKHR_OK) return s;
+    VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_words + WORD_LAYOUT_CURSOR, 0, sizeof(unsigned long long), st));
+    const unsigned blocks = std::min(vkhr_blocks(nb, kRangeThreads * kRangeItems), (unsigned)ctx->sm_count * 8);
+    VKHR_LAUNCH(ctx, layout_kernel, blocks, kRangeThreads, 0, st, ctx->brick_visits, nb, ctx->layout, ctx->d_words);
+    VKHR_CUDA_TRY(ctx, cudaGetLastError());
+    ctx->layout_shape = shape;
+    ctx->layout_bricks = nb;
+    ctx->layout_slots = slots;
     return VKHR_OK;
 }
 
@@ -1407,8 +1516,6 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
     s = vkhr_reserve(ctx, (void**)&ctx->brick_list, &ctx->brick_list_cap, total_bricks + 1ull, sizeof(uint32_t));
     if (s != VKHR_OK) return s;
     if (segments && total_items) {
-        s = vkhr_reserve(ctx, (void**)&ctx->pair_rec, &ctx->pair_rec_cap, 2ull * total_items, sizeof(float4));
-        if (s != VKHR_OK) return s;
         if (tang) {
             s = vkhr_reserve(ctx, (void**)&ctx->pair_tan, &ctx->pair_tan_cap, total_items, sizeof(float4));
             if (s != VKHR_OK) return s;
@@ -1431,26 +1538,39 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
         s = vkhr_reserve(ctx, (void**)&ctx->items, &ctx->items_cap, visits_total ? visits_total : 1, sizeof(uint2));
         if (s != VKHR_OK) return s;
     }
-    // One walk instead of two: when the context knows a per-brick capacity
-    // (its earlier calls' largest brick) and the fixed slices fit in memory,
-    // the counting walk also writes every run into its brick's slice
-    // [brick * capacity, + count) of a separate buffer.  A brick past the
-    // capacity is counted but not written.  Without a budget the visit
-    // read-back shows it and the call fills again compactly; with a budget
-    // (one style; no read-back, the call may be captured) the device decides:
-    // the fill pass runs only if the largest brick outgrew the capacity, and
-    // the brick kernel reads whichever layout holds the entries.
+    // One walk instead of two: when the context knows a slice per brick and
+    // the slices fit in memory, the counting walk also writes every run into
+    // its brick's slice of a separate buffer.  One style: the slices are
+    // [brick * capacity, + capacity), the capacity learned from earlier
+    // calls' largest brick.  A batch: the layout learned from the last
+    // counted call of the same shape (each visited brick its count + 25%).
+    // A brick past its slice is counted but not written and raises the
+    // call's overflow word.  Without a budget the read-back shows it and the
+    // call fills again compactly; with a budget (no read-back, the call may
+    // be captured) the device decides: the fill pass runs only after an
+    // overflow, and the brick kernel reads whichever layout holds the entries.
     const size_t entry_bytes = pack ? sizeof(uint32_t) : sizeof(uint2);
+    const uint64_t shape = (segments && nj > 1) ? batch_shape(jobs, nj, tang, pack) : 0;
     uint32_t direct_cap = 0;
-    if (segments && total_items && ctx->direct_cap && (!bounded || nj == 1)) {
+    size_t slots_n = 0;
+    bool use_layout = shape && total_items && ctx->layout && ctx->layout_shape == shape &&
+                      ctx->layout_bricks == total_bricks;
+    if (use_layout) {
+        s = vkhr_reserve(ctx, (void**)&ctx->slots, &ctx->slots_cap, (ctx->layout_slots * entry_bytes + 7) / 8,
+                         sizeof(uint2));
+        if (s != VKHR_OK) return s;
+        slots_n = ctx->layout_slots;
+    } else if (segments && total_items && ctx->direct_cap && nj == 1) {
         const uint64_t slots = (uint64_t)total_bricks * ctx->direct_cap;
         if (slots < (1ull << 32) && slots * entry_bytes <= kDirectBytes) {
             s = vkhr_reserve(ctx, (void**)&ctx->slots, &ctx->slots_cap, (slots * entry_bytes + 7) / 8, sizeof(uint2));
             if (s != VKHR_OK) return s;
             direct_cap = ctx->direct_cap;
+            slots_n = slots;
         }
     }
-    const bool speculative = bounded && direct_cap != 0; // the device picks the layout
+    const bool one_walk = direct_cap != 0 || use_layout;
+    const bool speculative = bounded && one_walk; // the device picks the layout
     // per-call words; the status bits stay until a check reports them
     VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_words, 0, WORD_STATUS * sizeof(unsigned long long), st));
     VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_words + WORD_STATUS + 1, 0,
@@ -1464,37 +1584,39 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
                                        : std::min(vkhr_blocks(total_items, threads), (unsigned)ctx->sm_count * 16);
     const size_t bin_smem_bytes = (size_t)nj * (sizeof(VoxJob) + sizeof(uint32_t));
     const bool single = nj == 1;
+    const uint2* layout = use_layout ? ctx->layout : nullptr;
 #define VKHR_DIRECT(PACK_)                                                                                        \
     do {                                                                                                         \
         if (single)                                                                                              \
             VKHR_LAUNCH(ctx, (bin_kernel<false, true, PACK_, true, false, true>), in_blocks, threads, 0, st,       \
-                        jobs[0], d_jobs, nj, total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits,        \
-                        ctx->brick_cursor, ctx->slots, (size_t)direct_cap, ctx->d_words, 0u);                         \
+                        jobs[0], d_jobs, nj, total_items, ctx->pair_tan, ctx->brick_visits,                      \
+                        ctx->brick_cursor, ctx->slots, (size_t)direct_cap, layout, ctx->d_words, 0);              \
         else                                                                                                     \
             VKHR_LAUNCH(ctx, (bin_kernel<false, true, PACK_, false, false, true>), in_blocks, threads,             \
-                        bin_smem_bytes, st, jobs[0], d_jobs, nj, total_items, ctx->pair_rec, ctx->pair_tan,       \
-                        ctx->brick_visits, ctx->brick_cursor, ctx->slots, (size_t)direct_cap, ctx->d_words, 0u);      \
+                        bin_smem_bytes, st, jobs[0], d_jobs, nj, total_items, ctx->pair_tan,                     \
+                        ctx->brick_visits, ctx->brick_cursor, ctx->slots, (size_t)direct_cap, layout, ctx->d_words, \
+                        0);                                                                                      \
     } while (0)
-    if (total_items && direct_cap) {
+    if (total_items && one_walk) {
         if (pack) VKHR_DIRECT(true);
         else VKHR_DIRECT(false);
     } else if (total_items) {
         if (segments && single)
             VKHR_LAUNCH(ctx, (bin_kernel<false, true, false, true>), in_blocks, threads, 0, st, jobs[0], d_jobs, nj,
-                        total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, nullptr,
-                        (size_t)0, ctx->d_words, 0u);
+                        total_items, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, nullptr,
+                        (size_t)0, nullptr, ctx->d_words, 0);
         else if (segments)
             VKHR_LAUNCH(ctx, (bin_kernel<false, true, false, false>), in_blocks, threads, bin_smem_bytes, st, jobs[0],
-                        d_jobs, nj, total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor,
-                        nullptr, (size_t)0, ctx->d_words, 0u);
+                        d_jobs, nj, total_items, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor,
+                        nullptr, (size_t)0, nullptr, ctx->d_words, 0);
         else if (single)
             VKHR_LAUNCH(ctx, (bin_kernel<false, false, false, true>), in_blocks, threads, 0, st, jobs[0], d_jobs, nj,
-                        total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, nullptr,
-                        (size_t)0, ctx->d_words, 0u);
+                        total_items, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, nullptr,
+                        (size_t)0, nullptr, ctx->d_words, 0);
         else
             VKHR_LAUNCH(ctx, (bin_kernel<false, false, false, false>), in_blocks, threads, bin_smem_bytes, st, jobs[0],
-                        d_jobs, nj, total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor,
-                        nullptr, (size_t)0, ctx->d_words, 0u);
+                        d_jobs, nj, total_items, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor,
+                        nullptr, (size_t)0, nullptr, ctx->d_words, 0);
     }
 #undef VKHR_DIRECT
     const unsigned rblocks = std::min(vkhr_blocks(total_bricks, kRangeThreads * kRangeItems), (unsigned)ctx->sm_count * 8);
@@ -1519,10 +1641,19 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
         const uint64_t largest = ctx->h_words[WORD_MAX_BRICK_VISITS];
         const uint64_t want = (largest + largest / 4 + 63) / 64 * 64;
         if (want > ctx->direct_cap && want < (1ull << 31)) ctx->direct_cap = (uint32_t)want;
-        if (direct_cap && largest > direct_cap) direct_cap = 0; // a brick outgrew its slice: fill compactly
-        if (!direct_cap) {
+        if (one_walk && ctx->h_words[WORD_DIRECT_OVERFLOW]) { // a brick outgrew its slice: fill compactly
+            direct_cap = 0;
+            use_layout = false;
+        }
+        if (!direct_cap && !use_layout) {
             s = vkhr_reserve(ctx, (void**)&ctx->items, &ctx->items_cap, visits_total ? visits_total : 1, sizeof(uint2));
             if (s != VKHR_OK) return s;
+            // a batch learns (again) the layout its next calls walk once into
+            if (shape) {
+                s = learn_layout(ctx, shape, total_bricks, visits_total,
+                                 ctx->h_words[WORD_BRICK_LIST] + ctx->h_words[WORD_BIG_LIST], entry_bytes, st);
+                if (s != VKHR_OK) return s;
+            }
         }
     }
     // capacities the kernels check against (the budget, not the grown scratch)
@@ -1540,9 +1671,9 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
     if (s != VKHR_OK) return s;
     VKHR_LAUNCH(ctx, zero_empty_kernel, std::min(vkhr_blocks(total_groups, 256), (unsigned)ctx->sm_count * 16), 256, 0,
                 ctx->side, d_jobs, nj, total_groups, ctx->brick_visits);
-    if (total_items && (!direct_cap || speculative)) {
+    if (total_items && (!(direct_cap || use_layout) || speculative)) {
         void* ent = ctx->items;
-        const uint32_t skip_if_fits = speculative ? direct_cap : 0u; // the fill is the fallback
+        const int fallback = speculative ? 1 : 0; // the fill runs only after an overflow
         // spread a one-style fill's warps over distant strands when its visit
         // list is within twice the L2 size: most scattered entry stores still
         // merge in L2 (measured: a 123 MB list gains, a 1.8 GB list loses)
@@ -1552,16 +1683,16 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
     do {                                                                                                         \
         if (single && SEG_ && spread)                                                                            \
             VKHR_LAUNCH(ctx, (bin_kernel<true, SEG_, PACK_, true, true>), in_blocks, threads, 0, st, jobs[0],      \
-                        d_jobs, nj, total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits,                 \
-                        ctx->brick_cursor, ent, cap_visits, ctx->d_words, skip_if_fits);                          \
+                        d_jobs, nj, total_items, ctx->pair_tan, ctx->brick_visits,                 \
+                        ctx->brick_cursor, ent, cap_visits, nullptr, ctx->d_words, fallback);                          \
         else if (single)                                                                                         \
             VKHR_LAUNCH(ctx, (bin_kernel<true, SEG_, PACK_, true>), in_blocks, threads, 0, st, jobs[0], d_jobs, nj,  \
-                        total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ent,     \
-                        cap_visits, ctx->d_words, skip_if_fits);                                                  \
+                        total_items, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ent,     \
+                        cap_visits, nullptr, ctx->d_words, fallback);                                                  \
         else                                                                                                     \
             VKHR_LAUNCH(ctx, (bin_kernel<true, SEG_, PACK_, false>), in_blocks, threads, bin_smem_bytes, st,       \
-                        jobs[0], d_jobs, nj, total_items, ctx->pair_rec, ctx->pair_tan, ctx->brick_visits,        \
-                        ctx->brick_cursor, ent, cap_visits, ctx->d_words, skip_if_fits);                          \
+                        jobs[0], d_jobs, nj, total_items, ctx->pair_tan, ctx->brick_visits,        \
+                        ctx->brick_cursor, ent, cap_visits, nullptr, ctx->d_words, fallback);                          \
     } while (0)
         if (segments && pack) VKHR_FILL(true, true);
         else if (segments) VKHR_FILL(true, false);
@@ -1572,7 +1703,7 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
     const unsigned bblocks = std::min(total_bricks, (unsigned)ctx->sm_count * 2);
 #define VKHR_BRICK(SEG_, TANG_, PACK_)                                                                            \
     launch_brick<SEG_, TANG_, PACK_>(ctx, d_jobs, nj, total_bricks, st, bblocks, cap_visits, cap_visits, direct_cap,     \
-                                     speculative)
+                                     use_layout ? ctx->layout : nullptr, slots_n, speculative)
     if (segments) {
         if (!tang) s = VKHR_BRICK(true, false, true);
         else if (pack) s = VKHR_BRICK(true, true, true);
