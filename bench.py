@@ -280,7 +280,9 @@ def batched_comparison(args, dev, stream, rank, world, flush):
         ctx_b.voxelize_batched(True, vjobs, st_handle)
         ctx_b.raymarch_batched(rjobs, st_handle)
 
-    # the visit budget from one counted run (+25%), then a warm-up at that budget and the capture
+    # the one-walk residency for this batch (counts it, learns its layout), then the visit budget from
+    # one counted run (+25%), a warm-up at that budget and the capture
+    bwalk, bwalk_ms = ctx_b.autotune_voxelize(vjobs, s)
     ctx_b.voxelize_batched(True, vjobs, s)
     ctx_b.check_status(s)
     visits = int(sum(int(x["counts_b"].sum(dtype=torch.int64).item()) for x in styles))
@@ -360,6 +362,8 @@ def batched_comparison(args, dev, stream, rank, world, flush):
         "batched_graph_msegments_per_s": world * segs / (ms["batched_graph"] / 1e3) / 1e6,
         "batched_graph_region_mpixels_per_s": world * pixels / (ms["batched_graph"] / 1e3) / 1e6,
         "identical_to_plain": bool(same),
+        "autotune": {"voxelize_walk_ctas_per_sm": bwalk,
+                     "walk_ms": {str(k): round(m, 4) for k, m in zip(_abi.WALK_CHOICES, bwalk_ms)}},
     }
     ctx_b.set_visit_budget(0)
     return out
@@ -1009,6 +1013,20 @@ def gb300_arm(args):
     torch.cuda.synchronize()
     # the ray-packet variant for this view (vkhr_autotune_raymarch), kept in the context
     tuned, tuned_ms = ctx.autotune_raymarch(p, dens.data_ptr(), tq.data_ptr(), rgba.data_ptr(), s)
+    # the one-walk kernel's resident CTAs per SM for this style (vkhr_autotune_voxelize), kept in the context
+    vjob = _abi.VoxelJob()
+    vjob.d_vertices, vjob.d_tangent_in, vjob.d_indices = dv.data_ptr(), dt.data_ptr(), di.data_ptr()
+    vjob.item_count = int(idx.shape[0])
+    vjob.bounds = b
+    vjob.width, vjob.height, vjob.depth = res
+    vjob.index_mode = _abi.INDEX_REF_FP32
+    vjob.d_counts, vjob.d_densities, vjob.d_tangents = counts.data_ptr(), dens.data_ptr(), tq.data_ptr()
+    walk, walk_ms = ctx.autotune_voxelize([vjob], s)
+    for _ in range(2):  # back to the timed calls' own (unbudgeted) path
+        flush.zero_()
+        voxelize()
+        raymarch()
+    torch.cuda.synchronize()
 
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
            torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
@@ -1225,7 +1243,9 @@ def gb300_arm(args):
                 "serial_value": world * px / (e2e_serial_ms / 1e3) / 1e6},
         "gpu_launches": launches,
         "clocks": clocks.summary(),
-        "autotune": {"raymarch_variant": tuned, "variant_ms": tuned_ms,
+        "autotune": {"voxelize_walk_ctas_per_sm": walk,
+                     "walk_ms": {str(k): round(m, 4) for k, m in zip(_abi.WALK_CHOICES, walk_ms)},
+                     "raymarch_variant": tuned, "variant_ms": tuned_ms,
                      "variants": ["8x4 tiles", "16x2 tiles", "4x8 tiles", "8x4 tiles, 64 registers",
                                   "8x4 tiles, density bricks staged in shared memory by TMA",
                                   "8x4 tiles, density through the texture unit (not tuned: 8-bit filter weights)",

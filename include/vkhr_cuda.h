@@ -303,6 +303,27 @@ vkhr_status vkhr_voxelize_batched(vkhr_ctx* ctx, int32_t segments, const vkhr_vo
  * No reference counterpart. */
 vkhr_status vkhr_set_visit_budget(vkhr_ctx* ctx, uint64_t max_visits);
 
+/* Resident CTAs per SM of the one-walk segment kernel (the counting walk that
+ * also writes each visit into its brick's slice), no reference counterpart:
+ * 0 = as many as registers allow (8), else 1..8.  Fewer resident walks
+ * queue less on the per-brick counters whose returning atomics reserve the
+ * slices.  which: 0 = one-style calls, 1 = batches.  Defaults: 4 and 0.
+ * The results do not depend on it. */
+vkhr_status vkhr_set_voxelize_walk(vkhr_ctx* ctx, int32_t which, int32_t ctas_per_sm);
+
+/* Autotuner for the above (no reference counterpart): voxelizes the segment
+ * jobs (one-style calls for job_count == 1, else a batch) once without a
+ * budget (counting its visits, learning the one-walk slices), then times
+ * each residency of {0, 2, 3, 4, 5, 6} (one warm-up and three timed runs
+ * each) under the context's visit budget, or the counted visits + 25% +
+ * 4096 when it has none (restored afterwards); keeps the fastest for that
+ * kind of call and writes it to *chosen and, when ms is not NULL, each
+ * choice's median time (VKHR_WALK_CHOICES floats, in that order).  The jobs'
+ * outputs receive the voxelization.  Synchronises the stream. */
+#define VKHR_WALK_CHOICES 6
+vkhr_status vkhr_autotune_voxelize(vkhr_ctx* ctx, const vkhr_voxel_job* jobs, int32_t job_count, int32_t* chosen,
+                                   float* ms, void* stream);
+
 /* Waits for the stream and reports errors that kernels recorded on the device
  * since the last report (e.g. a capacity overflow, a fragment outside the
  * image); reporting clears them.  A segment voxelization that reads its

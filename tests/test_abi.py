@@ -37,3 +37,15 @@ def test_status_strings_and_null_context(native_lib):
     assert native_lib.vkhr_voxelize_vertices(None, None, None, 0, None, 1, 1, 1, 0, None, None, None,
                                              None) == _abi.VKHR_ERR_INVALID_ARG
     assert native_lib.vkhr_raymarch(None, None, None, None, None, None, None, None) == _abi.VKHR_ERR_INVALID_ARG
+
+
+def test_constants_match_header(native_lib):
+    src = open(HEADER).read()
+
+    def define(name):
+        return int(re.search(r"#define %s (\d+)" % name, src).group(1))
+
+    assert define("VKHR_RAYMARCH_VARIANTS") == _abi.RAYMARCH_VARIANTS
+    assert define("VKHR_WALK_CHOICES") == len(_abi.WALK_CHOICES)
+    assert native_lib.vkhr_set_voxelize_walk(None, 0, 4) == _abi.VKHR_ERR_INVALID_ARG
+    assert native_lib.vkhr_autotune_voxelize(None, None, 1, None, None, None) == _abi.VKHR_ERR_INVALID_ARG

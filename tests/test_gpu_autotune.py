@@ -163,3 +163,50 @@ def test_texture_unit_variant(ctx, oracle_lib, fmt, variant):
         outs.append(o.cpu().numpy())
     ctx.set_raymarch_variant(_abi.DENSITY_U32_COUNT, pc.tangent_format, 0)
     assert np.array_equal(outs[0], outs[1])
+
+
+def test_voxelize_walk_residency(oracle_lib):
+    """The one-walk kernel's resident-CTA limit changes the timing only: every
+    choice gives the oracle's voxels bit for bit, for a one-style call and for
+    a batch; vkhr_autotune_voxelize times each and keeps the fastest."""
+    import torch
+
+    from vkhr_gb300 import _native
+    from tests.test_gpu_batched import _Batch, _styles
+    from tests.test_gpu_voxelize import _check
+
+    c = _native.Context(0)
+    try:
+        st, t, idx = style("disk", 3000, 14, seed=5)
+        res = (64, 64, 64)
+        b = oracle_lib.bounding_box(st.vertices)
+        _check(c, oracle_lib, "segments", st.vertices, t, idx, b, res)  # counted: learns a slice capacity
+        for k in (0, 1, 2, 4, 6, 8):
+            c.set_voxelize_walk(0, k)
+            _check(c, oracle_lib, "segments", st.vertices, t, idx, b, res)
+        with pytest.raises(VkhrError):
+            c.set_voxelize_walk(0, 9)
+        with pytest.raises(VkhrError):
+            c.set_voxelize_walk(2, 4)
+
+        batch = _Batch(torch, oracle_lib, _styles(8, 6), True)
+        s = torch.cuda.current_stream().cuda_stream
+        c.voxelize_batched(True, batch.jobs, s)  # counted: learns the layout
+        c.check_status(s)
+        for k in (0, 3, 8):
+            c.set_voxelize_walk(1, k)
+            batch.poison()
+            c.voxelize_batched(True, batch.jobs, s)
+            c.check_status(s)
+            batch.check(oracle_lib)
+
+        for jobs in ([batch.jobs[0]], batch.jobs):
+            batch.poison()
+            chosen, ms = c.autotune_voxelize(jobs, s)
+            torch.cuda.synchronize()
+            assert chosen in _abi.WALK_CHOICES and min(ms) > 0
+            assert ms[_abi.WALK_CHOICES.index(chosen)] == min(ms)
+            print("walk residency %s: %s ms, chose %d" % (list(_abi.WALK_CHOICES), np.round(ms, 4).tolist(), chosen))
+        batch.check(oracle_lib)  # the autotuner's runs leave the voxelization in the outputs
+    finally:
+        c.close()

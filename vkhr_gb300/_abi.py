@@ -37,6 +37,7 @@ TUNED_RAYMARCH_VARIANTS = 5  # variants 0-4 compute the same pixels; 5 and 6 sam
 RAYMARCH_TEXTURE_VARIANT = 5
 RAYMARCH_SHADE_TEXTURE_VARIANT = 6  # the texture unit for the shadow and AO samples only
 MAX_AO_DIRECTIONS = 32
+WALK_CHOICES = (0, 2, 3, 4, 5, 6)  # vkhr_autotune_voxelize: resident one-walk CTAs per SM (0: no limit)
 
 FILTER_MAX = 0
 FILTER_MIN = 1

@@ -62,6 +62,9 @@ def load():
                                            C.c_int32, C.c_int32, P, P, P, P]
     lib.vkhr_voxelize_batched.argtypes = [P, C.c_int32, C.POINTER(_abi.VoxelJob), C.c_int32, P]
     lib.vkhr_set_visit_budget.argtypes = [P, C.c_uint64]
+    lib.vkhr_set_voxelize_walk.argtypes = [P, C.c_int32, C.c_int32]
+    lib.vkhr_autotune_voxelize.argtypes = [P, C.POINTER(_abi.VoxelJob), C.c_int32, C.POINTER(C.c_int32),
+                                           C.POINTER(C.c_float), P]
     lib.vkhr_raymarch_batched.argtypes = [P, C.POINTER(_abi.RaymarchJob), C.c_int32, P]
     lib.vkhr_raymarch_footprint.argtypes = [C.POINTER(_abi.RaymarchParams), C.POINTER(C.c_int32)]
     lib.vkhr_normalize_densities.argtypes = [P, P, C.c_uint64, P]
@@ -274,6 +277,18 @@ class Context:
 
     def check_status(self, stream=None):
         self.check(self.lib.vkhr_check_status(self.handle, stream))
+
+    def set_voxelize_walk(self, which, ctas_per_sm):
+        """Resident CTAs per SM of the one-walk kernel (which: 0 one style, 1 batch; 0 = no limit)."""
+        self.check(self.lib.vkhr_set_voxelize_walk(self.handle, which, ctas_per_sm))
+
+    def autotune_voxelize(self, jobs, stream=None):
+        """Segment jobs: (chosen residency, [median ms of each of WALK_CHOICES])."""
+        arr = (_abi.VoxelJob * len(jobs))(*jobs)
+        chosen = C.c_int32(-1)
+        ms = (C.c_float * len(_abi.WALK_CHOICES))()
+        self.check(self.lib.vkhr_autotune_voxelize(self.handle, arr, len(jobs), C.byref(chosen), ms, stream))
+        return int(chosen.value), [float(x) for x in ms]
 
     def normalize_densities(self, d_densities, n, stream=None):
         self.check(self.lib.vkhr_normalize_densities(self.handle, d_densities, n, stream))

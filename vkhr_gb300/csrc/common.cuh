@@ -54,6 +54,9 @@ struct vkhr_ctx {
     int sm_count;
     int l2_bytes;              // L2 cache size
     uint32_t direct_cap;       // voxelizer: per-brick slice capacity of one-walk calls (0: not yet known)
+    int walk_ctas[2];          // voxelizer: resident CTAs per SM of the one-walk kernel (one style, batch; 0: no limit)
+    int smem_per_sm;           // shared memory per SM and reserved per block (bytes)
+    int smem_reserved;
     uint4* d_gather;           // strand reduction: the kept strands' (source, destination, vertices)
     uint32_t* comp;            // compositing: per-pixel counts, slice starts, sort queues, fragment keys
     size_t comp_cap;           // (in 32-bit words)

@@ -133,6 +133,12 @@ vkhr_status vkhr_create(int device, vkhr_ctx** out)
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->l2_bytes, cudaDevAttrL2CacheSize, device);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&ctx->smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&ctx->smem_reserved, cudaDevAttrReservedSharedMemoryPerBlock, device);
+    ctx->walk_ctas[0] = 4; // one-style one-walk calls: measured fastest on the production style
+    ctx->walk_ctas[1] = 0;
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_words, WORD_COUNT * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMemset(ctx->d_words, 0, WORD_COUNT * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_words, WORD_COUNT * sizeof(unsigned long long));

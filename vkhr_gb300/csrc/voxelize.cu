@@ -1098,9 +1098,13 @@ __device__ __forceinline__ void warp_sort(uint32_t (&v)[R])
     }
 }
 
-// One crowded voxel (c <= 32 * R keys at src) by one warp: sort, gather the
-// first min(c, 255) tangents into shared memory in parallel, then lanes 0..2
-// add the x, y and z components in key order.
+// One crowded voxel (c <= 32 * R keys at src) by one warp.  Up to 255
+// visits (every tangent is summed): the warp adds them in any order and
+// certifies the quantized result as resolve_brick does (the bound holds for
+// any order of the c - 1 additions); otherwise -- or past 255 visits, where
+// the 255 smallest keys are the ones summed -- sort, gather the first
+// min(c, 255) tangents into shared memory in parallel, then lanes 0..2 add
+// the x, y and z components in key order.
 template <int R>
 __device__ __forceinline__ void resolve_warp(const VoxJob& J, const float4* __restrict__ pair_tan_all,
                                              const uint32_t* __restrict__ src, uint32_t c, float (*wt)[kKeep],
@@ -1112,6 +1116,32 @@ __device__ __forceinline__ void resolve_warp(const VoxJob& J, const float4* __re
     for (int r = 0; r < R; ++r) { // coalesced load; a sorting network takes any input order
         const uint32_t i = (uint32_t)r * 32u + lane;
         v[r] = i < c ? __ldg(src + i) : 0xffffffffu;
+    }
+    if (c <= 255u) {
+        float sx = 0.0f, sy = 0.0f, sz = 0.0f, am = 0.0f;
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+            if ((uint32_t)r * 32u + lane < c) {
+                float x, y, z;
+                key_tangent(J, pair_tan_all, v[r], x, y, z);
+                sx = __fadd_rn(sx, x);
+                sy = __fadd_rn(sy, y);
+                sz = __fadd_rn(sz, z);
+                am = __fadd_ru(am, fmaxf(fmaxf(fabsf(x), fabsf(y)), fabsf(z)));
+            }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) { // every lane ends with the same sums
+            sx = __fadd_rn(sx, __shfl_xor_sync(0xffffffffu, sx, o));
+            sy = __fadd_rn(sy, __shfl_xor_sync(0xffffffffu, sy, o));
+            sz = __fadd_rn(sz, __shfl_xor_sync(0xffffffffu, sz, o));
+            am = __fadd_ru(am, __shfl_xor_sync(0xffffffffu, am, o));
+        }
+        const float scale = __fmul_ru((float)(c - 1), 2.05f * 5.9604645e-8f), fm = (float)c;
+        int qx, qy, qz;
+        if (certify(sx, am, scale, fm, qx) && certify(sy, am, scale, fm, qy) && certify(sz, am, scale, fm, qz)) {
+            if (lane == 0) *out = ((uint32_t)(qx & 0xff)) | ((uint32_t)(qy & 0xff) << 8) | ((uint32_t)(qz & 0xff) << 16);
+            return;
+        }
     }
     warp_sort<R>(v);
     const uint32_t m = c < 255u ? c : 255u;
@@ -1419,6 +1449,18 @@ vkhr_status make_job(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job& in, Vox
     return VKHR_OK;
 }
 
+// Dynamic shared memory of a launch that keeps at most k of its CTAs
+// resident per SM (k CTAs of it fit in an SM's shared memory, k + 1 do
+// not), at least `base` bytes; k <= 0 or k >= 8 (the register limit of the
+// walk kernels): base.
+size_t residency_smem(const vkhr_ctx* ctx, int k, size_t base)
+{
+    if (k <= 0 || k >= 8 || ctx->smem_per_sm <= 0) return base;
+    const size_t per_block = (size_t)ctx->smem_per_sm / (size_t)k;
+    const size_t s = per_block > (size_t)ctx->smem_reserved ? per_block - (size_t)ctx->smem_reserved : 0;
+    return std::max(s, base);
+}
+
 // The shape a learned batch layout is kept for: the styles' grids and pair
 // counts, tangents requested, entry size.
 uint64_t batch_shape(const VoxJob* jobs, int nj, bool tang, bool pack)
@@ -1585,17 +1627,23 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
     const size_t bin_smem_bytes = (size_t)nj * (sizeof(VoxJob) + sizeof(uint32_t));
     const bool single = nj == 1;
     const uint2* layout = use_layout ? ctx->layout : nullptr;
+    // the one walk's dynamic shared memory, sized to keep walk_ctas CTAs resident per SM
+    const size_t walk_smem = residency_smem(ctx, ctx->walk_ctas[single ? 0 : 1], single ? 0 : bin_smem_bytes);
 #define VKHR_DIRECT(PACK_)                                                                                        \
     do {                                                                                                         \
-        if (single)                                                                                              \
-            VKHR_LAUNCH(ctx, (bin_kernel<false, true, PACK_, true, false, true>), in_blocks, threads, 0, st,       \
-                        jobs[0], d_jobs, nj, total_items, ctx->pair_tan, ctx->brick_visits,                      \
+        if (single) {                                                                                            \
+            VKHR_CUDA_TRY(ctx, cudaFuncSetAttribute(bin_kernel<false, true, PACK_, true, false, true>,            \
+                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)walk_smem)); \
+            VKHR_LAUNCH(ctx, (bin_kernel<false, true, PACK_, true, false, true>), in_blocks, threads, walk_smem,   \
+                        st, jobs[0], d_jobs, nj, total_items, ctx->pair_tan, ctx->brick_visits,                  \
                         ctx->brick_cursor, ctx->slots, (size_t)direct_cap, layout, ctx->d_words, 0);              \
-        else                                                                                                     \
-            VKHR_LAUNCH(ctx, (bin_kernel<false, true, PACK_, false, false, true>), in_blocks, threads,             \
-                        bin_smem_bytes, st, jobs[0], d_jobs, nj, total_items, ctx->pair_tan,                     \
-                        ctx->brick_visits, ctx->brick_cursor, ctx->slots, (size_t)direct_cap, layout, ctx->d_words, \
-                        0);                                                                                      \
+        } else {                                                                                                 \
+            VKHR_CUDA_TRY(ctx, cudaFuncSetAttribute(bin_kernel<false, true, PACK_, false, false, true>,           \
+                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)walk_smem)); \
+            VKHR_LAUNCH(ctx, (bin_kernel<false, true, PACK_, false, false, true>), in_blocks, threads, walk_smem,  \
+                        st, jobs[0], d_jobs, nj, total_items, ctx->pair_tan, ctx->brick_visits,                  \
+                        ctx->brick_cursor, ctx->slots, (size_t)direct_cap, layout, ctx->d_words, 0);              \
+        }                                                                                                        \
     } while (0)
     if (total_items && one_walk) {
         if (pack) VKHR_DIRECT(true);
@@ -1784,6 +1832,75 @@ vkhr_status vkhr_set_visit_budget(vkhr_ctx* ctx, uint64_t max_visits)
     if (!ctx) return VKHR_ERR_INVALID_ARG;
     if (max_visits >= (1ull << 32)) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "budget must be below 2^32 visits");
     ctx->visit_budget = max_visits;
+    return VKHR_OK;
+}
+
+vkhr_status vkhr_set_voxelize_walk(vkhr_ctx* ctx, int32_t which, int32_t ctas_per_sm)
+{
+    if (!ctx) return VKHR_ERR_INVALID_ARG;
+    if (which != 0 && which != 1) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "which must be 0 (one style) or 1 (batch)");
+    if (ctas_per_sm < 0 || ctas_per_sm > 8) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "ctas_per_sm must be in [0, 8]");
+    ctx->walk_ctas[which] = ctas_per_sm;
+    return VKHR_OK;
+}
+
+vkhr_status vkhr_autotune_voxelize(vkhr_ctx* ctx, const vkhr_voxel_job* jobs, int32_t job_count, int32_t* chosen,
+                                   float* ms_out, void* stream)
+{
+    static const int kChoices[VKHR_WALK_CHOICES] = {0, 2, 3, 4, 5, 6};
+    if (!ctx) return VKHR_ERR_INVALID_ARG;
+    if (!chosen) return vkhr_fail(ctx, VKHR_ERR_INVALID_ARG, "chosen is required");
+    VKHR_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    const int which = job_count == 1 ? 0 : 1;
+    // counted once, without a budget: the sizes, the one-walk capacity or
+    // layout, and the visits; then timed under the budget
+    const uint64_t saved_budget = ctx->visit_budget;
+    ctx->visit_budget = 0;
+    vkhr_status s = voxelize_batch(ctx, true, jobs, job_count, st, true);
+    if (s != VKHR_OK) {
+        ctx->visit_budget = saved_budget;
+        return s;
+    }
+    const uint64_t v = ctx->h_words[WORD_TOTAL_VISITS];
+    ctx->visit_budget = saved_budget ? saved_budget : std::min<uint64_t>(v + v / 4 + 4096, (1ull << 32) - 1);
+    cudaEvent_t e[2];
+    VKHR_CUDA_TRY(ctx, cudaEventCreate(&e[0]));
+    if (cudaEventCreate(&e[1]) != cudaSuccess) {
+        cudaEventDestroy(e[0]);
+        ctx->visit_budget = saved_budget;
+        return vkhr_fail(ctx, VKHR_ERR_CUDA, "cudaEventCreate failed");
+    }
+    const int previous = ctx->walk_ctas[which];
+    float ms[VKHR_WALK_CHOICES] = {0.0f};
+    int best = 0;
+    for (int c = 0; c < VKHR_WALK_CHOICES && s == VKHR_OK; ++c) {
+        ctx->walk_ctas[which] = kChoices[c];
+        float t[3] = {0.0f, 0.0f, 0.0f};
+        for (int r = -1; r < 3 && s == VKHR_OK; ++r) { // one warm-up, three timed runs
+            if (cudaEventRecord(e[0], st) != cudaSuccess) s = vkhr_fail(ctx, VKHR_ERR_CUDA, "cudaEventRecord failed");
+            if (s == VKHR_OK) s = voxelize_batch(ctx, true, jobs, job_count, st);
+            if (s == VKHR_OK && (cudaEventRecord(e[1], st) != cudaSuccess || cudaEventSynchronize(e[1]) != cudaSuccess))
+                s = vkhr_fail(ctx, VKHR_ERR_CUDA, "timing the autotune runs failed");
+            if (s == VKHR_OK && r >= 0 && cudaEventElapsedTime(&t[r], e[0], e[1]) != cudaSuccess)
+                s = vkhr_fail(ctx, VKHR_ERR_CUDA, "cudaEventElapsedTime failed");
+        }
+        std::sort(t, t + 3);
+        ms[c] = t[1];
+        if (c > 0 && ms[c] < ms[best]) best = c;
+    }
+    cudaEventDestroy(e[0]);
+    cudaEventDestroy(e[1]);
+    ctx->visit_budget = saved_budget;
+    if (s == VKHR_OK) s = vkhr_check_status(ctx, stream); // a run that overflowed its budget
+    if (s != VKHR_OK) {
+        ctx->walk_ctas[which] = previous;
+        return s;
+    }
+    ctx->walk_ctas[which] = kChoices[best];
+    *chosen = kChoices[best];
+    if (ms_out)
+        for (int c = 0; c < VKHR_WALK_CHOICES; ++c) ms_out[c] = ms[c];
     return VKHR_OK;
 }
 
