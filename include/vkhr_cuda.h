@@ -307,7 +307,7 @@ vkhr_status vkhr_set_visit_budget(vkhr_ctx* ctx, uint64_t max_visits);
  * also writes each visit into its brick's slice), no reference counterpart:
  * 0 = as many as registers allow (8), else 1..8.  Fewer resident walks
  * queue less on the per-brick counters whose returning atomics reserve the
- * slices.  which: 0 = one-style calls, 1 = batches.  Defaults: 4 and 0.
+ * slices.  which: 0 = one-style calls, 1 = batches.  Default: 0 for both.
  * The results do not depend on it. */
 vkhr_status vkhr_set_voxelize_walk(vkhr_ctx* ctx, int32_t which, int32_t ctas_per_sm);
 
