@@ -842,7 +842,9 @@ RAY_AB = {
                  "5": "8x4 packets sampling through the texture unit (3D array copy + hardware trilinear, "
                       "8-bit weights)",
                  "6": "variant 5's texture for the deep-shadow and AO samples only; the isosurface search reads "
-                      "memory"},
+                      "memory",
+                 "7": "8x4 packets reading exact texels through the texture unit's 2x2 gathers (slices tiled into a "
+                      "2D array, copied per call); the software trilinear filters them"},
     "warm": "the volume L2-resident, as right after the voxelizer wrote it; cold: L2 flushed (512 MiB write) first",
 }
 
@@ -1249,7 +1251,8 @@ def gb300_arm(args):
                      "variants": ["8x4 tiles", "16x2 tiles", "4x8 tiles", "8x4 tiles, 64 registers",
                                   "8x4 tiles, density bricks staged in shared memory by TMA",
                                   "8x4 tiles, density through the texture unit (not tuned: 8-bit filter weights)",
-                                  "8x4 tiles, shadow and AO samples through the texture unit (not tuned)"]},
+                                  "8x4 tiles, shadow and AO samples through the texture unit (not tuned)",
+                                  "8x4 tiles, exact texels by texture gathers"]},
     }
     if batched is not None:
         line["batched_speedup_vs_plain"] = round(batched["speedup_vs_plain"]["batched_graph"], 3)

@@ -382,11 +382,16 @@ vkhr_status vkhr_raymarch(vkhr_ctx* ctx, const vkhr_raymarch_params* params,
  * densities only (variant 0 for counts).  6 = variant 5's texture for the
  * shading's samples only (deep-shadow march and ambient-occlusion taps),
  * while the isosurface search reads the texels in memory as variant 0 does.
- * The autotuner tries neither 5 nor 6. */
-#define VKHR_RAYMARCH_VARIANTS 7
+ * The autotuner tries neither 5 nor 6.  7 = 8x4 tiles reading the texels
+ * through the texture unit's 2x2 gathers (exact values, no filtering) from a
+ * 2D array of the grid's z slices, tiled and framed by zeros, that the call
+ * copies the density into; the software trilinear filters them, so its
+ * pixels are variant 0's, bit for bit (variant 0 where the tiled slices
+ * exceed the gather limits). */
+#define VKHR_RAYMARCH_VARIANTS 8
 
 /* Autotuner (no reference counterpart): times each variant of vkhr_raymarch
- * that computes the reference's pixels (0-4) on these inputs (one warm-up
+ * that computes the reference's pixels (0-4 and 7) on these inputs (one warm-up
  * and three timed runs each, d_rgba receiving the image) and keeps the
  * fastest in the context for params' texel formats; later vkhr_raymarch
  * calls with those formats use it.  Writes the choice to *chosen and, when

@@ -23,7 +23,7 @@ def test_variants_render_the_same_image(ctx, oracle_lib):
     p = scene.make_params(b, res, 333, 251, raycast_steps=256.0, shadow_steps=32.0)
     dd, dt = to_dev(dn, torch), to_dev(tq, torch)
     imgs = []
-    for v in range(_abi.TUNED_RAYMARCH_VARIANTS):
+    for v in _abi.TUNED_RAYMARCH_VARIANTS:
         ctx.set_raymarch_variant(p.density_format, p.tangent_format, v)
         rgba = torch.full((p.height, p.width, 4), -7.0, dtype=torch.float32, device="cuda")
         ctx.raymarch(p, dd.data_ptr(), dt.data_ptr(), None, rgba.data_ptr(), None)
@@ -34,8 +34,8 @@ def test_variants_render_the_same_image(ctx, oracle_lib):
     assert (imgs[0][..., 3] > 0).sum() > 1000
     rgba = torch.empty((p.height, p.width, 4), dtype=torch.float32, device="cuda")
     chosen, ms = ctx.autotune_raymarch(p, dd.data_ptr(), dt.data_ptr(), rgba.data_ptr())
-    tuned = ms[:_abi.TUNED_RAYMARCH_VARIANTS]
-    assert 0 <= chosen < _abi.TUNED_RAYMARCH_VARIANTS and min(tuned) > 0 and ms[chosen] == min(tuned)
+    tuned = [ms[v] for v in _abi.TUNED_RAYMARCH_VARIANTS]
+    assert chosen in _abi.TUNED_RAYMARCH_VARIANTS and min(tuned) > 0 and ms[chosen] == min(tuned)
     assert ms[_abi.RAYMARCH_TEXTURE_VARIANT] == 0.0 and ms[_abi.RAYMARCH_SHADE_TEXTURE_VARIANT] == 0.0  # not candidates
     assert np.array_equal(rgba.cpu().numpy(), imgs[0])
     with pytest.raises(VkhrError):
@@ -50,13 +50,16 @@ def test_variants_render_the_same_image(ctx, oracle_lib):
     (_abi.DENSITY_F32, _abi.TANGENT_F32X4, (36, 28, 52), (0.2, -0.5, -1.0), True),
     (_abi.DENSITY_U8_UNORM, _abi.TANGENT_I8_SNORM, (37, 50, 29), (0.3, 0.2, 1.0), False),  # pitch: no TMA
 ])
-def test_staged_variant_equals_l2_march(ctx, oracle_lib, fmt, tfmt, res, view, depth):
+def test_staged_and_gather_variants_equal_l2_march(ctx, oracle_lib, fmt, tfmt, res, view, depth):
     """Variant 4 (each occupied brick a warp's rays need staged into shared
-    memory by one TMA copy) against variant 0 (texels from L2): the same
-    pixels bit for bit, with and without a depth buffer, for every density
-    format, for a view whose volume straddles the image's edge, and for a
-    grid whose row pitch TMA cannot address (which falls back to variant 0);
-    and against the FP64 oracle."""
+    memory by one TMA copy) and variant 7 (texels through the texture unit's
+    2x2 gathers from the tiled, zero-framed slices) against variant 0
+    (texels from L2): the same pixels bit for bit, with and without a depth
+    buffer, for every density format, for grids whose depth is not a power
+    of two (a partly filled last row of tiles), for a view whose volume
+    straddles the image's edge, and for a grid whose row pitch TMA cannot
+    address (variant 4 falls back to variant 0); and against the FP64
+    oracle."""
     import torch
 
     from tests._helpers import compare_images
@@ -87,7 +90,7 @@ def test_staged_variant_equals_l2_march(ctx, oracle_lib, fmt, tfmt, res, view, d
         depth_np[:, : p.width // 2] = 1.0
         din = torch.from_numpy(depth_np).cuda()
     imgs = []
-    for v in (0, 4):
+    for v in (0, 4, _abi.RAYMARCH_GATHER_VARIANT):
         ctx.set_raymarch_variant(fmt, tfmt, v)
         rgba = torch.full((p.height, p.width, 4), -7.0, dtype=torch.float32, device="cuda")
         dep = torch.full((p.height, p.width), -7.0, dtype=torch.float32, device="cuda")
@@ -97,8 +100,9 @@ def test_staged_variant_equals_l2_march(ctx, oracle_lib, fmt, tfmt, res, view, d
         torch.cuda.synchronize()
         imgs.append((rgba.cpu().numpy(), dep.cpu().numpy()))
     ctx.set_raymarch_variant(fmt, tfmt, 0)
-    assert np.array_equal(imgs[0][0], imgs[1][0]), int((imgs[0][0] != imgs[1][0]).any(axis=2).sum())
-    assert np.array_equal(imgs[0][1], imgs[1][1])
+    for k, name in ((1, "staged"), (2, "gather")):
+        assert np.array_equal(imgs[0][0], imgs[k][0]), (name, int((imgs[0][0] != imgs[k][0]).any(axis=2).sum()))
+        assert np.array_equal(imgs[0][1], imgs[k][1]), name
     assert (imgs[1][0][..., 3] > 0).sum() > 200
     ref, rdepth, diag = oracle_lib.raymarch(p, dens, tan, depth_in=depth_np, diag=True)
     # small views (300x220) whose depth buffer cuts rays mid-volume: up to 2% excluded

@@ -32,10 +32,11 @@ STATUS_NAMES = {
 INDEX_REF_FP32 = 0
 INDEX_EXACT = 1
 
-RAYMARCH_VARIANTS = 7
-TUNED_RAYMARCH_VARIANTS = 5  # variants 0-4 compute the same pixels; 5 and 6 sample through the texture unit
+RAYMARCH_VARIANTS = 8
+TUNED_RAYMARCH_VARIANTS = (0, 1, 2, 3, 4, 7)  # the variants that compute the same pixels (autotuned)
 RAYMARCH_TEXTURE_VARIANT = 5
 RAYMARCH_SHADE_TEXTURE_VARIANT = 6  # the texture unit for the shadow and AO samples only
+RAYMARCH_GATHER_VARIANT = 7  # exact texels through the texture unit's gathers
 MAX_AO_DIRECTIONS = 32
 WALK_CHOICES = (0, 2, 3, 4, 5, 6)  # vkhr_autotune_voxelize: resident one-walk CTAs per SM (0: no limit)
 

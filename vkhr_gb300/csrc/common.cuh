@@ -103,6 +103,12 @@ struct vkhr_ctx {
     cudaArray_t tex_array;     // raymarch, texture-unit variant: the density copied into a 3D array
     cudaTextureObject_t tex_obj; // (LINEAR filter, border 0) and its texture object
     int tex_res[3], tex_fmt;   // the array's extent and density format
+    cudaArray_t gat_array;     // raymarch, gather variant: the density's slices tiled into a 2D array
+    cudaTextureObject_t gat_obj; // (POINT filter, element type, border 0) and its texture object
+    cudaSurfaceObject_t gat_surf; // its surface, when the array could be made writable (else 0: staged copies)
+    int gat_res[3], gat_fmt, gat_shift; // the grid it holds, its density format, log2 tiles per row
+    void* gat_stage;           // linear staging of the tiled slices
+    size_t gat_stage_cap;      // in bytes
     unsigned long long* d_words;
     unsigned long long* h_words; // pinned mirror
     cudaEvent_t ev;

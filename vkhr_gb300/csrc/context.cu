@@ -171,6 +171,10 @@ vkhr_status vkhr_destroy(vkhr_ctx* ctx)
     if (ctx->occ) cudaFree(ctx->occ);
     if (ctx->tex_obj) cudaDestroyTextureObject(ctx->tex_obj);
     if (ctx->tex_array) cudaFreeArray(ctx->tex_array);
+    if (ctx->gat_obj) cudaDestroyTextureObject(ctx->gat_obj);
+    if (ctx->gat_surf) cudaDestroySurfaceObject(ctx->gat_surf);
+    if (ctx->gat_array) cudaFreeArray(ctx->gat_array);
+    if (ctx->gat_stage) cudaFree(ctx->gat_stage);
     if (ctx->d_words) cudaFree(ctx->d_words);
     if (ctx->h_words) cudaFreeHost(ctx->h_words);
     if (ctx->ev) cudaEventDestroy(ctx->ev);

@@ -40,17 +40,26 @@ struct RayConsts {
     float shift[2];               // tangent shift of each lobe (0: the reference's unshifted lobe)
     int ao_n;                     // directional AO taps (0: the ao_kernel^3 cube)
     float ao_off[kMaxAoDirections][3]; // world-space offsets of the directional taps
-    unsigned long long tex;       // the density as a 3D texture object (texture-unit variant only; else 0)
+    unsigned long long tex;       // the density as a texture object (texture-unit and gather variants; else 0)
+    int gshift;                   // gather variant: log2 of the slice tiles per row of its 2D texture
 };
 
 // Where the march's density samples come from: the texels in memory with the
-// software trilinear below, or the texture unit's hardware trilinear filter,
+// software trilinear below; the texture unit's hardware trilinear filter,
 // whose weights have 8 fractional bits -- for every sample (kSampleTexture),
 // or for the shadow and ambient-occlusion samples of the shading only while
-// the isosurface search reads memory (kSampleShadeTexture).
-constexpr int kSampleMemory = 0, kSampleTexture = 1, kSampleShadeTexture = 2;
-__host__ __device__ constexpr int march_source(int src) { return src == kSampleTexture ? kSampleTexture : kSampleMemory; }
-__host__ __device__ constexpr int shade_source(int src) { return src == kSampleMemory ? kSampleMemory : kSampleTexture; }
+// the isosurface search reads memory (kSampleShadeTexture); or the texture
+// unit's 2x2 gathers of exact texel values, which the software trilinear
+// then filters (kSampleGather: the memory path's pixels, bit for bit).
+constexpr int kSampleMemory = 0, kSampleTexture = 1, kSampleShadeTexture = 2, kSampleGather = 3;
+__host__ __device__ constexpr int march_source(int src)
+{
+    return src == kSampleTexture || src == kSampleGather ? src : kSampleMemory;
+}
+__host__ __device__ constexpr int shade_source(int src)
+{
+    return src == kSampleMemory || src == kSampleGather ? src : kSampleTexture;
+}
 
 constexpr int kBrick = 8;          // occupancy brick edge in texel cells
 constexpr float kSkipMargin = 0.01f; // texels kept between a predicted sample and a brick face
@@ -117,6 +126,19 @@ __device__ __forceinline__ bool tex_setup(const RayConsts& c, Vec3 p, int i0[3],
     return true;
 }
 
+// The reference sampler's filter of the eight taps v (x fastest, then y, then z)
+// at fractions a.
+__device__ __forceinline__ float trilinear(const float v[8], const float a[3])
+{
+    const float x00 = fmaf(a[0], v[1] - v[0], v[0]);
+    const float x10 = fmaf(a[0], v[3] - v[2], v[2]);
+    const float x01 = fmaf(a[0], v[5] - v[4], v[4]);
+    const float x11 = fmaf(a[0], v[7] - v[6], v[6]);
+    const float y0 = fmaf(a[1], x10 - x00, x00);
+    const float y1 = fmaf(a[1], x11 - x01, x01);
+    return fmaf(a[2], y1 - y0, y0);
+}
+
 template <int DF>
 __device__ __forceinline__ float sample_density(const RayConsts& c, const typename DensityTexel<DF>::T* __restrict__ d,
                                                 Vec3 p)
@@ -147,19 +169,74 @@ __device__ __forceinline__ float sample_density(const RayConsts& c, const typena
                        : 0.0f;
         }
     }
-    const float x00 = fmaf(a[0], v[1] - v[0], v[0]);
-    const float x10 = fmaf(a[0], v[3] - v[2], v[2]);
-    const float x01 = fmaf(a[0], v[5] - v[4], v[4]);
-    const float x11 = fmaf(a[0], v[7] - v[6], v[6]);
-    const float y0 = fmaf(a[1], x10 - x00, x00);
-    const float y1 = fmaf(a[1], x11 - x01, x01);
-    return fmaf(a[2], y1 - y0, y0) * TX::scale;
+    return trilinear(v, a) * TX::scale;
+}
+
+// The 2x2 texels of a gather as floats: element-type reads, so each value is
+// the texel's own (u8 and u32 converted exactly as the memory path does).
+template <int DF>
+struct GatherTexel;
+template <>
+struct GatherTexel<VKHR_DENSITY_U8_UNORM> {
+    static __device__ __forceinline__ float4 get(unsigned long long t, float x, float y)
+    {
+        const uchar4 g = tex2Dgather<uchar4>((cudaTextureObject_t)t, x, y, 0);
+        return make_float4((float)g.x, (float)g.y, (float)g.z, (float)g.w);
+    }
+};
+template <>
+struct GatherTexel<VKHR_DENSITY_U32_COUNT> {
+    static __device__ __forceinline__ float4 get(unsigned long long t, float x, float y)
+    {
+        const uint4 g = tex2Dgather<uint4>((cudaTextureObject_t)t, x, y, 0);
+        return make_float4((float)g.x, (float)g.y, (float)g.z, (float)g.w);
+    }
+};
+template <>
+struct GatherTexel<VKHR_DENSITY_F32> {
+    static __device__ __forceinline__ float4 get(unsigned long long t, float x, float y)
+    {
+        return tex2Dgather<float4>((cudaTextureObject_t)t, x, y, 0);
+    }
+};
+
+// sample_density through the texture unit's gathers.  The density is a 2D
+// texture of the grid's z slices, tiled 2^gshift per row, each slice framed
+// by a one-texel border of zeros (tiles of (w + 2) x (h + 2)); texel (x, y)
+// of slice z sits at column (z mod 2^gshift) (w + 2) + 1 + x and row
+// (z >> gshift) (h + 2) + 1 + y.  One gather per slice returns the four
+// texels (x0..x0+1, y0..y0+1) -- the frames and the texture's border give
+// the zeros outside the grid -- in the order (x0, y1), (x1, y1), (x1, y0),
+// (x0, y0); the software trilinear filters them as sample_density does.
+template <int DF>
+__device__ __forceinline__ float sample_density_gather(const RayConsts& c, Vec3 p)
+{
+    typedef DensityTexel<DF> TX;
+    int i0[3];
+    float a[3];
+    if (!tex_setup(c, p, i0, a)) return 0.0f;
+    const int tw = c.res[0] + 2, th = c.res[1] + 2, mask = (1 << c.gshift) - 1;
+    float v[8];
+#pragma unroll
+    for (int dz = 0; dz < 2; ++dz) {
+        const int z = i0[2] + dz;
+        float4 g = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (z >= 0 && z < c.res[2]) // coordinates between the two columns / rows: exact integers + 1
+            g = GatherTexel<DF>::get(c.tex, (float)((z & mask) * tw + i0[0] + 2),
+                                     (float)((z >> c.gshift) * th + i0[1] + 2));
+        v[4 * dz + 0] = g.w;
+        v[4 * dz + 1] = g.z;
+        v[4 * dz + 2] = g.x;
+        v[4 * dz + 3] = g.y;
+    }
+    return trilinear(v, a) * TX::scale;
 }
 
 template <int DF, int SRC>
 __device__ __forceinline__ float density_at(const RayConsts& c, const typename DensityTexel<DF>::T* __restrict__ d,
                                             Vec3 p)
 {
+    if (SRC == kSampleGather) return sample_density_gather<DF>(c, p);
     if (SRC == kSampleTexture) { // texel centres at integer + 0.5 in the texture's unnormalised coordinates
         const float u = fmaf(p.x, c.tsc[0], c.tbias[0]), v = fmaf(p.y, c.tsc[1], c.tbias[1]),
                     w = fmaf(p.z, c.tsc[2], c.tbias[2]);
@@ -874,6 +951,7 @@ inline vkhr_status make_consts(vkhr_ctx* ctx, const vkhr_raymarch_params* p, Ray
     c.shadow_pow2 = pow2(c.shadow_steps) ? 1 : 0;
     for (int k = 0; k < 3; ++k) c.nb[k] = (c.res[k] + kBrick) / kBrick;
     c.tex = 0;
+    c.gshift = 0;
     c.exponent2 = p->spec_exponent2 > 0.0f ? p->spec_exponent2 : 0.0f;
     c.shift[0] = p->spec_shift[0];
     c.shift[1] = p->spec_shift[1];

@@ -35,8 +35,10 @@ constexpr int kPacketVariants = 4;   // raymarch_kernel instantiations; variant 
 constexpr int kStagedVariant = 4;
 constexpr int kTextureVariant = 5;   // the texture unit's filter: other pixels, never autotuned
 constexpr int kShadeTextureVariant = 6; // the same filter for the shading's samples only
-constexpr int kTunedVariants = 5;    // the variants that compute the same pixels
-static_assert(VKHR_RAYMARCH_VARIANTS == kShadeTextureVariant + 1, "variant table");
+constexpr int kGatherVariant = 7;    // exact texels by texture gathers: the same pixels
+// the variants that compute the same pixels (the autotuner's candidates)
+constexpr int kTunedVariants[] = {0, 1, 2, 3, 4, kGatherVariant};
+static_assert(VKHR_RAYMARCH_VARIANTS == kGatherVariant + 1, "variant table");
 constexpr RayVariant kRayVariants[kPacketVariants] = {{8, 6}, {16, 6}, {4, 6}, {8, 8}};
 
 template <int DF, int TF, int TW = 8, int MINB = 6, int SRC = kSampleMemory>
@@ -450,6 +452,97 @@ vkhr_status texture_density(vkhr_ctx* ctx, const RayConsts& c, const void* dens,
     return VKHR_OK;
 }
 
+// The gather variant's texture: the grid's z slices tiled 2^shift per row
+// into a 2D array, each slice framed by zeros (see sample_density_gather).
+// One thread per texel of the array, a block row per array row (blockIdx.y);
+// written through a surface of the array when it has one, else into a
+// linear staging buffer (row pitch `width` texels) that is copied in after.
+template <typename T>
+__global__ void gather_tile_kernel(const T* __restrict__ src, cudaSurfaceObject_t surf, T* __restrict__ dst, int nx,
+                                   int ny, int nz, int shift, uint32_t width)
+{
+    const uint32_t X = blockIdx.x * blockDim.x + threadIdx.x, Y = blockIdx.y;
+    if (X >= width) return;
+    const uint32_t tw = (uint32_t)nx + 2, th = (uint32_t)ny + 2;
+    const uint32_t tx = X / tw, ty = Y / th;
+    const int x = (int)(X - tx * tw) - 1, y = (int)(Y - ty * th) - 1;
+    const int z = (int)((ty << shift) + tx);
+    T v = T(0);
+    if (x >= 0 && x < nx && y >= 0 && y < ny && z < nz)
+        v = __ldg(src + (size_t)x + (size_t)nx * ((size_t)y + (size_t)ny * z));
+    if (surf) surf2Dwrite(v, surf, (int)(X * sizeof(T)), (int)Y);
+    else dst[(size_t)Y * width + X] = v;
+}
+
+// Copies the density into the context's gather texture (allocated, or
+// reallocated when the grid or format changes); false (ok) when the tiled
+// slices exceed the texture unit's gather limits.
+template <int DF>
+vkhr_status gather_density(vkhr_ctx* ctx, const RayConsts& c, const void* dens, cudaStream_t st, bool& ok)
+{
+    typedef typename DensityTexel<DF>::T T;
+    ok = false;
+    int shift = 0;
+    while ((1 << shift) * (1 << shift) < c.res[2]) ++shift; // 2^shift >= sqrt(depth)
+    const uint64_t per_row = 1ull << shift, rows = ((uint64_t)c.res[2] + per_row - 1) / per_row;
+    const uint64_t width = per_row * ((uint64_t)c.res[0] + 2), height = rows * ((uint64_t)c.res[1] + 2);
+    int max_w = 0, max_h = 0;
+    VKHR_CUDA_TRY(ctx, cudaDeviceGetAttribute(&max_w, cudaDevAttrMaxTexture2DGatherWidth, ctx->device));
+    VKHR_CUDA_TRY(ctx, cudaDeviceGetAttribute(&max_h, cudaDevAttrMaxTexture2DGatherHeight, ctx->device));
+    if (width > (uint64_t)max_w || height > (uint64_t)max_h) return VKHR_OK;
+    if (!ctx->gat_array || ctx->gat_fmt != DF || ctx->gat_res[0] != c.res[0] || ctx->gat_res[1] != c.res[1] ||
+        ctx->gat_res[2] != c.res[2]) {
+        if (ctx->gat_array && ctx->live_graphs > 0)
+            return vkhr_fail(ctx, VKHR_ERR_CAPACITY, "the density texture would have to change while a frame graph lives");
+        if (ctx->gat_obj) cudaDestroyTextureObject(ctx->gat_obj);
+        if (ctx->gat_array) {
+            VKHR_CUDA_TRY(ctx, cudaDeviceSynchronize()); // earlier launches may still read it
+            cudaFreeArray(ctx->gat_array);
+        }
+        if (ctx->gat_surf) cudaDestroySurfaceObject(ctx->gat_surf);
+        ctx->gat_obj = 0;
+        ctx->gat_surf = 0;
+        ctx->gat_array = nullptr;
+        const cudaChannelFormatDesc fd = cudaCreateChannelDesc<T>();
+        // writable as a surface where the driver allows it with gathers, else filled by a copy
+        bool surface = true;
+        if (cudaMallocArray(&ctx->gat_array, &fd, (size_t)width, (size_t)height,
+                            cudaArrayTextureGather | cudaArraySurfaceLoadStore) != cudaSuccess) {
+            cudaGetLastError();
+            surface = false;
+            VKHR_CUDA_TRY(ctx, cudaMallocArray(&ctx->gat_array, &fd, (size_t)width, (size_t)height,
+                                               cudaArrayTextureGather));
+        }
+        cudaResourceDesc rd = {};
+        rd.resType = cudaResourceTypeArray;
+        rd.res.array.array = ctx->gat_array;
+        cudaTextureDesc td = {};
+        td.addressMode[0] = td.addressMode[1] = cudaAddressModeBorder; // border colour 0
+        td.filterMode = cudaFilterModePoint;
+        td.readMode = cudaReadModeElementType;
+        td.normalizedCoords = 0;
+        VKHR_CUDA_TRY(ctx, cudaCreateTextureObject(&ctx->gat_obj, &rd, &td, nullptr));
+        if (surface) VKHR_CUDA_TRY(ctx, cudaCreateSurfaceObject(&ctx->gat_surf, &rd));
+        for (int k = 0; k < 3; ++k) ctx->gat_res[k] = c.res[k];
+        ctx->gat_fmt = DF;
+        ctx->gat_shift = shift;
+    }
+    if (!ctx->gat_surf) {
+        vkhr_status s = vkhr_reserve(ctx, &ctx->gat_stage, &ctx->gat_stage_cap, (size_t)(width * height * sizeof(T)), 1);
+        if (s != VKHR_OK) return s;
+    }
+    const dim3 grid((unsigned)((width + 255) / 256), (unsigned)height);
+    VKHR_LAUNCH(ctx, gather_tile_kernel<T>, grid, 256, 0, st, (const T*)dens, ctx->gat_surf, (T*)ctx->gat_stage,
+                c.res[0], c.res[1], c.res[2], shift, (uint32_t)width);
+    VKHR_CUDA_TRY(ctx, cudaGetLastError());
+    if (!ctx->gat_surf)
+        VKHR_CUDA_TRY(ctx, cudaMemcpy2DToArrayAsync(ctx->gat_array, 0, 0, ctx->gat_stage, (size_t)width * sizeof(T),
+                                                    (size_t)width * sizeof(T), (size_t)height, cudaMemcpyDeviceToDevice,
+                                                    st));
+    ok = true;
+    return VKHR_OK;
+}
+
 // cuTensorMapEncodeTiled from the driver (looked up once; NULL if unavailable).
 typedef CUresult (*TensorMapEncoder)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                      const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
@@ -558,6 +651,22 @@ vkhr_status launch(vkhr_ctx* ctx, const RayConsts& c, const void* dens, const vo
         }
         v = 0; // integer counts: the default packets
     }
+    if (v == kGatherVariant) {
+        bool ok = false;
+        vkhr_status gs = gather_density<DF>(ctx, c, dens, st, ok);
+        if (gs != VKHR_OK) return gs;
+        if (ok) {
+            RayConsts ct = c;
+            ct.tex = (unsigned long long)ctx->gat_obj;
+            ct.gshift = ctx->gat_shift;
+            const dim3 grid((rect[2] + kTileW * kWarpsX - 1) / (kTileW * kWarpsX),
+                            (rect[3] + kTileH * kWarpsY - 1) / (kTileH * kWarpsY));
+            VKHR_LAUNCH(ctx, (raymarch_kernel<DF, TF, 8, 6, kSampleGather>), grid, block, 0, st, ct,
+                        (const typename DensityTexel<DF>::T*)dens, tang, ctx->occ, din, out, dout, x0, y0, x1, y1);
+            return background ? vkhr_join_side(ctx, st) : VKHR_OK;
+        }
+        v = 0; // beyond the gather limits: the default packets
+    }
     const int tw = kRayVariants[v].tw, th = 32 / tw;
     const dim3 grid((rect[2] + tw * kWarpsX - 1) / (tw * kWarpsX), (rect[3] + th * kWarpsY - 1) / (th * kWarpsY));
     const typename DensityTexel<DF>::T* d = (const typename DensityTexel<DF>::T*)dens;
@@ -645,7 +754,8 @@ extern "C" vkhr_status vkhr_autotune_raymarch(vkhr_ctx* ctx, const vkhr_raymarch
     int best = 0;
     vkhr_status s = VKHR_OK;
     for (int v = 0; v < VKHR_RAYMARCH_VARIANTS; ++v) ms[v] = 0.0f;
-    for (int v = 0; v < kTunedVariants && s == VKHR_OK; ++v) {
+    for (const int v : kTunedVariants) {
+        if (s != VKHR_OK) break;
         ctx->ray_variant[df][tf] = v;
         float t[3] = {0.0f, 0.0f, 0.0f};
         for (int r = -1; r < 3 && s == VKHR_OK; ++r) { // one warm-up, three timed runs
@@ -658,7 +768,7 @@ extern "C" vkhr_status vkhr_autotune_raymarch(vkhr_ctx* ctx, const vkhr_raymarch
         }
         std::sort(t, t + 3);
         ms[v] = t[1];
-        if (v > 0 && ms[v] < ms[best]) best = v;
+        if (ms[v] < ms[best]) best = v;
     }
     cudaEventDestroy(e[0]);
     cudaEventDestroy(e[1]);
