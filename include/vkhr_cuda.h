@@ -495,9 +495,8 @@ vkhr_status vkhr_splat_vertices_adjoint(vkhr_ctx* ctx, const float* d_vertices, 
  *   - It runs on the current device (cudaSetDevice): the pointers and the
  *     stream must belong to that device.
  *   - The first call on a device looks up the array's device address (and
- *     the SM count); make that first call before any stream capture.  A
- *     lookup that fails returns VKHR_ERR_CUDA and is tried again by the
- *     next call.
+ *     the SM count).  A lookup that fails returns VKHR_ERR_CUDA and is tried
+ *     again by the next call.
  *   - All calls share the one array and it keeps the previous call's bits
  *     (each call clears the part it uses): calls that can overlap on the GPU
  *     (different streams, or different host threads) race; order them.
