@@ -157,9 +157,9 @@ def test_adjoint_vs_oracle_gradient(ctx, oracle_lib, shading):
         assert np.linalg.norm(g - r) <= 1e-3 * np.linalg.norm(r), np.linalg.norm(g - r) / np.linalg.norm(r)
     # kd and the exponents are sums over 12,288 pixels of terms of both signs;
     # the cancellation amplifies the FP32 image's error (dL/drgba is formed
-    # from it) to a few 1e-3 of the net sum
+    # from it): measured up to 7e-4 of the net sum (kd, reference shading)
     print("shading params", shading, gp, gp_ref[:len(gp)])
-    assert np.allclose(gp, gp_ref[:len(gp)], rtol=5e-3), (gp, gp_ref)
+    assert np.allclose(gp, gp_ref[:len(gp)], rtol=1e-3), (gp, gp_ref)
 
 
 def test_checkpoint_interval_does_not_matter(ctx, oracle_lib):
@@ -174,9 +174,12 @@ def test_checkpoint_interval_does_not_matter(ctx, oracle_lib):
 
 
 def test_splat_and_vertex_gradient(ctx, oracle_lib):
-    """splat(V) on the GPU against the FP64 oracle, and dL/dV of the loss of
+    """splat(V) on the GPU against the FP64 oracle; dL/dV of the loss of
     raymarch(splat(V)) through torch.autograd against the oracle's chain
-    (FP64 loss gradient -> FP64 splat adjoint)."""
+    (FP64 loss gradient -> FP64 splat adjoint), and, on the 24 vertex
+    coordinates of largest gradient, against FP64 central differences of the
+    oracle's loss of raymarch(splat(V)) (h = 1e-3 and h / 2 must agree,
+    else the coordinate is excluded; relative L2 <= 1e-3 over the rest)."""
     import torch
 
     O = oracle_lib
@@ -195,7 +198,35 @@ def test_splat_and_vertex_gradient(ctx, oracle_lib):
     _, gd_ref, _, _ = O.diff_loss(p, dg.detach().double().cpu().numpy(), tan.astype(np.float32), target, grads=True)
     gv_ref = O.splat_adjoint(st.vertices, b, res, gd_ref)
     assert np.linalg.norm(gv_ref) > 0
-    assert np.linalg.norm(gv - gv_ref) <= 2e-3 * np.linalg.norm(gv_ref), np.linalg.norm(gv - gv_ref) / np.linalg.norm(gv_ref)
+    rel_chain = np.linalg.norm(gv - gv_ref) / np.linalg.norm(gv_ref)
+    assert rel_chain <= 2e-4, rel_chain  # measured 1.4e-5
+
+    # FP64 central differences of the oracle's loss with respect to vertex coordinates
+    t32 = tan.astype(np.float32)
+
+    def loss_at(v):
+        return O.diff_loss(p, O.splat(v, b, res), t32, target)
+
+    coords = np.argsort(-np.abs(gv_ref).ravel())[:24]
+    got, want = [], []
+    for c in coords:
+        fds = []
+        for h in (H, H / 2):
+            lo_v, hi_v = st.vertices.copy(), st.vertices.copy()
+            x = st.vertices.ravel()[c]
+            lo_v.ravel()[c] = np.float32(x - h)
+            hi_v.ravel()[c] = np.float32(x + h)
+            span = float(hi_v.ravel()[c]) - float(lo_v.ravel()[c])
+            fds.append((loss_at(hi_v) - loss_at(lo_v)) / span)
+        if abs(fds[0] - fds[1]) <= max(TOL * max(abs(fds[0]), abs(fds[1])), FLOOR):
+            got.append(gv.ravel()[c])
+            want.append(fds[0])
+    got, want = np.array(got), np.array(want)
+    rel_fd = np.linalg.norm(got - want) / np.linalg.norm(want)
+    print("vertex gradient: chain rel %.2e; vs FP64 differences on %d of 24 coordinates rel %.2e"
+          % (rel_chain, len(got), rel_fd))
+    assert len(got) >= 16, len(got)
+    assert rel_fd <= 1e-3, rel_fd
 
 
 def test_rejects_other_formats(ctx, oracle_lib):

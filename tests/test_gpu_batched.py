@@ -267,3 +267,33 @@ def test_batch_learns_one_walk_layout(oracle_lib):
     finally:
         c.set_visit_budget(0)
         c.close()
+
+
+def test_batch_one_walk_with_wide_keys(oracle_lib):
+    """A batch one of whose styles has more than 2^23 index pairs keeps
+    (key, local voxel) visit entries of 8 bytes; its learned one-walk layout
+    and the walk into it give the oracle's voxels bit for bit."""
+    import torch
+
+    from vkhr_gb300 import _native
+
+    big = style("hemi", 700_000, 13, seed=21)  # 8.4M pairs: keys past 2^23
+    assert big[2].shape[0] // 2 > (1 << 23)
+    styles = [(big, (64, 64, 64), _abi.INDEX_REF_FP32),
+              (style("disk", 2500, 14, seed=22), (48, 48, 48), _abi.INDEX_REF_FP32)]
+    c = _native.Context(0)
+    try:
+        batch = _Batch(torch, oracle_lib, styles, True)
+        s = torch.cuda.current_stream().cuda_stream
+        for _ in range(2):  # counted (learns the layout), then one walk into it
+            batch.poison()
+            c.set_profiling(True)
+            c.voxelize_batched(True, batch.jobs, s)
+            c.check_status(s)
+            torch.cuda.synchronize()
+            names = [n for n, _ in c.profile()]
+            c.set_profiling(False)
+            batch.check(oracle_lib)
+        assert any(n.startswith("(bin_kernel<false, true, false, false, false, true>") for n in names), names
+    finally:
+        c.close()
