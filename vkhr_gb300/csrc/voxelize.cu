@@ -1737,6 +1737,8 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
     if (total_items && (!(direct_cap || use_layout) || speculative)) {
         void* ent = ctx->items;
         const int fallback = speculative ? 1 : 0; // the fill runs only after an overflow
+        // as a fallback its blocks mostly return at once: a grid of 8 per SM (grid-stride)
+        const unsigned fill_blocks = speculative ? std::min(in_blocks, (unsigned)ctx->sm_count * 8) : in_blocks;
         // spread a one-style fill's warps over distant strands when its visit
         // list is within twice the L2 size: most scattered entry stores still
         // merge in L2 (measured: a 123 MB list gains, a 1.8 GB list loses)
@@ -1745,15 +1747,15 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
 #define VKHR_FILL(SEG_, PACK_)                                                                                    \
     do {                                                                                                         \
         if (single && SEG_ && spread)                                                                            \
-            VKHR_LAUNCH(ctx, (bin_kernel<true, SEG_, PACK_, true, true>), in_blocks, threads, 0, st, jobs[0],      \
+            VKHR_LAUNCH(ctx, (bin_kernel<true, SEG_, PACK_, true, true>), fill_blocks, threads, 0, st, jobs[0],      \
                         d_jobs, nj, total_items, ctx->pair_tan, ctx->brick_visits,                 \
                         ctx->brick_cursor, ent, cap_visits, nullptr, ctx->d_words, fallback);                          \
         else if (single)                                                                                         \
-            VKHR_LAUNCH(ctx, (bin_kernel<true, SEG_, PACK_, true>), in_blocks, threads, 0, st, jobs[0], d_jobs, nj,  \
+            VKHR_LAUNCH(ctx, (bin_kernel<true, SEG_, PACK_, true>), fill_blocks, threads, 0, st, jobs[0], d_jobs, nj,  \
                         total_items, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ent,     \
                         cap_visits, nullptr, ctx->d_words, fallback);                                                  \
         else                                                                                                     \
-            VKHR_LAUNCH(ctx, (bin_kernel<true, SEG_, PACK_, false>), in_blocks, threads, bin_smem_bytes, st,       \
+            VKHR_LAUNCH(ctx, (bin_kernel<true, SEG_, PACK_, false>), fill_blocks, threads, bin_smem_bytes, st,       \
                         jobs[0], d_jobs, nj, total_items, ctx->pair_tan, ctx->brick_visits,        \
                         ctx->brick_cursor, ent, cap_visits, nullptr, ctx->d_words, fallback);                          \
     } while (0)
