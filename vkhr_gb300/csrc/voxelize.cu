@@ -236,8 +236,34 @@ struct Entry<false> {
 constexpr uint32_t kPackedKeyLimit = 1u << 23;
 constexpr uint64_t kDirectBytes = 8ull << 30; // fixed per-brick slices of a one-walk call: at most 8 GB
 
-// A run of `len` (<= 7) consecutive visits of one pair / vertex inside brick b,
-// their local voxels packed 9 bits each: counted per brick (FILL = false),
+// The local voxels (9 bits each) of a run of up to kMaxRun visits: 7 per word.
+constexpr uint32_t kMaxRun = 14;
+struct Locals {
+    uint64_t lo, hi;
+    __device__ __forceinline__ void start(uint32_t l)
+    {
+        lo = l;
+        hi = 0;
+    }
+    __device__ __forceinline__ void put(uint32_t j, uint32_t l)
+    {
+        if (j < 7) lo |= (uint64_t)l << (9 * j);
+        else hi |= (uint64_t)l << (9 * (j - 7));
+    }
+    __device__ __forceinline__ uint32_t get(uint32_t j) const
+    {
+        return (uint32_t)((j < 7 ? lo >> (9 * j) : hi >> (9 * (j - 7)))) & 511u;
+    }
+    static __device__ __forceinline__ Locals one(uint32_t l)
+    {
+        Locals r;
+        r.start(l);
+        return r;
+    }
+};
+
+// A run of `len` (<= kMaxRun) consecutive visits of one pair / vertex inside brick b,
+// their local voxels packed 9 bits each (Locals): counted per brick (FILL = false),
 // or written as (key, local voxel) entries into the brick's slice of the
 // visit list.
 // DIRECT (a counting walk that also fills): the brick's count is its cursor
@@ -246,7 +272,7 @@ constexpr uint64_t kDirectBytes = 8ull << 30; // fixed per-brick slices of a one
 // the slice is counted but not written, and raises the call's overflow word
 // (the fill pass then lays the call out compactly from the exact counts).
 template <bool FILL, bool PACK, bool DIRECT = false>
-__device__ __forceinline__ void emit_run(uint32_t b, uint32_t key, uint64_t locals, uint32_t len, uint32_t* visits,
+__device__ __forceinline__ void emit_run(uint32_t b, uint32_t key, Locals locals, uint32_t len, uint32_t* visits,
                                          uint32_t* cursor, typename Entry<PACK>::T* entries, size_t entries_cap,
                                          const uint2* __restrict__ layout, unsigned long long* words, unsigned& status)
 {
@@ -275,7 +301,7 @@ __device__ __forceinline__ void emit_run(uint32_t b, uint32_t key, uint64_t loca
         }
         if ((uint64_t)at + len <= cap) {
             typename Entry<PACK>::T* e = entries + first + at;
-            for (uint32_t j = 0; j < len; ++j) e[j] = Entry<PACK>::make(key, (uint32_t)(locals >> (9 * j)) & 511u);
+            for (uint32_t j = 0; j < len; ++j) e[j] = Entry<PACK>::make(key, locals.get(j));
         } else {
             *reinterpret_cast<volatile unsigned long long*>(words + WORD_DIRECT_OVERFLOW) = 1ull;
         }
@@ -285,7 +311,7 @@ __device__ __forceinline__ void emit_run(uint32_t b, uint32_t key, uint64_t loca
         const uint32_t base = atomicAdd(cursor + b, len);
         if ((uint64_t)base + len <= entries_cap) {
             for (uint32_t j = 0; j < len; ++j)
-                entries[base + j] = Entry<PACK>::make(key, (uint32_t)(locals >> (9 * j)) & 511u);
+                entries[base + j] = Entry<PACK>::make(key, locals.get(j));
         } else {
             status |= VKHR_DEV_LIST_OVERFLOW;
         }
@@ -344,12 +370,12 @@ __global__ void bin_kernel(const __grid_constant__ VoxJob job0, const VoxJob* __
                 pair_tan[q] = make_float4(__ldg(J.tan + 3 * (size_t)ij.x), __ldg(J.tan + 3 * (size_t)ij.x + 1),
                                           __ldg(J.tan + 3 * (size_t)ij.x + 2), 0.0f);
             uint32_t cur = kNoBrick, len = 0;
-            uint64_t locals = 0;
+            Locals locals;
             for (uint32_t k = 0; k < s.n; ++k) {
                 Visit o;
                 const bool ok = seg_visit(g, s, o);
-                if (ok && o.brick == cur && len < 7u) {
-                    locals |= (uint64_t)o.local << (9 * len);
+                if (ok && o.brick == cur && len < kMaxRun) {
+                    locals.put(len, o.local);
                     ++len;
                 } else {
                     if (len)
@@ -357,7 +383,7 @@ __global__ void bin_kernel(const __grid_constant__ VoxJob job0, const VoxJob* __
                                                      entries_cap, layout, words, status);
                     cur = ok ? o.brick : kNoBrick;
                     len = ok ? 1u : 0u;
-                    locals = ok ? (uint64_t)o.local : 0ull;
+                    locals.start(ok ? o.local : 0u);
                 }
                 seg_advance(s);
             }
@@ -367,7 +393,7 @@ __global__ void bin_kernel(const __grid_constant__ VoxJob job0, const VoxJob* __
         } else {
             Visit o;
             if (vertex_visit(g, J.v, p, o))
-                emit_run<FILL, PACK>(J.brick_base + o.brick, p, (uint64_t)o.local, 1u, visits, cursor, entries, entries_cap,
+                emit_run<FILL, PACK>(J.brick_base + o.brick, p, Locals::one(o.local), 1u, visits, cursor, entries, entries_cap,
                                      layout, words, status);
         }
     }
