@@ -277,22 +277,7 @@ __device__ __forceinline__ void emit_run(uint32_t b, uint32_t key, Locals locals
                                          const uint2* __restrict__ layout, unsigned long long* words, unsigned& status)
 {
     if (DIRECT) {
-        // The lanes that emit a run into the same brick together reserve
-        // their ranges with one returning atomic (the leader's), each lane's
-        // range after those of the lower lanes of its group.
-        const unsigned lane = lane_id();
-        const unsigned peers = __match_any_sync(__activemask(), b);
-        uint32_t before = 0, total = 0;
-        for (unsigned m = peers; m; m &= m - 1) {
-            const int src = __ffs(m) - 1;
-            const uint32_t l = __shfl_sync(peers, len, src);
-            total += l;
-            if ((unsigned)src < lane) before += l;
-        }
-        const int leader = __ffs(peers) - 1;
-        uint32_t base = 0;
-        if ((int)lane == leader) base = atomicAdd(visits + b, total);
-        const uint32_t at = __shfl_sync(peers, base, leader) + before;
+        const uint32_t at = atomicAdd(visits + b, len); // the run's range in the brick's slice
         uint64_t first = (uint64_t)b * entries_cap, cap = entries_cap;
         if (layout) {
             const uint2 sl = __ldg(layout + b);
