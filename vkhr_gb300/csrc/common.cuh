@@ -33,10 +33,12 @@ enum {
     WORD_BRICK_LIST = 9,        // brick path: occupied bricks resolved in shared memory
     WORD_BHEAVY_BIG = 10,       // brick path: crowded voxels above kCrowdWarpMax visits (listed from the back)
     WORD_DIRECT_OVERFLOW = 11,  // one-walk call: a brick outgrew its fixed slice (the fill pass lays it out)
-    WORD_NORM = 12,             // normalize: min, max (2 slots); words below are cleared per voxelization
-    WORD_AABB = 14,             // bounding-box scratch (8 slots)
-    WORD_RAY_QUEUE = 22,        // batched raymarch: next tile
-    WORD_LAYOUT_CURSOR = 24,    // voxelizer: slice cursor of a learned batch layout
+    WORD_LIGHT_LIST = 12,       // brick path: bricks of up to kLightBrick visits (a warp each)
+    WORD_LIGHT_QUEUE = 13,      // brick path: next entry of that list
+    WORD_NORM = 14,             // normalize: min, max (2 slots); words below are cleared per voxelization
+    WORD_AABB = 16,             // bounding-box scratch (8 slots)
+    WORD_RAY_QUEUE = 24,        // batched raymarch: next tile
+    WORD_LAYOUT_CURSOR = 25,    // voxelizer: slice cursor of a learned batch layout
     WORD_COUNT = 26
 };
 

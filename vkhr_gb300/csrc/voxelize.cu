@@ -47,6 +47,8 @@ namespace {
 
 constexpr int kBrickThreads = 512;     // one thread per voxel of an 8^3 brick
 constexpr int kBrickCap = 22528;       // visits a brick resolves in shared memory
+constexpr int kLightBrick = 512;       // <= this many visits: the brick is resolved by one warp
+constexpr int kLightWarps = 4;         // warps per CTA of light_brick_kernel (24 KB of shared memory)
 constexpr int kBrickThread = 16;       // <= this many visits: sorted and summed by the voxel's thread
 constexpr int kBrickSmall = 64;        // <= this many visits: sorted by one warp (2 keys per lane)
 constexpr int kBrickWarps = kBrickThreads / 32;
@@ -441,15 +443,21 @@ __global__ void __launch_bounds__(kRangeThreads) bin_ranges_kernel(const uint32_
             const uint64_t i = base + (uint64_t)j * kRangeThreads + threadIdx.x;
             if (i < nb) cursor[i] = start;
             start += c[j];
-            // visited bricks: up to kBrickCap visits listed from the front, more from the back
-            const bool small = c[j] > 0u && c[j] <= (uint32_t)kBrickCap, big = c[j] > (uint32_t)kBrickCap;
+            // visited bricks: up to kLightBrick visits listed in list[nb, 2 nb) (a warp each), up to
+            // kBrickCap from the front of list[0, nb), more from its back
+            const bool light = c[j] > 0u && c[j] <= (uint32_t)kLightBrick;
+            const bool small = c[j] > (uint32_t)kLightBrick && c[j] <= (uint32_t)kBrickCap, big = c[j] > (uint32_t)kBrickCap;
+            const unsigned ml = __ballot_sync(0xffffffffu, light);
             const unsigned m = __ballot_sync(0xffffffffu, small), mb = __ballot_sync(0xffffffffu, big);
-            uint32_t at = 0, atb = 0;
+            uint32_t at = 0, atb = 0, atl = 0;
+            if (lane == 0 && ml) atl = (uint32_t)atomicAdd(words + WORD_LIGHT_LIST, (unsigned long long)__popc(ml));
             if (lane == 0 && m) at = (uint32_t)atomicAdd(words + WORD_BRICK_LIST, (unsigned long long)__popc(m));
             if (lane == 0 && mb) atb = (uint32_t)atomicAdd(words + WORD_BIG_LIST, (unsigned long long)__popc(mb));
+            atl = __shfl_sync(0xffffffffu, atl, 0);
             at = __shfl_sync(0xffffffffu, at, 0);
             atb = __shfl_sync(0xffffffffu, atb, 0);
             const unsigned below = (1u << lane) - 1u;
+            if (light) list[nb + atl + __popc(ml & below)] = (uint32_t)i;
             if (small) list[at + __popc(m & below)] = (uint32_t)i;
             if (big) list[nb - 1u - (atb + __popc(mb & below))] = (uint32_t)i;
         }
@@ -956,6 +964,175 @@ brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__
     if (status) atomicOr(words + WORD_STATUS, (unsigned long long)status);
 }
 
+// Bricks of up to kLightBrick visits, one warp each from a device queue over
+// list[nb, 2 nb): the same results as brick_kernel with a warp's resources
+// instead of a 512-thread CTA's.  31% of the production style's visited
+// bricks are this light, with 1.2% of its visits; a CTA's phases and
+// barriers cost them as much as a full brick.  The warp counts its brick's
+// visits per local voxel, groups the keys by voxel (counting sort in its
+// shared memory), then lane l resolves the voxels l, l + 32, ...: counts and
+// u8, and the tangent from an any-order sum when certify settles it, else
+// from the keys sorted in place (insertion sort, up to kBrickSmall visits)
+// or, above that, by the crowded kernels through a descriptor.
+template <bool SEG, bool TANG, bool PACK>
+__global__ void __launch_bounds__(32 * kLightWarps)
+light_brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__ pair_tan_all,
+                   const uint32_t* __restrict__ visits, const uint32_t* __restrict__ cursor,
+                   const uint32_t* __restrict__ list, uint32_t list_n, const void* __restrict__ entries_raw,
+                   size_t entries_cap, const void* __restrict__ slots_raw, size_t slots_n, uint32_t direct_cap,
+                   const uint2* __restrict__ layout, int speculative, uint4* hdesc, size_t hdesc_cap, uint32_t* hkeys,
+                   size_t hkeys_cap, unsigned long long* words)
+{
+    typedef Entry<PACK> E;
+    typedef typename E::T ET;
+    __shared__ uint32_t s_cnt[kLightWarps][kBrickThreads]; // visits per local voxel
+    __shared__ uint32_t s_off[kLightWarps][kBrickThreads]; // each voxel's key range (end after the grouping)
+    __shared__ uint32_t s_keys[kLightWarps][kLightBrick];  // the keys grouped by voxel
+    __shared__ uint32_t s_brick_base[kMaxJobs];
+    load_bases(jobs, nj, nullptr, s_brick_base);
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    uint32_t* cnt = s_cnt[warp];
+    uint32_t* off = s_off[warp];
+    uint32_t* keys = s_keys[warp];
+    // the layout (as brick_kernel chooses it)
+    const bool direct = (direct_cap || layout) && !(speculative && words[WORD_DIRECT_OVERFLOW]);
+    const ET* ent = reinterpret_cast<const ET*>(direct ? slots_raw : entries_raw);
+    const unsigned long long ent_cap = direct ? (unsigned long long)slots_n : (unsigned long long)entries_cap;
+    const uint32_t listed = (uint32_t)words[WORD_LIGHT_LIST];
+    unsigned status = 0;
+    for (;;) {
+        uint32_t qi = 0;
+        if (lane == 0) qi = (uint32_t)atomicAdd(words + WORD_LIGHT_QUEUE, 1ull);
+        qi = __shfl_sync(0xffffffffu, qi, 0);
+        if (qi >= listed) break;
+        const uint32_t gb = list[list_n + qi];
+        const uint32_t nv = visits[gb];
+        uint32_t start, cap;
+        if (direct && layout) {
+            const uint2 sl = layout[gb];
+            start = sl.x;
+            cap = sl.y;
+        } else if (direct) {
+            start = gb * direct_cap;
+            cap = direct_cap;
+        } else {
+            start = cursor[gb] - nv;
+            cap = 0xffffffffu;
+        }
+        if ((uint64_t)start + nv > ent_cap || nv > cap || nv > (uint32_t)kLightBrick) {
+            status |= VKHR_DEV_LIST_OVERFLOW;
+            continue;
+        }
+        const uint32_t job = (uint32_t)find_job(s_brick_base, nj, gb);
+        const VoxJob& J = jobs[job];
+        const Grid& g = J.g;
+        const uint32_t b = gb - J.brick_base;
+        const float4* pair_tan = pair_tan_all + J.item_base;
+        const ET* src = ent + start;
+        for (uint32_t v = lane; v < (uint32_t)kBrickThreads; v += 32) cnt[v] = 0u;
+        __syncwarp();
+        for (uint32_t i = lane; i < nv; i += 32) atomicAdd(cnt + E::local(__ldg(src + i)), 1u);
+        __syncwarp();
+        if (TANG) { // counting sort of the keys by voxel: lane l owns the counters [16 l, 16 l + 16)
+            uint32_t run = 0;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) run += cnt[16 * lane + j];
+            uint32_t incl = run;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= (unsigned)o) incl += y;
+            }
+            run = incl - run;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                off[16 * lane + j] = run;
+                run += cnt[16 * lane + j];
+            }
+            __syncwarp();
+            for (uint32_t i = lane; i < nv; i += 32) {
+                const ET e = __ldg(src + i);
+                keys[atomicAdd(off + E::local(e), 1u)] = E::key(e);
+            }
+            __syncwarp();
+        }
+        const uint32_t bx = b % g.nbx, by = (b / g.nbx) % g.nby, bz = b / (g.nbx * g.nby);
+        for (uint32_t v = lane; v < (uint32_t)kBrickThreads; v += 32) {
+            const uint32_t x = bx * 8 + (v & 7), y = by * 8 + ((v >> 3) & 7), z = bz * 8 + (v >> 6);
+            if (!(x < g.w && y < g.h && z < g.d)) continue;
+            const uint32_t c = cnt[v];
+            const uint32_t vi = x + g.w * (y + g.h * z);
+            J.counts[vi] = c;
+            if (J.dens) J.dens[vi] = (uint8_t)(c < 255u ? c : 255u);
+            if (!TANG) continue;
+            if (c == 0u) {
+                J.tq[vi] = 0u;
+                continue;
+            }
+            uint32_t* k = keys + (off[v] - c);
+            if (c <= 255u) { // any-order sum, certified (c <= 2: every order gives the serial sum)
+                float sx = 0.0f, sy = 0.0f, sz = 0.0f, am = 0.0f;
+                for (uint32_t i0 = 0; i0 < c; i0 += kGather) {
+                    float4 tv[kGather];
+#pragma unroll
+                    for (int j = 0; j < kGather; ++j)
+                        if (i0 + j < c) tv[j] = visit_tangent<SEG>(pair_tan, J.tan, k[i0 + j]);
+#pragma unroll
+                    for (int j = 0; j < kGather; ++j)
+                        if (i0 + j < c) {
+                            sx = __fadd_rn(sx, tv[j].x);
+                            sy = __fadd_rn(sy, tv[j].y);
+                            sz = __fadd_rn(sz, tv[j].z);
+                            am = __fadd_ru(am, fmaxf(fmaxf(fabsf(tv[j].x), fabsf(tv[j].y)), fabsf(tv[j].z)));
+                        }
+                }
+                if (c <= 2u) {
+                    J.tq[vi] = pack_tangent(sx, sy, sz, c);
+                    continue;
+                }
+                const float scale = __fmul_ru((float)(c - 1), 2.05f * 5.9604645e-8f), fm = (float)c;
+                int qx, qy, qz;
+                if (certify(sx, am, scale, fm, qx) && certify(sy, am, scale, fm, qy) && certify(sz, am, scale, fm, qz)) {
+                    J.tq[vi] = ((uint32_t)(qx & 0xff)) | ((uint32_t)(qy & 0xff) << 8) | ((uint32_t)(qz & 0xff) << 16);
+                    continue;
+                }
+            }
+            if (c <= (uint32_t)kBrickSmall) { // uncertified: the keys in order (insertion sort), added in that order
+                for (uint32_t i = 1; i < c; ++i) {
+                    const uint32_t key = k[i];
+                    uint32_t j = i;
+                    while (j > 0 && k[j - 1] > key) {
+                        k[j] = k[j - 1];
+                        --j;
+                    }
+                    k[j] = key;
+                }
+                float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+                for (uint32_t i = 0; i < c; ++i) {
+                    const float4 t = visit_tangent<SEG>(pair_tan, J.tan, k[i]);
+                    sx = __fadd_rn(sx, t.x);
+                    sy = __fadd_rn(sy, t.y);
+                    sz = __fadd_rn(sz, t.z);
+                }
+                J.tq[vi] = pack_tangent(sx, sy, sz, c);
+                continue;
+            }
+            // crowded: the keys to the global scratch and a descriptor for the crowded kernels
+            const bool by_warp = c <= (uint32_t)kCrowdWarpMax;
+            const unsigned long long hd = atomicAdd(words + (by_warp ? WORD_BHEAVY_COUNT : WORD_BHEAVY_BIG), 1ull);
+            const unsigned long long hb = atomicAdd(words + WORD_HKEYS_CURSOR, (unsigned long long)c);
+            if (hb + c <= hkeys_cap && hd < hdesc_cap) {
+                for (uint32_t i = 0; i < c; ++i) hkeys[hb + i] = k[i];
+                hdesc[by_warp ? (size_t)hd : hdesc_cap - 1 - (size_t)hd] = make_uint4(vi, (uint32_t)hb, c, job);
+            } else {
+                status |= VKHR_DEV_LIST_OVERFLOW;
+            }
+        }
+        __syncwarp(); // the warp's arrays are reused by its next brick
+    }
+    if (status) atomicOr(words + WORD_STATUS, (unsigned long long)status);
+}
+
 __device__ void block_bitonic_sort(uint32_t* s, int n)
 {
     for (int k = 2; k <= n; k <<= 1)
@@ -1438,6 +1615,12 @@ vkhr_status launch_brick(vkhr_ctx* ctx, const VoxJob* d_jobs, int nj, uint32_t t
                 d_jobs, nj, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->brick_list, total_bricks,
                 ctx->items, entries_cap, ctx->slots, slots_n, direct_cap, layout, spec, ctx->hdesc, ctx->hdesc_cap,
                 ctx->hkeys, keys_cap, ctx->d_words);
+    // bricks of up to kLightBrick visits, a warp each, also on the side stream (launched before the
+    // shared-memory bricks' persistent CTAs take the SMs)
+    VKHR_LAUNCH(ctx, (light_brick_kernel<SEG, TANG, PACK>), (unsigned)ctx->sm_count * 8, 32 * kLightWarps, 0, ctx->side,
+                d_jobs, nj, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->brick_list, total_bricks,
+                ctx->items, entries_cap, ctx->slots, slots_n, direct_cap, layout, spec, ctx->hdesc, ctx->hdesc_cap,
+                ctx->hkeys, keys_cap, ctx->d_words);
     VKHR_CUDA_TRY(ctx, cudaFuncSetAttribute(brick_kernel<SEG, TANG, false, PACK>,
                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG, false, PACK>), blocks, kBrickThreads, smem, st, d_jobs, nj,
@@ -1581,7 +1764,8 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
     if (s != VKHR_OK) return s;
     ctx->brick_visits = ctx->brick_runs;
     ctx->brick_cursor = ctx->brick_runs + total_bricks;
-    s = vkhr_reserve(ctx, (void**)&ctx->brick_list, &ctx->brick_list_cap, total_bricks + 1ull, sizeof(uint32_t));
+    // visited bricks: [0, nb) the shared-memory and global-scratch bricks, [nb, 2 nb) the light ones
+    s = vkhr_reserve(ctx, (void**)&ctx->brick_list, &ctx->brick_list_cap, 2ull * total_bricks + 1ull, sizeof(uint32_t));
     if (s != VKHR_OK) return s;
     if (segments && total_items) {
         if (tang) {
@@ -1725,7 +1909,9 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
             // a batch learns (again) the layout its next calls walk once into
             if (shape) {
                 s = learn_layout(ctx, shape, total_bricks, visits_total,
-                                 ctx->h_words[WORD_BRICK_LIST] + ctx->h_words[WORD_BIG_LIST], entry_bytes, st);
+                                 ctx->h_words[WORD_LIGHT_LIST] + ctx->h_words[WORD_BRICK_LIST] +
+                                     ctx->h_words[WORD_BIG_LIST],
+                                 entry_bytes, st);
                 if (s != VKHR_OK) return s;
             }
         }
