@@ -137,8 +137,8 @@ vkhr_status vkhr_create(int device, vkhr_ctx** out)
         e = cudaDeviceGetAttribute(&ctx->smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device);
     if (e == cudaSuccess)
         e = cudaDeviceGetAttribute(&ctx->smem_reserved, cudaDevAttrReservedSharedMemoryPerBlock, device);
-    ctx->walk_ctas[0] = 0; // no residency limit: measured fastest for both kinds of call with the
-    ctx->walk_ctas[1] = 0; // warp-aggregated reservations (vkhr_autotune_voxelize retunes per workload)
+    ctx->walk_ctas[0] = 0; // no residency limit for the one walk: measured fastest on both workloads
+    ctx->walk_ctas[1] = 0; // (vkhr_autotune_voxelize retunes per workload)
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_words, WORD_COUNT * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMemset(ctx->d_words, 0, WORD_COUNT * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_words, WORD_COUNT * sizeof(unsigned long long));

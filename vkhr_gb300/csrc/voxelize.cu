@@ -337,7 +337,7 @@ __global__ void bin_kernel(const __grid_constant__ VoxJob job0, const VoxJob* __
     // stores merge in L2 there; a much larger list would reach DRAM as
     // partial sectors, so it keeps consecutive items per warp, as do the
     // counting and one-walk passes (coalesced index, vertex and pair-tangent
-    // accesses, and the one walk's warp-aggregated reservations) and a batch.
+    // accesses) and a batch.
     constexpr bool sp = FILL && SINGLE && SEG && SPREAD;
     const uint64_t cols = (total_items + 31) / 32;
     const uint64_t span = sp ? cols * 32 : total_items;
