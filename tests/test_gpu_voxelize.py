@@ -311,3 +311,32 @@ def test_downsample(ctx, oracle_lib, filt):
     assert np.array_equal(out.cpu().numpy(), ref)
     with pytest.raises(Exception):
         ctx.downsample_densities(din.data_ptr(), (63, 38, 50), filt, out.data_ptr())  # odd width
+
+
+def test_light_brick_rare_paths(ctx, oracle_lib):
+    """Bricks of up to 512 visits are resolved by one warp each; their rare
+    paths against the oracle, in both modes: a voxel of 100 visits (a crowded
+    voxel's keys handed to the crowded kernels), one of 300 (past the stop at
+    255), and voxels of 3..64 visits whose tangents all sit next to one
+    quantization step (k / 127 per cluster, jittered by 1e-6), so that
+    certification fails and the keys are sorted in place.  Each cluster is one
+    voxel in its own brick of a 64^3 grid, every brick below 512 visits."""
+    rng = np.random.default_rng(12)
+    b = _abi.aabb_from((0.0, 0.0, 0.0), (1.0, 1.0, 1.0))
+    vox = 1.0 / 64.0
+    clusters = [(100, (4, 4, 4)), (300, (20, 4, 4)), (40, (36, 4, 4)), (17, (52, 4, 4)), (5, (4, 20, 4)),
+                (64, (4, 36, 4)), (3, (4, 52, 4))]
+    for mode in ("vertices", "segments"):
+        verts, tans = [], []
+        for n, (x, y, z) in clusters:  # n visits: n vertices, or n pairs of two vertices in the voxel
+            centre = (np.array([x, y, z], dtype=np.float64) + 0.5) * vox
+            k = int(rng.integers(20, 100))
+            for _ in range(n if mode == "vertices" else 2 * n):
+                verts.append(centre + rng.uniform(-0.3, 0.3, 3) * vox)
+                tans.append([k / 127.0 + rng.normal(0.0, 1e-6), -(k / 127.0) + rng.normal(0.0, 1e-6),
+                             0.5 + rng.normal(0.0, 1e-6)])
+        v = np.asarray(verts, dtype=np.float32)
+        t = np.asarray(tans, dtype=np.float32)
+        idx = np.arange(v.shape[0], dtype=np.uint32)
+        c = _check(ctx, oracle_lib, mode, v, t, idx, b, (64, 64, 64))
+        assert sorted(c[c > 0].tolist()) == sorted(n for n, _ in clusters)
