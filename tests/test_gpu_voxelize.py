@@ -340,3 +340,42 @@ def test_light_brick_rare_paths(ctx, oracle_lib):
         idx = np.arange(v.shape[0], dtype=np.uint32)
         c = _check(ctx, oracle_lib, mode, v, t, idx, b, (64, 64, 64))
         assert sorted(c[c > 0].tolist()) == sorted(n for n, _ in clusters)
+
+
+def test_uncertified_voxels_past_the_descriptor_list(native_lib, oracle_lib):
+    """Voxels of up to 64 visits whose tangents all sit next to a
+    quantization step (k / 127 jittered by a few ulps) cannot be certified;
+    the brick kernels hand them to the crowded-warp kernel through a
+    descriptor list behind the crowded voxels' (as long as theirs), and past
+    its end the voxel's own thread sorts its keys in place.  A fresh context
+    per call, so the list is no longer than one call sizes it: 4 bricks of
+    512 voxels of 3 visits (keys in shared memory), then 24 bricks of 512
+    voxels of 45 visits (552,960 visits: keys in the global scratch), each
+    with more uncertified voxels than the list holds, in both modes, against
+    the oracle (the sums of some of these voxels differ by order)."""
+    from vkhr_gb300 import _native
+
+    rng = np.random.default_rng(21)
+    b = _abi.aabb_from((0.0, 0.0, 0.0), (1.0, 1.0, 1.0))
+    vox = 1.0 / 32.0
+    cases = [(4, 3, 3e-8), (24, 45, 3e-7)]  # bricks, visits per voxel, tangent jitter
+    for mode in ("vertices", "segments"):
+        for nb, n, jitter in cases:
+            per = n if mode == "vertices" else 2 * n   # points per voxel: n vertices, or n pairs
+            lx = np.arange(512) % 8
+            ly = (np.arange(512) // 8) % 8
+            lz = np.arange(512) // 64
+            cells = np.concatenate([np.stack([8 * (j % 4) + lx, 8 * ((j // 4) % 4) + ly, 8 * (j // 16) + lz], 1)
+                                    for j in range(nb)])
+            centre = np.repeat((cells + 0.5) * vox, per, axis=0)
+            v = (centre + rng.uniform(-0.3, 0.3, centre.shape) * vox).astype(np.float32)
+            k = np.repeat(rng.integers(20, 100, len(cells)), per)
+            t = np.stack([(k / 127.0).astype(np.float32) + rng.normal(0.0, jitter, len(k)),
+                          np.full(len(k), 0.25), np.full(len(k), 0.5)], 1).astype(np.float32)
+            idx = np.arange(v.shape[0], dtype=np.uint32)
+            c = _native.Context(0)
+            try:
+                got = _check(c, oracle_lib, mode, v, t, idx, b, (32, 32, 32))
+            finally:
+                c.close()
+            assert (got == n).sum() == 512 * nb and got.sum() == 512 * nb * n

@@ -35,11 +35,12 @@ enum {
     WORD_DIRECT_OVERFLOW = 11,  // one-walk call: a brick outgrew its fixed slice (the fill pass lays it out)
     WORD_LIGHT_LIST = 12,       // brick path: bricks of up to kLightBrick visits (a warp each)
     WORD_LIGHT_QUEUE = 13,      // brick path: next entry of that list
-    WORD_NORM = 14,             // normalize: min, max (2 slots); words below are cleared per voxelization
-    WORD_AABB = 16,             // bounding-box scratch (8 slots)
-    WORD_RAY_QUEUE = 24,        // batched raymarch: next tile
-    WORD_LAYOUT_CURSOR = 25,    // voxelizer: slice cursor of a learned batch layout
-    WORD_COUNT = 26
+    WORD_UNCERT_COUNT = 14,     // brick path: uncertified voxels handed to the crowded-warp kernel
+    WORD_NORM = 15,             // normalize: min, max (2 slots); words below are cleared per voxelization
+    WORD_AABB = 17,             // bounding-box scratch (8 slots)
+    WORD_RAY_QUEUE = 25,        // batched raymarch: next tile
+    WORD_LAYOUT_CURSOR = 26,    // voxelizer: slice cursor of a learned batch layout
+    WORD_COUNT = 27
 };
 
 // Visit total of an earlier unbudgeted one-style segment voxelization, by
@@ -83,7 +84,7 @@ struct vkhr_ctx {
     size_t pair_tan_cap;
     uint32_t* hkeys;           // voxelizer: key scratch (crowded voxels, bricks above the shared-memory cap)
     size_t hkeys_cap;
-    uint4* hdesc;              // voxelizer: crowded voxels (voxel, key offset, count, job)
+    uint4* hdesc;              // voxelizer: crowded, then uncertified voxels (voxel, key offset, count, job)
     size_t hdesc_cap;
     void* d_jobs;              // voxelizer: device job table of the current batch
     size_t jobs_cap;           // in bytes

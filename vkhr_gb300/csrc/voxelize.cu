@@ -49,9 +49,7 @@ constexpr int kBrickThreads = 512;     // one thread per voxel of an 8^3 brick
 constexpr int kBrickCap = 22528;       // visits a brick resolves in shared memory
 constexpr int kLightBrick = 512;       // <= this many visits: the brick is resolved by one warp
 constexpr int kLightWarps = 4;         // warps per CTA of light_brick_kernel (24 KB of shared memory)
-constexpr int kBrickThread = 16;       // <= this many visits: sorted and summed by the voxel's thread
 constexpr int kBrickSmall = 64;        // <= this many visits: sorted by one warp (2 keys per lane)
-constexpr int kBrickWarps = kBrickThreads / 32;
 constexpr int kCrowdWarpMax = 256;     // crowded voxels up to this many visits: one warp each
 constexpr int kGather = 4;             // tangent loads in flight per voxel thread (64 registers at 2 CTAs / SM)
 constexpr int kHeavyTile = 2048;       // crowded voxels: shared-memory sort tile
@@ -608,60 +606,6 @@ __device__ __forceinline__ uint32_t block_exclusive_scan_512(uint32_t x, uint32_
     return warp_sums[warp] + incl - x;
 }
 
-// Ascending bitonic sort of 64 keys held two per lane (index lane and lane + 32).
-__device__ __forceinline__ void warp_sort64(uint32_t& a, uint32_t& b)
-{
-    const unsigned lane = lane_id();
-#pragma unroll
-    for (unsigned k = 2; k <= 64; k <<= 1) {
-#pragma unroll
-        for (unsigned j = k >> 1; j > 0; j >>= 1) {
-            if (j == 32) { // partner is the lane's other register
-                const bool up = (lane & k) == 0;
-                if ((a > b) == up) { const uint32_t t = a; a = b; b = t; }
-            } else {
-                const bool lower = (lane & j) == 0;
-                const uint32_t oa = __shfl_xor_sync(0xffffffffu, a, j), ob = __shfl_xor_sync(0xffffffffu, b, j);
-                const bool upa = (lane & k) == 0, upb = ((lane + 32) & k) == 0;
-                a = (lower == upa) ? min(a, oa) : max(a, oa);
-                b = (lower == upb) ? min(b, ob) : max(b, ob);
-            }
-        }
-    }
-}
-
-// Ascending sort of a voxel's c <= N keys at k (shared memory) in registers:
-// a bitonic network (compile-time indices, so every compare-exchange is a
-// min and a max), the slots past c padded with the largest key.  The loads
-// and stores are independent of one another, unlike an insertion sort's
-// chain of dependent shared-memory reads.
-template <int N>
-__device__ __forceinline__ void sort_keys(uint32_t* k, uint32_t c)
-{
-    uint32_t r[N];
-#pragma unroll
-    for (int i = 0; i < N; ++i) r[i] = (uint32_t)i < c ? k[i] : 0xffffffffu;
-#pragma unroll
-    for (int s = 2; s <= N; s <<= 1) {
-#pragma unroll
-        for (int j = s >> 1; j > 0; j >>= 1) {
-#pragma unroll
-            for (int i = 0; i < N; ++i) {
-                const int l = i ^ j;
-                if (l > i) {
-                    const uint32_t a = r[i], b = r[l];
-                    const bool up = (i & s) == 0;
-                    r[i] = up ? min(a, b) : max(a, b);
-                    r[l] = up ? max(a, b) : min(a, b);
-                }
-            }
-        }
-    }
-#pragma unroll
-    for (int i = 0; i < N; ++i)
-        if ((uint32_t)i < c) k[i] = r[i];
-}
-
 template <bool SEG>
 __device__ __forceinline__ float4 visit_tangent(const float4* __restrict__ pair_tan, const float* __restrict__ tan,
                                                 uint32_t key)
@@ -693,18 +637,19 @@ __device__ __forceinline__ bool certify(float f, float a, float bound_scale, flo
 // Per-voxel results of one brick whose visit keys are grouped by local voxel
 // at `keys` (shared memory, or the global scratch for bricks above
 // kBrickCap): counts and u8 densities, and the tangents.  Every voxel's thread
-// adds its tangents in the order its keys were grouped and certifies the
-// quantized result (certify); the voxels it cannot certify have their keys
-// sorted in place -- up to kBrickThread by the voxel's own thread (register
-// sorting network), up to kBrickSmall by a warp (64-key register bitonic
-// sort) -- and summed again in key order; more than kBrickSmall visits go to
-// crowded_kernel through a descriptor.  Block-wide.
+// of up to kBrickSmall visits adds its tangents in the order its keys were
+// grouped and certifies the quantized result (certify).  The voxels it cannot
+// certify, and those of more than kBrickSmall visits, go to the crowded
+// kernels through a descriptor (their keys copied to the global scratch),
+// which sort the keys and add the tangents in key order; should the
+// descriptor list be full, an uncertified voxel's thread sorts its keys in
+// place (insertion sort) and adds them in order itself.  Block-wide.
 template <bool SEG, bool TANG>
 __device__ __forceinline__ void resolve_brick(const VoxJob& J, const Grid& g, uint32_t b, const float4* pair_tan,
                                               const uint32_t* cnt, const uint32_t* off, uint32_t* keys,
-                                              bool keys_global, uint32_t keys_at, uint32_t* wlist, uint32_t& wcount,
-                                              uint4* hdesc, size_t hdesc_cap, uint32_t* hkeys, size_t hkeys_cap,
-                                              uint32_t job, unsigned long long* words, unsigned& status)
+                                              bool keys_global, uint32_t keys_at,
+                                              uint4* hdesc, size_t hdesc_cap, size_t uncert_cap, uint32_t* hkeys,
+                                              size_t hkeys_cap, uint32_t job, unsigned long long* words, unsigned& status)
 {
     const int tid = threadIdx.x;
     const float* tan = J.tan;
@@ -756,64 +701,56 @@ __device__ __forceinline__ void resolve_brick(const VoxJob& J, const Grid& g, ui
             }
         }
     }
-    if (inside && c > (uint32_t)kBrickSmall) { // crowded: a warp or a CTA of its own sorts the keys
-        // descriptors of up to kCrowdWarpMax visits from the front, larger ones from the back
-        const bool by_warp = c <= (uint32_t)kCrowdWarpMax;
-        const unsigned long long hd = atomicAdd(words + (by_warp ? WORD_BHEAVY_COUNT : WORD_BHEAVY_BIG), 1ull);
-        const size_t at = by_warp ? (size_t)hd : hdesc_cap - 1 - (size_t)hd;
-        if (keys_global) { // already in the scratch
-            if (hd < hdesc_cap) hdesc[at] = make_uint4(vi, keys_at + off[tid] - c, c, job);
-            else status |= VKHR_DEV_LIST_OVERFLOW;
+    if (inside && (c > (uint32_t)kBrickSmall || sorted_needed)) {
+        // crowded: the crowded kernels sort the keys (a warp up to kCrowdWarpMax visits,
+        // descriptors from the front of the crowded list; a CTA above, from its back);
+        // uncertified: a warp of the crowded-warp kernel, from the list behind it
+        unsigned long long hd;
+        size_t at;
+        bool slot;
+        if (sorted_needed) {
+            hd = atomicAdd(words + WORD_UNCERT_COUNT, 1ull);
+            at = hdesc_cap + (size_t)hd;
+            slot = hd < uncert_cap;
         } else {
+            const bool by_warp = c <= (uint32_t)kCrowdWarpMax;
+            hd = atomicAdd(words + (by_warp ? WORD_BHEAVY_COUNT : WORD_BHEAVY_BIG), 1ull);
+            at = by_warp ? (size_t)hd : hdesc_cap - 1 - (size_t)hd;
+            slot = hd < hdesc_cap;
+        }
+        bool listed = false;
+        if (slot && keys_global) { // already in the scratch
+            hdesc[at] = make_uint4(vi, keys_at + off[tid] - c, c, job);
+            listed = true;
+        } else if (slot) {
             const unsigned long long hb = atomicAdd(words + WORD_HKEYS_CURSOR, (unsigned long long)c);
-            if (hb + c <= hkeys_cap && hd < hdesc_cap) {
+            listed = hb + c <= hkeys_cap;
+            if (listed)
                 for (uint32_t i = 0; i < c; ++i) hkeys[hb + i] = k[i];
-                hdesc[at] = make_uint4(vi, (uint32_t)hb, c, job);
-            } else {
-                status |= VKHR_DEV_LIST_OVERFLOW;
-            }
+            // every slot below the count is written: count 0 marks one the crowded kernels skip
+            hdesc[at] = listed ? make_uint4(vi, (uint32_t)hb, c, job) : make_uint4(0u, 0u, 0u, 0u);
         }
-    } else if (sorted_needed && c > (uint32_t)kBrickThread) {
-        wlist[atomicAdd(&wcount, 1u)] = (uint32_t)tid; // sorted by a warp below
-    }
-    {   // up to kBrickThread keys: sorted by the voxel's thread in registers, with the
-        // network of the warp's largest such voxel (only voxels that need it)
-        const uint32_t ct = sorted_needed && c <= (uint32_t)kBrickThread ? c : 0u;
-        const uint32_t nmax = __reduce_max_sync(0xffffffffu, ct);
-        if (nmax > 8) sort_keys<16>(k, ct);
-        else if (nmax > 4) sort_keys<8>(k, ct);
-        else if (nmax > 1) sort_keys<4>(k, ct);
-    }
-    __syncthreads();
-    {   // kBrickThread < count <= kBrickSmall, uncertified: a warp sorts the keys in place (two per lane)
-        const unsigned lane = lane_id(), warp = (unsigned)tid >> 5;
-        for (uint32_t m = warp; m < wcount; m += kBrickWarps) {
-            const uint32_t l = wlist[m], cl = cnt[l];
-            uint32_t* kl = keys + (off[l] - cl);
-            uint32_t ka = lane < cl ? kl[lane] : 0xffffffffu, kb = lane + 32 < cl ? kl[lane + 32] : 0xffffffffu;
-            warp_sort64(ka, kb);
-            if (lane < cl) kl[lane] = ka;
-            if (lane + 32 < cl) kl[lane + 32] = kb;
-        }
-    }
-    __syncthreads();
-    if (sorted_needed) { // the uncertified voxels: their tangents added in key order
-        const uint32_t* ks = keys + (off[tid] - c);
-        float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-        for (uint32_t i0 = 0; i0 < c; i0 += kGather) {
-            float4 tv[kGather];
-#pragma unroll
-            for (int j = 0; j < kGather; ++j)
-                if (i0 + j < c) tv[j] = visit_tangent<SEG>(pair_tan, tan, ks[i0 + j]);
-#pragma unroll
-            for (int j = 0; j < kGather; ++j)
-                if (i0 + j < c) {
-                    sx = __fadd_rn(sx, tv[j].x);
-                    sy = __fadd_rn(sy, tv[j].y);
-                    sz = __fadd_rn(sz, tv[j].z);
+        if (!listed && sorted_needed) { // the list is full: this thread sorts the keys in place
+            for (uint32_t i = 1; i < c; ++i) {
+                const uint32_t key = k[i];
+                uint32_t j = i;
+                while (j > 0 && k[j - 1] > key) {
+                    k[j] = k[j - 1];
+                    --j;
                 }
+                k[j] = key;
+            }
+            float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+            for (uint32_t i = 0; i < c; ++i) {
+                const float4 t = visit_tangent<SEG>(pair_tan, tan, k[i]);
+                sx = __fadd_rn(sx, t.x);
+                sy = __fadd_rn(sy, t.y);
+                sz = __fadd_rn(sz, t.z);
+            }
+            tq[vi] = pack_tangent(sx, sy, sz, c);
+        } else if (!listed) {
+            status |= VKHR_DEV_LIST_OVERFLOW;
         }
-        tq[vi] = pack_tangent(sx, sy, sz, c);
     }
 }
 
@@ -827,7 +764,9 @@ __device__ __forceinline__ void resolve_brick(const VoxJob& J, const Grid& g, ui
 // call: [brick * direct_cap, + count), or with a learned layout
 // [layout[brick].x, + count).  The next brick's queue slot
 // and bounds are fetched while the current one is processed, and the entry
-// passes keep kBrickUnroll loads in flight per thread.
+// passes keep kBrickUnroll loads in flight per thread.  Descriptors for the
+// crowded kernels: crowded voxels in hdesc[0, hdesc_cap) (from the front and
+// the back), uncertified ones in hdesc[hdesc_cap, + uncert_cap).
 constexpr int kBrickUnroll = 4;
 
 template <bool SEG, bool TANG, bool BIG, bool PACK>
@@ -836,8 +775,8 @@ brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__
              const uint32_t* __restrict__ visits, const uint32_t* __restrict__ cursor, const uint32_t* __restrict__ list,
              uint32_t list_n, const void* __restrict__ entries_raw, size_t entries_cap,
              const void* __restrict__ slots_raw, size_t slots_n, uint32_t direct_cap, const uint2* __restrict__ layout,
-             int speculative, uint4* hdesc, size_t hdesc_cap, uint32_t* hkeys, size_t hkeys_cap,
-             unsigned long long* words)
+             int speculative, uint4* hdesc, size_t hdesc_cap, size_t uncert_cap, uint32_t* hkeys,
+             size_t hkeys_cap, unsigned long long* words)
 {
     typedef Entry<PACK> E;
     typedef typename E::T ET;
@@ -860,9 +799,8 @@ brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__
     uint32_t* cnt = sm;                       // visits per local voxel
     uint32_t* off = sm + kBrickThreads;       // slice cursor per local voxel
     uint32_t* warp_sums = sm + 2 * kBrickThreads;
-    uint32_t* wlist = sm + 2 * kBrickThreads + 32;             // voxels for the warp sort
-    uint32_t* keys = wlist + kBrickThreads;                    // (BIG = false only)
-    __shared__ uint32_t s_gb, s_nv, s_start, s_cap, wcount, s_job, s_hb;
+    uint32_t* keys = sm + 2 * kBrickThreads + 32;              // (BIG = false only)
+    __shared__ uint32_t s_gb, s_nv, s_start, s_cap, s_job, s_hb;
     __shared__ uint32_t s_brick_base[kMaxJobs];
     load_bases(jobs, nj, nullptr, s_brick_base);
     const int tid = threadIdx.x;
@@ -899,7 +837,6 @@ brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__
             s_nv = nnv;
             s_start = nstart;
             s_cap = ncap;
-            wcount = 0;
             if (nq < listed) {
                 s_job = (uint32_t)find_job(s_brick_base, nj, ngb);
                 s_hb = (TANG && BIG) ? (uint32_t)atomicAdd(words + WORD_HKEYS_CURSOR, (unsigned long long)nnv) : 0u;
@@ -956,7 +893,7 @@ brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __restrict__
                 }
                 __syncthreads(); // also orders the scratch writes before the block's reads
             }
-            resolve_brick<SEG, TANG>(J, g, b, pair_tan, cnt, off, kbase, BIG, s_hb, wlist, wcount, hdesc, hdesc_cap,
+            resolve_brick<SEG, TANG>(J, g, b, pair_tan, cnt, off, kbase, BIG, s_hb, hdesc, hdesc_cap, uncert_cap,
                                      hkeys, hkeys_cap, s_job, words, status);
         }
         __syncthreads();
@@ -1120,10 +1057,15 @@ light_brick_kernel(const VoxJob* __restrict__ jobs, int nj, const float4* __rest
             // crowded: the keys to the global scratch and a descriptor for the crowded kernels
             const bool by_warp = c <= (uint32_t)kCrowdWarpMax;
             const unsigned long long hd = atomicAdd(words + (by_warp ? WORD_BHEAVY_COUNT : WORD_BHEAVY_BIG), 1ull);
-            const unsigned long long hb = atomicAdd(words + WORD_HKEYS_CURSOR, (unsigned long long)c);
-            if (hb + c <= hkeys_cap && hd < hdesc_cap) {
-                for (uint32_t i = 0; i < c; ++i) hkeys[hb + i] = k[i];
-                hdesc[by_warp ? (size_t)hd : hdesc_cap - 1 - (size_t)hd] = make_uint4(vi, (uint32_t)hb, c, job);
+            if (hd < hdesc_cap) {
+                const unsigned long long hb = atomicAdd(words + WORD_HKEYS_CURSOR, (unsigned long long)c);
+                const bool fits = hb + c <= hkeys_cap;
+                if (fits)
+                    for (uint32_t i = 0; i < c; ++i) hkeys[hb + i] = k[i];
+                // every slot below the count is written: count 0 marks one the crowded kernels skip
+                hdesc[by_warp ? (size_t)hd : hdesc_cap - 1 - (size_t)hd] =
+                    fits ? make_uint4(vi, (uint32_t)hb, c, job) : make_uint4(0u, 0u, 0u, 0u);
+                if (!fits) status |= VKHR_DEV_LIST_OVERFLOW;
             } else {
                 status |= VKHR_DEV_LIST_OVERFLOW;
             }
@@ -1370,17 +1312,19 @@ constexpr int kCrowdWarps = 8; // warps per CTA of crowded_warp_kernel
 __global__ void __launch_bounds__(32 * kCrowdWarps) crowded_warp_kernel(const VoxJob* __restrict__ jobs,
                                                                         const float4* __restrict__ pair_tan_all,
                                                                         const uint4* __restrict__ hdesc,
-                                                                        size_t hdesc_cap,
+                                                                        size_t hdesc_cap, size_t uncert_cap,
                                                                         const uint32_t* __restrict__ hkeys,
                                                                         const unsigned long long* words)
 {
     __shared__ float wt[kCrowdWarps][3][kKeep];
-    unsigned long long nh = words[WORD_BHEAVY_COUNT];
+    unsigned long long nh = words[WORD_BHEAVY_COUNT], nu = words[WORD_UNCERT_COUNT];
     if (nh > hdesc_cap) nh = hdesc_cap;
+    if (nu > uncert_cap) nu = uncert_cap;
     const unsigned warp = threadIdx.x >> 5;
-    for (unsigned long long h = (unsigned long long)blockIdx.x * kCrowdWarps + warp; h < nh;
+    for (unsigned long long h = (unsigned long long)blockIdx.x * kCrowdWarps + warp; h < nh + nu;
          h += (unsigned long long)gridDim.x * kCrowdWarps) {
-        const uint4 d = hdesc[h];
+        const uint4 d = hdesc[h < nh ? h : hdesc_cap + (h - nh)];
+        if (d.z == 0u) continue; // a slot whose keys did not fit the scratch
         const VoxJob& J = jobs[d.w];
         if (d.z <= 128u) resolve_warp<4>(J, pair_tan_all, hkeys + d.y, d.z, wt[warp], J.tq + d.x);
         else resolve_warp<8>(J, pair_tan_all, hkeys + d.y, d.z, wt[warp], J.tq + d.x);
@@ -1400,6 +1344,7 @@ __global__ void __launch_bounds__(kCrowdThreads) crowded_kernel(const VoxJob* __
     if (nh > hdesc_cap) nh = hdesc_cap;
     for (unsigned long long h = blockIdx.x; h < nh; h += gridDim.x) {
         const uint4 d = hdesc[hdesc_cap - 1 - h];
+        if (d.z == 0u) continue; // a slot whose keys did not fit the scratch
         const VoxJob& J = jobs[d.w];
         resolve_crowded(hkeys + d.y, d.z, J.tan, J.pairs, keys, tv, J.tq + d.x);
     }
@@ -1602,31 +1547,31 @@ void learn_visits(vkhr_ctx* ctx, const vkhr_voxel_job& j, bool tang, uint64_t vi
 template <bool SEG, bool TANG, bool PACK>
 vkhr_status launch_brick(vkhr_ctx* ctx, const VoxJob* d_jobs, int nj, uint32_t total_bricks, cudaStream_t st,
                          unsigned blocks, size_t entries_cap, size_t keys_cap, uint32_t direct_cap,
-                         const uint2* layout, size_t slots_n, bool speculative)
+                         const uint2* layout, size_t slots_n, bool speculative, size_t crowd_cap, size_t uncert_cap)
 {
     const int spec = speculative ? 1 : 0;
     // bricks above kBrickCap (their keys go to the global scratch) on the side
     // stream, alongside the rest on st; the caller joins the side stream
-    const size_t small = (size_t)(2 * kBrickThreads + 32 + kBrickThreads) * sizeof(uint32_t);
+    const size_t small = (size_t)(2 * kBrickThreads + 32) * sizeof(uint32_t); // counters, cursors, warp sums
     const size_t smem = small + (TANG ? (size_t)kBrickCap * sizeof(uint32_t) : 0);
     vkhr_status s = vkhr_fork_side(ctx, st); // after the fill
     if (s != VKHR_OK) return s;
     VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG, true, PACK>), (unsigned)ctx->sm_count * 2, kBrickThreads, small, ctx->side,
                 d_jobs, nj, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->brick_list, total_bricks,
-                ctx->items, entries_cap, ctx->slots, slots_n, direct_cap, layout, spec, ctx->hdesc, ctx->hdesc_cap,
-                ctx->hkeys, keys_cap, ctx->d_words);
+                ctx->items, entries_cap, ctx->slots, slots_n, direct_cap, layout, spec, ctx->hdesc, crowd_cap,
+                uncert_cap, ctx->hkeys, keys_cap, ctx->d_words);
     // bricks of up to kLightBrick visits, a warp each, also on the side stream (launched before the
     // shared-memory bricks' persistent CTAs take the SMs)
     VKHR_LAUNCH(ctx, (light_brick_kernel<SEG, TANG, PACK>), (unsigned)ctx->sm_count * 8, 32 * kLightWarps, 0, ctx->side,
                 d_jobs, nj, ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->brick_list, total_bricks,
-                ctx->items, entries_cap, ctx->slots, slots_n, direct_cap, layout, spec, ctx->hdesc, ctx->hdesc_cap,
+                ctx->items, entries_cap, ctx->slots, slots_n, direct_cap, layout, spec, ctx->hdesc, crowd_cap,
                 ctx->hkeys, keys_cap, ctx->d_words);
     VKHR_CUDA_TRY(ctx, cudaFuncSetAttribute(brick_kernel<SEG, TANG, false, PACK>,
                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     VKHR_LAUNCH(ctx, (brick_kernel<SEG, TANG, false, PACK>), blocks, kBrickThreads, smem, st, d_jobs, nj,
                 ctx->pair_tan, ctx->brick_visits, ctx->brick_cursor, ctx->brick_list, total_bricks, ctx->items,
-                entries_cap, ctx->slots, slots_n, direct_cap, layout, spec, ctx->hdesc, ctx->hdesc_cap, ctx->hkeys, keys_cap,
-                ctx->d_words);
+                entries_cap, ctx->slots, slots_n, direct_cap, layout, spec, ctx->hdesc, crowd_cap, uncert_cap, ctx->hkeys,
+                keys_cap, ctx->d_words);
     return VKHR_OK;
 }
 
@@ -1918,13 +1863,16 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
     }
     // capacities the kernels check against (the budget, not the grown scratch)
     const size_t cap_visits = visits_total ? (size_t)visits_total : 1;
+    const size_t crowd_cap = (size_t)(visits_total / (kBrickSmall + 1)) + 1;
     if (tang) {
         s = vkhr_reserve(ctx, (void**)&ctx->hkeys, &ctx->hkeys_cap, visits_total ? visits_total : 1, sizeof(uint32_t));
         if (s != VKHR_OK) return s;
-        s = vkhr_reserve(ctx, (void**)&ctx->hdesc, &ctx->hdesc_cap, visits_total / (kBrickSmall + 1) + 1,
-                         sizeof(uint4));
+        // crowded voxels (above kBrickSmall visits: at most crowd_cap of them), then as many
+        // uncertified ones at least (past the list's end their own threads sort their keys)
+        s = vkhr_reserve(ctx, (void**)&ctx->hdesc, &ctx->hdesc_cap, 2 * crowd_cap, sizeof(uint4));
         if (s != VKHR_OK) return s;
     }
+    const size_t uncert_cap = tang ? ctx->hdesc_cap - crowd_cap : 0;
     // Unvisited bricks are zeroed on the side stream, alongside the fill and
     // the brick kernel (disjoint voxels); every return below joins it.
     s = vkhr_fork_side(ctx, st);
@@ -1965,7 +1913,7 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
     const unsigned bblocks = std::min(total_bricks, (unsigned)ctx->sm_count * 2);
 #define VKHR_BRICK(SEG_, TANG_, PACK_)                                                                            \
     launch_brick<SEG_, TANG_, PACK_>(ctx, d_jobs, nj, total_bricks, st, bblocks, cap_visits, cap_visits, direct_cap,     \
-                                     use_layout ? ctx->layout : nullptr, slots_n, speculative)
+                                     use_layout ? ctx->layout : nullptr, slots_n, speculative, crowd_cap, uncert_cap)
     if (segments) {
         if (!tang) s = VKHR_BRICK(true, false, true);
         else if (pack) s = VKHR_BRICK(true, true, true);
@@ -1983,9 +1931,9 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
         s = vkhr_fork_side(ctx, st);
         if (s != VKHR_OK) return s;
         VKHR_LAUNCH(ctx, crowded_kernel, (unsigned)ctx->sm_count * 6, kCrowdThreads, 0, ctx->side, d_jobs, ctx->hdesc,
-                    ctx->hdesc_cap, ctx->hkeys, ctx->d_words);
+                    crowd_cap, ctx->hkeys, ctx->d_words);
         VKHR_LAUNCH(ctx, crowded_warp_kernel, (unsigned)ctx->sm_count * 8, 32 * kCrowdWarps, 0, st, d_jobs,
-                    ctx->pair_tan, ctx->hdesc, ctx->hdesc_cap, ctx->hkeys, ctx->d_words);
+                    ctx->pair_tan, ctx->hdesc, crowd_cap, uncert_cap, ctx->hkeys, ctx->d_words);
         s = vkhr_join_side(ctx, st);
         if (s != VKHR_OK) return s;
     }
