@@ -303,6 +303,116 @@ __device__ __forceinline__ void emit_run(uint32_t b, uint32_t key, Locals locals
     }
 }
 
+// The visits of pair p (set up in s) in order, emitted as runs of up to
+// kMaxRun consecutive visits inside one brick.
+template <bool FILL, bool PACK, bool DIRECT>
+__device__ __forceinline__ void walk_pair(const VoxJob& J, uint32_t p, Seg& s, uint32_t* visits, uint32_t* cursor,
+                                          typename Entry<PACK>::T* entries, size_t entries_cap,
+                                          const uint2* __restrict__ layout, unsigned long long* words,
+                                          unsigned& status)
+{
+    const Grid& g = J.g;
+    uint32_t cur = kNoBrick, len = 0;
+    Locals locals;
+    for (uint32_t k = 0; k < s.n; ++k) {
+        Visit o;
+        const bool ok = seg_visit(g, s, o);
+        if (ok && o.brick == cur && len < kMaxRun) {
+            locals.put(len, o.local);
+            ++len;
+        } else {
+            if (len)
+                emit_run<FILL, PACK, DIRECT>(J.brick_base + cur, p, locals, len, visits, cursor, entries, entries_cap,
+                                             layout, words, status);
+            cur = ok ? o.brick : kNoBrick;
+            len = ok ? 1u : 0u;
+            locals.start(ok ? o.local : 0u);
+        }
+        seg_advance(s);
+    }
+    if (len)
+        emit_run<FILL, PACK, DIRECT>(J.brick_base + cur, p, locals, len, visits, cursor, entries, entries_cap, layout,
+                                     words, status);
+}
+
+constexpr int kWalkThreads = 256; // threads per block of the bin kernels
+constexpr int kWalkBuckets = 64;  // walk lengths a block groups its pairs by (the last: 63 visits or more)
+constexpr size_t kWalkStaticSmem = (8 * kWalkThreads + kWalkBuckets) * sizeof(uint32_t); // balanced_walk's arrays
+
+// The one walk (counts and entries in one pass) of a one-style call, in
+// rounds of 256 pairs per block, its warps' lanes matched by walk length: each thread sets up the pair
+// of its own index (coalesced index and vertex loads, the pair-tangent
+// store), the block ranks the 256 pairs by visit count (a counting sort over
+// kWalkBuckets lengths in shared memory), and thread t walks the pair of rank
+// t.  A warp then runs about as many steps as its lanes' walks take, where 32
+// consecutive pairs (1 to about 40 visits each) run as long as their longest
+// (production style: one walk 0.273 -> 0.262 ms).  A batch's grid-stride
+// rounds keep the consecutive pairs: a barrier per round measured slower.
+template <bool PACK, bool SINGLE>
+__device__ __forceinline__ void balanced_walk(const VoxJob& job0, const VoxJob* s_jobs, const uint32_t* s_item_base,
+                                              int nj, uint32_t total_items, float4* pair_tan, uint32_t* visits,
+                                              typename Entry<PACK>::T* entries, size_t entries_cap,
+                                              const uint2* __restrict__ layout, unsigned long long* words,
+                                              unsigned& status)
+{
+    __shared__ uint32_t s_walk[8][kWalkThreads]; // root x y z, direction x y z, visits, pair (by rank)
+    __shared__ uint32_t s_rank[kWalkBuckets];
+    const uint32_t t = threadIdx.x;
+    for (uint64_t base = (uint64_t)blockIdx.x * kWalkThreads; base < total_items;
+         base += (uint64_t)gridDim.x * kWalkThreads) {
+        const uint64_t q = base + t;
+        Seg s = {};
+        if (q < total_items) {
+            const VoxJob& J = SINGLE ? job0 : s_jobs[find_job(s_item_base, nj, (uint32_t)q)];
+            const uint2 ij = __ldg(J.pairs + ((uint32_t)q - J.item_base));
+            seg_setup(J.g, J.v, ij, s, status);
+            if (J.tan) // tangents[indices[i]]: every visit of the pair adds this one
+                pair_tan[q] = make_float4(__ldg(J.tan + 3 * (size_t)ij.x), __ldg(J.tan + 3 * (size_t)ij.x + 1),
+                                          __ldg(J.tan + 3 * (size_t)ij.x + 2), 0.0f);
+        }
+        if (t < (uint32_t)kWalkBuckets) s_rank[t] = 0u;
+        __syncthreads();
+        const uint32_t bucket = s.n < (uint32_t)kWalkBuckets ? s.n : (uint32_t)kWalkBuckets - 1;
+        const uint32_t r = atomicAdd(s_rank + bucket, 1u);
+        __syncthreads();
+        if (t < 32) { // exclusive scan of the bucket sizes, two per lane
+            const uint32_t a = s_rank[2 * t], b = s_rank[2 * t + 1];
+            uint32_t incl = a + b;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (t >= (uint32_t)o) incl += y;
+            }
+            s_rank[2 * t] = incl - a - b;
+            s_rank[2 * t + 1] = incl - b;
+        }
+        __syncthreads();
+        const uint32_t at = s_rank[bucket] + r;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            s_walk[a][at] = __float_as_uint(s.root[a]);
+            s_walk[3 + a][at] = __float_as_uint(s.dir[a]);
+        }
+        s_walk[6][at] = s.n;
+        s_walk[7][at] = (uint32_t)q;
+        __syncthreads();
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            s.root[a] = __uint_as_float(s_walk[a][t]);
+            s.dir[a] = __uint_as_float(s_walk[3 + a][t]);
+        }
+        s.n = s_walk[6][t];
+        const uint32_t wq = s_walk[7][t];
+        if (s.n) {
+            const VoxJob& J = SINGLE ? job0 : s_jobs[find_job(s_item_base, nj, wq)];
+            walk_pair<false, PACK, true>(J, wq - J.item_base, s, visits, nullptr, entries, entries_cap, layout, words,
+                                         status);
+        }
+        // the next round writes the shared arrays only after its first barrier, which every
+        // thread reaches after its reads of this round
+    }
+}
+
 // SINGLE = true: a one-style call; the style comes as the kernel parameter
 // job0 (constant bank, free to read in the visit loop).  Otherwise the job
 // table is copied into shared memory and each item looks its style up.
@@ -336,6 +446,12 @@ __global__ void bin_kernel(const __grid_constant__ VoxJob job0, const VoxJob* __
     // partial sectors, so it keeps consecutive items per warp, as do the
     // counting and one-walk passes (coalesced index, vertex and pair-tangent
     // accesses) and a batch.
+    if constexpr (SEG && DIRECT && !FILL && SINGLE) { // a batch keeps its grid-stride rounds barrier-free
+        balanced_walk<PACK, SINGLE>(job0, s_jobs, s_item_base, nj, total_items, pair_tan, visits, entries,
+                                    entries_cap, layout, words, status);
+        if (status) atomicOr(words + WORD_STATUS, (unsigned long long)status);
+        return;
+    }
     constexpr bool sp = FILL && SINGLE && SEG && SPREAD;
     const uint64_t cols = (total_items + 31) / 32;
     const uint64_t span = sp ? cols * 32 : total_items;
@@ -354,27 +470,7 @@ __global__ void bin_kernel(const __grid_constant__ VoxJob job0, const VoxJob* __
             if (!FILL && J.tan) // tangents[indices[i]]: every visit of the pair adds this one
                 pair_tan[q] = make_float4(__ldg(J.tan + 3 * (size_t)ij.x), __ldg(J.tan + 3 * (size_t)ij.x + 1),
                                           __ldg(J.tan + 3 * (size_t)ij.x + 2), 0.0f);
-            uint32_t cur = kNoBrick, len = 0;
-            Locals locals;
-            for (uint32_t k = 0; k < s.n; ++k) {
-                Visit o;
-                const bool ok = seg_visit(g, s, o);
-                if (ok && o.brick == cur && len < kMaxRun) {
-                    locals.put(len, o.local);
-                    ++len;
-                } else {
-                    if (len)
-                        emit_run<FILL, PACK, DIRECT>(J.brick_base + cur, p, locals, len, visits, cursor, entries,
-                                                     entries_cap, layout, words, status);
-                    cur = ok ? o.brick : kNoBrick;
-                    len = ok ? 1u : 0u;
-                    locals.start(ok ? o.local : 0u);
-                }
-                seg_advance(s);
-            }
-            if (len)
-                emit_run<FILL, PACK, DIRECT>(J.brick_base + cur, p, locals, len, visits, cursor, entries, entries_cap,
-                                             layout, words, status);
+            walk_pair<FILL, PACK, DIRECT>(J, p, s, visits, cursor, entries, entries_cap, layout, words, status);
         } else {
             Visit o;
             if (vertex_visit(g, J.v, p, o))
@@ -1605,13 +1701,15 @@ vkhr_status make_job(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job& in, Vox
 
 // Dynamic shared memory of a launch that keeps at most k of its CTAs
 // resident per SM (k CTAs of it fit in an SM's shared memory, k + 1 do
-// not), at least `base` bytes; k <= 0 or k >= 8 (the register limit of the
-// walk kernels): base.
-size_t residency_smem(const vkhr_ctx* ctx, int k, size_t base)
+// not), at least `base` bytes, next to the kernel's `static_bytes` of static
+// shared memory; k <= 0 or k >= 8 (the register limit of the walk kernels):
+// base.
+size_t residency_smem(const vkhr_ctx* ctx, int k, size_t base, size_t static_bytes)
 {
     if (k <= 0 || k >= 8 || ctx->smem_per_sm <= 0) return base;
     const size_t per_block = (size_t)ctx->smem_per_sm / (size_t)k;
-    const size_t s = per_block > (size_t)ctx->smem_reserved ? per_block - (size_t)ctx->smem_reserved : 0;
+    const size_t fixed = (size_t)ctx->smem_reserved + static_bytes;
+    const size_t s = per_block > fixed ? per_block - fixed : 0;
     return std::max(s, base);
 }
 
@@ -1773,7 +1871,7 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
     VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_words + WORD_STATUS + 1, 0,
                                        (WORD_NORM - WORD_STATUS - 1) * sizeof(unsigned long long), st));
     VKHR_CUDA_TRY(ctx, cudaMemsetAsync(ctx->brick_visits, 0, (size_t)total_bricks * sizeof(uint32_t), st));
-    const unsigned threads = 256;
+    const unsigned threads = kWalkThreads;
     // one style: one item per thread (blocks retire and start staggered, so
     // their set-up loads overlap other blocks' walks); a batch caps the grid,
     // as every block copies the job table into shared memory
@@ -1783,7 +1881,8 @@ vkhr_status voxelize_batch(vkhr_ctx* ctx, bool segments, const vkhr_voxel_job* j
     const bool single = nj == 1;
     const uint2* layout = use_layout ? ctx->layout : nullptr;
     // the one walk's dynamic shared memory, sized to keep walk_ctas CTAs resident per SM
-    const size_t walk_smem = residency_smem(ctx, ctx->walk_ctas[single ? 0 : 1], single ? 0 : bin_smem_bytes);
+    const size_t walk_smem = residency_smem(ctx, ctx->walk_ctas[single ? 0 : 1], single ? 0 : bin_smem_bytes,
+                                           single ? kWalkStaticSmem : 0);
 #define VKHR_DIRECT(PACK_)                                                                                        \
     do {                                                                                                         \
         if (single) {                                                                                            \
