@@ -49,7 +49,7 @@ constexpr int kBrickThreads = 512;     // one thread per voxel of an 8^3 brick
 constexpr int kBrickCap = 22528;       // visits a brick resolves in shared memory
 constexpr int kLightBrick = 512;       // <= this many visits: the brick is resolved by one warp
 constexpr int kLightWarps = 4;         // warps per CTA of light_brick_kernel (24 KB of shared memory)
-constexpr int kBrickSmall = 64;        // <= this many visits: sorted by one warp (2 keys per lane)
+constexpr int kBrickSmall = 64;        // <= this many visits: resolved by the voxel's own thread in the brick kernels
 constexpr int kCrowdWarpMax = 256;     // crowded voxels up to this many visits: one warp each
 constexpr int kGather = 4;             // tangent loads in flight per voxel thread (64 registers at 2 CTAs / SM)
 constexpr int kHeavyTile = 2048;       // crowded voxels: shared-memory sort tile
