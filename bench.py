@@ -680,9 +680,18 @@ def schedule_section(args, dev, stream):
 
     out = {"config": {"workload": "the reference's raymarcher benchmark schedule on the synthetic ponytail "
                                   "(136,320 x 13, 256^3), 1280x720; median of %d runs per point" % reps,
-                      "distance_scale": scale}}
-    out["distance"] = [[d, timed(march(params(distance=d)))]
-                       for d in (200.0 + k * (1800.0 / 64.0) for k in range(64))]
+                      "distance_scale": scale,
+                      "distance": "[distance, ms of variant 0, ms of the variant the autotuner picks for that "
+                                  "view, that variant]"}}
+    rows = []
+    for d in (200.0 + k * (1800.0 / 64.0) for k in range(64)):
+        p = params(distance=d)
+        ctx.set_raymarch_variant(p.density_format, p.tangent_format, 0)
+        ms0 = timed(march(p))
+        chosen, _ = ctx.autotune_raymarch(p, dens.data_ptr(), tq.data_ptr(), rgba.data_ptr(), s)
+        rows.append([d, ms0, timed(march(p)), chosen])
+    ctx.set_raymarch_variant(_abi.DENSITY_U8_UNORM, _abi.TANGENT_I8_SNORM, 0)
+    out["distance"] = rows
     out["samples"] = [[k, timed(march(params(samples=k)))] for k in range(512, 63, -(448 // 64))]
     ov, ot = torch.empty_like(dv), torch.empty_like(dt)
     segs = st.segments.astype(np.uint16)
@@ -833,9 +842,10 @@ def composite_section(args, dev, stream, flush, st, t, idx, b, res):
 
 
 RAY_AB = {
-    "workload": "raymarch variants on two views: the production frame's 1920x1080 view of its normalized 256^3 "
-                "volume (512 steps, 64-step shadows, 8-tap AO), and a 3840x2160 view of the 512^3 scale volume "
-                "(1024 steps, 128-step shadows, 16-direction AO); workloads' Kajiya-Kay",
+    "workload": "raymarch variants on three views: the production frame's 1920x1080 view of its normalized 256^3 "
+                "volume (512 steps, 64-step shadows, 8-tap AO), the same from 4x the camera distance (a 74x80-pixel "
+                "footprint), and a 3840x2160 view of the 512^3 scale volume (1024 steps, 128-step shadows, "
+                "16-direction AO); workloads' Kajiya-Kay",
     "variants": {"0-3": "ray packets reading texels from L2/HBM (8x4, 16x2, 4x8, 8x4 at 64 registers)",
                  "4": "8x4 packets, each occupied density brick a warp's rays need staged into shared memory by one "
                       "TMA tensor copy",
@@ -844,13 +854,16 @@ RAY_AB = {
                  "6": "variant 5's texture for the deep-shadow and AO samples only; the isosurface search reads "
                       "memory",
                  "7": "8x4 packets reading exact texels through the texture unit's 2x2 gathers (slices tiled into a "
-                      "2D array, copied per call); the software trilinear filters them"},
+                      "2D array, copied per call); the software trilinear filters them",
+                 "8-10": "ray groups: 4 / 2 / 8 lanes per pixel take as many consecutive samples of its primary "
+                         "march, shadow march and AO taps at once and replay them in order (4x2 / 4x4 / 2x2 pixels "
+                         "per warp)"},
     "warm": "the volume L2-resident, as right after the voxelizer wrote it; cold: L2 flushed (512 MiB write) first",
 }
 
 
 def raymarch_ab_section(args, dev, stream, flush):
-    """Time every raymarch variant on the headline view and a 512^3 view."""
+    """Time every raymarch variant on the headline view, a distant view and a 512^3 view."""
     import torch
 
     from vkhr_gb300 import _abi, _native, scene, strands
@@ -870,6 +883,10 @@ def raymarch_ab_section(args, dev, stream, flush):
                           counts.data_ptr(), dens.data_ptr(), tq.data_ptr(), s)
     ctx.normalize_densities(dens.data_ptr(), n, s)
     views["production 1920x1080, 256^3"] = (frame_params(b, res), dens, tq)
+    far_p = scene.make_params(b, res, WORKLOAD["width"], WORKLOAD["height"], camera_distance=16.0,
+                              raycast_steps=float(WORKLOAD["raycast_steps"]),
+                              shadow_steps=float(WORKLOAD["shadow_steps"]), **scene.CONFIG_SHADING)
+    views["production style from 4x the distance (74x80-pixel footprint)"] = (far_p, dens, tq)
     if not args.no_scale:
         sst = strands.hemisphere_style(1_048_576, 32, radius=1.2, step_length=0.04, seed=4)
         st_t = strands.generate_tangents(sst.vertices, sst.segments)

@@ -387,11 +387,16 @@ vkhr_status vkhr_raymarch(vkhr_ctx* ctx, const vkhr_raymarch_params* params,
  * 2D array of the grid's z slices, tiled and framed by zeros, that the call
  * copies the density into; the software trilinear filters them, so its
  * pixels are variant 0's, bit for bit (variant 0 where the tiled slices
- * exceed the gather limits). */
-#define VKHR_RAYMARCH_VARIANTS 8
+ * exceed the gather limits).  8 / 9 / 10 = ray groups, the steps-per-thread
+ * knob: 4 / 2 / 8 lanes march each pixel's ray, taking as many consecutive
+ * samples of its primary march, its shadow march and its occlusion taps at
+ * once and replaying them in order (4x2 / 4x4 / 2x2 pixels per warp);
+ * variant 0's pixels, bit for bit.  They pay where few rays march far (a
+ * distant volume's small footprint) and lose where many rays fill the GPU. */
+#define VKHR_RAYMARCH_VARIANTS 11
 
 /* Autotuner (no reference counterpart): times each variant of vkhr_raymarch
- * that computes the reference's pixels (0-4 and 7) on these inputs (one warm-up
+ * that computes the reference's pixels (0-4 and 7-10) on these inputs (one warm-up
  * and three timed runs each, d_rgba receiving the image) and keeps the
  * fastest in the context for params' texel formats; later vkhr_raymarch
  * calls with those formats use it.  Writes the choice to *chosen and, when

@@ -52,8 +52,9 @@ def test_variants_render_the_same_image(ctx, oracle_lib):
 ])
 def test_staged_and_gather_variants_equal_l2_march(ctx, oracle_lib, fmt, tfmt, res, view, depth):
     """Variant 4 (each occupied brick a warp's rays need staged into shared
-    memory by one TMA copy) and variant 7 (texels through the texture unit's
-    2x2 gathers from the tiled, zero-framed slices) against variant 0
+    memory by one TMA copy), variant 7 (texels through the texture unit's
+    2x2 gathers from the tiled, zero-framed slices) and variants 8-10 (ray
+    groups of 4, 2 and 8 lanes) against variant 0
     (texels from L2): the same pixels bit for bit, with and without a depth
     buffer, for every density format, for grids whose depth is not a power
     of two (a partly filled last row of tiles), for a view whose volume
@@ -90,7 +91,7 @@ def test_staged_and_gather_variants_equal_l2_march(ctx, oracle_lib, fmt, tfmt, r
         depth_np[:, : p.width // 2] = 1.0
         din = torch.from_numpy(depth_np).cuda()
     imgs = []
-    for v in (0, 4, _abi.RAYMARCH_GATHER_VARIANT):
+    for v in (0, 4, _abi.RAYMARCH_GATHER_VARIANT) + _abi.RAYMARCH_GROUP_VARIANTS:
         ctx.set_raymarch_variant(fmt, tfmt, v)
         rgba = torch.full((p.height, p.width, 4), -7.0, dtype=torch.float32, device="cuda")
         dep = torch.full((p.height, p.width), -7.0, dtype=torch.float32, device="cuda")
@@ -100,13 +101,54 @@ def test_staged_and_gather_variants_equal_l2_march(ctx, oracle_lib, fmt, tfmt, r
         torch.cuda.synchronize()
         imgs.append((rgba.cpu().numpy(), dep.cpu().numpy()))
     ctx.set_raymarch_variant(fmt, tfmt, 0)
-    for k, name in ((1, "staged"), (2, "gather")):
+    for k, name in ((1, "staged"), (2, "gather"), (3, "groups of 4"), (4, "groups of 2"), (5, "groups of 8")):
         assert np.array_equal(imgs[0][0], imgs[k][0]), (name, int((imgs[0][0] != imgs[k][0]).any(axis=2).sum()))
         assert np.array_equal(imgs[0][1], imgs[k][1]), name
     assert (imgs[1][0][..., 3] > 0).sum() > 200
     ref, rdepth, diag = oracle_lib.raymarch(p, dens, tan, depth_in=depth_np, diag=True)
     # small views (300x220) whose depth buffer cuts rays mid-volume: up to 2% excluded
     compare_images(imgs[1][0], imgs[1][1], ref, rdepth, diag, label="staged variant", max_excluded=0.02)
+
+
+@pytest.mark.parametrize("steps,shadow_steps,ao_kernel,ao_dirs,distance", [
+    (256.0, 32.0, 2.0, 0, 4.0),   # power-of-two steps: empty-space jumps in both marches
+    (200.0, 40.0, 3.0, 0, 4.0),   # no jumps; a 27-tap cube
+    (512.0, 48.0, 2.0, 16, 12.0),  # jumps in the primary march only; 16 directions; a distant view
+    (384.0, 64.0, 2.6, 5, 4.0),   # a cube of a non-integer size; directions not a multiple of a group
+])
+def test_ray_group_variants_equal_one_lane_march(ctx, oracle_lib, steps, shadow_steps, ao_kernel, ao_dirs, distance):
+    """Ray groups (variants 8-10: 4, 2 or 8 lanes take consecutive samples
+    of one ray at once and replay them in order) against the one-lane march
+    of variant 0, bit for bit, with and without the empty-space jumps, for
+    ambient-occlusion cubes and directions whose tap counts are not
+    multiples of the group."""
+    import torch
+
+    st, t, idx = style("hemi", 3000, 14, seed=23)
+    res = (48, 40, 44)
+    b = oracle_lib.bounding_box(st.vertices)
+    c, d, tq, _ = oracle_lib.voxelize("segments", st.vertices, t, idx, b, res)
+    dens = oracle_lib.normalize(d)
+    o, sz = np.asarray(b.origin, dtype=np.float64), np.asarray(b.size, dtype=np.float64)
+    p = scene.make_params(b, res, 256, 192, camera_distance=distance, raycast_steps=steps, shadow_steps=shadow_steps,
+                          isosurface=0.115, view_direction=(0.3, 0.4, 1.0), target=o + 0.5 * sz,
+                          ao_directions=ao_dirs, **scene.CONFIG_SHADING)
+    p.ao_kernel_size = ao_kernel
+    dd, dt = to_dev(dens, torch), to_dev(tq, torch)
+    imgs = []
+    for v in (0,) + _abi.RAYMARCH_GROUP_VARIANTS:
+        ctx.set_raymarch_variant(p.density_format, p.tangent_format, v)
+        rgba = torch.full((p.height, p.width, 4), -7.0, dtype=torch.float32, device="cuda")
+        dep = torch.full((p.height, p.width), -7.0, dtype=torch.float32, device="cuda")
+        ctx.raymarch(p, dd.data_ptr(), dt.data_ptr(), None, rgba.data_ptr(), dep.data_ptr())
+        ctx.check_status(None)
+        torch.cuda.synchronize()
+        imgs.append((rgba.cpu().numpy(), dep.cpu().numpy()))
+    ctx.set_raymarch_variant(p.density_format, p.tangent_format, 0)
+    assert (imgs[0][0][..., 3] > 0).sum() > 100
+    for k, v in enumerate(_abi.RAYMARCH_GROUP_VARIANTS, start=1):
+        assert np.array_equal(imgs[0][0], imgs[k][0]), (v, int((imgs[0][0] != imgs[k][0]).any(axis=2).sum()))
+        assert np.array_equal(imgs[0][1], imgs[k][1]), v
 
 
 @pytest.mark.parametrize("variant", [_abi.RAYMARCH_TEXTURE_VARIANT, _abi.RAYMARCH_SHADE_TEXTURE_VARIANT])

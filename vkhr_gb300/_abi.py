@@ -32,11 +32,12 @@ STATUS_NAMES = {
 INDEX_REF_FP32 = 0
 INDEX_EXACT = 1
 
-RAYMARCH_VARIANTS = 8
-TUNED_RAYMARCH_VARIANTS = (0, 1, 2, 3, 4, 7)  # the variants that compute the same pixels (autotuned)
+RAYMARCH_VARIANTS = 11
+TUNED_RAYMARCH_VARIANTS = (0, 1, 2, 3, 4, 7, 8, 9, 10)  # the variants that compute the same pixels (autotuned)
 RAYMARCH_TEXTURE_VARIANT = 5
 RAYMARCH_SHADE_TEXTURE_VARIANT = 6  # the texture unit for the shadow and AO samples only
 RAYMARCH_GATHER_VARIANT = 7  # exact texels through the texture unit's gathers
+RAYMARCH_GROUP_VARIANTS = (8, 9, 10)  # ray groups of 4, 2 and 8 lanes per pixel
 MAX_AO_DIRECTIONS = 32
 WALK_CHOICES = (0, 2, 3, 4, 5, 6)  # vkhr_autotune_voxelize: resident one-walk CTAs per SM (0: no limit)
 

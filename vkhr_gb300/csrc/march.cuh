@@ -641,11 +641,49 @@ __device__ __forceinline__ bool ray_entry(const RayConsts& c, int px, int py, Ve
     return true;
 }
 
+// Ray groups: G lanes (a power of two, G <= 8) march one pixel's ray.  The
+// lanes evaluate G consecutive samples at once (classification, the empty-
+// space jump length, the density), then every lane replays the G outcomes
+// in order -- the serial loop's decisions and sums in the serial order, so
+// the pixel is the one-lane march's bit for bit -- and the group goes on
+// from where the replay stopped or jumped.  A ray's chain of dependent L2
+// loads gets up to G times shorter; the shadow march and the ambient-
+// occlusion taps are split the same way.  Every branch the lanes of a group
+// take is decided on values they share, so the group stays converged.
+template <int G>
+__device__ __forceinline__ unsigned group_mask()
+{
+    static_assert(G >= 2 && G <= 8 && (G & (G - 1)) == 0, "ray groups of 2, 4 or 8 lanes");
+    return ((1u << G) - 1u) << ((threadIdx.x & 31u) & ~(unsigned)(G - 1));
+}
+
+// The outcome of one sample of a march: 0 sampled (val = density), 1 exactly
+// zero (val = the empty-space jump in steps, < 1: none), 2 left the grid, 3
+// behind the depth buffer, 4 past the end of the march.
+template <int G>
+__device__ __forceinline__ void group_outcomes(int code, float val, int (&cs)[G], float (&vs)[G])
+{
+    const unsigned gm = group_mask<G>();
+#pragma unroll
+    for (int j = 0; j < G; ++j) {
+        cs[j] = __shfl_sync(gm, code, j, G);
+        vs[j] = __shfl_sync(gm, val, j, G);
+    }
+}
+
+// The t of this lane's sample: `rank` plain steps past t, added one at a
+// time as the serial loop adds them.
+__device__ __forceinline__ float group_t(float t, float step, int rank)
+{
+    for (int i = 0; i < rank; ++i) t += step;
+    return t;
+}
+
 // The fragment of a ray whose primary march ended with accumulated density
 // acc and surface point surf (volume.frag:45-103): shading, density shadows,
 // ambient occlusion, coverage and depth.  Leaves out / out_depth (background)
 // alone when acc is 0 (the shader's discard).
-template <int DF, int TF, bool TAPE = false, int SRC = kSampleMemory>
+template <int DF, int TF, bool TAPE = false, int SRC = kSampleMemory, int G = 1>
 __device__ __forceinline__ void shade_fragment(const RayConsts& c, const typename DensityTexel<DF>::T* __restrict__ dens,
                                                const void* __restrict__ tang, const uint32_t* __restrict__ occ,
                                                Vec3 surf, float acc, float4& out, float& out_depth,
@@ -690,19 +728,56 @@ __device__ __forceinline__ void shade_fragment(const RayConsts& c, const typenam
             float inv_dl[3];
             reciprocals(dl, inv_dl);
             float strands = 0.0f;
-            for (float t = 0.0f; t < 1.0f;) {
-                const Vec3 Q = mix(surf, light, t);
-                float u[3], lo[3], hi[3];
-                texel_coords(c, Q, u);
-                const int z = classify(c, occ, u, inv_dl, lo, hi);
-                if (z == 2) break;
-                if (z == 1) {
-                    const float n = c.shadow_pow2 ? steps_inside(u, inv_dl, lo, hi, c.shadow_steps) : 0.0f;
-                    t = n >= 1.0f ? fmaf(n, sstep, t) : t + sstep;
-                    continue;
+            if constexpr (G == 1) {
+                for (float t = 0.0f; t < 1.0f;) {
+                    const Vec3 Q = mix(surf, light, t);
+                    float u[3], lo[3], hi[3];
+                    texel_coords(c, Q, u);
+                    const int z = classify(c, occ, u, inv_dl, lo, hi);
+                    if (z == 2) break;
+                    if (z == 1) {
+                        const float n = c.shadow_pow2 ? steps_inside(u, inv_dl, lo, hi, c.shadow_steps) : 0.0f;
+                        t = n >= 1.0f ? fmaf(n, sstep, t) : t + sstep;
+                        continue;
+                    }
+                    strands += density_at<DF, shade_source(SRC)>(c, dens, Q) * c.thickness;
+                    t += sstep;
                 }
-                strands += density_at<DF, shade_source(SRC)>(c, dens, Q) * c.thickness;
-                t += sstep;
+            } else { // the same samples and sum, G at a time
+                const int rank = (int)(threadIdx.x & (G - 1));
+                for (float t = 0.0f; t < 1.0f;) {
+                    const float tr = group_t(t, sstep, rank);
+                    int code = 4;
+                    float val = 0.0f;
+                    if (tr < 1.0f) {
+                        const Vec3 Q = mix(surf, light, tr);
+                        float u[3], lo[3], hi[3];
+                        texel_coords(c, Q, u);
+                        code = classify(c, occ, u, inv_dl, lo, hi);
+                        if (code == 1) val = c.shadow_pow2 ? steps_inside(u, inv_dl, lo, hi, c.shadow_steps) : 0.0f;
+                        else if (code == 0) val = density_at<DF, shade_source(SRC)>(c, dens, Q);
+                    }
+                    int cs[G];
+                    float vs[G];
+                    group_outcomes<G>(code, val, cs, vs);
+                    bool stop = false, jumped = false;
+                    float tc = t;
+#pragma unroll
+                    for (int j = 0; j < G; ++j) {
+                        if (stop || jumped) continue;
+                        if (cs[j] >= 2) {
+                            stop = true;
+                        } else if (cs[j] == 1 && vs[j] >= 1.0f) {
+                            t = fmaf(vs[j], sstep, tc);
+                            jumped = true;
+                        } else {
+                            if (cs[j] == 0) strands += vs[j] * c.thickness;
+                            tc += sstep;
+                        }
+                    }
+                    if (stop) break;
+                    if (!jumped) t = tc;
+                }
             }
             const float os = powf(1.0f - c.alpha, strands);
             if (TAPE) tape->occl_s = os;
@@ -712,21 +787,61 @@ __device__ __forceinline__ void shade_fragment(const RayConsts& c, const typenam
         if (c.shading_model != VKHR_SHADING_ADSM) {
             float dsum = 0.0f, taps;
             if (c.ao_n > 0) { // the directional extension
-                for (int i = 0; i < c.ao_n; ++i) {
-                    const Vec3 q = v3(surf.x + c.ao_off[i][0], surf.y + c.ao_off[i][1], surf.z + c.ao_off[i][2]);
-                    dsum += fminf(density_at<DF, shade_source(SRC)>(c, dens, q), c.ao_max);
+                if constexpr (G == 1) {
+                    for (int i = 0; i < c.ao_n; ++i) {
+                        const Vec3 q = v3(surf.x + c.ao_off[i][0], surf.y + c.ao_off[i][1], surf.z + c.ao_off[i][2]);
+                        dsum += fminf(density_at<DF, shade_source(SRC)>(c, dens, q), c.ao_max);
+                    }
+                } else { // G taps at a time, added in tap order
+                    const int rank = (int)(threadIdx.x & (G - 1));
+                    for (int base = 0; base < c.ao_n; base += G) {
+                        const int i = base + rank;
+                        float d = 0.0f;
+                        if (i < c.ao_n) {
+                            const Vec3 q = v3(surf.x + c.ao_off[i][0], surf.y + c.ao_off[i][1], surf.z + c.ao_off[i][2]);
+                            d = density_at<DF, shade_source(SRC)>(c, dens, q);
+                        }
+                        int cs[G];
+                        float vs[G];
+                        group_outcomes<G>(0, d, cs, vs);
+#pragma unroll
+                        for (int j = 0; j < G; ++j)
+                            if (base + j < c.ao_n) dsum += fminf(vs[j], c.ao_max);
+                    }
                 }
                 taps = (float)c.ao_n;
             } else {
                 const float kr = (c.ao_kernel - 1.0f) / 2.0f;
                 const float scale = c.ao_radius / kr;
                 const Vec3 sc = v3(c.voxel_space[0] * scale, c.voxel_space[1] * scale, c.voxel_space[2] * scale);
-                for (float z = -kr; z <= kr; z += 1.0f)
-                    for (float y = -kr; y <= kr; y += 1.0f)
-                        for (float x = -kr; x <= kr; x += 1.0f) {
+                if constexpr (G == 1) {
+                    for (float z = -kr; z <= kr; z += 1.0f)
+                        for (float y = -kr; y <= kr; y += 1.0f)
+                            for (float x = -kr; x <= kr; x += 1.0f) {
+                                const Vec3 q = v3(surf.x + x * sc.x, surf.y + y * sc.y, surf.z + z * sc.z);
+                                dsum += fminf(density_at<DF, shade_source(SRC)>(c, dens, q), c.ao_max);
+                            }
+                } else { // the cube's taps in loop order, G at a time; each offset by the loop's own additions
+                    int m = 0;
+                    for (float x = -kr; x <= kr; x += 1.0f) ++m;
+                    const int n = m * m * m, rank = (int)(threadIdx.x & (G - 1));
+                    for (int base = 0; base < n; base += G) {
+                        const int i = base + rank;
+                        float d = 0.0f;
+                        if (i < n) {
+                            const float x = group_t(-kr, 1.0f, i % m), y = group_t(-kr, 1.0f, (i / m) % m),
+                                        z = group_t(-kr, 1.0f, i / (m * m));
                             const Vec3 q = v3(surf.x + x * sc.x, surf.y + y * sc.y, surf.z + z * sc.z);
-                            dsum += fminf(density_at<DF, shade_source(SRC)>(c, dens, q), c.ao_max);
+                            d = density_at<DF, shade_source(SRC)>(c, dens, q);
                         }
+                        int cs[G];
+                        float vs[G];
+                        group_outcomes<G>(0, d, cs, vs);
+#pragma unroll
+                        for (int j = 0; j < G; ++j)
+                            if (base + j < n) dsum += fminf(vs[j], c.ao_max);
+                    }
+                }
                 taps = c.ao_kernel * c.ao_kernel * c.ao_kernel;
             }
             if (TAPE) tape->dsum = dsum;
@@ -743,7 +858,8 @@ __device__ __forceinline__ void shade_fragment(const RayConsts& c, const typenam
 // and depth.  depth_at points at the pixel's depth-buffer value (NULL: 1.0).
 // TAPE = true also records the pixel's PixelTape and the march's t every K
 // iterations into ckpt[0, nckpt) (the checkpoints the adjoint replays from).
-template <int DF, int TF, bool TAPE = false, int SRC = kSampleMemory>
+// G > 1: the ray group's form (G lanes, the same pixel in each).
+template <int DF, int TF, bool TAPE = false, int SRC = kSampleMemory, int G = 1>
 __device__ __forceinline__ void march_pixel(const RayConsts& c, const typename DensityTexel<DF>::T* __restrict__ dens,
                                             const void* __restrict__ tang, const uint32_t* __restrict__ occ,
                                             const float* depth_at, int px, int py, float4& out, float& out_depth,
@@ -780,6 +896,69 @@ __device__ __forceinline__ void march_pixel(const RayConsts& c, const typename D
         Vec3 surf = v3(0.0f, 0.0f, 0.0f), entry = v3(0.0f, 0.0f, 0.0f);
         bool found = false, entered = false;
         uint32_t k = 0; // iterations (TAPE only)
+        static_assert(G == 1 || !TAPE, "the adjoint's tape records one lane's march");
+        if constexpr (G > 1) { // G samples at a time, replayed in order
+            const int rank = (int)(threadIdx.x & (G - 1));
+            float t_surf = 0.0f, t_entry = 0.0f;
+            bool at_surf = false;
+            for (float t = 0.0f; t < 1.0f;) {
+                const float tr = group_t(t, step, rank);
+                int code = 4;
+                float val = 0.0f;
+                if (tr < 1.0f) {
+                    const Vec3 P = mix(start, end, tr);
+                    if (depth_test && db < clip_depth(c, P)) {
+                        code = 3;
+                    } else {
+                        float u[3], lo[3], hi[3];
+                        texel_coords(c, P, u);
+                        code = classify(c, occ, u, inv_du, lo, hi);
+                        if (code == 1) val = jump ? steps_inside(u, inv_du, lo, hi, c.steps) : 0.0f;
+                        else if (code == 0) val = density_at<DF, march_source(SRC)>(c, dens, P);
+                    }
+                }
+                int cs[G];
+                float vs[G];
+                group_outcomes<G>(code, val, cs, vs);
+                bool stop = false, jumped = false;
+                float tc = t;
+#pragma unroll
+                for (int j = 0; j < G; ++j) {
+                    if (stop || jumped) continue;
+                    if (cs[j] >= 2) {
+                        stop = true;
+                    } else if (cs[j] == 1) {
+                        if (vs[j] >= 1.0f) {
+                            t = fmaf(vs[j], step, tc);
+                            jumped = true;
+                        } else {
+                            tc += step;
+                        }
+                    } else {
+                        const float rho = vs[j];
+                        acc += rho;
+                        if (rho != 0.0f) {
+                            if (acc <= c.iso) {
+                                t_surf = tc;
+                                at_surf = true;
+                            }
+                            if (acc >= c.iso) found = true;
+                            if (!entered) {
+                                t_entry = tc;
+                                entered = true;
+                            }
+                            if (acc > c.iso && c.lod * (acc / c.iso) * c.alpha >= 1.0f) stop = true; // outputs final
+                        }
+                        if (!stop) tc += step;
+                    }
+                }
+                if (stop) break;
+                if (!jumped) t = tc;
+            }
+            // the points the serial loop kept, from their t (mix gives the same point for the same t)
+            if (at_surf) surf = mix(start, end, t_surf);
+            if (entered) entry = mix(start, end, t_entry);
+        } else
         for (float t = 0.0f; t < 1.0f;) {
             if (TAPE && !jump && k % K == 0 && k / K < nckpt) ckpt[k / K] = t;
             const Vec3 P = mix(start, end, t);
@@ -819,7 +998,7 @@ __device__ __forceinline__ void march_pixel(const RayConsts& c, const typename D
             tape->n = k;
             tape->flags = kTapeHit;
         }
-        shade_fragment<DF, TF, TAPE, SRC>(c, dens, tang, occ, surf, acc, out, out_depth, tape);
+        shade_fragment<DF, TF, TAPE, SRC, G>(c, dens, tang, occ, surf, acc, out, out_depth, tape);
     }
 }
 

@@ -36,9 +36,12 @@ constexpr int kStagedVariant = 4;
 constexpr int kTextureVariant = 5;   // the texture unit's filter: other pixels, never autotuned
 constexpr int kShadeTextureVariant = 6; // the same filter for the shading's samples only
 constexpr int kGatherVariant = 7;    // exact texels by texture gathers: the same pixels
+constexpr int kGroup4Variant = 8;    // ray groups of 4 lanes, 4x2-pixel warp tiles: the same pixels
+constexpr int kGroup2Variant = 9;    // ray groups of 2 lanes, 4x4-pixel warp tiles: the same pixels
+constexpr int kGroup8Variant = 10;   // ray groups of 8 lanes, 2x2-pixel warp tiles: the same pixels
 // the variants that compute the same pixels (the autotuner's candidates)
-constexpr int kTunedVariants[] = {0, 1, 2, 3, 4, kGatherVariant};
-static_assert(VKHR_RAYMARCH_VARIANTS == kGatherVariant + 1, "variant table");
+constexpr int kTunedVariants[] = {0, 1, 2, 3, 4, kGatherVariant, kGroup4Variant, kGroup2Variant, kGroup8Variant};
+static_assert(VKHR_RAYMARCH_VARIANTS == kGroup8Variant + 1, "variant table");
 constexpr RayVariant kRayVariants[kPacketVariants] = {{8, 6}, {16, 6}, {4, 6}, {8, 8}};
 
 template <int DF, int TF, int TW = 8, int MINB = 6, int SRC = kSampleMemory>
@@ -59,6 +62,33 @@ raymarch_kernel(const __grid_constant__ RayConsts c, const typename DensityTexel
     march_pixel<DF, TF, false, SRC>(c, dens, tang, occ, depth_in ? depth_in + at : nullptr, px, py, out, out_depth);
     rgba[at] = out;
     if (depth_out) depth_out[at] = out_depth;
+}
+
+// Ray groups: G lanes march each pixel's ray (march_pixel's group form), a
+// warp's 32 / G pixels as a TW x (32 / G / TW) tile; the group's first lane
+// writes the pixel.
+template <int DF, int TF, int G, int TW>
+__global__ void __launch_bounds__(32 * kWarpsX * kWarpsY, 6)
+raymarch_group_kernel(const __grid_constant__ RayConsts c, const typename DensityTexel<DF>::T* __restrict__ dens,
+                      const void* __restrict__ tang, const uint32_t* __restrict__ occ,
+                      const float* __restrict__ depth_in, float4* __restrict__ rgba, float* __restrict__ depth_out,
+                      int x0, int y0, int x1, int y1)
+{
+    constexpr int TH = 32 / G / TW;
+    static_assert(TW * TH * G == 32, "a warp's tile");
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, pix = lane / G;
+    const int px = x0 + (blockIdx.x * kWarpsX + (warp % kWarpsX)) * TW + (pix % TW);
+    const int py = y0 + (blockIdx.y * kWarpsY + (warp / kWarpsX)) * TH + (pix / TW);
+    if (px >= x1 || py >= y1) return; // the whole group: its lanes share the pixel
+    const size_t at = (size_t)py * c.W + px;
+    float4 out;
+    float out_depth;
+    march_pixel<DF, TF, false, kSampleMemory, G>(c, dens, tang, occ, depth_in ? depth_in + at : nullptr, px, py, out,
+                                                 out_depth);
+    if ((lane & (G - 1)) == 0) {
+        rgba[at] = out;
+        if (depth_out) depth_out[at] = out_depth;
+    }
 }
 
 // ---- TMA-staged primary march ----------------------------------------------------
@@ -667,9 +697,23 @@ vkhr_status launch(vkhr_ctx* ctx, const RayConsts& c, const void* dens, const vo
         }
         v = 0; // beyond the gather limits: the default packets
     }
+    const typename DensityTexel<DF>::T* d = (const typename DensityTexel<DF>::T*)dens;
+    if (v == kGroup4Variant || v == kGroup2Variant || v == kGroup8Variant) { // 4x2 / 4x4 / 2x2 pixels per warp
+        const int gw = v == kGroup8Variant ? 2 : 4, gh = v == kGroup2Variant ? 4 : 2;
+        const dim3 grid((rect[2] + gw * kWarpsX - 1) / (gw * kWarpsX), (rect[3] + gh * kWarpsY - 1) / (gh * kWarpsY));
+        if (v == kGroup4Variant)
+            VKHR_LAUNCH(ctx, (raymarch_group_kernel<DF, TF, 4, 4>), grid, block, 0, st, c, d, tang, ctx->occ, din, out,
+                        dout, x0, y0, x1, y1);
+        else if (v == kGroup2Variant)
+            VKHR_LAUNCH(ctx, (raymarch_group_kernel<DF, TF, 2, 4>), grid, block, 0, st, c, d, tang, ctx->occ, din, out,
+                        dout, x0, y0, x1, y1);
+        else
+            VKHR_LAUNCH(ctx, (raymarch_group_kernel<DF, TF, 8, 2>), grid, block, 0, st, c, d, tang, ctx->occ, din, out,
+                        dout, x0, y0, x1, y1);
+        return background ? vkhr_join_side(ctx, st) : VKHR_OK;
+    }
     const int tw = kRayVariants[v].tw, th = 32 / tw;
     const dim3 grid((rect[2] + tw * kWarpsX - 1) / (tw * kWarpsX), (rect[3] + th * kWarpsY - 1) / (th * kWarpsY));
-    const typename DensityTexel<DF>::T* d = (const typename DensityTexel<DF>::T*)dens;
 #define VKHR_RAY(TW_, MINB_)                                                                                      \
     VKHR_LAUNCH(ctx, (raymarch_kernel<DF, TF, TW_, MINB_>), grid, block, 0, st, c, d, tang, ctx->occ, din, out, dout, x0, \
                 y0, x1, y1)
