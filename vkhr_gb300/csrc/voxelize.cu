@@ -340,14 +340,15 @@ constexpr int kWalkBuckets = 64;  // walk lengths a block groups its pairs by (t
 constexpr size_t kWalkStaticSmem = (8 * kWalkThreads + kWalkBuckets) * sizeof(uint32_t); // balanced_walk's arrays
 
 // The one walk (counts and entries in one pass) of a one-style call, in
-// rounds of 256 pairs per block, its warps' lanes matched by walk length: each thread sets up the pair
-// of its own index (coalesced index and vertex loads, the pair-tangent
-// store), the block ranks the 256 pairs by visit count (a counting sort over
-// kWalkBuckets lengths in shared memory), and thread t walks the pair of rank
-// t.  A warp then runs about as many steps as its lanes' walks take, where 32
-// consecutive pairs (1 to about 40 visits each) run as long as their longest
-// (production style: one walk 0.273 -> 0.262 ms).  A batch's grid-stride
-// rounds keep the consecutive pairs: a barrier per round measured slower.
+// rounds of 256 pairs per block, its warps' lanes matched by walk length:
+// each thread sets up the pair of its own index (coalesced index and vertex
+// loads, the pair-tangent store), the block ranks the 256 pairs by visit
+// count (a counting sort over kWalkBuckets lengths in shared memory), and
+// thread t walks the pair of rank t.  A warp then runs about as many steps
+// as its lanes' walks take, where 32 consecutive pairs (1 to about 40 visits
+// each) run as long as their longest (production style: one walk 0.273 ->
+// 0.262 ms).  A batch's grid-stride rounds keep the consecutive pairs: a
+// barrier per round measured slower.
 template <bool PACK, bool SINGLE>
 __device__ __forceinline__ void balanced_walk(const VoxJob& job0, const VoxJob* s_jobs, const uint32_t* s_item_base,
                                               int nj, uint32_t total_items, float4* pair_tan, uint32_t* visits,
