@@ -219,3 +219,51 @@ def test_errors(ctx, oracle_lib):
         with pytest.raises(VkhrError) as e:
             _gpu_raymarch(ctx, p, dn, tq)
         assert e.value.status == _abi.VKHR_ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_seeded_random_views(ctx, oracle_lib, seed):
+    """Seeded random views against the FP64 oracle at the raymarch bar:
+    hemisphere or disk styles in non-cubic grids, any view direction and
+    distance, power-of-two and other step counts, separate shadow steps or
+    none, every shading model with or without shadows, both lobes and
+    shifts, cube or directional occlusion, u8 / count / float densities, an
+    isosurface drawn per case, and each of the variants the autotuner picks
+    from (all give the same pixels)."""
+    import torch
+
+    rng = np.random.default_rng(2000 + seed)
+    kind = ("hemi", "disk")[int(rng.integers(0, 2))]
+    res = tuple(int(x) for x in rng.integers(24, 65, 3))
+    b, c, dn, tq = _volume(oracle_lib, kind, int(rng.integers(500, 4001)), int(rng.integers(8, 17)), res, seed=seed)
+    fmt = (_abi.DENSITY_U8_UNORM, _abi.DENSITY_U32_COUNT, _abi.DENSITY_F32)[int(rng.integers(0, 3))]
+    if fmt == _abi.DENSITY_U8_UNORM:
+        dens, iso = dn, float(rng.uniform(0.05, 0.3))
+    elif fmt == _abi.DENSITY_U32_COUNT:
+        dens, iso = c, float(rng.integers(1, 4))
+    else:
+        dens, iso = c.astype(np.float32) * np.float32(0.25), float(rng.uniform(0.2, 0.8))
+    vd = rng.normal(size=3)
+    model = (_abi.SHADING_KAJIYA_KAY, _abi.SHADING_ADSM, _abi.SHADING_LAO)[int(rng.integers(0, 3))]
+    p = scene.make_params(b, res, int(rng.integers(96, 201)), int(rng.integers(72, 161)),
+                          camera_distance=float(rng.uniform(2.5, 8.0)), view_direction=tuple(vd),
+                          raycast_steps=float(rng.choice([64.0, 128.0, 200.0, 256.0, 300.0, 512.0])),
+                          shadow_steps=float(rng.choice([0.0, 16.0, 32.0, 48.0])), isosurface=iso,
+                          shading_model=model, deep_shadows_on=int(rng.integers(0, 2)),
+                          kd=float(rng.uniform(0.3, 1.0)), spec_exponent2=float(rng.choice([0.0, 8.0])),
+                          spec_shift=(float(rng.uniform(-0.15, 0.15)), float(rng.uniform(-0.15, 0.15))),
+                          ao_directions=int(rng.choice([0, 0, 5, 16])), density_format=fmt)
+    p.ao_kernel_size = float(rng.choice([2.0, 3.0]))
+    variant = int(rng.choice(_abi.TUNED_RAYMARCH_VARIANTS))
+    ctx.set_raymarch_variant(fmt, p.tangent_format, variant)
+    try:
+        gpu, gdepth = _gpu_raymarch(ctx, p, dens, tq)
+    finally:
+        ctx.set_raymarch_variant(fmt, p.tangent_format, 0)
+    ref, rdepth, diag = oracle_lib.raymarch(p, dens, tq, diag=True)
+    label = "seed %d: %s %s, format %d, model %d, steps %g, variant %d" % (seed, kind, res, fmt, model,
+                                                                         p.raycast_steps, variant)
+    if (ref[..., 3] > 0).sum() == 0:  # the view missed the volume: background everywhere
+        assert np.array_equal(gpu, ref) and np.array_equal(gdepth, rdepth), label
+        return
+    compare_images(gpu, gdepth, ref, rdepth, diag, label=label, max_excluded=0.03)

@@ -379,3 +379,39 @@ def test_uncertified_voxels_past_the_descriptor_list(native_lib, oracle_lib):
             finally:
                 c.close()
             assert (got == n).sum() == 512 * nb and got.sum() == 512 * nb * n
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_seeded_random_styles(ctx, oracle_lib, seed):
+    """Seeded random cases over the voxelizer's whole input space, against
+    the oracle bit for bit: strand counts of 1..3000 (pair counts that are
+    rarely a multiple of a block), 2..24 vertices, hemisphere or disk roots,
+    segment lengths from a fraction of a voxel to many voxels, grids of 1..96
+    per axis (non-cubic, down to a few voxels, so that voxels crowd past 64
+    and 255 visits), the style's bounding box or a box that cuts it, both
+    index modes, both voxelization modes, with and without tangents."""
+    rng = np.random.default_rng(1000 + seed)
+    kind = ("hemi", "disk")[int(rng.integers(0, 2))]
+    n_strands = int(rng.integers(1, 3001))
+    verts = int(rng.integers(2, 25))
+    step = float(rng.choice([0.005, 0.02, 0.05, 0.15]))
+    st, t, idx = style(kind, n_strands, verts, seed=seed, step_length=step)
+    if rng.random() < 0.25:
+        res = tuple(int(x) for x in rng.integers(1, 9, 3))      # a handful of voxels: crowded
+    else:
+        res = tuple(int(x) for x in rng.integers(8, 97, 3))
+    b = oracle_lib.bounding_box(st.vertices)
+    if rng.random() < 0.3:  # a box that cuts the style: visits outside it are dropped
+        o = np.asarray(b.origin, dtype=np.float64)
+        s = np.asarray(b.size, dtype=np.float64)
+        b = _abi.aabb_from(tuple(o + s * rng.uniform(0.0, 0.3, 3)), tuple(s * rng.uniform(0.4, 0.8, 3)))
+    mode = ("vertices", "segments")[int(rng.integers(0, 2))]
+    index_mode = (_abi.INDEX_REF_FP32, _abi.INDEX_EXACT)[int(rng.integers(0, 2))]
+    if rng.random() < 0.2:  # counts and densities only
+        c_ref, d_ref, _, _ = oracle_lib.voxelize(mode, st.vertices, t, idx, b, res, index_mode)
+        c, d, _ = gpu_voxelize(ctx, mode, st.vertices, t, idx, b, res, index_mode, want_tangents=False)
+        assert np.array_equal(c, c_ref) and np.array_equal(d, d_ref)
+    else:
+        c = _check(ctx, oracle_lib, mode, st.vertices, t, idx, b, res, index_mode)
+    print("seed %d: %s %d x %d, step %.3f, %s, grid %s, %s, max %d visits in a voxel"
+          % (seed, kind, n_strands, verts, step, mode, res, "exact" if index_mode else "fp32", int(c.max())))
