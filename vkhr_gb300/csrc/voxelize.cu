@@ -55,7 +55,7 @@ constexpr int kGather = 4;             // tangent loads in flight per voxel thre
 constexpr int kHeavyTile = 2048;       // crowded voxels: shared-memory sort tile
 constexpr int kKeep = 256;             // crowded voxels: tangents summed (>= 255)
 constexpr int kRangeThreads = 256;
-constexpr int kRangeItems = 16;
+constexpr int kRangeItems = 2;   // bricks per thread of the range passes (short atomic chains)
 constexpr uint32_t kNoBrick = 0xffffffffu;
 
 struct Grid {
@@ -482,9 +482,11 @@ __global__ void bin_kernel(const __grid_constant__ VoxJob job0, const VoxJob* __
     if (status) atomicOr(words + WORD_STATUS, (unsigned long long)status);
 }
 
-// Slices of the visit list per brick (one atomic per 4096 bricks), the
-// visit total, the largest brick, and the list of bricks the shared-memory
-// resolve handles.
+// Slices of the visit list per brick (one atomic per 512 bricks), the
+// visit total, the largest brick, and the lists of visited bricks by size.
+// Two bricks per thread: each list append is a warp's returning atomic, so
+// a thread's bricks form a chain of them (16 per thread: 0.014 ms for the
+// 32,768 bricks of a 256^3 grid; 2 per thread: 0.008 ms).
 __global__ void __launch_bounds__(kRangeThreads) bin_ranges_kernel(const uint32_t* __restrict__ visits, uint32_t nb,
                                                                  uint32_t* cursor, uint32_t* list,
                                                                  unsigned long long* words)
