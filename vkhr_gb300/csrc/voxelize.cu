@@ -1512,14 +1512,18 @@ __global__ void rescale_u8_kernel(uint8_t* d, uint64_t n, const unsigned long lo
 {
     const uint32_t lo = (uint32_t)words[WORD_NORM + 0], hi = (uint32_t)words[WORD_NORM + 1];
     const float scaling = hi > lo ? __fdiv_rn(255.0f, (float)(int)(hi - lo)) : 0.0f;
-    const uint64_t n4 = n / 4;
-    uint32_t* d4 = reinterpret_cast<uint32_t*>(d);
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n4; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t q = d4[i];
-        d4[i] = rescale1(q & 0xffu, lo, hi, scaling) | (rescale1((q >> 8) & 0xffu, lo, hi, scaling) << 8) |
-                (rescale1((q >> 16) & 0xffu, lo, hi, scaling) << 16) | (rescale1(q >> 24, lo, hi, scaling) << 24);
+    auto word = [&](uint32_t q) {
+        return rescale1(q & 0xffu, lo, hi, scaling) | (rescale1((q >> 8) & 0xffu, lo, hi, scaling) << 8) |
+               (rescale1((q >> 16) & 0xffu, lo, hi, scaling) << 16) | (rescale1(q >> 24, lo, hi, scaling) << 24);
+    };
+    const uint64_t n16 = n / 16; // 16 texels (one 16-byte load and store) per item
+    uint4* d16 = reinterpret_cast<uint4*>(d);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n16; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint4 q = d16[i];
+        d16[i] = make_uint4(word(q.x), word(q.y), word(q.z), word(q.w));
     }
-    for (uint64_t i = n4 * 4 + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    for (uint64_t i = n16 * 16 + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
         d[i] = (uint8_t)rescale1(d[i], lo, hi, scaling);
 }
 
@@ -2211,7 +2215,7 @@ vkhr_status vkhr_normalize_densities(vkhr_ctx* ctx, uint8_t* d, uint64_t n, void
     const unsigned blocks = std::min(vkhr_blocks(n / 16 + 1, 256), (unsigned)ctx->sm_count * 4);
     VKHR_LAUNCH(ctx, minmax_u8_kernel, blocks, 256, 0, st, d, n, ctx->d_words);
     VKHR_CUDA_TRY(ctx, cudaGetLastError());
-    const unsigned rb = std::min(vkhr_blocks(n / 4 + 1, 256), (unsigned)ctx->sm_count * 8);
+    const unsigned rb = std::min(vkhr_blocks(n / 16 + 1, 256), (unsigned)ctx->sm_count * 16);
     VKHR_LAUNCH(ctx, rescale_u8_kernel, rb, 256, 0, st, d, n, ctx->d_words);
     VKHR_CUDA_TRY(ctx, cudaGetLastError());
     return VKHR_OK;
