@@ -57,8 +57,8 @@ WORKLOAD = {
 # frame (profiles/voxelizer_kernels_production_frame.md and
 # profiles/raymarch_kernel_production_frame.md), by kernel family.
 TRAFFIC = {
-    "bin_kernel<false, true, true, true, false, true": 56_505_856 + 95_293_184,  # one walk
-    "brick_kernel<SEG, TANG, false": 153_476_352 + 27_694_592,
+    "bin_kernel<false, true, true, true, false, true": 57_001_472 + 96_199_168,  # one walk
+    "brick_kernel<SEG, TANG, false": 154_601_472 + 26_825_472,
     "bin_kernel<true": 55_134_208 + 72_237_312,
     "bin_kernel<false": 55_694_080 + 24_500_992,
     "raymarch_kernel": 8_215_040 + 0,
